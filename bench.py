@@ -1,0 +1,347 @@
+"""Benchmark of the trace path on one GB300 (or N replicas under torchrun).
+
+Workload (one "step"): closest-hit ray cast of 2,097,152 rays — a 1024x1024 pinhole camera at distance 3
+plus 1,048,576 rays with origins uniform in the sphere's AABB expanded 1.5x and directions uniform on
+the sphere — against the 1.3M-triangle scene (level-8 displaced icosphere, 1,310,720 triangles, plus a
+2-triangle ground plane and a 2-triangle area light; 1,310,724 triangles).  Inputs and outputs stay
+resident in HBM for `value`; `e2e` runs the same step through the host-buffer C ABI call
+(reina_raycast) with the rays copied in from pinned host memory and the hits copied back every step.
+L2 (129 MB) is flushed by writing a 512 MB buffer between timed steps (outside the timed events).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+`--impl reference` times the CPU restatement of the path (oracle/, FP32, all host threads) on a bounded
+sample of the same rays per step; the reference's own Vulkan ray-tracing path cannot run on this
+hardware (no graphics stack, no RT cores).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "reina-vk_gb300"))
+sys.path.insert(0, str(ROOT))
+sys.path.insert(0, str(ROOT / "tests"))
+
+NODE_BYTES = 80
+TRI_BYTES = 48
+RAY_BYTES = 32
+HIT_BYTES = 16
+FALLBACK_HBM_GBS = 6800.0
+L2_FLUSH_BYTES = 512 << 20
+N_CAMERA_SIDE = 1024
+N_RANDOM = 1 << 20
+METRIC = "rays/s on 1.3M-tri scene (closest-hit ray cast)"
+
+
+def _peak_hbm() -> tuple[float, str]:
+    p = ROOT / "MEASURED_PEAKS.json"
+    try:
+        return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def _profiled_traffic() -> float | None:
+    """DRAM bytes per launch of the ray-cast kernel from the committed ncu summary (None if absent)."""
+    p = ROOT / "profiles" / "raycast_closest_l8.md"
+    if not p.exists():
+        return None
+    m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", p.read_text())
+    return float(m.group(1)) if m else None
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu_index = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+        self._t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.gpu_index)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def _build_workload(R, ctx):
+    import scenes
+
+    t0 = time.perf_counter()
+    scene, tris, geo = scenes.large_scene(R, ctx, 8)
+    build_s = time.perf_counter() - t0
+    rays = scenes.raycast_rays(R, 8, N_CAMERA_SIDE, N_CAMERA_SIDE, N_RANDOM, geo[0][0])
+    return scene, tris, rays, build_s
+
+
+def run_ours(args) -> dict | None:
+    import torch
+
+    import build as pkg_build
+    import reina_gb300 as R
+
+    ws, rank, local = _dist()
+    pkg_build.build()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    ctx = R.Context(local)
+    scene, tris, rays, build_s = _build_workload(R, ctx)
+    st = scene.stats()
+    n = rays.shape[0]
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+    d_rays = torch.from_numpy(rays.view(np.float32).reshape(n, 8).copy()).cuda()
+    d_hits = torch.empty((n, 4), dtype=torch.float32, device="cuda")
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+
+    # Counting build (not timed): BVH8 nodes visited and triangles tested by these rays.
+    nodes_v, tris_t = R.raycast_counters(ctx, scene, d_rays.data_ptr(), n, R.RAY_CLOSEST, sptr)
+    bytes_per_ray = RAY_BYTES + HIT_BYTES + NODE_BYTES * nodes_v / n + TRI_BYTES * tris_t / n
+    any_nodes, any_tris = R.raycast_counters(ctx, scene, d_rays.data_ptr(), n, R.RAY_ANY, sptr)
+
+    def step(flags=R.RAY_CLOSEST):
+        R.raycast_device(ctx, scene, d_rays.data_ptr(), n, d_hits.data_ptr(), flags, sptr)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    wall0 = time.perf_counter()
+    for k in range(args.steps):
+        flush.zero_()
+        starts[k].record(stream)
+        step()
+        ends[k].record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    # any-hit (shadow-ray form) on the same rays, reported beside the headline
+    any_ms = []
+    for k in range(args.steps):
+        flush.zero_()
+        starts[k].record(stream)
+        step(R.RAY_ANY)
+        ends[k].record(stream)
+    torch.cuda.synchronize()
+    any_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    clk = clocks.stop()
+
+    # e2e through the host-buffer C ABI call, pinned host memory, copies in the timed region.
+    h_rays = torch.from_numpy(rays.view(np.float32).reshape(n, 8).copy()).pin_memory()
+    h_hits = torch.empty((n, 4), dtype=torch.float32).pin_memory()
+    for _ in range(max(1, args.warmup)):
+        R.raycast_into(ctx, scene, h_rays.data_ptr(), n, h_hits.data_ptr(), R.RAY_CLOSEST)
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        R.raycast_into(ctx, scene, h_rays.data_ptr(), n, h_hits.data_ptr(), R.RAY_CLOSEST)
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+
+    mean_ms = float(np.mean(step_ms))
+    if ws > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([mean_ms, e2e_s], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        mean_ms, e2e_s = float(t[0]), float(t[1])
+    if rank != 0:
+        return None
+    peak, peak_kind = _peak_hbm()
+    achieved = bytes_per_ray * n / (mean_ms * 1e-3) / 1e9
+    traffic = _profiled_traffic()
+    hits_np = d_hits.cpu().numpy().view(np.uint32)[:, 0]
+    out = {
+        "metric": METRIC,
+        "value": ws * n / (mean_ms * 1e-3),
+        "unit": "rays/s",
+        "n_gpus": ws,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": mean_ms,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded generators; the reference publishes no dataset)",
+        "config": {
+            "workload": "raycast_l8: closest hit, 1024x1024 camera + 1,048,576 random rays (2,097,152) "
+                        "on the level-8 displaced icosphere + ground + light (1,310,724 tris)",
+            "rays_per_step": n,
+            "triangles": int(st["triangle_count"]),
+            "bvh8_nodes": int(st["node_count"]),
+            "bvh_build_s": round(st["build_seconds"], 3),
+            "scene_build_s": round(build_s, 3),
+            "l2": "flushed between timed steps (512 MB write, outside the timed events)",
+            "parallelism": f"replicas x{ws}",
+            "hit_fraction": float((hits_np != 0xFFFFFFFF).mean()),
+        },
+        "e2e": {"value": ws * n / e2e_s, "unit": "rays/s", "h2d_bytes_per_step": n * RAY_BYTES,
+                "d2h_bytes_per_step": n * HIT_BYTES},
+        "gpu_launches": args.steps * 2,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_kind,
+                     "traffic": traffic,
+                     "algorithmic_bytes_per_ray": bytes_per_ray,
+                     "nodes_per_ray": nodes_v / n, "tris_per_ray": tris_t / n,
+                     "kernel": "raycast_kernel<closest>"},
+        "anyhit": {"rays_per_s": n / (float(np.mean(any_ms)) * 1e-3), "ms_per_step": float(np.mean(any_ms)),
+                   "nodes_per_ray": any_nodes / n, "tris_per_ray": any_tris / n},
+        "clocks": clk,
+        "wall_timed_s": wall,
+    }
+    if not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(tris, rays, args.cpu_sample)
+    return out
+
+
+def cpu_baseline(tris, rays, sample: int) -> dict:
+    from oracle import oracle as O
+
+    sub = np.ascontiguousarray(rays[:: max(1, rays.shape[0] // sample)][:sample])
+    b = O.Bvh(tris)
+    threads = O.hw_threads()
+    b.raycast(sub[:1024], threads=threads)
+    t0 = time.perf_counter()
+    b.raycast(sub, threads=threads)
+    dt = time.perf_counter() - t0
+    return {"value": sub.shape[0] / dt, "unit": "rays/s", "cores": threads, "kind": "port",
+            "sample": f"{sub.shape[0]} of the {rays.shape[0]} rays (every {rays.shape[0] // sub.shape[0]}th), "
+                      f"FP32 oracle BVH traversal, std::thread x{threads}, BVH build excluded",
+            "seconds": dt}
+
+
+def run_reference(args) -> dict | None:
+    ws, rank, local = _dist()
+    if rank != 0:
+        return None
+    import build as pkg_build
+    import reina_gb300 as R
+    from oracle import oracle as O
+
+    pkg_build.build()
+    ctx = R.Context(-1)   # host-only: scene assembly only, no GPU work
+    scene, tris, rays, _ = _build_workload(R, ctx)
+    sample = args.cpu_sample
+    sub = np.ascontiguousarray(rays[:: max(1, rays.shape[0] // sample)][:sample])
+    b = O.Bvh(tris)
+    threads = O.hw_threads()
+    for _ in range(args.warmup):
+        b.raycast(sub[:4096], threads=threads)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        b.raycast(sub, threads=threads)
+        times.append(time.perf_counter() - t0)
+    dt = float(np.mean(times))
+    v = sub.shape[0] / dt
+    return {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": v,
+        "unit": "rays/s",
+        "n_gpus": ws,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": dt * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded generators)",
+        "config": {"workload": "raycast_l8 (same rays and scene as the GPU arm; each step a bounded sample)",
+                   "rays_per_step": sub.shape[0], "parallelism": "host threads"},
+        "cpu_baseline": {"value": v, "unit": "rays/s", "cores": threads, "kind": "port",
+                         "sample": f"{sub.shape[0]} rays per step, FP32 oracle BVH traversal (oracle/), "
+                                   f"std::thread x{threads}"},
+        "e2e": {"value": v, "unit": "rays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main() -> int:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--cpu-sample", type=int, default=1 << 21)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
+    out = run_reference(args) if args.impl == "reference" else run_ours(args)
+    if out is not None:
+        print(json.dumps(out), flush=True)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

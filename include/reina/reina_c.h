@@ -1,0 +1,235 @@
+/*
+ * reina_c.h — C ABI of the GB300 trace path (BVH build -> traversal -> wavefront integrator ->
+ * accumulation -> post-process) that stands in for Reina's Vulkan ray-tracing pipeline.
+ *
+ * The entry points mirror the reference's scene API and per-frame calls one for one; each declaration
+ * names the reference interface (file:line, relative to the reina-vk project root) that it replaces.
+ * Conventions:
+ *   - every function returns an int status: REINA_OK (0) or a negative REINA_ERR_* code; the message of
+ *     the last failure on the calling thread is returned by reina_last_error().  No C++ exception
+ *     crosses this boundary (the reference throws std::runtime_error, caught in src/main.cpp:11-14).
+ *   - handles are opaque and owned by the library; release them with the matching *_destroy call.
+ *   - "host" buffers are plain CPU pointers; "device" buffers are CUDA device pointers on the context's
+ *     GPU; `stream` arguments are cudaStream_t values passed as void* (NULL = the legacy default stream).
+ */
+#ifndef REINA_C_H
+#define REINA_C_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "polyglot.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------------------------------------ */
+/* Status codes                                                                                      */
+/* ------------------------------------------------------------------------------------------------ */
+enum {
+    REINA_OK = 0,
+    REINA_ERR_INVALID = -1,      /* bad argument (null pointer, out-of-range id, size mismatch) */
+    REINA_ERR_CUDA = -2,         /* a CUDA runtime call failed */
+    REINA_ERR_OOM = -3,          /* device or host allocation failed */
+    REINA_ERR_STATE = -4,        /* call made in the wrong state (e.g. add to a built scene) */
+    REINA_ERR_IO = -5,           /* file could not be read or parsed */
+    REINA_ERR_NO_EMISSIVE = -6,  /* scene has no emissive geometry (src/scene/Instances.cpp:125-127) */
+    REINA_ERR_DEVICE = -7,       /* a kernel raised its error flag (e.g. traversal stack overflow) */
+    REINA_ERR_BUDGET = -8        /* request does not fit the device-memory admission budget */
+};
+
+/* Message of the last failed call on this thread ("" if none).  The pointer stays valid until the
+ * next failing call on the same thread. */
+const char* reina_last_error(void);
+
+/* Library version string, e.g. "reina-gb300 0.1 sm_103a". */
+const char* reina_version(void);
+
+/* ------------------------------------------------------------------------------------------------ */
+/* Context                                                                                           */
+/* ------------------------------------------------------------------------------------------------ */
+typedef struct reina_ctx reina_ctx;
+
+typedef struct reina_ctx_options {
+    int32_t device;              /* CUDA device ordinal; the context makes it current on each call.
+                                  * -1 = host-only context: scenes are assembled and their BVH built
+                                  * on the CPU, nothing is uploaded and GPU calls fail. */
+    uint32_t flags;              /* reserved, 0 */
+} reina_ctx_options;
+
+/* Creates the per-GPU context (replaces the Vulkan instance/device set-up of src/Reina.cpp:61-74). */
+int reina_ctx_create(const reina_ctx_options* options, reina_ctx** out_ctx);
+void reina_ctx_destroy(reina_ctx* ctx);
+/* Number of streaming multiprocessors of the context's GPU (0 if unknown). */
+int reina_ctx_sm_count(const reina_ctx* ctx);
+
+/* ------------------------------------------------------------------------------------------------ */
+/* Scene API  (src/scene/Scene.h:62-138)                                                             */
+/* ------------------------------------------------------------------------------------------------ */
+typedef struct reina_scene reina_scene;
+
+/* ModelData (src/scene/Models.h:23-30), passed as borrowed arrays; the scene copies them. */
+typedef struct reina_model_data {
+    const float* vertices;       /* 4 floats per vertex (x, y, z, w = 1) */
+    uint64_t vertex_count;
+    const uint32_t* indices;     /* 3 per triangle, relative to this model */
+    uint64_t index_count;
+    const float* tbns;           /* 9 floats per entry: mat3 column-major, columns T, B, N */
+    uint64_t tbn_count;
+    const uint32_t* tbn_indices; /* 3 per triangle */
+    uint64_t tbn_index_count;
+    const float* tex_coords;     /* 2 floats per entry; may be NULL */
+    uint64_t tex_coord_count;
+    const uint32_t* tex_indices; /* 3 per triangle; may be NULL */
+    uint64_t tex_index_count;
+} reina_model_data;
+
+/* Material (src/scene/Scene.h:21-46).  material_idx: 0 Lambertian, 1 metal, 2 dielectric, 3 Disney
+ * (the shader-binding-table offset of src/tools/vktools.cpp:483). */
+typedef struct reina_material {
+    uint32_t material_idx;
+    int32_t texture_id;
+    int32_t normal_map_id;
+    int32_t bump_map_id;
+    float albedo[3];
+    float emission[3];
+    float roughness;
+    float ior;
+    uint32_t interp_normals;
+    float absorption;
+    uint32_t cull_backface;
+    float anisotropic;
+    float subsurface;
+    float clearcoat_gloss;
+    float sheen_tint[3];
+    float specular_tint[3];
+    float metallic;
+    float clearcoat;
+    float specular_transmission;
+    float sheen;
+} reina_material;
+
+/* Scene::Scene() */
+int reina_scene_create(reina_ctx* ctx, reina_scene** out_scene);
+void reina_scene_destroy(reina_scene* scene);
+
+/* Scene::defineObject(const ModelData&)  (src/scene/Scene.h:78, src/scene/Models.cpp:24-92) */
+int reina_scene_define_object(reina_scene* scene, const reina_model_data* model, uint32_t* out_object_id);
+
+/* Scene::addInstance(objectID, transform, material)  (src/scene/Scene.h:114, Scene.cpp:27-54).
+ * transform: 16 floats, column-major object-to-world matrix (glm::mat4). */
+int reina_scene_add_instance(reina_scene* scene, uint32_t object_id, const float transform[16],
+                             const reina_material* material);
+
+/* Extension for per-face materials: face f of the object uses materials[face_material[f]].  Each
+ * distinct material becomes one InstanceProperties record; emission of per-face materials must be 0. */
+int reina_scene_add_instance_per_face(reina_scene* scene, uint32_t object_id, const float transform[16],
+                                      const reina_material* materials, uint32_t material_count,
+                                      const uint32_t* face_material);
+
+/* Scene::build(...)  (src/scene/Scene.cpp:56-125): assembles the global vertex/index/TBN/UV buffers,
+ * InstanceProperties and the emissive CDFs, builds the binned-SAH BVH collapsed to quantized BVH8
+ * nodes (replacing the BLAS/TLAS builds of src/graphics/Blas.cpp:8-124, src/tools/vktools.cpp:460-596)
+ * and uploads everything to the GPU.  Returns REINA_ERR_NO_EMISSIVE when `require_emissive` is set
+ * and the scene has no emissive instance (src/scene/Instances.cpp:125-127). */
+int reina_scene_build(reina_scene* scene, uint32_t require_emissive);
+
+/* Scene::getEmissiveWeight()  (src/scene/Scene.h:118): total emissive weight Σ area·luminance. */
+float reina_scene_emissive_weight(const reina_scene* scene);
+
+typedef struct reina_scene_stats {
+    uint64_t triangle_count;
+    uint64_t instance_count;
+    uint64_t node_count;         /* BVH8 nodes */
+    uint64_t node_bytes;         /* bytes of one BVH8 node (80) */
+    uint64_t triangle_bytes;     /* bytes of one traversal triangle record (48) */
+    uint64_t device_bytes;       /* device memory held by the scene */
+    uint32_t max_depth;          /* depth of the BVH8 tree (root = 1) */
+    uint32_t leaf_triangles_max; /* largest triangle count of one leaf child (<= 3) */
+    double build_seconds;        /* host BVH build time */
+    float bounds_min[3];
+    float bounds_max[3];
+} reina_scene_stats;
+int reina_scene_get_stats(const reina_scene* scene, reina_scene_stats* out_stats);
+
+/* Copies the scene's BVH8 nodes (node_count * 80 bytes) and traversal triangles (triangle_count * 48
+ * bytes) to host buffers, for inspection and structural checks.  Either pointer may be NULL. */
+int reina_scene_export_bvh(const reina_scene* scene, void* nodes_out, void* triangles_out);
+
+/* Maps a global triangle id (as returned in reina_hit.prim) to (instance index, primitive index
+ * within the instance's object) — the pair (gl_InstanceID, gl_PrimitiveID) of the reference. */
+int reina_scene_prim_info(const reina_scene* scene, uint32_t prim, uint32_t* out_instance,
+                          uint32_t* out_primitive);
+
+/* ------------------------------------------------------------------------------------------------ */
+/* Ray casting (closest hit / any hit) — replaces traceRayEXT (shaders/raytrace/raytrace.rgen.glsl:  */
+/* 159-171, closest hit, opaque) and the shadow query of shaders/raytrace/nee.h.glsl:126-144          */
+/* (gl_RayFlagsTerminateOnFirstHitEXT).                                                              */
+/* ------------------------------------------------------------------------------------------------ */
+typedef struct reina_ray {       /* 32 bytes */
+    float org[3];
+    float tmin;
+    float dir[3];
+    float tmax;
+} reina_ray;
+
+typedef struct reina_hit {       /* 16 bytes */
+    uint32_t prim;               /* global triangle id, 0xFFFFFFFF = miss */
+    float t;
+    float u;                     /* barycentric weight of vertex 1 (gl hit attribute .x) */
+    float v;                     /* barycentric weight of vertex 2 (gl hit attribute .y) */
+} reina_hit;
+
+enum {
+    REINA_RAY_CLOSEST = 0,       /* closest hit; ties in t go to the lower triangle id */
+    REINA_RAY_ANY = 1            /* first hit found in [tmin, tmax]; terminate traversal */
+};
+
+/* Host buffers: copies the rays to the GPU, traces them and copies the hits back (blocking). */
+int reina_raycast(reina_ctx* ctx, const reina_scene* scene, const reina_ray* rays, uint64_t count,
+                  reina_hit* hits, uint32_t flags);
+
+/* Device buffers: enqueues the trace on `stream` and returns without synchronizing. */
+int reina_raycast_device(reina_ctx* ctx, const reina_scene* scene, const void* d_rays, uint64_t count,
+                         void* d_hits, uint32_t flags, void* stream);
+
+/* Traversal statistics for the same rays (a separate counting build of the traversal kernel, never
+ * used for timing): per-ray BVH8 nodes visited and triangles tested, summed into the two outputs. */
+int reina_raycast_counters(reina_ctx* ctx, const reina_scene* scene, const void* d_rays, uint64_t count,
+                           uint32_t flags, uint64_t* out_nodes_visited, uint64_t* out_triangles_tested,
+                           void* stream);
+
+/* ------------------------------------------------------------------------------------------------ */
+/* Camera  (src/graphics/Camera.cpp:10-11)                                                           */
+/* ------------------------------------------------------------------------------------------------ */
+/* inverse(perspective(fovy_radians, aspect, near, far)) and inverse(lookAt(pos, pos + front, up)),
+ * column-major, as glm computes them. */
+int reina_camera_matrices(const float pos[3], const float front[3], const float up[3], float fovy_radians,
+                          float aspect, float z_near, float z_far, float inv_view[16], float inv_proj[16]);
+
+/* ------------------------------------------------------------------------------------------------ */
+/* Synthetic workloads (seeded, deterministic)                                                        */
+/* ------------------------------------------------------------------------------------------------ */
+/* Vertex and triangle counts of a level-`level` subdivided icosphere: 10*4^L + 2 and 20*4^L. */
+int reina_icosphere_counts(uint32_t level, uint64_t* out_vertices, uint64_t* out_triangles);
+
+/* Level-`level` icosphere of radius 1, each vertex displaced radially to r = 1 + amplitude * n(p)
+ * with n a 3-octave value noise in [-1, 1] keyed by `seed`.  vertices: 4 floats per vertex (w = 1);
+ * normals (optional, 3 floats per vertex): normalized vertex positions before displacement. */
+int reina_gen_icosphere(uint32_t level, float amplitude, uint64_t seed, float* vertices,
+                        uint32_t* indices, float* normals);
+
+/* The two ray sets of the ray-cast workload: `n_camera` pinhole rays through pixel centres of a
+ * width x height image from `cam_pos` looking at `cam_target` (fovy degrees), followed by `n_random`
+ * rays with origins uniform in `box_min..box_max` and directions uniform on the sphere (SplitMix64
+ * keyed by `seed`).  tmin = 0, tmax = 1e4.  Returns n_camera = width*height rays first. */
+int reina_gen_raycast_rays(uint32_t width, uint32_t height, const float cam_pos[3], const float cam_target[3],
+                           float fovy_degrees, uint64_t n_random, const float box_min[3],
+                           const float box_max[3], uint64_t seed, reina_ray* rays_out);
+
+#ifdef __cplusplus
+}  /* extern "C" */
+#endif
+
+#endif  /* REINA_C_H */

@@ -1,0 +1,366 @@
+// ORACLE — test infrastructure only (see oracle_common.h).
+//
+// CPU ray casting: the watertight ray/triangle test of Woop, Benthin and Wald (JCGT 2013) templated on
+// float/double, a brute-force closest/any hit over all triangles, and an independent binary SAH BVH
+// with a conservative slab test.  Restates the traversal semantics of traceRayEXT as the reference
+// uses it: closest hit with tmin 0 / tmax 1e4 (shaders/raytrace/raytrace.rgen.glsl:159-171) and the
+// terminate-on-first-hit shadow query (shaders/raytrace/nee.h.glsl:126-144).  Ties in t are broken
+// towards the lower triangle id so that the closest hit does not depend on traversal order.
+//
+// In float mode every operation is a single IEEE binary32 operation in a fixed order (this file must be
+// compiled with -ffp-contract=off), so its hits are bit-identical to any other IEEE evaluation of the
+// same expressions.
+#include <algorithm>
+#include <atomic>
+#include <cstring>
+#include <limits>
+#include <memory>
+#include <thread>
+#include <vector>
+
+#include "oracle_common.h"
+
+namespace oracle {
+
+template <class T>
+struct PreRay {
+    Vec3<T> o, d;
+    T tmin, tmax;
+    int kx, ky, kz;
+    T sx, sy, sz;
+};
+
+template <class T>
+PreRay<T> precompute(const RayRec& r) {
+    PreRay<T> p;
+    p.o = Vec3<T>((T)r.ox, (T)r.oy, (T)r.oz);
+    p.d = Vec3<T>((T)r.dx, (T)r.dy, (T)r.dz);
+    p.tmin = (T)r.tmin;
+    p.tmax = (T)r.tmax;
+    const T ax = std::fabs(p.d.x), ay = std::fabs(p.d.y), az = std::fabs(p.d.z);
+    int kz;
+    if (ax >= ay) kz = (ax >= az) ? 0 : 2;
+    else kz = (ay >= az) ? 1 : 2;
+    int kx = (kz + 1) % 3, ky = (kx + 1) % 3;
+    if (p.d[kz] < (T)0) std::swap(kx, ky);
+    p.kx = kx; p.ky = ky; p.kz = kz;
+    p.sx = p.d[kx] / p.d[kz];
+    p.sy = p.d[ky] / p.d[kz];
+    p.sz = (T)1 / p.d[kz];
+    return p;
+}
+
+// Returns true on a hit with t in [tmin, tmax_now]; u weights vertex 1, v weights vertex 2.
+template <class T>
+bool watertight(const PreRay<T>& r, const float* tri, T tmax_now, T& t_out, T& u_out, T& v_out) {
+    const Vec3<T> A = Vec3<T>((T)tri[0], (T)tri[1], (T)tri[2]) - r.o;
+    const Vec3<T> B = Vec3<T>((T)tri[3], (T)tri[4], (T)tri[5]) - r.o;
+    const Vec3<T> C = Vec3<T>((T)tri[6], (T)tri[7], (T)tri[8]) - r.o;
+    const T Ax = A[r.kx] - r.sx * A[r.kz];
+    const T Ay = A[r.ky] - r.sy * A[r.kz];
+    const T Bx = B[r.kx] - r.sx * B[r.kz];
+    const T By = B[r.ky] - r.sy * B[r.kz];
+    const T Cx = C[r.kx] - r.sx * C[r.kz];
+    const T Cy = C[r.ky] - r.sy * C[r.kz];
+    T U = Cx * By - Cy * Bx;
+    T V = Ax * Cy - Ay * Cx;
+    T W = Bx * Ay - By * Ax;
+    if (sizeof(T) == sizeof(float) && (U == (T)0 || V == (T)0 || W == (T)0)) {
+        const double CxBy = (double)Cx * (double)By, CyBx = (double)Cy * (double)Bx;
+        const double AxCy = (double)Ax * (double)Cy, AyCx = (double)Ay * (double)Cx;
+        const double BxAy = (double)Bx * (double)Ay, ByAx = (double)By * (double)Ax;
+        U = (T)(float)(CxBy - CyBx);
+        V = (T)(float)(AxCy - AyCx);
+        W = (T)(float)(BxAy - ByAx);
+    }
+    if ((U < (T)0 || V < (T)0 || W < (T)0) && (U > (T)0 || V > (T)0 || W > (T)0)) return false;
+    const T det = (U + V) + W;
+    if (det == (T)0) return false;
+    const T Az = r.sz * A[r.kz], Bz = r.sz * B[r.kz], Cz = r.sz * C[r.kz];
+    const T Tn = (U * Az + V * Bz) + W * Cz;
+    const T rcp = (T)1 / det;
+    const T t = Tn * rcp;
+    if (!(t >= r.tmin && t <= tmax_now)) return false;
+    t_out = t;
+    u_out = V * rcp;
+    v_out = W * rcp;
+    return true;
+}
+
+template <class T>
+struct BestHit {
+    uint32_t prim = kMiss;
+    T t, u = 0, v = 0;
+};
+
+template <class T>
+inline void consider(const PreRay<T>& r, const float* tris9, uint32_t id, bool any, BestHit<T>& best, bool& done) {
+    T t, u, v;
+    if (!watertight(r, tris9 + 9ull * id, best.t, t, u, v)) return;
+    if (any) {
+        best.prim = id; best.t = t; best.u = u; best.v = v;
+        done = true;
+        return;
+    }
+    if (t < best.t || id < best.prim) {
+        best.prim = id; best.t = t; best.u = u; best.v = v;
+    }
+}
+
+// ---------------------------------------------------------------------------------------------------
+// Independent binary BVH (binned SAH over the largest centroid axis, leaves of up to 4 triangles).
+struct BNode {
+    float lo[3], hi[3];
+    uint32_t left_or_first;
+    uint32_t count;        // 0 = internal (children left_or_first, left_or_first + 1)
+};
+
+struct Bvh {
+    std::vector<BNode> nodes;
+    std::vector<uint32_t> order;
+    std::vector<float> tris;   // 9 per triangle, original ids
+};
+
+static void build_node(Bvh& b, const std::vector<float>& cen, uint32_t node, uint32_t first, uint32_t count) {
+    BNode& n = b.nodes[node];
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    float clo[3] = {INFINITY, INFINITY, INFINITY}, chi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (uint32_t i = first; i < first + count; ++i) {
+        const uint32_t p = b.order[i];
+        for (int j = 0; j < 3; ++j)
+            for (int k = 0; k < 3; ++k) {
+                lo[k] = std::min(lo[k], b.tris[9ull * p + 3 * j + k]);
+                hi[k] = std::max(hi[k], b.tris[9ull * p + 3 * j + k]);
+            }
+        for (int k = 0; k < 3; ++k) {
+            clo[k] = std::min(clo[k], cen[3ull * p + k]);
+            chi[k] = std::max(chi[k], cen[3ull * p + k]);
+        }
+    }
+    for (int k = 0; k < 3; ++k) { n.lo[k] = lo[k]; n.hi[k] = hi[k]; }
+    if (count <= 4) { n.left_or_first = first; n.count = count; return; }
+    int axis = 0;
+    for (int k = 1; k < 3; ++k)
+        if (chi[k] - clo[k] > chi[axis] - clo[axis]) axis = k;
+    uint32_t mid = first + count / 2;
+    const float ext = chi[axis] - clo[axis];
+    if (ext > 0.0f) {
+        constexpr int NB = 12;
+        float blo[NB][3], bhi[NB][3];
+        uint32_t bc[NB] = {0};
+        for (int i = 0; i < NB; ++i)
+            for (int k = 0; k < 3; ++k) { blo[i][k] = INFINITY; bhi[i][k] = -INFINITY; }
+        auto bin_of = [&](uint32_t p) { return std::min(NB - 1, (int)((cen[3ull * p + axis] - clo[axis]) * (NB / ext))); };
+        for (uint32_t i = first; i < first + count; ++i) {
+            const uint32_t p = b.order[i];
+            const int bi = bin_of(p);
+            bc[bi]++;
+            for (int j = 0; j < 3; ++j)
+                for (int k = 0; k < 3; ++k) {
+                    blo[bi][k] = std::min(blo[bi][k], b.tris[9ull * p + 3 * j + k]);
+                    bhi[bi][k] = std::max(bhi[bi][k], b.tris[9ull * p + 3 * j + k]);
+                }
+        }
+        auto area = [](const float* l, const float* h) {
+            const double dx = std::max(0.0f, h[0] - l[0]), dy = std::max(0.0f, h[1] - l[1]), dz = std::max(0.0f, h[2] - l[2]);
+            return dx * dy + dy * dz + dz * dx;
+        };
+        double best = INFINITY;
+        int best_split = -1;
+        for (int s = 1; s < NB; ++s) {
+            float l0[3] = {INFINITY, INFINITY, INFINITY}, h0[3] = {-INFINITY, -INFINITY, -INFINITY};
+            float l1[3] = {INFINITY, INFINITY, INFINITY}, h1[3] = {-INFINITY, -INFINITY, -INFINITY};
+            uint32_t c0 = 0, c1 = 0;
+            for (int i = 0; i < NB; ++i) {
+                float* L = i < s ? l0 : l1;
+                float* H = i < s ? h0 : h1;
+                (i < s ? c0 : c1) += bc[i];
+                for (int k = 0; k < 3; ++k) { L[k] = std::min(L[k], blo[i][k]); H[k] = std::max(H[k], bhi[i][k]); }
+            }
+            if (c0 == 0 || c1 == 0) continue;
+            const double cost = area(l0, h0) * c0 + area(l1, h1) * c1;
+            if (cost < best) { best = cost; best_split = s; }
+        }
+        if (best_split > 0) {
+            auto it = std::partition(b.order.begin() + first, b.order.begin() + first + count,
+                                     [&](uint32_t p) { return bin_of(p) < best_split; });
+            mid = (uint32_t)(it - b.order.begin());
+            if (mid == first || mid == first + count) mid = first + count / 2;
+        }
+    }
+    const uint32_t left = (uint32_t)b.nodes.size();
+    b.nodes.push_back(BNode{});
+    b.nodes.push_back(BNode{});
+    b.nodes[node].left_or_first = left;
+    b.nodes[node].count = 0;
+    build_node(b, cen, left, first, mid - first);
+    build_node(b, cen, left + 1, mid, first + count - mid);
+}
+
+static Bvh* build_bvh(const float* tris9, uint64_t n) {
+    auto b = std::make_unique<Bvh>();
+    b->tris.assign(tris9, tris9 + 9 * n);
+    b->order.resize(n);
+    std::vector<float> cen(3 * n);
+    for (uint64_t i = 0; i < n; ++i) {
+        b->order[i] = (uint32_t)i;
+        for (int k = 0; k < 3; ++k) {
+            float lo = std::min(std::min(tris9[9 * i + k], tris9[9 * i + 3 + k]), tris9[9 * i + 6 + k]);
+            float hi = std::max(std::max(tris9[9 * i + k], tris9[9 * i + 3 + k]), tris9[9 * i + 6 + k]);
+            cen[3 * i + k] = 0.5f * (lo + hi);
+        }
+    }
+    b->nodes.reserve(2 * n + 1);
+    b->nodes.push_back(BNode{});
+    if (n > 0) build_node(*b, cen, 0, 0, (uint32_t)n);
+    return b.release();
+}
+
+// Slab test with generous slack so that it never culls a box containing a hit the triangle test
+// accepts (the entry distance is lowered and the exit distance raised by a relative 1e-5).
+template <class T>
+inline bool box_hit(const PreRay<T>& r, const BNode& n, T tmax_now, T& tnear) {
+    T t0 = r.tmin, t1 = tmax_now;
+    for (int k = 0; k < 3; ++k) {
+        const T o = r.o[k], d = r.d[k];
+        const T lo = (T)n.lo[k], hi = (T)n.hi[k];
+        if (d == (T)0) {
+            if (o < lo || o > hi) return false;
+            continue;
+        }
+        T a = (lo - o) / d, b = (hi - o) / d;
+        if (a > b) std::swap(a, b);
+        a = a - std::fabs(a) * (T)1e-5 - (T)1e-30;
+        b = b + std::fabs(b) * (T)1e-5 + (T)1e-30;
+        t0 = std::max(t0, a);
+        t1 = std::min(t1, b);
+        if (t0 > t1) return false;
+    }
+    tnear = t0;
+    return true;
+}
+
+template <class T>
+BestHit<T> trace_bvh(const Bvh& b, const RayRec& ray, bool any, uint64_t* nodes_visited) {
+    const PreRay<T> r = precompute<T>(ray);
+    BestHit<T> best;
+    best.t = r.tmax;
+    if (b.tris.empty()) return best;
+    uint32_t stack[128];
+    int sp = 0;
+    stack[sp++] = 0;
+    bool done = false;
+    while (sp > 0 && !done) {
+        const BNode& n = b.nodes[stack[--sp]];
+        T tn;
+        if (nodes_visited) (*nodes_visited)++;
+        if (!box_hit(r, n, best.t + std::fabs(best.t) * (T)1e-5, tn)) continue;
+        if (n.count > 0) {
+            for (uint32_t i = 0; i < n.count && !done; ++i) consider(r, b.tris.data(), b.order[n.left_or_first + i], any, best, done);
+            continue;
+        }
+        // push far child first (by the sign of the ray direction on the node's largest axis)
+        const BNode& l = b.nodes[n.left_or_first];
+        const BNode& rr = b.nodes[n.left_or_first + 1];
+        int axis = 0;
+        float best_ext = -1.0f;
+        for (int k = 0; k < 3; ++k) {
+            const float e = n.hi[k] - n.lo[k];
+            if (e > best_ext) { best_ext = e; axis = k; }
+        }
+        const bool left_first = (l.lo[axis] + l.hi[axis]) <= (rr.lo[axis] + rr.hi[axis]) ? (r.d[axis] >= (T)0) : (r.d[axis] < (T)0);
+        if (sp + 2 > 128) break;
+        if (left_first) { stack[sp++] = n.left_or_first + 1; stack[sp++] = n.left_or_first; }
+        else { stack[sp++] = n.left_or_first; stack[sp++] = n.left_or_first + 1; }
+    }
+    return best;
+}
+
+template <class T>
+BestHit<T> trace_brute(const float* tris9, uint64_t ntri, const RayRec& ray, bool any) {
+    const PreRay<T> r = precompute<T>(ray);
+    BestHit<T> best;
+    best.t = r.tmax;
+    bool done = false;
+    for (uint64_t i = 0; i < ntri && !done; ++i) consider(r, tris9, (uint32_t)i, any, best, done);
+    return best;
+}
+
+template <class F>
+static void parallel_for(uint64_t n, int threads, F&& f) {
+    if (threads <= 0) threads = (int)std::max(1u, std::thread::hardware_concurrency());
+    if (threads == 1 || n < 256) { for (uint64_t i = 0; i < n; ++i) f(i); return; }
+    std::atomic<uint64_t> next{0};
+    std::vector<std::thread> pool;
+    for (int t = 0; t < threads; ++t)
+        pool.emplace_back([&] {
+            for (;;) {
+                const uint64_t b = next.fetch_add(256);
+                if (b >= n) break;
+                const uint64_t e = std::min(n, b + 256);
+                for (uint64_t i = b; i < e; ++i) f(i);
+            }
+        });
+    for (auto& th : pool) th.join();
+}
+
+}  // namespace oracle
+
+using namespace oracle;
+
+extern "C" {
+
+int oracle_hw_threads(void) { return (int)std::max(1u, std::thread::hardware_concurrency()); }
+
+void oracle_rng(uint32_t seed, int n, uint32_t* words, float* values, double* values64) {
+    uint32_t s = seed;
+    for (int i = 0; i < n; ++i) {
+        const uint32_t w = rng_step(s);
+        if (words) words[i] = w;
+        if (values) values[i] = (float)w / 4294967295.0f;
+        if (values64) values64[i] = (double)w / 4294967295.0;
+    }
+}
+
+void* oracle_bvh_build(const float* tris9, uint64_t n) { return build_bvh(tris9, n); }
+
+void oracle_bvh_destroy(void* h) { delete static_cast<Bvh*>(h); }
+
+// precision: 32 -> HitRec (float) output in hits32; 64 -> HitRec64 output in hits64.
+void oracle_raycast(void* h, const RayRec* rays, uint64_t n, int any, int precision, int threads, HitRec* hits32,
+                    HitRec64* hits64) {
+    const Bvh& b = *static_cast<Bvh*>(h);
+    parallel_for(n, threads, [&](uint64_t i) {
+        if (precision == 64) {
+            BestHit<double> r = trace_bvh<double>(b, rays[i], any != 0, nullptr);
+            hits64[i] = HitRec64{r.prim, 0u, r.t, r.u, r.v};
+        } else {
+            BestHit<float> r = trace_bvh<float>(b, rays[i], any != 0, nullptr);
+            hits32[i] = HitRec{r.prim, r.t, r.u, r.v};
+        }
+    });
+}
+
+void oracle_raycast_brute(const float* tris9, uint64_t ntri, const RayRec* rays, uint64_t n, int any, int precision,
+                          int threads, HitRec* hits32, HitRec64* hits64) {
+    parallel_for(n, threads, [&](uint64_t i) {
+        if (precision == 64) {
+            BestHit<double> r = trace_brute<double>(tris9, ntri, rays[i], any != 0);
+            hits64[i] = HitRec64{r.prim, 0u, r.t, r.u, r.v};
+        } else {
+            BestHit<float> r = trace_brute<float>(tris9, ntri, rays[i], any != 0);
+            hits32[i] = HitRec{r.prim, r.t, r.u, r.v};
+        }
+    });
+}
+
+// Tests one ray against one triangle (float mode) with the full [tmin, tmax] range; returns 1 on a hit.
+int oracle_test_triangle(const float* tri9, const RayRec* ray, HitRec* out) {
+    const PreRay<float> r = precompute<float>(*ray);
+    float t, u, v;
+    if (!watertight(r, tri9, r.tmax, t, u, v)) return 0;
+    if (out) *out = HitRec{0u, t, u, v};
+    return 1;
+}
+
+}  // extern "C"

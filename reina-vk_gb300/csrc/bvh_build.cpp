@@ -1,0 +1,366 @@
+// Binned-SAH BVH build, 8-wide collapse and conservative 8-bit child-box quantization (host C++).
+#include "bvh_build.h"
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <stdexcept>
+#include <thread>
+
+namespace rt {
+namespace {
+
+struct Box {
+    float lo[3], hi[3];
+};
+
+inline Box empty_box() {
+    Box b;
+    for (int k = 0; k < 3; ++k) {
+        b.lo[k] = INFINITY;
+        b.hi[k] = -INFINITY;
+    }
+    return b;
+}
+
+inline void grow(Box& b, const Box& o) {
+    for (int k = 0; k < 3; ++k) {
+        b.lo[k] = std::min(b.lo[k], o.lo[k]);
+        b.hi[k] = std::max(b.hi[k], o.hi[k]);
+    }
+}
+
+inline float half_area(const Box& b) {
+    float d[3];
+    for (int k = 0; k < 3; ++k) d[k] = std::max(0.0f, b.hi[k] - b.lo[k]);
+    return d[0] * d[1] + d[1] * d[2] + d[2] * d[0];
+}
+
+struct BNode {
+    Box box;
+    uint32_t left;    // internal: index of the left child (the right child is left + 1)
+    uint32_t first;   // leaf: first entry of the primitive index array
+    uint32_t count;   // leaf: primitive count (0 for internal nodes)
+};
+
+constexpr int kForceMedianDepth = 48;   // past this depth splits are object medians (bounds the depth)
+
+struct BinaryBuilder {
+    const float* verts = nullptr;
+    std::vector<Box> prim_box;
+    std::vector<float> centroid;        // 3 per primitive
+    std::vector<uint32_t> idx;
+    std::vector<BNode> nodes;
+    std::atomic<uint32_t> next{1};
+    std::atomic<int> spare_threads{0};
+    int bins = 32;
+
+    void range_bounds(uint32_t b, uint32_t e, Box& box, Box& cbox) const {
+        box = empty_box();
+        cbox = empty_box();
+        for (uint32_t i = b; i < e; ++i) {
+            uint32_t p = idx[i];
+            grow(box, prim_box[p]);
+            for (int k = 0; k < 3; ++k) {
+                float c = centroid[3 * p + k];
+                cbox.lo[k] = std::min(cbox.lo[k], c);
+                cbox.hi[k] = std::max(cbox.hi[k], c);
+            }
+        }
+    }
+
+    void make_leaf(uint32_t node, uint32_t b, uint32_t e) {
+        nodes[node].first = b;
+        nodes[node].count = e - b;
+        nodes[node].left = 0;
+    }
+
+    // Splits idx[b, e) at its middle along the largest centroid axis (object median).
+    uint32_t median_split(uint32_t b, uint32_t e, const Box& cbox) {
+        int axis = 0;
+        float best = -1.0f;
+        for (int k = 0; k < 3; ++k) {
+            float ext = cbox.hi[k] - cbox.lo[k];
+            if (ext > best) { best = ext; axis = k; }
+        }
+        uint32_t mid = b + (e - b) / 2;
+        std::nth_element(idx.begin() + b, idx.begin() + mid, idx.begin() + e, [&](uint32_t x, uint32_t y) {
+            float cx = centroid[3 * x + axis], cy = centroid[3 * y + axis];
+            return cx < cy || (cx == cy && x < y);
+        });
+        return mid;
+    }
+
+    void build(uint32_t node, uint32_t b, uint32_t e, int depth) {
+        Box box, cbox;
+        range_bounds(b, e, box, cbox);
+        nodes[node].box = box;
+        const uint32_t n = e - b;
+        if (n <= 1) { make_leaf(node, b, e); return; }
+
+        uint32_t mid = b;
+        if (depth >= kForceMedianDepth) {
+            if (n <= (uint32_t)kMaxLeafTris) { make_leaf(node, b, e); return; }
+            mid = median_split(b, e, cbox);
+        } else {
+            // Binned SAH over the three axes: cost(split) = 1 + (A_L n_L + A_R n_R) / A, cost(leaf) = n.
+            float best_cost = INFINITY;
+            int best_axis = -1, best_bin = -1;
+            const float parent_area = std::max(half_area(box), 1e-30f);
+            std::vector<Box> bin_box(bins);
+            std::vector<uint32_t> bin_cnt(bins);
+            std::vector<float> right_area(bins);
+            std::vector<uint32_t> right_cnt(bins);
+            for (int axis = 0; axis < 3; ++axis) {
+                const float lo = cbox.lo[axis], ext = cbox.hi[axis] - cbox.lo[axis];
+                if (!(ext > 0.0f)) continue;
+                const float scale = (float)bins / ext;
+                for (int i = 0; i < bins; ++i) { bin_box[i] = empty_box(); bin_cnt[i] = 0; }
+                for (uint32_t i = b; i < e; ++i) {
+                    uint32_t p = idx[i];
+                    int bi = std::min(bins - 1, (int)((centroid[3 * p + axis] - lo) * scale));
+                    grow(bin_box[bi], prim_box[p]);
+                    bin_cnt[bi]++;
+                }
+                Box acc = empty_box();
+                uint32_t cnt = 0;
+                for (int i = bins - 1; i > 0; --i) {
+                    grow(acc, bin_box[i]);
+                    cnt += bin_cnt[i];
+                    right_area[i] = half_area(acc);
+                    right_cnt[i] = cnt;
+                }
+                acc = empty_box();
+                cnt = 0;
+                for (int i = 0; i < bins - 1; ++i) {
+                    grow(acc, bin_box[i]);
+                    cnt += bin_cnt[i];
+                    if (cnt == 0 || right_cnt[i + 1] == 0) continue;
+                    float cost = 1.0f + (half_area(acc) * cnt + right_area[i + 1] * right_cnt[i + 1]) / parent_area;
+                    if (cost < best_cost) { best_cost = cost; best_axis = axis; best_bin = i; }
+                }
+            }
+            if (n <= (uint32_t)kMaxLeafTris && (float)n <= best_cost) { make_leaf(node, b, e); return; }
+            if (best_axis < 0) {
+                if (n <= (uint32_t)kMaxLeafTris) { make_leaf(node, b, e); return; }
+                mid = median_split(b, e, cbox);
+            } else {
+                const float lo = cbox.lo[best_axis], ext = cbox.hi[best_axis] - cbox.lo[best_axis];
+                const float scale = (float)bins / ext;
+                auto it = std::partition(idx.begin() + b, idx.begin() + e, [&](uint32_t p) {
+                    int bi = std::min(bins - 1, (int)((centroid[3 * p + best_axis] - lo) * scale));
+                    return bi <= best_bin;
+                });
+                mid = (uint32_t)(it - idx.begin());
+                if (mid == b || mid == e) mid = median_split(b, e, cbox);
+            }
+        }
+
+        const uint32_t left = next.fetch_add(2);
+        nodes[node].left = left;
+        nodes[node].count = 0;
+        if (n > 65536 && spare_threads.fetch_sub(1) > 0) {
+            std::thread t([&, left, b, mid, depth] { build(left, b, mid, depth + 1); });
+            build(left + 1, mid, e, depth + 1);
+            t.join();
+        } else {
+            build(left, b, mid, depth + 1);
+            build(left + 1, mid, e, depth + 1);
+        }
+    }
+};
+
+struct WideBuilder {
+    const BinaryBuilder& bb;
+    Bvh8& out;
+    double delta;   // conservative dilation of every quantized child box, in world units
+
+    bool is_leaf(uint32_t n) const { return bb.nodes[n].count > 0; }
+
+    void emit(uint32_t wi, uint32_t bn, uint32_t depth) {
+        out.depth = std::max(out.depth, depth);
+        uint32_t ch[8];
+        int nch = 0;
+        if (is_leaf(bn)) {
+            ch[nch++] = bn;
+        } else {
+            ch[nch++] = bb.nodes[bn].left;
+            ch[nch++] = bb.nodes[bn].left + 1;
+        }
+        // Greedy collapse: open the internal child of largest surface area until 8 children.
+        while (nch < 8) {
+            int pick = -1;
+            float best = -1.0f;
+            for (int i = 0; i < nch; ++i) {
+                if (is_leaf(ch[i])) continue;
+                float a = half_area(bb.nodes[ch[i]].box);
+                if (a > best) { best = a; pick = i; }
+            }
+            if (pick < 0) break;
+            uint32_t l = bb.nodes[ch[pick]].left;
+            ch[pick] = l;
+            ch[nch++] = l + 1;
+        }
+
+        // Union box and octant-based slot assignment (greedy maximum of dot(centroid - centre, dir_s)).
+        Box u = empty_box();
+        for (int i = 0; i < nch; ++i) grow(u, bb.nodes[ch[i]].box);
+        float centre[3];
+        for (int k = 0; k < 3; ++k) centre[k] = 0.5f * (u.lo[k] + u.hi[k]);
+        int slot_of[8];
+        int child_in_slot[8];
+        for (int s = 0; s < 8; ++s) child_in_slot[s] = -1;
+        bool assigned[8] = {false, false, false, false, false, false, false, false};
+        for (int step = 0; step < nch; ++step) {
+            float best = -INFINITY;
+            int bc = -1, bs = -1;
+            for (int i = 0; i < nch; ++i) {
+                if (assigned[i]) continue;
+                const Box& cb = bb.nodes[ch[i]].box;
+                float c[3];
+                for (int k = 0; k < 3; ++k) c[k] = 0.5f * (cb.lo[k] + cb.hi[k]) - centre[k];
+                for (int s = 0; s < 8; ++s) {
+                    if (child_in_slot[s] >= 0) continue;
+                    float score = ((s & 1) ? c[0] : -c[0]) + ((s & 2) ? c[1] : -c[1]) + ((s & 4) ? c[2] : -c[2]);
+                    if (score > best) { best = score; bc = i; bs = s; }
+                }
+            }
+            assigned[bc] = true;
+            slot_of[bc] = bs;
+            child_in_slot[bs] = bc;
+        }
+        (void)slot_of;
+
+        Bvh8Node node;
+        std::memset(&node, 0, sizeof(node));
+
+        // Quantization frame: p = union.lo - delta, scale 2^e with 255 * 2^e >= extent + 2 delta.
+        double scale[3];
+        float p[3];
+        uint8_t ebias[3];
+        for (int k = 0; k < 3; ++k) {
+            double lo = (double)u.lo[k] - delta;
+            float pf = (float)lo;
+            if ((double)pf > lo) pf = std::nextafter(pf, -INFINITY);
+            double extent = ((double)u.hi[k] + delta) - (double)pf;
+            int e = 0;
+            std::frexp(extent / 255.0, &e);
+            if (e < -126) e = -126;
+            if (e > 127) throw std::runtime_error("BVH build: scene coordinates out of range");
+            // guard against rounding in the test above
+            while (std::ldexp(255.0, e) < extent) ++e;
+            p[k] = pf;
+            scale[k] = std::ldexp(1.0, e);
+            ebias[k] = (uint8_t)(e + 127);
+        }
+        node.px = p[0];
+        node.py = p[1];
+        node.pz = p[2];
+        node.ex = ebias[0];
+        node.ey = ebias[1];
+        node.ez = ebias[2];
+
+        // Children in slot order: internal ones get consecutive node indices, leaf triangles are
+        // appended to the triangle array.
+        uint32_t inner_bnodes[8];
+        int n_inner = 0;
+        node.tri_base = (uint32_t)out.tris.size();
+        uint32_t tri_off = 0;
+        uint8_t imask = 0;
+        for (int s = 0; s < 8; ++s) {
+            int ci = child_in_slot[s];
+            if (ci < 0) continue;
+            const BNode& c = bb.nodes[ch[ci]];
+            auto q = [&](int k, float lo, float hi, uint8_t& qlo, uint8_t& qhi) {
+                double a = std::floor(((double)lo - delta - (double)p[k]) / scale[k]);
+                double b = std::ceil(((double)hi + delta - (double)p[k]) / scale[k]);
+                a = std::max(0.0, std::min(255.0, a));
+                b = std::max(0.0, std::min(255.0, b));
+                qlo = (uint8_t)a;
+                qhi = (uint8_t)b;
+            };
+            q(0, c.box.lo[0], c.box.hi[0], node.qlo_x[s], node.qhi_x[s]);
+            q(1, c.box.lo[1], c.box.hi[1], node.qlo_y[s], node.qhi_y[s]);
+            q(2, c.box.lo[2], c.box.hi[2], node.qlo_z[s], node.qhi_z[s]);
+            if (c.count == 0) {
+                imask |= (uint8_t)(1u << s);
+                node.meta[s] = (uint8_t)((1u << 5) | (24u + (uint32_t)s));
+                inner_bnodes[n_inner++] = ch[ci];
+            } else {
+                const uint32_t cnt = c.count;   // 1..3
+                const uint32_t unary = (1u << cnt) - 1u;
+                node.meta[s] = (uint8_t)((unary << 5) | tri_off);
+                for (uint32_t j = 0; j < cnt; ++j) {
+                    uint32_t prim = bb.idx[c.first + j];
+                    const float* v = bb.verts + 9ull * prim;
+                    TriRecord r;
+                    r.v0x = v[0]; r.v0y = v[1]; r.v0z = v[2]; r.prim = prim;
+                    r.v1x = v[3]; r.v1y = v[4]; r.v1z = v[5]; r.pad1 = 0.0f;
+                    r.v2x = v[6]; r.v2y = v[7]; r.v2z = v[8]; r.pad2 = 0.0f;
+                    out.tris.push_back(r);
+                }
+                tri_off += cnt;
+            }
+        }
+        node.imask = imask;
+        node.child_base = (uint32_t)out.nodes.size();
+        out.nodes.resize(out.nodes.size() + n_inner);
+        out.nodes[wi] = node;
+        const uint32_t base = node.child_base;
+        for (int i = 0; i < n_inner; ++i) emit(base + (uint32_t)i, inner_bnodes[i], depth + 1);
+    }
+};
+
+}  // namespace
+
+Bvh8 build_bvh8(const float* verts, uint64_t tri_count, const BvhBuildOptions& opt) {
+    auto t0 = std::chrono::steady_clock::now();
+    Bvh8 out;
+    if (tri_count == 0) return out;
+    if (tri_count >= 0x7FFFFFFFull) throw std::runtime_error("BVH build: too many triangles");
+    const uint32_t n = (uint32_t)tri_count;
+
+    BinaryBuilder bb;
+    bb.verts = verts;
+    bb.bins = std::max(4, std::min(256, opt.sah_bins));
+    bb.prim_box.resize(n);
+    bb.centroid.resize(3ull * n);
+    bb.idx.resize(n);
+    double mag = 0.0;
+    for (uint32_t i = 0; i < n; ++i) {
+        const float* v = verts + 9ull * i;
+        Box b = empty_box();
+        for (int j = 0; j < 3; ++j) {
+            for (int k = 0; k < 3; ++k) {
+                float c = v[3 * j + k];
+                if (!std::isfinite(c)) throw std::runtime_error("BVH build: non-finite vertex coordinate");
+                b.lo[k] = std::min(b.lo[k], c);
+                b.hi[k] = std::max(b.hi[k], c);
+                mag = std::max(mag, (double)std::fabs(c));
+            }
+        }
+        bb.prim_box[i] = b;
+        for (int k = 0; k < 3; ++k) bb.centroid[3ull * i + k] = 0.5f * (b.lo[k] + b.hi[k]);
+        bb.idx[i] = i;
+    }
+    bb.nodes.resize(2ull * n);
+    int hw = opt.max_threads > 0 ? opt.max_threads : (int)std::thread::hardware_concurrency();
+    bb.spare_threads = std::max(0, hw - 1);
+    bb.build(0, 0, n, 0);
+    out.binary_nodes = bb.next.load();
+
+    // Dilation of quantized boxes: 2^-18 of the scene's coordinate magnitude, which covers the float
+    // rounding of the slab test for ray origins within ~20x that magnitude.
+    double delta = std::ldexp(std::max(mag, 1e-20), -18);
+    out.nodes.resize(1);
+    out.tris.reserve(n);
+    WideBuilder wb{bb, out, delta};
+    wb.emit(0, 0, 1);
+    if (out.depth > kMaxBvhDepth) throw std::runtime_error("BVH build: tree deeper than the traversal stack");
+    out.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return out;
+}
+
+}  // namespace rt

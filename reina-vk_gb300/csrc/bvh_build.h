@@ -1,0 +1,33 @@
+// Host BVH builder: binned-SAH binary BVH -> 8-wide collapse -> conservatively quantized BVH8 nodes.
+// Replaces the opaque driver builds of the reference (BLAS per model, src/graphics/Blas.cpp:41-113;
+// TLAS over instances, src/tools/vktools.cpp:460-596) with an explicit structure that software
+// traversal on the GB300 can read.
+#pragma once
+
+#include <cstdint>
+#include <vector>
+
+#include "rt_common.h"
+
+namespace rt {
+
+struct Bvh8 {
+    std::vector<Bvh8Node> nodes;   // node 0 is the root (empty vector for an empty scene)
+    std::vector<TriRecord> tris;   // leaf-ordered traversal triangles
+    uint32_t depth = 0;            // number of BVH8 levels
+    uint32_t binary_nodes = 0;
+    double seconds = 0.0;
+};
+
+struct BvhBuildOptions {
+    int sah_bins = 32;
+    int max_threads = 0;           // 0 = std::thread::hardware_concurrency()
+};
+
+// `verts` holds 9 floats per triangle (v0, v1, v2 in world space); triangle i gets id i.
+Bvh8 build_bvh8(const float* verts, uint64_t tri_count, const BvhBuildOptions& opt = BvhBuildOptions());
+
+// Maximum BVH8 depth the traversal kernels accept (their stack holds one entry per level).
+constexpr uint32_t kMaxBvhDepth = 64;
+
+}  // namespace rt

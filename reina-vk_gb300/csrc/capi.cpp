@@ -1,0 +1,327 @@
+// C ABI of the library (include/reina/reina_c.h): handles, status codes and thread-local messages.
+#include <cstring>
+#include <memory>
+#include <new>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime_api.h>
+
+#include "../../include/reina/reina_c.h"
+#include "errors.h"
+#include "generators.h"
+#include "kernels.h"
+#include "scene.h"
+
+using rt::check_cuda;
+using rt::fail;
+
+struct reina_ctx {
+    int device = 0;
+    int sm_count = 0;
+    cudaStream_t streams[2] = {nullptr, nullptr};
+    rt::DeviceBuffer err;        // u32 device error flag, OR-ed by kernels
+    rt::DeviceBuffer counters;   // u64 x 2 traversal counters
+    rt::DeviceBuffer rays, hits; // staging for host-buffer ray casts
+};
+
+struct reina_scene {
+    reina_ctx* ctx = nullptr;
+    std::unique_ptr<rt::Scene> s;
+};
+
+namespace {
+
+thread_local std::string g_error;
+
+template <class F>
+int guard(F&& f) {
+    try {
+        f();
+        return REINA_OK;
+    } catch (const rt::Error& e) {
+        g_error = e.what();
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        g_error = "host allocation failed";
+        return REINA_ERR_OOM;
+    } catch (const std::exception& e) {
+        g_error = e.what();
+        return REINA_ERR_INVALID;
+    } catch (...) {
+        g_error = "unknown error";
+        return REINA_ERR_INVALID;
+    }
+}
+
+void need(bool cond, const char* msg) {
+    if (!cond) fail(REINA_ERR_INVALID, msg);
+}
+
+void use_device(const reina_ctx* ctx) {
+    if (ctx->device < 0) fail(REINA_ERR_STATE, "host-only context (device -1) cannot run GPU work");
+    check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
+}
+
+const rt::Scene& built_scene(const reina_scene* scene) {
+    need(scene && scene->s, "scene is NULL");
+    if (!scene->s->built()) fail(REINA_ERR_STATE, "scene is not built (call reina_scene_build)");
+    return *scene->s;
+}
+
+rt::ModelData to_model(const reina_model_data* m) {
+    need(m != nullptr, "model data is NULL");
+    need(m->vertices || m->vertex_count == 0, "vertices is NULL");
+    need(m->indices || m->index_count == 0, "indices is NULL");
+    need(m->tbns || m->tbn_count == 0, "tbns is NULL");
+    need(m->tbn_indices || m->tbn_index_count == 0, "tbn_indices is NULL");
+    need(m->tex_coords || m->tex_coord_count == 0, "tex_coords is NULL");
+    need(m->tex_indices || m->tex_index_count == 0, "tex_indices is NULL");
+    rt::ModelData d;
+    d.vertices.assign(m->vertices, m->vertices + 4 * m->vertex_count);
+    d.indices.assign(m->indices, m->indices + m->index_count);
+    d.tbns.assign(m->tbns, m->tbns + 9 * m->tbn_count);
+    d.tbn_indices.assign(m->tbn_indices, m->tbn_indices + m->tbn_index_count);
+    d.tex_coords.assign(m->tex_coords, m->tex_coords + 2 * m->tex_coord_count);
+    d.tex_indices.assign(m->tex_indices, m->tex_indices + m->tex_index_count);
+    return d;
+}
+
+uint32_t check_device_errors(reina_ctx* ctx, cudaStream_t st) {
+    uint32_t e = 0;
+    check_cuda(cudaMemcpyAsync(&e, ctx->err.get(), sizeof(uint32_t), cudaMemcpyDeviceToHost, st), "cudaMemcpyAsync err");
+    check_cuda(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+    if (e) {
+        check_cuda(cudaMemsetAsync(ctx->err.get(), 0, sizeof(uint32_t), st), "cudaMemsetAsync err");
+        check_cuda(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+    }
+    return e;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* reina_last_error(void) { return g_error.c_str(); }
+
+const char* reina_version(void) { return "reina-gb300 0.1 sm_103a"; }
+
+int reina_ctx_create(const reina_ctx_options* options, reina_ctx** out_ctx) {
+    return guard([&] {
+        need(out_ctx != nullptr, "out_ctx is NULL");
+        *out_ctx = nullptr;
+        auto ctx = std::make_unique<reina_ctx>();
+        ctx->device = options ? options->device : 0;
+        if (ctx->device == -1) {   // host-only: scene assembly and BVH build without a GPU
+            *out_ctx = ctx.release();
+            return;
+        }
+        int count = 0;
+        check_cuda(cudaGetDeviceCount(&count), "cudaGetDeviceCount");
+        if (ctx->device < 0 || ctx->device >= count) fail(REINA_ERR_INVALID, "device ordinal out of range");
+        use_device(ctx.get());
+        check_cuda(cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, ctx->device), "cudaDeviceGetAttribute");
+        for (auto& s : ctx->streams) check_cuda(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "cudaStreamCreate");
+        ctx->err.alloc(sizeof(uint32_t));
+        ctx->counters.alloc(2 * sizeof(unsigned long long));
+        check_cuda(cudaMemset(ctx->err.get(), 0, sizeof(uint32_t)), "cudaMemset");
+        *out_ctx = ctx.release();
+    });
+}
+
+void reina_ctx_destroy(reina_ctx* ctx) {
+    if (!ctx) return;
+    if (ctx->device >= 0) cudaSetDevice(ctx->device);
+    for (auto& s : ctx->streams)
+        if (s) cudaStreamDestroy(s);
+    delete ctx;
+}
+
+int reina_ctx_sm_count(const reina_ctx* ctx) { return ctx ? ctx->sm_count : 0; }
+
+int reina_scene_create(reina_ctx* ctx, reina_scene** out_scene) {
+    return guard([&] {
+        need(ctx && out_scene, "NULL argument");
+        auto s = std::make_unique<reina_scene>();
+        s->ctx = ctx;
+        s->s = std::make_unique<rt::Scene>(ctx->device);
+        *out_scene = s.release();
+    });
+}
+
+void reina_scene_destroy(reina_scene* scene) {
+    if (!scene) return;
+    if (scene->ctx && scene->ctx->device >= 0) cudaSetDevice(scene->ctx->device);
+    delete scene;
+}
+
+int reina_scene_define_object(reina_scene* scene, const reina_model_data* model, uint32_t* out_object_id) {
+    return guard([&] {
+        need(scene && scene->s && out_object_id, "NULL argument");
+        *out_object_id = scene->s->define_object(to_model(model));
+    });
+}
+
+int reina_scene_add_instance(reina_scene* scene, uint32_t object_id, const float transform[16],
+                             const reina_material* material) {
+    return guard([&] {
+        need(scene && scene->s && transform && material, "NULL argument");
+        scene->s->add_instance(object_id, transform, *material);
+    });
+}
+
+int reina_scene_add_instance_per_face(reina_scene* scene, uint32_t object_id, const float transform[16],
+                                      const reina_material* materials, uint32_t material_count,
+                                      const uint32_t* face_material) {
+    return guard([&] {
+        need(scene && scene->s && transform, "NULL argument");
+        scene->s->add_instance_per_face(object_id, transform, materials, material_count, face_material);
+    });
+}
+
+int reina_scene_build(reina_scene* scene, uint32_t require_emissive) {
+    return guard([&] {
+        need(scene && scene->s, "scene is NULL");
+        if (scene->ctx->device >= 0) use_device(scene->ctx);
+        scene->s->build(require_emissive != 0);
+    });
+}
+
+float reina_scene_emissive_weight(const reina_scene* scene) {
+    return (scene && scene->s) ? scene->s->emissive_weight() : 0.0f;
+}
+
+int reina_scene_get_stats(const reina_scene* scene, reina_scene_stats* out) {
+    return guard([&] {
+        const rt::Scene& s = built_scene(scene);
+        need(out != nullptr, "out_stats is NULL");
+        std::memset(out, 0, sizeof(*out));
+        out->triangle_count = s.triangle_count();
+        out->instance_count = s.instance_count();
+        out->node_count = s.bvh().nodes.size();
+        out->node_bytes = sizeof(rt::Bvh8Node);
+        out->triangle_bytes = sizeof(rt::TriRecord);
+        out->device_bytes = s.device_bytes();
+        out->max_depth = s.bvh().depth;
+        out->leaf_triangles_max = rt::kMaxLeafTris;
+        out->build_seconds = s.bvh().seconds;
+        s.bounds(out->bounds_min, out->bounds_max);
+    });
+}
+
+int reina_scene_export_bvh(const reina_scene* scene, void* nodes_out, void* triangles_out) {
+    return guard([&] {
+        const rt::Scene& s = built_scene(scene);
+        if (nodes_out) std::memcpy(nodes_out, s.bvh().nodes.data(), s.bvh().nodes.size() * sizeof(rt::Bvh8Node));
+        if (triangles_out) std::memcpy(triangles_out, s.bvh().tris.data(), s.bvh().tris.size() * sizeof(rt::TriRecord));
+    });
+}
+
+int reina_scene_prim_info(const reina_scene* scene, uint32_t prim, uint32_t* out_instance, uint32_t* out_primitive) {
+    return guard([&] { built_scene(scene).prim_info(prim, out_instance, out_primitive); });
+}
+
+int reina_raycast_device(reina_ctx* ctx, const reina_scene* scene, const void* d_rays, uint64_t count, void* d_hits,
+                         uint32_t flags, void* stream) {
+    return guard([&] {
+        need(ctx != nullptr, "ctx is NULL");
+        const rt::Scene& s = built_scene(scene);
+        need(flags <= REINA_RAY_ANY, "flags must be REINA_RAY_CLOSEST or REINA_RAY_ANY");
+        need(count == 0 || (d_rays && d_hits), "NULL ray or hit buffer");
+        need(((uintptr_t)d_rays % 16) == 0 && ((uintptr_t)d_hits % 16) == 0, "ray and hit buffers must be 16-byte aligned");
+        use_device(ctx);
+        rt::launch_raycast(s.device_view(), static_cast<const rt::Ray*>(d_rays), count, static_cast<rt::Hit*>(d_hits),
+                           flags == REINA_RAY_ANY, ctx->err.as<uint32_t>(), static_cast<cudaStream_t>(stream));
+        check_cuda(cudaGetLastError(), "raycast launch");
+    });
+}
+
+int reina_raycast(reina_ctx* ctx, const reina_scene* scene, const reina_ray* rays, uint64_t count, reina_hit* hits,
+                  uint32_t flags) {
+    return guard([&] {
+        need(ctx != nullptr, "ctx is NULL");
+        const rt::Scene& s = built_scene(scene);
+        need(flags <= REINA_RAY_ANY, "flags must be REINA_RAY_CLOSEST or REINA_RAY_ANY");
+        need(count == 0 || (rays && hits), "NULL ray or hit buffer");
+        if (count == 0) return;
+        use_device(ctx);
+        ctx->rays.reserve(count * sizeof(rt::Ray));
+        ctx->hits.reserve(count * sizeof(rt::Hit));
+        // Pipeline copies and traversal over chunks on two streams.
+        const uint64_t chunk = count < (1ull << 20) ? count : std::max<uint64_t>(1ull << 19, (count + 7) / 8);
+        int k = 0;
+        for (uint64_t off = 0; off < count; off += chunk, ++k) {
+            const uint64_t n = std::min(chunk, count - off);
+            cudaStream_t st = ctx->streams[k & 1];
+            rt::Ray* dr = ctx->rays.as<rt::Ray>() + off;
+            rt::Hit* dh = ctx->hits.as<rt::Hit>() + off;
+            check_cuda(cudaMemcpyAsync(dr, rays + off, n * sizeof(rt::Ray), cudaMemcpyHostToDevice, st), "cudaMemcpyAsync H2D");
+            rt::launch_raycast(s.device_view(), dr, n, dh, flags == REINA_RAY_ANY, ctx->err.as<uint32_t>(), st);
+            check_cuda(cudaGetLastError(), "raycast launch");
+            check_cuda(cudaMemcpyAsync(hits + off, dh, n * sizeof(rt::Hit), cudaMemcpyDeviceToHost, st), "cudaMemcpyAsync D2H");
+        }
+        check_cuda(cudaStreamSynchronize(ctx->streams[1]), "cudaStreamSynchronize");
+        const uint32_t e = check_device_errors(ctx, ctx->streams[0]);
+        if (e) fail(REINA_ERR_DEVICE, "traversal kernel raised error flag " + std::to_string(e));
+    });
+}
+
+int reina_raycast_counters(reina_ctx* ctx, const reina_scene* scene, const void* d_rays, uint64_t count, uint32_t flags,
+                           uint64_t* out_nodes_visited, uint64_t* out_triangles_tested, void* stream) {
+    return guard([&] {
+        need(ctx != nullptr, "ctx is NULL");
+        const rt::Scene& s = built_scene(scene);
+        need(flags <= REINA_RAY_ANY, "flags must be REINA_RAY_CLOSEST or REINA_RAY_ANY");
+        need(count == 0 || d_rays, "NULL ray buffer");
+        use_device(ctx);
+        cudaStream_t st = static_cast<cudaStream_t>(stream);
+        check_cuda(cudaMemsetAsync(ctx->counters.get(), 0, 2 * sizeof(unsigned long long), st), "cudaMemsetAsync");
+        rt::launch_raycast_counters(s.device_view(), static_cast<const rt::Ray*>(d_rays), count, flags == REINA_RAY_ANY,
+                                    ctx->counters.as<unsigned long long>(), ctx->err.as<uint32_t>(), st);
+        check_cuda(cudaGetLastError(), "raycast counters launch");
+        unsigned long long c[2] = {0, 0};
+        check_cuda(cudaMemcpyAsync(c, ctx->counters.get(), sizeof(c), cudaMemcpyDeviceToHost, st), "cudaMemcpyAsync");
+        check_cuda(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+        if (out_nodes_visited) *out_nodes_visited = c[0];
+        if (out_triangles_tested) *out_triangles_tested = c[1];
+    });
+}
+
+int reina_camera_matrices(const float pos[3], const float front[3], const float up[3], float fovy_radians, float aspect,
+                          float z_near, float z_far, float inv_view[16], float inv_proj[16]) {
+    return guard([&] {
+        need(pos && front && up && inv_view && inv_proj, "NULL argument");
+        need(aspect > 0.0f && fovy_radians > 0.0f && z_far > z_near, "bad camera parameters");
+        rt::camera_matrices(pos, front, up, fovy_radians, aspect, z_near, z_far, inv_view, inv_proj);
+    });
+}
+
+int reina_icosphere_counts(uint32_t level, uint64_t* out_vertices, uint64_t* out_triangles) {
+    return guard([&] {
+        need(level <= 12, "icosphere level must be <= 12");
+        uint64_t nv, nt;
+        rt::icosphere_counts(level, nv, nt);
+        if (out_vertices) *out_vertices = nv;
+        if (out_triangles) *out_triangles = nt;
+    });
+}
+
+int reina_gen_icosphere(uint32_t level, float amplitude, uint64_t seed, float* vertices, uint32_t* indices, float* normals) {
+    return guard([&] {
+        need(level <= 12, "icosphere level must be <= 12");
+        need(vertices && indices, "NULL output buffer");
+        rt::gen_icosphere(level, amplitude, seed, vertices, indices, normals);
+    });
+}
+
+int reina_gen_raycast_rays(uint32_t width, uint32_t height, const float cam_pos[3], const float cam_target[3],
+                           float fovy_degrees, uint64_t n_random, const float box_min[3], const float box_max[3],
+                           uint64_t seed, reina_ray* rays_out) {
+    return guard([&] {
+        need(cam_pos && cam_target && box_min && box_max && rays_out, "NULL argument");
+        rt::gen_raycast_rays(width, height, cam_pos, cam_target, fovy_degrees, n_random, box_min, box_max, seed,
+                             reinterpret_cast<rt::Ray*>(rays_out));
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,111 @@
+// Scene assembly on the host (the reference's Scene/Models/Instance/Instances classes) and the upload
+// of the assembled buffers plus the BVH8 to the GPU.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "bvh_build.h"
+#include "device_scene.h"
+#include "errors.h"
+
+namespace rt {
+
+// ModelData (src/scene/Models.h:23-30).
+struct ModelData {
+    std::vector<float> vertices;        // 4 per vertex
+    std::vector<uint32_t> indices;
+    std::vector<float> tbns;            // 9 per entry (column-major T, B, N)
+    std::vector<uint32_t> tbn_indices;
+    std::vector<float> tex_coords;      // 2 per entry
+    std::vector<uint32_t> tex_indices;
+};
+
+// ModelRange (src/scene/Models.h:9-18).
+struct ModelRange {
+    uint32_t first_vertex, first_normal, index_offset, tbns_index_offset, tex_index_offset;
+    uint32_t index_count, tbns_index_count, tex_index_count;
+};
+
+// One emissive instance's sampling data before packing (src/scene/Instance.cpp:5-53).
+struct EmissiveInfo {
+    bool emissive = false;
+    std::vector<float> cdf;
+    float area = 0.0f;
+    float weight = 0.0f;
+};
+
+struct InstanceRecord {
+    uint32_t object = 0;
+    uint32_t props_id = 0;         // instanceCustomIndex (src/tools/vktools.cpp:481)
+    uint32_t material_idx = 0;     // SBT offset (src/tools/vktools.cpp:483)
+    float transform[16];           // column-major object-to-world
+    bool per_face = false;
+    std::vector<uint32_t> face_props;   // per-face InstanceProperties ids when per_face
+    EmissiveInfo light;
+    uint32_t first_prim = 0;
+};
+
+class Scene {
+public:
+    explicit Scene(int device) : device_(device) {}
+
+    uint32_t define_object(ModelData&& model);
+    void add_instance(uint32_t object, const float transform[16], const reina_material& mat);
+    void add_instance_per_face(uint32_t object, const float transform[16], const reina_material* mats,
+                               uint32_t mat_count, const uint32_t* face_material);
+    void build(bool require_emissive);
+
+    bool built() const { return built_; }
+    float emissive_weight() const { return emissive_total_; }
+    const DeviceScene& device_view() const { return dev_; }
+    const Bvh8& bvh() const { return bvh_; }
+    uint64_t triangle_count() const { return tri_total_; }
+    size_t instance_count() const { return instances_.size(); }
+    size_t device_bytes() const;
+    int device() const { return device_; }
+    void prim_info(uint32_t prim, uint32_t* inst, uint32_t* local) const;
+    void bounds(float lo[3], float hi[3]) const;
+
+    // Host copies of the assembled buffers (as uploaded), used by the C ABI's inspection calls.
+    const std::vector<InstanceProperties>& instance_properties() const { return props_; }
+    const std::vector<EmissiveInstanceData>& emissive_data() const { return emissive_data_; }
+    const std::vector<float>& cdf_triangles() const { return cdf_triangles_; }
+    const std::vector<float>& cdf_instances() const { return cdf_instances_; }
+
+private:
+    InstanceProperties make_props(uint32_t object, const reina_material& mat) const;
+    void compute_emissive(InstanceRecord& inst, const float emission[3]);
+    void pack_emissives();
+
+    int device_;
+    bool built_ = false;
+    // Models (src/scene/Models.cpp)
+    std::vector<ModelData> models_;
+    std::vector<ModelRange> ranges_;
+    std::vector<float> all_vertices_, all_tbns_, all_tex_coords_;
+    std::vector<uint32_t> all_indices_offset_, all_tex_indices_offset_, all_tbns_indices_offset_, all_indices_non_offset_;
+    // Instances
+    std::vector<InstanceProperties> props_;
+    std::vector<InstanceRecord> instances_;
+    // Emissive packing (src/scene/Instances.cpp)
+    std::vector<EmissiveInstanceData> emissive_data_;
+    std::vector<float> cdf_triangles_, cdf_instances_;
+    float emissive_total_ = 0.0f;
+    // Flattened traversal data
+    uint64_t tri_total_ = 0;
+    std::vector<uint32_t> prim_instance_, prim_props_;
+    float bounds_lo_[3] = {0, 0, 0}, bounds_hi_[3] = {0, 0, 0};
+    Bvh8 bvh_;
+    // Device buffers
+    DeviceBuffer d_nodes_, d_tris_, d_vertices_, d_indices_, d_tbns_, d_tbn_indices_, d_tex_coords_,
+        d_tex_indices_, d_props_, d_instances_, d_prim_instance_, d_prim_props_, d_emissive_, d_cdf_tris_,
+        d_cdf_inst_;
+    DeviceScene dev_;
+};
+
+// glm-style column-major helpers shared by the scene code and the C ABI.
+void mat4_identity(float m[16]);
+
+}  // namespace rt

@@ -1,0 +1,238 @@
+// Device-side BVH8 traversal (closest hit and any hit) with a per-thread short stack in shared memory,
+// and the watertight ray/triangle test of Woop, Benthin and Wald, "Watertight Ray/Triangle
+// Intersection", JCGT 2(1), 2013.  Replaces the hardware traversal behind traceRayEXT
+// (shaders/raytrace/raytrace.rgen.glsl:159-171 and shaders/raytrace/nee.h.glsl:129-141).
+//
+// The triangle test is written with explicitly rounded intrinsics (__fmul_rn, __fadd_rn, ...), which
+// nvcc never contracts into FMAs, so that its results (hit/miss, t, u, v) are bit-identical to an IEEE
+// single-precision evaluation of the same expressions on the host.
+#pragma once
+
+#include <stdint.h>
+
+#include "device_scene.h"
+#include "rt_common.h"
+
+namespace rt {
+
+// Shared-memory stack entries per thread; deeper levels spill to a small local array.
+#ifndef RT_SMEM_STACK
+#define RT_SMEM_STACK 12
+#endif
+constexpr int kSmemStack = RT_SMEM_STACK;
+constexpr int kTotalStack = 64;          // == kMaxBvhDepth: one entry per BVH8 level at most
+constexpr uint32_t kMaxTraversalSteps = 1u << 22;
+
+constexpr uint32_t kErrStackOverflow = 1u;
+constexpr uint32_t kErrStepLimit = 2u;
+
+struct TraceRay {
+    float ox, oy, oz;
+    float dx, dy, dz;
+    float idx, idy, idz;        // reciprocal direction (box test only)
+    float tmin, tmax;
+    float sx, sy, sz;           // watertight shear constants
+    int kx, ky, kz;
+    uint32_t oct_inv;
+};
+
+__device__ __forceinline__ float pick3(float x, float y, float z, int k) { return k == 0 ? x : (k == 1 ? y : z); }
+
+__device__ __forceinline__ float safe_rcp(float d) {
+    // Only the box test uses this reciprocal; zero components become a huge finite value.
+    const float ad = fabsf(d);
+    return ad > 1e-30f ? 1.0f / d : copysignf(1e30f, d);
+}
+
+__device__ __forceinline__ TraceRay make_trace_ray(float ox, float oy, float oz, float dx, float dy, float dz,
+                                                   float tmin, float tmax) {
+    TraceRay r;
+    r.ox = ox; r.oy = oy; r.oz = oz;
+    r.dx = dx; r.dy = dy; r.dz = dz;
+    r.tmin = tmin; r.tmax = tmax;
+    r.idx = safe_rcp(dx); r.idy = safe_rcp(dy); r.idz = safe_rcp(dz);
+    const float ax = fabsf(dx), ay = fabsf(dy), az = fabsf(dz);
+    int kz = (ax >= ay) ? ((ax >= az) ? 0 : 2) : ((ay >= az) ? 1 : 2);
+    int kx = kz + 1; if (kx == 3) kx = 0;
+    int ky = kx + 1; if (ky == 3) ky = 0;
+    const float dkz = pick3(dx, dy, dz, kz);
+    if (dkz < 0.0f) { int t = kx; kx = ky; ky = t; }
+    r.kx = kx; r.ky = ky; r.kz = kz;
+    r.sx = __fdiv_rn(pick3(dx, dy, dz, kx), dkz);
+    r.sy = __fdiv_rn(pick3(dx, dy, dz, ky), dkz);
+    r.sz = __frcp_rn(dkz);
+    const uint32_t oct = (dx < 0.0f ? 1u : 0u) | (dy < 0.0f ? 2u : 0u) | (dz < 0.0f ? 4u : 0u);
+    r.oct_inv = 7u - oct;
+    return r;
+}
+
+// Watertight test; on a hit within [tmin, tmax] writes t and the barycentric weights (u of v1, v of v2).
+__device__ __forceinline__ bool intersect_triangle(const TraceRay& r, const float4& a4, const float4& b4,
+                                                   const float4& c4, float tmax, float& t_out, float& u_out,
+                                                   float& v_out) {
+    const float Ax0 = __fsub_rn(a4.x, r.ox), Ay0 = __fsub_rn(a4.y, r.oy), Az0 = __fsub_rn(a4.z, r.oz);
+    const float Bx0 = __fsub_rn(b4.x, r.ox), By0 = __fsub_rn(b4.y, r.oy), Bz0 = __fsub_rn(b4.z, r.oz);
+    const float Cx0 = __fsub_rn(c4.x, r.ox), Cy0 = __fsub_rn(c4.y, r.oy), Cz0 = __fsub_rn(c4.z, r.oz);
+    const float Akx = pick3(Ax0, Ay0, Az0, r.kx), Aky = pick3(Ax0, Ay0, Az0, r.ky), Akz = pick3(Ax0, Ay0, Az0, r.kz);
+    const float Bkx = pick3(Bx0, By0, Bz0, r.kx), Bky = pick3(Bx0, By0, Bz0, r.ky), Bkz = pick3(Bx0, By0, Bz0, r.kz);
+    const float Ckx = pick3(Cx0, Cy0, Cz0, r.kx), Cky = pick3(Cx0, Cy0, Cz0, r.ky), Ckz = pick3(Cx0, Cy0, Cz0, r.kz);
+    const float Ax = __fsub_rn(Akx, __fmul_rn(r.sx, Akz));
+    const float Ay = __fsub_rn(Aky, __fmul_rn(r.sy, Akz));
+    const float Bx = __fsub_rn(Bkx, __fmul_rn(r.sx, Bkz));
+    const float By = __fsub_rn(Bky, __fmul_rn(r.sy, Bkz));
+    const float Cx = __fsub_rn(Ckx, __fmul_rn(r.sx, Ckz));
+    const float Cy = __fsub_rn(Cky, __fmul_rn(r.sy, Ckz));
+    float U = __fsub_rn(__fmul_rn(Cx, By), __fmul_rn(Cy, Bx));
+    float V = __fsub_rn(__fmul_rn(Ax, Cy), __fmul_rn(Ay, Cx));
+    float W = __fsub_rn(__fmul_rn(Bx, Ay), __fmul_rn(By, Ax));
+    if (U == 0.0f || V == 0.0f || W == 0.0f) {
+        // Exact-sign fallback of the paper: float products are exact in double.
+        const double CxBy = __dmul_rn((double)Cx, (double)By), CyBx = __dmul_rn((double)Cy, (double)Bx);
+        const double AxCy = __dmul_rn((double)Ax, (double)Cy), AyCx = __dmul_rn((double)Ay, (double)Cx);
+        const double BxAy = __dmul_rn((double)Bx, (double)Ay), ByAx = __dmul_rn((double)By, (double)Ax);
+        U = __double2float_rn(__dsub_rn(CxBy, CyBx));
+        V = __double2float_rn(__dsub_rn(AxCy, AyCx));
+        W = __double2float_rn(__dsub_rn(BxAy, ByAx));
+    }
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
+    const float det = __fadd_rn(__fadd_rn(U, V), W);
+    if (det == 0.0f) return false;
+    const float Az = __fmul_rn(r.sz, Akz), Bz = __fmul_rn(r.sz, Bkz), Cz = __fmul_rn(r.sz, Ckz);
+    const float T = __fadd_rn(__fadd_rn(__fmul_rn(U, Az), __fmul_rn(V, Bz)), __fmul_rn(W, Cz));
+    const float rcp = __frcp_rn(det);
+    const float t = __fmul_rn(T, rcp);
+    if (!(t >= r.tmin && t <= tmax)) return false;
+    t_out = t;
+    u_out = __fmul_rn(V, rcp);
+    v_out = __fmul_rn(W, rcp);
+    return true;
+}
+
+__device__ __forceinline__ float u8f(uint32_t word, int byte) {
+    return __uint2float_rn((word >> (8 * byte)) & 0xFFu);
+}
+
+// Intersects the 8 quantized child boxes of one node; returns the hit mask in the CWBVH layout
+// (bits 24..31: internal children, reordered by the ray octant; bits 0..23: leaf triangles).
+__device__ __forceinline__ uint32_t intersect_children(const TraceRay& r, const uint4& w0, const uint4& w1,
+                                                       const uint4& w2, const uint4& w3, const uint4& w4,
+                                                       float tmax) {
+    const float px = __uint_as_float(w0.x), py = __uint_as_float(w0.y), pz = __uint_as_float(w0.z);
+    const uint32_t ex = w0.w & 0xFFu, ey = (w0.w >> 8) & 0xFFu, ez = (w0.w >> 16) & 0xFFu;
+    const uint32_t imask = w0.w >> 24;
+    const float sxd = __uint_as_float(ex << 23) * r.idx;
+    const float syd = __uint_as_float(ey << 23) * r.idy;
+    const float szd = __uint_as_float(ez << 23) * r.idz;
+    const float oxd = (px - r.ox) * r.idx;
+    const float oyd = (py - r.oy) * r.idy;
+    const float ozd = (pz - r.oz) * r.idz;
+    // Near/far plane words by direction sign (qlo_x = w2.xy, qlo_y = w2.zw, qlo_z = w3.xy,
+    // qhi_x = w3.zw, qhi_y = w4.xy, qhi_z = w4.zw).
+    const bool nx = r.idx < 0.0f, ny = r.idy < 0.0f, nz = r.idz < 0.0f;
+    const uint32_t nearx0 = nx ? w3.z : w2.x, nearx1 = nx ? w3.w : w2.y;
+    const uint32_t farx0 = nx ? w2.x : w3.z, farx1 = nx ? w2.y : w3.w;
+    const uint32_t neary0 = ny ? w4.x : w2.z, neary1 = ny ? w4.y : w2.w;
+    const uint32_t fary0 = ny ? w2.z : w4.x, fary1 = ny ? w2.w : w4.y;
+    const uint32_t nearz0 = nz ? w4.z : w3.x, nearz1 = nz ? w4.w : w3.y;
+    const uint32_t farz0 = nz ? w3.x : w4.z, farz1 = nz ? w3.y : w4.w;
+    uint32_t hitmask = 0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const int b = i & 3;
+        const uint32_t meta_word = i < 4 ? w1.z : w1.w;
+        const uint32_t meta = (meta_word >> (8 * b)) & 0xFFu;
+        const float tnx = fmaf(u8f(i < 4 ? nearx0 : nearx1, b), sxd, oxd);
+        const float tny = fmaf(u8f(i < 4 ? neary0 : neary1, b), syd, oyd);
+        const float tnz = fmaf(u8f(i < 4 ? nearz0 : nearz1, b), szd, ozd);
+        const float tfx = fmaf(u8f(i < 4 ? farx0 : farx1, b), sxd, oxd);
+        const float tfy = fmaf(u8f(i < 4 ? fary0 : fary1, b), syd, oyd);
+        const float tfz = fmaf(u8f(i < 4 ? farz0 : farz1, b), szd, ozd);
+        const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, r.tmin));
+        const float tf = fminf(fminf(tfx, tfy), fminf(tfz, tmax));
+        if (tn <= tf && meta != 0u) {
+            const uint32_t inner = (imask >> i) & 1u;
+            const uint32_t bit = (meta & 31u) ^ (inner ? r.oct_inv : 0u);
+            hitmask |= (meta >> 5) << bit;
+        }
+    }
+    return hitmask;
+}
+
+struct TraceCounters {
+    uint32_t nodes;
+    uint32_t tris;
+};
+
+// Traverses the BVH8.  `stack` points at this thread's first shared-memory stack entry; consecutive
+// entries are `stride` elements apart.  Closest hit: the lowest (t, prim) over all triangles hit in
+// [tmin, tmax].  Any hit: the first triangle found hit in [tmin, tmax].  Returns an error code
+// (0 = ok) for the caller's error flag.
+template <bool ANY, bool COUNT>
+__device__ __forceinline__ uint32_t traverse(const Bvh8Node* __restrict__ nodes, const TriRecord* __restrict__ tris,
+                                             const TraceRay& r, uint2* stack, int stride, Hit& hit,
+                                             TraceCounters& cnt) {
+    hit.prim = kMiss;
+    hit.t = r.tmax;
+    hit.u = 0.0f;
+    hit.v = 0.0f;
+    uint2 spill[kTotalStack - kSmemStack];
+    int sp = 0;
+    uint2 group = make_uint2(0u, 0x80000000u);
+    float best_t = r.tmax;
+    uint32_t err = 0;
+    const uint4* nptr = reinterpret_cast<const uint4*>(nodes);
+    const float4* tptr = reinterpret_cast<const float4*>(tris);
+    for (uint32_t step = 0;; ++step) {
+        if (step >= kMaxTraversalSteps) { err |= kErrStepLimit; break; }
+        // group.y holds node hits in bits 24..31 here.
+        const uint32_t slot_bit = 31u - __clz(group.y);
+        const uint32_t slot = (slot_bit - 24u) ^ r.oct_inv;
+        const uint32_t rel = __popc(group.y & ((1u << slot) - 1u));
+        const uint32_t child = group.x + rel;
+        group.y &= ~(1u << slot_bit);
+        if (group.y > 0x00FFFFFFu) {
+            if (sp < kSmemStack) stack[sp * stride] = group;
+            else if (sp < kTotalStack) spill[sp - kSmemStack] = group;
+            else { err |= kErrStackOverflow; break; }
+            ++sp;
+        }
+        const uint4* np = nptr + 5ull * child;
+        const uint4 w0 = __ldg(np + 0), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3), w4 = __ldg(np + 4);
+        if (COUNT) cnt.nodes++;
+        const uint32_t hm = intersect_children(r, w0, w1, w2, w3, w4, best_t);
+        group = make_uint2(w1.x, (hm & 0xFF000000u) | (w0.w >> 24));
+        uint32_t thits = hm & 0x00FFFFFFu;
+        const uint32_t tri_base = w1.y;
+        bool done = false;
+        while (thits) {
+            const int k = __ffs(thits) - 1;
+            thits &= thits - 1u;
+            const float4* tp = tptr + 3ull * (tri_base + (uint32_t)k);
+            const float4 a = __ldg(tp + 0), b = __ldg(tp + 1), c = __ldg(tp + 2);
+            if (COUNT) cnt.tris++;
+            float t, u, v;
+            if (intersect_triangle(r, a, b, c, best_t, t, u, v)) {
+                const uint32_t prim = __float_as_uint(a.w);
+                if (ANY) {
+                    hit.prim = prim; hit.t = t; hit.u = u; hit.v = v;
+                    done = true;
+                    break;
+                }
+                if (t < best_t || prim < hit.prim) {   // t <= best_t holds; equal t: lower id wins
+                    best_t = t;
+                    hit.prim = prim; hit.t = t; hit.u = u; hit.v = v;
+                }
+            }
+        }
+        if (done) break;
+        if (group.y <= 0x00FFFFFFu) {
+            if (sp == 0) break;
+            --sp;
+            group = sp < kSmemStack ? stack[sp * stride] : spill[sp - kSmemStack];
+        }
+    }
+    if (hit.prim == kMiss) hit.t = r.tmax;
+    return err;
+}
+
+}  // namespace rt

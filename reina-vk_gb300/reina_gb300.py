@@ -1,0 +1,390 @@
+"""Python mirror of the trace path's C ABI (include/reina/reina_c.h) over ctypes.
+
+It follows the reference's scene API one for one — `Scene.define_object` (src/scene/Scene.h:78),
+`Scene.add_instance` (Scene.h:114), `Scene.build` (Scene.h:116), `Scene.emissive_weight`
+(Scene.h:118) — plus the ray-cast entry points that replace traceRayEXT.  Errors raise `ReinaError`
+carrying the library's status code and message, where the reference throws std::runtime_error.
+
+The shared library `_build/libreina_gb300.so` must have been built (build.py); there is no fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass, field, fields
+from pathlib import Path
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "_build" / "libreina_gb300.so"
+
+REINA_OK = 0
+REINA_ERR_INVALID = -1
+REINA_ERR_CUDA = -2
+REINA_ERR_OOM = -3
+REINA_ERR_STATE = -4
+REINA_ERR_IO = -5
+REINA_ERR_NO_EMISSIVE = -6
+REINA_ERR_DEVICE = -7
+REINA_ERR_BUDGET = -8
+
+RAY_CLOSEST = 0
+RAY_ANY = 1
+MISS = 0xFFFFFFFF
+
+RAY_DTYPE = np.dtype([("org", np.float32, 3), ("tmin", np.float32), ("dir", np.float32, 3), ("tmax", np.float32)])
+HIT_DTYPE = np.dtype([("prim", np.uint32), ("t", np.float32), ("u", np.float32), ("v", np.float32)])
+NODE_BYTES = 80
+TRI_BYTES = 48
+
+
+class ReinaError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"[{code}] {message}")
+        self.code = code
+
+
+class _ModelData(C.Structure):
+    _fields_ = [
+        ("vertices", C.POINTER(C.c_float)), ("vertex_count", C.c_uint64),
+        ("indices", C.POINTER(C.c_uint32)), ("index_count", C.c_uint64),
+        ("tbns", C.POINTER(C.c_float)), ("tbn_count", C.c_uint64),
+        ("tbn_indices", C.POINTER(C.c_uint32)), ("tbn_index_count", C.c_uint64),
+        ("tex_coords", C.POINTER(C.c_float)), ("tex_coord_count", C.c_uint64),
+        ("tex_indices", C.POINTER(C.c_uint32)), ("tex_index_count", C.c_uint64),
+    ]
+
+
+class _Material(C.Structure):
+    _fields_ = [
+        ("material_idx", C.c_uint32), ("texture_id", C.c_int32), ("normal_map_id", C.c_int32),
+        ("bump_map_id", C.c_int32), ("albedo", C.c_float * 3), ("emission", C.c_float * 3),
+        ("roughness", C.c_float), ("ior", C.c_float), ("interp_normals", C.c_uint32),
+        ("absorption", C.c_float), ("cull_backface", C.c_uint32), ("anisotropic", C.c_float),
+        ("subsurface", C.c_float), ("clearcoat_gloss", C.c_float), ("sheen_tint", C.c_float * 3),
+        ("specular_tint", C.c_float * 3), ("metallic", C.c_float), ("clearcoat", C.c_float),
+        ("specular_transmission", C.c_float), ("sheen", C.c_float),
+    ]
+
+
+class _SceneStats(C.Structure):
+    _fields_ = [
+        ("triangle_count", C.c_uint64), ("instance_count", C.c_uint64), ("node_count", C.c_uint64),
+        ("node_bytes", C.c_uint64), ("triangle_bytes", C.c_uint64), ("device_bytes", C.c_uint64),
+        ("max_depth", C.c_uint32), ("leaf_triangles_max", C.c_uint32), ("build_seconds", C.c_double),
+        ("bounds_min", C.c_float * 3), ("bounds_max", C.c_float * 3),
+    ]
+
+
+class _CtxOptions(C.Structure):
+    _fields_ = [("device", C.c_int32), ("flags", C.c_uint32)]
+
+
+@dataclass
+class Material:
+    """reina::scene::Material (src/scene/Scene.h:21-46); material_idx 0 Lambertian, 1 metal,
+    2 dielectric, 3 Disney."""
+    material_idx: int = 0
+    texture_id: int = -1
+    normal_map_id: int = -1
+    bump_map_id: int = -1
+    albedo: tuple = (1.0, 1.0, 1.0)
+    emission: tuple = (0.0, 0.0, 0.0)
+    roughness: float = 0.0
+    ior: float = 1.5
+    interp_normals: bool = False
+    absorption: float = 0.0
+    cull_backface: bool = False
+    anisotropic: float = 0.0
+    subsurface: float = 0.0
+    clearcoat_gloss: float = 0.0
+    sheen_tint: tuple = (1.0, 1.0, 1.0)
+    specular_tint: tuple = (1.0, 1.0, 1.0)
+    metallic: float = 0.0
+    clearcoat: float = 0.0
+    specular_transmission: float = 0.0
+    sheen: float = 0.0
+
+    def to_c(self) -> _Material:
+        m = _Material()
+        for f in fields(self):
+            v = getattr(self, f.name)
+            if isinstance(v, (tuple, list, np.ndarray)):
+                arr = getattr(m, f.name)
+                for i in range(3):
+                    arr[i] = float(v[i])
+            elif isinstance(v, bool):
+                setattr(m, f.name, 1 if v else 0)
+            else:
+                setattr(m, f.name, v)
+        return m
+
+
+_lib = None
+
+
+def library_path() -> Path:
+    return Path(os.environ.get("REINA_GB300_LIB", str(LIB_PATH)))
+
+
+def load_library() -> C.CDLL:
+    """Loads the CUDA library; raises if it has not been built (the trace path has no CPU fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = library_path()
+    if not path.exists():
+        raise RuntimeError(f"trace-path library not built: {path} (run reina-vk_gb300/build.py)")
+    lib = C.CDLL(str(path))
+    P, U32, U64, I32, F = C.c_void_p, C.c_uint32, C.c_uint64, C.c_int, C.c_float
+    sig = {
+        "reina_last_error": (C.c_char_p, []),
+        "reina_version": (C.c_char_p, []),
+        "reina_ctx_create": (I32, [C.POINTER(_CtxOptions), C.POINTER(P)]),
+        "reina_ctx_destroy": (None, [P]),
+        "reina_ctx_sm_count": (I32, [P]),
+        "reina_scene_create": (I32, [P, C.POINTER(P)]),
+        "reina_scene_destroy": (None, [P]),
+        "reina_scene_define_object": (I32, [P, C.POINTER(_ModelData), C.POINTER(U32)]),
+        "reina_scene_add_instance": (I32, [P, U32, C.POINTER(C.c_float), C.POINTER(_Material)]),
+        "reina_scene_add_instance_per_face": (I32, [P, U32, C.POINTER(C.c_float), C.POINTER(_Material), U32,
+                                                    C.POINTER(U32)]),
+        "reina_scene_build": (I32, [P, U32]),
+        "reina_scene_emissive_weight": (F, [P]),
+        "reina_scene_get_stats": (I32, [P, C.POINTER(_SceneStats)]),
+        "reina_scene_export_bvh": (I32, [P, P, P]),
+        "reina_scene_prim_info": (I32, [P, U32, C.POINTER(U32), C.POINTER(U32)]),
+        "reina_raycast": (I32, [P, P, P, U64, P, U32]),
+        "reina_raycast_device": (I32, [P, P, P, U64, P, U32, P]),
+        "reina_raycast_counters": (I32, [P, P, P, U64, U32, C.POINTER(U64), C.POINTER(U64), P]),
+        "reina_camera_matrices": (I32, [P, P, P, F, F, F, F, P, P]),
+        "reina_icosphere_counts": (I32, [U32, C.POINTER(U64), C.POINTER(U64)]),
+        "reina_gen_icosphere": (I32, [U32, F, U64, P, P, P]),
+        "reina_gen_raycast_rays": (I32, [U32, U32, P, P, F, U64, P, P, U64, P]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _check(status: int) -> None:
+    if status != REINA_OK:
+        msg = _lib.reina_last_error().decode("utf-8", "replace")
+        raise ReinaError(status, msg)
+
+
+def _ptr(a: np.ndarray | None):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _f32(a, shape_last=None) -> np.ndarray:
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    return a
+
+
+def _u32(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.uint32)
+
+
+def transform_to_c(m) -> np.ndarray:
+    """4x4 matrix in math (row, column) indexing -> 16 floats column-major (glm::mat4 memory order)."""
+    m = np.asarray(m, dtype=np.float32).reshape(4, 4)
+    return np.ascontiguousarray(m.T.reshape(16))
+
+
+class Context:
+    def __init__(self, device: int = 0):
+        lib = load_library()
+        opts = _CtxOptions(device, 0)
+        h = C.c_void_p()
+        _check(lib.reina_ctx_create(C.byref(opts), C.byref(h)))
+        self._h = h
+        self.device = device
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def sm_count(self) -> int:
+        return int(_lib.reina_ctx_sm_count(self._h))
+
+    def close(self) -> None:
+        if self._h:
+            _lib.reina_ctx_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Scene:
+    """reina::scene::Scene (src/scene/Scene.h:62-138)."""
+
+    def __init__(self, ctx: Context):
+        self.ctx = ctx
+        h = C.c_void_p()
+        _check(_lib.reina_scene_create(ctx.handle, C.byref(h)))
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self) -> None:
+        if self._h:
+            _lib.reina_scene_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def define_object(self, vertices, indices, tbns=None, tbn_indices=None, tex_coords=None, tex_indices=None) -> int:
+        """Scene::defineObject(ModelData) — vertices (N,4) or (N,3) (w = 1 added), indices (3M,)."""
+        v = np.asarray(vertices, dtype=np.float32)
+        if v.ndim == 2 and v.shape[1] == 3:
+            v = np.concatenate([v, np.ones((v.shape[0], 1), np.float32)], axis=1)
+        v = np.ascontiguousarray(v.reshape(-1, 4))
+        idx = _u32(np.asarray(indices).reshape(-1))
+        tb = None if tbns is None else _f32(np.asarray(tbns).reshape(-1, 9))
+        tbi = None if tbn_indices is None else _u32(np.asarray(tbn_indices).reshape(-1))
+        tc = None if tex_coords is None else _f32(np.asarray(tex_coords).reshape(-1, 2))
+        ti = None if tex_indices is None else _u32(np.asarray(tex_indices).reshape(-1))
+        md = _ModelData(
+            v.ctypes.data_as(C.POINTER(C.c_float)), v.shape[0],
+            idx.ctypes.data_as(C.POINTER(C.c_uint32)), idx.size,
+            None if tb is None else tb.ctypes.data_as(C.POINTER(C.c_float)), 0 if tb is None else tb.shape[0],
+            None if tbi is None else tbi.ctypes.data_as(C.POINTER(C.c_uint32)), 0 if tbi is None else tbi.size,
+            None if tc is None else tc.ctypes.data_as(C.POINTER(C.c_float)), 0 if tc is None else tc.shape[0],
+            None if ti is None else ti.ctypes.data_as(C.POINTER(C.c_uint32)), 0 if ti is None else ti.size,
+        )
+        out = C.c_uint32()
+        _check(_lib.reina_scene_define_object(self._h, C.byref(md), C.byref(out)))
+        return int(out.value)
+
+    def add_instance(self, object_id: int, transform=None, material: Material | None = None) -> None:
+        t = transform_to_c(np.eye(4) if transform is None else transform)
+        m = (material or Material()).to_c()
+        _check(_lib.reina_scene_add_instance(self._h, object_id, t.ctypes.data_as(C.POINTER(C.c_float)), C.byref(m)))
+
+    def add_object(self, vertices, indices, transform=None, material: Material | None = None, **kw) -> int:
+        """Scene::addObject(ModelData, transform, material) (src/scene/Scene.h:106)."""
+        oid = self.define_object(vertices, indices, **kw)
+        self.add_instance(oid, transform, material)
+        return oid
+
+    def add_instance_per_face(self, object_id: int, transform, materials: list, face_material) -> None:
+        t = transform_to_c(np.eye(4) if transform is None else transform)
+        arr = (_Material * len(materials))(*[m.to_c() for m in materials])
+        fm = _u32(face_material)
+        _check(_lib.reina_scene_add_instance_per_face(self._h, object_id, t.ctypes.data_as(C.POINTER(C.c_float)), arr,
+                                                      len(materials), fm.ctypes.data_as(C.POINTER(C.c_uint32))))
+
+    def build(self, require_emissive: bool = False) -> None:
+        _check(_lib.reina_scene_build(self._h, 1 if require_emissive else 0))
+
+    @property
+    def emissive_weight(self) -> float:
+        return float(_lib.reina_scene_emissive_weight(self._h))
+
+    def stats(self) -> dict:
+        s = _SceneStats()
+        _check(_lib.reina_scene_get_stats(self._h, C.byref(s)))
+        d = {f[0]: getattr(s, f[0]) for f in _SceneStats._fields_}
+        d["bounds_min"] = list(s.bounds_min)
+        d["bounds_max"] = list(s.bounds_max)
+        return d
+
+    def export_bvh(self) -> tuple[np.ndarray, np.ndarray]:
+        st = self.stats()
+        nodes = np.zeros((st["node_count"], NODE_BYTES), np.uint8)
+        tris = np.zeros((st["triangle_count"], TRI_BYTES), np.uint8)
+        _check(_lib.reina_scene_export_bvh(self._h, _ptr(nodes), _ptr(tris)))
+        return nodes, tris
+
+    def prim_info(self, prim: int) -> tuple[int, int]:
+        a, b = C.c_uint32(), C.c_uint32()
+        _check(_lib.reina_scene_prim_info(self._h, prim, C.byref(a), C.byref(b)))
+        return int(a.value), int(b.value)
+
+
+def raycast(ctx: Context, scene: Scene, rays: np.ndarray, flags: int = RAY_CLOSEST) -> np.ndarray:
+    """Host-buffer ray cast: rays -> hits (structured arrays RAY_DTYPE / HIT_DTYPE)."""
+    rays = np.ascontiguousarray(rays)
+    if rays.dtype != RAY_DTYPE:
+        rays = np.ascontiguousarray(rays.view(np.float32).reshape(-1, 8)).view(RAY_DTYPE).reshape(-1)
+    hits = np.empty(rays.shape[0], HIT_DTYPE)
+    _check(_lib.reina_raycast(ctx.handle, scene.handle, _ptr(rays), rays.shape[0], _ptr(hits), flags))
+    return hits
+
+
+def raycast_into(ctx: Context, scene: Scene, rays_ptr: int, count: int, hits_ptr: int, flags: int = RAY_CLOSEST) -> None:
+    """Host-buffer ray cast on caller-provided (ideally pinned) host memory."""
+    _check(_lib.reina_raycast(ctx.handle, scene.handle, C.c_void_p(rays_ptr), count, C.c_void_p(hits_ptr), flags))
+
+
+def raycast_device(ctx: Context, scene: Scene, d_rays: int, count: int, d_hits: int, flags: int = RAY_CLOSEST,
+                   stream: int = 0) -> None:
+    _check(_lib.reina_raycast_device(ctx.handle, scene.handle, C.c_void_p(d_rays), count, C.c_void_p(d_hits), flags,
+                                     C.c_void_p(stream)))
+
+
+def raycast_counters(ctx: Context, scene: Scene, d_rays: int, count: int, flags: int = RAY_CLOSEST,
+                     stream: int = 0) -> tuple[int, int]:
+    a, b = C.c_uint64(), C.c_uint64()
+    _check(_lib.reina_raycast_counters(ctx.handle, scene.handle, C.c_void_p(d_rays), count, flags, C.byref(a),
+                                       C.byref(b), C.c_void_p(stream)))
+    return int(a.value), int(b.value)
+
+
+def camera_matrices(pos, front, up=(0.0, 1.0, 0.0), fovy_radians=np.radians(45.0), aspect=1.0, z_near=0.1,
+                    z_far=100.0) -> tuple[np.ndarray, np.ndarray]:
+    """inverse(glm::lookAt) and inverse(glm::perspective), 16 floats column-major each."""
+    lib = load_library()
+    p, f, u = (np.asarray(x, np.float32) for x in (pos, front, up))
+    iv, ip = np.zeros(16, np.float32), np.zeros(16, np.float32)
+    _check(lib.reina_camera_matrices(_ptr(p), _ptr(f), _ptr(u), float(fovy_radians), float(aspect), float(z_near),
+                                     float(z_far), _ptr(iv), _ptr(ip)))
+    return iv, ip
+
+
+def icosphere(level: int, amplitude: float = 0.0, seed: int = 1) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+    """Level-L icosphere, vertices radially displaced by 3-octave value noise; returns (V (N,4), I (3M,), N (N,3))."""
+    lib = load_library()
+    nv, nt = C.c_uint64(), C.c_uint64()
+    _check(lib.reina_icosphere_counts(level, C.byref(nv), C.byref(nt)))
+    v = np.zeros((nv.value, 4), np.float32)
+    i = np.zeros(3 * nt.value, np.uint32)
+    n = np.zeros((nv.value, 3), np.float32)
+    _check(lib.reina_gen_icosphere(level, float(amplitude), seed, _ptr(v), _ptr(i), _ptr(n)))
+    return v, i, n
+
+
+def raycast_rays(width: int, height: int, cam_pos, cam_target, fovy_degrees: float, n_random: int, box_min, box_max,
+                 seed: int = 1) -> np.ndarray:
+    lib = load_library()
+    out = np.zeros(width * height + n_random, RAY_DTYPE)
+    cp, ct, bmin, bmax = (np.asarray(x, np.float32) for x in (cam_pos, cam_target, box_min, box_max))
+    _check(lib.reina_gen_raycast_rays(width, height, _ptr(cp), _ptr(ct), float(fovy_degrees), n_random, _ptr(bmin),
+                                      _ptr(bmax), seed, _ptr(out)))
+    return out
+
+
+def version() -> str:
+    return load_library().reina_version().decode()
