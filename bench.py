@@ -162,6 +162,17 @@ def run_ours(args) -> dict | None:
     def step(flags=R.RAY_CLOSEST):
         R.raycast_device(ctx, scene, d_rays.data_ptr(), n, d_hits.data_ptr(), flags, sptr)
 
+    if args.profile:
+        # Profiling mode (for ncu): one warm-up, then `steps` closest-hit launches and one any-hit launch.
+        step()
+        for _ in range(args.steps):
+            step()
+        step(R.RAY_ANY)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile": "raycast_l8", "launches": args.steps + 2, "nodes_per_ray": nodes_v / n,
+                          "tris_per_ray": tris_t / n, "bytes_per_ray": bytes_per_ray}))
+        return None
+
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
@@ -335,6 +346,7 @@ def main() -> int:
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cpu-sample", type=int, default=1 << 21)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", action="store_true", help="launch the kernels a few times for ncu and exit")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     out = run_reference(args) if args.impl == "reference" else run_ours(args)

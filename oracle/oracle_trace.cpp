@@ -87,6 +87,33 @@ bool watertight(const PreRay<T>& r, const float* tri, T tmax_now, T& t_out, T& u
     return true;
 }
 
+// The reported t, u, v of a float-mode hit: the same watertight expressions evaluated in double for the
+// selected triangle (no range or sign checks) and rounded to float.  Ray-cast APIs report these values;
+// the float test above only decides which triangle is hit.
+// Barycentric weights from exact double-precision signed volumes d . (C x B), d . (A x C), d . (B x A);
+// t = (U A_kz + V B_kz + W C_kz) / (det d_kz); the ratios are taken in float.
+inline void refine64(const RayRec& ray, const float* tri, float& t, float& u, float& v) {
+    const PreRay<double> r = precompute<double>(ray);
+    const Vec3<double> A = Vec3<double>(tri[0], tri[1], tri[2]) - r.o;
+    const Vec3<double> B = Vec3<double>(tri[3], tri[4], tri[5]) - r.o;
+    const Vec3<double> C = Vec3<double>(tri[6], tri[7], tri[8]) - r.o;
+    auto trip = [&](const Vec3<double>& p, const Vec3<double>& q) {
+        const double cx = p.y * q.z - p.z * q.y;
+        const double cy = p.z * q.x - p.x * q.z;
+        const double cz = p.x * q.y - p.y * q.x;
+        return (r.d.x * cx + r.d.y * cy) + r.d.z * cz;
+    };
+    const double U = trip(C, B), V = trip(A, C), W = trip(B, A);
+    const double det = (U + V) + W;
+    if (det == 0.0) return;
+    const double Tn = (U * A[r.kz] + V * B[r.kz]) + W * C[r.kz];
+    const double den = det * r.d[r.kz];
+    const float fdet = (float)det;
+    t = (float)Tn / (float)den;
+    u = (float)V / fdet;
+    v = (float)W / fdet;
+}
+
 template <class T>
 struct BestHit {
     uint32_t prim = kMiss;
@@ -286,6 +313,32 @@ BestHit<T> trace_brute(const float* tris9, uint64_t ntri, const RayRec& ray, boo
     return best;
 }
 
+inline HitRec finish32(const BestHit<float>& r, const RayRec& ray, const float* tri) {
+    HitRec h{r.prim, r.t, r.u, r.v};
+    if (tri) refine64(ray, tri, h.t, h.u, h.v);
+    return h;
+}
+
+// Closest hit as the renderer sees it: float mode reports the refined t/u/v (what the GPU reports).
+int trace_closest_f(void* bvh, const RayRec& r, uint32_t& prim, double& t, double& u, double& v, int precision) {
+    const Bvh& b = *static_cast<Bvh*>(bvh);
+    if (precision == 64) {
+        const BestHit<double> h = trace_bvh<double>(b, r, false, nullptr);
+        prim = h.prim; t = h.t; u = h.u; v = h.v;
+    } else {
+        const BestHit<float> h = trace_bvh<float>(b, r, false, nullptr);
+        const HitRec f = finish32(h, r, h.prim == kMiss ? nullptr : b.tris.data() + 9ull * h.prim);
+        prim = f.prim; t = f.t; u = f.u; v = f.v;
+    }
+    return prim != kMiss;
+}
+
+bool trace_occluded(void* bvh, const RayRec& r, int precision) {
+    const Bvh& b = *static_cast<Bvh*>(bvh);
+    if (precision == 64) return trace_bvh<double>(b, r, true, nullptr).prim != kMiss;
+    return trace_bvh<float>(b, r, true, nullptr).prim != kMiss;
+}
+
 template <class F>
 static void parallel_for(uint64_t n, int threads, F&& f) {
     if (threads <= 0) threads = (int)std::max(1u, std::thread::hardware_concurrency());
@@ -330,26 +383,28 @@ void oracle_bvh_destroy(void* h) { delete static_cast<Bvh*>(h); }
 void oracle_raycast(void* h, const RayRec* rays, uint64_t n, int any, int precision, int threads, HitRec* hits32,
                     HitRec64* hits64) {
     const Bvh& b = *static_cast<Bvh*>(h);
+    auto tris_of = [&](uint32_t p) { return p == kMiss ? nullptr : b.tris.data() + 9ull * p; };
     parallel_for(n, threads, [&](uint64_t i) {
         if (precision == 64) {
             BestHit<double> r = trace_bvh<double>(b, rays[i], any != 0, nullptr);
             hits64[i] = HitRec64{r.prim, 0u, r.t, r.u, r.v};
         } else {
             BestHit<float> r = trace_bvh<float>(b, rays[i], any != 0, nullptr);
-            hits32[i] = HitRec{r.prim, r.t, r.u, r.v};
+            hits32[i] = finish32(r, rays[i], tris_of(r.prim));
         }
     });
 }
 
 void oracle_raycast_brute(const float* tris9, uint64_t ntri, const RayRec* rays, uint64_t n, int any, int precision,
                           int threads, HitRec* hits32, HitRec64* hits64) {
+    auto tris_of = [&](uint32_t p) { return p == kMiss ? nullptr : tris9 + 9ull * p; };
     parallel_for(n, threads, [&](uint64_t i) {
         if (precision == 64) {
             BestHit<double> r = trace_brute<double>(tris9, ntri, rays[i], any != 0);
             hits64[i] = HitRec64{r.prim, 0u, r.t, r.u, r.v};
         } else {
             BestHit<float> r = trace_brute<float>(tris9, ntri, rays[i], any != 0);
-            hits32[i] = HitRec{r.prim, r.t, r.u, r.v};
+            hits32[i] = finish32(r, rays[i], tris_of(r.prim));
         }
     });
 }
@@ -359,6 +414,7 @@ int oracle_test_triangle(const float* tri9, const RayRec* ray, HitRec* out) {
     const PreRay<float> r = precompute<float>(*ray);
     float t, u, v;
     if (!watertight(r, tri9, r.tmax, t, u, v)) return 0;
+    refine64(*ray, tri9, t, u, v);
     if (out) *out = HitRec{0u, t, u, v};
     return 1;
 }

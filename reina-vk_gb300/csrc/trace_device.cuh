@@ -37,6 +37,7 @@ struct TraceRay {
 };
 
 __device__ __forceinline__ float pick3(float x, float y, float z, int k) { return k == 0 ? x : (k == 1 ? y : z); }
+__device__ __forceinline__ double pick3d(double x, double y, double z, int k) { return k == 0 ? x : (k == 1 ? y : z); }
 
 __device__ __forceinline__ float safe_rcp(float d) {
     // Only the box test uses this reciprocal; zero components become a huge finite value.
@@ -108,8 +109,42 @@ __device__ __forceinline__ bool intersect_triangle(const TraceRay& r, const floa
     return true;
 }
 
+// Recomputes t, u, v of the selected triangle from double-precision signed volumes and rounds them to
+// float.  The FP32 test above decides which triangle is hit; this only sharpens the reported values
+// (FP32 barycentrics lose ~1e-5 of the triangle size when the origin is far from the triangle).
+// Vertices relative to the origin are exact in double; U, V, W = d . (C x B), d . (A x C), d . (B x A)
+// are the vertices' barycentric weights times det = U + V + W; t = (U A_kz + V B_kz + W C_kz) /
+// (det d_kz).  Only the final ratios are taken in float (no double division: GB300's FP64 rate is low).
+__device__ __forceinline__ void refine_hit(const TraceRay& r, const float4& a4, const float4& b4, const float4& c4,
+                                           Hit& h) {
+    const double ox = r.ox, oy = r.oy, oz = r.oz, dx = r.dx, dy = r.dy, dz = r.dz;
+    const double Ax = __dsub_rn(a4.x, ox), Ay = __dsub_rn(a4.y, oy), Az = __dsub_rn(a4.z, oz);
+    const double Bx = __dsub_rn(b4.x, ox), By = __dsub_rn(b4.y, oy), Bz = __dsub_rn(b4.z, oz);
+    const double Cx = __dsub_rn(c4.x, ox), Cy = __dsub_rn(c4.y, oy), Cz = __dsub_rn(c4.z, oz);
+    auto trip = [&](double px, double py, double pz, double qx, double qy, double qz) {   // d . (p x q)
+        const double cx = __dsub_rn(__dmul_rn(py, qz), __dmul_rn(pz, qy));
+        const double cy = __dsub_rn(__dmul_rn(pz, qx), __dmul_rn(px, qz));
+        const double cz = __dsub_rn(__dmul_rn(px, qy), __dmul_rn(py, qx));
+        return __dadd_rn(__dadd_rn(__dmul_rn(dx, cx), __dmul_rn(dy, cy)), __dmul_rn(dz, cz));
+    };
+    const double U = trip(Cx, Cy, Cz, Bx, By, Bz);
+    const double V = trip(Ax, Ay, Az, Cx, Cy, Cz);
+    const double W = trip(Bx, By, Bz, Ax, Ay, Az);
+    const double det = __dadd_rn(__dadd_rn(U, V), W);
+    if (det == 0.0) return;
+    const double Akz = pick3d(Ax, Ay, Az, r.kz), Bkz = pick3d(Bx, By, Bz, r.kz), Ckz = pick3d(Cx, Cy, Cz, r.kz);
+    const double Tn = __dadd_rn(__dadd_rn(__dmul_rn(U, Akz), __dmul_rn(V, Bkz)), __dmul_rn(W, Ckz));
+    const double den = __dmul_rn(det, pick3d(dx, dy, dz, r.kz));
+    const float fdet = __double2float_rn(det);
+    h.t = __fdiv_rn(__double2float_rn(Tn), __double2float_rn(den));
+    h.u = __fdiv_rn(__double2float_rn(V), fdet);
+    h.v = __fdiv_rn(__double2float_rn(W), fdet);
+}
+
+// Byte `byte` of `word` as a float, exactly: the byte placed in the mantissa of 2^23 (one byte permute),
+// minus 2^23 (one add) — cheaper than an integer-to-float conversion.
 __device__ __forceinline__ float u8f(uint32_t word, int byte) {
-    return __uint2float_rn((word >> (8 * byte)) & 0xFFu);
+    return __uint_as_float(__byte_perm(word, 0x4B000000u, 0x7540u + (uint32_t)byte)) - 8388608.0f;
 }
 
 // Intersects the 8 quantized child boxes of one node; returns the hit mask in the CWBVH layout
@@ -165,9 +200,10 @@ struct TraceCounters {
 
 // Traverses the BVH8.  `stack` points at this thread's first shared-memory stack entry; consecutive
 // entries are `stride` elements apart.  Closest hit: the lowest (t, prim) over all triangles hit in
-// [tmin, tmax].  Any hit: the first triangle found hit in [tmin, tmax].  Returns an error code
-// (0 = ok) for the caller's error flag.
-template <bool ANY, bool COUNT>
+// [tmin, tmax].  Any hit: the first triangle found hit in [tmin, tmax].  With REFINE the reported
+// t, u, v of the selected triangle are recomputed in double precision (refine_hit).  Returns an error
+// code (0 = ok) for the caller's error flag.
+template <bool ANY, bool COUNT, bool REFINE = true>
 __device__ __forceinline__ uint32_t traverse(const Bvh8Node* __restrict__ nodes, const TriRecord* __restrict__ tris,
                                              const TraceRay& r, uint2* stack, int stride, Hit& hit,
                                              TraceCounters& cnt) {
@@ -175,6 +211,7 @@ __device__ __forceinline__ uint32_t traverse(const Bvh8Node* __restrict__ nodes,
     hit.t = r.tmax;
     hit.u = 0.0f;
     hit.v = 0.0f;
+    uint32_t best_rec = 0;
     uint2 spill[kTotalStack - kSmemStack];
     int sp = 0;
     uint2 group = make_uint2(0u, 0x80000000u);
@@ -215,12 +252,14 @@ __device__ __forceinline__ uint32_t traverse(const Bvh8Node* __restrict__ nodes,
                 const uint32_t prim = __float_as_uint(a.w);
                 if (ANY) {
                     hit.prim = prim; hit.t = t; hit.u = u; hit.v = v;
+                    best_rec = tri_base + (uint32_t)k;
                     done = true;
                     break;
                 }
                 if (t < best_t || prim < hit.prim) {   // t <= best_t holds; equal t: lower id wins
                     best_t = t;
                     hit.prim = prim; hit.t = t; hit.u = u; hit.v = v;
+                    best_rec = tri_base + (uint32_t)k;
                 }
             }
         }
@@ -231,7 +270,12 @@ __device__ __forceinline__ uint32_t traverse(const Bvh8Node* __restrict__ nodes,
             group = sp < kSmemStack ? stack[sp * stride] : spill[sp - kSmemStack];
         }
     }
-    if (hit.prim == kMiss) hit.t = r.tmax;
+    if (hit.prim == kMiss) {
+        hit.t = r.tmax;
+    } else if (REFINE) {
+        const float4* tp = tptr + 3ull * best_rec;
+        refine_hit(r, __ldg(tp + 0), __ldg(tp + 1), __ldg(tp + 2), hit);
+    }
     return err;
 }
 
