@@ -201,6 +201,50 @@ int reina_raycast_counters(reina_ctx* ctx, const reina_scene* scene, const void*
                            void* stream);
 
 /* ------------------------------------------------------------------------------------------------ */
+/* Rendering — replaces Reina::traceRays (src/Reina.cpp:425-470), i.e. vkCmdTraceRaysKHR over the     */
+/* image with the raygen shader of shaders/raytrace/raytrace.rgen.glsl:250-285.                       */
+/* ------------------------------------------------------------------------------------------------ */
+enum {
+    REINA_MODE_REINA = 0,        /* the reference's integrator as shipped: NEE off (raytrace.rgen.glsl:146),
+                                  * per-pixel seed (sampleBatch*H + y)*W + x carried across samples */
+    REINA_MODE_NEE_MIS = 1       /* NEE on Lambertian and Disney hits with power-heuristic MIS; per-path
+                                  * seed hash(pixel, sampleBatch*spp + sample, seed) */
+};
+enum {
+    REINA_ENV_SKY = 0,           /* sky gradient of shaders/raytrace/raytrace.rmiss.glsl:10-19 */
+    REINA_ENV_CONSTANT = 1       /* constant environment radiance env_color */
+};
+
+typedef struct reina_render_options {
+    uint32_t width;
+    uint32_t height;
+    uint32_t mode;               /* REINA_MODE_* */
+    uint32_t seed;               /* key of the per-path seeds in REINA_MODE_NEE_MIS */
+    uint32_t env_mode;           /* REINA_ENV_* */
+    float env_color[3];
+} reina_render_options;
+
+typedef struct reina_render_stats {
+    uint64_t rays;               /* closest-hit rays traced (path segments) */
+    uint64_t shadow_rays;        /* any-hit shadow rays traced */
+    double seconds;              /* wall time of the call */
+} reina_render_stats;
+
+/* One frame of the wavefront path tracer: push_consts->samplesPerPixel samples per pixel, at most
+ * push_consts->maxBounces segments per sample, samples clamped to [0, directClamp] with NaN samples
+ * dropped, and the frame's mean blended into `accum_rgba32f` (width*height RGBA32F, host memory) as
+ * (prev*sampleBatch + mean)/(sampleBatch + 1) when sampleBatch > 0 (raytrace.rgen.glsl:264-284).
+ * `samples_rgb32f` (optional, width*height*spp*3 floats) receives every sample's clamped colour. */
+int reina_render(reina_ctx* ctx, const reina_scene* scene, const RtPushConsts* push_consts,
+                 const reina_render_options* options, float* accum_rgba32f, float* samples_rgb32f,
+                 reina_render_stats* stats);
+
+/* Same on device buffers, enqueued on `stream` without synchronizing.  d_samples may be NULL. */
+int reina_render_device(reina_ctx* ctx, const reina_scene* scene, const RtPushConsts* push_consts,
+                        const reina_render_options* options, void* d_accum_rgba32f, void* d_samples_rgb32f,
+                        void* stream);
+
+/* ------------------------------------------------------------------------------------------------ */
 /* Camera  (src/graphics/Camera.cpp:10-11)                                                           */
 /* ------------------------------------------------------------------------------------------------ */
 /* inverse(perspective(fovy_radians, aspect, near, far)) and inverse(lookAt(pos, pos + front, up)),

@@ -112,6 +112,126 @@ def raycast_brute(tris9: np.ndarray, rays: np.ndarray, any_hit: bool = False, pr
     return out
 
 
+class OMaterial(C.Structure):
+    """Same field order as the C ABI's reina_material (src/scene/Scene.h:21-46)."""
+    _fields_ = [
+        ("material_idx", C.c_uint32), ("texture_id", C.c_int32), ("normal_map_id", C.c_int32),
+        ("bump_map_id", C.c_int32), ("albedo", C.c_float * 3), ("emission", C.c_float * 3),
+        ("roughness", C.c_float), ("ior", C.c_float), ("interp_normals", C.c_uint32),
+        ("absorption", C.c_float), ("cull_backface", C.c_uint32), ("anisotropic", C.c_float),
+        ("subsurface", C.c_float), ("clearcoat_gloss", C.c_float), ("sheen_tint", C.c_float * 3),
+        ("specular_tint", C.c_float * 3), ("metallic", C.c_float), ("clearcoat", C.c_float),
+        ("specular_transmission", C.c_float), ("sheen", C.c_float),
+    ]
+
+    @classmethod
+    def from_obj(cls, m) -> "OMaterial":
+        o = cls()
+        for name, _ in cls._fields_:
+            v = getattr(m, name)
+            if isinstance(v, (tuple, list, np.ndarray)):
+                arr = getattr(o, name)
+                for i in range(3):
+                    arr[i] = float(v[i])
+            elif isinstance(v, bool):
+                setattr(o, name, int(v))
+            else:
+                setattr(o, name, v)
+        return o
+
+
+class OPush(C.Structure):
+    """polyglot/raytrace.h:43-54."""
+    _fields_ = [("invView", C.c_float * 16), ("invProjection", C.c_float * 16), ("sampleBatch", C.c_uint32),
+                ("totalEmissiveWeight", C.c_float), ("focusDist", C.c_float), ("defocusMultiplier", C.c_float),
+                ("directClamp", C.c_float), ("indirectClamp", C.c_float), ("samplesPerPixel", C.c_uint32),
+                ("maxBounces", C.c_uint32)]
+
+    @classmethod
+    def copy_of(cls, pc) -> "OPush":
+        o = cls()
+        C.memmove(C.byref(o), C.byref(pc), C.sizeof(cls))
+        return o
+
+
+class ORenderOptions(C.Structure):
+    _fields_ = [("mode", C.c_uint32), ("seed", C.c_uint32), ("env_mode", C.c_uint32), ("env_color", C.c_float * 3),
+                ("x0", C.c_uint32), ("y0", C.c_uint32), ("x1", C.c_uint32), ("y1", C.c_uint32)]
+
+
+_SHADING_SIGS.update({
+    "oracle_scene_new": (C.c_void_p, []),
+    "oracle_scene_free": (None, [C.c_void_p]),
+    "oracle_scene_add_object": (C.c_uint32, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint64, C.c_void_p,
+                                             C.c_uint64, C.c_void_p, C.c_uint64]),
+    "oracle_scene_add_instance": (None, [C.c_void_p, C.c_uint32, C.c_void_p, C.POINTER(OMaterial), C.c_uint32,
+                                         C.c_void_p]),
+    "oracle_scene_finalize": (None, [C.c_void_p]),
+    "oracle_scene_emissive_weight": (C.c_float, [C.c_void_p]),
+    "oracle_render": (None, [C.c_void_p, C.POINTER(OPush), C.POINTER(ORenderOptions), C.c_uint32, C.c_uint32, C.c_int,
+                             C.c_int, C.c_void_p, C.c_void_p]),
+    "oracle_seed_hash": (C.c_uint32, [C.c_uint32, C.c_uint32, C.c_uint32]),
+})
+
+
+class Scene:
+    """The oracle's own scene: objects, instances (column-major transforms) and materials."""
+
+    def __init__(self):
+        self._h = lib().oracle_scene_new()
+        self._keep = []
+
+    def __del__(self):
+        try:
+            if self._h:
+                lib().oracle_scene_free(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+    def add_object(self, v4, idx, tbn9=None, tbn_idx=None) -> int:
+        v = np.ascontiguousarray(v4, np.float32).reshape(-1, 4)
+        i = np.ascontiguousarray(idx, np.uint32).reshape(-1)
+        t = None if tbn9 is None else np.ascontiguousarray(tbn9, np.float32).reshape(-1, 9)
+        ti = None if tbn_idx is None else np.ascontiguousarray(tbn_idx, np.uint32).reshape(-1)
+        return int(lib().oracle_scene_add_object(self._h, _p(v), v.shape[0], _p(i), i.size, _p(t),
+                                                 0 if t is None else t.shape[0], _p(ti), 0 if ti is None else ti.size))
+
+    def add_instance(self, obj: int, transform16, materials: list, face_material=None) -> None:
+        T = np.ascontiguousarray(transform16, np.float32).reshape(16)
+        arr = (OMaterial * len(materials))(*[OMaterial.from_obj(m) for m in materials])
+        fm = None if face_material is None else np.ascontiguousarray(face_material, np.uint32)
+        lib().oracle_scene_add_instance(self._h, obj, _p(T), arr, len(materials), _p(fm))
+
+    def finalize(self) -> None:
+        lib().oracle_scene_finalize(self._h)
+
+    @property
+    def emissive_weight(self) -> float:
+        return float(lib().oracle_scene_emissive_weight(self._h))
+
+    def render(self, pc, width: int, height: int, mode: int = 0, seed: int = 1, env_mode: int = 0,
+               env_color=(0.0, 0.0, 0.0), window=None, precision: int = 32, threads: int = 0, accum=None,
+               want_samples: bool = False):
+        o = ORenderOptions(mode, seed, env_mode)
+        for k in range(3):
+            o.env_color[k] = float(env_color[k])
+        x0, y0, x1, y1 = window if window is not None else (0, 0, width, height)
+        o.x0, o.y0, o.x1, o.y1 = x0, y0, x1, y1
+        if accum is None:
+            accum = np.zeros((height, width, 4), np.float32)
+        accum = np.ascontiguousarray(accum, np.float32)
+        samples = np.zeros((width * height, pc.samplesPerPixel, 3), np.float32) if want_samples else None
+        push = OPush.copy_of(pc)
+        lib().oracle_render(self._h, C.byref(push), C.byref(o), width, height, precision, threads, _p(accum),
+                            _p(samples))
+        return accum, samples
+
+
+def seed_hash(pixel: int, sample: int, seed: int) -> int:
+    return int(lib().oracle_seed_hash(pixel, sample, seed))
+
+
 def test_triangle(tri9: np.ndarray, ray) -> tuple[bool, np.ndarray]:
     tri = np.ascontiguousarray(tri9, dtype=np.float32).reshape(9)
     r = np.ascontiguousarray(np.asarray(ray).reshape(1)).view(RAY_DTYPE)

@@ -1,4 +1,5 @@
 // C ABI of the library (include/reina/reina_c.h): handles, status codes and thread-local messages.
+#include <chrono>
 #include <cstring>
 #include <memory>
 #include <new>
@@ -11,6 +12,7 @@
 #include "errors.h"
 #include "generators.h"
 #include "kernels.h"
+#include "render.h"
 #include "scene.h"
 
 using rt::check_cuda;
@@ -23,6 +25,8 @@ struct reina_ctx {
     rt::DeviceBuffer err;        // u32 device error flag, OR-ed by kernels
     rt::DeviceBuffer counters;   // u64 x 2 traversal counters
     rt::DeviceBuffer rays, hits; // staging for host-buffer ray casts
+    rt::RenderWorkspace render;  // wavefront path state and queues
+    rt::DeviceBuffer accum, samples;   // staging for host-buffer renders
 };
 
 struct reina_scene {
@@ -284,6 +288,77 @@ int reina_raycast_counters(reina_ctx* ctx, const reina_scene* scene, const void*
         check_cuda(cudaStreamSynchronize(st), "cudaStreamSynchronize");
         if (out_nodes_visited) *out_nodes_visited = c[0];
         if (out_triangles_tested) *out_triangles_tested = c[1];
+    });
+}
+
+static rt::RenderOpts render_opts(const RtPushConsts* pc, const reina_render_options* o) {
+    need(pc != nullptr && o != nullptr, "NULL push constants or options");
+    need(o->width > 0 && o->height > 0, "image size must be positive");
+    need((uint64_t)o->width * o->height <= (1ull << 28), "image too large (at most 2^28 pixels)");
+    need(o->mode <= REINA_MODE_NEE_MIS, "mode must be REINA_MODE_REINA or REINA_MODE_NEE_MIS");
+    need(o->env_mode <= REINA_ENV_CONSTANT, "env_mode must be REINA_ENV_SKY or REINA_ENV_CONSTANT");
+    need(pc->samplesPerPixel > 0, "samplesPerPixel must be positive");
+    rt::RenderOpts r;
+    r.width = o->width;
+    r.height = o->height;
+    r.mode = o->mode;
+    r.seed = o->seed;
+    r.env_mode = o->env_mode;
+    for (int k = 0; k < 3; ++k) r.env_color[k] = o->env_color[k];
+    return r;
+}
+
+static void check_render_scene(const rt::Scene& s, const RtPushConsts* pc, const reina_render_options* o) {
+    if (o->mode == REINA_MODE_NEE_MIS && s.device_view().emissive_count > 0 && !(pc->totalEmissiveWeight > 0.0f))
+        fail(REINA_ERR_INVALID, "totalEmissiveWeight must be positive for NEE (use reina_scene_emissive_weight)");
+}
+
+int reina_render_device(reina_ctx* ctx, const reina_scene* scene, const RtPushConsts* pc, const reina_render_options* o,
+                        void* d_accum, void* d_samples, void* stream) {
+    return guard([&] {
+        need(ctx != nullptr, "ctx is NULL");
+        const rt::Scene& s = built_scene(scene);
+        const rt::RenderOpts r = render_opts(pc, o);
+        check_render_scene(s, pc, o);
+        need(d_accum != nullptr && ((uintptr_t)d_accum % 16) == 0, "accumulation buffer must be non-NULL and 16-byte aligned");
+        use_device(ctx);
+        rt::render_frame(ctx->render, s.device_view(), *pc, r, static_cast<float*>(d_accum), static_cast<float*>(d_samples),
+                         ctx->sm_count, static_cast<cudaStream_t>(stream), nullptr);
+    });
+}
+
+int reina_render(reina_ctx* ctx, const reina_scene* scene, const RtPushConsts* pc, const reina_render_options* o,
+                 float* accum, float* samples, reina_render_stats* stats) {
+    return guard([&] {
+        need(ctx != nullptr, "ctx is NULL");
+        const rt::Scene& s = built_scene(scene);
+        const rt::RenderOpts r = render_opts(pc, o);
+        check_render_scene(s, pc, o);
+        need(accum != nullptr, "accumulation buffer is NULL");
+        use_device(ctx);
+        auto t0 = std::chrono::steady_clock::now();
+        const size_t P = (size_t)r.width * r.height;
+        cudaStream_t st = ctx->streams[0];
+        ctx->accum.reserve(P * 4 * sizeof(float));
+        check_cuda(cudaMemcpyAsync(ctx->accum.get(), accum, P * 4 * sizeof(float), cudaMemcpyHostToDevice, st), "H2D accum");
+        float* d_samples = nullptr;
+        if (samples) {
+            ctx->samples.reserve(P * pc->samplesPerPixel * 3 * sizeof(float));
+            d_samples = ctx->samples.as<float>();
+        }
+        rt::RenderStats rs;
+        rt::render_frame(ctx->render, s.device_view(), *pc, r, ctx->accum.as<float>(), d_samples, ctx->sm_count, st, &rs);
+        check_cuda(cudaMemcpyAsync(accum, ctx->accum.get(), P * 4 * sizeof(float), cudaMemcpyDeviceToHost, st), "D2H accum");
+        if (samples)
+            check_cuda(cudaMemcpyAsync(samples, d_samples, P * pc->samplesPerPixel * 3 * sizeof(float), cudaMemcpyDeviceToHost, st),
+                       "D2H samples");
+        check_cuda(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+        if (rs.error) fail(REINA_ERR_DEVICE, "render kernel raised error flag " + std::to_string(rs.error));
+        if (stats) {
+            stats->rays = rs.rays;
+            stats->shadow_rays = rs.shadow_rays;
+            stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        }
     });
 }
 

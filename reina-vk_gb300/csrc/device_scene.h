@@ -38,6 +38,8 @@ struct DeviceScene {
     const InstanceGpu* instances = nullptr;
     const uint32_t* prim_instance = nullptr;  // per global triangle
     const uint32_t* prim_props = nullptr;     // per global triangle: InstanceProperties index
+    const uint32_t* props_material = nullptr; // per InstanceProperties: material_idx (the SBT offset)
+    const uint8_t* has_tbn = nullptr;         // per object: 1 if the model supplied TBN data
     uint32_t instance_count = 0;
     uint32_t props_count = 0;
     // emissive sampling data (src/scene/Instances.cpp:129-191, packed as in :197-232)

@@ -112,6 +112,7 @@ void Scene::add_instance(uint32_t object, const float transform[16], const reina
     if (object >= ranges_.size()) fail(REINA_ERR_INVALID, "Index " + std::to_string(object) + " out of range for models");
     check_material(mat);
     props_.push_back(make_props(object, mat));
+    props_material_.push_back(mat.material_idx);
     InstanceRecord inst;
     inst.object = object;
     inst.props_id = (uint32_t)(props_.size() - 1);
@@ -135,6 +136,7 @@ void Scene::add_instance_per_face(uint32_t object, const float transform[16], co
         if (e[0] != 0.0f || e[1] != 0.0f || e[2] != 0.0f)
             fail(REINA_ERR_INVALID, "per-face materials must not be emissive");
         props_.push_back(make_props(object, mats[i]));
+        props_material_.push_back(mats[i].material_idx);
     }
     InstanceRecord inst;
     inst.object = object;
@@ -371,6 +373,10 @@ void Scene::build(bool require_emissive) {
     up(d_emissive_, emissive_data_.data(), emissive_data_.size() * sizeof(EmissiveInstanceData));
     up(d_cdf_tris_, cdf_triangles_.data(), cdf_triangles_.size() * sizeof(float));
     up(d_cdf_inst_, cdf_instances_.data(), cdf_instances_.size() * sizeof(float));
+    up(d_props_material_, props_material_.data(), props_material_.size() * sizeof(uint32_t));
+    std::vector<uint8_t> has_tbn(models_.size());
+    for (size_t o = 0; o < models_.size(); ++o) has_tbn[o] = models_[o].tbn_indices.empty() ? 0 : 1;
+    up(d_has_tbn_, has_tbn.data(), has_tbn.size());
 
     dev_ = DeviceScene{};
     dev_.nodes = d_nodes_.as<Bvh8Node>();
@@ -387,6 +393,8 @@ void Scene::build(bool require_emissive) {
     dev_.instances = d_instances_.as<InstanceGpu>();
     dev_.prim_instance = d_prim_instance_.as<uint32_t>();
     dev_.prim_props = d_prim_props_.as<uint32_t>();
+    dev_.props_material = d_props_material_.as<uint32_t>();
+    dev_.has_tbn = d_has_tbn_.as<uint8_t>();
     dev_.instance_count = (uint32_t)instances_.size();
     dev_.props_count = (uint32_t)props_.size();
     dev_.emissive = d_emissive_.as<EmissiveInstanceData>();
@@ -401,7 +409,7 @@ size_t Scene::device_bytes() const {
     return d_nodes_.bytes() + d_tris_.bytes() + d_vertices_.bytes() + d_indices_.bytes() + d_tbns_.bytes() +
            d_tbn_indices_.bytes() + d_tex_coords_.bytes() + d_tex_indices_.bytes() + d_props_.bytes() +
            d_instances_.bytes() + d_prim_instance_.bytes() + d_prim_props_.bytes() + d_emissive_.bytes() +
-           d_cdf_tris_.bytes() + d_cdf_inst_.bytes();
+           d_cdf_tris_.bytes() + d_cdf_inst_.bytes() + d_props_material_.bytes() + d_has_tbn_.bytes();
 }
 
 void Scene::prim_info(uint32_t prim, uint32_t* inst, uint32_t* local) const {

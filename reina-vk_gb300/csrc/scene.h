@@ -88,6 +88,7 @@ private:
     std::vector<uint32_t> all_indices_offset_, all_tex_indices_offset_, all_tbns_indices_offset_, all_indices_non_offset_;
     // Instances
     std::vector<InstanceProperties> props_;
+    std::vector<uint32_t> props_material_;
     std::vector<InstanceRecord> instances_;
     // Emissive packing (src/scene/Instances.cpp)
     std::vector<EmissiveInstanceData> emissive_data_;
@@ -101,7 +102,7 @@ private:
     // Device buffers
     DeviceBuffer d_nodes_, d_tris_, d_vertices_, d_indices_, d_tbns_, d_tbn_indices_, d_tex_coords_,
         d_tex_indices_, d_props_, d_instances_, d_prim_instance_, d_prim_props_, d_emissive_, d_cdf_tris_,
-        d_cdf_inst_;
+        d_cdf_inst_, d_props_material_, d_has_tbn_;
     DeviceScene dev_;
 };
 

@@ -81,6 +81,53 @@ class _CtxOptions(C.Structure):
     _fields_ = [("device", C.c_int32), ("flags", C.c_uint32)]
 
 
+class RtPushConsts(C.Structure):
+    """polyglot/raytrace.h:43-54 (160 bytes; matrices column-major)."""
+    _fields_ = [("invView", C.c_float * 16), ("invProjection", C.c_float * 16), ("sampleBatch", C.c_uint32),
+                ("totalEmissiveWeight", C.c_float), ("focusDist", C.c_float), ("defocusMultiplier", C.c_float),
+                ("directClamp", C.c_float), ("indirectClamp", C.c_float), ("samplesPerPixel", C.c_uint32),
+                ("maxBounces", C.c_uint32)]
+
+
+class RenderOptions(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("mode", C.c_uint32), ("seed", C.c_uint32),
+                ("env_mode", C.c_uint32), ("env_color", C.c_float * 3)]
+
+
+class _RenderStats(C.Structure):
+    _fields_ = [("rays", C.c_uint64), ("shadow_rays", C.c_uint64), ("seconds", C.c_double)]
+
+
+MODE_REINA = 0
+MODE_NEE_MIS = 1
+ENV_SKY = 0
+ENV_CONSTANT = 1
+
+
+def push_consts(inv_view, inv_proj, sample_batch=0, total_emissive_weight=0.0, focus_dist=1.0, defocus=0.0,
+                direct_clamp=100.0, indirect_clamp=10.0, spp=1, max_bounces=8) -> RtPushConsts:
+    pc = RtPushConsts()
+    for k in range(16):
+        pc.invView[k] = float(inv_view[k])
+        pc.invProjection[k] = float(inv_proj[k])
+    pc.sampleBatch = sample_batch
+    pc.totalEmissiveWeight = total_emissive_weight
+    pc.focusDist = focus_dist
+    pc.defocusMultiplier = defocus
+    pc.directClamp = direct_clamp
+    pc.indirectClamp = indirect_clamp
+    pc.samplesPerPixel = spp
+    pc.maxBounces = max_bounces
+    return pc
+
+
+def render_options(width, height, mode=MODE_REINA, seed=1, env_mode=ENV_SKY, env_color=(0.0, 0.0, 0.0)) -> RenderOptions:
+    o = RenderOptions(width, height, mode, seed, env_mode)
+    for k in range(3):
+        o.env_color[k] = float(env_color[k])
+    return o
+
+
 @dataclass
 class Material:
     """reina::scene::Material (src/scene/Scene.h:21-46); material_idx 0 Lambertian, 1 metal,
@@ -158,6 +205,8 @@ def load_library() -> C.CDLL:
         "reina_raycast": (I32, [P, P, P, U64, P, U32]),
         "reina_raycast_device": (I32, [P, P, P, U64, P, U32, P]),
         "reina_raycast_counters": (I32, [P, P, P, U64, U32, C.POINTER(U64), C.POINTER(U64), P]),
+        "reina_render": (I32, [P, P, C.POINTER(RtPushConsts), C.POINTER(RenderOptions), P, P, C.POINTER(_RenderStats)]),
+        "reina_render_device": (I32, [P, P, C.POINTER(RtPushConsts), C.POINTER(RenderOptions), P, P, P]),
         "reina_camera_matrices": (I32, [P, P, P, F, F, F, F, P, P]),
         "reina_icosphere_counts": (I32, [U32, C.POINTER(U64), C.POINTER(U64)]),
         "reina_gen_icosphere": (I32, [U32, F, U64, P, P, P]),
@@ -351,6 +400,27 @@ def raycast_counters(ctx: Context, scene: Scene, d_rays: int, count: int, flags:
     _check(_lib.reina_raycast_counters(ctx.handle, scene.handle, C.c_void_p(d_rays), count, flags, C.byref(a),
                                        C.byref(b), C.c_void_p(stream)))
     return int(a.value), int(b.value)
+
+
+def render(ctx: Context, scene: Scene, pc: RtPushConsts, opts: RenderOptions, accum: np.ndarray | None = None,
+           want_samples: bool = False):
+    """One frame (Reina::traceRays): returns (accum (H, W, 4) float32, samples (H*W, spp, 3) or None, stats)."""
+    n = opts.width * opts.height
+    if accum is None:
+        accum = np.zeros((opts.height, opts.width, 4), np.float32)
+    accum = np.ascontiguousarray(accum, dtype=np.float32)
+    assert accum.size == 4 * n
+    samples = np.zeros((n, pc.samplesPerPixel, 3), np.float32) if want_samples else None
+    st = _RenderStats()
+    _check(_lib.reina_render(ctx.handle, scene.handle, C.byref(pc), C.byref(opts), _ptr(accum), _ptr(samples),
+                             C.byref(st)))
+    return accum, samples, {"rays": st.rays, "shadow_rays": st.shadow_rays, "seconds": st.seconds}
+
+
+def render_device(ctx: Context, scene: Scene, pc: RtPushConsts, opts: RenderOptions, d_accum: int, d_samples: int = 0,
+                  stream: int = 0) -> None:
+    _check(_lib.reina_render_device(ctx.handle, scene.handle, C.byref(pc), C.byref(opts), C.c_void_p(d_accum),
+                                    C.c_void_p(d_samples or None), C.c_void_p(stream)))
 
 
 def camera_matrices(pos, front, up=(0.0, 1.0, 0.0), fovy_radians=np.radians(45.0), aspect=1.0, z_near=0.1,

@@ -105,3 +105,156 @@ def large_scene(R, ctx, level: int = 8, seed: int = 1, light_emission=(17.0, 12.
     scene.build(require_emissive=True)
     tris = np.concatenate([world_triangles(a, b) for a, b in geo])
     return scene, tris, geo
+
+
+# ---------------------------------------------------------------------------------------------------
+# Scene descriptions built identically through the library's scene API and through the oracle.
+
+def translate(x, y, z):
+    m = np.eye(4, dtype=np.float32)
+    m[:3, 3] = (x, y, z)
+    return m
+
+
+def rotate_y(deg):
+    a = np.radians(deg)
+    c, s = np.cos(a), np.sin(a)
+    m = np.eye(4, dtype=np.float32)
+    m[0, 0], m[0, 2], m[2, 0], m[2, 2] = c, s, -s, c
+    return m
+
+
+def scale(x, y, z):
+    return np.diag([x, y, z, 1.0]).astype(np.float32)
+
+
+def col_major(m) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(m, np.float32).T.reshape(16))
+
+
+class SceneDesc:
+    def __init__(self):
+        self.objects = []     # (v4, idx, tbn9, tbn_idx)
+        self.instances = []   # (obj, 4x4 math transform, [materials], face_material or None)
+
+    def add_object(self, v4, idx, tbn9=None, tbn_idx=None) -> int:
+        v4 = np.asarray(v4, np.float32)
+        if v4.shape[1] == 3:
+            v4 = np.concatenate([v4, np.ones((v4.shape[0], 1), np.float32)], 1)
+        self.objects.append((v4, np.asarray(idx, np.uint32).reshape(-1), tbn9, tbn_idx))
+        return len(self.objects) - 1
+
+    def add_instance(self, obj, transform=None, material=None, materials=None, face_material=None):
+        T = np.eye(4, dtype=np.float32) if transform is None else np.asarray(transform, np.float32)
+        self.instances.append((obj, T, materials if materials is not None else [material], face_material))
+
+    def to_product(self, R, ctx, require_emissive=False):
+        s = R.Scene(ctx)
+        for v4, idx, t9, ti in self.objects:
+            s.define_object(v4, idx, tbns=t9, tbn_indices=ti)
+        for obj, T, mats, fm in self.instances:
+            if fm is None:
+                s.add_instance(obj, T, mats[0])
+            else:
+                s.add_instance_per_face(obj, T, mats, fm)
+        s.build(require_emissive=require_emissive)
+        return s
+
+    def to_oracle(self, O):
+        s = O.Scene()
+        for v4, idx, t9, ti in self.objects:
+            s.add_object(v4, idx, t9, ti)
+        for obj, T, mats, fm in self.instances:
+            s.add_instance(obj, col_major(T), mats, fm)
+        s.finalize()
+        return s
+
+
+def quad(corner, e1, e2):
+    """Quad corner, corner+e1, corner+e1+e2, corner+e2 with normal along e1 x e2."""
+    c, a, b = (np.asarray(x, np.float32) for x in (corner, e1, e2))
+    v = np.stack([c, c + a, c + a + b, c + b])
+    return v, np.array([0, 1, 2, 0, 2, 3], np.uint32)
+
+
+def unit_cube():
+    v = np.array([[-.5, -.5, -.5], [.5, -.5, -.5], [.5, .5, -.5], [-.5, .5, -.5],
+                  [-.5, -.5, .5], [.5, -.5, .5], [.5, .5, .5], [-.5, .5, .5]], np.float32)
+    i = np.array([0, 2, 1, 0, 3, 2, 4, 5, 6, 4, 6, 7, 0, 4, 7, 0, 7, 3, 1, 2, 6, 1, 6, 5, 0, 1, 5, 0, 5, 4,
+                  3, 7, 6, 3, 6, 2], np.uint32)
+    return v, i
+
+
+GREY = (0.73, 0.73, 0.73)
+RED = (0.65, 0.05, 0.05)
+GREEN = (0.12, 0.45, 0.15)
+CORNELL_LIGHT = (17.0, 12.0, 4.0)
+
+
+def cornell(R, seed: int = 1) -> SceneDesc:
+    """The procedural Cornell-style room: 5 walls (10 tris), 2 boxes rotated about y by seeded angles
+    (24 tris, one cube object instanced twice), an emissive back-face-culled ceiling quad (2 tris)."""
+    u = uniform(2, seed)
+    d = SceneDesc()
+    lam = lambda c: R.Material(material_idx=0, albedo=c)
+    walls = [
+        (quad((-1, -1, 1), (2, 0, 0), (0, 0, -2)), GREY),    # floor, normal +y
+        (quad((-1, 1, -1), (2, 0, 0), (0, 0, 2)), GREY),     # ceiling, normal -y
+        (quad((-1, -1, -1), (2, 0, 0), (0, 2, 0)), GREY),    # back, normal +z
+        (quad((-1, -1, 1), (0, 0, -2), (0, 2, 0)), RED),     # left, normal +x
+        (quad((1, -1, -1), (0, 0, 2), (0, 2, 0)), GREEN),    # right, normal -x
+    ]
+    for (v, i), col in walls:
+        d.add_instance(d.add_object(v, i), None, lam(col))
+    cube = d.add_object(*unit_cube())
+    t1 = 15.0 + 5.0 * u[0]
+    t2 = 15.0 + 5.0 * u[1]
+    d.add_instance(cube, translate(-0.35, -0.4, -0.3) @ rotate_y(t1) @ scale(0.6, 1.2, 0.6), lam(GREY))
+    d.add_instance(cube, translate(0.35, -0.7, 0.35) @ rotate_y(-t2) @ scale(0.6, 0.6, 0.6), lam(GREY))
+    lv, li = quad((-0.25, 0.999, -0.2), (0.5, 0, 0), (0, 0, 0.4))   # normal -y
+    d.add_instance(d.add_object(lv, li), None,
+                   R.Material(material_idx=0, albedo=(0.78, 0.78, 0.78), emission=CORNELL_LIGHT, cull_backface=True))
+    return d
+
+
+def cornell_camera(R, width: int, height: int):
+    iv, ip = R.camera_matrices((0.0, 0.0, 3.4), (0.0, 0.0, -1.0), (0.0, 1.0, 0.0), np.radians(40.0), width / height)
+    return iv, ip
+
+
+def sphere_tbn(level: int, amplitude: float, seed: int, R):
+    """Icosphere with per-vertex TBNs (N = undisplaced radial direction, T = normalize(up x N))."""
+    v, i, n = R.icosphere(level, amplitude, seed)
+    up = np.where(np.abs(n[:, 1:2]) > 0.99, np.array([[1.0, 0, 0]]), np.array([[0, 1.0, 0]]))
+    t = np.cross(up, n)
+    t /= np.linalg.norm(t, axis=1, keepdims=True)
+    b = np.cross(n, t)
+    tbn = np.concatenate([t, b, n], axis=1).astype(np.float32)   # columns T, B, N
+    return v, i, tbn, i.copy()
+
+
+def material_zoo(R, seed: int = 3) -> SceneDesc:
+    """Cornell room plus spheres of every material: metal (fuzzy), dielectric with Beer absorption, and
+    Disney variants (diffuse+sheen+subsurface, metallic, clearcoat, transmissive glass lobe), one of them
+    back-face culled and one scaled/rotated by its instance transform."""
+    d = cornell(R, seed)
+    v, i, tbn, ti = sphere_tbn(3, 0.05, seed, R)
+    sph = d.add_object(v, i, tbn, ti)
+    mats = [
+        R.Material(material_idx=1, albedo=(0.9, 0.8, 0.6), roughness=0.2),
+        R.Material(material_idx=2, albedo=(0.8, 0.9, 0.95), ior=1.5, absorption=1.5, roughness=0.05, interp_normals=True),
+        R.Material(material_idx=3, albedo=(0.7, 0.3, 0.2), roughness=0.6, subsurface=0.4, sheen=0.8,
+                   sheen_tint=(0.5, 0.5, 0.5), specular_tint=(1, 1, 1), interp_normals=True),
+        R.Material(material_idx=3, albedo=(0.95, 0.75, 0.3), metallic=0.9, roughness=0.3, anisotropic=0.5,
+                   specular_tint=(1, 1, 1), sheen_tint=(1, 1, 1)),
+        R.Material(material_idx=3, albedo=(0.2, 0.4, 0.8), clearcoat=1.0, clearcoat_gloss=0.7, roughness=0.4,
+                   specular_tint=(1, 1, 1), sheen_tint=(1, 1, 1), cull_backface=True),
+        R.Material(material_idx=3, albedo=(0.9, 0.95, 0.9), specular_transmission=0.8, ior=1.45, roughness=0.15,
+                   specular_tint=(1, 1, 1), sheen_tint=(1, 1, 1)),
+    ]
+    pos = [(-0.6, -0.75, 0.5), (0.0, -0.75, 0.6), (0.6, -0.75, 0.5), (-0.55, 0.3, 0.2), (0.55, 0.2, 0.1),
+           (0.0, 0.35, 0.4)]
+    for k, (m, p) in enumerate(zip(mats, pos)):
+        T = translate(*p) @ rotate_y(20.0 * k) @ scale(0.22, 0.22 if k != 3 else 0.3, 0.22)
+        d.add_instance(sph, T, m)
+    return d
