@@ -270,8 +270,58 @@ def run_ours(args) -> dict | None:
         "clocks": clk,
         "wall_timed_s": wall,
     }
+    if not args.no_render:
+        out["render"] = render_metrics(R, ctx, torch, args.render_frames, scene)
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(tris, rays, args.cpu_sample)
+    return out
+
+
+def _timed_frames(torch, fn, frames: int) -> float:
+    """Mean device time (s) of `frames` calls of fn() on the current stream, after one warm-up call."""
+    stream = torch.cuda.current_stream()
+    fn()
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record(stream)
+    for _ in range(frames):
+        fn()
+    e.record(stream)
+    torch.cuda.synchronize()
+    return s.elapsed_time(e) * 1e-3 / frames
+
+
+def render_metrics(R, ctx, torch, frames: int, scene_large) -> dict:
+    """The large scene (1920x1080, 64 spp, 12 bounces, NEE+MIS, light + constant environment) rendered by
+    the wavefront integrator and by the plain megakernel; and the Cornell room (256x256, 16 spp, 8)."""
+    import scenes
+
+    out = {}
+    sptr = torch.cuda.current_stream().cuda_stream
+    W, H = 1920, 1080
+    iv, ip = R.camera_matrices((0.0, 0.4, 3.6), (0.0, -0.12, -1.0), (0.0, 1.0, 0.0), np.radians(40.0), W / H)
+    pc = R.push_consts(iv, ip, total_emissive_weight=scene_large.emissive_weight, spp=64, max_bounces=12,
+                       focus_dist=3.6)
+    acc = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
+    for name, mega in (("wavefront", False), ("megakernel", True)):
+        opts = R.render_options(W, H, R.MODE_NEE_MIS, 1, R.ENV_CONSTANT, (0.3, 0.3, 0.35), megakernel=mega)
+        _, _, st = R.render(ctx, scene_large, pc, opts)   # ray counts of one frame
+        dt = _timed_frames(torch, lambda: R.render_device(ctx, scene_large, pc, opts, acc.data_ptr(), 0, sptr), frames)
+        out[f"large_{name}"] = {"s_per_frame": dt, "segments_per_s": st["rays"] / dt,
+                                "rays_per_s": (st["rays"] + st["shadow_rays"]) / dt,
+                                "segments_per_frame": st["rays"], "shadow_rays_per_frame": st["shadow_rays"]}
+    d = scenes.cornell(R)
+    sc = d.to_product(R, ctx)
+    iv, ip = scenes.cornell_camera(R, 256, 256)
+    pc = R.push_consts(iv, ip, total_emissive_weight=sc.emissive_weight, spp=16, max_bounces=8)
+    acc = torch.zeros((256, 256, 4), dtype=torch.float32, device="cuda")
+    for name, mega in (("wavefront", False), ("megakernel", True)):
+        opts = R.render_options(256, 256, R.MODE_NEE_MIS, 1, megakernel=mega)
+        _, _, st = R.render(ctx, sc, pc, opts)
+        dt = _timed_frames(torch, lambda: R.render_device(ctx, sc, pc, opts, acc.data_ptr(), 0, sptr), frames)
+        out[f"cornell_{name}"] = {"s_per_frame": dt, "paths_per_s": 256 * 256 * 16 / dt,
+                                  "segments_per_s": st["rays"] / dt,
+                                  "rays_per_s": (st["rays"] + st["shadow_rays"]) / dt}
     return out
 
 
@@ -347,6 +397,8 @@ def main() -> int:
     ap.add_argument("--cpu-sample", type=int, default=1 << 21)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile", action="store_true", help="launch the kernels a few times for ncu and exit")
+    ap.add_argument("--no-render", action="store_true", help="skip the render metrics")
+    ap.add_argument("--render-frames", type=int, default=2)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     out = run_reference(args) if args.impl == "reference" else run_ours(args)

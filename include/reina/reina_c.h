@@ -222,7 +222,14 @@ typedef struct reina_render_options {
     uint32_t seed;               /* key of the per-path seeds in REINA_MODE_NEE_MIS */
     uint32_t env_mode;           /* REINA_ENV_* */
     float env_color[3];
+    uint32_t flags;              /* REINA_RENDER_* */
 } reina_render_options;
+
+enum {
+    REINA_RENDER_MEGAKERNEL = 1  /* plain form: one kernel with one thread per pixel running all of its
+                                  * samples and segments (the reference's raygen structure), instead of
+                                  * the wavefront of queue-driven kernels */
+};
 
 typedef struct reina_render_stats {
     uint64_t rays;               /* closest-hit rays traced (path segments) */
@@ -243,6 +250,22 @@ int reina_render(reina_ctx* ctx, const reina_scene* scene, const RtPushConsts* p
 int reina_render_device(reina_ctx* ctx, const reina_scene* scene, const RtPushConsts* push_consts,
                         const reina_render_options* options, void* d_accum_rgba32f, void* d_samples_rgb32f,
                         void* stream);
+
+/* ------------------------------------------------------------------------------------------------ */
+/* Post-process — replaces Reina::applyBloom + Reina::applyTonemapping (src/Reina.cpp:472-577):        */
+/* blurX (threshold) -> blurY -> combine (shaders/postprocessing/bloom), then exposure and the          */
+/* ACES fitted curve to RGBA8 UNORM (shaders/postprocessing/tonemap/tonemapping.comp.glsl:66-84).      */
+/* ------------------------------------------------------------------------------------------------ */
+/* Host buffers: accum width*height RGBA32F in, rgba8 width*height*4 bytes out; combined_rgba32f
+ * (optional) receives the bloomed HDR image before tone mapping. */
+int reina_postprocess(reina_ctx* ctx, const float* accum_rgba32f, uint32_t width, uint32_t height,
+                      const BloomPushConsts* bloom, const TonemappingPushConsts* tonemap, uint8_t* rgba8,
+                      float* combined_rgba32f);
+
+/* Device buffers, enqueued on `stream`. */
+int reina_postprocess_device(reina_ctx* ctx, const void* d_accum_rgba32f, uint32_t width, uint32_t height,
+                             const BloomPushConsts* bloom, const TonemappingPushConsts* tonemap, void* d_rgba8,
+                             void* d_combined_rgba32f, void* stream);
 
 /* ------------------------------------------------------------------------------------------------ */
 /* Camera  (src/graphics/Camera.cpp:10-11)                                                           */

@@ -228,6 +228,20 @@ class Scene:
         return accum, samples
 
 
+_SHADING_SIGS["oracle_postprocess"] = (None, [C.c_void_p, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float,
+                                              C.c_float, C.c_int, C.c_void_p, C.c_void_p])
+
+
+def postprocess(accum: np.ndarray, radius=5.0, threshold=1.0, intensity=0.05, exposure=1.0, precision=32):
+    """Bloom + ACES tone map of accum (H, W, 4) -> (rgba8 (H, W, 4), combined HDR (H, W, 4))."""
+    accum = np.ascontiguousarray(accum, np.float32)
+    H, W = accum.shape[:2]
+    out = np.zeros((H, W, 4), np.uint8)
+    comb = np.zeros((H, W, 4), np.float32)
+    lib().oracle_postprocess(_p(accum), W, H, radius, threshold, intensity, exposure, precision, _p(out), _p(comb))
+    return out, comb
+
+
 def seed_hash(pixel: int, sample: int, seed: int) -> int:
     return int(lib().oracle_seed_hash(pixel, sample, seed))
 

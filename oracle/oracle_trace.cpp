@@ -90,28 +90,64 @@ bool watertight(const PreRay<T>& r, const float* tri, T tmax_now, T& t_out, T& u
 // The reported t, u, v of a float-mode hit: the same watertight expressions evaluated in double for the
 // selected triangle (no range or sign checks) and rounded to float.  Ray-cast APIs report these values;
 // the float test above only decides which triangle is hit.
-// Barycentric weights from exact double-precision signed volumes d . (C x B), d . (A x C), d . (B x A);
-// t = (U A_kz + V B_kz + W C_kz) / (det d_kz); the ratios are taken in float.
+// Re-evaluation of the selected triangle from an origin moved along the ray onto the hit point.  The
+// moved origin o + t0 d (t0 from the watertight test) is formed exactly as hi + lo with FMA-based
+// TwoProduct and TwoSum (error-free transforms, Ogita/Rump/Oishi 2005), so the vertex offsets
+// s = o' - v0 are small and accurate; a Möller–Trumbore evaluation there gives barycentrics without the
+// cancellation that a far origin causes, and t = t0 + t'.  Every step is one IEEE binary32 operation
+// (std::fma is correctly rounded), so the GPU's evaluation of the same sequence gives the same bits.
+inline void two_sum(float a, float b, float& s, float& e) {
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+inline void two_prod(float a, float b, float& p, float& e) {
+    p = a * b;
+    e = std::fma(a, b, -p);
+}
+
+// a*b - c*d with one rounding error (Kahan's FMA algorithm).
+inline float diff_prod(float a, float b, float c, float d) {
+    const float w = c * d;
+    const float e = std::fma(-c, d, w);
+    const float f = std::fma(a, b, -w);
+    return f + e;
+}
+// Compensated dot product Dot2 (Ogita, Rump, Oishi): as if computed in twice the working precision.
+inline float dot2(const float x[3], const float y[3]) {
+    float p, s;
+    two_prod(x[0], y[0], p, s);
+    for (int i = 1; i < 3; ++i) {
+        float h, r, q;
+        two_prod(x[i], y[i], h, r);
+        two_sum(p, h, p, q);
+        s = s + (q + r);
+    }
+    return p + s;
+}
+
 inline void refine64(const RayRec& ray, const float* tri, float& t, float& u, float& v) {
-    const PreRay<double> r = precompute<double>(ray);
-    const Vec3<double> A = Vec3<double>(tri[0], tri[1], tri[2]) - r.o;
-    const Vec3<double> B = Vec3<double>(tri[3], tri[4], tri[5]) - r.o;
-    const Vec3<double> C = Vec3<double>(tri[6], tri[7], tri[8]) - r.o;
-    auto trip = [&](const Vec3<double>& p, const Vec3<double>& q) {
-        const double cx = p.y * q.z - p.z * q.y;
-        const double cy = p.z * q.x - p.x * q.z;
-        const double cz = p.x * q.y - p.y * q.x;
-        return (r.d.x * cx + r.d.y * cy) + r.d.z * cz;
-    };
-    const double U = trip(C, B), V = trip(A, C), W = trip(B, A);
-    const double det = (U + V) + W;
-    if (det == 0.0) return;
-    const double Tn = (U * A[r.kz] + V * B[r.kz]) + W * C[r.kz];
-    const double den = det * r.d[r.kz];
-    const float fdet = (float)det;
-    t = (float)Tn / (float)den;
-    u = (float)V / fdet;
-    v = (float)W / fdet;
+    const float o[3] = {ray.ox, ray.oy, ray.oz}, d[3] = {ray.dx, ray.dy, ray.dz};
+    const float t0 = t;
+    float s[3], e1[3], e2[3];
+    for (int k = 0; k < 3; ++k) {
+        float ph, pl, sh, sl;
+        two_prod(t0, d[k], ph, pl);
+        two_sum(o[k], ph, sh, sl);
+        const float lo = sl + pl;
+        s[k] = (sh - tri[k]) + lo;          // o' - v0
+        e1[k] = tri[3 + k] - tri[k];
+        e2[k] = tri[6 + k] - tri[k];
+    }
+    const float p[3] = {diff_prod(d[1], e2[2], d[2], e2[1]), diff_prod(d[2], e2[0], d[0], e2[2]),
+                        diff_prod(d[0], e2[1], d[1], e2[0])};
+    const float det = dot2(e1, p);
+    if (det == 0.0f) return;
+    const float q[3] = {diff_prod(s[1], e1[2], s[2], e1[1]), diff_prod(s[2], e1[0], s[0], e1[2]),
+                        diff_prod(s[0], e1[1], s[1], e1[0])};
+    u = dot2(s, p) / det;
+    v = dot2(d, q) / det;
+    t = t0 + dot2(e2, q) / det;
 }
 
 template <class T>

@@ -12,6 +12,7 @@
 #include "errors.h"
 #include "generators.h"
 #include "kernels.h"
+#include "post.h"
 #include "render.h"
 #include "scene.h"
 
@@ -27,6 +28,8 @@ struct reina_ctx {
     rt::DeviceBuffer rays, hits; // staging for host-buffer ray casts
     rt::RenderWorkspace render;  // wavefront path state and queues
     rt::DeviceBuffer accum, samples;   // staging for host-buffer renders
+    rt::PostWorkspace post;      // bloom intermediate images
+    rt::DeviceBuffer rgba8, combined;  // staging for host-buffer post-processing
 };
 
 struct reina_scene {
@@ -305,6 +308,8 @@ static rt::RenderOpts render_opts(const RtPushConsts* pc, const reina_render_opt
     r.seed = o->seed;
     r.env_mode = o->env_mode;
     for (int k = 0; k < 3; ++k) r.env_color[k] = o->env_color[k];
+    need((o->flags & ~(uint32_t)REINA_RENDER_MEGAKERNEL) == 0, "unknown render flags");
+    r.megakernel = (o->flags & REINA_RENDER_MEGAKERNEL) != 0;
     return r;
 }
 
@@ -359,6 +364,44 @@ int reina_render(reina_ctx* ctx, const reina_scene* scene, const RtPushConsts* p
             stats->shadow_rays = rs.shadow_rays;
             stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         }
+    });
+}
+
+int reina_postprocess_device(reina_ctx* ctx, const void* d_accum, uint32_t width, uint32_t height,
+                             const BloomPushConsts* bloom, const TonemappingPushConsts* tm, void* d_rgba8, void* d_combined,
+                             void* stream) {
+    return guard([&] {
+        need(ctx && bloom && tm, "NULL argument");
+        need(d_accum && d_rgba8, "NULL image buffer");
+        need(((uintptr_t)d_accum % 16) == 0 && ((uintptr_t)d_rgba8 % 4) == 0 && ((uintptr_t)d_combined % 16) == 0,
+             "misaligned image buffer");
+        need((uint64_t)width * height <= (1ull << 28), "image too large");
+        use_device(ctx);
+        rt::postprocess(ctx->post, static_cast<const float*>(d_accum), (int)width, (int)height, *bloom, *tm,
+                        static_cast<uint8_t*>(d_rgba8), static_cast<float*>(d_combined), ctx->sm_count,
+                        static_cast<cudaStream_t>(stream));
+    });
+}
+
+int reina_postprocess(reina_ctx* ctx, const float* accum, uint32_t width, uint32_t height, const BloomPushConsts* bloom,
+                      const TonemappingPushConsts* tm, uint8_t* rgba8, float* combined) {
+    return guard([&] {
+        need(ctx && bloom && tm && accum && rgba8, "NULL argument");
+        need((uint64_t)width * height <= (1ull << 28), "image too large");
+        use_device(ctx);
+        const size_t n = (size_t)width * height;
+        if (n == 0) return;
+        cudaStream_t st = ctx->streams[0];
+        ctx->accum.reserve(n * 4 * sizeof(float));
+        ctx->rgba8.reserve(n * 4);
+        if (combined) ctx->combined.reserve(n * 4 * sizeof(float));
+        check_cuda(cudaMemcpyAsync(ctx->accum.get(), accum, n * 4 * sizeof(float), cudaMemcpyHostToDevice, st), "H2D");
+        rt::postprocess(ctx->post, ctx->accum.as<float>(), (int)width, (int)height, *bloom, *tm, ctx->rgba8.as<uint8_t>(),
+                        combined ? ctx->combined.as<float>() : nullptr, ctx->sm_count, st);
+        check_cuda(cudaMemcpyAsync(rgba8, ctx->rgba8.get(), n * 4, cudaMemcpyDeviceToHost, st), "D2H");
+        if (combined)
+            check_cuda(cudaMemcpyAsync(combined, ctx->combined.get(), n * 4 * sizeof(float), cudaMemcpyDeviceToHost, st), "D2H");
+        check_cuda(cudaStreamSynchronize(st), "cudaStreamSynchronize");
     });
 }
 

@@ -543,6 +543,156 @@ __global__ void __launch_bounds__(kBlock) k_resolve(RenderLaunch L) {
 }
 
 // ------------------------------------------------------------------------------------------------
+// Plain form: the reference's megakernel structure (raytrace.rgen.glsl:250-285) — one thread per pixel
+// runs every sample and segment, with the closest-hit shading and NEE shadow rays inline.  Same device
+// functions as the wavefront kernels; used as the single-kernel baseline the wavefront is compared with.
+__global__ void __launch_bounds__(kBlock) k_megakernel(RenderLaunch L) {
+    __shared__ uint2 stack[kSmemStack * kBlock];
+    const PathState& ps = L.ps;
+    const uint32_t spp = L.pc.samplesPerPixel;
+    const bool nee = L.mode == kModeNeeMis;
+    unsigned long long n_rays = 0, n_shadow = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < L.P; i += gridDim.x * blockDim.x) {
+        const uint32_t x = i % L.W, y = i / L.W;
+        uint32_t rng = (L.pc.sampleBatch * L.H + y) * L.W + x;
+        float acc = 0.0f;
+        V3 sum{0.0f, 0.0f, 0.0f};
+        uint32_t kept = 0;
+        for (uint32_t smp = 0; smp < spp; ++smp) {
+            if (nee) {
+                rng = path_seed(i, L.pc.sampleBatch * spp + smp, L.seed);
+                acc = 0.0f;
+            }
+            // getStartingRay
+            const float u1 = fmaxf(1e-5f, rng_next(rng));
+            const float u2 = rng_next(rng);
+            const float rr = sqrtf(-2.0f * logf(u1));
+            float st, ct;
+            sincosf(2.0f * kPi * u2, &st, &ct);
+            const float cx = (float)x + 0.5f + 0.375f * (rr * ct);
+            const float cy = (float)y + 0.5f + 0.375f * (rr * st);
+            const float ndcx = (cx / (float)L.W) * 2.0f - 1.0f;
+            const float ndcy = -((cy / (float)L.H) * 2.0f - 1.0f);
+            const float* P = L.pc.invProjection;
+            float vp[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) vp[k] = P[0 * 4 + k] * ndcx + P[1 * 4 + k] * ndcy + P[2 * 4 + k] * -1.0f + P[3 * 4 + k] * 1.0f;
+            const V3 viewDir = norm3(V3{vp[0] / vp[3], vp[1] / vp[3], vp[2] / vp[3]});
+            const float* V = L.pc.invView;
+            const V3 rd0 = norm3(V3{V[0] * viewDir.x + V[4] * viewDir.y + V[8] * viewDir.z,
+                                    V[1] * viewDir.x + V[5] * viewDir.y + V[9] * viewDir.z,
+                                    V[2] * viewDir.x + V[6] * viewDir.y + V[10] * viewDir.z});
+            const V3 origin{V[12], V[13], V[14]};
+            const V3 focal = origin + rd0 * L.pc.focusDist;
+            uint32_t hs = rng;
+            const float sqrt3 = 1.73205080757f;
+            float hx = 0.0f, hy = 0.0f;
+            for (int it = 0; it < 1 << 16; ++it) {
+                hx = 2.0f * rng_next(hs) - 1.0f;
+                hy = (rng_next(hs) - 0.5f) * sqrt3;
+                if (!(fabsf(hy) > sqrt3 * 0.5f || (sqrt3 * fabsf(hx) + fabsf(hy)) > sqrt3)) break;
+            }
+            V3 ro = origin + norm3(V3{V[0], V[1], V[2]}) * (hx * L.pc.defocusMultiplier) +
+                    norm3(V3{V[4], V[5], V[6]}) * (hy * L.pc.defocusMultiplier);
+            V3 rd = norm3(focal - ro);
+            // traceSegments
+            V3 thr{1.0f, 1.0f, 1.0f}, rad{0.0f, 0.0f, 0.0f};
+            bool inside = false, prev_nee = false;
+            float ppdf = 0.0f;
+            for (uint32_t seg = 0; seg < L.pc.maxBounces; ++seg) {
+                const TraceRay r = make_trace_ray(ro.x, ro.y, ro.z, rd.x, rd.y, rd.z, 0.0f, 10000.0f);
+                Hit h;
+                TraceCounters c{0u, 0u};
+                uint32_t e = 0;
+                if (L.s.node_count) e = traverse<false, false, true>(L.s.nodes, L.s.tris, r, stack + threadIdx.x, kBlock, h, c);
+                else h.prim = kMiss;
+                if (e) atomicOr(ps.counters + kCntError, e);
+                ++n_rays;
+                if (h.prim == kMiss) {
+                    V3 sky;
+                    if (L.env_mode == 1) {
+                        sky = V3{L.env[0], L.env[1], L.env[2]};
+                    } else {
+                        const float t = 0.5f * (norm3(rd).y + 1.0f);
+                        sky = mix3(V3{0.1f, 0.1f, 0.1f}, V3{0.4f, 1.7f, 2.0f}, t) * 0.07f;
+                    }
+                    rad = rad + sky * thr;
+                    break;
+                }
+                const HitInfo hi = hit_info(L.s, h.prim, h.u, h.v, rd);
+                const InstanceProperties& pr = L.s.props[hi.props];
+                const uint32_t mat = L.s.props_material[hi.props];
+                Vertex vx;
+                if (mat == 0) vx = shade_lambert(hi, pr, rd, rng, inside, acc);
+                else if (mat == 1) vx = shade_metal(hi, pr, rd, rng, inside, acc);
+                else if (mat == 2) vx = shade_dielectric(hi, pr, ro, rd, rng, inside, acc);
+                else vx = shade_disney(hi, pr, ro, rd, rng, inside, acc);
+                const V3 ray_org = ro, ray_in = rd;
+                ro = vx.newO;
+                rd = vx.newD;
+                if (vx.skip) {
+                    prev_nee = false;
+                    continue;
+                }
+                inside = vx.inside;
+                if (!inside) {
+                    V3 contrib = vx.emission;
+                    if (nee) {
+                        if (prev_nee && (vx.emission.x != 0.0f || vx.emission.y != 0.0f || vx.emission.z != 0.0f))
+                            contrib = contrib * power_heuristic(ppdf, light_pdf_sa(L, h.prim, ray_org, vx.newO));
+                        const bool do_nee = (mat == 0 || mat == 3) && L.s.emissive_count > 0;
+                        if (do_nee) {
+                            ShadowRec sh;
+                            if (next_event(L, rng, mat == 3, vx.newO, hi.n, vx.albedo, pr, hi.tbn, ray_in, thr, sh)) {
+                                const TraceRay sr = make_trace_ray(sh.o.x, sh.o.y, sh.o.z, sh.d.x, sh.d.y, sh.d.z, 0.0f, sh.tmax);
+                                Hit sh_hit;
+                                uint32_t e2 = 0;
+                                e2 = traverse<true, false, false>(L.s.nodes, L.s.tris, sr, stack + threadIdx.x, kBlock, sh_hit, c);
+                                if (e2) atomicOr(ps.counters + kCntError, e2);
+                                ++n_shadow;
+                                if (sh_hit.prim == kMiss) rad = rad + sh.contrib;
+                            }
+                        }
+                        prev_nee = do_nee;
+                        ppdf = vx.pdf;
+                    }
+                    rad = rad + contrib * thr;
+                    thr = thr * vx.color;
+                } else {
+                    prev_nee = false;
+                }
+            }
+            const V3 col = clamp_keep_nan(rad, L.pc.directClamp);
+            if (L.samples) {
+                float* o = L.samples + 3ull * ((uint64_t)i * spp + smp);
+                o[0] = col.x; o[1] = col.y; o[2] = col.z;
+            }
+            if (!has_nan3(col)) {
+                sum = sum + col;
+                kept++;
+            }
+        }
+        const float k = (float)kept;
+        V3 fin{sum.x / k, sum.y / k, sum.z / k};
+        float4* a = reinterpret_cast<float4*>(L.accum) + i;
+        if (L.pc.sampleBatch > 0) {
+            const float4 prev = *a;
+            fin = div3(V3{prev.x, prev.y, prev.z} * (float)L.pc.sampleBatch + fin, (float)(L.pc.sampleBatch + 1));
+        }
+        *a = make_float4(fin.x, fin.y, fin.z, 1.0f);
+    }
+    // every lane of the warp reaches this point: reduce the per-thread ray counts
+    for (int o = 16; o > 0; o >>= 1) {
+        n_rays += __shfl_down_sync(0xFFFFFFFFu, n_rays, o);
+        n_shadow += __shfl_down_sync(0xFFFFFFFFu, n_shadow, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(reinterpret_cast<unsigned long long*>(ps.counters + kCntRays), n_rays);
+        atomicAdd(reinterpret_cast<unsigned long long*>(ps.counters + kCntShadowRays), n_shadow);
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
 // Host side
 void RenderWorkspace::ensure(uint32_t paths) {
     if (paths <= capacity_ && buf_.get()) return;
@@ -613,7 +763,16 @@ void render_frame(RenderWorkspace& ws, const DeviceScene& s, const RtPushConsts&
     const int simple_blocks = (int)std::min<uint64_t>((P + kBlock - 1) / kBlock, (uint64_t)g_simple);
     uint32_t* cnt = L.ps.counters;
     check_cuda(cudaMemsetAsync(cnt, 0, kNumCounters * sizeof(uint32_t), st), "cudaMemsetAsync counters");
-    for (uint32_t smp = 0; smp < pc.samplesPerPixel; ++smp) {
+    if (opt.megakernel) {
+        static int g_mega = 0, g_mega_sm = -1;
+        if (g_mega_sm != sm_count) {
+            g_mega = occupancy_blocks((const void*)k_megakernel, sm_count);
+            g_mega_sm = sm_count;
+        }
+        const int blocks = (int)std::min<uint64_t>((P + kBlock - 1) / kBlock, (uint64_t)g_mega);
+        k_megakernel<<<blocks, kBlock, 0, st>>>(L);
+    }
+    for (uint32_t smp = 0; smp < (opt.megakernel ? 0u : pc.samplesPerPixel); ++smp) {
         L.sample = smp;
         k_init<<<simple_blocks, kBlock, 0, st>>>(L);
         int cur = 0;
@@ -632,7 +791,7 @@ void render_frame(RenderWorkspace& ws, const DeviceScene& s, const RtPushConsts&
         }
         k_finish<<<simple_blocks, kBlock, 0, st>>>(L);
     }
-    k_resolve<<<simple_blocks, kBlock, 0, st>>>(L);
+    if (!opt.megakernel) k_resolve<<<simple_blocks, kBlock, 0, st>>>(L);
     check_cuda(cudaGetLastError(), "render launch");
     if (stats) {
         uint32_t c[kNumCounters];

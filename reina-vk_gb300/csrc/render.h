@@ -19,6 +19,7 @@ struct RenderOpts {
     uint32_t seed = 1;
     uint32_t env_mode = 0;          // 0 sky gradient (raytrace.rmiss.glsl), 1 constant colour
     float env_color[3] = {0, 0, 0};
+    bool megakernel = false;        // plain form: one kernel, one thread per pixel (no queues)
 };
 
 // Queue indices of the per-material shade queues (0 = miss, then material_idx + 1).

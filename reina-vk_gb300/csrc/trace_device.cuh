@@ -109,36 +109,61 @@ __device__ __forceinline__ bool intersect_triangle(const TraceRay& r, const floa
     return true;
 }
 
-// Recomputes t, u, v of the selected triangle from double-precision signed volumes and rounds them to
-// float.  The FP32 test above decides which triangle is hit; this only sharpens the reported values
-// (FP32 barycentrics lose ~1e-5 of the triangle size when the origin is far from the triangle).
-// Vertices relative to the origin are exact in double; U, V, W = d . (C x B), d . (A x C), d . (B x A)
-// are the vertices' barycentric weights times det = U + V + W; t = (U A_kz + V B_kz + W C_kz) /
-// (det d_kz).  Only the final ratios are taken in float (no double division: GB300's FP64 rate is low).
+// Re-evaluates t, u, v of the selected triangle from an origin moved along the ray onto the hit point.
+// The FP32 test above decides which triangle is hit; this only sharpens the reported values (with a far
+// origin, FP32 barycentrics lose ~1e-5 of the triangle's size to cancellation).  The moved origin
+// o + t0 d is formed exactly as hi + lo with FMA-based TwoProduct and TwoSum (error-free transforms,
+// Ogita, Rump and Oishi, SIAM J. Sci. Comput. 26(6), 2005), so the vertex offsets are small and accurate;
+// a Möller–Trumbore evaluation there, with Kahan's FMA difference of products for the cross products
+// and the compensated dot product Dot2, gives barycentrics within ~1e-5 of exact, and t = t0 + t'.
+// Single precision only: GB300's FP64 rate is too low for a per-ray double evaluation.
+__device__ __forceinline__ void two_sum_f(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+__device__ __forceinline__ void two_prod_f(float a, float b, float& p, float& e) {
+    p = __fmul_rn(a, b);
+    e = __fmaf_rn(a, b, -p);
+}
+__device__ __forceinline__ float diff_prod_f(float a, float b, float c, float d) {   // a*b - c*d
+    const float w = __fmul_rn(c, d);
+    const float e = __fmaf_rn(-c, d, w);
+    const float f = __fmaf_rn(a, b, -w);
+    return __fadd_rn(f, e);
+}
+__device__ __forceinline__ float dot2_f(float x0, float x1, float x2, float y0, float y1, float y2) {
+    float p, s, h, r, q;
+    two_prod_f(x0, y0, p, s);
+    two_prod_f(x1, y1, h, r);
+    two_sum_f(p, h, p, q);
+    s = __fadd_rn(s, __fadd_rn(q, r));
+    two_prod_f(x2, y2, h, r);
+    two_sum_f(p, h, p, q);
+    s = __fadd_rn(s, __fadd_rn(q, r));
+    return __fadd_rn(p, s);
+}
+
 __device__ __forceinline__ void refine_hit(const TraceRay& r, const float4& a4, const float4& b4, const float4& c4,
                                            Hit& h) {
-    const double ox = r.ox, oy = r.oy, oz = r.oz, dx = r.dx, dy = r.dy, dz = r.dz;
-    const double Ax = __dsub_rn(a4.x, ox), Ay = __dsub_rn(a4.y, oy), Az = __dsub_rn(a4.z, oz);
-    const double Bx = __dsub_rn(b4.x, ox), By = __dsub_rn(b4.y, oy), Bz = __dsub_rn(b4.z, oz);
-    const double Cx = __dsub_rn(c4.x, ox), Cy = __dsub_rn(c4.y, oy), Cz = __dsub_rn(c4.z, oz);
-    auto trip = [&](double px, double py, double pz, double qx, double qy, double qz) {   // d . (p x q)
-        const double cx = __dsub_rn(__dmul_rn(py, qz), __dmul_rn(pz, qy));
-        const double cy = __dsub_rn(__dmul_rn(pz, qx), __dmul_rn(px, qz));
-        const double cz = __dsub_rn(__dmul_rn(px, qy), __dmul_rn(py, qx));
-        return __dadd_rn(__dadd_rn(__dmul_rn(dx, cx), __dmul_rn(dy, cy)), __dmul_rn(dz, cz));
+    const float t0 = h.t;
+    auto moved = [&](float o, float d, float v0) {   // (o + t0 d) - v0 with the moved origin kept exactly
+        float ph, pl, sh, sl;
+        two_prod_f(t0, d, ph, pl);
+        two_sum_f(o, ph, sh, sl);
+        return __fadd_rn(__fsub_rn(sh, v0), __fadd_rn(sl, pl));
     };
-    const double U = trip(Cx, Cy, Cz, Bx, By, Bz);
-    const double V = trip(Ax, Ay, Az, Cx, Cy, Cz);
-    const double W = trip(Bx, By, Bz, Ax, Ay, Az);
-    const double det = __dadd_rn(__dadd_rn(U, V), W);
-    if (det == 0.0) return;
-    const double Akz = pick3d(Ax, Ay, Az, r.kz), Bkz = pick3d(Bx, By, Bz, r.kz), Ckz = pick3d(Cx, Cy, Cz, r.kz);
-    const double Tn = __dadd_rn(__dadd_rn(__dmul_rn(U, Akz), __dmul_rn(V, Bkz)), __dmul_rn(W, Ckz));
-    const double den = __dmul_rn(det, pick3d(dx, dy, dz, r.kz));
-    const float fdet = __double2float_rn(det);
-    h.t = __fdiv_rn(__double2float_rn(Tn), __double2float_rn(den));
-    h.u = __fdiv_rn(__double2float_rn(V), fdet);
-    h.v = __fdiv_rn(__double2float_rn(W), fdet);
+    const float s0 = moved(r.ox, r.dx, a4.x), s1 = moved(r.oy, r.dy, a4.y), s2 = moved(r.oz, r.dz, a4.z);
+    const float e10 = __fsub_rn(b4.x, a4.x), e11 = __fsub_rn(b4.y, a4.y), e12 = __fsub_rn(b4.z, a4.z);
+    const float e20 = __fsub_rn(c4.x, a4.x), e21 = __fsub_rn(c4.y, a4.y), e22 = __fsub_rn(c4.z, a4.z);
+    const float p0 = diff_prod_f(r.dy, e22, r.dz, e21), p1 = diff_prod_f(r.dz, e20, r.dx, e22),
+                p2 = diff_prod_f(r.dx, e21, r.dy, e20);
+    const float det = dot2_f(e10, e11, e12, p0, p1, p2);
+    if (det == 0.0f) return;
+    const float q0 = diff_prod_f(s1, e12, s2, e11), q1 = diff_prod_f(s2, e10, s0, e12), q2 = diff_prod_f(s0, e11, s1, e10);
+    h.u = __fdiv_rn(dot2_f(s0, s1, s2, p0, p1, p2), det);
+    h.v = __fdiv_rn(dot2_f(r.dx, r.dy, r.dz, q0, q1, q2), det);
+    h.t = __fadd_rn(t0, __fdiv_rn(dot2_f(e20, e21, e22, q0, q1, q2), det));
 }
 
 // Byte `byte` of `word` as a float, exactly: the byte placed in the mantissa of 2^23 (one byte permute),

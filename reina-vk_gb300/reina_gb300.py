@@ -91,7 +91,20 @@ class RtPushConsts(C.Structure):
 
 class RenderOptions(C.Structure):
     _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("mode", C.c_uint32), ("seed", C.c_uint32),
-                ("env_mode", C.c_uint32), ("env_color", C.c_float * 3)]
+                ("env_mode", C.c_uint32), ("env_color", C.c_float * 3), ("flags", C.c_uint32)]
+
+
+RENDER_MEGAKERNEL = 1
+
+
+class BloomPushConsts(C.Structure):
+    """polyglot/bloom.h:4-8."""
+    _fields_ = [("radius", C.c_float), ("threshold", C.c_float), ("intensity", C.c_float)]
+
+
+class TonemappingPushConsts(C.Structure):
+    """polyglot/tonemapping.h:4-6."""
+    _fields_ = [("exposure", C.c_float)]
 
 
 class _RenderStats(C.Structure):
@@ -121,10 +134,12 @@ def push_consts(inv_view, inv_proj, sample_batch=0, total_emissive_weight=0.0, f
     return pc
 
 
-def render_options(width, height, mode=MODE_REINA, seed=1, env_mode=ENV_SKY, env_color=(0.0, 0.0, 0.0)) -> RenderOptions:
+def render_options(width, height, mode=MODE_REINA, seed=1, env_mode=ENV_SKY, env_color=(0.0, 0.0, 0.0),
+                   megakernel=False) -> RenderOptions:
     o = RenderOptions(width, height, mode, seed, env_mode)
     for k in range(3):
         o.env_color[k] = float(env_color[k])
+    o.flags = RENDER_MEGAKERNEL if megakernel else 0
     return o
 
 
@@ -207,6 +222,9 @@ def load_library() -> C.CDLL:
         "reina_raycast_counters": (I32, [P, P, P, U64, U32, C.POINTER(U64), C.POINTER(U64), P]),
         "reina_render": (I32, [P, P, C.POINTER(RtPushConsts), C.POINTER(RenderOptions), P, P, C.POINTER(_RenderStats)]),
         "reina_render_device": (I32, [P, P, C.POINTER(RtPushConsts), C.POINTER(RenderOptions), P, P, P]),
+        "reina_postprocess": (I32, [P, P, U32, U32, C.POINTER(BloomPushConsts), C.POINTER(TonemappingPushConsts), P, P]),
+        "reina_postprocess_device": (I32, [P, P, U32, U32, C.POINTER(BloomPushConsts),
+                                           C.POINTER(TonemappingPushConsts), P, P, P]),
         "reina_camera_matrices": (I32, [P, P, P, F, F, F, F, P, P]),
         "reina_icosphere_counts": (I32, [U32, C.POINTER(U64), C.POINTER(U64)]),
         "reina_gen_icosphere": (I32, [U32, F, U64, P, P, P]),
@@ -421,6 +439,19 @@ def render_device(ctx: Context, scene: Scene, pc: RtPushConsts, opts: RenderOpti
                   stream: int = 0) -> None:
     _check(_lib.reina_render_device(ctx.handle, scene.handle, C.byref(pc), C.byref(opts), C.c_void_p(d_accum),
                                     C.c_void_p(d_samples or None), C.c_void_p(stream)))
+
+
+def postprocess(ctx: Context, accum: np.ndarray, radius: float = 5.0, threshold: float = 1.0, intensity: float = 0.05,
+                exposure: float = 1.0, want_combined: bool = False):
+    """Reina::applyBloom + applyTonemapping: accum (H, W, 4) float32 -> (rgba8 (H, W, 4) uint8, combined)."""
+    accum = np.ascontiguousarray(accum, np.float32)
+    H, W = accum.shape[:2]
+    out = np.zeros((H, W, 4), np.uint8)
+    comb = np.zeros((H, W, 4), np.float32) if want_combined else None
+    b = BloomPushConsts(radius, threshold, intensity)
+    t = TonemappingPushConsts(exposure)
+    _check(_lib.reina_postprocess(ctx.handle, _ptr(accum), W, H, C.byref(b), C.byref(t), _ptr(out), _ptr(comb)))
+    return out, comb
 
 
 def camera_matrices(pos, front, up=(0.0, 1.0, 0.0), fovy_radians=np.radians(45.0), aspect=1.0, z_near=0.1,

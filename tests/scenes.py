@@ -60,7 +60,8 @@ LIGHT_Y = 2.5
 
 
 def large_scene_geometry(R, level: int = 8, seed: int = 1):
-    """Returns [(vertices (N,4), indices)] for sphere, ground plane and light quad (world space)."""
+    """Returns [(vertices (N,4), indices)] for sphere, ground plane and light quad (world space).
+    large_scene_tbn() gives the sphere's per-vertex tangent frames."""
     v, i, _ = R.icosphere(level, 0.1, seed)
     g = 10.0
     plane_v = np.array([[-g, GROUND_Y, -g, 1], [g, GROUND_Y, -g, 1], [g, GROUND_Y, g, 1], [-g, GROUND_Y, g, 1]], np.float32)
@@ -92,11 +93,21 @@ def large_scene_materials(R, n_faces: int, seed: int = 1):
     return mats, face
 
 
+def large_scene_tbn(R, level: int = 8, seed: int = 1):
+    """Per-vertex TBNs of the large scene's sphere (N = undisplaced radial direction)."""
+    _, _, n = R.icosphere(level, 0.1, seed)
+    up = np.where(np.abs(n[:, 1:2]) > 0.99, np.array([[1.0, 0, 0]]), np.array([[0, 1.0, 0]]))
+    t = np.cross(up, n)
+    t /= np.linalg.norm(t, axis=1, keepdims=True)
+    b = np.cross(n, t)
+    return np.concatenate([t, b, n], axis=1).astype(np.float32)
+
+
 def large_scene(R, ctx, level: int = 8, seed: int = 1, light_emission=(17.0, 12.0, 4.0)):
     geo = large_scene_geometry(R, level, seed)
     scene = R.Scene(ctx)
     (sv, si), (pv, pi), (lv, li) = geo
-    sid = scene.define_object(sv, si)
+    sid = scene.define_object(sv, si, tbns=large_scene_tbn(R, level, seed), tbn_indices=si)
     mats, face = large_scene_materials(R, si.size // 3, seed)
     scene.add_instance_per_face(sid, None, mats, face)
     scene.add_object(pv, pi, material=R.Material(material_idx=0, albedo=(0.5, 0.5, 0.5)))

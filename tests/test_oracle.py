@@ -113,3 +113,33 @@ def test_fp64_agrees_with_fp32(O):
     for k in "tuv":
         err = np.abs(h32[k][hit] - h64[k][hit]) / np.maximum(np.abs(h64[k][hit]), 1.0)
         assert np.quantile(err, 0.999) < 1e-5
+
+
+def test_tonemap_matches_golden(O):
+    kat = json.loads((GOLDEN / "tonemap_kat.json").read_text())
+    hdr = np.asarray(kat["hdr"], np.float32)
+    img = np.concatenate([hdr, np.ones((hdr.shape[0], 1), np.float32)], 1).reshape(1, -1, 4)
+    for ex, ref in kat["out"].items():
+        # intensity 0 isolates the tone map from the bloom
+        out, comb = O.postprocess(img, radius=5.0, threshold=1.0, intensity=0.0, exposure=float(ex))
+        assert np.array_equal(out[0, :, :3], np.asarray(ref, np.uint8)), ex
+        assert (out[0, :, 3] == 255).all()
+
+
+def test_bloom_matches_golden(O):
+    kat = json.loads((GOLDEN / "bloom_kat.json").read_text())
+    img = np.asarray(kat["image"], np.float32)
+    ref = np.asarray(kat["combined"], np.float32)
+    for precision in (32, 64):
+        _, comb = O.postprocess(img, kat["radius"], kat["threshold"], kat["intensity"], 0.0, precision=precision)
+        assert np.allclose(comb, ref, rtol=2e-6, atol=1e-7)
+
+
+def test_bloom_spreads_nan_like_the_reference(O):
+    """A NaN pixel reaches every output within the kernel support (its weight is multiplied, not tested)."""
+    img = np.zeros((8, 40, 4), np.float32)
+    img[4, 20, :3] = np.nan
+    _, comb = O.postprocess(img, radius=5.0, threshold=1.0, intensity=0.05, exposure=0.0)
+    K = int(40 * 5.0 / 100 * 3 + 0.5)
+    assert np.isnan(comb[4, 20 - K:20 + K + 1, 0]).all()
+    assert not np.isnan(comb[4, 20 + K + 1:, 0]).any()

@@ -114,7 +114,7 @@ def test_large_scene_crop_parity(R, O, gpu_ctx):
     (sv, si), (pv, pi), (lv, li) = geo
     mats, face = S.large_scene_materials(R, si.size // 3, 1)
     d = S.SceneDesc()
-    d.add_instance(d.add_object(sv, si), None, materials=mats, face_material=face)
+    d.add_instance(d.add_object(sv, si, S.large_scene_tbn(R, 8, 1), si), None, materials=mats, face_material=face)
     d.add_instance(d.add_object(pv, pi), None, R.Material(material_idx=0, albedo=(0.5, 0.5, 0.5)))
     d.add_instance(d.add_object(lv, li), None,
                    R.Material(material_idx=0, albedo=(0.9, 0.9, 0.9), emission=(17.0, 12.0, 4.0), cull_backface=True))
@@ -127,3 +127,20 @@ def test_large_scene_crop_parity(R, O, gpu_ctx):
     pix = (ys * W + xs).reshape(-1)
     frac = agree(g_smp[pix], o_smp[pix]).mean()
     assert frac >= 0.98, frac
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_megakernel_matches_wavefront(R, O, gpu_ctx, mode):
+    """The plain single-kernel form and the wavefront form compute the same samples."""
+    d = scenes.material_zoo(R)
+    scene = d.to_product(R, gpu_ctx)
+    W = H = 96
+    iv, ip = scenes.cornell_camera(R, W, H)
+    pc = R.push_consts(iv, ip, total_emissive_weight=scene.emissive_weight, spp=4, max_bounces=8, focus_dist=3.4)
+    a_w, s_w, st_w = R.render(gpu_ctx, scene, pc, R.render_options(W, H, mode, 1), want_samples=True)
+    a_m, s_m, st_m = R.render(gpu_ctx, scene, pc, R.render_options(W, H, mode, 1, megakernel=True), want_samples=True)
+    assert agree(s_m, s_w).mean() >= 0.995
+    assert abs(int(st_w["rays"]) - int(st_m["rays"])) <= 0.01 * st_w["rays"]
+    osc = d.to_oracle(O)
+    _, o_smp = osc.render(pc, W, H, mode=mode, want_samples=True)
+    assert agree(s_m, o_smp).mean() >= 0.99
