@@ -251,6 +251,24 @@ int reina_render_device(reina_ctx* ctx, const reina_scene* scene, const RtPushCo
                         const reina_render_options* options, void* d_accum_rgba32f, void* d_samples_rgb32f,
                         void* stream);
 
+/* Allocation-free render.  No counterpart in the reference: this entry point exists for callers that
+ * cannot call cudaMalloc while they run — a host whose allocator owns all device memory and gives none
+ * to plug-ins, a process whose device-memory budget is already handed out, or a frame loop that cannot
+ * afford the device-wide synchronization a cudaMalloc may cause.  It renders exactly like
+ * reina_render_device, but keeps the wavefront's path state and queues in a fixed array inside the
+ * library (REINA_NOALLOC_MAX_PIXELS pixels, 11.3 MB, held by every GPU that loads the library until
+ * the process exits) and calls no cudaMalloc, cudaFree or other allocating routine.  The caller still
+ * passes the accumulation image (and, optionally, the per-sample buffer) as device memory.
+ *   - width*height above REINA_NOALLOC_MAX_PIXELS is rejected with REINA_ERR_INVALID.
+ *   - The first call on a device looks up the array's device address (cudaGetSymbolAddress) with that
+ *     device current; make that first call before any stream capture.
+ *   - Every call uses the same array: calls whose work overlaps on the GPU (different streams, or
+ *     different host threads) race and corrupt each other's images; serialize them. */
+enum { REINA_NOALLOC_MAX_PIXELS = 65536 };
+int reina_render_device_noalloc(reina_ctx* ctx, const reina_scene* scene, const RtPushConsts* push_consts,
+                                const reina_render_options* options, void* d_accum_rgba32f, void* d_samples_rgb32f,
+                                void* stream);
+
 /* ------------------------------------------------------------------------------------------------ */
 /* Post-process — replaces Reina::applyBloom + Reina::applyTonemapping (src/Reina.cpp:472-577):        */
 /* blurX (threshold) -> blurY -> combine (shaders/postprocessing/bloom), then exposure and the          */

@@ -332,6 +332,20 @@ int reina_render_device(reina_ctx* ctx, const reina_scene* scene, const RtPushCo
     });
 }
 
+int reina_render_device_noalloc(reina_ctx* ctx, const reina_scene* scene, const RtPushConsts* pc,
+                                const reina_render_options* o, void* d_accum, void* d_samples, void* stream) {
+    return guard([&] {
+        need(ctx != nullptr, "ctx is NULL");
+        const rt::Scene& s = built_scene(scene);
+        const rt::RenderOpts r = render_opts(pc, o);
+        check_render_scene(s, pc, o);
+        need(d_accum != nullptr && ((uintptr_t)d_accum % 16) == 0, "accumulation buffer must be non-NULL and 16-byte aligned");
+        use_device(ctx);
+        rt::render_frame_noalloc(ctx->device, s.device_view(), *pc, r, static_cast<float*>(d_accum),
+                                 static_cast<float*>(d_samples), ctx->sm_count, static_cast<cudaStream_t>(stream));
+    });
+}
+
 int reina_render(reina_ctx* ctx, const reina_scene* scene, const RtPushConsts* pc, const reina_render_options* o,
                  float* accum, float* samples, reina_render_stats* stats) {
     return guard([&] {

@@ -12,6 +12,8 @@
 
 #include <algorithm>
 #include <cstring>
+#include <mutex>
+#include <string>
 
 #include "kernels.h"
 #include "render.h"
@@ -694,20 +696,21 @@ __global__ void __launch_bounds__(kBlock) k_megakernel(RenderLaunch L) {
 
 // ------------------------------------------------------------------------------------------------
 // Host side
-void RenderWorkspace::ensure(uint32_t paths) {
-    if (paths <= capacity_ && buf_.get()) return;
-    const size_t P = paths;
-    // 4-byte words per path: ray 6, hit 3, throughput 3, radiance 3, rng, flags, acc, ppdf (19);
-    // per pixel: rng, acc, sum 3, count (6); queues: active 2, shade 5, shadow 1 (8); shadow rays 10.
-    const size_t words = P * (19 + 6 + 8 + 10) + kNumCounters + 64;
-    buf_.alloc(words * 4);
-    uint32_t* w = buf_.as<uint32_t>();
+// 4-byte words per path: ray 6, hit 3, throughput 3, radiance 3, rng, flags, acc, ppdf (19);
+// per pixel: rng, acc, sum 3, count (6); queues: active 2, shade 5, shadow 1 (8); shadow rays 10.
+constexpr size_t kWordsPerPath = 19 + 6 + 8 + 10;
+constexpr size_t kHeaderWords = 64;   // counters, padded so that the arrays start 256-byte aligned
+
+static size_t path_state_words(size_t paths) { return paths * kWordsPerPath + kHeaderWords; }
+
+// Carves the SoA path state for `paths` slots out of `w` (path_state_words(paths) words).
+static PathState layout_path_state(uint32_t* w, size_t P) {
     size_t off = 0;
     auto f = [&]() { float* r = reinterpret_cast<float*>(w + off); off += P; return r; };
     auto u = [&]() { uint32_t* r = w + off; off += P; return r; };
     PathState s;
     s.counters = w;
-    off = 64;   // counters first (64 words, 256-byte aligned start of the arrays)
+    off = kHeaderWords;
     s.ox = f(); s.oy = f(); s.oz = f(); s.dx = f(); s.dy = f(); s.dz = f();
     s.hprim = u(); s.hu = f(); s.hv = f();
     s.tr = f(); s.tg = f(); s.tb = f();
@@ -719,7 +722,13 @@ void RenderWorkspace::ensure(uint32_t paths) {
     s.q_shadow = u();
     s.s_ox = f(); s.s_oy = f(); s.s_oz = f(); s.s_dx = f(); s.s_dy = f(); s.s_dz = f(); s.s_tmax = f();
     s.s_cr = f(); s.s_cg = f(); s.s_cb = f();
-    ps_ = s;
+    return s;
+}
+
+void RenderWorkspace::ensure(uint32_t paths) {
+    if (paths <= capacity_ && buf_.get()) return;
+    buf_.alloc(path_state_words(paths) * 4);
+    ps_ = layout_path_state(buf_.as<uint32_t>(), paths);
     capacity_ = paths;
 }
 
@@ -729,15 +738,14 @@ static int occupancy_blocks(const void* fn, int sm_count) {
     return std::max(1, per_sm) * std::max(1, sm_count);
 }
 
-void render_frame(RenderWorkspace& ws, const DeviceScene& s, const RtPushConsts& pc, const RenderOpts& opt,
-                  float* d_accum, float* d_samples, int sm_count, cudaStream_t st, RenderStats* stats) {
+// The frame's launch sequence over path state `ps` (at least width*height slots).
+static void launch_frame(const PathState& ps, const DeviceScene& s, const RtPushConsts& pc, const RenderOpts& opt,
+                         float* d_accum, float* d_samples, int sm_count, cudaStream_t st, RenderStats* stats) {
     const uint32_t P = opt.width * opt.height;
-    if (P == 0) return;
-    ws.ensure(P);
     RenderLaunch L;
     L.s = s;
     L.pc = pc;
-    L.ps = ws.view();
+    L.ps = ps;
     L.W = opt.width;
     L.H = opt.height;
     L.P = P;
@@ -804,6 +812,50 @@ void render_frame(RenderWorkspace& ws, const DeviceScene& s, const RtPushConsts&
         stats->shadow_rays = srays;
         stats->error = c[kCntError];
     }
+}
+
+void render_frame(RenderWorkspace& ws, const DeviceScene& s, const RtPushConsts& pc, const RenderOpts& opt,
+                  float* d_accum, float* d_samples, int sm_count, cudaStream_t st, RenderStats* stats) {
+    const uint32_t P = opt.width * opt.height;
+    if (P == 0) return;
+    ws.ensure(P);
+    launch_frame(ws.view(), s, pc, opt, d_accum, d_samples, sm_count, st, stats);
+}
+
+// ------------------------------------------------------------------------------------------------
+// Allocation-free variant (reina_render_device_noalloc): the path state and queues live in this
+// file-scope device array instead of a cudaMalloc'd workspace.  Every GPU that loads the library holds
+// it (path_state_words(kNoAllocMaxPixels) words = 11.3 MB) until the process exits.  All calls share
+// it: the launch sequence clears what must start at zero (the queue counters, the per-pixel sums at
+// sample 0), and calls whose work overlaps on the GPU race on it.
+static __device__ __align__(256) uint32_t g_noalloc_scratch[kNoAllocMaxPixels * kWordsPerPath + kHeaderWords];
+
+static std::mutex g_noalloc_mutex;
+static uint32_t* g_noalloc_addr[kNoAllocMaxDevices] = {};
+
+// Device address of the array on `device` (which must be current).  Host code only sees a host-side
+// stand-in under the array's name, so the address is looked up once per device, on that device's first
+// call, and cached.
+static uint32_t* noalloc_scratch(int device) {
+    if (device < 0 || device >= kNoAllocMaxDevices) fail(REINA_ERR_INVALID, "device ordinal out of range for the allocation-free render");
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_addr[device]) {
+        void* p = nullptr;
+        check_cuda(cudaGetSymbolAddress(&p, g_noalloc_scratch), "cudaGetSymbolAddress(allocation-free render scratch)");
+        g_noalloc_addr[device] = static_cast<uint32_t*>(p);
+    }
+    return g_noalloc_addr[device];
+}
+
+void render_frame_noalloc(int device, const DeviceScene& s, const RtPushConsts& pc, const RenderOpts& opt,
+                          float* d_accum, float* d_samples, int sm_count, cudaStream_t st) {
+    const uint64_t P = (uint64_t)opt.width * opt.height;
+    if (P > kNoAllocMaxPixels)
+        fail(REINA_ERR_INVALID, "allocation-free render is limited to " + std::to_string(kNoAllocMaxPixels) +
+                                    " pixels (e.g. 256x256); got " + std::to_string(opt.width) + "x" + std::to_string(opt.height));
+    if (P == 0) return;
+    uint32_t* base = noalloc_scratch(device);
+    launch_frame(layout_path_state(base, P), s, pc, opt, d_accum, d_samples, sm_count, st, nullptr);
 }
 
 }  // namespace rt

@@ -96,4 +96,11 @@ struct RenderStats {
 void render_frame(RenderWorkspace& ws, const DeviceScene& s, const RtPushConsts& pc, const RenderOpts& opt,
                   float* d_accum, float* d_samples, int sm_count, cudaStream_t st, RenderStats* stats);
 
+// The same frame with the path state in a fixed device array of the library (no allocation); at most
+// kNoAllocMaxPixels pixels.  `device` must be the current device.
+constexpr uint32_t kNoAllocMaxPixels = 65536;
+constexpr int kNoAllocMaxDevices = 64;
+void render_frame_noalloc(int device, const DeviceScene& s, const RtPushConsts& pc, const RenderOpts& opt,
+                          float* d_accum, float* d_samples, int sm_count, cudaStream_t st);
+
 }  // namespace rt

@@ -222,6 +222,7 @@ def load_library() -> C.CDLL:
         "reina_raycast_counters": (I32, [P, P, P, U64, U32, C.POINTER(U64), C.POINTER(U64), P]),
         "reina_render": (I32, [P, P, C.POINTER(RtPushConsts), C.POINTER(RenderOptions), P, P, C.POINTER(_RenderStats)]),
         "reina_render_device": (I32, [P, P, C.POINTER(RtPushConsts), C.POINTER(RenderOptions), P, P, P]),
+        "reina_render_device_noalloc": (I32, [P, P, C.POINTER(RtPushConsts), C.POINTER(RenderOptions), P, P, P]),
         "reina_postprocess": (I32, [P, P, U32, U32, C.POINTER(BloomPushConsts), C.POINTER(TonemappingPushConsts), P, P]),
         "reina_postprocess_device": (I32, [P, P, U32, U32, C.POINTER(BloomPushConsts),
                                            C.POINTER(TonemappingPushConsts), P, P, P]),
@@ -452,6 +453,17 @@ def postprocess(ctx: Context, accum: np.ndarray, radius: float = 5.0, threshold:
     t = TonemappingPushConsts(exposure)
     _check(_lib.reina_postprocess(ctx.handle, _ptr(accum), W, H, C.byref(b), C.byref(t), _ptr(out), _ptr(comb)))
     return out, comb
+
+
+NOALLOC_MAX_PIXELS = 65536
+
+
+def render_device_noalloc(ctx: Context, scene: Scene, pc: RtPushConsts, opts: RenderOptions, d_accum: int,
+                          d_samples: int = 0, stream: int = 0) -> None:
+    """reina_render_device_noalloc: the render without any device allocation, for callers that cannot
+    allocate while they run; at most NOALLOC_MAX_PIXELS pixels; overlapping calls race."""
+    _check(_lib.reina_render_device_noalloc(ctx.handle, scene.handle, C.byref(pc), C.byref(opts), C.c_void_p(d_accum),
+                                            C.c_void_p(d_samples or None), C.c_void_p(stream)))
 
 
 def camera_matrices(pos, front, up=(0.0, 1.0, 0.0), fovy_radians=np.radians(45.0), aspect=1.0, z_near=0.1,
