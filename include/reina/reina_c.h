@@ -64,6 +64,16 @@ void reina_ctx_destroy(reina_ctx* ctx);
 /* Number of streaming multiprocessors of the context's GPU (0 if unknown). */
 int reina_ctx_sm_count(const reina_ctx* ctx);
 
+/* Launch parameters of the traversal kernels (no counterpart in the reference, whose traversal is the
+ * driver's).  refill = 0: one thread per ray (grid form, the default); refill = 1..32: persistent warps
+ * that fetch new rays when `refill` of their 32 lanes are idle. */
+typedef struct reina_tuning {
+    uint32_t refill;
+    uint32_t reserved[3];
+} reina_tuning;
+int reina_ctx_set_tuning(reina_ctx* ctx, const reina_tuning* tuning);
+int reina_ctx_get_tuning(const reina_ctx* ctx, reina_tuning* out_tuning);
+
 /* ------------------------------------------------------------------------------------------------ */
 /* Scene API  (src/scene/Scene.h:62-138)                                                             */
 /* ------------------------------------------------------------------------------------------------ */

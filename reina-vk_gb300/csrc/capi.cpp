@@ -1,4 +1,5 @@
 // C ABI of the library (include/reina/reina_c.h): handles, status codes and thread-local messages.
+#include <atomic>
 #include <chrono>
 #include <cstring>
 #include <memory>
@@ -25,6 +26,11 @@ struct reina_ctx {
     cudaStream_t streams[2] = {nullptr, nullptr};
     rt::DeviceBuffer err;        // u32 device error flag, OR-ed by kernels
     rt::DeviceBuffer counters;   // u64 x 2 traversal counters
+    rt::DeviceBuffer fetch;      // ring of u32 ray-fetch counters, one per ray-cast launch in flight
+    std::atomic<uint32_t> fetch_slot{0};
+    int refill = rt::kDefaultRefill;
+    uint32_t* next_fetch_counter() { return fetch.as<uint32_t>() + (fetch_slot.fetch_add(1) % kFetchSlots); }
+    static constexpr uint32_t kFetchSlots = 256;
     rt::DeviceBuffer rays, hits; // staging for host-buffer ray casts
     rt::RenderWorkspace render;  // wavefront path state and queues
     rt::DeviceBuffer accum, samples;   // staging for host-buffer renders
@@ -131,6 +137,7 @@ int reina_ctx_create(const reina_ctx_options* options, reina_ctx** out_ctx) {
         for (auto& s : ctx->streams) check_cuda(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "cudaStreamCreate");
         ctx->err.alloc(sizeof(uint32_t));
         ctx->counters.alloc(2 * sizeof(unsigned long long));
+        ctx->fetch.alloc(reina_ctx::kFetchSlots * sizeof(uint32_t));
         check_cuda(cudaMemset(ctx->err.get(), 0, sizeof(uint32_t)), "cudaMemset");
         *out_ctx = ctx.release();
     });
@@ -145,6 +152,22 @@ void reina_ctx_destroy(reina_ctx* ctx) {
 }
 
 int reina_ctx_sm_count(const reina_ctx* ctx) { return ctx ? ctx->sm_count : 0; }
+
+int reina_ctx_set_tuning(reina_ctx* ctx, const reina_tuning* t) {
+    return guard([&] {
+        need(ctx && t, "NULL argument");
+        need(t->refill <= 32, "refill must be in 0..32");
+        ctx->refill = (int)t->refill;
+    });
+}
+
+int reina_ctx_get_tuning(const reina_ctx* ctx, reina_tuning* out) {
+    return guard([&] {
+        need(ctx && out, "NULL argument");
+        std::memset(out, 0, sizeof(*out));
+        out->refill = (uint32_t)ctx->refill;
+    });
+}
 
 int reina_scene_create(reina_ctx* ctx, reina_scene** out_scene) {
     return guard([&] {
@@ -236,9 +259,11 @@ int reina_raycast_device(reina_ctx* ctx, const reina_scene* scene, const void* d
         need(flags <= REINA_RAY_ANY, "flags must be REINA_RAY_CLOSEST or REINA_RAY_ANY");
         need(count == 0 || (d_rays && d_hits), "NULL ray or hit buffer");
         need(((uintptr_t)d_rays % 16) == 0 && ((uintptr_t)d_hits % 16) == 0, "ray and hit buffers must be 16-byte aligned");
+        need(count < (1ull << 32), "at most 2^32 - 1 rays per call");
         use_device(ctx);
         rt::launch_raycast(s.device_view(), static_cast<const rt::Ray*>(d_rays), count, static_cast<rt::Hit*>(d_hits),
-                           flags == REINA_RAY_ANY, ctx->err.as<uint32_t>(), static_cast<cudaStream_t>(stream));
+                           flags == REINA_RAY_ANY, ctx->err.as<uint32_t>(), ctx->next_fetch_counter(), ctx->sm_count,
+                           ctx->refill, static_cast<cudaStream_t>(stream));
         check_cuda(cudaGetLastError(), "raycast launch");
     });
 }
@@ -263,7 +288,8 @@ int reina_raycast(reina_ctx* ctx, const reina_scene* scene, const reina_ray* ray
             rt::Ray* dr = ctx->rays.as<rt::Ray>() + off;
             rt::Hit* dh = ctx->hits.as<rt::Hit>() + off;
             check_cuda(cudaMemcpyAsync(dr, rays + off, n * sizeof(rt::Ray), cudaMemcpyHostToDevice, st), "cudaMemcpyAsync H2D");
-            rt::launch_raycast(s.device_view(), dr, n, dh, flags == REINA_RAY_ANY, ctx->err.as<uint32_t>(), st);
+            rt::launch_raycast(s.device_view(), dr, n, dh, flags == REINA_RAY_ANY, ctx->err.as<uint32_t>(),
+                               ctx->next_fetch_counter(), ctx->sm_count, ctx->refill, st);
             check_cuda(cudaGetLastError(), "raycast launch");
             check_cuda(cudaMemcpyAsync(hits + off, dh, n * sizeof(rt::Hit), cudaMemcpyDeviceToHost, st), "cudaMemcpyAsync D2H");
         }
@@ -283,8 +309,10 @@ int reina_raycast_counters(reina_ctx* ctx, const reina_scene* scene, const void*
         use_device(ctx);
         cudaStream_t st = static_cast<cudaStream_t>(stream);
         check_cuda(cudaMemsetAsync(ctx->counters.get(), 0, 2 * sizeof(unsigned long long), st), "cudaMemsetAsync");
+        need(count < (1ull << 32), "at most 2^32 - 1 rays per call");
         rt::launch_raycast_counters(s.device_view(), static_cast<const rt::Ray*>(d_rays), count, flags == REINA_RAY_ANY,
-                                    ctx->counters.as<unsigned long long>(), ctx->err.as<uint32_t>(), st);
+                                    ctx->counters.as<unsigned long long>(), ctx->err.as<uint32_t>(),
+                                    ctx->next_fetch_counter(), ctx->sm_count, st);
         check_cuda(cudaGetLastError(), "raycast counters launch");
         unsigned long long c[2] = {0, 0};
         check_cuda(cudaMemcpyAsync(c, ctx->counters.get(), sizeof(c), cudaMemcpyDeviceToHost, st), "cudaMemcpyAsync");
@@ -323,7 +351,8 @@ int reina_render_device(reina_ctx* ctx, const reina_scene* scene, const RtPushCo
     return guard([&] {
         need(ctx != nullptr, "ctx is NULL");
         const rt::Scene& s = built_scene(scene);
-        const rt::RenderOpts r = render_opts(pc, o);
+        rt::RenderOpts r = render_opts(pc, o);
+        r.refill = ctx->refill;
         check_render_scene(s, pc, o);
         need(d_accum != nullptr && ((uintptr_t)d_accum % 16) == 0, "accumulation buffer must be non-NULL and 16-byte aligned");
         use_device(ctx);
@@ -337,7 +366,8 @@ int reina_render_device_noalloc(reina_ctx* ctx, const reina_scene* scene, const 
     return guard([&] {
         need(ctx != nullptr, "ctx is NULL");
         const rt::Scene& s = built_scene(scene);
-        const rt::RenderOpts r = render_opts(pc, o);
+        rt::RenderOpts r = render_opts(pc, o);
+        r.refill = ctx->refill;
         check_render_scene(s, pc, o);
         need(d_accum != nullptr && ((uintptr_t)d_accum % 16) == 0, "accumulation buffer must be non-NULL and 16-byte aligned");
         use_device(ctx);
@@ -351,7 +381,8 @@ int reina_render(reina_ctx* ctx, const reina_scene* scene, const RtPushConsts* p
     return guard([&] {
         need(ctx != nullptr, "ctx is NULL");
         const rt::Scene& s = built_scene(scene);
-        const rt::RenderOpts r = render_opts(pc, o);
+        rt::RenderOpts r = render_opts(pc, o);
+        r.refill = ctx->refill;
         check_render_scene(s, pc, o);
         need(accum != nullptr, "accumulation buffer is NULL");
         use_device(ctx);

@@ -128,8 +128,8 @@ __global__ void __launch_bounds__(kBlock) k_init(RenderLaunch L) {
 }
 
 // ------------------------------------------------------------------------------------------------
-// extend: closest hit + classification
-__global__ void __launch_bounds__(kBlock) k_extend(RenderLaunch L, int cur) {
+// extend: closest hit + classification.  Grid form: each warp takes 32 consecutive queue entries.
+__global__ void __launch_bounds__(kBlock) k_extend_grid(RenderLaunch L, int cur) {
     __shared__ uint2 stack[kSmemStack * kBlock];
     const PathState& ps = L.ps;
     const uint32_t n = ps.counters[kCntActive + cur];
@@ -161,6 +161,43 @@ __global__ void __launch_bounds__(kBlock) k_extend(RenderLaunch L, int cur) {
             if (mine) ps.q_shade[(size_t)k * L.P + pos] = p;
         }
     }
+}
+
+// Persistent form: warps refill idle lanes from the queue (dynamic ray fetch).
+__global__ void __launch_bounds__(kBlock) k_extend(RenderLaunch L, int cur) {
+    __shared__ uint2 stack[kSmemStack * kBlock];
+    const PathState& ps = L.ps;
+    const uint32_t n = ps.counters[kCntActive + cur];
+    const uint32_t* q = ps.q_active[cur];
+    TraceCounters c{0u, 0u};
+    auto load = [&](uint32_t i, TraceRay& r) {
+        const uint32_t p = q[i];
+        r = make_trace_ray(ps.ox[p], ps.oy[p], ps.oz[p], ps.dx[p], ps.dy[p], ps.dz[p], 0.0f, 10000.0f);
+        return true;
+    };
+    auto store = [&](uint32_t i, const Hit& h, bool valid) {   // called by all 32 lanes
+        if (__ballot_sync(0xFFFFFFFFu, valid) == 0u) return;
+        int m = -1;
+        uint32_t p = 0;
+        if (valid) {
+            p = q[i];
+            ps.hprim[p] = h.prim;
+            ps.hu[p] = h.u;
+            ps.hv[p] = h.v;
+            m = h.prim == kMiss ? kQueueMiss : 1 + (int)L.s.props_material[L.s.prim_props[h.prim]];
+        }
+        warp_count64(reinterpret_cast<unsigned long long*>(ps.counters + kCntRays), valid);
+#pragma unroll
+        for (int k = 0; k < kNumQueues; ++k) {
+            const bool mine = valid && m == k;
+            const uint32_t pos = warp_append(ps.counters + kCntQueue + k, mine);
+            if (mine) ps.q_shade[(size_t)k * L.P + pos] = p;
+        }
+    };
+    const uint32_t e = persistent_trace<false, false, true>(L.s.nodes, L.s.tris, L.s.node_count, n,
+                                                           ps.counters + kCntFetchExtend, stack + threadIdx.x, kBlock,
+                                                           L.refill, load, store, c);
+    if (e) atomicOr(ps.counters + kCntError, e);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -481,8 +518,8 @@ __global__ void __launch_bounds__(kBlock) k_shade_miss(RenderLaunch L) {
     }
 }
 
-// nee.h.glsl:126-144: any hit in [0, dist - 0.001]; unoccluded contributions are added.
-__global__ void __launch_bounds__(kBlock) k_shadow(RenderLaunch L) {
+// nee.h.glsl:126-144: any hit in [0, dist - 0.001]; unoccluded contributions are added.  Grid form.
+__global__ void __launch_bounds__(kBlock) k_shadow_grid(RenderLaunch L) {
     __shared__ uint2 stack[kSmemStack * kBlock];
     const PathState& ps = L.ps;
     const uint32_t n = ps.counters[kCntShadow];
@@ -505,6 +542,29 @@ __global__ void __launch_bounds__(kBlock) k_shadow(RenderLaunch L) {
         }
         warp_count64(reinterpret_cast<unsigned long long*>(ps.counters + kCntShadowRays), active);
     }
+}
+
+// Persistent form of the shadow kernel.
+__global__ void __launch_bounds__(kBlock) k_shadow(RenderLaunch L) {
+    __shared__ uint2 stack[kSmemStack * kBlock];
+    const PathState& ps = L.ps;
+    const uint32_t n = ps.counters[kCntShadow];
+    TraceCounters c{0u, 0u};
+    auto load = [&](uint32_t i, TraceRay& r) {
+        r = make_trace_ray(ps.s_ox[i], ps.s_oy[i], ps.s_oz[i], ps.s_dx[i], ps.s_dy[i], ps.s_dz[i], 0.0f, ps.s_tmax[i]);
+        return true;
+    };
+    auto store = [&](uint32_t i, const Hit& h, bool valid) {   // called by all 32 lanes
+        if (valid && h.prim == kMiss) {
+            const uint32_t p = ps.q_shadow[i];
+            store_rad(ps, p, load_rad(ps, p) + V3{ps.s_cr[i], ps.s_cg[i], ps.s_cb[i]});
+        }
+        warp_count64(reinterpret_cast<unsigned long long*>(ps.counters + kCntShadowRays), valid);
+    };
+    const uint32_t e = persistent_trace<true, false, false>(L.s.nodes, L.s.tris, L.s.node_count, n,
+                                                           ps.counters + kCntFetchShadow, stack + threadIdx.x, kBlock,
+                                                           L.refill, load, store, c);
+    if (e) atomicOr(ps.counters + kCntError, e);
 }
 
 // raytrace.rgen.glsl:264-275: clamp to [0, directClamp] (NaN kept), drop NaN samples, sum the rest.
@@ -755,6 +815,7 @@ static void launch_frame(const PathState& ps, const DeviceScene& s, const RtPush
     for (int k = 0; k < 3; ++k) L.env[k] = opt.env_color[k];
     L.accum = d_accum;
     L.samples = d_samples;
+    L.refill = opt.refill;
 
     static int g_ext = 0, g_sh = 0, g_shade[5] = {0, 0, 0, 0, 0}, g_simple = 0;
     static int g_sm = -1;
@@ -788,13 +849,18 @@ static void launch_frame(const PathState& ps, const DeviceScene& s, const RtPush
             // next active queue and the shade / shadow queues start empty
             check_cuda(cudaMemsetAsync(cnt + kCntActive + (cur ^ 1), 0, sizeof(uint32_t), st), "cudaMemsetAsync");
             check_cuda(cudaMemsetAsync(cnt + kCntQueue, 0, 6 * sizeof(uint32_t), st), "cudaMemsetAsync");
-            k_extend<<<g_ext, kBlock, 0, st>>>(L, cur);
+            check_cuda(cudaMemsetAsync(cnt + kCntFetchExtend, 0, 2 * sizeof(uint32_t), st), "cudaMemsetAsync");
+            if (opt.refill > 0) k_extend<<<g_ext, kBlock, 0, st>>>(L, cur);
+            else k_extend_grid<<<g_ext, kBlock, 0, st>>>(L, cur);
             k_shade_miss<<<simple_blocks, kBlock, 0, st>>>(L);
             k_shade<1><<<g_shade[1], kBlock, 0, st>>>(L, cur);
             k_shade<2><<<g_shade[2], kBlock, 0, st>>>(L, cur);
             k_shade<3><<<g_shade[3], kBlock, 0, st>>>(L, cur);
             k_shade<4><<<g_shade[4], kBlock, 0, st>>>(L, cur);
-            if (opt.mode == kModeNeeMis) k_shadow<<<g_sh, kBlock, 0, st>>>(L);
+            if (opt.mode == kModeNeeMis) {
+                if (opt.refill > 0) k_shadow<<<g_sh, kBlock, 0, st>>>(L);
+                else k_shadow_grid<<<g_sh, kBlock, 0, st>>>(L);
+            }
             cur ^= 1;
         }
         k_finish<<<simple_blocks, kBlock, 0, st>>>(L);

@@ -20,6 +20,7 @@ struct RenderOpts {
     uint32_t env_mode = 0;          // 0 sky gradient (raytrace.rmiss.glsl), 1 constant colour
     float env_color[3] = {0, 0, 0};
     bool megakernel = false;        // plain form: one kernel, one thread per pixel (no queues)
+    int refill = 0;                 // traversal form: 0 grid, 1..32 persistent (idle lanes that trigger a fetch)
 };
 
 // Queue indices of the per-material shade queues (0 = miss, then material_idx + 1).
@@ -34,6 +35,8 @@ constexpr int kCntShadow = 7;
 constexpr int kCntError = 8;
 constexpr int kCntRays = 10;
 constexpr int kCntShadowRays = 12;
+constexpr int kCntFetchExtend = 14;   // ray-fetch counters of the persistent extend / shadow kernels
+constexpr int kCntFetchShadow = 15;
 constexpr int kNumCounters = 16;
 
 // Plain-pointer view of the path state (SoA) passed to every kernel.
@@ -68,6 +71,7 @@ struct RenderLaunch {
     uint32_t mode, seed, env_mode;
     float env[3];
     uint32_t sample;          // sample index within the frame (one wave per sample)
+    int refill;               // persistent traversal refill threshold
     float* accum;             // W*H*4 RGBA32F (device)
     float* samples;           // optional W*H*spp*3 per-sample colours (device)
 };

@@ -223,83 +223,167 @@ struct TraceCounters {
     uint32_t tris;
 };
 
-// Traverses the BVH8.  `stack` points at this thread's first shared-memory stack entry; consecutive
-// entries are `stride` elements apart.  Closest hit: the lowest (t, prim) over all triangles hit in
-// [tmin, tmax].  Any hit: the first triangle found hit in [tmin, tmax].  With REFINE the reported
-// t, u, v of the selected triangle are recomputed in double precision (refine_hit).  Returns an error
-// code (0 = ok) for the caller's error flag.
-template <bool ANY, bool COUNT, bool REFINE = true>
-__device__ __forceinline__ uint32_t traverse(const Bvh8Node* __restrict__ nodes, const TriRecord* __restrict__ tris,
-                                             const TraceRay& r, uint2* stack, int stride, Hit& hit,
-                                             TraceCounters& cnt) {
+// Resumable traversal state of one ray (the shared-memory stack and the local spill array live with
+// the caller).  Closest hit: the lowest (t, prim) over all triangles hit in [tmin, tmax].  Any hit: the
+// first triangle found hit in [tmin, tmax].
+struct TravState {
+    uint2 group;        // current node group: child base, node hits (bits 24..31) | internal mask
+    float best_t;
+    uint32_t best_rec;  // triangle record of the current best hit
+    int sp;
+    uint32_t steps;
+};
+
+__device__ __forceinline__ void trav_init(const TraceRay& r, TravState& s, Hit& hit) {
+    s.group = make_uint2(0u, 0x80000000u);
+    s.best_t = r.tmax;
+    s.best_rec = 0;
+    s.sp = 0;
+    s.steps = 0;
     hit.prim = kMiss;
     hit.t = r.tmax;
     hit.u = 0.0f;
     hit.v = 0.0f;
-    uint32_t best_rec = 0;
-    uint2 spill[kTotalStack - kSmemStack];
-    int sp = 0;
-    uint2 group = make_uint2(0u, 0x80000000u);
-    float best_t = r.tmax;
-    uint32_t err = 0;
+}
+
+// One traversal step: visits the nearest pending child node and tests the triangles of its leaf
+// children.  Returns true when the ray is finished.
+template <bool ANY, bool COUNT>
+__device__ __forceinline__ bool trav_step(const Bvh8Node* __restrict__ nodes, const TriRecord* __restrict__ tris,
+                                          const TraceRay& r, TravState& s, Hit& hit, uint2* stack, int stride,
+                                          uint2* spill, TraceCounters& cnt, uint32_t& err) {
+    if (++s.steps > kMaxTraversalSteps) { err |= kErrStepLimit; return true; }
     const uint4* nptr = reinterpret_cast<const uint4*>(nodes);
     const float4* tptr = reinterpret_cast<const float4*>(tris);
-    for (uint32_t step = 0;; ++step) {
-        if (step >= kMaxTraversalSteps) { err |= kErrStepLimit; break; }
-        // group.y holds node hits in bits 24..31 here.
-        const uint32_t slot_bit = 31u - __clz(group.y);
-        const uint32_t slot = (slot_bit - 24u) ^ r.oct_inv;
-        const uint32_t rel = __popc(group.y & ((1u << slot) - 1u));
-        const uint32_t child = group.x + rel;
-        group.y &= ~(1u << slot_bit);
-        if (group.y > 0x00FFFFFFu) {
-            if (sp < kSmemStack) stack[sp * stride] = group;
-            else if (sp < kTotalStack) spill[sp - kSmemStack] = group;
-            else { err |= kErrStackOverflow; break; }
-            ++sp;
-        }
-        const uint4* np = nptr + 5ull * child;
-        const uint4 w0 = __ldg(np + 0), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3), w4 = __ldg(np + 4);
-        if (COUNT) cnt.nodes++;
-        const uint32_t hm = intersect_children(r, w0, w1, w2, w3, w4, best_t);
-        group = make_uint2(w1.x, (hm & 0xFF000000u) | (w0.w >> 24));
-        uint32_t thits = hm & 0x00FFFFFFu;
-        const uint32_t tri_base = w1.y;
-        bool done = false;
-        while (thits) {
-            const int k = __ffs(thits) - 1;
-            thits &= thits - 1u;
-            const float4* tp = tptr + 3ull * (tri_base + (uint32_t)k);
-            const float4 a = __ldg(tp + 0), b = __ldg(tp + 1), c = __ldg(tp + 2);
-            if (COUNT) cnt.tris++;
-            float t, u, v;
-            if (intersect_triangle(r, a, b, c, best_t, t, u, v)) {
-                const uint32_t prim = __float_as_uint(a.w);
-                if (ANY) {
-                    hit.prim = prim; hit.t = t; hit.u = u; hit.v = v;
-                    best_rec = tri_base + (uint32_t)k;
-                    done = true;
-                    break;
-                }
-                if (t < best_t || prim < hit.prim) {   // t <= best_t holds; equal t: lower id wins
-                    best_t = t;
-                    hit.prim = prim; hit.t = t; hit.u = u; hit.v = v;
-                    best_rec = tri_base + (uint32_t)k;
-                }
+    // s.group.y holds node hits in bits 24..31 here.
+    const uint32_t slot_bit = 31u - __clz(s.group.y);
+    const uint32_t slot = (slot_bit - 24u) ^ r.oct_inv;
+    const uint32_t rel = __popc(s.group.y & ((1u << slot) - 1u));
+    const uint32_t child = s.group.x + rel;
+    s.group.y &= ~(1u << slot_bit);
+    if (s.group.y > 0x00FFFFFFu) {
+        if (s.sp < kSmemStack) stack[s.sp * stride] = s.group;
+        else if (s.sp < kTotalStack) spill[s.sp - kSmemStack] = s.group;
+        else { err |= kErrStackOverflow; return true; }
+        ++s.sp;
+    }
+    const uint4* np = nptr + 5ull * child;
+    const uint4 w0 = __ldg(np + 0), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3), w4 = __ldg(np + 4);
+    if (COUNT) cnt.nodes++;
+    const uint32_t hm = intersect_children(r, w0, w1, w2, w3, w4, s.best_t);
+    s.group = make_uint2(w1.x, (hm & 0xFF000000u) | (w0.w >> 24));
+    uint32_t thits = hm & 0x00FFFFFFu;
+    const uint32_t tri_base = w1.y;
+    while (thits) {
+        const int k = __ffs(thits) - 1;
+        thits &= thits - 1u;
+        const float4* tp = tptr + 3ull * (tri_base + (uint32_t)k);
+        const float4 a = __ldg(tp + 0), b = __ldg(tp + 1), c = __ldg(tp + 2);
+        if (COUNT) cnt.tris++;
+        float t, u, v;
+        if (intersect_triangle(r, a, b, c, s.best_t, t, u, v)) {
+            const uint32_t prim = __float_as_uint(a.w);
+            if (ANY) {
+                hit.prim = prim; hit.t = t; hit.u = u; hit.v = v;
+                s.best_rec = tri_base + (uint32_t)k;
+                return true;
+            }
+            if (t < s.best_t || prim < hit.prim) {   // t <= best_t holds; equal t: lower id wins
+                s.best_t = t;
+                hit.prim = prim; hit.t = t; hit.u = u; hit.v = v;
+                s.best_rec = tri_base + (uint32_t)k;
             }
         }
-        if (done) break;
-        if (group.y <= 0x00FFFFFFu) {
-            if (sp == 0) break;
-            --sp;
-            group = sp < kSmemStack ? stack[sp * stride] : spill[sp - kSmemStack];
-        }
     }
+    if (s.group.y <= 0x00FFFFFFu) {
+        if (s.sp == 0) return true;
+        --s.sp;
+        s.group = s.sp < kSmemStack ? stack[s.sp * stride] : spill[s.sp - kSmemStack];
+    }
+    return false;
+}
+
+// After the last step: a miss reports t = tmax; a hit gets its reported t, u, v refined (refine_hit).
+template <bool REFINE>
+__device__ __forceinline__ void trav_finish(const Bvh8Node* __restrict__ nodes, const TriRecord* __restrict__ tris,
+                                            const TraceRay& r, const TravState& s, Hit& hit) {
+    (void)nodes;
     if (hit.prim == kMiss) {
         hit.t = r.tmax;
     } else if (REFINE) {
-        const float4* tp = tptr + 3ull * best_rec;
+        const float4* tp = reinterpret_cast<const float4*>(tris) + 3ull * s.best_rec;
         refine_hit(r, __ldg(tp + 0), __ldg(tp + 1), __ldg(tp + 2), hit);
+    }
+}
+
+// Traverses the BVH8 for one ray to completion.  `stack` points at this thread's first shared-memory
+// stack entry; consecutive entries are `stride` elements apart.  Returns an error code (0 = ok).
+template <bool ANY, bool COUNT, bool REFINE = true>
+__device__ __forceinline__ uint32_t traverse(const Bvh8Node* __restrict__ nodes, const TriRecord* __restrict__ tris,
+                                             const TraceRay& r, uint2* stack, int stride, Hit& hit,
+                                             TraceCounters& cnt) {
+    TravState s;
+    trav_init(r, s, hit);
+    uint2 spill[kTotalStack - kSmemStack];
+    uint32_t err = 0;
+    while (!trav_step<ANY, COUNT>(nodes, tris, r, s, hit, stack, stride, spill, cnt, err)) {
+    }
+    trav_finish<REFINE>(nodes, tris, r, s, hit);
+    return err;
+}
+
+// Persistent traversal with dynamic ray fetch (Aila and Laine, "Understanding the Efficiency of Ray
+// Traversal on GPUs", HPG 2009): every warp keeps 32 rays in flight; whenever at least `refill` lanes
+// have finished, those lanes take the next rays from the global counter `next` (one atomic per warp),
+// so short rays do not idle their lane until the warp's longest ray ends.
+//   load(idx, ray) -> false if item idx has no ray to trace (then store is called at once with a miss)
+//   store(idx, hit, valid): called by all 32 lanes after every step; valid marks lanes that finished
+//   an item in that step (store may use warp-collective operations).
+// Requires blockDim.x to be a multiple of 32.
+template <bool ANY, bool COUNT, bool REFINE, class Load, class Store>
+__device__ __forceinline__ uint32_t persistent_trace(const Bvh8Node* __restrict__ nodes, const TriRecord* __restrict__ tris,
+                                                     uint32_t node_count, uint32_t n, uint32_t* next, uint2* stack,
+                                                     int stride, int refill, Load load, Store store, TraceCounters& cnt) {
+    const uint32_t lane = threadIdx.x & 31u;
+    uint2 spill[kTotalStack - kSmemStack];
+    uint32_t err = 0;
+    bool has = false, exhausted = false;
+    uint32_t idx = 0;
+    TraceRay r;
+    TravState st;
+    Hit hit;
+    for (;;) {
+        const unsigned idle = __ballot_sync(0xFFFFFFFFu, !has);
+        if (!exhausted && __popc(idle) >= refill) {
+            uint32_t base = 0;
+            if (lane == 0) base = atomicAdd(next, (uint32_t)__popc(idle));
+            base = __shfl_sync(0xFFFFFFFFu, base, 0);
+            if (base + (uint32_t)__popc(idle) >= n) exhausted = true;
+            bool fresh = false;
+            if (!has) {
+                idx = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
+                if (idx < n) {
+                    fresh = true;
+                    if (load(idx, r) && node_count) {
+                        trav_init(r, st, hit);
+                        has = true;
+                    } else {
+                        hit.prim = kMiss; hit.t = r.tmax; hit.u = 0.0f; hit.v = 0.0f;
+                    }
+                }
+            }
+            store(idx, hit, fresh && !has);   // items without a ray (or an empty scene) finish at once
+        }
+        if (exhausted && __ballot_sync(0xFFFFFFFFu, has) == 0u) break;
+        bool done = false;
+        if (has) {
+            done = trav_step<ANY, COUNT>(nodes, tris, r, st, hit, stack, stride, spill, cnt, err);
+            if (done) {
+                trav_finish<REFINE>(nodes, tris, r, st, hit);
+                has = false;
+            }
+        }
+        store(idx, hit, done);
     }
     return err;
 }

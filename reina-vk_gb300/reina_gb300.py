@@ -81,6 +81,10 @@ class _CtxOptions(C.Structure):
     _fields_ = [("device", C.c_int32), ("flags", C.c_uint32)]
 
 
+class _Tuning(C.Structure):
+    _fields_ = [("refill", C.c_uint32), ("reserved", C.c_uint32 * 3)]
+
+
 class RtPushConsts(C.Structure):
     """polyglot/raytrace.h:43-54 (160 bytes; matrices column-major)."""
     _fields_ = [("invView", C.c_float * 16), ("invProjection", C.c_float * 16), ("sampleBatch", C.c_uint32),
@@ -206,6 +210,8 @@ def load_library() -> C.CDLL:
         "reina_ctx_create": (I32, [C.POINTER(_CtxOptions), C.POINTER(P)]),
         "reina_ctx_destroy": (None, [P]),
         "reina_ctx_sm_count": (I32, [P]),
+        "reina_ctx_set_tuning": (I32, [P, C.POINTER(_Tuning)]),
+        "reina_ctx_get_tuning": (I32, [P, C.POINTER(_Tuning)]),
         "reina_scene_create": (I32, [P, C.POINTER(P)]),
         "reina_scene_destroy": (None, [P]),
         "reina_scene_define_object": (I32, [P, C.POINTER(_ModelData), C.POINTER(U32)]),
@@ -280,6 +286,18 @@ class Context:
     @property
     def sm_count(self) -> int:
         return int(_lib.reina_ctx_sm_count(self._h))
+
+    @property
+    def refill(self) -> int:
+        t = _Tuning()
+        _check(_lib.reina_ctx_get_tuning(self._h, C.byref(t)))
+        return int(t.refill)
+
+    @refill.setter
+    def refill(self, value: int) -> None:
+        t = _Tuning()
+        t.refill = int(value)
+        _check(_lib.reina_ctx_set_tuning(self._h, C.byref(t)))
 
     def close(self) -> None:
         if self._h:
