@@ -64,13 +64,23 @@ void reina_ctx_destroy(reina_ctx* ctx);
 /* Number of streaming multiprocessors of the context's GPU (0 if unknown). */
 int reina_ctx_sm_count(const reina_ctx* ctx);
 
-/* Launch parameters of the traversal kernels (no counterpart in the reference, whose traversal is the
- * driver's).  refill = 0: one thread per ray (grid form, the default); refill = 1..32: persistent warps
- * that fetch new rays when `refill` of their 32 lanes are idle. */
+/* Launch parameters of the traversal kernels and of batched renders (no counterpart in the reference,
+ * whose traversal and scheduling are the driver's).
+ *   refill = 0: one thread per ray (grid form, the default); refill = 1..32: persistent warps that fetch
+ *            new rays when `refill` of their 32 lanes are idle.
+ *   wave_paths: path slots of one wave of a batched render (0 = REINA_DEFAULT_WAVE_PATHS); the path
+ *            state costs 164 bytes per slot.
+ *   batch_flags: REINA_BATCH_NO_GRAPHS launches each wave's kernels one by one instead of replaying a
+ *            captured CUDA graph.
+ * Changing wave_paths or batch_flags releases the batch engine; the next batched call rebuilds it. */
 typedef struct reina_tuning {
     uint32_t refill;
-    uint32_t reserved[3];
+    uint32_t wave_paths;
+    uint32_t batch_flags;
+    uint32_t reserved;
 } reina_tuning;
+enum { REINA_DEFAULT_WAVE_PATHS = 2097152 };
+enum { REINA_BATCH_NO_GRAPHS = 1 };
 int reina_ctx_set_tuning(reina_ctx* ctx, const reina_tuning* tuning);
 int reina_ctx_get_tuning(const reina_ctx* ctx, reina_tuning* out_tuning);
 
@@ -278,6 +288,27 @@ enum { REINA_NOALLOC_MAX_PIXELS = 65536 };
 int reina_render_device_noalloc(reina_ctx* ctx, const reina_scene* scene, const RtPushConsts* push_consts,
                                 const reina_render_options* options, void* d_accum_rgba32f, void* d_samples_rgb32f,
                                 void* stream);
+
+/* Batched renders.  No counterpart in the reference, which renders one scene per vkCmdTraceRaysKHR:
+ * here many frames — different scenes, resolutions, sample counts, depths and modes — are traced
+ * together in shared waves of `wave_paths` path slots, each wave a replayed CUDA graph of the wavefront
+ * kernels.  Every job gives the same image (and per-sample colours) as reina_render_device on its own:
+ * a job's samples of one pixel are traced and summed in sample order, whatever else shares the waves.
+ * options.flags must be 0. */
+typedef struct reina_render_job {
+    const reina_scene* scene;    /* built scene of this context */
+    RtPushConsts push_consts;
+    reina_render_options options;
+    void* accum_rgba32f;         /* width*height RGBA32F: read when sampleBatch > 0, then written */
+    void* samples_rgb32f;        /* optional width*height*spp*3 floats */
+} reina_render_job;
+
+/* Host buffers: copies the images in and out; blocks until every job is done. */
+int reina_render_batch(reina_ctx* ctx, const reina_render_job* jobs, uint32_t count, reina_render_stats* stats);
+/* Device buffers (16-byte aligned accumulation images); runs the waves on `stream` and returns when the
+ * last one has finished. */
+int reina_render_batch_device(reina_ctx* ctx, const reina_render_job* jobs, uint32_t count, void* stream,
+                              reina_render_stats* stats);
 
 /* ------------------------------------------------------------------------------------------------ */
 /* Post-process — replaces Reina::applyBloom + Reina::applyTonemapping (src/Reina.cpp:472-577):        */

@@ -1,0 +1,514 @@
+// Multi-job wavefront engine.  A wave is a set of path slots, each one (job, pixel, sample); it runs the
+// same kernel sequence as the single-frame wavefront (init, extend, per-material shade, shadow, finish),
+// with every kernel reading its path's job record for the scene, camera and integrator options.  A job
+// contributes at most one sample per pixel to a wave and its samples are scheduled in order, so each
+// pixel's samples are summed in sample order: a job's image does not depend on the jobs it shares waves
+// with.  The per-wave launch sequence is captured once per (bounces, NEE) into a CUDA
+// graph and replayed; only the wave descriptor (segments + job table) is copied in before each wave.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+
+#include "batch.h"
+#include "trace_device.cuh"
+#include "wavefront_device.cuh"
+
+namespace rt {
+
+struct BatchPaths {
+    PathState ps;      // per-slot path state and queues (its per-pixel arrays are unused here)
+    uint32_t* job;     // per slot: index into the wave's job table
+    uint32_t* pix;     // per slot: pixel within its job
+    uint32_t* smp;     // per slot: sample index
+    uint32_t* depth;   // per slot: segments traced
+};
+
+struct BatchLaunch {
+    BatchPaths bp;
+    const WaveHeader* hdr;
+    const WaveSeg* segs;
+    const JobGpu* jobs;
+    uint32_t P;
+};
+
+// Sets up slot i (job, pixel, sample, camera ray — raytrace.rgen.glsl:250-263); returns whether its job
+// traces any segment (paths of jobs with maxBounces = 0 finish with zero radiance).
+__device__ __forceinline__ bool init_slot(const BatchLaunch& B, uint32_t i) {
+    const PathState& ps = B.bp.ps;
+    int lo = 0, hi = (int)B.hdr->nseg - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) / 2;
+        if (B.segs[mid].wave_start <= i) lo = mid;
+        else hi = mid - 1;
+    }
+    const WaveSeg sg = B.segs[lo];
+    const JobGpu& J = B.jobs[sg.job];
+    const uint32_t pixel = sg.pixel_start + (i - sg.wave_start);
+    const uint32_t k = sg.sample;
+    const uint32_t x = pixel % J.W, y = pixel / J.W;
+    uint32_t rng;
+    float acc;
+    if (J.mode == kModeNeeMis) {
+        rng = path_seed(pixel, J.pc.sampleBatch * J.spp + k, J.seed);
+        acc = 0.0f;
+    } else if (k == 0) {
+        rng = (J.pc.sampleBatch * J.H + y) * J.W + x;
+        acc = 0.0f;
+    } else {
+        rng = J.pix_rng[pixel];
+        acc = J.pix_acc[pixel];
+    }
+    if (k == 0) {
+        J.sr[pixel] = 0.0f; J.sg[pixel] = 0.0f; J.sb[pixel] = 0.0f;
+        J.cnt[pixel] = 0;
+    }
+    V3 o, d;
+    camera_ray(J.pc, J.W, J.H, x, y, rng, o, d);
+    store_ray(ps, i, o, d);
+    store_thr(ps, i, V3{1.0f, 1.0f, 1.0f});
+    store_rad(ps, i, V3{0.0f, 0.0f, 0.0f});
+    ps.rng[i] = rng;
+    ps.acc[i] = acc;
+    ps.flags[i] = 0u;
+    ps.ppdf[i] = 0.0f;
+    B.bp.job[i] = sg.job;
+    B.bp.pix[i] = pixel;
+    B.bp.smp[i] = k;
+    B.bp.depth[i] = 0;
+    return J.max_bounces > 0;
+}
+
+// The active-path counter is zero at launch (cleared with the other counters before the wave).
+__global__ void __launch_bounds__(kBlock) kb_init(BatchLaunch B) {
+    const PathState& ps = B.bp.ps;
+    const uint32_t n = B.hdr->count;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const uint32_t i = base + threadIdx.x;
+        const bool live = i < n && init_slot(B, i);
+        const uint32_t pos = warp_append(ps.counters + kCntActive, live);
+        if (live) ps.q_active[0][pos] = i;
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) kb_extend(BatchLaunch B, int cur) {
+    __shared__ uint2 stack[kSmemStack * kBlock];
+    const PathState& ps = B.bp.ps;
+    const uint32_t n = ps.counters[kCntActive + cur];
+    const uint32_t* q = ps.q_active[cur];
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const uint32_t i = base + threadIdx.x;
+        const bool active = i < n;
+        int m = -1;
+        uint32_t p = 0;
+        if (active) {
+            p = q[i];
+            const DeviceScene& s = B.jobs[B.bp.job[p]].s;
+            const TraceRay r = make_trace_ray(ps.ox[p], ps.oy[p], ps.oz[p], ps.dx[p], ps.dy[p], ps.dz[p], 0.0f, 10000.0f);
+            Hit h;
+            TraceCounters c{0u, 0u};
+            uint32_t e = 0;
+            if (s.node_count) e = traverse<false, false, true>(s.nodes, s.tris, r, stack + threadIdx.x, kBlock, h, c);
+            else h.prim = kMiss;
+            if (e) atomicOr(ps.counters + kCntError, e);
+            ps.hprim[p] = h.prim;
+            ps.hu[p] = h.u;
+            ps.hv[p] = h.v;
+            m = h.prim == kMiss ? kQueueMiss : 1 + (int)s.props_material[s.prim_props[h.prim]];
+        }
+        warp_count64(reinterpret_cast<unsigned long long*>(ps.counters + kCntRays), active);
+#pragma unroll
+        for (int k = 0; k < kNumQueues; ++k) {
+            const bool mine = active && m == k;
+            const uint32_t pos = warp_append(ps.counters + kCntQueue + k, mine);
+            if (mine) ps.q_shade[(size_t)k * B.P + pos] = p;
+        }
+    }
+}
+
+template <int MAT>
+__global__ void __launch_bounds__(kBlock) kb_shade(BatchLaunch B, int cur) {
+    const PathState& ps = B.bp.ps;
+    const uint32_t n = ps.counters[kCntQueue + MAT];
+    const uint32_t* q = ps.q_shade + (size_t)MAT * B.P;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const uint32_t i = base + threadIdx.x;
+        const bool active = i < n;
+        bool emit = false, cont = false;
+        ShadowRec sh;
+        uint32_t p = 0;
+        if (active) {
+            p = q[i];
+            const JobGpu& J = B.jobs[B.bp.job[p]];
+            const bool nee = J.mode == kModeNeeMis;
+            const V3 ro{ps.ox[p], ps.oy[p], ps.oz[p]};
+            const V3 rd{ps.dx[p], ps.dy[p], ps.dz[p]};
+            const uint32_t prim = ps.hprim[p];
+            const HitInfo h = hit_info(J.s, prim, ps.hu[p], ps.hv[p], rd);
+            const InstanceProperties& pr = J.s.props[h.props];
+            uint32_t rng = ps.rng[p];
+            uint32_t flags = ps.flags[p];
+            float acc = ps.acc[p];
+            const bool inside = (flags & kFlagInside) != 0;
+            Vertex vx;
+            if (MAT == 1) vx = shade_lambert(h, pr, rd, rng, inside, acc);
+            else if (MAT == 2) vx = shade_metal(h, pr, rd, rng, inside, acc);
+            else if (MAT == 3) vx = shade_dielectric(h, pr, ro, rd, rng, inside, acc);
+            else vx = shade_disney(h, pr, ro, rd, rng, inside, acc);
+            if (vx.skip) {
+                flags &= ~kFlagPrevNee;
+            } else {
+                flags = vx.inside ? (flags | kFlagInside) : (flags & ~kFlagInside);
+                if (!vx.inside) {
+                    V3 thr = load_thr(ps, p), rad = load_rad(ps, p);
+                    V3 contrib = vx.emission;
+                    if (nee) {
+                        const float tw = J.pc.totalEmissiveWeight;
+                        if ((flags & kFlagPrevNee) && (vx.emission.x != 0.0f || vx.emission.y != 0.0f || vx.emission.z != 0.0f))
+                            contrib = contrib * power_heuristic(ps.ppdf[p], light_pdf_sa(J.s, tw, prim, ro, vx.newO));
+                        const bool do_nee = (MAT == 1 || MAT == 4) && J.s.emissive_count > 0;
+                        if (do_nee) emit = next_event(J.s, tw, rng, MAT == 4, vx.newO, h.n, vx.albedo, pr, h.tbn, rd, thr, sh);
+                        flags = do_nee ? (flags | kFlagPrevNee) : (flags & ~kFlagPrevNee);
+                        ps.ppdf[p] = vx.pdf;
+                    }
+                    rad = rad + contrib * thr;
+                    thr = thr * vx.color;
+                    store_thr(ps, p, thr);
+                    store_rad(ps, p, rad);
+                } else {
+                    flags &= ~kFlagPrevNee;
+                }
+            }
+            store_ray(ps, p, vx.newO, vx.newD);
+            ps.rng[p] = rng;
+            ps.flags[p] = flags;
+            ps.acc[p] = acc;
+            const uint32_t dep = B.bp.depth[p] + 1;
+            B.bp.depth[p] = dep;
+            cont = dep < J.max_bounces;
+        }
+        const uint32_t pos = warp_append(ps.counters + kCntActive + (cur ^ 1), cont);
+        if (cont) ps.q_active[cur ^ 1][pos] = p;
+        const uint32_t spos = warp_append(ps.counters + kCntShadow, emit);
+        if (emit) {
+            ps.q_shadow[spos] = p;
+            ps.s_ox[spos] = sh.o.x; ps.s_oy[spos] = sh.o.y; ps.s_oz[spos] = sh.o.z;
+            ps.s_dx[spos] = sh.d.x; ps.s_dy[spos] = sh.d.y; ps.s_dz[spos] = sh.d.z;
+            ps.s_tmax[spos] = sh.tmax;
+            ps.s_cr[spos] = sh.contrib.x; ps.s_cg[spos] = sh.contrib.y; ps.s_cb[spos] = sh.contrib.z;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) kb_shade_miss(BatchLaunch B) {
+    const PathState& ps = B.bp.ps;
+    const uint32_t n = ps.counters[kCntQueue + kQueueMiss];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t p = ps.q_shade[i];
+        const JobGpu& J = B.jobs[B.bp.job[p]];
+        V3 sky;
+        if (J.env_mode == 1) {
+            sky = V3{J.env[0], J.env[1], J.env[2]};
+        } else {
+            const float y = norm3(V3{ps.dx[p], ps.dy[p], ps.dz[p]}).y;
+            const float t = 0.5f * (y + 1.0f);
+            sky = mix3(V3{0.1f, 0.1f, 0.1f}, V3{0.4f, 1.7f, 2.0f}, t) * 0.07f;
+        }
+        store_rad(ps, p, load_rad(ps, p) + sky * load_thr(ps, p));
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) kb_shadow(BatchLaunch B) {
+    __shared__ uint2 stack[kSmemStack * kBlock];
+    const PathState& ps = B.bp.ps;
+    const uint32_t n = ps.counters[kCntShadow];
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const uint32_t i = base + threadIdx.x;
+        const bool active = i < n;
+        if (active) {
+            const uint32_t p = ps.q_shadow[i];
+            const DeviceScene& s = B.jobs[B.bp.job[p]].s;
+            const TraceRay r = make_trace_ray(ps.s_ox[i], ps.s_oy[i], ps.s_oz[i], ps.s_dx[i], ps.s_dy[i], ps.s_dz[i], 0.0f,
+                                              ps.s_tmax[i]);
+            Hit h;
+            TraceCounters c{0u, 0u};
+            uint32_t e = 0;
+            if (s.node_count) e = traverse<true, false, false>(s.nodes, s.tris, r, stack + threadIdx.x, kBlock, h, c);
+            else h.prim = kMiss;
+            if (e) atomicOr(ps.counters + kCntError, e);
+            if (h.prim == kMiss) store_rad(ps, p, load_rad(ps, p) + V3{ps.s_cr[i], ps.s_cg[i], ps.s_cb[i]});
+        }
+        warp_count64(reinterpret_cast<unsigned long long*>(ps.counters + kCntShadowRays), active);
+    }
+}
+
+// raytrace.rgen.glsl:264-275 per slot: clamp (NaN kept), sample output, NaN drop, sum; carry the
+// RNG state and accumulatedDistance to the pixel's next sample.
+__global__ void __launch_bounds__(kBlock) kb_finish(BatchLaunch B) {
+    const PathState& ps = B.bp.ps;
+    const uint32_t n = B.hdr->count;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const JobGpu& J = B.jobs[B.bp.job[i]];
+        const uint32_t pixel = B.bp.pix[i];
+        const V3 c = clamp_keep_nan(load_rad(ps, i), J.pc.directClamp);
+        if (J.samples) {
+            float* o = J.samples + 3ull * ((uint64_t)pixel * J.spp + B.bp.smp[i]);
+            o[0] = c.x; o[1] = c.y; o[2] = c.z;
+        }
+        if (!has_nan3(c)) {
+            J.sr[pixel] += c.x;
+            J.sg[pixel] += c.y;
+            J.sb[pixel] += c.z;
+            J.cnt[pixel] += 1;
+        }
+        J.pix_rng[pixel] = ps.rng[i];
+        J.pix_acc[pixel] = ps.acc[i];
+    }
+}
+
+// raytrace.rgen.glsl:277-284 for one finished job.
+__global__ void __launch_bounds__(kBlock) kb_resolve(JobGpu J) {
+    const uint32_t n = J.W * J.H;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float k = (float)J.cnt[i];
+        V3 fin{J.sr[i] / k, J.sg[i] / k, J.sb[i] / k};
+        float4* a = reinterpret_cast<float4*>(J.accum) + i;
+        if (J.pc.sampleBatch > 0) {
+            const float4 prev = *a;
+            fin = div3(V3{prev.x, prev.y, prev.z} * (float)J.pc.sampleBatch + fin, (float)(J.pc.sampleBatch + 1));
+        }
+        *a = make_float4(fin.x, fin.y, fin.z, 1.0f);
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// Host side
+constexpr size_t kBatchWordsPerPath = 19 + 8 + 10 + 4;   // path state, queues, shadow records, job/pix/smp/depth
+constexpr uint32_t kMaxWaveJobs = kMaxWaveSegments / 2;
+
+static BatchPaths layout_batch(uint32_t* w, size_t P) {
+    size_t off = 64;   // 16 counters, padded to 256 bytes
+    auto f = [&]() { float* r = reinterpret_cast<float*>(w + off); off += P; return r; };
+    auto u = [&]() { uint32_t* r = w + off; off += P; return r; };
+    BatchPaths b;
+    PathState& s = b.ps;
+    std::memset(&s, 0, sizeof(s));
+    s.counters = w;
+    s.ox = f(); s.oy = f(); s.oz = f(); s.dx = f(); s.dy = f(); s.dz = f();
+    s.hprim = u(); s.hu = f(); s.hv = f();
+    s.tr = f(); s.tg = f(); s.tb = f();
+    s.rr = f(); s.rg = f(); s.rb = f();
+    s.rng = u(); s.flags = u(); s.acc = f(); s.ppdf = f();
+    s.q_active[0] = u(); s.q_active[1] = u();
+    s.q_shade = w + off; off += P * kNumQueues;
+    s.q_shadow = u();
+    s.s_ox = f(); s.s_oy = f(); s.s_oz = f(); s.s_dx = f(); s.s_dy = f(); s.s_dz = f(); s.s_tmax = f();
+    s.s_cr = f(); s.s_cg = f(); s.s_cb = f();
+    b.job = u(); b.pix = u(); b.smp = u(); b.depth = u();
+    return b;
+}
+
+static int occupancy(const void* fn, int sm_count) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kBlock, 0);
+    return std::max(1, per_sm) * std::max(1, sm_count);
+}
+
+BatchEngine::BatchEngine(int device, int sm_count, uint32_t wave_capacity, bool use_graphs)
+    : device_(device), sm_count_(sm_count), capacity_(wave_capacity), use_graphs_(use_graphs) {
+    if (wave_capacity == 0) fail(REINA_ERR_INVALID, "wave capacity must be positive");
+    paths_.alloc((64 + kBatchWordsPerPath * (size_t)capacity_) * 4);
+    desc_bytes_ = sizeof(WaveHeader) + kMaxWaveSegments * sizeof(WaveSeg) + kMaxWaveJobs * sizeof(JobGpu);
+    desc_.alloc(desc_bytes_);
+    check_cuda(cudaMallocHost(&host_desc_, desc_bytes_), "cudaMallocHost");
+    blocks_ext_ = occupancy((const void*)kb_extend, sm_count);
+    blocks_sh_ = occupancy((const void*)kb_shadow, sm_count);
+    blocks_shade_[1] = occupancy((const void*)kb_shade<1>, sm_count);
+    blocks_shade_[2] = occupancy((const void*)kb_shade<2>, sm_count);
+    blocks_shade_[3] = occupancy((const void*)kb_shade<3>, sm_count);
+    blocks_shade_[4] = occupancy((const void*)kb_shade<4>, sm_count);
+    blocks_simple_ = occupancy((const void*)kb_finish, sm_count);
+}
+
+BatchEngine::~BatchEngine() {
+    for (auto& g : graphs_)
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+    if (host_desc_) cudaFreeHost(host_desc_);
+}
+
+void BatchEngine::prepare(BatchJob& job) {
+    const size_t px = (size_t)job.opt.width * job.opt.height;
+    job.total = (uint64_t)job.pc.samplesPerPixel * px;
+    job.cursor = 0;
+    job.resolved = false;
+    job.pixel_state.alloc(px * 6 * sizeof(uint32_t));
+}
+
+static JobGpu job_record(const BatchJob& j) {
+    JobGpu g;
+    std::memset(&g, 0, sizeof(g));
+    g.s = j.scene;
+    g.pc = j.pc;
+    g.W = j.opt.width;
+    g.H = j.opt.height;
+    g.mode = j.opt.mode;
+    g.seed = j.opt.seed;
+    g.env_mode = j.opt.env_mode;
+    for (int k = 0; k < 3; ++k) g.env[k] = j.opt.env_color[k];
+    g.spp = j.pc.samplesPerPixel;
+    g.max_bounces = j.pc.maxBounces;
+    g.accum = j.d_accum;
+    g.samples = j.d_samples;
+    const size_t px = (size_t)g.W * g.H;
+    uint32_t* w = j.pixel_state.as<uint32_t>();
+    g.pix_rng = w;
+    g.pix_acc = reinterpret_cast<float*>(w + px);
+    g.sr = reinterpret_cast<float*>(w + 2 * px);
+    g.sg = reinterpret_cast<float*>(w + 3 * px);
+    g.sb = reinterpret_cast<float*>(w + 4 * px);
+    g.cnt = w + 5 * px;
+    return g;
+}
+
+void BatchEngine::launch_wave(const WaveHeader& h, bool any_nee, cudaStream_t st) {
+    uint8_t* d = desc_.as<uint8_t>();
+    BatchLaunch B;
+    B.bp = layout_batch(paths_.as<uint32_t>(), capacity_);
+    B.hdr = reinterpret_cast<const WaveHeader*>(d);
+    B.segs = reinterpret_cast<const WaveSeg*>(d + sizeof(WaveHeader));
+    B.jobs = reinterpret_cast<const JobGpu*>(d + sizeof(WaveHeader) + kMaxWaveSegments * sizeof(WaveSeg));
+    B.P = capacity_;
+    uint32_t* cnt = B.bp.ps.counters;
+    const int simple = std::min<int>(blocks_simple_, (int)((capacity_ + kBlock - 1) / kBlock));
+    auto sequence = [&](cudaStream_t s) {
+        check_cuda(cudaMemsetAsync(cnt, 0, kNumCounters * sizeof(uint32_t), s), "cudaMemsetAsync");
+        kb_init<<<simple, kBlock, 0, s>>>(B);
+        int cur = 0;
+        for (uint32_t seg = 0; seg < h.max_bounces; ++seg) {
+            check_cuda(cudaMemsetAsync(cnt + kCntActive + (cur ^ 1), 0, sizeof(uint32_t), s), "cudaMemsetAsync");
+            check_cuda(cudaMemsetAsync(cnt + kCntQueue, 0, 6 * sizeof(uint32_t), s), "cudaMemsetAsync");
+            kb_extend<<<blocks_ext_, kBlock, 0, s>>>(B, cur);
+            kb_shade_miss<<<simple, kBlock, 0, s>>>(B);
+            kb_shade<1><<<blocks_shade_[1], kBlock, 0, s>>>(B, cur);
+            kb_shade<2><<<blocks_shade_[2], kBlock, 0, s>>>(B, cur);
+            kb_shade<3><<<blocks_shade_[3], kBlock, 0, s>>>(B, cur);
+            kb_shade<4><<<blocks_shade_[4], kBlock, 0, s>>>(B, cur);
+            if (any_nee) kb_shadow<<<blocks_sh_, kBlock, 0, s>>>(B);
+            cur ^= 1;
+        }
+        kb_finish<<<simple, kBlock, 0, s>>>(B);
+    };
+    if (!use_graphs_) {
+        sequence(st);
+        check_cuda(cudaGetLastError(), "batch wave launch");
+        return;
+    }
+    GraphSlot* slot = nullptr;
+    for (auto& g : graphs_)
+        if (g.bounces == h.max_bounces && g.nee == any_nee) slot = &g;
+    if (!slot) {
+        cudaStream_t cap;
+        check_cuda(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking), "cudaStreamCreate");
+        cudaGraph_t graph;
+        check_cuda(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+        sequence(cap);
+        check_cuda(cudaStreamEndCapture(cap, &graph), "cudaStreamEndCapture");
+        cudaStreamDestroy(cap);
+        GraphSlot g;
+        g.bounces = h.max_bounces;
+        g.nee = any_nee;
+        check_cuda(cudaGraphInstantiate(&g.exec, graph, 0), "cudaGraphInstantiate");
+        cudaGraphDestroy(graph);
+        graphs_.push_back(g);
+        slot = &graphs_.back();
+    }
+    check_cuda(cudaGraphLaunch(slot->exec, st), "cudaGraphLaunch");
+}
+
+uint64_t BatchEngine::run_wave(const std::vector<BatchJob*>& jobs, cudaStream_t st) {
+    // active jobs (at most kMaxWaveJobs per wave; the rest wait for a later wave)
+    std::vector<BatchJob*> active;
+    for (BatchJob* j : jobs)
+        if (j->cursor < j->total && active.size() < kMaxWaveJobs) active.push_back(j);
+    if (active.empty()) return 0;
+    // fair share of the capacity, then leftovers to the oldest jobs
+    std::vector<uint64_t> take(active.size(), 0);
+    const uint64_t fair = std::max<uint64_t>(1, capacity_ / active.size());
+    uint64_t used = 0;
+    for (size_t a = 0; a < active.size(); ++a) {
+        const BatchJob* j = active[a];
+        const uint64_t px = (uint64_t)j->opt.width * j->opt.height;
+        take[a] = std::min({fair, px, j->total - j->cursor, (uint64_t)capacity_ - used});
+        used += take[a];
+    }
+    for (size_t a = 0; a < active.size() && used < capacity_; ++a) {
+        const BatchJob* j = active[a];
+        const uint64_t px = (uint64_t)j->opt.width * j->opt.height;
+        const uint64_t more = std::min(std::min(px, j->total - j->cursor) - take[a], (uint64_t)capacity_ - used);
+        take[a] += more;
+        used += more;
+    }
+    uint8_t* h = static_cast<uint8_t*>(host_desc_);
+    WaveHeader* hdr = reinterpret_cast<WaveHeader*>(h);
+    WaveSeg* segs = reinterpret_cast<WaveSeg*>(h + sizeof(WaveHeader));
+    JobGpu* jt = reinterpret_cast<JobGpu*>(h + sizeof(WaveHeader) + kMaxWaveSegments * sizeof(WaveSeg));
+    uint32_t nseg = 0, njobs = 0, wave_pos = 0, bounces = 0;
+    bool any_nee = false;
+    for (size_t a = 0; a < active.size(); ++a) {
+        if (take[a] == 0) continue;
+        BatchJob* j = active[a];
+        const uint64_t px = (uint64_t)j->opt.width * j->opt.height;
+        const uint32_t ji = njobs++;
+        jt[ji] = job_record(*j);
+        bounces = std::max(bounces, j->pc.maxBounces);
+        any_nee = any_nee || j->opt.mode == kModeNeeMis;
+        uint64_t m = take[a];
+        while (m > 0) {
+            const uint64_t sample = j->cursor / px, pixel = j->cursor % px;
+            const uint64_t c = std::min(m, px - pixel);
+            WaveSeg& s = segs[nseg++];
+            s.job = ji;
+            s.wave_start = wave_pos;
+            s.pixel_start = (uint32_t)pixel;
+            s.count = (uint32_t)c;
+            s.sample = (uint32_t)sample;
+            wave_pos += (uint32_t)c;
+            j->cursor += c;
+            m -= c;
+        }
+    }
+    hdr->count = wave_pos;
+    hdr->nseg = nseg;
+    hdr->njobs = njobs;
+    hdr->max_bounces = bounces;
+    uint8_t* d = desc_.as<uint8_t>();
+    check_cuda(cudaMemcpyAsync(d, h, sizeof(WaveHeader) + nseg * sizeof(WaveSeg), cudaMemcpyHostToDevice, st), "H2D wave");
+    const size_t job_off = sizeof(WaveHeader) + kMaxWaveSegments * sizeof(WaveSeg);
+    check_cuda(cudaMemcpyAsync(d + job_off, h + job_off, njobs * sizeof(JobGpu), cudaMemcpyHostToDevice, st), "H2D jobs");
+    launch_wave(*hdr, any_nee, st);
+    // resolve the jobs this wave completed
+    for (size_t a = 0; a < active.size(); ++a) {
+        BatchJob* j = active[a];
+        if (j->cursor == j->total && !j->resolved) {
+            const JobGpu g = job_record(*j);
+            const uint32_t px = g.W * g.H;
+            const int blocks = (int)std::min<uint32_t>((px + kBlock - 1) / kBlock, (uint32_t)blocks_simple_);
+            kb_resolve<<<blocks, kBlock, 0, st>>>(g);
+            j->resolved = true;
+        }
+    }
+    check_cuda(cudaGetLastError(), "batch launch");
+    uint32_t c[kNumCounters];
+    check_cuda(cudaMemcpyAsync(c, paths_.get(), sizeof(c), cudaMemcpyDeviceToHost, st), "D2H counters");
+    check_cuda(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+    uint64_t r, sr;
+    std::memcpy(&r, c + kCntRays, 8);
+    std::memcpy(&sr, c + kCntShadowRays, 8);
+    rays_ += r;
+    shadow_rays_ += sr;
+    waves_++;
+    if (c[kCntError]) fail(REINA_ERR_DEVICE, "batch wave kernels raised error flag " + std::to_string(c[kCntError]));
+    return wave_pos;
+}
+
+}  // namespace rt

@@ -3,13 +3,16 @@
 #include <chrono>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <new>
 #include <string>
+#include <unordered_set>
 #include <vector>
 
 #include <cuda_runtime_api.h>
 
 #include "../../include/reina/reina_c.h"
+#include "batch.h"
 #include "errors.h"
 #include "generators.h"
 #include "kernels.h"
@@ -36,6 +39,11 @@ struct reina_ctx {
     rt::DeviceBuffer accum, samples;   // staging for host-buffer renders
     rt::PostWorkspace post;      // bloom intermediate images
     rt::DeviceBuffer rgba8, combined;  // staging for host-buffer post-processing
+    uint32_t wave_paths = REINA_DEFAULT_WAVE_PATHS;
+    uint32_t batch_flags = 0;
+    std::unique_ptr<rt::BatchEngine> batch;   // built on the first batched render
+    std::mutex scenes_mu;
+    std::unordered_set<reina_scene*> scenes;  // live scenes; detached (device memory freed) on destroy
 };
 
 struct reina_scene {
@@ -77,7 +85,8 @@ void use_device(const reina_ctx* ctx) {
 }
 
 const rt::Scene& built_scene(const reina_scene* scene) {
-    need(scene && scene->s, "scene is NULL");
+    need(scene != nullptr, "scene is NULL");
+    if (!scene->ctx) fail(REINA_ERR_STATE, "the scene's context has been destroyed");
     if (!scene->s->built()) fail(REINA_ERR_STATE, "scene is not built (call reina_scene_build)");
     return *scene->s;
 }
@@ -146,6 +155,15 @@ int reina_ctx_create(const reina_ctx_options* options, reina_ctx** out_ctx) {
 void reina_ctx_destroy(reina_ctx* ctx) {
     if (!ctx) return;
     if (ctx->device >= 0) cudaSetDevice(ctx->device);
+    {
+        // scenes outliving their context keep only their handle: free their device memory now
+        std::lock_guard<std::mutex> lock(ctx->scenes_mu);
+        for (reina_scene* sc : ctx->scenes) {
+            sc->s.reset();
+            sc->ctx = nullptr;
+        }
+        ctx->scenes.clear();
+    }
     for (auto& s : ctx->streams)
         if (s) cudaStreamDestroy(s);
     delete ctx;
@@ -157,7 +175,16 @@ int reina_ctx_set_tuning(reina_ctx* ctx, const reina_tuning* t) {
     return guard([&] {
         need(ctx && t, "NULL argument");
         need(t->refill <= 32, "refill must be in 0..32");
+        need((t->batch_flags & ~(uint32_t)REINA_BATCH_NO_GRAPHS) == 0, "unknown batch flags");
+        const uint32_t wave = t->wave_paths ? t->wave_paths : (uint32_t)REINA_DEFAULT_WAVE_PATHS;
+        need(wave <= (1u << 26), "wave_paths must be at most 2^26");
         ctx->refill = (int)t->refill;
+        if (wave != ctx->wave_paths || t->batch_flags != ctx->batch_flags) {
+            if (ctx->batch && ctx->device >= 0) check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
+            ctx->batch.reset();
+            ctx->wave_paths = wave;
+            ctx->batch_flags = t->batch_flags;
+        }
     });
 }
 
@@ -166,6 +193,8 @@ int reina_ctx_get_tuning(const reina_ctx* ctx, reina_tuning* out) {
         need(ctx && out, "NULL argument");
         std::memset(out, 0, sizeof(*out));
         out->refill = (uint32_t)ctx->refill;
+        out->wave_paths = ctx->wave_paths;
+        out->batch_flags = ctx->batch_flags;
     });
 }
 
@@ -175,13 +204,21 @@ int reina_scene_create(reina_ctx* ctx, reina_scene** out_scene) {
         auto s = std::make_unique<reina_scene>();
         s->ctx = ctx;
         s->s = std::make_unique<rt::Scene>(ctx->device);
+        std::lock_guard<std::mutex> lock(ctx->scenes_mu);
+        ctx->scenes.insert(s.get());
         *out_scene = s.release();
     });
 }
 
 void reina_scene_destroy(reina_scene* scene) {
     if (!scene) return;
-    if (scene->ctx && scene->ctx->device >= 0) cudaSetDevice(scene->ctx->device);
+    if (reina_ctx* ctx = scene->ctx) {
+        {
+            std::lock_guard<std::mutex> lock(ctx->scenes_mu);
+            ctx->scenes.erase(scene);
+        }
+        if (ctx->device >= 0) cudaSetDevice(ctx->device);
+    }
     delete scene;
 }
 
@@ -410,6 +447,90 @@ int reina_render(reina_ctx* ctx, const reina_scene* scene, const RtPushConsts* p
             stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         }
     });
+}
+
+static rt::BatchEngine& batch_engine(reina_ctx* ctx) {
+    if (!ctx->batch)
+        ctx->batch = std::make_unique<rt::BatchEngine>(ctx->device, ctx->sm_count, ctx->wave_paths,
+                                                       (ctx->batch_flags & REINA_BATCH_NO_GRAPHS) == 0);
+    return *ctx->batch;
+}
+
+// Validates every job, then runs waves until all are resolved.  `host`: the job buffers are host memory
+// and are staged through per-job device copies.
+static void render_batch(reina_ctx* ctx, const reina_render_job* jobs, uint32_t count, bool host, cudaStream_t st,
+                         reina_render_stats* stats) {
+    need(ctx != nullptr, "ctx is NULL");
+    need(count == 0 || jobs != nullptr, "jobs is NULL");
+    std::vector<rt::BatchJob> bj(count);
+    for (uint32_t k = 0; k < count; ++k) {
+        const reina_render_job& j = jobs[k];
+        const rt::Scene& s = built_scene(j.scene);
+        need(j.scene->ctx == ctx, "scene belongs to another context");
+        const rt::RenderOpts r = render_opts(&j.push_consts, &j.options);
+        need(!r.megakernel, "batched jobs run the wavefront (options.flags must be 0)");
+        check_render_scene(s, &j.push_consts, &j.options);
+        need(j.accum_rgba32f != nullptr, "accumulation buffer is NULL");
+        if (!host) need(((uintptr_t)j.accum_rgba32f % 16) == 0, "accumulation buffer must be 16-byte aligned");
+        bj[k].scene = s.device_view();
+        bj[k].pc = j.push_consts;
+        bj[k].opt = r;
+    }
+    use_device(ctx);
+    const auto t0 = std::chrono::steady_clock::now();
+    rt::BatchEngine& eng = batch_engine(ctx);
+    std::vector<rt::DeviceBuffer> acc(host ? count : 0), smp(host ? count : 0);
+    std::vector<rt::BatchJob*> ptrs(count);
+    for (uint32_t k = 0; k < count; ++k) {
+        const reina_render_job& j = jobs[k];
+        const size_t px = (size_t)j.options.width * j.options.height;
+        rt::BatchEngine::prepare(bj[k]);
+        if (host) {
+            acc[k].alloc(px * 4 * sizeof(float));
+            if (j.push_consts.sampleBatch > 0)
+                check_cuda(cudaMemcpyAsync(acc[k].get(), j.accum_rgba32f, px * 4 * sizeof(float), cudaMemcpyHostToDevice, st),
+                           "H2D accum");
+            bj[k].d_accum = acc[k].as<float>();
+            if (j.samples_rgb32f) {
+                smp[k].alloc(px * j.push_consts.samplesPerPixel * 3 * sizeof(float));
+                bj[k].d_samples = smp[k].as<float>();
+            }
+        } else {
+            bj[k].d_accum = static_cast<float*>(j.accum_rgba32f);
+            bj[k].d_samples = static_cast<float*>(j.samples_rgb32f);
+        }
+        ptrs[k] = &bj[k];
+    }
+    const uint64_t r0 = eng.rays(), s0 = eng.shadow_rays();
+    while (eng.run_wave(ptrs, st) > 0) {
+    }
+    if (host) {
+        for (uint32_t k = 0; k < count; ++k) {
+            const reina_render_job& j = jobs[k];
+            const size_t px = (size_t)j.options.width * j.options.height;
+            check_cuda(cudaMemcpyAsync(j.accum_rgba32f, acc[k].get(), px * 4 * sizeof(float), cudaMemcpyDeviceToHost, st),
+                       "D2H accum");
+            if (j.samples_rgb32f)
+                check_cuda(cudaMemcpyAsync(j.samples_rgb32f, smp[k].get(), px * j.push_consts.samplesPerPixel * 3 * sizeof(float),
+                                           cudaMemcpyDeviceToHost, st),
+                           "D2H samples");
+        }
+    }
+    check_cuda(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+    if (stats) {
+        stats->rays = eng.rays() - r0;
+        stats->shadow_rays = eng.shadow_rays() - s0;
+        stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    }
+}
+
+int reina_render_batch(reina_ctx* ctx, const reina_render_job* jobs, uint32_t count, reina_render_stats* stats) {
+    return guard([&] { render_batch(ctx, jobs, count, true, ctx ? ctx->streams[0] : nullptr, stats); });
+}
+
+int reina_render_batch_device(reina_ctx* ctx, const reina_render_job* jobs, uint32_t count, void* stream,
+                              reina_render_stats* stats) {
+    return guard([&] { render_batch(ctx, jobs, count, false, static_cast<cudaStream_t>(stream), stats); });
 }
 
 int reina_postprocess_device(reina_ctx* ctx, const void* d_accum, uint32_t width, uint32_t height,

@@ -82,7 +82,12 @@ class _CtxOptions(C.Structure):
 
 
 class _Tuning(C.Structure):
-    _fields_ = [("refill", C.c_uint32), ("reserved", C.c_uint32 * 3)]
+    _fields_ = [("refill", C.c_uint32), ("wave_paths", C.c_uint32), ("batch_flags", C.c_uint32),
+                ("reserved", C.c_uint32)]
+
+
+DEFAULT_WAVE_PATHS = 2097152
+BATCH_NO_GRAPHS = 1
 
 
 class RtPushConsts(C.Structure):
@@ -113,6 +118,11 @@ class TonemappingPushConsts(C.Structure):
 
 class _RenderStats(C.Structure):
     _fields_ = [("rays", C.c_uint64), ("shadow_rays", C.c_uint64), ("seconds", C.c_double)]
+
+
+class _RenderJob(C.Structure):
+    _fields_ = [("scene", C.c_void_p), ("push_consts", RtPushConsts), ("options", RenderOptions),
+                ("accum", C.c_void_p), ("samples", C.c_void_p)]
 
 
 MODE_REINA = 0
@@ -229,6 +239,8 @@ def load_library() -> C.CDLL:
         "reina_render": (I32, [P, P, C.POINTER(RtPushConsts), C.POINTER(RenderOptions), P, P, C.POINTER(_RenderStats)]),
         "reina_render_device": (I32, [P, P, C.POINTER(RtPushConsts), C.POINTER(RenderOptions), P, P, P]),
         "reina_render_device_noalloc": (I32, [P, P, C.POINTER(RtPushConsts), C.POINTER(RenderOptions), P, P, P]),
+        "reina_render_batch": (I32, [P, C.POINTER(_RenderJob), U32, C.POINTER(_RenderStats)]),
+        "reina_render_batch_device": (I32, [P, C.POINTER(_RenderJob), U32, P, C.POINTER(_RenderStats)]),
         "reina_postprocess": (I32, [P, P, U32, U32, C.POINTER(BloomPushConsts), C.POINTER(TonemappingPushConsts), P, P]),
         "reina_postprocess_device": (I32, [P, P, U32, U32, C.POINTER(BloomPushConsts),
                                            C.POINTER(TonemappingPushConsts), P, P, P]),
@@ -287,17 +299,28 @@ class Context:
     def sm_count(self) -> int:
         return int(_lib.reina_ctx_sm_count(self._h))
 
-    @property
-    def refill(self) -> int:
+    def tuning(self) -> dict:
         t = _Tuning()
         _check(_lib.reina_ctx_get_tuning(self._h, C.byref(t)))
-        return int(t.refill)
+        return {"refill": int(t.refill), "wave_paths": int(t.wave_paths), "batch_flags": int(t.batch_flags)}
+
+    def set_tuning(self, **kw) -> None:
+        """reina_ctx_set_tuning with the given fields changed (refill, wave_paths, batch_flags)."""
+        t = _Tuning()
+        _check(_lib.reina_ctx_get_tuning(self._h, C.byref(t)))
+        for k, v in kw.items():
+            if k not in ("refill", "wave_paths", "batch_flags"):
+                raise TypeError(f"unknown tuning field {k}")
+            setattr(t, k, int(v))
+        _check(_lib.reina_ctx_set_tuning(self._h, C.byref(t)))
+
+    @property
+    def refill(self) -> int:
+        return self.tuning()["refill"]
 
     @refill.setter
     def refill(self, value: int) -> None:
-        t = _Tuning()
-        t.refill = int(value)
-        _check(_lib.reina_ctx_set_tuning(self._h, C.byref(t)))
+        self.set_tuning(refill=value)
 
     def close(self) -> None:
         if self._h:
@@ -471,6 +494,57 @@ def postprocess(ctx: Context, accum: np.ndarray, radius: float = 5.0, threshold:
     t = TonemappingPushConsts(exposure)
     _check(_lib.reina_postprocess(ctx.handle, _ptr(accum), W, H, C.byref(b), C.byref(t), _ptr(out), _ptr(comb)))
     return out, comb
+
+
+class RenderJob:
+    """One frame of a batched render: scene, push constants, options and the images it writes."""
+
+    def __init__(self, scene: Scene, pc: RtPushConsts, opts: RenderOptions, accum: np.ndarray | None = None,
+                 want_samples: bool = False):
+        n = opts.width * opts.height
+        self.scene, self.pc, self.opts = scene, pc, opts
+        if accum is None:
+            accum = np.zeros((opts.height, opts.width, 4), np.float32)
+        self.accum = np.ascontiguousarray(accum, dtype=np.float32)
+        assert self.accum.size == 4 * n
+        self.samples = np.zeros((n, pc.samplesPerPixel, 3), np.float32) if want_samples else None
+
+
+def _jobs_array(jobs, device: bool):
+    arr = (_RenderJob * max(1, len(jobs)))()
+    for k, j in enumerate(jobs):
+        arr[k].scene = j.scene.handle
+        arr[k].push_consts = j.pc
+        arr[k].options = j.opts
+        if device:
+            arr[k].accum = j.d_accum
+            arr[k].samples = j.d_samples or None
+        else:
+            arr[k].accum = j.accum.ctypes.data
+            arr[k].samples = None if j.samples is None else j.samples.ctypes.data
+    return arr
+
+
+def render_batch(ctx: Context, jobs: list) -> dict:
+    """reina_render_batch: every RenderJob's frame traced in shared waves; fills job.accum / job.samples."""
+    arr = _jobs_array(jobs, False)
+    st = _RenderStats()
+    _check(_lib.reina_render_batch(ctx.handle, arr, len(jobs), C.byref(st)))
+    return {"rays": st.rays, "shadow_rays": st.shadow_rays, "seconds": st.seconds}
+
+
+class DeviceRenderJob:
+    """A batched-render job on device buffers (addresses of 16-byte aligned device memory)."""
+
+    def __init__(self, scene: Scene, pc: RtPushConsts, opts: RenderOptions, d_accum: int, d_samples: int = 0):
+        self.scene, self.pc, self.opts, self.d_accum, self.d_samples = scene, pc, opts, d_accum, d_samples
+
+
+def render_batch_device(ctx: Context, jobs: list, stream: int = 0) -> dict:
+    arr = _jobs_array(jobs, True)
+    st = _RenderStats()
+    _check(_lib.reina_render_batch_device(ctx.handle, arr, len(jobs), C.c_void_p(stream), C.byref(st)))
+    return {"rays": st.rays, "shadow_rays": st.shadow_rays, "seconds": st.seconds}
 
 
 NOALLOC_MAX_PIXELS = 65536

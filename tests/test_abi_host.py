@@ -187,3 +187,46 @@ def test_bvh8_structure_is_complete_and_conservative(R, host_ctx, level):
 
     subtree(0, 1)
     assert seen_nodes.all() and seen_tris.all()
+
+
+def test_scene_outliving_its_context(R):
+    """Destroying a context detaches its scenes: later calls on them fail with REINA_ERR_STATE and
+    destroying them is safe."""
+    ctx = R.Context(-1)
+    s = R.Scene(ctx)
+    v, i = _quad()
+    s.add_object(v, i, material=R.Material(emission=(1.0, 1.0, 1.0)))
+    s.build()
+    ctx.close()
+    iv, ip = R.camera_matrices((0, 0, 3), (0, 0, -1))
+    pc = R.push_consts(iv, ip, spp=1)
+    with pytest.raises(R.ReinaError) as e:
+        R.render(ctx2 := R.Context(-1), s, pc, R.render_options(4, 4))
+    assert e.value.code == R.REINA_ERR_STATE and "destroyed" in str(e.value)
+    ctx2.close()
+    s.close()
+
+
+def test_batch_validation_on_host(R, host_ctx):
+    """Batched-render arguments are checked before any GPU work: the plain-form flag is refused."""
+    s = R.Scene(host_ctx)
+    v, i = _quad()
+    s.add_object(v, i, material=R.Material(emission=(1.0, 1.0, 1.0)))
+    s.build()
+    iv, ip = R.camera_matrices((0, 0, 3), (0, 0, -1))
+    pc = R.push_consts(iv, ip, spp=1, total_emissive_weight=s.emissive_weight)
+    bad = R.render_options(4, 4, megakernel=True)
+    with pytest.raises(R.ReinaError) as e:
+        R.render_batch(host_ctx, [R.RenderJob(s, pc, bad)])
+    assert e.value.code == R.REINA_ERR_INVALID
+    with pytest.raises(R.ReinaError) as e:
+        R.render_batch(host_ctx, [R.RenderJob(s, pc, R.render_options(4, 4))])
+    assert e.value.code == R.REINA_ERR_STATE   # host-only context
+    other = R.Context(-1)
+    try:
+        with pytest.raises(R.ReinaError) as e:
+            R.render_batch(other, [R.RenderJob(s, pc, R.render_options(4, 4))])
+        assert e.value.code == R.REINA_ERR_INVALID   # scene of another context
+    finally:
+        other.close()
+    s.close()
