@@ -285,6 +285,8 @@ def run_ours(args) -> dict | None:
     }
     if not args.no_render:
         out["render"] = render_metrics(R, ctx, torch, args.render_frames, scene)
+    if args.batch_scenes > 0:
+        out["batched"] = batch_metrics(R, ctx, torch, args.batch_scenes, args.batch_mega_scenes)
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(tris, rays, args.cpu_sample)
     return out
@@ -335,6 +337,93 @@ def render_metrics(R, ctx, torch, frames: int, scene_large) -> dict:
         out[f"cornell_{name}"] = {"s_per_frame": dt, "paths_per_s": 256 * 256 * 16 / dt,
                                   "segments_per_s": st["rays"] / dt,
                                   "rays_per_s": (st["rays"] + st["shadow_rays"]) / dt}
+    return out
+
+
+def batch_metrics(R, ctx, torch, n_scenes: int, mega_scenes: int) -> dict:
+    """The batched workload: n_scenes independent scenes (geodesic spheres with 1k-500k triangles, per-face
+    Disney/glass materials, ground, quad light, constant environment; side U[128,1024], spp U{1..64},
+    depth U{4..12}, NEE+MIS), all rendered once (a) in one reina_render_batch_device call and (b) one
+    scene at a time with the single-scene wavefront (reina_render_device); (a) and (b) give the same
+    images (checked here).  The first mega_scenes scenes are also rendered (c) one at a time by the plain
+    megakernel, with (a) re-timed on the same subset.  Device time by CUDA events around each form."""
+    import scenes
+
+    t0 = time.perf_counter()
+    built = [scenes.batch_scene(R, ctx, k) for k in range(n_scenes)]
+    setup_s = time.perf_counter() - t0
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+    jobs, accs = [], []
+    for scene, p in built:
+        pc, opts = scenes.batch_job(R, scene, p)
+        acc = torch.zeros((p["side"], p["side"], 4), dtype=torch.float32, device="cuda")
+        accs.append(acc)
+        jobs.append(R.DeviceRenderJob(scene, pc, opts, acc.data_ptr()))
+    samples = [p["side"] ** 2 * p["spp"] for _, p in built]
+    # warm-up: small jobs of every depth (captures each wave graph), and the largest single-scene frame
+    # at 1 spp (grows the single-scene path state to its final size)
+    warm_acc = torch.zeros((1024, 1024, 4), dtype=torch.float32, device="cuda")
+    warm = []
+    for depth in range(4, 13):
+        pc, opts = scenes.batch_job(R, built[0][0], {"side": 8, "spp": 1, "depth": depth, "seed": 1})
+        warm.append(R.DeviceRenderJob(built[0][0], pc, opts, warm_acc.data_ptr()))
+    R.render_batch_device(ctx, warm, sptr)
+    big = max(range(n_scenes), key=lambda k: built[k][1]["side"])
+    pc, opts = scenes.batch_job(R, built[big][0], dict(built[big][1], spp=1, depth=4))
+    R.render_device(ctx, built[big][0], pc, opts, warm_acc.data_ptr(), 0, sptr)
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        ev[0].record(stream)
+        r = fn()
+        ev[1].record(stream)
+        torch.cuda.synchronize()
+        return ev[0].elapsed_time(ev[1]) * 1e-3, r
+
+    def plain(js, mega: bool):
+        for j in js:
+            o = R.render_options(j.opts.width, j.opts.height, j.opts.mode, j.opts.seed, j.opts.env_mode,
+                                 tuple(j.opts.env_color), megakernel=mega)
+            R.render_device(ctx, j.scene, j.pc, o, j.d_accum, 0, sptr)
+
+    t_batch, st = timed(lambda: R.render_batch_device(ctx, jobs, sptr))
+    batched_imgs = [a.clone() for a in accs]
+    t_plain, _ = timed(lambda: plain(jobs, False))
+    identical = all(torch.equal(a, b) for a, b in zip(accs, batched_imgs))
+    del batched_imgs
+    seg, shadow = st["rays"], st["shadow_rays"]
+    n_smp = sum(samples)
+    out = {
+        "workload": f"{n_scenes} scenes: geodesic sphere (log-uniform 1k-500k tris) + ground + quad light, "
+                    "per-face Disney/20% glass, side U[128,1024], spp U{1..64}, depth U{4..12}, NEE+MIS",
+        "scenes": n_scenes,
+        "triangles_total": int(sum(p["triangles"] for _, p in built)),
+        "pixels_total": int(sum(p["side"] ** 2 for _, p in built)),
+        "samples_total": int(n_smp),
+        "scene_setup_s": round(setup_s, 2),
+        "wave_paths": ctx.tuning()["wave_paths"],
+        "batched": {"s": t_batch, "renders_per_s": n_scenes / t_batch, "segments_per_s": seg / t_batch,
+                    "rays_per_s": (seg + shadow) / t_batch, "samples_per_s": n_smp / t_batch},
+        "plain_wavefront": {"s": t_plain, "renders_per_s": n_scenes / t_plain, "segments_per_s": seg / t_plain,
+                            "samples_per_s": n_smp / t_plain},
+        "images_identical_batched_vs_plain_wavefront": bool(identical),
+        "speedup_vs_plain_wavefront": t_plain / t_batch,
+    }
+    m = min(mega_scenes, n_scenes)
+    if m > 0:
+        sub = jobs[:m]
+        t_sub, _ = timed(lambda: R.render_batch_device(ctx, sub, sptr))
+        t_mega, _ = timed(lambda: plain(sub, True))
+        out["megakernel_subset"] = {
+            "scenes": m, "samples_total": int(sum(samples[:m])),
+            "batched": {"s": t_sub, "renders_per_s": m / t_sub},
+            "plain_megakernel": {"s": t_mega, "renders_per_s": m / t_mega},
+            "speedup_vs_plain_megakernel": t_mega / t_sub}
+    for s_, _ in built:
+        s_.close()
     return out
 
 
@@ -413,6 +502,10 @@ def main() -> int:
     ap.add_argument("--profile-render", action="store_true", help="render a small frame twice for ncu and exit")
     ap.add_argument("--no-render", action="store_true", help="skip the render metrics")
     ap.add_argument("--render-frames", type=int, default=2)
+    ap.add_argument("--batch-scenes", type=int, default=256,
+                    help="scenes of the batched-render metrics (0 skips them)")
+    ap.add_argument("--batch-mega-scenes", type=int, default=32,
+                    help="leading scenes also rendered one at a time by the plain megakernel")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     out = run_reference(args) if args.impl == "reference" else run_ours(args)

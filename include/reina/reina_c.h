@@ -346,6 +346,15 @@ int reina_icosphere_counts(uint32_t level, uint64_t* out_vertices, uint64_t* out
 int reina_gen_icosphere(uint32_t level, float amplitude, uint64_t seed, float* vertices,
                         uint32_t* indices, float* normals);
 
+/* Class-I geodesic sphere of frequency n (each icosahedron face cut into an n x n triangular grid):
+ * 10*n^2 + 2 vertices and 20*n^2 triangles, so triangle counts between icosphere levels are reachable.
+ * Grid points are placed on the flat face and then projected (the icosphere projects at every halving,
+ * so frequency 2^L is not the level-L icosphere).  Displacement, vertex and normal layout as
+ * reina_gen_icosphere. */
+int reina_geodesic_counts(uint32_t frequency, uint64_t* out_vertices, uint64_t* out_triangles);
+int reina_gen_geodesic(uint32_t frequency, float amplitude, uint64_t seed, float* vertices, uint32_t* indices,
+                       float* normals);
+
 /* The two ray sets of the ray-cast workload: `n_camera` pinhole rays through pixel centres of a
  * width x height image from `cam_pos` looking at `cam_target` (fovy degrees), followed by `n_random`
  * rays with origins uniform in `box_min..box_max` and directions uniform on the sphere (SplitMix64

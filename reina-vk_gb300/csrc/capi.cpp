@@ -598,6 +598,25 @@ int reina_gen_icosphere(uint32_t level, float amplitude, uint64_t seed, float* v
     });
 }
 
+int reina_geodesic_counts(uint32_t frequency, uint64_t* out_vertices, uint64_t* out_triangles) {
+    return guard([&] {
+        need(frequency >= 1 && frequency <= 4096, "geodesic frequency must be in 1..4096");
+        uint64_t nv, nt;
+        rt::geodesic_counts(frequency, nv, nt);
+        if (out_vertices) *out_vertices = nv;
+        if (out_triangles) *out_triangles = nt;
+    });
+}
+
+int reina_gen_geodesic(uint32_t frequency, float amplitude, uint64_t seed, float* vertices, uint32_t* indices,
+                       float* normals) {
+    return guard([&] {
+        need(frequency >= 1 && frequency <= 4096, "geodesic frequency must be in 1..4096");
+        need(vertices && indices, "NULL output buffer");
+        rt::gen_geodesic(frequency, amplitude, seed, vertices, indices, normals);
+    });
+}
+
 int reina_gen_raycast_rays(uint32_t width, uint32_t height, const float cam_pos[3], const float cam_target[3],
                            float fovy_degrees, uint64_t n_random, const float box_min[3], const float box_max[3],
                            uint64_t seed, reina_ray* rays_out) {

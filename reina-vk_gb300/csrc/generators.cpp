@@ -65,17 +65,43 @@ void icosphere_counts(uint32_t level, uint64_t& nv, uint64_t& nt) {
     nt = 20 * p;
 }
 
-void gen_icosphere(uint32_t level, float amplitude, uint64_t seed, float* out_vertices, uint32_t* out_indices,
-                   float* out_normals) {
+// Unit icosahedron: 12 vertices (3 doubles each) and 20 outward-wound faces.
+static void icosahedron(std::vector<double>& v, std::vector<uint32_t>& f) {
     const double t = (1.0 + std::sqrt(5.0)) / 2.0;
-    std::vector<double> v = {-1, t, 0, 1, t, 0, -1, -t, 0, 1, -t, 0, 0, -1, t, 0, 1, t,
-                             0, -1, -t, 0, 1, -t, t, 0, -1, t, 0, 1, -t, 0, -1, -t, 0, 1};
+    v = {-1, t, 0, 1, t, 0, -1, -t, 0, 1, -t, 0, 0, -1, t, 0, 1, t,
+         0, -1, -t, 0, 1, -t, t, 0, -1, t, 0, 1, -t, 0, -1, -t, 0, 1};
     for (size_t i = 0; i < v.size(); i += 3) {
         const double l = std::sqrt(v[i] * v[i] + v[i + 1] * v[i + 1] + v[i + 2] * v[i + 2]);
         v[i] /= l; v[i + 1] /= l; v[i + 2] /= l;
     }
-    std::vector<uint32_t> f = {0, 11, 5, 0, 5, 1, 0, 1, 7, 0, 7, 10, 0, 10, 11, 1, 5, 9, 5, 11, 4, 11, 10, 2, 10, 7, 6, 7, 1, 8,
-                               3, 9, 4, 3, 4, 2, 3, 2, 6, 3, 6, 8, 3, 8, 9, 4, 9, 5, 2, 4, 11, 6, 2, 10, 8, 6, 7, 9, 8, 1};
+    f = {0, 11, 5, 0, 5, 1, 0, 1, 7, 0, 7, 10, 0, 10, 11, 1, 5, 9, 5, 11, 4, 11, 10, 2, 10, 7, 6, 7, 1, 8,
+         3, 9, 4, 3, 4, 2, 3, 2, 6, 3, 6, 8, 3, 8, 9, 4, 9, 5, 2, 4, 11, 6, 2, 10, 8, 6, 7, 9, 8, 1};
+}
+
+// Unit-sphere points -> vertices displaced radially to r = 1 + amplitude * noise (w = 1), plus the
+// undisplaced directions as normals.
+static void displace(const std::vector<double>& v, float amplitude, uint64_t seed, float* out_vertices, float* out_normals) {
+    const size_t nv = v.size() / 3;
+    for (size_t i = 0; i < nv; ++i) {
+        const double x = v[3 * i], y = v[3 * i + 1], z = v[3 * i + 2];
+        const double r = 1.0 + (double)amplitude * fractal_noise3(x, y, z, seed);
+        out_vertices[4 * i + 0] = (float)(x * r);
+        out_vertices[4 * i + 1] = (float)(y * r);
+        out_vertices[4 * i + 2] = (float)(z * r);
+        out_vertices[4 * i + 3] = 1.0f;
+        if (out_normals) {
+            out_normals[3 * i + 0] = (float)x;
+            out_normals[3 * i + 1] = (float)y;
+            out_normals[3 * i + 2] = (float)z;
+        }
+    }
+}
+
+void gen_icosphere(uint32_t level, float amplitude, uint64_t seed, float* out_vertices, uint32_t* out_indices,
+                   float* out_normals) {
+    std::vector<double> v;
+    std::vector<uint32_t> f;
+    icosahedron(v, f);
     for (uint32_t l = 0; l < level; ++l) {
         std::unordered_map<uint64_t, uint32_t> mid;
         mid.reserve(f.size());
@@ -101,21 +127,99 @@ void gen_icosphere(uint32_t level, float amplitude, uint64_t seed, float* out_ve
         }
         f.swap(nf);
     }
-    const size_t nv = v.size() / 3;
-    for (size_t i = 0; i < nv; ++i) {
-        const double x = v[3 * i], y = v[3 * i + 1], z = v[3 * i + 2];
-        const double r = 1.0 + (double)amplitude * fractal_noise3(x, y, z, seed);
-        out_vertices[4 * i + 0] = (float)(x * r);
-        out_vertices[4 * i + 1] = (float)(y * r);
-        out_vertices[4 * i + 2] = (float)(z * r);
-        out_vertices[4 * i + 3] = 1.0f;
-        if (out_normals) {
-            out_normals[3 * i + 0] = (float)x;
-            out_normals[3 * i + 1] = (float)y;
-            out_normals[3 * i + 2] = (float)z;
+    displace(v, amplitude, seed, out_vertices, out_normals);
+    std::memcpy(out_indices, f.data(), f.size() * sizeof(uint32_t));
+}
+
+void geodesic_counts(uint32_t frequency, uint64_t& nv, uint64_t& nt) {
+    const uint64_t n = frequency;
+    nv = 10 * n * n + 2;
+    nt = 20 * n * n;
+}
+
+// Class-I geodesic sphere: every icosahedron face cut into a frequency x frequency triangular grid and
+// projected to the unit sphere.  Vertices shared by faces (corners, then the frequency-1 interior points
+// of each edge, then face interiors) are generated once, an edge's points always from its lower-indexed
+// end, so neighbouring faces meet exactly.
+void gen_geodesic(uint32_t frequency, float amplitude, uint64_t seed, float* out_vertices, uint32_t* out_indices,
+                  float* out_normals) {
+    const uint32_t n = frequency;
+    std::vector<double> v;
+    std::vector<uint32_t> f;
+    icosahedron(v, f);
+    const uint32_t inner = n - 1;   // interior points per edge
+    std::unordered_map<uint64_t, uint32_t> edge_id;
+    std::vector<uint32_t> edges;    // (lo, hi) pairs in id order
+    for (size_t t = 0; t < f.size(); t += 3)
+        for (int e = 0; e < 3; ++e) {
+            const uint32_t a = f[t + e], b = f[t + (e + 1) % 3];
+            const uint32_t lo = a < b ? a : b, hi = a < b ? b : a;
+            if (edge_id.emplace((uint64_t)lo << 32 | hi, (uint32_t)(edges.size() / 2)).second) {
+                edges.push_back(lo);
+                edges.push_back(hi);
+            }
+        }
+    auto push_point = [&](const double p[3]) {
+        const double l = std::sqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2]);
+        v.push_back(p[0] / l); v.push_back(p[1] / l); v.push_back(p[2] / l);
+    };
+    for (size_t e = 0; e < edges.size(); e += 2) {
+        const double* A = &v[3 * edges[e]];
+        const double* B = &v[3 * edges[e + 1]];
+        const double a0 = A[0], a1 = A[1], a2 = A[2], b0 = B[0], b1 = B[1], b2 = B[2];
+        for (uint32_t k = 1; k <= inner; ++k) {
+            const double t = (double)k / n;
+            const double p[3] = {a0 + (b0 - a0) * t, a1 + (b1 - a1) * t, a2 + (b2 - a2) * t};
+            push_point(p);
         }
     }
-    std::memcpy(out_indices, f.data(), f.size() * sizeof(uint32_t));
+    const uint32_t face_base = (uint32_t)(v.size() / 3);
+    const uint32_t per_face = n >= 2 ? (n - 1) * (n - 2) / 2 : 0;
+    // vertex id of grid point (i, j) of face (A, B, C): A + (B - A) i/n + (C - A) j/n
+    auto on_edge = [&](uint32_t a, uint32_t b, uint32_t k) {   // k of n steps from a towards b
+        const uint32_t lo = a < b ? a : b, hi = a < b ? b : a;
+        const uint32_t kk = a < b ? k : n - k;
+        return 12 + edge_id.at((uint64_t)lo << 32 | hi) * inner + (kk - 1);
+    };
+    auto grid_id = [&](uint32_t face, uint32_t i, uint32_t j) -> uint32_t {
+        const uint32_t A = f[3 * face], B = f[3 * face + 1], C = f[3 * face + 2];
+        if (i == 0 && j == 0) return A;
+        if (i == n) return B;
+        if (j == n) return C;
+        if (j == 0) return on_edge(A, B, i);
+        if (i == 0) return on_edge(A, C, j);
+        if (i + j == n) return on_edge(B, C, j);
+        // interior: row j (1..n-2), column i (1..n-1-j)
+        const uint32_t idx = (j - 1) * (n - 1) - (j - 1) * j / 2;   // points in rows 1..j-1
+        return face_base + face * per_face + idx + (i - 1);
+    };
+    for (uint32_t face = 0; face < 20; ++face) {
+        const double* A = &v[3 * f[3 * face]];
+        const double* B = &v[3 * f[3 * face + 1]];
+        const double* C = &v[3 * f[3 * face + 2]];
+        const double a[3] = {A[0], A[1], A[2]}, b[3] = {B[0], B[1], B[2]}, c[3] = {C[0], C[1], C[2]};
+        for (uint32_t j = 1; j + 1 < n; ++j)
+            for (uint32_t i = 1; i + j < n; ++i) {
+                const double s = (double)i / n, t = (double)j / n;
+                const double p[3] = {a[0] + (b[0] - a[0]) * s + (c[0] - a[0]) * t, a[1] + (b[1] - a[1]) * s + (c[1] - a[1]) * t,
+                                     a[2] + (b[2] - a[2]) * s + (c[2] - a[2]) * t};
+                push_point(p);
+            }
+    }
+    uint32_t* out = out_indices;
+    for (uint32_t face = 0; face < 20; ++face)
+        for (uint32_t j = 0; j < n; ++j)
+            for (uint32_t i = 0; i + j < n; ++i) {
+                *out++ = grid_id(face, i, j);
+                *out++ = grid_id(face, i + 1, j);
+                *out++ = grid_id(face, i, j + 1);
+                if (i + j + 1 < n) {
+                    *out++ = grid_id(face, i + 1, j);
+                    *out++ = grid_id(face, i + 1, j + 1);
+                    *out++ = grid_id(face, i, j + 1);
+                }
+            }
+    displace(v, amplitude, seed, out_vertices, out_normals);
 }
 
 static void normalize3(double v[3]) {

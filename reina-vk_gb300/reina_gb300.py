@@ -247,6 +247,8 @@ def load_library() -> C.CDLL:
         "reina_camera_matrices": (I32, [P, P, P, F, F, F, F, P, P]),
         "reina_icosphere_counts": (I32, [U32, C.POINTER(U64), C.POINTER(U64)]),
         "reina_gen_icosphere": (I32, [U32, F, U64, P, P, P]),
+        "reina_geodesic_counts": (I32, [U32, C.POINTER(U64), C.POINTER(U64)]),
+        "reina_gen_geodesic": (I32, [U32, F, U64, P, P, P]),
         "reina_gen_raycast_rays": (I32, [U32, U32, P, P, F, U64, P, P, U64, P]),
     }
     for name, (res, args) in sig.items():
@@ -578,6 +580,18 @@ def icosphere(level: int, amplitude: float = 0.0, seed: int = 1) -> tuple[np.nda
     i = np.zeros(3 * nt.value, np.uint32)
     n = np.zeros((nv.value, 3), np.float32)
     _check(lib.reina_gen_icosphere(level, float(amplitude), seed, _ptr(v), _ptr(i), _ptr(n)))
+    return v, i, n
+
+
+def geodesic(frequency: int, amplitude: float = 0.0, seed: int = 1) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+    """Frequency-n geodesic sphere (20 n^2 triangles), displaced like icosphere(); returns (V, I, N)."""
+    lib = load_library()
+    nv, nt = C.c_uint64(), C.c_uint64()
+    _check(lib.reina_geodesic_counts(frequency, C.byref(nv), C.byref(nt)))
+    v = np.zeros((nv.value, 4), np.float32)
+    i = np.zeros(3 * nt.value, np.uint32)
+    n = np.zeros((nv.value, 3), np.float32)
+    _check(lib.reina_gen_geodesic(frequency, float(amplitude), seed, _ptr(v), _ptr(i), _ptr(n)))
     return v, i, n
 
 

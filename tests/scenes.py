@@ -63,20 +63,25 @@ def large_scene_geometry(R, level: int = 8, seed: int = 1):
     """Returns [(vertices (N,4), indices)] for sphere, ground plane and light quad (world space).
     large_scene_tbn() gives the sphere's per-vertex tangent frames."""
     v, i, _ = R.icosphere(level, 0.1, seed)
+    _, plane, light = large_scene_geometry_planes()
+    return [(v, i), plane, light]
+
+
+def large_scene_geometry_planes():
+    """(None, ground plane, light quad) of the large scene, world space."""
     g = 10.0
     plane_v = np.array([[-g, GROUND_Y, -g, 1], [g, GROUND_Y, -g, 1], [g, GROUND_Y, g, 1], [-g, GROUND_Y, g, 1]], np.float32)
     plane_i = np.array([0, 2, 1, 0, 3, 2], np.uint32)  # normal +y
     s = 0.75
     light_v = np.array([[-s, LIGHT_Y, -s, 1], [s, LIGHT_Y, -s, 1], [s, LIGHT_Y, s, 1], [-s, LIGHT_Y, s, 1]], np.float32)
     light_i = np.array([0, 1, 2, 0, 2, 3], np.uint32)  # normal -y
-    return [(v, i), (plane_v, plane_i), (light_v, light_i)]
+    return None, (plane_v, plane_i), (light_v, light_i)
 
 
-def large_scene_materials(R, n_faces: int, seed: int = 1):
+def large_scene_materials(R, n_faces: int, seed: int = 1, n_mat: int = 4096):
     """Per-face Disney parameters (baseColor U[0,1]^3, metallic, roughness U[0.05,1], specular, clearcoat,
     sheen) with 20% of the faces glass (dielectric, IOR 1.5, absorption U[0,2]).  To keep the number of
-    InstanceProperties records bounded, faces draw from a palette of 4096 materials."""
-    n_mat = 4096
+    InstanceProperties records bounded, faces draw from a palette of n_mat materials."""
     u = uniform(n_mat * 12, seed).reshape(n_mat, 12)
     mats = []
     for k in range(n_mat):
@@ -96,6 +101,11 @@ def large_scene_materials(R, n_faces: int, seed: int = 1):
 def large_scene_tbn(R, level: int = 8, seed: int = 1):
     """Per-vertex TBNs of the large scene's sphere (N = undisplaced radial direction)."""
     _, _, n = R.icosphere(level, 0.1, seed)
+    return tbn_from_normals(n)
+
+
+def tbn_from_normals(n: np.ndarray) -> np.ndarray:
+    """Per-vertex frames (columns T, B, N) with T = normalize(up x N)."""
     up = np.where(np.abs(n[:, 1:2]) > 0.99, np.array([[1.0, 0, 0]]), np.array([[0, 1.0, 0]]))
     t = np.cross(up, n)
     t /= np.linalg.norm(t, axis=1, keepdims=True)
@@ -116,6 +126,48 @@ def large_scene(R, ctx, level: int = 8, seed: int = 1, light_emission=(17.0, 12.
     scene.build(require_emissive=True)
     tris = np.concatenate([world_triangles(a, b) for a, b in geo])
     return scene, tris, geo
+
+
+# ---------------------------------------------------------------------------------------------------
+# Batched workload: independent scenes of uneven size, each a displaced geodesic sphere (triangle count
+# log-uniform over [1k, 500k]) with per-face Disney / glass materials, a ground plane and one quad light
+# under a constant environment, rendered at a square resolution with side U[128, 1024], spp U{1..64} and
+# depth U{4..12} with NEE + MIS.
+
+BATCH_ENV = (0.3, 0.3, 0.35)
+
+
+def batch_job_params(index: int, seed: int = 1) -> dict:
+    u = uniform(4, 1_000_003 * seed + index)
+    tris = float(np.exp(np.log(1000.0) + u[0] * (np.log(500000.0) - np.log(1000.0))))
+    freq = int(np.clip(round(np.sqrt(tris / 20.0)), 7, 158))
+    return {"frequency": freq, "triangles": 20 * freq * freq + 4, "side": 128 + min(896, int(u[1] * 897)),
+            "spp": 1 + min(63, int(u[2] * 64)), "depth": 4 + min(8, int(u[3] * 9)), "seed": index + 1}
+
+
+def batch_scene(R, ctx, index: int, seed: int = 1, n_mat: int = 256):
+    p = batch_job_params(index, seed)
+    v, i, n = R.geodesic(p["frequency"], 0.1, 7919 * seed + index)
+    scene = R.Scene(ctx)
+    sid = scene.define_object(v, i, tbns=tbn_from_normals(n), tbn_indices=i)
+    mats, face = large_scene_materials(R, i.size // 3, 7919 * seed + index, n_mat)
+    scene.add_instance_per_face(sid, None, mats, face)
+    _, (pv, pi), (lv, li) = large_scene_geometry_planes()
+    scene.add_object(pv, pi, material=R.Material(material_idx=0, albedo=(0.5, 0.5, 0.5)))
+    scene.add_object(lv, li, material=R.Material(material_idx=0, albedo=(0.9, 0.9, 0.9), emission=(17.0, 12.0, 4.0),
+                                                 cull_backface=True))
+    scene.build(require_emissive=True)
+    return scene, p
+
+
+def batch_job(R, scene, p: dict):
+    """(push constants, options) of one batched job."""
+    side = p["side"]
+    iv, ip = R.camera_matrices((0.0, 0.4, 3.6), (0.0, -0.12, -1.0), (0.0, 1.0, 0.0), np.radians(40.0), 1.0)
+    pc = R.push_consts(iv, ip, total_emissive_weight=scene.emissive_weight, spp=p["spp"], max_bounces=p["depth"],
+                       focus_dist=3.6)
+    opts = R.render_options(side, side, R.MODE_NEE_MIS, p["seed"], R.ENV_CONSTANT, BATCH_ENV)
+    return pc, opts
 
 
 # ---------------------------------------------------------------------------------------------------

@@ -230,3 +230,23 @@ def test_batch_validation_on_host(R, host_ctx):
     finally:
         other.close()
     s.close()
+
+
+@pytest.mark.parametrize("n", [1, 2, 5, 12])
+def test_geodesic_sphere_is_closed_and_outward(R, n):
+    """Frequency-n geodesic sphere: 10n^2+2 vertices, 20n^2 triangles, every edge shared by exactly two
+    oppositely wound triangles (no cracks between icosahedron faces), all faces wound outward."""
+    v, i, nrm = R.geodesic(n, 0.0, 1)
+    assert v.shape == (10 * n * n + 2, 4) and i.size == 60 * n * n
+    t = i.reshape(-1, 3)
+    e = np.concatenate([t[:, [0, 1]], t[:, [1, 2]], t[:, [2, 0]]]).tolist()
+    fwd = set(map(tuple, e))
+    assert len(fwd) == len(e) and fwd == {(b, a) for a, b in fwd}
+    p = v[t][:, :, :3].astype(np.float64)
+    cr = np.cross(p[:, 1] - p[:, 0], p[:, 2] - p[:, 0])
+    assert ((cr * p.mean(1)).sum(1) > 0).all()
+    assert np.allclose(np.linalg.norm(v[:, :3], axis=1), 1.0, atol=1e-6)
+    assert np.unique(i).size == v.shape[0]
+    vd, _, _ = R.geodesic(n, 0.1, 3)
+    r = np.linalg.norm(vd[:, :3], axis=1)
+    assert (np.abs(r - 1.0) <= 0.1 + 1e-6).all()
