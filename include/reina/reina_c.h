@@ -311,6 +311,89 @@ int reina_render_batch_device(reina_ctx* ctx, const reina_render_job* jobs, uint
                               reina_render_stats* stats);
 
 /* ------------------------------------------------------------------------------------------------ */
+/* Request server.  No counterpart in the reference, whose run loop renders one scene frame after      */
+/* frame (src/Reina.cpp:425-470 driven by src/main.cpp).  A server owns a loop thread that admits      */
+/* render requests as they arrive — while device memory within the budget allows — and runs every      */
+/* admitted request in shared waves of the batched wavefront; requests join and leave between waves.   */
+/* Scenes and kept images stay resident and are evicted least-recently-used when admission needs room */
+/* (evicted images are kept in host memory and restored on their next use).  A request's image is the */
+/* one reina_render gives for the same scene, push constants and options.                            */
+/* ------------------------------------------------------------------------------------------------ */
+typedef struct reina_server reina_server;
+
+typedef struct reina_server_options {
+    uint64_t memory_budget_bytes; /* device memory for resident scenes, kept images, running requests and
+                                   * the wave path state (0 = 120e9 bytes) */
+    uint32_t max_active_jobs;     /* requests sharing the waves, 1..512 (0 = 512) */
+    uint32_t wave_paths;          /* path slots per wave (0 = REINA_DEFAULT_WAVE_PATHS) */
+    uint32_t flags;               /* REINA_BATCH_NO_GRAPHS */
+    uint32_t reserved;
+} reina_server_options;
+
+/* A server runs on its context's GPU; destroying the context destroys its servers first. */
+int reina_server_create(reina_ctx* ctx, const reina_server_options* options, reina_server** out_server);
+/* Cancels queued and running requests, joins the loop thread, destroys the server's scenes. */
+void reina_server_destroy(reina_server* server);
+
+/* Hands a built scene of the server's context to the server, which owns it from now on (do not use or
+ * destroy the handle afterwards). */
+int reina_server_add_scene(reina_server* server, reina_scene* scene, uint32_t* out_scene_id);
+
+typedef struct reina_request {
+    uint32_t scene_id;            /* from reina_server_add_scene */
+    uint32_t reserved;
+    uint64_t image_key;           /* 0: the image lives only for the request.  Otherwise the finished image
+                                   * stays with the server under this key, and a later request with the
+                                   * same key, size and sampleBatch > 0 accumulates onto it (progressive
+                                   * rendering) without a host round trip. */
+    RtPushConsts push_consts;
+    reina_render_options options; /* flags must be 0 */
+    float* accum_rgba32f;         /* host, width*height RGBA32F: written when the request completes (and
+                                   * read at admission when sampleBatch > 0 and image_key is 0); it must
+                                   * stay valid until then.  May be NULL when image_key != 0. */
+} reina_request;
+
+enum {
+    REINA_REQ_QUEUED = 0,
+    REINA_REQ_RUNNING = 1,
+    REINA_REQ_DONE = 2,
+    REINA_REQ_FAILED = 3,
+    REINA_REQ_CANCELLED = 4
+};
+
+typedef struct reina_request_status {
+    uint32_t state;               /* REINA_REQ_* */
+    int32_t error;                /* REINA_ERR_* of a failed request */
+    double latency_s;             /* submit -> result in the host image (or -> failure / cancellation) */
+    double queue_s;               /* submit -> admission */
+    char message[160];
+} reina_request_status;
+
+/* Queues a request (does not block on the GPU).  REINA_ERR_BUDGET if the request can never fit the
+ * budget, even with everything else evicted. */
+int reina_server_submit(reina_server* server, const reina_request* request, uint64_t* out_request_id);
+int reina_server_poll(reina_server* server, uint64_t request_id, reina_request_status* out_status);
+/* Blocks until the request is done, failed or cancelled, or for timeout_s seconds (< 0: no limit). */
+int reina_server_wait(reina_server* server, uint64_t request_id, double timeout_s, reina_request_status* out_status);
+int reina_server_cancel(reina_server* server, uint64_t request_id);
+/* Copies the finished image kept under image_key to the host (accum_rgba32f may be NULL to query the
+ * size). */
+int reina_server_fetch_image(reina_server* server, uint64_t image_key, float* accum_rgba32f, uint32_t* out_width,
+                             uint32_t* out_height);
+
+typedef struct reina_server_stats {
+    uint64_t submitted, completed, failed, cancelled, queued, running;
+    double latency_p50_s, latency_p99_s, latency_mean_s, latency_max_s;   /* completed requests */
+    double uptime_s;
+    double busy_s;                /* wall time spent in waves */
+    double first_submit_to_last_done_s;
+    uint64_t rays, shadow_rays, waves;
+    uint64_t scene_uploads, scene_evictions, image_evictions, image_restores;
+    uint64_t resident_bytes, peak_resident_bytes, budget_bytes, reserved_bytes;
+} reina_server_stats;
+int reina_server_get_stats(reina_server* server, reina_server_stats* out_stats);
+
+/* ------------------------------------------------------------------------------------------------ */
 /* Post-process — replaces Reina::applyBloom + Reina::applyTonemapping (src/Reina.cpp:472-577):        */
 /* blurX (threshold) -> blurY -> combine (shaders/postprocessing/bloom), then exposure and the          */
 /* ACES fitted curve to RGBA8 UNORM (shaders/postprocessing/tonemap/tonemapping.comp.glsl:66-84).      */

@@ -19,6 +19,7 @@
 #include "post.h"
 #include "render.h"
 #include "scene.h"
+#include "server.h"
 
 using rt::check_cuda;
 using rt::fail;
@@ -44,11 +45,18 @@ struct reina_ctx {
     std::unique_ptr<rt::BatchEngine> batch;   // built on the first batched render
     std::mutex scenes_mu;
     std::unordered_set<reina_scene*> scenes;  // live scenes; detached (device memory freed) on destroy
+    std::unordered_set<reina_server*> servers;   // destroyed before the context
 };
 
 struct reina_scene {
     reina_ctx* ctx = nullptr;
     std::unique_ptr<rt::Scene> s;
+};
+
+struct reina_server {
+    reina_ctx* ctx = nullptr;
+    std::unique_ptr<rt::Server> srv;
+    std::vector<reina_scene*> scenes;   // owned
 };
 
 namespace {
@@ -88,6 +96,7 @@ const rt::Scene& built_scene(const reina_scene* scene) {
     need(scene != nullptr, "scene is NULL");
     if (!scene->ctx) fail(REINA_ERR_STATE, "the scene's context has been destroyed");
     if (!scene->s->built()) fail(REINA_ERR_STATE, "scene is not built (call reina_scene_build)");
+    if (scene->ctx->device >= 0 && !scene->s->resident()) fail(REINA_ERR_STATE, "scene is not resident on the GPU");
     return *scene->s;
 }
 
@@ -154,6 +163,7 @@ int reina_ctx_create(const reina_ctx_options* options, reina_ctx** out_ctx) {
 
 void reina_ctx_destroy(reina_ctx* ctx) {
     if (!ctx) return;
+    while (!ctx->servers.empty()) reina_server_destroy(*ctx->servers.begin());
     if (ctx->device >= 0) cudaSetDevice(ctx->device);
     {
         // scenes outliving their context keep only their handle: free their device memory now
@@ -624,6 +634,133 @@ int reina_gen_raycast_rays(uint32_t width, uint32_t height, const float cam_pos[
         need(cam_pos && cam_target && box_min && box_max && rays_out, "NULL argument");
         rt::gen_raycast_rays(width, height, cam_pos, cam_target, fovy_degrees, n_random, box_min, box_max, seed,
                              reinterpret_cast<rt::Ray*>(rays_out));
+    });
+}
+
+// ------------------------------------------------------------------------------------------------
+// Request server
+
+int reina_server_create(reina_ctx* ctx, const reina_server_options* o, reina_server** out) {
+    return guard([&] {
+        need(ctx && out, "NULL argument");
+        *out = nullptr;
+        use_device(ctx);
+        rt::ServerConfig cfg;
+        cfg.budget = (o && o->memory_budget_bytes) ? o->memory_budget_bytes : 120000000000ull;
+        cfg.max_active = (o && o->max_active_jobs) ? o->max_active_jobs : 512;
+        cfg.wave_paths = o ? o->wave_paths : 0;
+        need(!o || (o->flags & ~(uint32_t)REINA_BATCH_NO_GRAPHS) == 0, "unknown server flags");
+        cfg.graphs = !(o && (o->flags & REINA_BATCH_NO_GRAPHS));
+        auto s = std::make_unique<reina_server>();
+        s->ctx = ctx;
+        s->srv = std::make_unique<rt::Server>(ctx->device, ctx->sm_count, cfg);
+        ctx->servers.insert(s.get());
+        *out = s.release();
+    });
+}
+
+void reina_server_destroy(reina_server* server) {
+    if (!server) return;
+    if (server->ctx) {
+        if (server->ctx->device >= 0) cudaSetDevice(server->ctx->device);
+        server->ctx->servers.erase(server);
+    }
+    server->srv.reset();
+    for (reina_scene* sc : server->scenes) reina_scene_destroy(sc);
+    delete server;
+}
+
+int reina_server_add_scene(reina_server* server, reina_scene* scene, uint32_t* out_id) {
+    return guard([&] {
+        need(server && scene && out_id, "NULL argument");
+        need(scene->ctx == server->ctx, "scene belongs to another context");
+        built_scene(scene);
+        for (reina_scene* sc : server->scenes) need(sc != scene, "scene was already added");
+        server->scenes.reserve(server->scenes.size() + 1);
+        *out_id = server->srv->add_scene(scene->s.get());
+        server->scenes.push_back(scene);
+    });
+}
+
+int reina_server_submit(reina_server* server, const reina_request* req, uint64_t* out_id) {
+    return guard([&] {
+        need(server && req && out_id, "NULL argument");
+        rt::RequestSpec spec;
+        spec.scene = req->scene_id;
+        spec.image_key = req->image_key;
+        spec.pc = req->push_consts;
+        spec.opt = render_opts(&req->push_consts, &req->options);
+        spec.host_out = req->accum_rgba32f;
+        *out_id = server->srv->submit(spec);
+    });
+}
+
+static void to_status(const rt::RequestStatus& s, reina_request_status* out) {
+    std::memset(out, 0, sizeof(*out));
+    out->state = s.state;
+    out->error = s.error;
+    out->latency_s = s.latency_s;
+    out->queue_s = s.queue_s;
+    std::strncpy(out->message, s.message.c_str(), sizeof(out->message) - 1);
+}
+
+int reina_server_poll(reina_server* server, uint64_t id, reina_request_status* out) {
+    return guard([&] {
+        need(server && out, "NULL argument");
+        to_status(server->srv->poll(id), out);
+    });
+}
+
+int reina_server_wait(reina_server* server, uint64_t id, double timeout_s, reina_request_status* out) {
+    return guard([&] {
+        need(server && out, "NULL argument");
+        to_status(server->srv->wait(id, timeout_s), out);
+    });
+}
+
+int reina_server_cancel(reina_server* server, uint64_t id) {
+    return guard([&] {
+        need(server != nullptr, "NULL argument");
+        server->srv->cancel(id);
+    });
+}
+
+int reina_server_fetch_image(reina_server* server, uint64_t key, float* accum, uint32_t* w, uint32_t* h) {
+    return guard([&] {
+        need(server != nullptr, "NULL argument");
+        server->srv->fetch_image(key, accum, w, h);
+    });
+}
+
+int reina_server_get_stats(reina_server* server, reina_server_stats* out) {
+    return guard([&] {
+        need(server && out, "NULL argument");
+        const rt::ServerStats s = server->srv->stats();
+        std::memset(out, 0, sizeof(*out));
+        out->submitted = s.submitted;
+        out->completed = s.completed;
+        out->failed = s.failed;
+        out->cancelled = s.cancelled;
+        out->queued = s.queued;
+        out->running = s.running;
+        out->latency_p50_s = s.p50;
+        out->latency_p99_s = s.p99;
+        out->latency_mean_s = s.mean;
+        out->latency_max_s = s.max;
+        out->uptime_s = s.uptime_s;
+        out->busy_s = s.busy_s;
+        out->first_submit_to_last_done_s = s.first_submit_to_last_done_s;
+        out->rays = s.rays;
+        out->shadow_rays = s.shadow_rays;
+        out->waves = s.waves;
+        out->scene_uploads = s.scene_uploads;
+        out->scene_evictions = s.scene_evictions;
+        out->image_evictions = s.image_evictions;
+        out->image_restores = s.image_restores;
+        out->resident_bytes = s.resident_bytes;
+        out->peak_resident_bytes = s.peak_resident_bytes;
+        out->budget_bytes = s.budget_bytes;
+        out->reserved_bytes = s.reserved_bytes;
     });
 }
 

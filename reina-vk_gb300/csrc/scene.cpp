@@ -331,10 +331,10 @@ void Scene::build(bool require_emissive) {
         fail(REINA_ERR_INVALID, e.what());
     }
 
-    std::vector<InstanceGpu> inst_gpu(instances_.size());
+    inst_gpu_.assign(instances_.size(), InstanceGpu{});
     for (size_t ii = 0; ii < instances_.size(); ++ii) {
         const InstanceRecord& inst = instances_[ii];
-        InstanceGpu& g = inst_gpu[ii];
+        InstanceGpu& g = inst_gpu_[ii];
         std::memset(&g, 0, sizeof(g));
         for (int r = 0; r < 3; ++r)
             for (int c = 0; c < 4; ++c) g.m[r * 4 + c] = inst.transform[c * 4 + r];
@@ -346,13 +346,45 @@ void Scene::build(bool require_emissive) {
         g.light_area = inst.light.emissive ? inst.light.area : 0.0f;
     }
 
+    has_tbn_.resize(models_.size());
+    for (size_t o = 0; o < models_.size(); ++o) has_tbn_[o] = models_[o].tbn_indices.empty() ? 0 : 1;
+    built_ = true;
     if (host_only) {   // host-only scenes keep the assembled buffers and the BVH, nothing is uploaded
         dev_ = DeviceScene{};
         dev_.node_count = (uint32_t)bvh_.nodes.size();
         dev_.tri_count = (uint32_t)bvh_.tris.size();
-        built_ = true;
         return;
     }
+    upload();
+}
+
+size_t Scene::upload_bytes() const {
+    return bvh_.nodes.size() * sizeof(Bvh8Node) + bvh_.tris.size() * sizeof(TriRecord) +
+           (all_vertices_.size() + all_tbns_.size() + std::max<size_t>(1, all_tex_coords_.size()) +
+            cdf_triangles_.size() + cdf_instances_.size()) * sizeof(float) +
+           (all_indices_offset_.size() + all_tbns_indices_offset_.size() + all_tex_indices_offset_.size() +
+            prim_instance_.size() + prim_props_.size() + props_material_.size()) * sizeof(uint32_t) +
+           props_.size() * sizeof(InstanceProperties) + inst_gpu_.size() * sizeof(InstanceGpu) +
+           emissive_data_.size() * sizeof(EmissiveInstanceData) + has_tbn_.size();
+}
+
+void Scene::release_device() {
+    for (DeviceBuffer* b : {&d_nodes_, &d_tris_, &d_vertices_, &d_indices_, &d_tbns_, &d_tbn_indices_, &d_tex_coords_,
+                            &d_tex_indices_, &d_props_, &d_instances_, &d_prim_instance_, &d_prim_props_, &d_emissive_,
+                            &d_cdf_tris_, &d_cdf_inst_, &d_props_material_, &d_has_tbn_})
+        b->release();
+    const uint32_t nodes = dev_.node_count, tris = dev_.tri_count;
+    dev_ = DeviceScene{};
+    dev_.node_count = nodes;
+    dev_.tri_count = tris;
+    resident_ = false;
+}
+
+void Scene::upload() {
+    if (!built_) fail(REINA_ERR_STATE, "scene is not built");
+    if (device_ < 0) fail(REINA_ERR_STATE, "host-only scene cannot be uploaded");
+    if (resident_) return;
+    check_cuda(cudaSetDevice(device_), "cudaSetDevice");
     // Upload (src/scene/Models.cpp:94-115 uploads the same arrays; an empty texcoord buffer gets one
     // float there and here so that the pointer stays valid).
     auto up = [](DeviceBuffer& b, const void* p, size_t bytes) { b.upload(p, bytes); };
@@ -367,16 +399,14 @@ void Scene::build(bool require_emissive) {
     else up(d_tex_coords_, all_tex_coords_.data(), all_tex_coords_.size() * sizeof(float));
     up(d_tex_indices_, all_tex_indices_offset_.data(), all_tex_indices_offset_.size() * sizeof(uint32_t));
     up(d_props_, props_.data(), props_.size() * sizeof(InstanceProperties));
-    up(d_instances_, inst_gpu.data(), inst_gpu.size() * sizeof(InstanceGpu));
+    up(d_instances_, inst_gpu_.data(), inst_gpu_.size() * sizeof(InstanceGpu));
     up(d_prim_instance_, prim_instance_.data(), prim_instance_.size() * sizeof(uint32_t));
     up(d_prim_props_, prim_props_.data(), prim_props_.size() * sizeof(uint32_t));
     up(d_emissive_, emissive_data_.data(), emissive_data_.size() * sizeof(EmissiveInstanceData));
     up(d_cdf_tris_, cdf_triangles_.data(), cdf_triangles_.size() * sizeof(float));
     up(d_cdf_inst_, cdf_instances_.data(), cdf_instances_.size() * sizeof(float));
     up(d_props_material_, props_material_.data(), props_material_.size() * sizeof(uint32_t));
-    std::vector<uint8_t> has_tbn(models_.size());
-    for (size_t o = 0; o < models_.size(); ++o) has_tbn[o] = models_[o].tbn_indices.empty() ? 0 : 1;
-    up(d_has_tbn_, has_tbn.data(), has_tbn.size());
+    up(d_has_tbn_, has_tbn_.data(), has_tbn_.size());
 
     dev_ = DeviceScene{};
     dev_.nodes = d_nodes_.as<Bvh8Node>();
@@ -402,7 +432,7 @@ void Scene::build(bool require_emissive) {
     dev_.cdf_instances = d_cdf_inst_.as<float>();
     dev_.emissive_count = (uint32_t)emissive_data_.size();
     dev_.emissive_weight = emissive_total_;
-    built_ = true;
+    resident_ = true;
 }
 
 size_t Scene::device_bytes() const {

@@ -64,6 +64,12 @@ public:
     uint64_t triangle_count() const { return tri_total_; }
     size_t instance_count() const { return instances_.size(); }
     size_t device_bytes() const;
+    // Device residency (used by the request server's LRU): the host keeps every assembled buffer, so a
+    // released scene can be uploaded again.  upload_bytes() is the device memory an upload takes.
+    bool resident() const { return resident_; }
+    size_t upload_bytes() const;
+    void upload();
+    void release_device();
     int device() const { return device_; }
     void prim_info(uint32_t prim, uint32_t* inst, uint32_t* local) const;
     void bounds(float lo[3], float hi[3]) const;
@@ -81,6 +87,7 @@ private:
 
     int device_;
     bool built_ = false;
+    bool resident_ = false;
     // Models (src/scene/Models.cpp)
     std::vector<ModelData> models_;
     std::vector<ModelRange> ranges_;
@@ -99,6 +106,8 @@ private:
     std::vector<uint32_t> prim_instance_, prim_props_;
     float bounds_lo_[3] = {0, 0, 0}, bounds_hi_[3] = {0, 0, 0};
     Bvh8 bvh_;
+    std::vector<InstanceGpu> inst_gpu_;
+    std::vector<uint8_t> has_tbn_;
     // Device buffers
     DeviceBuffer d_nodes_, d_tris_, d_vertices_, d_indices_, d_tbns_, d_tbn_indices_, d_tex_coords_,
         d_tex_indices_, d_props_, d_instances_, d_prim_instance_, d_prim_props_, d_emissive_, d_cdf_tris_,

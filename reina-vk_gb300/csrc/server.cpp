@@ -1,0 +1,438 @@
+// Render-request server (see server.h).  One loop thread owns every device resource of the server:
+// admission, uploads, evictions and the waves all run there; client threads only queue requests, read
+// statuses and copy kept images out.
+#include "server.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+
+namespace rt {
+
+namespace {
+constexpr size_t kPixelStateBytes = 24;   // per pixel: carried RNG, accumulatedDistance, sums, count
+constexpr size_t kImageBytes = 16;        // per pixel: RGBA32F
+constexpr size_t kPathBytes = 164;        // per wave slot of the batch engine
+}  // namespace
+
+double Server::now() const {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+Server::Server(int device, int sm_count, const ServerConfig& cfg) : device_(device), cfg_(cfg) {
+    if (cfg_.max_active == 0 || cfg_.max_active > kMaxWaveSegments / 2)
+        fail(REINA_ERR_INVALID, "max_active_jobs must be in 1.." + std::to_string(kMaxWaveSegments / 2));
+    const uint32_t wave = cfg_.wave_paths ? cfg_.wave_paths : 2097152u;
+    reserved_ = (uint64_t)wave * kPathBytes + (64u << 20);   // path state + descriptors and slack
+    if (cfg_.budget < reserved_)
+        fail(REINA_ERR_BUDGET, "memory budget " + std::to_string(cfg_.budget) + " B is below the engine's " +
+                                   std::to_string(reserved_) + " B of path state");
+    check_cuda(cudaSetDevice(device_), "cudaSetDevice");
+    check_cuda(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+    engine_ = std::make_unique<BatchEngine>(device_, sm_count, wave, cfg_.graphs);
+    t0_ = now();
+    thread_ = std::thread([this] { loop(); });
+}
+
+Server::~Server() {
+    {
+        std::lock_guard<std::mutex> lk(mu_);
+        stop_ = true;
+    }
+    cv_work_.notify_all();
+    if (thread_.joinable()) thread_.join();
+    cudaSetDevice(device_);
+    {
+        std::lock_guard<std::mutex> lk(mu_);
+        for (Request* r : running_) finish(*r, kReqCancelled, 0, "server destroyed");
+        for (Request* r : queue_) finish(*r, kReqCancelled, 0, "server destroyed");
+        running_.clear();
+        queue_.clear();
+    }
+    cv_done_.notify_all();
+    requests_.clear();
+    images_.clear();
+    engine_.reset();
+    if (stream_) cudaStreamDestroy(stream_);
+}
+
+uint32_t Server::add_scene(Scene* scene) {
+    if (!scene || !scene->built()) fail(REINA_ERR_STATE, "scene is not built");
+    if (scene->device() != device_) fail(REINA_ERR_INVALID, "scene belongs to another device");
+    std::lock_guard<std::mutex> lk(mu_);
+    SceneSlot s;
+    s.scene = scene;
+    s.last_use = ++tick_;
+    if (scene->resident()) {
+        const size_t b = scene->upload_bytes();
+        if (resident_ + b + reserved_ <= cfg_.budget) {
+            resident_ += b;
+            peak_ = std::max(peak_, resident_);
+        } else {
+            check_cuda(cudaSetDevice(device_), "cudaSetDevice");
+            scene->release_device();
+        }
+    }
+    scenes_.push_back(s);
+    return (uint32_t)(scenes_.size() - 1);
+}
+
+size_t Server::request_bytes(const RequestSpec& s) const {
+    const size_t px = (size_t)s.opt.width * s.opt.height;
+    return px * (kPixelStateBytes + kImageBytes);
+}
+
+uint64_t Server::submit(const RequestSpec& spec) {
+    if (spec.opt.megakernel) fail(REINA_ERR_INVALID, "served requests run the wavefront (options.flags must be 0)");
+    if (!spec.host_out && spec.image_key == 0) fail(REINA_ERR_INVALID, "a request needs a host image or an image key");
+    std::lock_guard<std::mutex> lk(mu_);
+    if (stop_) fail(REINA_ERR_STATE, "server is shutting down");
+    if (spec.scene >= scenes_.size()) fail(REINA_ERR_INVALID, "unknown server scene id");
+    const Scene& sc = *scenes_[spec.scene].scene;
+    if (spec.opt.mode == kModeNeeMis && sc.emissive_data().size() > 0 && !(spec.pc.totalEmissiveWeight > 0.0f))
+        fail(REINA_ERR_INVALID, "totalEmissiveWeight must be positive for NEE");
+    const uint64_t need = request_bytes(spec) + sc.upload_bytes();
+    if (need + reserved_ > cfg_.budget)
+        fail(REINA_ERR_BUDGET, "request needs " + std::to_string(need) + " B of device memory; the budget leaves " +
+                                   std::to_string(cfg_.budget - reserved_) + " B");
+    auto r = std::make_unique<Request>();
+    r->id = next_id_++;
+    r->spec = spec;
+    r->t_submit = now();
+    if (first_submit_ < 0) first_submit_ = r->t_submit;
+    Request* p = r.get();
+    requests_.emplace(p->id, std::move(r));
+    queue_.push_back(p);
+    counters_.submitted++;
+    cv_work_.notify_one();
+    return p->id;
+}
+
+RequestStatus Server::poll(uint64_t id) {
+    std::lock_guard<std::mutex> lk(mu_);
+    auto it = requests_.find(id);
+    if (it == requests_.end()) fail(REINA_ERR_INVALID, "unknown request id");
+    return it->second->status;
+}
+
+RequestStatus Server::wait(uint64_t id, double timeout_s) {
+    std::unique_lock<std::mutex> lk(mu_);
+    auto it = requests_.find(id);
+    if (it == requests_.end()) fail(REINA_ERR_INVALID, "unknown request id");
+    Request* r = it->second.get();
+    auto done = [&] { return r->status.state >= kReqDone; };
+    if (timeout_s < 0) cv_done_.wait(lk, done);
+    else cv_done_.wait_for(lk, std::chrono::duration<double>(timeout_s), done);
+    return r->status;
+}
+
+void Server::cancel(uint64_t id) {
+    std::lock_guard<std::mutex> lk(mu_);
+    auto it = requests_.find(id);
+    if (it == requests_.end()) fail(REINA_ERR_INVALID, "unknown request id");
+    it->second->cancel = true;
+    cv_work_.notify_one();
+}
+
+void Server::fetch_image(uint64_t key, float* host_out, uint32_t* w, uint32_t* h) {
+    std::lock_guard<std::mutex> lk(mu_);
+    auto it = images_.find(key);
+    if (it == images_.end() || !it->second.valid) fail(REINA_ERR_STATE, "no finished image under this key");
+    ImageSlot& im = it->second;
+    if (im.busy) fail(REINA_ERR_STATE, "a running request is writing this image");
+    if (w) *w = im.w;
+    if (h) *h = im.h;
+    if (!host_out) return;
+    const size_t bytes = (size_t)im.w * im.h * kImageBytes;
+    if (im.dev.get()) {
+        check_cuda(cudaSetDevice(device_), "cudaSetDevice");
+        check_cuda(cudaMemcpy(host_out, im.dev.get(), bytes, cudaMemcpyDeviceToHost), "D2H image");
+    } else {
+        std::memcpy(host_out, im.host.data(), bytes);
+    }
+}
+
+ServerStats Server::stats() {
+    std::lock_guard<std::mutex> lk(mu_);
+    ServerStats s = counters_;
+    s.queued = queue_.size();
+    s.running = running_.size();
+    std::vector<double> l = latencies_;
+    std::sort(l.begin(), l.end());
+    auto pct = [&](double q) {
+        if (l.empty()) return 0.0;
+        const size_t k = (size_t)std::min<double>((double)l.size() - 1, std::ceil(q * (double)l.size()) - 1);
+        return l[k];
+    };
+    s.p50 = pct(0.50);
+    s.p99 = pct(0.99);
+    double sum = 0;
+    for (double x : l) sum += x;
+    s.mean = l.empty() ? 0.0 : sum / (double)l.size();
+    s.max = l.empty() ? 0.0 : l.back();
+    s.uptime_s = now() - t0_;
+    s.first_submit_to_last_done_s = first_submit_ < 0 ? 0.0 : std::max(0.0, last_done_ - first_submit_);
+    s.resident_bytes = resident_;
+    s.peak_resident_bytes = peak_;
+    s.budget_bytes = cfg_.budget;
+    s.reserved_bytes = reserved_;
+    return s;
+}
+
+// Evicts least-recently-used idle scenes and kept images (never those `r` needs) until `need` more bytes
+// fit the budget.  Returns false if they cannot.
+bool Server::make_room(size_t need, const Request& r) {
+    while (resident_ + need + reserved_ > cfg_.budget) {
+        uint64_t best = UINT64_MAX;
+        SceneSlot* bs = nullptr;
+        ImageSlot* bi = nullptr;
+        for (size_t k = 0; k < scenes_.size(); ++k) {
+            SceneSlot& s = scenes_[k];
+            if (k != r.spec.scene && s.active == 0 && s.scene->resident() && s.last_use < best) {
+                best = s.last_use;
+                bs = &s;
+                bi = nullptr;
+            }
+        }
+        for (auto& [key, im] : images_) {
+            if (key != r.spec.image_key && !im.busy && im.dev.get() && im.last_use < best) {
+                best = im.last_use;
+                bi = &im;
+                bs = nullptr;
+            }
+        }
+        if (bs) {
+            resident_ -= bs->scene->upload_bytes();
+            bs->scene->release_device();
+            counters_.scene_evictions++;
+        } else if (bi) {
+            const size_t bytes = (size_t)bi->w * bi->h * kImageBytes;
+            bi->host.resize((size_t)bi->w * bi->h * 4);
+            check_cuda(cudaMemcpy(bi->host.data(), bi->dev.get(), bytes, cudaMemcpyDeviceToHost), "D2H evicted image");
+            bi->dev.release();
+            resident_ -= bytes;
+            counters_.image_evictions++;
+        } else {
+            return false;
+        }
+    }
+    return true;
+}
+
+bool Server::try_admit(Request& r) {
+    const RequestSpec& s = r.spec;
+    SceneSlot& sc = scenes_[s.scene];
+    const size_t px = (size_t)s.opt.width * s.opt.height;
+    size_t need = px * kPixelStateBytes;
+    ImageSlot* img = nullptr;
+    bool fresh_image = false;
+    if (s.image_key) {
+        auto it = images_.find(s.image_key);
+        if (it != images_.end()) {
+            img = &it->second;
+            if (img->busy) return false;   // the previous request on this key is still running
+            const bool same = img->w == s.opt.width && img->h == s.opt.height;
+            if (s.pc.sampleBatch > 0 && (!img->valid || !same))
+                fail(REINA_ERR_STATE, "progressive request: no finished image of this size under the key");
+            if (!same) {
+                if (img->dev.get()) resident_ -= (size_t)img->w * img->h * kImageBytes;
+                images_.erase(it);
+                img = nullptr;
+            }
+        } else if (s.pc.sampleBatch > 0) {
+            fail(REINA_ERR_STATE, "progressive request: no finished image under the key");
+        }
+        if (!img) fresh_image = true;
+        if (!img || !img->dev.get()) need += px * kImageBytes;
+    } else {
+        need += px * kImageBytes;
+    }
+    if (!sc.scene->resident()) need += sc.scene->upload_bytes();
+    if (!make_room(need, r)) return false;
+
+    if (!sc.scene->resident()) {
+        sc.scene->upload();
+        resident_ += sc.scene->upload_bytes();
+        counters_.scene_uploads++;
+    }
+    float* d_accum = nullptr;
+    try {
+        if (s.image_key) {
+            if (fresh_image) {
+                img = &images_[s.image_key];
+                img->w = s.opt.width;
+                img->h = s.opt.height;
+            }
+            if (!img->dev.get()) {
+                img->dev.alloc(px * kImageBytes);
+                resident_ += px * kImageBytes;
+                if (!img->host.empty()) {
+                    check_cuda(cudaMemcpy(img->dev.get(), img->host.data(), px * kImageBytes, cudaMemcpyHostToDevice),
+                               "H2D restored image");
+                    img->host.clear();
+                    img->host.shrink_to_fit();
+                    counters_.image_restores++;
+                }
+            }
+            d_accum = img->dev.as<float>();
+        } else {
+            r.accum.alloc(px * kImageBytes);
+            resident_ += px * kImageBytes;
+            if (s.pc.sampleBatch > 0)
+                check_cuda(cudaMemcpy(r.accum.get(), s.host_out, px * kImageBytes, cudaMemcpyHostToDevice),
+                           "H2D previous image");
+            d_accum = r.accum.as<float>();
+        }
+        r.job.scene = sc.scene->device_view();
+        r.job.pc = s.pc;
+        r.job.opt = s.opt;
+        r.job.d_accum = d_accum;
+        r.job.d_samples = nullptr;
+        BatchEngine::prepare(r.job);
+    } catch (...) {
+        if (r.accum.get()) {
+            resident_ -= px * kImageBytes;
+            r.accum.release();
+        }
+        throw;
+    }
+    if (img) img->busy = true;
+    resident_ += px * kPixelStateBytes;
+    r.job_bytes = px * kPixelStateBytes + (s.image_key ? 0 : px * kImageBytes);
+    peak_ = std::max(peak_, resident_);
+    sc.active++;
+    sc.last_use = ++tick_;
+    r.t_admit = now();
+    r.status.state = kReqRunning;
+    r.status.queue_s = r.t_admit - r.t_submit;
+    return true;
+}
+
+// Releases what a request holds (if it was admitted) and records its final state.
+void Server::finish(Request& r, uint32_t state, int error, const std::string& msg) {
+    if (r.status.state == kReqRunning) {
+        SceneSlot& sc = scenes_[r.spec.scene];
+        sc.active--;
+        sc.last_use = ++tick_;
+        if (r.spec.image_key) {
+            auto it = images_.find(r.spec.image_key);
+            if (it != images_.end()) {
+                it->second.busy = false;
+                it->second.last_use = ++tick_;
+                if (state == kReqDone) it->second.valid = true;   // the image is written only at completion
+            }
+        }
+        r.job.pixel_state.release();
+        r.accum.release();
+        resident_ -= r.job_bytes;
+    }
+    const double t = now();
+    r.status.state = state;
+    r.status.error = error;
+    r.status.message = msg;
+    r.status.latency_s = t - r.t_submit;
+    if (state == kReqDone) {
+        counters_.completed++;
+        latencies_.push_back(r.status.latency_s);
+        last_done_ = t;
+    } else if (state == kReqFailed) {
+        counters_.failed++;
+    } else {
+        counters_.cancelled++;
+    }
+}
+
+void Server::loop() {
+    cudaSetDevice(device_);
+    std::unique_lock<std::mutex> lk(mu_);
+    for (;;) {
+        cv_work_.wait(lk, [&] { return stop_ || !queue_.empty() || !running_.empty(); });
+        if (stop_) return;
+        for (auto it = running_.begin(); it != running_.end();) {
+            if ((*it)->cancel) {
+                finish(**it, kReqCancelled, 0, "cancelled");
+                it = running_.erase(it);
+            } else {
+                ++it;
+            }
+        }
+        while (!queue_.empty() && running_.size() < cfg_.max_active) {
+            Request* r = queue_.front();
+            if (r->cancel) {
+                queue_.pop_front();
+                finish(*r, kReqCancelled, 0, "cancelled");
+                continue;
+            }
+            bool ok = false;
+            try {
+                ok = try_admit(*r);
+            } catch (const Error& e) {
+                queue_.pop_front();
+                finish(*r, kReqFailed, e.code, e.what());
+                continue;
+            }
+            if (!ok) {
+                if (running_.empty()) {   // nothing to wait for: everything evictable was tried
+                    queue_.pop_front();
+                    finish(*r, kReqFailed, REINA_ERR_BUDGET, "request does not fit the memory budget");
+                    continue;
+                }
+                break;
+            }
+            queue_.pop_front();
+            running_.push_back(r);
+        }
+        cv_done_.notify_all();
+        if (running_.empty()) continue;
+        std::vector<BatchJob*> jobs;
+        jobs.reserve(running_.size());
+        for (Request* r : running_) jobs.push_back(&r->job);
+        lk.unlock();
+        int code = 0;
+        std::string err;
+        const double t = now();
+        try {
+            engine_->run_wave(jobs, stream_);
+        } catch (const Error& e) {
+            code = e.code;
+            err = e.what();
+        }
+        const double dt = now() - t;
+        // results of the requests this wave completed go to their host images outside the lock
+        std::vector<Request*> done;
+        if (!code) {
+            for (Request* r : running_)
+                if (r->job.resolved && r->spec.host_out) {
+                    const size_t bytes = (size_t)r->spec.opt.width * r->spec.opt.height * kImageBytes;
+                    const cudaError_t ce = cudaMemcpy(r->spec.host_out, r->job.d_accum, bytes, cudaMemcpyDeviceToHost);
+                    if (ce != cudaSuccess) {
+                        code = REINA_ERR_CUDA;
+                        err = std::string("D2H result: ") + cudaGetErrorString(ce);
+                        break;
+                    }
+                }
+        }
+        lk.lock();
+        counters_.busy_s += dt;
+        counters_.rays = engine_->rays();
+        counters_.shadow_rays = engine_->shadow_rays();
+        counters_.waves = engine_->waves();
+        if (code) {
+            for (Request* r : running_) finish(*r, kReqFailed, code, err);
+            running_.clear();
+        } else {
+            for (auto it = running_.begin(); it != running_.end();) {
+                if ((*it)->job.resolved) {
+                    finish(**it, kReqDone, 0, "");
+                    it = running_.erase(it);
+                } else {
+                    ++it;
+                }
+            }
+        }
+        cv_done_.notify_all();
+    }
+}
+
+}  // namespace rt

@@ -11,6 +11,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+import weakref
 from dataclasses import dataclass, field, fields
 from pathlib import Path
 
@@ -118,6 +119,35 @@ class TonemappingPushConsts(C.Structure):
 
 class _RenderStats(C.Structure):
     _fields_ = [("rays", C.c_uint64), ("shadow_rays", C.c_uint64), ("seconds", C.c_double)]
+
+
+class _ServerOptions(C.Structure):
+    _fields_ = [("memory_budget_bytes", C.c_uint64), ("max_active_jobs", C.c_uint32), ("wave_paths", C.c_uint32),
+                ("flags", C.c_uint32), ("reserved", C.c_uint32)]
+
+
+class _Request(C.Structure):
+    _fields_ = [("scene_id", C.c_uint32), ("reserved", C.c_uint32), ("image_key", C.c_uint64),
+                ("push_consts", RtPushConsts), ("options", RenderOptions), ("accum", C.c_void_p)]
+
+
+class _RequestStatus(C.Structure):
+    _fields_ = [("state", C.c_uint32), ("error", C.c_int32), ("latency_s", C.c_double), ("queue_s", C.c_double),
+                ("message", C.c_char * 160)]
+
+
+_SERVER_STAT_FIELDS = ["submitted", "completed", "failed", "cancelled", "queued", "running", "latency_p50_s",
+                       "latency_p99_s", "latency_mean_s", "latency_max_s", "uptime_s", "busy_s",
+                       "first_submit_to_last_done_s", "rays", "shadow_rays", "waves", "scene_uploads",
+                       "scene_evictions", "image_evictions", "image_restores", "resident_bytes",
+                       "peak_resident_bytes", "budget_bytes", "reserved_bytes"]
+
+
+class _ServerStats(C.Structure):
+    _fields_ = [(n, C.c_double if n.endswith("_s") else C.c_uint64) for n in _SERVER_STAT_FIELDS]
+
+
+REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED, REQ_CANCELLED = range(5)
 
 
 class _RenderJob(C.Structure):
@@ -240,6 +270,15 @@ def load_library() -> C.CDLL:
         "reina_render_device": (I32, [P, P, C.POINTER(RtPushConsts), C.POINTER(RenderOptions), P, P, P]),
         "reina_render_device_noalloc": (I32, [P, P, C.POINTER(RtPushConsts), C.POINTER(RenderOptions), P, P, P]),
         "reina_render_batch": (I32, [P, C.POINTER(_RenderJob), U32, C.POINTER(_RenderStats)]),
+        "reina_server_create": (I32, [P, C.POINTER(_ServerOptions), C.POINTER(P)]),
+        "reina_server_destroy": (None, [P]),
+        "reina_server_add_scene": (I32, [P, P, C.POINTER(U32)]),
+        "reina_server_submit": (I32, [P, C.POINTER(_Request), C.POINTER(U64)]),
+        "reina_server_poll": (I32, [P, U64, C.POINTER(_RequestStatus)]),
+        "reina_server_wait": (I32, [P, U64, C.c_double, C.POINTER(_RequestStatus)]),
+        "reina_server_cancel": (I32, [P, U64]),
+        "reina_server_fetch_image": (I32, [P, U64, P, C.POINTER(U32), C.POINTER(U32)]),
+        "reina_server_get_stats": (I32, [P, C.POINTER(_ServerStats)]),
         "reina_render_batch_device": (I32, [P, C.POINTER(_RenderJob), U32, P, C.POINTER(_RenderStats)]),
         "reina_postprocess": (I32, [P, P, U32, U32, C.POINTER(BloomPushConsts), C.POINTER(TonemappingPushConsts), P, P]),
         "reina_postprocess_device": (I32, [P, P, U32, U32, C.POINTER(BloomPushConsts),
@@ -292,6 +331,7 @@ class Context:
         _check(lib.reina_ctx_create(C.byref(opts), C.byref(h)))
         self._h = h
         self.device = device
+        self._servers = weakref.WeakSet()
 
     @property
     def handle(self):
@@ -326,6 +366,8 @@ class Context:
 
     def close(self) -> None:
         if self._h:
+            for srv in list(self._servers):
+                srv._h = None   # destroyed with the context
             _lib.reina_ctx_destroy(self._h)
             self._h = None
 
@@ -547,6 +589,91 @@ def render_batch_device(ctx: Context, jobs: list, stream: int = 0) -> dict:
     st = _RenderStats()
     _check(_lib.reina_render_batch_device(ctx.handle, arr, len(jobs), C.c_void_p(stream), C.byref(st)))
     return {"rays": st.rays, "shadow_rays": st.shadow_rays, "seconds": st.seconds}
+
+
+def _status(st: _RequestStatus) -> dict:
+    return {"state": int(st.state), "error": int(st.error), "latency_s": st.latency_s, "queue_s": st.queue_s,
+            "message": st.message.decode("utf-8", "replace")}
+
+
+class Server:
+    """reina_server_*: a request loop that admits render requests by device-memory budget, keeps scenes and
+    kept images resident with LRU eviction and runs admitted requests together in shared waves."""
+
+    def __init__(self, ctx: Context, budget_bytes: int = 0, max_active: int = 0, wave_paths: int = 0,
+                 graphs: bool = True):
+        self.ctx = ctx
+        o = _ServerOptions(budget_bytes, max_active, wave_paths, 0 if graphs else BATCH_NO_GRAPHS, 0)
+        h = C.c_void_p()
+        _check(_lib.reina_server_create(ctx.handle, C.byref(o), C.byref(h)))
+        self._h = h
+        ctx._servers.add(self)
+        self._outputs = {}   # request id -> host image kept alive until the request ends
+
+    @property
+    def handle(self):
+        if not self._h:
+            raise ReinaError(REINA_ERR_STATE, "server is closed")
+        return self._h
+
+    def close(self) -> None:
+        # A context destroys its servers; when garbage collection finalizes the context first (its
+        # weak set of servers may already be cleared then), the server's handle is gone with it.
+        if self._h and self.ctx._h:
+            _lib.reina_server_destroy(self._h)
+        self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_scene(self, scene: Scene) -> int:
+        """Hands the scene over: the server owns and destroys it; the Scene object becomes unusable."""
+        sid = C.c_uint32()
+        _check(_lib.reina_server_add_scene(self.handle, scene.handle, C.byref(sid)))
+        scene._h = None
+        return sid.value
+
+    def submit(self, scene_id: int, pc: RtPushConsts, opts: RenderOptions, out: np.ndarray | None = None,
+               image_key: int = 0) -> int:
+        """Queues a request; `out` ((H, W, 4) float32, or None with an image key) receives the image."""
+        if out is not None:
+            assert out.dtype == np.float32 and out.flags.c_contiguous and out.size == 4 * opts.width * opts.height
+        r = _Request(scene_id, 0, image_key, pc, opts, None if out is None else out.ctypes.data)
+        rid = C.c_uint64()
+        _check(_lib.reina_server_submit(self.handle, C.byref(r), C.byref(rid)))
+        self._outputs[rid.value] = out
+        return rid.value
+
+    def poll(self, rid: int) -> dict:
+        st = _RequestStatus()
+        _check(_lib.reina_server_poll(self.handle, rid, C.byref(st)))
+        return _status(st)
+
+    def wait(self, rid: int, timeout_s: float = -1.0) -> dict:
+        st = _RequestStatus()
+        _check(_lib.reina_server_wait(self.handle, rid, float(timeout_s), C.byref(st)))
+        d = _status(st)
+        if d["state"] >= REQ_DONE:
+            self._outputs.pop(rid, None)
+        return d
+
+    def cancel(self, rid: int) -> None:
+        _check(_lib.reina_server_cancel(self.handle, rid))
+
+    def fetch_image(self, key: int) -> np.ndarray:
+        w, h = C.c_uint32(), C.c_uint32()
+        _check(_lib.reina_server_fetch_image(self.handle, key, None, C.byref(w), C.byref(h)))
+        out = np.zeros((h.value, w.value, 4), np.float32)
+        _check(_lib.reina_server_fetch_image(self.handle, key, _ptr(out), C.byref(w), C.byref(h)))
+        return out
+
+    def stats(self) -> dict:
+        st = _ServerStats()
+        _check(_lib.reina_server_get_stats(self.handle, C.byref(st)))
+        return {n: getattr(st, n) for n in _SERVER_STAT_FIELDS}
 
 
 NOALLOC_MAX_PIXELS = 65536

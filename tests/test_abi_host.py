@@ -250,3 +250,9 @@ def test_geodesic_sphere_is_closed_and_outward(R, n):
     vd, _, _ = R.geodesic(n, 0.1, 3)
     r = np.linalg.norm(vd[:, :3], axis=1)
     assert (np.abs(r - 1.0) <= 0.1 + 1e-6).all()
+
+
+def test_server_needs_a_gpu_context(R, host_ctx):
+    with pytest.raises(R.ReinaError) as e:
+        R.Server(host_ctx)
+    assert e.value.code == R.REINA_ERR_STATE
