@@ -286,7 +286,10 @@ def run_ours(args) -> dict | None:
     if not args.no_render:
         out["render"] = render_metrics(R, ctx, torch, args.render_frames, scene)
     if args.batch_scenes > 0:
-        out["batched"] = batch_metrics(R, ctx, torch, args.batch_scenes, args.batch_mega_scenes)
+        pool, setup_s = build_pool(R, ctx, args.batch_scenes)
+        out["batched"] = batch_metrics(R, ctx, torch, pool, setup_s, args.batch_mega_scenes)
+        if args.serve_seconds > 0:
+            out["served"] = serve_metrics(R, ctx, torch, pool, args.serve_seconds, args.serve_rate)
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(tris, rays, args.cpu_sample)
     return out
@@ -340,7 +343,16 @@ def render_metrics(R, ctx, torch, frames: int, scene_large) -> dict:
     return out
 
 
-def batch_metrics(R, ctx, torch, n_scenes: int, mega_scenes: int) -> dict:
+def build_pool(R, ctx, n_scenes: int):
+    """The seeded scenes of the batched workload: [(scene, job parameters)] and the host build time."""
+    import scenes
+
+    t0 = time.perf_counter()
+    built = [scenes.batch_scene(R, ctx, k) for k in range(n_scenes)]
+    return built, time.perf_counter() - t0
+
+
+def batch_metrics(R, ctx, torch, built, setup_s: float, mega_scenes: int) -> dict:
     """The batched workload: n_scenes independent scenes (geodesic spheres with 1k-500k triangles, per-face
     Disney/glass materials, ground, quad light, constant environment; side U[128,1024], spp U{1..64},
     depth U{4..12}, NEE+MIS), all rendered once (a) in one reina_render_batch_device call and (b) one
@@ -349,9 +361,7 @@ def batch_metrics(R, ctx, torch, n_scenes: int, mega_scenes: int) -> dict:
     megakernel, with (a) re-timed on the same subset.  Device time by CUDA events around each form."""
     import scenes
 
-    t0 = time.perf_counter()
-    built = [scenes.batch_scene(R, ctx, k) for k in range(n_scenes)]
-    setup_s = time.perf_counter() - t0
+    n_scenes = len(built)
     stream = torch.cuda.current_stream()
     sptr = stream.cuda_stream
     jobs, accs = [], []
@@ -422,9 +432,93 @@ def batch_metrics(R, ctx, torch, n_scenes: int, mega_scenes: int) -> dict:
             "batched": {"s": t_sub, "renders_per_s": m / t_sub},
             "plain_megakernel": {"s": t_mega, "renders_per_s": m / t_mega},
             "speedup_vs_plain_megakernel": t_mega / t_sub}
-    for s_, _ in built:
-        s_.close()
     return out
+
+
+def serve_metrics(R, ctx, torch, pool, seconds: float, rate: float) -> dict:
+    """The served workload: a seeded Poisson stream of requests (rate per second over `seconds`), each a
+    scene of the pool with side/spp/depth drawn like the batched workload, submitted in real time (a)
+    one request at a time to reina_render_device in arrival order (the plain form) and (b) to the
+    request server (120 GB admission budget, continuous batching).  Latency is arrival -> image on the
+    host; throughput is requests and rays over first arrival -> last completion."""
+    import scenes
+
+    rng = np.random.default_rng(2026)
+    arrivals, t = [], 0.0
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t >= seconds:
+            break
+        arrivals.append(t)
+    reqs = []
+    for k, at in enumerate(arrivals):
+        si = int(rng.integers(0, len(pool)))
+        p = dict(scenes.batch_job_params(100000 + k))
+        p["seed"] = k + 1
+        scene = pool[si][0]
+        pc, opts = scenes.batch_job(R, scene, p)
+        reqs.append((at, si, pc, opts, p["side"]))
+    n = len(reqs)
+    samples = sum(r[3].width * r[3].height * r[2].samplesPerPixel for r in reqs)
+
+    def pct(lat):
+        return float(np.percentile(lat, 50)), float(np.percentile(lat, 99))
+
+    # (a) plain: one request at a time, in arrival order, images copied to the host
+    sptr = torch.cuda.current_stream().cuda_stream
+    host = {}
+    for at, si, pc, opts, side in reqs:
+        host.setdefault(side, np.zeros((side, side, 4), np.float32))
+    dev = torch.zeros((1024, 1024, 4), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    lat = []
+    rays = 0
+    t0 = time.perf_counter()
+    for at, si, pc, opts, side in reqs:
+        now = time.perf_counter() - t0
+        if now < at:
+            time.sleep(at - now)
+        R.render_device(ctx, pool[si][0], pc, opts, dev.data_ptr(), 0, sptr)
+        torch.cuda.synchronize()
+        host[side][...] = dev.view(-1)[: side * side * 4].view(side, side, 4).cpu().numpy()
+        lat.append(time.perf_counter() - t0 - at)
+    plain_span = time.perf_counter() - t0 - reqs[0][0]
+    p50, p99 = pct(lat)
+    plain = {"p50_s": p50, "p99_s": p99, "mean_s": float(np.mean(lat)), "renders_per_s": n / plain_span,
+             "samples_per_s": samples / plain_span, "span_s": plain_span}
+
+    # (b) served
+    srv = R.Server(ctx, budget_bytes=120_000_000_000)
+    ids = [srv.add_scene(s) for s, _ in pool]
+    outs = [np.zeros((r[3].height, r[3].width, 4), np.float32) for r in reqs]
+    rids = [None] * n
+
+    def submitter():
+        t_start = time.perf_counter()
+        for k, (at, si, pc, opts, side) in enumerate(reqs):
+            now = time.perf_counter() - t_start
+            if now < at:
+                time.sleep(at - now)
+            rids[k] = srv.submit(ids[si], pc, opts, outs[k])
+
+    th = threading.Thread(target=submitter)
+    th.start()
+    th.join()
+    states = [srv.wait(r, -1.0)["state"] for r in rids]
+    st = srv.stats()
+    srv.close()
+    span = st["first_submit_to_last_done_s"]
+    served = {"p50_s": st["latency_p50_s"], "p99_s": st["latency_p99_s"], "mean_s": st["latency_mean_s"],
+              "renders_per_s": st["completed"] / span, "samples_per_s": samples / span,
+              "segments_per_s": st["rays"] / span, "rays_per_s": (st["rays"] + st["shadow_rays"]) / span,
+              "span_s": span, "completed": st["completed"], "failed": st["failed"], "waves": st["waves"],
+              "scene_uploads": st["scene_uploads"], "scene_evictions": st["scene_evictions"],
+              "peak_resident_gb": st["peak_resident_bytes"] / 1e9}
+    return {"workload": f"Poisson {rate:g}/s for {seconds:g} s ({n} requests) over the {len(pool)}-scene pool, "
+                        "side U[128,1024], spp U{1..64}, depth U{4..12}, NEE+MIS; 120 GB admission budget",
+            "requests": n, "samples_total": int(samples), "all_done": all(s == R.REQ_DONE for s in states),
+            "plain_one_at_a_time": plain, "served": served,
+            "renders_per_s_ratio": served["renders_per_s"] / plain["renders_per_s"]}
 
 
 def cpu_baseline(tris, rays, sample: int) -> dict:
@@ -506,6 +600,9 @@ def main() -> int:
                     help="scenes of the batched-render metrics (0 skips them)")
     ap.add_argument("--batch-mega-scenes", type=int, default=32,
                     help="leading scenes also rendered one at a time by the plain megakernel")
+    ap.add_argument("--serve-seconds", type=float, default=4.0,
+                    help="arrival window of the served workload (0 skips it; 120 is the full stream)")
+    ap.add_argument("--serve-rate", type=float, default=50.0, help="Poisson arrival rate (requests/s)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     out = run_reference(args) if args.impl == "reference" else run_ours(args)
