@@ -65,19 +65,27 @@ void reina_ctx_destroy(reina_ctx* ctx);
 int reina_ctx_sm_count(const reina_ctx* ctx);
 
 /* Launch parameters of the traversal kernels and of batched renders (no counterpart in the reference,
- * whose traversal and scheduling are the driver's).
+ * whose traversal and scheduling are the driver's).  Every setting gives the same results; only speed
+ * differs.  0 selects the default of a field.
  *   refill = 0: one thread per ray (grid form, the default); refill = 1..32: persistent warps that fetch
- *            new rays when `refill` of their 32 lanes are idle.
+ *            new rays when `refill` of their 32 lanes are idle (block 128, stack 12).
+ *   trace_block: threads per block of the grid-form traversal kernels (ray cast, wavefront extend and
+ *            shadow): 64, 128 or 256 (default 128).
+ *   trace_stack: shared-memory traversal stack entries per thread, 8, 12 or 16 (default 12); deeper
+ *            levels spill to local memory.
  *   wave_paths: path slots of one wave of a batched render (0 = REINA_DEFAULT_WAVE_PATHS); the path
  *            state costs 164 bytes per slot.
  *   batch_flags: REINA_BATCH_NO_GRAPHS launches each wave's kernels one by one instead of replaying a
  *            captured CUDA graph.
- * Changing wave_paths or batch_flags releases the batch engine; the next batched call rebuilds it. */
+ * Changing wave_paths, batch_flags, trace_block or trace_stack releases the batch engine; the next
+ * batched call rebuilds it. */
 typedef struct reina_tuning {
     uint32_t refill;
     uint32_t wave_paths;
     uint32_t batch_flags;
-    uint32_t reserved;
+    uint32_t trace_block;
+    uint32_t trace_stack;
+    uint32_t reserved[3];
 } reina_tuning;
 enum { REINA_DEFAULT_WAVE_PATHS = 2097152 };
 enum { REINA_BATCH_NO_GRAPHS = 1 };
@@ -416,6 +424,55 @@ int reina_postprocess_device(reina_ctx* ctx, const void* d_accum_rgba32f, uint32
  * column-major, as glm computes them. */
 int reina_camera_matrices(const float pos[3], const float front[3], const float up[3], float fovy_radians,
                           float aspect, float z_near, float z_far, float inv_view[16], float inv_proj[16]);
+
+/* ------------------------------------------------------------------------------------------------ */
+/* Autotuner                                                                                          */
+/* ------------------------------------------------------------------------------------------------ */
+/* Autotuner (no counterpart in the reference).  Each reina_autotune_* call times candidate
+ * configurations on the caller's own workload — the traversal launch form, block size and stack depth
+ * (every variant in reina_tuning), and for batched renders also the wave size — and stores the fastest
+ * in the context's cache under (kind, floor(log2(triangles)), floor(log2(work size))), where the work
+ * size is the ray count, the pixel count, or the batch's total samples.  With REINA_AUTOTUNE_CACHED,
+ * ray casts, renders and batched renders whose key is in the cache run with the cached configuration
+ * instead of the context's tuning.  Results never depend on the configuration. */
+enum {
+    REINA_TUNE_RAYCAST_CLOSEST = 0,
+    REINA_TUNE_RAYCAST_ANY = 1,
+    REINA_TUNE_RENDER = 2,
+    REINA_TUNE_BATCH = 3
+};
+enum { REINA_AUTOTUNE_OFF = 0, REINA_AUTOTUNE_CACHED = 1 };
+
+typedef struct reina_tune_result {
+    reina_tuning best;            /* the fastest candidate (refill, trace_block, trace_stack; wave_paths
+                                   * for REINA_TUNE_BATCH) */
+    double best_ms;               /* its time per call (median of the timed calls) */
+    double default_ms;            /* the default configuration's time per call */
+    uint32_t candidates;          /* configurations timed */
+    uint32_t kind;                /* REINA_TUNE_* */
+    uint32_t tri_bucket;          /* cache key parts */
+    uint32_t size_bucket;
+} reina_tune_result;
+
+/* Times the ray cast of `count` device rays into `d_hits` (flags as reina_raycast_device) on `stream`
+ * for every candidate; blocks until done.  The hit buffer holds the (configuration-independent) hits
+ * afterwards. */
+int reina_autotune_raycast(reina_ctx* ctx, const reina_scene* scene, const void* d_rays, uint64_t count,
+                           void* d_hits, uint32_t flags, void* stream, reina_tune_result* out_result);
+/* Times one-sample frames of the render (scratch image; the caller's images are not touched). */
+int reina_autotune_render(reina_ctx* ctx, const reina_scene* scene, const RtPushConsts* push_consts,
+                          const reina_render_options* options, reina_tune_result* out_result);
+/* Times a batched render of (up to 32 of) the jobs at no more than 2 samples per pixel, into scratch
+ * images. */
+int reina_autotune_batch(reina_ctx* ctx, const reina_render_job* jobs, uint32_t count, reina_tune_result* out_result);
+int reina_autotune_set_mode(reina_ctx* ctx, uint32_t mode);
+/* The cached configuration for a workload, if any (*out_found = 0 when there is none). */
+int reina_autotune_lookup(reina_ctx* ctx, uint32_t kind, uint64_t triangles, uint64_t work_size,
+                          reina_tuning* out_tuning, int32_t* out_found);
+/* Writes / merges the cache as text, one "kind tri_bucket size_bucket refill block stack wave_paths
+ * best_ms default_ms" line per entry. */
+int reina_autotune_save(reina_ctx* ctx, const char* path);
+int reina_autotune_load(reina_ctx* ctx, const char* path);
 
 /* ------------------------------------------------------------------------------------------------ */
 /* Synthetic workloads (seeded, deterministic)                                                        */

@@ -91,8 +91,9 @@ __global__ void __launch_bounds__(kBlock) kb_init(BatchLaunch B) {
     }
 }
 
-__global__ void __launch_bounds__(kBlock) kb_extend(BatchLaunch B, int cur) {
-    __shared__ uint2 stack[kSmemStack * kBlock];
+template <int BLOCK, int SS>
+__global__ void __launch_bounds__(BLOCK) kb_extend(BatchLaunch B, int cur) {
+    __shared__ uint2 stack[SS * BLOCK];
     const PathState& ps = B.bp.ps;
     const uint32_t n = ps.counters[kCntActive + cur];
     const uint32_t* q = ps.q_active[cur];
@@ -108,7 +109,7 @@ __global__ void __launch_bounds__(kBlock) kb_extend(BatchLaunch B, int cur) {
             Hit h;
             TraceCounters c{0u, 0u};
             uint32_t e = 0;
-            if (s.node_count) e = traverse<false, false, true>(s.nodes, s.tris, r, stack + threadIdx.x, kBlock, h, c);
+            if (s.node_count) e = traverse<false, false, true, SS>(s.nodes, s.tris, r, stack + threadIdx.x, BLOCK, h, c);
             else h.prim = kMiss;
             if (e) atomicOr(ps.counters + kCntError, e);
             ps.hprim[p] = h.prim;
@@ -218,8 +219,9 @@ __global__ void __launch_bounds__(kBlock) kb_shade_miss(BatchLaunch B) {
     }
 }
 
-__global__ void __launch_bounds__(kBlock) kb_shadow(BatchLaunch B) {
-    __shared__ uint2 stack[kSmemStack * kBlock];
+template <int BLOCK, int SS>
+__global__ void __launch_bounds__(BLOCK) kb_shadow(BatchLaunch B) {
+    __shared__ uint2 stack[SS * BLOCK];
     const PathState& ps = B.bp.ps;
     const uint32_t n = ps.counters[kCntShadow];
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
@@ -233,7 +235,7 @@ __global__ void __launch_bounds__(kBlock) kb_shadow(BatchLaunch B) {
             Hit h;
             TraceCounters c{0u, 0u};
             uint32_t e = 0;
-            if (s.node_count) e = traverse<true, false, false>(s.nodes, s.tris, r, stack + threadIdx.x, kBlock, h, c);
+            if (s.node_count) e = traverse<true, false, false, SS>(s.nodes, s.tris, r, stack + threadIdx.x, BLOCK, h, c);
             else h.prim = kMiss;
             if (e) atomicOr(ps.counters + kCntError, e);
             if (h.prim == kMiss) store_rad(ps, p, load_rad(ps, p) + V3{ps.s_cr[i], ps.s_cg[i], ps.s_cb[i]});
@@ -314,15 +316,17 @@ static int occupancy(const void* fn, int sm_count) {
     return std::max(1, per_sm) * std::max(1, sm_count);
 }
 
-BatchEngine::BatchEngine(int device, int sm_count, uint32_t wave_capacity, bool use_graphs)
-    : device_(device), sm_count_(sm_count), capacity_(wave_capacity), use_graphs_(use_graphs) {
+BatchEngine::BatchEngine(int device, int sm_count, uint32_t wave_capacity, bool use_graphs, const TraceConfig& trace)
+    : device_(device), sm_count_(sm_count), capacity_(wave_capacity), use_graphs_(use_graphs), trace_(trace) {
     if (wave_capacity == 0) fail(REINA_ERR_INVALID, "wave capacity must be positive");
     paths_.alloc((64 + kBatchWordsPerPath * (size_t)capacity_) * 4);
     desc_bytes_ = sizeof(WaveHeader) + kMaxWaveSegments * sizeof(WaveSeg) + kMaxWaveJobs * sizeof(JobGpu);
     desc_.alloc(desc_bytes_);
     check_cuda(cudaMallocHost(&host_desc_, desc_bytes_), "cudaMallocHost");
-    blocks_ext_ = occupancy((const void*)kb_extend, sm_count);
-    blocks_sh_ = occupancy((const void*)kb_shadow, sm_count);
+    with_trace_variant(trace_, [&](auto B, auto S) {
+        blocks_ext_ = resident_grid((const void*)kb_extend<B.value, S.value>, B.value, sm_count);
+        blocks_sh_ = resident_grid((const void*)kb_shadow<B.value, S.value>, B.value, sm_count);
+    });
     blocks_shade_[1] = occupancy((const void*)kb_shade<1>, sm_count);
     blocks_shade_[2] = occupancy((const void*)kb_shade<2>, sm_count);
     blocks_shade_[3] = occupancy((const void*)kb_shade<3>, sm_count);
@@ -387,13 +391,18 @@ void BatchEngine::launch_wave(const WaveHeader& h, bool any_nee, cudaStream_t st
         for (uint32_t seg = 0; seg < h.max_bounces; ++seg) {
             check_cuda(cudaMemsetAsync(cnt + kCntActive + (cur ^ 1), 0, sizeof(uint32_t), s), "cudaMemsetAsync");
             check_cuda(cudaMemsetAsync(cnt + kCntQueue, 0, 6 * sizeof(uint32_t), s), "cudaMemsetAsync");
-            kb_extend<<<blocks_ext_, kBlock, 0, s>>>(B, cur);
+            with_trace_variant(trace_, [&](auto BS, auto SS) {
+                kb_extend<BS.value, SS.value><<<blocks_ext_, BS.value, 0, s>>>(B, cur);
+            });
             kb_shade_miss<<<simple, kBlock, 0, s>>>(B);
             kb_shade<1><<<blocks_shade_[1], kBlock, 0, s>>>(B, cur);
             kb_shade<2><<<blocks_shade_[2], kBlock, 0, s>>>(B, cur);
             kb_shade<3><<<blocks_shade_[3], kBlock, 0, s>>>(B, cur);
             kb_shade<4><<<blocks_shade_[4], kBlock, 0, s>>>(B, cur);
-            if (any_nee) kb_shadow<<<blocks_sh_, kBlock, 0, s>>>(B);
+            if (any_nee)
+                with_trace_variant(trace_, [&](auto BS, auto SS) {
+                    kb_shadow<BS.value, SS.value><<<blocks_sh_, BS.value, 0, s>>>(B);
+                });
             cur ^= 1;
         }
         kb_finish<<<simple, kBlock, 0, s>>>(B);

@@ -67,7 +67,8 @@ struct BatchJob {
 
 class BatchEngine {
 public:
-    BatchEngine(int device, int sm_count, uint32_t wave_capacity, bool use_graphs);
+    BatchEngine(int device, int sm_count, uint32_t wave_capacity, bool use_graphs,
+                const TraceConfig& trace = TraceConfig());
     ~BatchEngine();
     BatchEngine(const BatchEngine&) = delete;
     BatchEngine& operator=(const BatchEngine&) = delete;
@@ -79,6 +80,7 @@ public:
     // Synchronizes the stream at the end of the wave.
     uint64_t run_wave(const std::vector<BatchJob*>& jobs, cudaStream_t st);
     uint32_t capacity() const { return capacity_; }
+    const TraceConfig& trace() const { return trace_; }
     uint64_t rays() const { return rays_; }
     uint64_t shadow_rays() const { return shadow_rays_; }
     uint32_t waves() const { return waves_; }
@@ -88,6 +90,7 @@ private:
     int device_, sm_count_;
     uint32_t capacity_;
     bool use_graphs_;
+    TraceConfig trace_;           // grid-form traversal variant of the extend and shadow kernels
     DeviceBuffer paths_;          // path state for `capacity_` slots (+ job, pixel, sample, depth arrays)
     DeviceBuffer desc_;           // header + segments + job table
     void* host_desc_ = nullptr;   // pinned staging of the descriptor

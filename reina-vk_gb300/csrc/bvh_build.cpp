@@ -236,21 +236,28 @@ struct WideBuilder {
         Bvh8Node node;
         std::memset(&node, 0, sizeof(node));
 
-        // Quantization frame: p = union.lo - delta, scale 2^e with 255 * 2^e >= extent + 2 delta.
+        // Quantization frame: p = union.lo - delta - slack, scale 2^e with 255 * 2^e >= extent + 2 delta
+        // + 2 slack, where slack = 2^-7 quanta.  The slack keeps every child's quantized box at least
+        // 2^-8 quanta outside its (delta-dilated) bounds without clamping at 0 or 255, which covers the
+        // extra rounding of the traversal's plane offsets (at most 2^-9 quanta, see intersect_children).
         double scale[3];
         float p[3];
         uint8_t ebias[3];
         for (int k = 0; k < 3; ++k) {
-            double lo = (double)u.lo[k] - delta;
-            float pf = (float)lo;
-            if ((double)pf > lo) pf = std::nextafter(pf, -INFINITY);
-            double extent = ((double)u.hi[k] + delta) - (double)pf;
+            const double lo = (double)u.lo[k] - delta;
+            const double hi = (double)u.hi[k] + delta;
             int e = 0;
-            std::frexp(extent / 255.0, &e);
+            std::frexp((hi - lo) / 255.0, &e);
             if (e < -126) e = -126;
-            if (e > 127) throw std::runtime_error("BVH build: scene coordinates out of range");
-            // guard against rounding in the test above
-            while (std::ldexp(255.0, e) < extent) ++e;
+            float pf = 0.0f;
+            for (;;) {
+                if (e > kMaxQuantExponent) throw std::runtime_error("BVH build: scene coordinates out of range");
+                const double slack = std::ldexp(1.0, e - 7);
+                pf = (float)(lo - slack);
+                if ((double)pf > lo - slack) pf = std::nextafter(pf, -INFINITY);
+                if (std::ldexp(255.0, e) >= (hi + slack) - (double)pf) break;
+                ++e;
+            }
             p[k] = pf;
             scale[k] = std::ldexp(1.0, e);
             ebias[k] = (uint8_t)(e + 127);
@@ -274,8 +281,8 @@ struct WideBuilder {
             if (ci < 0) continue;
             const BNode& c = bb.nodes[ch[ci]];
             auto q = [&](int k, float lo, float hi, uint8_t& qlo, uint8_t& qhi) {
-                double a = std::floor(((double)lo - delta - (double)p[k]) / scale[k]);
-                double b = std::ceil(((double)hi + delta - (double)p[k]) / scale[k]);
+                double a = std::floor(((double)lo - delta - (double)p[k]) / scale[k] - 0.00390625);
+                double b = std::ceil(((double)hi + delta - (double)p[k]) / scale[k] + 0.00390625);
                 a = std::max(0.0, std::min(255.0, a));
                 b = std::max(0.0, std::min(255.0, b));
                 qlo = (uint8_t)a;

@@ -29,5 +29,7 @@ Bvh8 build_bvh8(const float* verts, uint64_t tri_count, const BvhBuildOptions& o
 
 // Maximum BVH8 depth the traversal kernels accept (their stack holds one entry per level).
 constexpr uint32_t kMaxBvhDepth = 64;
+// Largest quantization exponent of a node (scale 2^e): the traversal forms 2^(e+15) in single precision.
+constexpr int kMaxQuantExponent = 110;
 
 }  // namespace rt

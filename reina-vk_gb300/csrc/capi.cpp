@@ -1,4 +1,5 @@
 // C ABI of the library (include/reina/reina_c.h): handles, status codes and thread-local messages.
+#include <algorithm>
 #include <atomic>
 #include <chrono>
 #include <cstring>
@@ -12,6 +13,7 @@
 #include <cuda_runtime_api.h>
 
 #include "../../include/reina/reina_c.h"
+#include "autotune.h"
 #include "batch.h"
 #include "errors.h"
 #include "generators.h"
@@ -32,7 +34,7 @@ struct reina_ctx {
     rt::DeviceBuffer counters;   // u64 x 2 traversal counters
     rt::DeviceBuffer fetch;      // ring of u32 ray-fetch counters, one per ray-cast launch in flight
     std::atomic<uint32_t> fetch_slot{0};
-    int refill = rt::kDefaultRefill;
+    rt::TraceConfig trace;       // traversal launch configuration (reina_tuning)
     uint32_t* next_fetch_counter() { return fetch.as<uint32_t>() + (fetch_slot.fetch_add(1) % kFetchSlots); }
     static constexpr uint32_t kFetchSlots = 256;
     rt::DeviceBuffer rays, hits; // staging for host-buffer ray casts
@@ -43,6 +45,8 @@ struct reina_ctx {
     uint32_t wave_paths = REINA_DEFAULT_WAVE_PATHS;
     uint32_t batch_flags = 0;
     std::unique_ptr<rt::BatchEngine> batch;   // built on the first batched render
+    rt::TuneCache tune;          // autotuned configurations
+    uint32_t autotune_mode = REINA_AUTOTUNE_OFF;
     std::mutex scenes_mu;
     std::unordered_set<reina_scene*> scenes;  // live scenes; detached (device memory freed) on destroy
     std::unordered_set<reina_server*> servers;   // destroyed before the context
@@ -129,6 +133,16 @@ uint32_t check_device_errors(reina_ctx* ctx, cudaStream_t st) {
     return e;
 }
 
+// The traversal configuration for a workload: the cached autotuned one when the context uses the
+// cache and has an entry, else the context's tuning.
+rt::TraceConfig trace_for(const reina_ctx* ctx, uint32_t kind, uint64_t triangles, uint64_t size) {
+    rt::TuneEntry e;
+    if (ctx->autotune_mode == REINA_AUTOTUNE_CACHED &&
+        ctx->tune.get(kind, rt::tune_bucket(triangles), rt::tune_bucket(size), &e))
+        return e.trace;
+    return ctx->trace;
+}
+
 }  // namespace
 
 extern "C" {
@@ -188,8 +202,14 @@ int reina_ctx_set_tuning(reina_ctx* ctx, const reina_tuning* t) {
         need((t->batch_flags & ~(uint32_t)REINA_BATCH_NO_GRAPHS) == 0, "unknown batch flags");
         const uint32_t wave = t->wave_paths ? t->wave_paths : (uint32_t)REINA_DEFAULT_WAVE_PATHS;
         need(wave <= (1u << 26), "wave_paths must be at most 2^26");
-        ctx->refill = (int)t->refill;
-        if (wave != ctx->wave_paths || t->batch_flags != ctx->batch_flags) {
+        rt::TraceConfig tc;
+        tc.refill = (int)t->refill;
+        tc.block = (int)(t->trace_block ? t->trace_block : rt::kTraceBlock);
+        tc.stack = (int)(t->trace_stack ? t->trace_stack : rt::kDefaultTraceStack);
+        need(rt::valid_trace_config(tc), "trace_block must be 64, 128 or 256 and trace_stack 8, 12 or 16");
+        const bool engine_changed = tc.block != ctx->trace.block || tc.stack != ctx->trace.stack;
+        ctx->trace = tc;
+        if (wave != ctx->wave_paths || t->batch_flags != ctx->batch_flags || engine_changed) {
             if (ctx->batch && ctx->device >= 0) check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
             ctx->batch.reset();
             ctx->wave_paths = wave;
@@ -202,7 +222,9 @@ int reina_ctx_get_tuning(const reina_ctx* ctx, reina_tuning* out) {
     return guard([&] {
         need(ctx && out, "NULL argument");
         std::memset(out, 0, sizeof(*out));
-        out->refill = (uint32_t)ctx->refill;
+        out->refill = (uint32_t)ctx->trace.refill;
+        out->trace_block = (uint32_t)ctx->trace.block;
+        out->trace_stack = (uint32_t)ctx->trace.stack;
         out->wave_paths = ctx->wave_paths;
         out->batch_flags = ctx->batch_flags;
     });
@@ -310,7 +332,7 @@ int reina_raycast_device(reina_ctx* ctx, const reina_scene* scene, const void* d
         use_device(ctx);
         rt::launch_raycast(s.device_view(), static_cast<const rt::Ray*>(d_rays), count, static_cast<rt::Hit*>(d_hits),
                            flags == REINA_RAY_ANY, ctx->err.as<uint32_t>(), ctx->next_fetch_counter(), ctx->sm_count,
-                           ctx->refill, static_cast<cudaStream_t>(stream));
+                           trace_for(ctx, flags, s.triangle_count(), count), static_cast<cudaStream_t>(stream));
         check_cuda(cudaGetLastError(), "raycast launch");
     });
 }
@@ -336,7 +358,8 @@ int reina_raycast(reina_ctx* ctx, const reina_scene* scene, const reina_ray* ray
             rt::Hit* dh = ctx->hits.as<rt::Hit>() + off;
             check_cuda(cudaMemcpyAsync(dr, rays + off, n * sizeof(rt::Ray), cudaMemcpyHostToDevice, st), "cudaMemcpyAsync H2D");
             rt::launch_raycast(s.device_view(), dr, n, dh, flags == REINA_RAY_ANY, ctx->err.as<uint32_t>(),
-                               ctx->next_fetch_counter(), ctx->sm_count, ctx->refill, st);
+                               ctx->next_fetch_counter(), ctx->sm_count, trace_for(ctx, flags, s.triangle_count(), count),
+                               st);
             check_cuda(cudaGetLastError(), "raycast launch");
             check_cuda(cudaMemcpyAsync(hits + off, dh, n * sizeof(rt::Hit), cudaMemcpyDeviceToHost, st), "cudaMemcpyAsync D2H");
         }
@@ -399,7 +422,7 @@ int reina_render_device(reina_ctx* ctx, const reina_scene* scene, const RtPushCo
         need(ctx != nullptr, "ctx is NULL");
         const rt::Scene& s = built_scene(scene);
         rt::RenderOpts r = render_opts(pc, o);
-        r.refill = ctx->refill;
+        r.trace = trace_for(ctx, rt::kTuneRender, s.triangle_count(), (uint64_t)r.width * r.height);
         check_render_scene(s, pc, o);
         need(d_accum != nullptr && ((uintptr_t)d_accum % 16) == 0, "accumulation buffer must be non-NULL and 16-byte aligned");
         use_device(ctx);
@@ -414,7 +437,7 @@ int reina_render_device_noalloc(reina_ctx* ctx, const reina_scene* scene, const 
         need(ctx != nullptr, "ctx is NULL");
         const rt::Scene& s = built_scene(scene);
         rt::RenderOpts r = render_opts(pc, o);
-        r.refill = ctx->refill;
+        r.trace = trace_for(ctx, rt::kTuneRender, s.triangle_count(), (uint64_t)r.width * r.height);
         check_render_scene(s, pc, o);
         need(d_accum != nullptr && ((uintptr_t)d_accum % 16) == 0, "accumulation buffer must be non-NULL and 16-byte aligned");
         use_device(ctx);
@@ -429,7 +452,7 @@ int reina_render(reina_ctx* ctx, const reina_scene* scene, const RtPushConsts* p
         need(ctx != nullptr, "ctx is NULL");
         const rt::Scene& s = built_scene(scene);
         rt::RenderOpts r = render_opts(pc, o);
-        r.refill = ctx->refill;
+        r.trace = trace_for(ctx, rt::kTuneRender, s.triangle_count(), (uint64_t)r.width * r.height);
         check_render_scene(s, pc, o);
         need(accum != nullptr, "accumulation buffer is NULL");
         use_device(ctx);
@@ -459,10 +482,36 @@ int reina_render(reina_ctx* ctx, const reina_scene* scene, const RtPushConsts* p
     });
 }
 
-static rt::BatchEngine& batch_engine(reina_ctx* ctx) {
+// Autotune key of a batch: the triangles of its distinct scenes and its total samples.
+static void batch_key(const reina_render_job* jobs, uint32_t count, uint64_t* tris, uint64_t* samples) {
+    std::unordered_set<const reina_scene*> seen;
+    *tris = 0;
+    *samples = 0;
+    for (uint32_t k = 0; k < count; ++k) {
+        if (seen.insert(jobs[k].scene).second) *tris += jobs[k].scene->s->triangle_count();
+        *samples += (uint64_t)jobs[k].options.width * jobs[k].options.height * jobs[k].push_consts.samplesPerPixel;
+    }
+}
+
+// The context's batch engine, rebuilt when the wanted wave size or traversal variant changed (the
+// cached autotuned ones for this batch when the context uses the cache, else the context's tuning).
+static rt::BatchEngine& batch_engine(reina_ctx* ctx, const reina_render_job* jobs, uint32_t count) {
+    uint32_t wave = ctx->wave_paths;
+    rt::TraceConfig trace = ctx->trace;
+    rt::TuneEntry e;
+    uint64_t tris = 0, samples = 0;
+    batch_key(jobs, count, &tris, &samples);
+    if (ctx->autotune_mode == REINA_AUTOTUNE_CACHED &&
+        ctx->tune.get(rt::kTuneBatch, rt::tune_bucket(tris), rt::tune_bucket(samples), &e)) {
+        trace = e.trace;
+        if (e.wave_paths) wave = e.wave_paths;
+    }
+    if (ctx->batch && (ctx->batch->capacity() != wave || ctx->batch->trace().block != trace.block ||
+                       ctx->batch->trace().stack != trace.stack))
+        ctx->batch.reset();
     if (!ctx->batch)
-        ctx->batch = std::make_unique<rt::BatchEngine>(ctx->device, ctx->sm_count, ctx->wave_paths,
-                                                       (ctx->batch_flags & REINA_BATCH_NO_GRAPHS) == 0);
+        ctx->batch = std::make_unique<rt::BatchEngine>(ctx->device, ctx->sm_count, wave,
+                                                       (ctx->batch_flags & REINA_BATCH_NO_GRAPHS) == 0, trace);
     return *ctx->batch;
 }
 
@@ -488,7 +537,7 @@ static void render_batch(reina_ctx* ctx, const reina_render_job* jobs, uint32_t 
     }
     use_device(ctx);
     const auto t0 = std::chrono::steady_clock::now();
-    rt::BatchEngine& eng = batch_engine(ctx);
+    rt::BatchEngine& eng = batch_engine(ctx, jobs, count);
     std::vector<rt::DeviceBuffer> acc(host ? count : 0), smp(host ? count : 0);
     std::vector<rt::BatchJob*> ptrs(count);
     for (uint32_t k = 0; k < count; ++k) {
@@ -761,6 +810,236 @@ int reina_server_get_stats(reina_server* server, reina_server_stats* out) {
         out->peak_resident_bytes = s.peak_resident_bytes;
         out->budget_bytes = s.budget_bytes;
         out->reserved_bytes = s.reserved_bytes;
+    });
+}
+
+// ------------------------------------------------------------------------------------------------
+// Autotuner
+
+}  // extern "C"
+
+namespace {
+
+// Median device time (ms) of `reps` calls of fn() on `st` after one warm-up call.
+template <class F>
+double time_calls(cudaStream_t st, int reps, F&& fn) {
+    cudaEvent_t e0, e1;
+    check_cuda(cudaEventCreate(&e0), "cudaEventCreate");
+    check_cuda(cudaEventCreate(&e1), "cudaEventCreate");
+    std::vector<float> ms;
+    try {
+        fn();
+        for (int k = 0; k < reps; ++k) {
+            check_cuda(cudaEventRecord(e0, st), "cudaEventRecord");
+            fn();
+            check_cuda(cudaEventRecord(e1, st), "cudaEventRecord");
+            check_cuda(cudaEventSynchronize(e1), "cudaEventSynchronize");
+            float t = 0.0f;
+            check_cuda(cudaEventElapsedTime(&t, e0, e1), "cudaEventElapsedTime");
+            ms.push_back(t);
+        }
+    } catch (...) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        throw;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    std::sort(ms.begin(), ms.end());
+    return ms[ms.size() / 2];
+}
+
+void fill_tuning(const reina_ctx* ctx, const rt::TuneEntry& e, reina_tuning* t) {
+    std::memset(t, 0, sizeof(*t));
+    t->refill = (uint32_t)e.trace.refill;
+    t->trace_block = (uint32_t)e.trace.block;
+    t->trace_stack = (uint32_t)e.trace.stack;
+    t->wave_paths = e.wave_paths ? e.wave_paths : ctx->wave_paths;
+    t->batch_flags = ctx->batch_flags;
+}
+
+void finish_tune(reina_ctx* ctx, uint32_t kind, uint64_t tris, uint64_t size, const rt::TuneEntry& best,
+                 uint32_t candidates, reina_tune_result* out) {
+    const uint32_t tb = rt::tune_bucket(tris), sb = rt::tune_bucket(size);
+    ctx->tune.put(kind, tb, sb, best);
+    if (out) {
+        std::memset(out, 0, sizeof(*out));
+        fill_tuning(ctx, best, &out->best);
+        out->best_ms = best.best_ms;
+        out->default_ms = best.default_ms;
+        out->candidates = candidates;
+        out->kind = kind;
+        out->tri_bucket = tb;
+        out->size_bucket = sb;
+    }
+}
+
+bool is_default(const rt::TraceConfig& c) {
+    return c.refill == 0 && c.block == rt::kTraceBlock && c.stack == rt::kDefaultTraceStack;
+}
+
+}  // namespace
+
+extern "C" {
+
+int reina_autotune_raycast(reina_ctx* ctx, const reina_scene* scene, const void* d_rays, uint64_t count, void* d_hits,
+                           uint32_t flags, void* stream, reina_tune_result* out) {
+    return guard([&] {
+        need(ctx != nullptr, "ctx is NULL");
+        const rt::Scene& s = built_scene(scene);
+        need(flags <= REINA_RAY_ANY, "flags must be REINA_RAY_CLOSEST or REINA_RAY_ANY");
+        need(count > 0 && d_rays && d_hits, "NULL ray or hit buffer");
+        need(((uintptr_t)d_rays % 16) == 0 && ((uintptr_t)d_hits % 16) == 0, "ray and hit buffers must be 16-byte aligned");
+        need(count < (1ull << 32), "at most 2^32 - 1 rays per call");
+        use_device(ctx);
+        cudaStream_t st = static_cast<cudaStream_t>(stream);
+        const auto cands = rt::trace_candidates(true);
+        rt::TuneEntry best;
+        best.best_ms = 1e30;
+        for (const rt::TraceConfig& c : cands) {
+            const double ms = time_calls(st, 3, [&] {
+                rt::launch_raycast(s.device_view(), static_cast<const rt::Ray*>(d_rays), count, static_cast<rt::Hit*>(d_hits),
+                                   flags == REINA_RAY_ANY, ctx->err.as<uint32_t>(), ctx->next_fetch_counter(), ctx->sm_count,
+                                   c, st);
+                check_cuda(cudaGetLastError(), "raycast launch");
+            });
+            if (is_default(c)) best.default_ms = ms;
+            if (ms < best.best_ms) {
+                best.best_ms = ms;
+                best.trace = c;
+            }
+        }
+        const uint32_t e = check_device_errors(ctx, st);
+        if (e) fail(REINA_ERR_DEVICE, "traversal kernel raised error flag " + std::to_string(e));
+        finish_tune(ctx, flags, s.triangle_count(), count, best, (uint32_t)cands.size(), out);
+    });
+}
+
+int reina_autotune_render(reina_ctx* ctx, const reina_scene* scene, const RtPushConsts* pc, const reina_render_options* o,
+                          reina_tune_result* out) {
+    return guard([&] {
+        need(ctx != nullptr, "ctx is NULL");
+        const rt::Scene& s = built_scene(scene);
+        rt::RenderOpts r = render_opts(pc, o);
+        need(!r.megakernel, "the autotuner times the wavefront (options.flags must be 0)");
+        check_render_scene(s, pc, o);
+        use_device(ctx);
+        RtPushConsts one = *pc;
+        one.samplesPerPixel = 1;
+        one.sampleBatch = 0;
+        const size_t P = (size_t)r.width * r.height;
+        ctx->accum.reserve(P * 4 * sizeof(float));
+        cudaStream_t st = ctx->streams[0];
+        const auto cands = rt::trace_candidates(false);
+        rt::TuneEntry best;
+        best.best_ms = 1e30;
+        for (const rt::TraceConfig& c : cands) {
+            r.trace = c;
+            const double ms = time_calls(st, 2, [&] {
+                rt::render_frame(ctx->render, s.device_view(), one, r, ctx->accum.as<float>(), nullptr, ctx->sm_count, st,
+                                 nullptr);
+            });
+            if (is_default(c)) best.default_ms = ms;
+            if (ms < best.best_ms) {
+                best.best_ms = ms;
+                best.trace = c;
+            }
+        }
+        finish_tune(ctx, rt::kTuneRender, s.triangle_count(), P, best, (uint32_t)cands.size(), out);
+    });
+}
+
+int reina_autotune_batch(reina_ctx* ctx, const reina_render_job* jobs, uint32_t count, reina_tune_result* out) {
+    return guard([&] {
+        need(ctx != nullptr, "ctx is NULL");
+        need(count > 0 && jobs != nullptr, "no jobs");
+        uint64_t tris = 0, samples = 0;
+        for (uint32_t k = 0; k < count; ++k) built_scene(jobs[k].scene);
+        batch_key(jobs, count, &tris, &samples);
+        // up to 32 jobs (spread over the list) at no more than 2 samples per pixel, into scratch images
+        const uint32_t n = std::min<uint32_t>(count, 32);
+        std::vector<reina_render_job> sub(n);
+        std::vector<rt::DeviceBuffer> scratch(n);
+        use_device(ctx);
+        for (uint32_t k = 0; k < n; ++k) {
+            sub[k] = jobs[(uint64_t)k * count / n];
+            sub[k].push_consts.samplesPerPixel = std::min<uint32_t>(sub[k].push_consts.samplesPerPixel, 2);
+            sub[k].push_consts.sampleBatch = 0;
+            scratch[k].alloc((size_t)sub[k].options.width * sub[k].options.height * 4 * sizeof(float));
+            sub[k].accum_rgba32f = scratch[k].get();
+            sub[k].samples_rgb32f = nullptr;
+        }
+        const uint32_t saved_wave = ctx->wave_paths;
+        const rt::TraceConfig saved_trace = ctx->trace;
+        const uint32_t saved_mode = ctx->autotune_mode;
+        ctx->autotune_mode = REINA_AUTOTUNE_OFF;
+        cudaStream_t st = ctx->streams[0];
+        rt::TuneEntry best;
+        best.best_ms = 1e30;
+        uint32_t cands = 0;
+        try {
+            for (uint32_t wave : {1u << 20, 1u << 21, 1u << 22})
+                for (int block : {128, 256}) {
+                    rt::TraceConfig c;
+                    c.block = block;
+                    ctx->wave_paths = wave;
+                    ctx->trace = c;
+                    ctx->batch.reset();
+                    const double ms = time_calls(st, 1, [&] { render_batch(ctx, sub.data(), n, false, st, nullptr); });
+                    ++cands;
+                    if (is_default(c) && wave == (uint32_t)REINA_DEFAULT_WAVE_PATHS) best.default_ms = ms;
+                    if (ms < best.best_ms) {
+                        best.best_ms = ms;
+                        best.trace = c;
+                        best.wave_paths = wave;
+                    }
+                }
+        } catch (...) {
+            ctx->wave_paths = saved_wave;
+            ctx->trace = saved_trace;
+            ctx->autotune_mode = saved_mode;
+            ctx->batch.reset();
+            throw;
+        }
+        ctx->wave_paths = saved_wave;
+        ctx->trace = saved_trace;
+        ctx->autotune_mode = saved_mode;
+        ctx->batch.reset();
+        finish_tune(ctx, rt::kTuneBatch, tris, samples, best, cands, out);
+    });
+}
+
+int reina_autotune_set_mode(reina_ctx* ctx, uint32_t mode) {
+    return guard([&] {
+        need(ctx != nullptr, "ctx is NULL");
+        need(mode <= REINA_AUTOTUNE_CACHED, "mode must be REINA_AUTOTUNE_OFF or REINA_AUTOTUNE_CACHED");
+        ctx->autotune_mode = mode;
+    });
+}
+
+int reina_autotune_lookup(reina_ctx* ctx, uint32_t kind, uint64_t triangles, uint64_t size, reina_tuning* out,
+                          int32_t* found) {
+    return guard([&] {
+        need(ctx && out && found, "NULL argument");
+        need(kind <= REINA_TUNE_BATCH, "unknown tune kind");
+        rt::TuneEntry e;
+        *found = ctx->tune.get(kind, rt::tune_bucket(triangles), rt::tune_bucket(size), &e) ? 1 : 0;
+        if (*found) fill_tuning(ctx, e, out);
+        else std::memset(out, 0, sizeof(*out));
+    });
+}
+
+int reina_autotune_save(reina_ctx* ctx, const char* path) {
+    return guard([&] {
+        need(ctx && path, "NULL argument");
+        ctx->tune.save(path);
+    });
+}
+
+int reina_autotune_load(reina_ctx* ctx, const char* path) {
+    return guard([&] {
+        need(ctx && path, "NULL argument");
+        ctx->tune.load(path);
     });
 }
 

@@ -17,9 +17,20 @@ constexpr int kTraceBlock = 128;
 // ray-cast workload: 0.91 ms vs 1.04 ms for the best refill threshold).
 constexpr int kDefaultRefill = 0;
 
+// Launch configuration of the traversal kernels: block size (64, 128, 256) and shared-memory stack
+// entries per thread (8, 12, 16) of the grid form, or the persistent form with its refill threshold
+// (refill > 0; block 128, stack 12).
+constexpr int kDefaultTraceStack = 12;
+struct TraceConfig {
+    int block = kTraceBlock;
+    int stack = kDefaultTraceStack;
+    int refill = kDefaultRefill;
+};
+bool valid_trace_config(const TraceConfig& c);
+
 // `d_next` is a device u32 used as the ray-fetch counter (reset by the launcher); n < 2^32.
 void launch_raycast(const DeviceScene& s, const Ray* d_rays, uint64_t n, Hit* d_hits, bool any, uint32_t* d_err,
-                    uint32_t* d_next, int sm_count, int refill, cudaStream_t st);
+                    uint32_t* d_next, int sm_count, const TraceConfig& cfg, cudaStream_t st);
 void launch_raycast_counters(const DeviceScene& s, const Ray* d_rays, uint64_t n, bool any,
                              unsigned long long* d_counters, uint32_t* d_err, uint32_t* d_next, int sm_count,
                              cudaStream_t st);

@@ -62,8 +62,9 @@ __global__ void __launch_bounds__(kBlock) k_init(RenderLaunch L) {
 
 // ------------------------------------------------------------------------------------------------
 // extend: closest hit + classification.  Grid form: each warp takes 32 consecutive queue entries.
-__global__ void __launch_bounds__(kBlock) k_extend_grid(RenderLaunch L, int cur) {
-    __shared__ uint2 stack[kSmemStack * kBlock];
+template <int BLOCK, int SS>
+__global__ void __launch_bounds__(BLOCK) k_extend_grid(RenderLaunch L, int cur) {
+    __shared__ uint2 stack[SS * BLOCK];
     const PathState& ps = L.ps;
     const uint32_t n = ps.counters[kCntActive + cur];
     const uint32_t* q = ps.q_active[cur];
@@ -78,7 +79,8 @@ __global__ void __launch_bounds__(kBlock) k_extend_grid(RenderLaunch L, int cur)
             Hit h;
             TraceCounters c{0u, 0u};
             uint32_t e = 0;
-            if (L.s.node_count) e = traverse<false, false, true>(L.s.nodes, L.s.tris, r, stack + threadIdx.x, kBlock, h, c);
+            if (L.s.node_count)
+                e = traverse<false, false, true, SS>(L.s.nodes, L.s.tris, r, stack + threadIdx.x, BLOCK, h, c);
             else h.prim = kMiss;
             if (e) atomicOr(ps.counters + kCntError, e);
             ps.hprim[p] = h.prim;
@@ -223,8 +225,9 @@ __global__ void __launch_bounds__(kBlock) k_shade_miss(RenderLaunch L) {
 }
 
 // nee.h.glsl:126-144: any hit in [0, dist - 0.001]; unoccluded contributions are added.  Grid form.
-__global__ void __launch_bounds__(kBlock) k_shadow_grid(RenderLaunch L) {
-    __shared__ uint2 stack[kSmemStack * kBlock];
+template <int BLOCK, int SS>
+__global__ void __launch_bounds__(BLOCK) k_shadow_grid(RenderLaunch L) {
+    __shared__ uint2 stack[SS * BLOCK];
     const PathState& ps = L.ps;
     const uint32_t n = ps.counters[kCntShadow];
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
@@ -236,7 +239,8 @@ __global__ void __launch_bounds__(kBlock) k_shadow_grid(RenderLaunch L) {
             Hit h;
             TraceCounters c{0u, 0u};
             uint32_t e = 0;
-            if (L.s.node_count) e = traverse<true, false, false>(L.s.nodes, L.s.tris, r, stack + threadIdx.x, kBlock, h, c);
+            if (L.s.node_count)
+                e = traverse<true, false, false, SS>(L.s.nodes, L.s.tris, r, stack + threadIdx.x, BLOCK, h, c);
             else h.prim = kMiss;
             if (e) atomicOr(ps.counters + kCntError, e);
             if (h.prim == kMiss) {
@@ -489,7 +493,7 @@ static void launch_frame(const PathState& ps, const DeviceScene& s, const RtPush
     for (int k = 0; k < 3; ++k) L.env[k] = opt.env_color[k];
     L.accum = d_accum;
     L.samples = d_samples;
-    L.refill = opt.refill;
+    L.refill = opt.trace.refill;
 
     static int g_ext = 0, g_sh = 0, g_shade[5] = {0, 0, 0, 0, 0}, g_simple = 0;
     static int g_sm = -1;
@@ -524,16 +528,36 @@ static void launch_frame(const PathState& ps, const DeviceScene& s, const RtPush
             check_cuda(cudaMemsetAsync(cnt + kCntActive + (cur ^ 1), 0, sizeof(uint32_t), st), "cudaMemsetAsync");
             check_cuda(cudaMemsetAsync(cnt + kCntQueue, 0, 6 * sizeof(uint32_t), st), "cudaMemsetAsync");
             check_cuda(cudaMemsetAsync(cnt + kCntFetchExtend, 0, 2 * sizeof(uint32_t), st), "cudaMemsetAsync");
-            if (opt.refill > 0) k_extend<<<g_ext, kBlock, 0, st>>>(L, cur);
-            else k_extend_grid<<<g_ext, kBlock, 0, st>>>(L, cur);
+            if (opt.trace.refill > 0) {
+                k_extend<<<g_ext, kBlock, 0, st>>>(L, cur);
+            } else {
+                with_trace_variant(opt.trace, [&](auto B, auto S) {
+                    static int grid = 0, grid_sm = -1;
+                    if (grid_sm != sm_count) {
+                        grid = resident_grid((const void*)k_extend_grid<B.value, S.value>, B.value, sm_count);
+                        grid_sm = sm_count;
+                    }
+                    k_extend_grid<B.value, S.value><<<grid, B.value, 0, st>>>(L, cur);
+                });
+            }
             k_shade_miss<<<simple_blocks, kBlock, 0, st>>>(L);
             k_shade<1><<<g_shade[1], kBlock, 0, st>>>(L, cur);
             k_shade<2><<<g_shade[2], kBlock, 0, st>>>(L, cur);
             k_shade<3><<<g_shade[3], kBlock, 0, st>>>(L, cur);
             k_shade<4><<<g_shade[4], kBlock, 0, st>>>(L, cur);
             if (opt.mode == kModeNeeMis) {
-                if (opt.refill > 0) k_shadow<<<g_sh, kBlock, 0, st>>>(L);
-                else k_shadow_grid<<<g_sh, kBlock, 0, st>>>(L);
+                if (opt.trace.refill > 0) {
+                    k_shadow<<<g_sh, kBlock, 0, st>>>(L);
+                } else {
+                    with_trace_variant(opt.trace, [&](auto B, auto S) {
+                        static int grid = 0, grid_sm = -1;
+                        if (grid_sm != sm_count) {
+                            grid = resident_grid((const void*)k_shadow_grid<B.value, S.value>, B.value, sm_count);
+                            grid_sm = sm_count;
+                        }
+                        k_shadow_grid<B.value, S.value><<<grid, B.value, 0, st>>>(L);
+                    });
+                }
             }
             cur ^= 1;
         }

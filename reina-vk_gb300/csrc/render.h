@@ -7,6 +7,7 @@
 
 #include "device_scene.h"
 #include "errors.h"
+#include "kernels.h"
 #include "../../include/reina/polyglot.h"
 
 namespace rt {
@@ -20,7 +21,7 @@ struct RenderOpts {
     uint32_t env_mode = 0;          // 0 sky gradient (raytrace.rmiss.glsl), 1 constant colour
     float env_color[3] = {0, 0, 0};
     bool megakernel = false;        // plain form: one kernel, one thread per pixel (no queues)
-    int refill = 0;                 // traversal form: 0 grid, 1..32 persistent (idle lanes that trigger a fetch)
+    TraceConfig trace;              // traversal kernels' launch configuration (same images for every setting)
 };
 
 // Queue indices of the per-material shade queues (0 = miss, then material_idx + 1).

@@ -166,26 +166,48 @@ __device__ __forceinline__ void refine_hit(const TraceRay& r, const float4& a4, 
     h.t = __fadd_rn(t0, __fdiv_rn(dot2_f(e20, e21, e22, q0, q1, q2), det));
 }
 
-// Byte `byte` of `word` as a float, exactly: the byte placed in the mantissa of 2^23 (one byte permute),
-// minus 2^23 (one add) — cheaper than an integer-to-float conversion.
-__device__ __forceinline__ float u8f(uint32_t word, int byte) {
-    return __uint_as_float(__byte_perm(word, 0x4B000000u, 0x7540u + (uint32_t)byte)) - 8388608.0f;
+// Byte `byte` of `word` as the float 1 + q * 2^-15, exactly: the byte placed in mantissa bits 8..15 of
+// 1.0 by one byte permute (no conversion or subtraction).
+__device__ __forceinline__ float q15(uint32_t word, int byte) {
+    return __uint_as_float(__byte_perm(word, 0x3F800000u, 0x7604u | ((uint32_t)byte << 4)));
+}
+
+// Three-input minimum / maximum (single instructions on sm_100 and later).
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+    float d;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+__device__ __forceinline__ float min3f(float a, float b, float c) {
+    float d;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+
+// Node meta bytes with the octant applied: internal children (meta bits 3 and 4 both set; leaf offsets
+// are below 24) get their bit index XOR-ed with the ray's inverse octant, four children per word.
+__device__ __forceinline__ uint32_t octant_meta(uint32_t m, uint32_t oct_inv) {
+    const uint32_t inner = (m & (m << 1)) & 0x10101010u;
+    return m ^ ((inner >> 4) * oct_inv);
 }
 
 // Intersects the 8 quantized child boxes of one node; returns the hit mask in the CWBVH layout
 // (bits 24..31: internal children, reordered by the ray octant; bits 0..23: leaf triangles).
+// A child plane at q quanta is at t = (1 + q 2^-15) S + O with S = 2^15 quanta in t units and
+// O = (p - o) / d - S: one byte permute and one FMA per plane.  Forming O adds one rounding of at most
+// 2^-9 quanta (2^-24 of |S|), which the builder's 2^-8-quantum margin around every child box covers.
+// Empty slots have meta 0 and contribute nothing to the mask.
 __device__ __forceinline__ uint32_t intersect_children(const TraceRay& r, const uint4& w0, const uint4& w1,
                                                        const uint4& w2, const uint4& w3, const uint4& w4,
                                                        float tmax) {
     const float px = __uint_as_float(w0.x), py = __uint_as_float(w0.y), pz = __uint_as_float(w0.z);
     const uint32_t ex = w0.w & 0xFFu, ey = (w0.w >> 8) & 0xFFu, ez = (w0.w >> 16) & 0xFFu;
-    const uint32_t imask = w0.w >> 24;
-    const float sxd = __uint_as_float(ex << 23) * r.idx;
-    const float syd = __uint_as_float(ey << 23) * r.idy;
-    const float szd = __uint_as_float(ez << 23) * r.idz;
-    const float oxd = (px - r.ox) * r.idx;
-    const float oyd = (py - r.oy) * r.idy;
-    const float ozd = (pz - r.oz) * r.idz;
+    const float sx = __uint_as_float((ex + 15u) << 23) * r.idx;
+    const float sy = __uint_as_float((ey + 15u) << 23) * r.idy;
+    const float sz = __uint_as_float((ez + 15u) << 23) * r.idz;
+    const float ox = (px - r.ox) * r.idx - sx;
+    const float oy = (py - r.oy) * r.idy - sy;
+    const float oz = (pz - r.oz) * r.idz - sz;
     // Near/far plane words by direction sign (qlo_x = w2.xy, qlo_y = w2.zw, qlo_z = w3.xy,
     // qhi_x = w3.zw, qhi_y = w4.xy, qhi_z = w4.zw).
     const bool nx = r.idx < 0.0f, ny = r.idy < 0.0f, nz = r.idz < 0.0f;
@@ -195,24 +217,22 @@ __device__ __forceinline__ uint32_t intersect_children(const TraceRay& r, const 
     const uint32_t fary0 = ny ? w2.z : w4.x, fary1 = ny ? w2.w : w4.y;
     const uint32_t nearz0 = nz ? w4.z : w3.x, nearz1 = nz ? w4.w : w3.y;
     const uint32_t farz0 = nz ? w3.x : w4.z, farz1 = nz ? w3.y : w4.w;
+    const uint32_t meta0 = octant_meta(w1.z, r.oct_inv), meta1 = octant_meta(w1.w, r.oct_inv);
     uint32_t hitmask = 0;
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
         const int b = i & 3;
-        const uint32_t meta_word = i < 4 ? w1.z : w1.w;
-        const uint32_t meta = (meta_word >> (8 * b)) & 0xFFu;
-        const float tnx = fmaf(u8f(i < 4 ? nearx0 : nearx1, b), sxd, oxd);
-        const float tny = fmaf(u8f(i < 4 ? neary0 : neary1, b), syd, oyd);
-        const float tnz = fmaf(u8f(i < 4 ? nearz0 : nearz1, b), szd, ozd);
-        const float tfx = fmaf(u8f(i < 4 ? farx0 : farx1, b), sxd, oxd);
-        const float tfy = fmaf(u8f(i < 4 ? fary0 : fary1, b), syd, oyd);
-        const float tfz = fmaf(u8f(i < 4 ? farz0 : farz1, b), szd, ozd);
-        const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, r.tmin));
-        const float tf = fminf(fminf(tfx, tfy), fminf(tfz, tmax));
-        if (tn <= tf && meta != 0u) {
-            const uint32_t inner = (imask >> i) & 1u;
-            const uint32_t bit = (meta & 31u) ^ (inner ? r.oct_inv : 0u);
-            hitmask |= (meta >> 5) << bit;
+        const float tnx = fmaf(q15(i < 4 ? nearx0 : nearx1, b), sx, ox);
+        const float tny = fmaf(q15(i < 4 ? neary0 : neary1, b), sy, oy);
+        const float tnz = fmaf(q15(i < 4 ? nearz0 : nearz1, b), sz, oz);
+        const float tfx = fmaf(q15(i < 4 ? farx0 : farx1, b), sx, ox);
+        const float tfy = fmaf(q15(i < 4 ? fary0 : fary1, b), sy, oy);
+        const float tfz = fmaf(q15(i < 4 ? farz0 : farz1, b), sz, oz);
+        const float tn = fmaxf(max3f(tnx, tny, tnz), r.tmin);
+        const float tf = fminf(min3f(tfx, tfy, tfz), tmax);
+        if (tn <= tf) {
+            const uint32_t meta = ((i < 4 ? meta0 : meta1) >> (8 * b)) & 0xFFu;
+            hitmask |= (meta >> 5) << (meta & 31u);
         }
     }
     return hitmask;
@@ -246,38 +266,65 @@ __device__ __forceinline__ void trav_init(const TraceRay& r, TravState& s, Hit& 
     hit.v = 0.0f;
 }
 
-// One traversal step: visits the nearest pending child node and tests the triangles of its leaf
-// children.  Returns true when the ray is finished.
-template <bool ANY, bool COUNT>
+// Triangle postponing (Ylitie, Karras and Laine, "Efficient Incoherent Ray Traversal on GPUs Through
+// Compressed Wide BVHs", HPG 2017): a lane with triangles to test defers them (pushes its triangle group
+// on the stack and goes on with nodes) while fewer than kPostpone/32 of the warp's traversing lanes have
+// triangles too, so that triangle tests run with more lanes active.  0 disables postponing; any-hit
+// traversal never postpones (its rays end at the first hit found).
+#ifndef RT_POSTPONE
+#define RT_POSTPONE 6
+#endif
+constexpr int kPostpone = RT_POSTPONE;
+
+// One traversal step.  Stack entries and the current group are node groups (child base, node hits in
+// bits 24..31 | internal mask) or postponed triangle groups (triangle base, triangle hits in bits
+// 0..23, bits 24..31 zero).  A step visits the nearest pending child node (or takes a popped triangle
+// group) and tests the group's triangles unless it postpones them.  Returns true when the ray is done.
+template <bool ANY, bool COUNT, int SS = kSmemStack>
 __device__ __forceinline__ bool trav_step(const Bvh8Node* __restrict__ nodes, const TriRecord* __restrict__ tris,
                                           const TraceRay& r, TravState& s, Hit& hit, uint2* stack, int stride,
                                           uint2* spill, TraceCounters& cnt, uint32_t& err) {
     if (++s.steps > kMaxTraversalSteps) { err |= kErrStepLimit; return true; }
+    constexpr bool kPost = kPostpone > 0 && !ANY;   // any-hit rays stop at their first hit: never postpone
+    const uint32_t traversing = kPost ? (uint32_t)__popc(__activemask()) : 0u;
     const uint4* nptr = reinterpret_cast<const uint4*>(nodes);
     const float4* tptr = reinterpret_cast<const float4*>(tris);
-    // s.group.y holds node hits in bits 24..31 here.
-    const uint32_t slot_bit = 31u - __clz(s.group.y);
-    const uint32_t slot = (slot_bit - 24u) ^ r.oct_inv;
-    const uint32_t rel = __popc(s.group.y & ((1u << slot) - 1u));
-    const uint32_t child = s.group.x + rel;
-    s.group.y &= ~(1u << slot_bit);
+    uint2 tgroup;
     if (s.group.y > 0x00FFFFFFu) {
-        if (s.sp < kSmemStack) stack[s.sp * stride] = s.group;
-        else if (s.sp < kTotalStack) spill[s.sp - kSmemStack] = s.group;
-        else { err |= kErrStackOverflow; return true; }
-        ++s.sp;
+        const uint32_t slot_bit = 31u - __clz(s.group.y);
+        const uint32_t slot = (slot_bit - 24u) ^ r.oct_inv;
+        const uint32_t rel = __popc(s.group.y & ((1u << slot) - 1u));
+        const uint32_t child = s.group.x + rel;
+        s.group.y &= ~(1u << slot_bit);
+        if (s.group.y > 0x00FFFFFFu) {
+            if (s.sp < SS) stack[s.sp * stride] = s.group;
+            else if (s.sp < kTotalStack) spill[s.sp - SS] = s.group;
+            else { err |= kErrStackOverflow; return true; }
+            ++s.sp;
+        }
+        const uint4* np = nptr + 5ull * child;
+        const uint4 w0 = __ldg(np + 0), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3), w4 = __ldg(np + 4);
+        if (COUNT) cnt.nodes++;
+        const uint32_t hm = intersect_children(r, w0, w1, w2, w3, w4, s.best_t);
+        s.group = make_uint2(w1.x, (hm & 0xFF000000u) | (w0.w >> 24));
+        tgroup = make_uint2(w1.y, hm & 0x00FFFFFFu);
+    } else {
+        tgroup = s.group;   // a postponed triangle group
+        s.group = make_uint2(0u, 0u);
     }
-    const uint4* np = nptr + 5ull * child;
-    const uint4 w0 = __ldg(np + 0), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3), w4 = __ldg(np + 4);
-    if (COUNT) cnt.nodes++;
-    const uint32_t hm = intersect_children(r, w0, w1, w2, w3, w4, s.best_t);
-    s.group = make_uint2(w1.x, (hm & 0xFF000000u) | (w0.w >> 24));
-    uint32_t thits = hm & 0x00FFFFFFu;
-    const uint32_t tri_base = w1.y;
-    while (thits) {
-        const int k = __ffs(thits) - 1;
-        thits &= thits - 1u;
-        const float4* tp = tptr + 3ull * (tri_base + (uint32_t)k);
+    while (tgroup.y) {
+        if (kPost && s.sp < kTotalStack) {
+            const uint32_t with_tris = (uint32_t)__popc(__activemask());
+            if (with_tris * 32u < traversing * (uint32_t)kPostpone) {
+                if (s.sp < SS) stack[s.sp * stride] = tgroup;
+                else spill[s.sp - SS] = tgroup;
+                ++s.sp;
+                break;
+            }
+        }
+        const int k = __ffs(tgroup.y) - 1;
+        tgroup.y &= tgroup.y - 1u;
+        const float4* tp = tptr + 3ull * (tgroup.x + (uint32_t)k);
         const float4 a = __ldg(tp + 0), b = __ldg(tp + 1), c = __ldg(tp + 2);
         if (COUNT) cnt.tris++;
         float t, u, v;
@@ -285,20 +332,20 @@ __device__ __forceinline__ bool trav_step(const Bvh8Node* __restrict__ nodes, co
             const uint32_t prim = __float_as_uint(a.w);
             if (ANY) {
                 hit.prim = prim; hit.t = t; hit.u = u; hit.v = v;
-                s.best_rec = tri_base + (uint32_t)k;
+                s.best_rec = tgroup.x + (uint32_t)k;
                 return true;
             }
             if (t < s.best_t || prim < hit.prim) {   // t <= best_t holds; equal t: lower id wins
                 s.best_t = t;
                 hit.prim = prim; hit.t = t; hit.u = u; hit.v = v;
-                s.best_rec = tri_base + (uint32_t)k;
+                s.best_rec = tgroup.x + (uint32_t)k;
             }
         }
     }
     if (s.group.y <= 0x00FFFFFFu) {
         if (s.sp == 0) return true;
         --s.sp;
-        s.group = s.sp < kSmemStack ? stack[s.sp * stride] : spill[s.sp - kSmemStack];
+        s.group = s.sp < SS ? stack[s.sp * stride] : spill[s.sp - SS];
     }
     return false;
 }
@@ -318,15 +365,15 @@ __device__ __forceinline__ void trav_finish(const Bvh8Node* __restrict__ nodes, 
 
 // Traverses the BVH8 for one ray to completion.  `stack` points at this thread's first shared-memory
 // stack entry; consecutive entries are `stride` elements apart.  Returns an error code (0 = ok).
-template <bool ANY, bool COUNT, bool REFINE = true>
+template <bool ANY, bool COUNT, bool REFINE = true, int SS = kSmemStack>
 __device__ __forceinline__ uint32_t traverse(const Bvh8Node* __restrict__ nodes, const TriRecord* __restrict__ tris,
                                              const TraceRay& r, uint2* stack, int stride, Hit& hit,
                                              TraceCounters& cnt) {
     TravState s;
     trav_init(r, s, hit);
-    uint2 spill[kTotalStack - kSmemStack];
+    uint2 spill[kTotalStack - SS];
     uint32_t err = 0;
-    while (!trav_step<ANY, COUNT>(nodes, tris, r, s, hit, stack, stride, spill, cnt, err)) {
+    while (!trav_step<ANY, COUNT, SS>(nodes, tris, r, s, hit, stack, stride, spill, cnt, err)) {
     }
     trav_finish<REFINE>(nodes, tris, r, s, hit);
     return err;
@@ -340,12 +387,12 @@ __device__ __forceinline__ uint32_t traverse(const Bvh8Node* __restrict__ nodes,
 //   store(idx, hit, valid): called by all 32 lanes after every step; valid marks lanes that finished
 //   an item in that step (store may use warp-collective operations).
 // Requires blockDim.x to be a multiple of 32.
-template <bool ANY, bool COUNT, bool REFINE, class Load, class Store>
+template <bool ANY, bool COUNT, bool REFINE, class Load, class Store, int SS = kSmemStack>
 __device__ __forceinline__ uint32_t persistent_trace(const Bvh8Node* __restrict__ nodes, const TriRecord* __restrict__ tris,
                                                      uint32_t node_count, uint32_t n, uint32_t* next, uint2* stack,
                                                      int stride, int refill, Load load, Store store, TraceCounters& cnt) {
     const uint32_t lane = threadIdx.x & 31u;
-    uint2 spill[kTotalStack - kSmemStack];
+    uint2 spill[kTotalStack - SS];
     uint32_t err = 0;
     bool has = false, exhausted = false;
     uint32_t idx = 0;
@@ -377,7 +424,7 @@ __device__ __forceinline__ uint32_t persistent_trace(const Bvh8Node* __restrict_
         if (exhausted && __ballot_sync(0xFFFFFFFFu, has) == 0u) break;
         bool done = false;
         if (has) {
-            done = trav_step<ANY, COUNT>(nodes, tris, r, st, hit, stack, stride, spill, cnt, err);
+            done = trav_step<ANY, COUNT, SS>(nodes, tris, r, st, hit, stack, stride, spill, cnt, err);
             if (done) {
                 trav_finish<REFINE>(nodes, tris, r, st, hit);
                 has = false;

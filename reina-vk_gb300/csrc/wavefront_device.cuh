@@ -6,7 +6,12 @@
 
 #include <stdint.h>
 
+#include <type_traits>
+
+#include <cuda_runtime.h>
+
 #include "device_scene.h"
+#include "kernels.h"
 #include "render.h"
 #include "shading_device.cuh"
 
@@ -313,6 +318,27 @@ __device__ __forceinline__ void camera_ray(const RtPushConsts& pc, uint32_t W, u
     const V3 up = norm3(V3{V[4], V[5], V[6]});
     o = origin + right * lx + up * ly;
     d = norm3(focal - o);
+}
+
+// Host: calls f(std::integral_constant<int, BLOCK>, std::integral_constant<int, STACK>) for the traversal
+// kernels' configured block size (64, 128, 256) and shared-memory stack depth (8, 12, 16).
+template <class F>
+inline void with_trace_variant(const TraceConfig& c, F&& f) {
+    auto by_stack = [&](auto blk) {
+        if (c.stack == 8) f(blk, std::integral_constant<int, 8>{});
+        else if (c.stack == 16) f(blk, std::integral_constant<int, 16>{});
+        else f(blk, std::integral_constant<int, 12>{});
+    };
+    if (c.block == 64) by_stack(std::integral_constant<int, 64>{});
+    else if (c.block == 256) by_stack(std::integral_constant<int, 256>{});
+    else by_stack(std::integral_constant<int, 128>{});
+}
+
+// Host: resident blocks of `kernel` at `block` threads, times the SM count (grid of a grid-stride kernel).
+inline int resident_grid(const void* kernel, int block, int sm_count) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0);
+    return (per_sm > 0 ? per_sm : 1) * (sm_count > 0 ? sm_count : 1);
 }
 
 }  // namespace rt

@@ -84,7 +84,10 @@ class _CtxOptions(C.Structure):
 
 class _Tuning(C.Structure):
     _fields_ = [("refill", C.c_uint32), ("wave_paths", C.c_uint32), ("batch_flags", C.c_uint32),
-                ("reserved", C.c_uint32)]
+                ("trace_block", C.c_uint32), ("trace_stack", C.c_uint32), ("reserved", C.c_uint32 * 3)]
+
+
+TUNING_FIELDS = ("refill", "wave_paths", "batch_flags", "trace_block", "trace_stack")
 
 
 DEFAULT_WAVE_PATHS = 2097152
@@ -148,6 +151,15 @@ class _ServerStats(C.Structure):
 
 
 REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED, REQ_CANCELLED = range(5)
+
+
+class _TuneResult(C.Structure):
+    _fields_ = [("best", _Tuning), ("best_ms", C.c_double), ("default_ms", C.c_double), ("candidates", C.c_uint32),
+                ("kind", C.c_uint32), ("tri_bucket", C.c_uint32), ("size_bucket", C.c_uint32)]
+
+
+TUNE_RAYCAST_CLOSEST, TUNE_RAYCAST_ANY, TUNE_RENDER, TUNE_BATCH = range(4)
+AUTOTUNE_OFF, AUTOTUNE_CACHED = 0, 1
 
 
 class _RenderJob(C.Structure):
@@ -270,6 +282,13 @@ def load_library() -> C.CDLL:
         "reina_render_device": (I32, [P, P, C.POINTER(RtPushConsts), C.POINTER(RenderOptions), P, P, P]),
         "reina_render_device_noalloc": (I32, [P, P, C.POINTER(RtPushConsts), C.POINTER(RenderOptions), P, P, P]),
         "reina_render_batch": (I32, [P, C.POINTER(_RenderJob), U32, C.POINTER(_RenderStats)]),
+        "reina_autotune_raycast": (I32, [P, P, P, U64, P, U32, P, C.POINTER(_TuneResult)]),
+        "reina_autotune_render": (I32, [P, P, C.POINTER(RtPushConsts), C.POINTER(RenderOptions), C.POINTER(_TuneResult)]),
+        "reina_autotune_batch": (I32, [P, C.POINTER(_RenderJob), U32, C.POINTER(_TuneResult)]),
+        "reina_autotune_set_mode": (I32, [P, U32]),
+        "reina_autotune_lookup": (I32, [P, U32, U64, U64, C.POINTER(_Tuning), C.POINTER(C.c_int32)]),
+        "reina_autotune_save": (I32, [P, C.c_char_p]),
+        "reina_autotune_load": (I32, [P, C.c_char_p]),
         "reina_server_create": (I32, [P, C.POINTER(_ServerOptions), C.POINTER(P)]),
         "reina_server_destroy": (None, [P]),
         "reina_server_add_scene": (I32, [P, P, C.POINTER(U32)]),
@@ -344,14 +363,14 @@ class Context:
     def tuning(self) -> dict:
         t = _Tuning()
         _check(_lib.reina_ctx_get_tuning(self._h, C.byref(t)))
-        return {"refill": int(t.refill), "wave_paths": int(t.wave_paths), "batch_flags": int(t.batch_flags)}
+        return {k: int(getattr(t, k)) for k in TUNING_FIELDS}
 
     def set_tuning(self, **kw) -> None:
-        """reina_ctx_set_tuning with the given fields changed (refill, wave_paths, batch_flags)."""
+        """reina_ctx_set_tuning with the given fields changed (TUNING_FIELDS)."""
         t = _Tuning()
         _check(_lib.reina_ctx_get_tuning(self._h, C.byref(t)))
         for k, v in kw.items():
-            if k not in ("refill", "wave_paths", "batch_flags"):
+            if k not in TUNING_FIELDS:
                 raise TypeError(f"unknown tuning field {k}")
             setattr(t, k, int(v))
         _check(_lib.reina_ctx_set_tuning(self._h, C.byref(t)))
@@ -674,6 +693,53 @@ class Server:
         st = _ServerStats()
         _check(_lib.reina_server_get_stats(self.handle, C.byref(st)))
         return {n: getattr(st, n) for n in _SERVER_STAT_FIELDS}
+
+
+def _tune_result(r: _TuneResult) -> dict:
+    return {"best": {k: int(getattr(r.best, k)) for k in TUNING_FIELDS}, "best_ms": r.best_ms,
+            "default_ms": r.default_ms, "candidates": int(r.candidates), "kind": int(r.kind),
+            "tri_bucket": int(r.tri_bucket), "size_bucket": int(r.size_bucket)}
+
+
+def autotune_raycast(ctx: Context, scene: Scene, d_rays: int, count: int, d_hits: int, flags: int = RAY_CLOSEST,
+                     stream: int = 0) -> dict:
+    r = _TuneResult()
+    _check(_lib.reina_autotune_raycast(ctx.handle, scene.handle, C.c_void_p(d_rays), count, C.c_void_p(d_hits), flags,
+                                       C.c_void_p(stream), C.byref(r)))
+    return _tune_result(r)
+
+
+def autotune_render(ctx: Context, scene: Scene, pc: RtPushConsts, opts: RenderOptions) -> dict:
+    r = _TuneResult()
+    _check(_lib.reina_autotune_render(ctx.handle, scene.handle, C.byref(pc), C.byref(opts), C.byref(r)))
+    return _tune_result(r)
+
+
+def autotune_batch(ctx: Context, jobs: list) -> dict:
+    """Times batch configurations on (up to 32 of) the jobs; jobs are RenderJob or DeviceRenderJob."""
+    arr = _jobs_array(jobs, isinstance(jobs[0], DeviceRenderJob))
+    r = _TuneResult()
+    _check(_lib.reina_autotune_batch(ctx.handle, arr, len(jobs), C.byref(r)))
+    return _tune_result(r)
+
+
+def autotune_set_mode(ctx: Context, mode: int) -> None:
+    _check(_lib.reina_autotune_set_mode(ctx.handle, mode))
+
+
+def autotune_lookup(ctx: Context, kind: int, triangles: int, work_size: int) -> dict | None:
+    t = _Tuning()
+    found = C.c_int32()
+    _check(_lib.reina_autotune_lookup(ctx.handle, kind, triangles, work_size, C.byref(t), C.byref(found)))
+    return {k: int(getattr(t, k)) for k in TUNING_FIELDS} if found.value else None
+
+
+def autotune_save(ctx: Context, path) -> None:
+    _check(_lib.reina_autotune_save(ctx.handle, str(path).encode()))
+
+
+def autotune_load(ctx: Context, path) -> None:
+    _check(_lib.reina_autotune_load(ctx.handle, str(path).encode()))
 
 
 NOALLOC_MAX_PIXELS = 65536

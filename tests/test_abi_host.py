@@ -136,7 +136,7 @@ def test_bvh8_structure_is_complete_and_conservative(R, host_ctx, level):
     assert st["triangle_count"] == ntri
     nodes, tris = s.export_bvh()
     assert 1 <= st["max_depth"] <= 64
-    tri_v = tris.reshape(-1, 12).view(np.float32) if False else tris.copy().view(np.float32).reshape(-1, 12)
+    tri_v = tris.copy().view(np.float32).reshape(-1, 12)
     prims = tris.copy().view(np.uint32).reshape(-1, 12)[:, 3]
     assert np.array_equal(np.sort(prims), np.arange(ntri, dtype=np.uint32))
     world = v[i.reshape(-1, 3)][:, :, :3].astype(np.float32)
@@ -180,6 +180,9 @@ def test_bvh8_structure_is_complete_and_conservative(R, host_ctx, level):
                     seen_tris[prims[t0 + k]] = True
                 clo, chi = pts.min(axis=0), pts.max(axis=0)
             assert (blo < clo).all() and (bhi > chi).all(), "quantized box must strictly contain its content"
+            # the traversal's plane offsets may round up to 2^-9 quanta inward: the builder keeps at
+            # least 2^-8 quanta of margin around the content
+            assert (clo - blo >= scale / 256).all() and (bhi - chi >= scale / 256).all()
             lo_all = np.minimum(lo_all, clo)
             hi_all = np.maximum(hi_all, chi)
         assert inner_rank == bin(int(imask[n])).count("1")

@@ -1,0 +1,103 @@
+"""The autotuner on the GPU: every traversal variant it chooses between (grid form in three block sizes
+x three stack depths, persistent form) gives bit-identical hits; autotuned ray casts, renders and batched
+renders pick a valid configuration, cache it, and with the cache in use give exactly the results of the
+default configuration."""
+import numpy as np
+import pytest
+
+import scenes
+
+pytestmark = pytest.mark.gpu
+
+VARIANTS = [dict(refill=0, trace_block=b, trace_stack=s) for b in (64, 128, 256) for s in (8, 12, 16)] + \
+           [dict(refill=8, trace_block=128, trace_stack=12), dict(refill=16, trace_block=128, trace_stack=12)]
+
+
+@pytest.fixture(scope="module")
+def rc_setup(R):
+    import torch
+
+    ctx = R.Context(0)
+    scene, v, i = scenes.sphere_scene(R, ctx, 5)
+    rays = scenes.raycast_rays(R, 5, 256, 256, 65536, v)
+    n = rays.shape[0]
+    d_rays = torch.from_numpy(rays.view(np.float32).reshape(n, 8).copy()).cuda()
+    yield ctx, scene, d_rays, n
+    scene.close()
+    ctx.close()
+
+
+@pytest.mark.parametrize("flags", [0, 1])
+def test_all_variants_give_identical_hits(R, rc_setup, flags):
+    import torch
+
+    ctx, scene, d_rays, n = rc_setup
+    ref = None
+    for v in VARIANTS:
+        ctx.set_tuning(**v)
+        d_hits = torch.empty((n, 4), dtype=torch.float32, device="cuda")
+        R.raycast_device(ctx, scene, d_rays.data_ptr(), n, d_hits.data_ptr(), flags, torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        h = d_hits.cpu().numpy().view(np.uint32)
+        if ref is None:
+            ref = h
+        else:
+            assert np.array_equal(h, ref), v
+    ctx.set_tuning(refill=0, trace_block=128, trace_stack=12)
+
+
+def test_autotune_raycast_caches_and_applies(R, rc_setup):
+    import torch
+
+    ctx, scene, d_rays, n = rc_setup
+    sp = torch.cuda.current_stream().cuda_stream
+    d_ref = torch.empty((n, 4), dtype=torch.float32, device="cuda")
+    R.raycast_device(ctx, scene, d_rays.data_ptr(), n, d_ref.data_ptr(), 0, sp)
+    d_hits = torch.empty((n, 4), dtype=torch.float32, device="cuda")
+    res = R.autotune_raycast(ctx, scene, d_rays.data_ptr(), n, d_hits.data_ptr(), 0, sp)
+    torch.cuda.synchronize()
+    assert res["candidates"] == 11 and 0 < res["best_ms"] <= res["default_ms"]
+    best = res["best"]
+    assert best["trace_block"] in (64, 128, 256) and best["trace_stack"] in (8, 12, 16)
+    assert R.autotune_lookup(ctx, R.TUNE_RAYCAST_CLOSEST, scene.stats()["triangle_count"], n) == best
+    assert np.array_equal(d_hits.cpu().numpy().view(np.uint32), d_ref.cpu().numpy().view(np.uint32))
+    R.autotune_set_mode(ctx, R.AUTOTUNE_CACHED)
+    try:
+        d2 = torch.empty((n, 4), dtype=torch.float32, device="cuda")
+        R.raycast_device(ctx, scene, d_rays.data_ptr(), n, d2.data_ptr(), 0, sp)
+        torch.cuda.synchronize()
+        assert np.array_equal(d2.cpu().numpy().view(np.uint32), d_ref.cpu().numpy().view(np.uint32))
+    finally:
+        R.autotune_set_mode(ctx, R.AUTOTUNE_OFF)
+
+
+def test_autotune_render_and_batch(R):
+    ctx = R.Context(0)
+    try:
+        d = scenes.material_zoo(R)
+        sc = d.to_product(R, ctx)
+        W, H = 96, 64
+        iv, ip = scenes.cornell_camera(R, W, H)
+        pc = R.push_consts(iv, ip, total_emissive_weight=sc.emissive_weight, spp=3, max_bounces=6, focus_dist=3.4)
+        opts = R.render_options(W, H, R.MODE_NEE_MIS, 3)
+        ref, _, _ = R.render(ctx, sc, pc, opts)
+        res = R.autotune_render(ctx, sc, pc, opts)
+        assert res["candidates"] == 9 and res["best_ms"] > 0 and res["kind"] == R.TUNE_RENDER
+        jobs = [R.RenderJob(sc, pc, opts)]
+        for k in range(5):
+            iv2, ip2 = scenes.cornell_camera(R, 40 + 8 * k, 32)
+            pc2 = R.push_consts(iv2, ip2, total_emissive_weight=sc.emissive_weight, spp=1 + k, max_bounces=4 + k,
+                                focus_dist=3.4)
+            jobs.append(R.RenderJob(sc, pc2, R.render_options(40 + 8 * k, 32, R.MODE_NEE_MIS, k + 1)))
+        bres = R.autotune_batch(ctx, jobs)
+        assert bres["candidates"] == 6 and bres["best"]["wave_paths"] in (1 << 20, 1 << 21, 1 << 22)
+        R.autotune_set_mode(ctx, R.AUTOTUNE_CACHED)
+        out, _, _ = R.render(ctx, sc, pc, opts)
+        assert np.array_equal(out, ref)
+        alone = [R.render(ctx, j.scene, j.pc, j.opts)[0] for j in jobs]
+        R.render_batch(ctx, jobs)
+        for j, a in zip(jobs, alone):
+            assert np.array_equal(j.accum, a)
+        sc.close()
+    finally:
+        ctx.close()
