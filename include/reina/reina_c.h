@@ -426,6 +426,73 @@ int reina_camera_matrices(const float pos[3], const float front[3], const float 
                           float aspect, float z_near, float z_far, float inv_view[16], float inv_proj[16]);
 
 /* ------------------------------------------------------------------------------------------------ */
+/* Loaders, run configuration and image output                                                      */
+/* ------------------------------------------------------------------------------------------------ */
+/* Scene::defineObject(filepath) (src/scene/Scene.h:70; Models::getObjData, src/scene/Models.cpp:117-175):
+ * a Wavefront OBJ file as one model — polygons fanned into triangles, one vertex per distinct
+ * (position, UV, normal) triple, smooth normals where the file has none, UVs flipped (v -> 1 - v),
+ * per-vertex tangent frames from the UVs (zero tangent and bitangent without UVs, as the reference
+ * leaves them). */
+int reina_scene_define_object_obj(reina_scene* scene, const char* path, uint32_t* out_object_id);
+
+typedef struct reina_gltf_stats {
+    uint32_t meshes;
+    uint32_t primitives;          /* objects defined (triangle primitives) */
+    uint32_t instances;           /* instances added (node x primitive) */
+    uint32_t skipped_primitives;  /* non-triangle or empty primitives */
+    uint32_t ignored_textures;    /* texture references left out (textures are not supported yet) */
+} reina_gltf_stats;
+/* gltf::loadScene (src/scene/gltf/gltfloader.cpp:432-456, less the build): adds the default scene of a
+ * .gltf or .glb file (buffers embedded, base64 data URIs or files beside it) to an unbuilt scene — one
+ * object per triangle primitive, one instance per (node, primitive) with the node's world matrix, the
+ * material mapped as gltfloader.cpp:380-412 maps it (Disney; emissive factor x strength when there is
+ * no emissive texture; metallic; roughness clamped to [0.1, 0.7]; base colour; cull unless double-sided;
+ * KHR_materials_ior; KHR_materials_transmission -> specular transmission, no culling).  A primitive
+ * without normals fails as in the reference. */
+int reina_scene_add_gltf(reina_scene* scene, const char* path, reina_gltf_stats* out_stats);
+
+/* Number of objects of a scene, and the model data stored for one (the arrays are copied out; pass NULL
+ * for any of them, and *_count pointers receive the sizes in elements: vertices, indices, TBNs, UVs). */
+int reina_scene_object_count(const reina_scene* scene, uint32_t* out_count);
+int reina_scene_export_object(const reina_scene* scene, uint32_t object_id, float* vertices4, uint64_t* vertex_count,
+                              uint32_t* indices, uint64_t* index_count, float* tbns9, uint64_t* tbn_count,
+                              float* tex_coords2, uint64_t* tex_coord_count);
+
+/* config/config.toml as the reference reads it (src/Reina.cpp:142-156,185,243-245;
+ * src/tools/SaveManager.cpp:6-24).  Every key is required; defocus_multiplier is divided by 100 as in
+ * src/Reina.cpp:150.  At most 64 save points of each kind. */
+enum { REINA_CONFIG_MAX_SAVES = 64 };
+typedef struct reina_config {
+    float focus_dist;
+    float defocus_multiplier;
+    uint32_t samples_per_pixel;
+    uint32_t max_bounces;
+    float direct_clamp;
+    float indirect_clamp;
+    BloomPushConsts bloom;
+    TonemappingPushConsts tonemap;
+    uint32_t save_on_samples_count;
+    uint32_t save_on_times_count;
+    int64_t save_on_samples[REINA_CONFIG_MAX_SAVES];
+    double save_on_times[REINA_CONFIG_MAX_SAVES];
+} reina_config;
+int reina_config_load(const char* path, reina_config* out_config);
+
+/* SaveManager (src/tools/SaveManager.cpp:26-39): each save point is taken once, the first time the
+ * sample count (time in seconds) exceeds it; next() writes "output_<N>spp.png" / "output_<T>sec.png"
+ * into name_out (at least 64 bytes), or "" when nothing is due (sample points are checked first; one
+ * per call). */
+typedef struct reina_save_schedule reina_save_schedule;
+int reina_save_schedule_create(const reina_config* config, reina_save_schedule** out_schedule);
+void reina_save_schedule_destroy(reina_save_schedule* schedule);
+int reina_save_schedule_next(reina_save_schedule* schedule, uint64_t samples, double seconds, char* name_out,
+                             size_t name_capacity);
+
+/* Writes an RGBA8 image (width*height*4 bytes, rows top to bottom) as a PNG file (the reference saves
+ * the tone-mapped image with stb_image_write, src/Reina.cpp:19-47). */
+int reina_write_png(const char* path, const uint8_t* rgba8, uint32_t width, uint32_t height);
+
+/* ------------------------------------------------------------------------------------------------ */
 /* Autotuner                                                                                          */
 /* ------------------------------------------------------------------------------------------------ */
 /* Autotuner (no counterpart in the reference).  Each reina_autotune_* call times candidate

@@ -15,9 +15,11 @@
 #include "../../include/reina/reina_c.h"
 #include "autotune.h"
 #include "batch.h"
+#include "config.h"
 #include "errors.h"
 #include "generators.h"
 #include "kernels.h"
+#include "loaders.h"
 #include "post.h"
 #include "render.h"
 #include "scene.h"
@@ -1040,6 +1042,112 @@ int reina_autotune_load(reina_ctx* ctx, const char* path) {
     return guard([&] {
         need(ctx && path, "NULL argument");
         ctx->tune.load(path);
+    });
+}
+
+// ------------------------------------------------------------------------------------------------
+// Loaders, configuration, output
+
+struct reina_save_schedule {
+    rt::SaveSchedule s;
+};
+
+int reina_scene_define_object_obj(reina_scene* scene, const char* path, uint32_t* out_id) {
+    return guard([&] {
+        need(scene && scene->s && path && out_id, "NULL argument");
+        *out_id = scene->s->define_object(rt::load_obj(path));
+    });
+}
+
+int reina_scene_add_gltf(reina_scene* scene, const char* path, reina_gltf_stats* out) {
+    return guard([&] {
+        need(scene && scene->s && path, "NULL argument");
+        if (scene->s->built()) fail(REINA_ERR_STATE, "scene is already built");
+        const rt::GltfLoadStats st = rt::load_gltf(path, *scene->s);
+        if (out) {
+            out->meshes = st.meshes;
+            out->primitives = st.primitives;
+            out->instances = st.instances;
+            out->skipped_primitives = st.skipped_primitives;
+            out->ignored_textures = st.ignored_textures;
+        }
+    });
+}
+
+int reina_scene_object_count(const reina_scene* scene, uint32_t* out) {
+    return guard([&] {
+        need(scene && scene->s && out, "NULL argument");
+        *out = (uint32_t)scene->s->object_count();
+    });
+}
+
+int reina_scene_export_object(const reina_scene* scene, uint32_t id, float* v, uint64_t* nv, uint32_t* idx, uint64_t* ni,
+                              float* tbn, uint64_t* nt, float* uv, uint64_t* nuv) {
+    return guard([&] {
+        need(scene && scene->s, "NULL argument");
+        const rt::ModelData& m = scene->s->model(id);
+        if (nv) *nv = m.vertices.size() / 4;
+        if (ni) *ni = m.indices.size();
+        if (nt) *nt = m.tbns.size() / 9;
+        if (nuv) *nuv = m.tex_coords.size() / 2;
+        if (v) std::memcpy(v, m.vertices.data(), m.vertices.size() * sizeof(float));
+        if (idx) std::memcpy(idx, m.indices.data(), m.indices.size() * sizeof(uint32_t));
+        if (tbn) std::memcpy(tbn, m.tbns.data(), m.tbns.size() * sizeof(float));
+        if (uv) std::memcpy(uv, m.tex_coords.data(), m.tex_coords.size() * sizeof(float));
+    });
+}
+
+int reina_config_load(const char* path, reina_config* out) {
+    return guard([&] {
+        need(path && out, "NULL argument");
+        const rt::RunConfig c = rt::load_config(path);
+        if (c.save_on_samples.size() > REINA_CONFIG_MAX_SAVES || c.save_on_times.size() > REINA_CONFIG_MAX_SAVES)
+            fail(REINA_ERR_IO, std::string(path) + ": more than " + std::to_string(REINA_CONFIG_MAX_SAVES) + " save points");
+        std::memset(out, 0, sizeof(*out));
+        out->focus_dist = c.focus_dist;
+        out->defocus_multiplier = c.defocus_multiplier;
+        out->samples_per_pixel = c.samples_per_pixel;
+        out->max_bounces = c.max_bounces;
+        out->direct_clamp = c.direct_clamp;
+        out->indirect_clamp = c.indirect_clamp;
+        out->bloom.radius = c.bloom_radius;
+        out->bloom.threshold = c.bloom_threshold;
+        out->bloom.intensity = c.bloom_intensity;
+        out->tonemap.exposure = c.exposure;
+        out->save_on_samples_count = (uint32_t)c.save_on_samples.size();
+        out->save_on_times_count = (uint32_t)c.save_on_times.size();
+        for (size_t k = 0; k < c.save_on_samples.size(); ++k) out->save_on_samples[k] = c.save_on_samples[k];
+        for (size_t k = 0; k < c.save_on_times.size(); ++k) out->save_on_times[k] = c.save_on_times[k];
+    });
+}
+
+int reina_save_schedule_create(const reina_config* c, reina_save_schedule** out) {
+    return guard([&] {
+        need(c && out, "NULL argument");
+        need(c->save_on_samples_count <= REINA_CONFIG_MAX_SAVES && c->save_on_times_count <= REINA_CONFIG_MAX_SAVES,
+             "too many save points");
+        std::vector<int64_t> smp(c->save_on_samples, c->save_on_samples + c->save_on_samples_count);
+        std::vector<double> tm(c->save_on_times, c->save_on_times + c->save_on_times_count);
+        *out = new reina_save_schedule{rt::SaveSchedule(std::move(smp), std::move(tm))};
+    });
+}
+
+void reina_save_schedule_destroy(reina_save_schedule* s) { delete s; }
+
+int reina_save_schedule_next(reina_save_schedule* s, uint64_t samples, double seconds, char* name, size_t cap) {
+    return guard([&] {
+        need(s && name, "NULL argument");
+        need(cap >= 64, "name buffer must hold at least 64 bytes");
+        const std::string n = s->s.next(samples, seconds);
+        need(n.size() < cap, "name buffer too small");
+        std::memcpy(name, n.c_str(), n.size() + 1);
+    });
+}
+
+int reina_write_png(const char* path, const uint8_t* rgba8, uint32_t w, uint32_t h) {
+    return guard([&] {
+        need(path && rgba8, "NULL argument");
+        rt::write_png(path, rgba8, w, h);
     });
 }
 

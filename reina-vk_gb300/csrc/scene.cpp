@@ -442,6 +442,11 @@ size_t Scene::device_bytes() const {
            d_cdf_tris_.bytes() + d_cdf_inst_.bytes() + d_props_material_.bytes() + d_has_tbn_.bytes();
 }
 
+const ModelData& Scene::model(uint32_t object) const {
+    if (object >= models_.size()) fail(REINA_ERR_INVALID, "object id out of range");
+    return models_[object];
+}
+
 void Scene::prim_info(uint32_t prim, uint32_t* inst, uint32_t* local) const {
     if (!built_) fail(REINA_ERR_STATE, "scene is not built");
     if (prim >= tri_total_) fail(REINA_ERR_INVALID, "triangle id out of range");

@@ -72,6 +72,8 @@ public:
     void release_device();
     int device() const { return device_; }
     void prim_info(uint32_t prim, uint32_t* inst, uint32_t* local) const;
+    size_t object_count() const { return models_.size(); }
+    const ModelData& model(uint32_t object) const;
     void bounds(float lo[3], float hi[3]) const;
 
     // Host copies of the assembled buffers (as uploaded), used by the C ABI's inspection calls.

@@ -313,13 +313,15 @@ __device__ __forceinline__ bool trav_step(const Bvh8Node* __restrict__ nodes, co
         s.group = make_uint2(0u, 0u);
     }
     while (tgroup.y) {
-        if (kPost && s.sp < kTotalStack) {
-            const uint32_t with_tris = (uint32_t)__popc(__activemask());
-            if (with_tris * 32u < traversing * (uint32_t)kPostpone) {
-                if (s.sp < SS) stack[s.sp * stride] = tgroup;
-                else spill[s.sp - SS] = tgroup;
-                ++s.sp;
-                break;
+        if constexpr (kPost) {
+            if (s.sp < kTotalStack) {
+                const uint32_t with_tris = (uint32_t)__popc(__activemask());
+                if (with_tris * 32u < traversing * (uint32_t)kPostpone) {
+                    if (s.sp < SS) stack[s.sp * stride] = tgroup;
+                    else spill[s.sp - SS] = tgroup;
+                    ++s.sp;
+                    break;
+                }
             }
         }
         const int k = __ffs(tgroup.y) - 1;

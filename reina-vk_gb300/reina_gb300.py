@@ -162,6 +162,23 @@ TUNE_RAYCAST_CLOSEST, TUNE_RAYCAST_ANY, TUNE_RENDER, TUNE_BATCH = range(4)
 AUTOTUNE_OFF, AUTOTUNE_CACHED = 0, 1
 
 
+class _GltfStats(C.Structure):
+    _fields_ = [("meshes", C.c_uint32), ("primitives", C.c_uint32), ("instances", C.c_uint32),
+                ("skipped_primitives", C.c_uint32), ("ignored_textures", C.c_uint32)]
+
+
+CONFIG_MAX_SAVES = 64
+
+
+class RunConfig(C.Structure):
+    """config/config.toml as the reference reads it (reina_config)."""
+    _fields_ = [("focus_dist", C.c_float), ("defocus_multiplier", C.c_float), ("samples_per_pixel", C.c_uint32),
+                ("max_bounces", C.c_uint32), ("direct_clamp", C.c_float), ("indirect_clamp", C.c_float),
+                ("bloom", BloomPushConsts), ("tonemap", TonemappingPushConsts),
+                ("save_on_samples_count", C.c_uint32), ("save_on_times_count", C.c_uint32),
+                ("save_on_samples", C.c_int64 * CONFIG_MAX_SAVES), ("save_on_times", C.c_double * CONFIG_MAX_SAVES)]
+
+
 class _RenderJob(C.Structure):
     _fields_ = [("scene", C.c_void_p), ("push_consts", RtPushConsts), ("options", RenderOptions),
                 ("accum", C.c_void_p), ("samples", C.c_void_p)]
@@ -282,6 +299,16 @@ def load_library() -> C.CDLL:
         "reina_render_device": (I32, [P, P, C.POINTER(RtPushConsts), C.POINTER(RenderOptions), P, P, P]),
         "reina_render_device_noalloc": (I32, [P, P, C.POINTER(RtPushConsts), C.POINTER(RenderOptions), P, P, P]),
         "reina_render_batch": (I32, [P, C.POINTER(_RenderJob), U32, C.POINTER(_RenderStats)]),
+        "reina_scene_define_object_obj": (I32, [P, C.c_char_p, C.POINTER(U32)]),
+        "reina_scene_add_gltf": (I32, [P, C.c_char_p, C.POINTER(_GltfStats)]),
+        "reina_scene_object_count": (I32, [P, C.POINTER(U32)]),
+        "reina_scene_export_object": (I32, [P, U32, P, C.POINTER(U64), P, C.POINTER(U64), P, C.POINTER(U64), P,
+                                            C.POINTER(U64)]),
+        "reina_config_load": (I32, [C.c_char_p, C.POINTER(RunConfig)]),
+        "reina_save_schedule_create": (I32, [C.POINTER(RunConfig), C.POINTER(P)]),
+        "reina_save_schedule_destroy": (None, [P]),
+        "reina_save_schedule_next": (I32, [P, U64, C.c_double, C.c_char_p, C.c_size_t]),
+        "reina_write_png": (I32, [C.c_char_p, P, U32, U32]),
         "reina_autotune_raycast": (I32, [P, P, P, U64, P, U32, P, C.POINTER(_TuneResult)]),
         "reina_autotune_render": (I32, [P, P, C.POINTER(RtPushConsts), C.POINTER(RenderOptions), C.POINTER(_TuneResult)]),
         "reina_autotune_batch": (I32, [P, C.POINTER(_RenderJob), U32, C.POINTER(_TuneResult)]),
@@ -467,6 +494,41 @@ class Scene:
         fm = _u32(face_material)
         _check(_lib.reina_scene_add_instance_per_face(self._h, object_id, t.ctypes.data_as(C.POINTER(C.c_float)), arr,
                                                       len(materials), fm.ctypes.data_as(C.POINTER(C.c_uint32))))
+
+    def define_object_obj(self, path) -> int:
+        """Scene::defineObject(filepath): a Wavefront OBJ file as one model."""
+        oid = C.c_uint32()
+        _check(_lib.reina_scene_define_object_obj(self._h, str(path).encode(), C.byref(oid)))
+        return oid.value
+
+    def add_object_obj(self, path, transform=None, material: "Material | None" = None) -> int:
+        oid = self.define_object_obj(path)
+        self.add_instance(oid, transform, material)
+        return oid
+
+    def add_gltf(self, path) -> dict:
+        """gltf::loadScene without the build: the default scene of a .gltf/.glb file."""
+        st = _GltfStats()
+        _check(_lib.reina_scene_add_gltf(self._h, str(path).encode(), C.byref(st)))
+        return {f: int(getattr(st, f)) for f, _ in _GltfStats._fields_}
+
+    def object_count(self) -> int:
+        n = C.c_uint32()
+        _check(_lib.reina_scene_object_count(self._h, C.byref(n)))
+        return n.value
+
+    def export_object(self, object_id: int) -> dict:
+        """The model data stored for an object: vertices (N,4), indices (3M,), tbns (K,9), tex_coords (L,2)."""
+        nv, ni, nt, nu = C.c_uint64(), C.c_uint64(), C.c_uint64(), C.c_uint64()
+        _check(_lib.reina_scene_export_object(self._h, object_id, None, C.byref(nv), None, C.byref(ni), None,
+                                              C.byref(nt), None, C.byref(nu)))
+        v = np.zeros((nv.value, 4), np.float32)
+        i = np.zeros(ni.value, np.uint32)
+        t = np.zeros((nt.value, 9), np.float32)
+        u = np.zeros((nu.value, 2), np.float32)
+        _check(_lib.reina_scene_export_object(self._h, object_id, _ptr(v), C.byref(nv), _ptr(i), C.byref(ni), _ptr(t),
+                                              C.byref(nt), _ptr(u), C.byref(nu)))
+        return {"vertices": v, "indices": i, "tbns": t, "tex_coords": u}
 
     def build(self, require_emissive: bool = False) -> None:
         _check(_lib.reina_scene_build(self._h, 1 if require_emissive else 0))
@@ -740,6 +802,46 @@ def autotune_save(ctx: Context, path) -> None:
 
 def autotune_load(ctx: Context, path) -> None:
     _check(_lib.reina_autotune_load(ctx.handle, str(path).encode()))
+
+
+def load_config(path) -> RunConfig:
+    """config/config.toml (reina_config_load)."""
+    lib = load_library()
+    c = RunConfig()
+    _check(lib.reina_config_load(str(path).encode(), C.byref(c)))
+    return c
+
+
+class SaveSchedule:
+    """SaveManager: file names due at (samples, seconds), each save point once."""
+
+    def __init__(self, config: RunConfig):
+        lib = load_library()
+        h = C.c_void_p()
+        _check(lib.reina_save_schedule_create(C.byref(config), C.byref(h)))
+        self._h = h
+
+    def next(self, samples: int, seconds: float) -> str:
+        buf = C.create_string_buffer(128)
+        _check(_lib.reina_save_schedule_next(self._h, samples, float(seconds), buf, 128))
+        return buf.value.decode()
+
+    def close(self) -> None:
+        if self._h:
+            _lib.reina_save_schedule_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def write_png(path, rgba8: np.ndarray) -> None:
+    rgba8 = np.ascontiguousarray(rgba8, np.uint8)
+    h, w = rgba8.shape[:2]
+    _check(load_library().reina_write_png(str(path).encode(), _ptr(rgba8), w, h))
 
 
 NOALLOC_MAX_PIXELS = 65536
