@@ -1,4 +1,5 @@
-"""Builds the trace-path library `_build/libreina_gb300.so` from `csrc/` (CUDA for sm_103a + host C++).
+"""Builds the trace-path library `_build/libreina_gb300.so` from `csrc/` (CUDA for sm_103a + host C++), and
+the headless renderer `_build/reina_render` from `cli/` against it.
 
 Usage: python reina-vk_gb300/build.py [--force] [--ptxas-verbose]
 
@@ -84,7 +85,23 @@ def build(force: bool = False, ptxas_verbose: bool = False, verbose: bool = Fals
         if res.returncode != 0:
             raise RuntimeError(f"link failed: {' '.join(cmd)}\n{res.stdout}\n{res.stderr}")
         os.replace(tmp, LIB)
+    _build_cli(force)
     return LIB
+
+
+CLI_SRC = PKG / "cli" / "reina_render.cpp"
+CLI = OUT / "reina_render"
+
+
+def _build_cli(force: bool) -> None:
+    """The headless renderer (cli/reina_render.cpp), linked against the library (rpath $ORIGIN)."""
+    if not force and CLI.exists() and CLI.stat().st_mtime >= max(CLI_SRC.stat().st_mtime, LIB.stat().st_mtime):
+        return
+    cmd = ["g++", "-O2", "-std=c++17", "-Wall", f"-I{ROOT / 'include'}", str(CLI_SRC), "-o", str(CLI), f"-L{OUT}",
+           "-lreina_gb300", "-Wl,-rpath,$ORIGIN", "-pthread"]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"CLI build failed: {' '.join(cmd)}\n{res.stdout}\n{res.stderr}")
 
 
 if __name__ == "__main__":
