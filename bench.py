@@ -10,6 +10,12 @@ L2 (129 MB) is flushed by writing a 512 MB buffer between timed steps (outside t
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
+Beside the headline line's required keys, the JSON carries: `render` (the 1.3M-triangle scene at
+1920x1080, 64 spp, 12 bounces, NEE+MIS, wavefront vs plain megakernel; the Cornell room), `batched` (256
+seeded scenes rendered in one batched call vs one at a time; `--batch-scenes`), `served` (a Poisson
+request stream through the request server vs one at a time; `--serve-seconds`), and `cpu_baseline`.
+`--profile`, `--profile-render` and `--profile-batch` launch small fixed workloads for ncu and exit.
+
 `--impl reference` times the CPU restatement of the path (oracle/, FP32, all host threads) on a bounded
 sample of the same rays per step; the reference's own Vulkan ray-tracing path cannot run on this
 hardware (no graphics stack, no RT cores).
@@ -173,6 +179,22 @@ def run_ours(args) -> dict | None:
             R.render_device(ctx, scene, pc, opts, acc.data_ptr(), 0, sptr)
         torch.cuda.synchronize()
         print(json.dumps({"profile": "render_large_480x270x4spp", "frames": 2}))
+        return None
+
+    if args.profile_batch:
+        # Profiling mode (for ncu): the first 16 scenes of the batched workload at 2 spp, batched once.
+        import scenes
+
+        pool, _ = build_pool(R, ctx, 16)
+        jobs, keep = [], []
+        for sc, p in pool:
+            pc, opts = scenes.batch_job(R, sc, dict(p, spp=min(p["spp"], 2)))
+            acc = torch.zeros((p["side"], p["side"], 4), dtype=torch.float32, device="cuda")
+            keep.append(acc)
+            jobs.append(R.DeviceRenderJob(sc, pc, opts, acc.data_ptr()))
+        st_b = R.render_batch_device(ctx, jobs, sptr)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile": "batch_16_scenes_2spp", "segments": st_b["rays"], "shadow_rays": st_b["shadow_rays"]}))
         return None
 
     if args.profile:
@@ -487,37 +509,44 @@ def serve_metrics(R, ctx, torch, pool, seconds: float, rate: float) -> dict:
     plain = {"p50_s": p50, "p99_s": p99, "mean_s": float(np.mean(lat)), "renders_per_s": n / plain_span,
              "samples_per_s": samples / plain_span, "span_s": plain_span}
 
-    # (b) served
-    srv = R.Server(ctx, budget_bytes=120_000_000_000)
-    ids = [srv.add_scene(s) for s, _ in pool]
-    outs = [np.zeros((r[3].height, r[3].width, 4), np.float32) for r in reqs]
-    rids = [None] * n
+    # (b) served: the same stream through a request server (the scenes are handed to the first server
+    # and stay with it; the second policy runs on a server of its own over fresh copies)
+    def serve(fifo: bool, scenes_pool) -> tuple[dict, bool]:
+        srv = R.Server(ctx, budget_bytes=120_000_000_000, fifo=fifo)
+        ids = [srv.add_scene(s) for s, _ in scenes_pool]
+        outs = [np.zeros((r[3].height, r[3].width, 4), np.float32) for r in reqs]
+        rids = [None] * n
 
-    def submitter():
-        t_start = time.perf_counter()
-        for k, (at, si, pc, opts, side) in enumerate(reqs):
-            now = time.perf_counter() - t_start
-            if now < at:
-                time.sleep(at - now)
-            rids[k] = srv.submit(ids[si], pc, opts, outs[k])
+        def submitter():
+            t_start = time.perf_counter()
+            for k, (at, si, pc, opts, side) in enumerate(reqs):
+                now = time.perf_counter() - t_start
+                if now < at:
+                    time.sleep(at - now)
+                rids[k] = srv.submit(ids[si], pc, opts, outs[k])
 
-    th = threading.Thread(target=submitter)
-    th.start()
-    th.join()
-    states = [srv.wait(r, -1.0)["state"] for r in rids]
-    st = srv.stats()
-    srv.close()
-    span = st["first_submit_to_last_done_s"]
-    served = {"p50_s": st["latency_p50_s"], "p99_s": st["latency_p99_s"], "mean_s": st["latency_mean_s"],
-              "renders_per_s": st["completed"] / span, "samples_per_s": samples / span,
-              "segments_per_s": st["rays"] / span, "rays_per_s": (st["rays"] + st["shadow_rays"]) / span,
-              "span_s": span, "completed": st["completed"], "failed": st["failed"], "waves": st["waves"],
-              "scene_uploads": st["scene_uploads"], "scene_evictions": st["scene_evictions"],
-              "peak_resident_gb": st["peak_resident_bytes"] / 1e9}
+        th = threading.Thread(target=submitter)
+        th.start()
+        th.join()
+        states = [srv.wait(r, -1.0)["state"] for r in rids]
+        st = srv.stats()
+        srv.close()
+        span = st["first_submit_to_last_done_s"]
+        return ({"policy": "fifo" if fifo else "fair share",
+                 "p50_s": st["latency_p50_s"], "p99_s": st["latency_p99_s"], "mean_s": st["latency_mean_s"],
+                 "renders_per_s": st["completed"] / span, "samples_per_s": samples / span,
+                 "segments_per_s": st["rays"] / span, "rays_per_s": (st["rays"] + st["shadow_rays"]) / span,
+                 "span_s": span, "completed": st["completed"], "failed": st["failed"], "waves": st["waves"],
+                 "scene_uploads": st["scene_uploads"], "scene_evictions": st["scene_evictions"],
+                 "peak_resident_gb": st["peak_resident_bytes"] / 1e9}, all(s == R.REQ_DONE for s in states))
+
+    served, ok1 = serve(False, pool)
+    pool2 = [scenes.batch_scene(R, ctx, k) for k in range(len(pool))]
+    served_fifo, ok2 = serve(True, pool2)
     return {"workload": f"Poisson {rate:g}/s for {seconds:g} s ({n} requests) over the {len(pool)}-scene pool, "
                         "side U[128,1024], spp U{1..64}, depth U{4..12}, NEE+MIS; 120 GB admission budget",
-            "requests": n, "samples_total": int(samples), "all_done": all(s == R.REQ_DONE for s in states),
-            "plain_one_at_a_time": plain, "served": served,
+            "requests": n, "samples_total": int(samples), "all_done": ok1 and ok2,
+            "plain_one_at_a_time": plain, "served": served, "served_fifo": served_fifo,
             "renders_per_s_ratio": served["renders_per_s"] / plain["renders_per_s"]}
 
 
@@ -594,6 +623,7 @@ def main() -> int:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile", action="store_true", help="launch the kernels a few times for ncu and exit")
     ap.add_argument("--profile-render", action="store_true", help="render a small frame twice for ncu and exit")
+    ap.add_argument("--profile-batch", action="store_true", help="one small batched render for ncu and exit")
     ap.add_argument("--no-render", action="store_true", help="skip the render metrics")
     ap.add_argument("--render-frames", type=int, default=2)
     ap.add_argument("--batch-scenes", type=int, default=256,

@@ -34,7 +34,7 @@ struct BatchLaunch {
 
 // Sets up slot i (job, pixel, sample, camera ray — raytrace.rgen.glsl:250-263); returns whether its job
 // traces any segment (paths of jobs with maxBounces = 0 finish with zero radiance).
-__device__ __forceinline__ bool init_slot(const BatchLaunch& B, uint32_t i) {
+__device__ __forceinline__ bool init_slot(const BatchLaunch& B, const JobGpu* __restrict__ jobs, uint32_t i) {
     const PathState& ps = B.bp.ps;
     int lo = 0, hi = (int)B.hdr->nseg - 1;
     while (lo < hi) {
@@ -43,7 +43,7 @@ __device__ __forceinline__ bool init_slot(const BatchLaunch& B, uint32_t i) {
         else hi = mid - 1;
     }
     const WaveSeg sg = B.segs[lo];
-    const JobGpu& J = B.jobs[sg.job];
+    const JobGpu& J = jobs[sg.job];
     const uint32_t pixel = sg.pixel_start + (i - sg.wave_start);
     const uint32_t k = sg.sample;
     const uint32_t x = pixel % J.W, y = pixel / J.W;
@@ -80,19 +80,19 @@ __device__ __forceinline__ bool init_slot(const BatchLaunch& B, uint32_t i) {
 }
 
 // The active-path counter is zero at launch (cleared with the other counters before the wave).
-__global__ void __launch_bounds__(kBlock) kb_init(BatchLaunch B) {
+__global__ void __launch_bounds__(kBlock) kb_init(BatchLaunch B, const JobGpu* __restrict__ jobs) {
     const PathState& ps = B.bp.ps;
     const uint32_t n = B.hdr->count;
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         const uint32_t i = base + threadIdx.x;
-        const bool live = i < n && init_slot(B, i);
+        const bool live = i < n && init_slot(B, jobs, i);
         const uint32_t pos = warp_append(ps.counters + kCntActive, live);
         if (live) ps.q_active[0][pos] = i;
     }
 }
 
 template <int BLOCK, int SS>
-__global__ void __launch_bounds__(BLOCK) kb_extend(BatchLaunch B, int cur) {
+__global__ void __launch_bounds__(BLOCK) kb_extend(BatchLaunch B, const JobGpu* __restrict__ jobs, int cur) {
     __shared__ uint2 stack[SS * BLOCK];
     const PathState& ps = B.bp.ps;
     const uint32_t n = ps.counters[kCntActive + cur];
@@ -104,7 +104,7 @@ __global__ void __launch_bounds__(BLOCK) kb_extend(BatchLaunch B, int cur) {
         uint32_t p = 0;
         if (active) {
             p = q[i];
-            const DeviceScene& s = B.jobs[B.bp.job[p]].s;
+            const DeviceScene& s = jobs[B.bp.job[p]].s;
             const TraceRay r = make_trace_ray(ps.ox[p], ps.oy[p], ps.oz[p], ps.dx[p], ps.dy[p], ps.dz[p], 0.0f, 10000.0f);
             Hit h;
             TraceCounters c{0u, 0u};
@@ -128,7 +128,7 @@ __global__ void __launch_bounds__(BLOCK) kb_extend(BatchLaunch B, int cur) {
 }
 
 template <int MAT>
-__global__ void __launch_bounds__(kBlock) kb_shade(BatchLaunch B, int cur) {
+__global__ void __launch_bounds__(kBlock, kShadeMinBlocks) kb_shade(BatchLaunch B, const JobGpu* __restrict__ jobs, int cur) {
     const PathState& ps = B.bp.ps;
     const uint32_t n = ps.counters[kCntQueue + MAT];
     const uint32_t* q = ps.q_shade + (size_t)MAT * B.P;
@@ -140,7 +140,7 @@ __global__ void __launch_bounds__(kBlock) kb_shade(BatchLaunch B, int cur) {
         uint32_t p = 0;
         if (active) {
             p = q[i];
-            const JobGpu& J = B.jobs[B.bp.job[p]];
+            const JobGpu& J = jobs[B.bp.job[p]];
             const bool nee = J.mode == kModeNeeMis;
             const V3 ro{ps.ox[p], ps.oy[p], ps.oz[p]};
             const V3 rd{ps.dx[p], ps.dy[p], ps.dz[p]};
@@ -201,12 +201,12 @@ __global__ void __launch_bounds__(kBlock) kb_shade(BatchLaunch B, int cur) {
     }
 }
 
-__global__ void __launch_bounds__(kBlock) kb_shade_miss(BatchLaunch B) {
+__global__ void __launch_bounds__(kBlock) kb_shade_miss(BatchLaunch B, const JobGpu* __restrict__ jobs) {
     const PathState& ps = B.bp.ps;
     const uint32_t n = ps.counters[kCntQueue + kQueueMiss];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t p = ps.q_shade[i];
-        const JobGpu& J = B.jobs[B.bp.job[p]];
+        const JobGpu& J = jobs[B.bp.job[p]];
         V3 sky;
         if (J.env_mode == 1) {
             sky = V3{J.env[0], J.env[1], J.env[2]};
@@ -220,7 +220,7 @@ __global__ void __launch_bounds__(kBlock) kb_shade_miss(BatchLaunch B) {
 }
 
 template <int BLOCK, int SS>
-__global__ void __launch_bounds__(BLOCK) kb_shadow(BatchLaunch B) {
+__global__ void __launch_bounds__(BLOCK) kb_shadow(BatchLaunch B, const JobGpu* __restrict__ jobs) {
     __shared__ uint2 stack[SS * BLOCK];
     const PathState& ps = B.bp.ps;
     const uint32_t n = ps.counters[kCntShadow];
@@ -229,7 +229,7 @@ __global__ void __launch_bounds__(BLOCK) kb_shadow(BatchLaunch B) {
         const bool active = i < n;
         if (active) {
             const uint32_t p = ps.q_shadow[i];
-            const DeviceScene& s = B.jobs[B.bp.job[p]].s;
+            const DeviceScene& s = jobs[B.bp.job[p]].s;
             const TraceRay r = make_trace_ray(ps.s_ox[i], ps.s_oy[i], ps.s_oz[i], ps.s_dx[i], ps.s_dy[i], ps.s_dz[i], 0.0f,
                                               ps.s_tmax[i]);
             Hit h;
@@ -246,11 +246,11 @@ __global__ void __launch_bounds__(BLOCK) kb_shadow(BatchLaunch B) {
 
 // raytrace.rgen.glsl:264-275 per slot: clamp (NaN kept), sample output, NaN drop, sum; carry the
 // RNG state and accumulatedDistance to the pixel's next sample.
-__global__ void __launch_bounds__(kBlock) kb_finish(BatchLaunch B) {
+__global__ void __launch_bounds__(kBlock) kb_finish(BatchLaunch B, const JobGpu* __restrict__ jobs) {
     const PathState& ps = B.bp.ps;
     const uint32_t n = B.hdr->count;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const JobGpu& J = B.jobs[B.bp.job[i]];
+        const JobGpu& J = jobs[B.bp.job[i]];
         const uint32_t pixel = B.bp.pix[i];
         const V3 c = clamp_keep_nan(load_rad(ps, i), J.pc.directClamp);
         if (J.samples) {
@@ -386,26 +386,26 @@ void BatchEngine::launch_wave(const WaveHeader& h, bool any_nee, cudaStream_t st
     const int simple = std::min<int>(blocks_simple_, (int)((capacity_ + kBlock - 1) / kBlock));
     auto sequence = [&](cudaStream_t s) {
         check_cuda(cudaMemsetAsync(cnt, 0, kNumCounters * sizeof(uint32_t), s), "cudaMemsetAsync");
-        kb_init<<<simple, kBlock, 0, s>>>(B);
+        kb_init<<<simple, kBlock, 0, s>>>(B, B.jobs);
         int cur = 0;
         for (uint32_t seg = 0; seg < h.max_bounces; ++seg) {
             check_cuda(cudaMemsetAsync(cnt + kCntActive + (cur ^ 1), 0, sizeof(uint32_t), s), "cudaMemsetAsync");
             check_cuda(cudaMemsetAsync(cnt + kCntQueue, 0, 6 * sizeof(uint32_t), s), "cudaMemsetAsync");
             with_trace_variant(trace_, [&](auto BS, auto SS) {
-                kb_extend<BS.value, SS.value><<<blocks_ext_, BS.value, 0, s>>>(B, cur);
+                kb_extend<BS.value, SS.value><<<blocks_ext_, BS.value, 0, s>>>(B, B.jobs, cur);
             });
-            kb_shade_miss<<<simple, kBlock, 0, s>>>(B);
-            kb_shade<1><<<blocks_shade_[1], kBlock, 0, s>>>(B, cur);
-            kb_shade<2><<<blocks_shade_[2], kBlock, 0, s>>>(B, cur);
-            kb_shade<3><<<blocks_shade_[3], kBlock, 0, s>>>(B, cur);
-            kb_shade<4><<<blocks_shade_[4], kBlock, 0, s>>>(B, cur);
+            kb_shade_miss<<<simple, kBlock, 0, s>>>(B, B.jobs);
+            kb_shade<1><<<blocks_shade_[1], kBlock, 0, s>>>(B, B.jobs, cur);
+            kb_shade<2><<<blocks_shade_[2], kBlock, 0, s>>>(B, B.jobs, cur);
+            kb_shade<3><<<blocks_shade_[3], kBlock, 0, s>>>(B, B.jobs, cur);
+            kb_shade<4><<<blocks_shade_[4], kBlock, 0, s>>>(B, B.jobs, cur);
             if (any_nee)
                 with_trace_variant(trace_, [&](auto BS, auto SS) {
-                    kb_shadow<BS.value, SS.value><<<blocks_sh_, BS.value, 0, s>>>(B);
+                    kb_shadow<BS.value, SS.value><<<blocks_sh_, BS.value, 0, s>>>(B, B.jobs);
                 });
             cur ^= 1;
         }
-        kb_finish<<<simple, kBlock, 0, s>>>(B);
+        kb_finish<<<simple, kBlock, 0, s>>>(B, B.jobs);
     };
     if (!use_graphs_) {
         sequence(st);
@@ -434,15 +434,16 @@ void BatchEngine::launch_wave(const WaveHeader& h, bool any_nee, cudaStream_t st
     check_cuda(cudaGraphLaunch(slot->exec, st), "cudaGraphLaunch");
 }
 
-uint64_t BatchEngine::run_wave(const std::vector<BatchJob*>& jobs, cudaStream_t st) {
+uint64_t BatchEngine::run_wave(const std::vector<BatchJob*>& jobs, cudaStream_t st, bool fifo) {
     // active jobs (at most kMaxWaveJobs per wave; the rest wait for a later wave)
     std::vector<BatchJob*> active;
     for (BatchJob* j : jobs)
         if (j->cursor < j->total && active.size() < kMaxWaveJobs) active.push_back(j);
     if (active.empty()) return 0;
-    // fair share of the capacity, then leftovers to the oldest jobs
+    // fair share of the capacity, then leftovers to the oldest jobs (or, first-come first-served, each
+    // job in order takes all it can use)
     std::vector<uint64_t> take(active.size(), 0);
-    const uint64_t fair = std::max<uint64_t>(1, capacity_ / active.size());
+    const uint64_t fair = fifo ? (uint64_t)capacity_ : std::max<uint64_t>(1, capacity_ / active.size());
     uint64_t used = 0;
     for (size_t a = 0; a < active.size(); ++a) {
         const BatchJob* j = active[a];

@@ -75,10 +75,10 @@ public:
 
     // Allocates the job's per-pixel state (24 bytes per pixel); the job must outlive its waves.
     static void prepare(BatchJob& job);
-    // Packs the next wave from `jobs` (fair share of the capacity, oldest first for leftovers), runs it
-    // and resolves the jobs it completes.  Returns the number of paths traced (0 = nothing to do).
-    // Synchronizes the stream at the end of the wave.
-    uint64_t run_wave(const std::vector<BatchJob*>& jobs, cudaStream_t st);
+    // Packs the next wave from `jobs` (fair share of the capacity, oldest first for leftovers; with
+    // `fifo`, each job in order takes all it can use), runs it and resolves the jobs it completes.
+    // Returns the number of paths traced (0 = nothing to do).  Synchronizes the stream at the end.
+    uint64_t run_wave(const std::vector<BatchJob*>& jobs, cudaStream_t st, bool fifo = false);
     uint32_t capacity() const { return capacity_; }
     const TraceConfig& trace() const { return trace_; }
     uint64_t rays() const { return rays_; }

@@ -138,7 +138,7 @@ __global__ void __launch_bounds__(kBlock) k_extend(RenderLaunch L, int cur) {
 // One kernel per material queue (MAT = 1 Lambertian, 2 metal, 3 dielectric, 4 Disney): the closest-hit
 // shader, then the raygen loop body (raytrace.rgen.glsl:124-180).
 template <int MAT>
-__global__ void __launch_bounds__(kBlock) k_shade(RenderLaunch L, int cur) {
+__global__ void __launch_bounds__(kBlock, kShadeMinBlocks) k_shade(RenderLaunch L, int cur) {
     const PathState& ps = L.ps;
     const uint32_t n = ps.counters[kCntQueue + MAT];
     const uint32_t* q = ps.q_shade + (size_t)MAT * L.P;

@@ -393,7 +393,7 @@ void Server::loop() {
         std::string err;
         const double t = now();
         try {
-            engine_->run_wave(jobs, stream_);
+            engine_->run_wave(jobs, stream_, cfg_.fifo);
         } catch (const Error& e) {
             code = e.code;
             err = e.what();

@@ -28,6 +28,7 @@ struct ServerConfig {
     uint32_t max_active = 512;    // requests sharing the waves
     uint32_t wave_paths = 0;
     bool graphs = true;
+    bool fifo = false;            // wave slots to the oldest requests first (default: fair share)
 };
 
 struct RequestSpec {
@@ -98,7 +99,7 @@ private:
     };
 
     void loop();
-    bool try_admit(Request& r);               // loop thread; device work outside the lock
+    bool try_admit(Request& r);               // loop thread, under the lock
     bool make_room(size_t need, const Request& r);
     void finish(Request& r, uint32_t state, int error, const std::string& msg);
     double now() const;

@@ -114,7 +114,8 @@ static void launch_grid_stack(int stack, const DeviceScene& s, const Ray* d_rays
 template <bool ANY>
 static void launch(const DeviceScene& s, const Ray* d_rays, uint64_t n, Hit* d_hits, uint32_t* d_err, uint32_t* d_next,
                    int sm_count, const TraceConfig& cfg, cudaStream_t st) {
-    if (cfg.refill <= 0) {   // grid form
+    // grid form (also for more than 2^31 rays, where the persistent form's fetch counter could wrap)
+    if (cfg.refill <= 0 || n > (1ull << 31)) {
         if (cfg.block == 64) launch_grid_stack<ANY, 64>(cfg.stack, s, d_rays, n, d_hits, d_err, st);
         else if (cfg.block == 256) launch_grid_stack<ANY, 256>(cfg.stack, s, d_rays, n, d_hits, d_err, st);
         else launch_grid_stack<ANY, kTraceBlock>(cfg.stack, s, d_rays, n, d_hits, d_err, st);

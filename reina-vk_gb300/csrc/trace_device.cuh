@@ -276,6 +276,7 @@ __device__ __forceinline__ void trav_init(const TraceRay& r, TravState& s, Hit& 
 #endif
 constexpr int kPostpone = RT_POSTPONE;
 
+
 // One traversal step.  Stack entries and the current group are node groups (child base, node hits in
 // bits 24..31 | internal mask) or postponed triangle groups (triangle base, triangle hits in bits
 // 0..23, bits 24..31 zero).  A step visits the nearest pending child node (or takes a popped triangle
@@ -383,12 +384,20 @@ __device__ __forceinline__ uint32_t traverse(const Bvh8Node* __restrict__ nodes,
 
 // Persistent traversal with dynamic ray fetch (Aila and Laine, "Understanding the Efficiency of Ray
 // Traversal on GPUs", HPG 2009): every warp keeps 32 rays in flight; whenever at least `refill` lanes
-// have finished, those lanes take the next rays from the global counter `next` (one atomic per warp),
-// so short rays do not idle their lane until the warp's longest ray ends.
+// have finished, those lanes take the next rays, so short rays do not idle their lane until the warp's
+// longest ray ends.  Rays are handed out from a warp-private chunk of kFetchChunk consecutive items,
+// refilled from the global counter `next` (one atomic per chunk, not per refill), which keeps the rays
+// of a warp close together in the input order.
 //   load(idx, ray) -> false if item idx has no ray to trace (then store is called at once with a miss)
 //   store(idx, hit, valid): called by all 32 lanes after every step; valid marks lanes that finished
 //   an item in that step (store may use warp-collective operations).
 // Requires blockDim.x to be a multiple of 32.
+#ifndef RT_FETCH_CHUNK
+#define RT_FETCH_CHUNK 128
+#endif
+constexpr uint32_t kFetchChunk = RT_FETCH_CHUNK;
+static_assert(kFetchChunk >= 32, "a chunk must cover a whole warp");
+
 template <bool ANY, bool COUNT, bool REFINE, class Load, class Store, int SS = kSmemStack>
 __device__ __forceinline__ uint32_t persistent_trace(const Bvh8Node* __restrict__ nodes, const TriRecord* __restrict__ tris,
                                                      uint32_t node_count, uint32_t n, uint32_t* next, uint2* stack,
@@ -398,20 +407,25 @@ __device__ __forceinline__ uint32_t persistent_trace(const Bvh8Node* __restrict_
     uint32_t err = 0;
     bool has = false, exhausted = false;
     uint32_t idx = 0;
+    uint32_t chunk_next = 0, chunk_end = 0;   // warp-uniform: the warp's unclaimed items [next, end)
     TraceRay r;
     TravState st;
     Hit hit;
     for (;;) {
         const unsigned idle = __ballot_sync(0xFFFFFFFFu, !has);
-        if (!exhausted && __popc(idle) >= refill) {
+        const uint32_t n_idle = (uint32_t)__popc(idle);
+        if (!exhausted && n_idle >= (uint32_t)refill) {
+            const uint32_t rem = chunk_end - chunk_next;
             uint32_t base = 0;
-            if (lane == 0) base = atomicAdd(next, (uint32_t)__popc(idle));
-            base = __shfl_sync(0xFFFFFFFFu, base, 0);
-            if (base + (uint32_t)__popc(idle) >= n) exhausted = true;
+            if (rem < n_idle) {   // the chunk runs out: the rest of it, then a fresh chunk
+                if (lane == 0) base = atomicAdd(next, kFetchChunk);
+                base = __shfl_sync(0xFFFFFFFFu, base, 0);
+            }
+            const uint32_t rank = (uint32_t)__popc(idle & ((1u << lane) - 1u));
             bool fresh = false;
             if (!has) {
-                idx = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
-                if (idx < n) {
+                idx = rank < rem ? chunk_next + rank : base + (rank - rem);
+                if (idx < n && (rank < rem || base < n)) {
                     fresh = true;
                     if (load(idx, r) && node_count) {
                         trav_init(r, st, hit);
@@ -420,6 +434,14 @@ __device__ __forceinline__ uint32_t persistent_trace(const Bvh8Node* __restrict_
                         hit.prim = kMiss; hit.t = r.tmax; hit.u = 0.0f; hit.v = 0.0f;
                     }
                 }
+            }
+            if (rem < n_idle) {
+                chunk_next = base + (n_idle - rem);
+                chunk_end = base + kFetchChunk;
+                if (base >= n) exhausted = true;
+                if (chunk_end > n) chunk_end = n > chunk_next ? n : chunk_next;
+            } else {
+                chunk_next += n_idle;
             }
             store(idx, hit, fresh && !has);   // items without a ray (or an empty scene) finish at once
         }

@@ -92,11 +92,13 @@ def submit_all(R, srv, ids, weights, specs, stagger_s=0.0, threads=1):
     return rids, outs
 
 
-def test_same_alone_and_in_the_mix(R, alone):
-    """Requests submitted from 3 threads while earlier ones run: each result equals its lone render."""
+@pytest.mark.parametrize("fifo", [False, True])
+def test_same_alone_and_in_the_mix(R, alone, fifo):
+    """Requests submitted from 3 threads while earlier ones run: each result equals its lone render
+    (fair-share and first-come first-served wave packing)."""
     weights, ref = alone
     ctx = R.Context(0)
-    ctx_srv, ids = start_server(R, ctx, wave_paths=4096)
+    ctx_srv, ids = start_server(R, ctx, wave_paths=4096, fifo=fifo)
     srv = ctx_srv
     rids, outs = submit_all(R, srv, ids, weights, request_specs(), stagger_s=0.002, threads=3)
     for n, rid in enumerate(rids):
