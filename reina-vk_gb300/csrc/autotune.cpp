@@ -39,12 +39,12 @@ void TuneCache::save(const std::string& path) const {
     std::lock_guard<std::mutex> lk(mu_);
     std::ofstream f(path);
     if (!f) fail(REINA_ERR_IO, "cannot write autotune cache: " + path);
-    f << "# kind tri_bucket size_bucket refill block stack wave_paths best_ms default_ms\n";
+    f << "# kind tri_bucket size_bucket refill block stack wave_paths best_ms default_ms order\n";
     f.precision(9);
     for (const auto& [k, e] : map_) {
         f << std::get<0>(k) << ' ' << std::get<1>(k) << ' ' << std::get<2>(k) << ' ' << e.trace.refill << ' '
           << e.trace.block << ' ' << e.trace.stack << ' ' << e.wave_paths << ' ' << e.best_ms << ' ' << e.default_ms
-          << '\n';
+          << ' ' << e.trace.sort << '\n';
     }
     if (!f) fail(REINA_ERR_IO, "cannot write autotune cache: " + path);
 }
@@ -65,7 +65,15 @@ void TuneCache::load(const std::string& path) {
         if (!(is >> kind >> tb >> sb >> e.trace.refill >> e.trace.block >> e.trace.stack >> wave >> e.best_ms >>
               e.default_ms))
             fail(REINA_ERR_IO, path + ":" + std::to_string(lineno) + ": malformed autotune entry");
+        uint32_t order = 0;   // optional tenth field: 0 input ray order (default), 1 coherence order
+        if (is >> order) {
+            if (order > 1) fail(REINA_ERR_IO, path + ":" + std::to_string(lineno) + ": invalid ray order");
+        } else if (!is.eof()) {
+            fail(REINA_ERR_IO, path + ":" + std::to_string(lineno) + ": malformed autotune entry");
+        }
+        e.trace.sort = (int)order;
         std::string rest;
+        is.clear();
         if (is >> rest) fail(REINA_ERR_IO, path + ":" + std::to_string(lineno) + ": trailing text in autotune entry");
         if (kind > kTuneBatch || !valid_trace_config(e.trace) || wave > (1u << 26))
             fail(REINA_ERR_IO, path + ":" + std::to_string(lineno) + ": invalid autotune entry");
@@ -86,6 +94,11 @@ std::vector<TraceConfig> trace_candidates(bool with_persistent) {
             c.refill = 0;
             out.push_back(c);
         }
+    if (with_persistent) {   // ray casts: also coherence order, in the default block size and stack depth
+        TraceConfig c;
+        c.sort = 1;
+        out.push_back(c);
+    }
     if (with_persistent)
         for (int refill : {8, 16}) {
             TraceConfig c;

@@ -32,7 +32,8 @@ public:
     bool get(uint32_t kind, uint32_t tri_bucket, uint32_t size_bucket, TuneEntry* out) const;
     size_t size() const;
     // Text format, one entry per line:
-    //   kind tri_bucket size_bucket refill block stack wave_paths best_ms default_ms
+    //   kind tri_bucket size_bucket refill block stack wave_paths best_ms default_ms [order]
+    // (order: 0 input ray order, the default when absent; 1 coherence order)
     // Lines starting with '#' are comments.  load() merges into the cache (later lines win).
     void save(const std::string& path) const;
     void load(const std::string& path);

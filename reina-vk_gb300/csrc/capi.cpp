@@ -169,6 +169,12 @@ int reina_ctx_create(const reina_ctx_options* options, reina_ctx** out_ctx) {
         use_device(ctx.get());
         check_cuda(cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, ctx->device), "cudaDeviceGetAttribute");
         for (auto& s : ctx->streams) check_cuda(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "cudaStreamCreate");
+        // ray casts take their ordering scratch from the device's default stream-ordered pool: keep freed
+        // blocks in the pool instead of returning them at every synchronization
+        cudaMemPool_t pool;
+        check_cuda(cudaDeviceGetDefaultMemPool(&pool, ctx->device), "cudaDeviceGetDefaultMemPool");
+        uint64_t keep = 1ull << 30;
+        check_cuda(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep), "cudaMemPoolSetAttribute");
         ctx->err.alloc(sizeof(uint32_t));
         ctx->counters.alloc(2 * sizeof(unsigned long long));
         ctx->fetch.alloc(reina_ctx::kFetchSlots * sizeof(uint32_t));
@@ -208,6 +214,8 @@ int reina_ctx_set_tuning(reina_ctx* ctx, const reina_tuning* t) {
         tc.refill = (int)t->refill;
         tc.block = (int)(t->trace_block ? t->trace_block : rt::kTraceBlock);
         tc.stack = (int)(t->trace_stack ? t->trace_stack : rt::kDefaultTraceStack);
+        need(t->trace_order <= REINA_ORDER_COHERENT, "trace_order must be REINA_ORDER_INPUT or REINA_ORDER_COHERENT");
+        tc.sort = t->trace_order == REINA_ORDER_COHERENT ? 1 : 0;
         need(rt::valid_trace_config(tc), "trace_block must be 64, 128 or 256 and trace_stack 8, 12 or 16");
         const bool engine_changed = tc.block != ctx->trace.block || tc.stack != ctx->trace.stack;
         ctx->trace = tc;
@@ -227,6 +235,7 @@ int reina_ctx_get_tuning(const reina_ctx* ctx, reina_tuning* out) {
         out->refill = (uint32_t)ctx->trace.refill;
         out->trace_block = (uint32_t)ctx->trace.block;
         out->trace_stack = (uint32_t)ctx->trace.stack;
+        out->trace_order = ctx->trace.sort ? REINA_ORDER_COHERENT : REINA_ORDER_INPUT;
         out->wave_paths = ctx->wave_paths;
         out->batch_flags = ctx->batch_flags;
     });
@@ -857,6 +866,7 @@ void fill_tuning(const reina_ctx* ctx, const rt::TuneEntry& e, reina_tuning* t) 
     t->refill = (uint32_t)e.trace.refill;
     t->trace_block = (uint32_t)e.trace.block;
     t->trace_stack = (uint32_t)e.trace.stack;
+    t->trace_order = e.trace.sort ? REINA_ORDER_COHERENT : REINA_ORDER_INPUT;
     t->wave_paths = e.wave_paths ? e.wave_paths : ctx->wave_paths;
     t->batch_flags = ctx->batch_flags;
 }
@@ -878,7 +888,7 @@ void finish_tune(reina_ctx* ctx, uint32_t kind, uint64_t tris, uint64_t size, co
 }
 
 bool is_default(const rt::TraceConfig& c) {
-    return c.refill == 0 && c.block == rt::kTraceBlock && c.stack == rt::kDefaultTraceStack;
+    return c.refill == 0 && c.block == rt::kTraceBlock && c.stack == rt::kDefaultTraceStack && c.sort == 0;
 }
 
 }  // namespace

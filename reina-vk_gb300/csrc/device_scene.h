@@ -48,6 +48,8 @@ struct DeviceScene {
     const float* cdf_instances = nullptr;     // numInstances entries
     uint32_t emissive_count = 0;
     float emissive_weight = 0.0f;             // the `allInstancesArea` field = Σ weights
+    float bounds_lo[3] = {0.0f, 0.0f, 0.0f};  // world-space triangle bounds (ray binning frame)
+    float bounds_hi[3] = {0.0f, 0.0f, 0.0f};
 };
 
 }  // namespace rt

@@ -25,6 +25,7 @@ struct TraceConfig {
     int block = kTraceBlock;
     int stack = kDefaultTraceStack;
     int refill = kDefaultRefill;
+    int sort = 0;                 // ray casts (grid form): 1 = trace the rays in coherence order
 };
 bool valid_trace_config(const TraceConfig& c);
 

@@ -432,6 +432,10 @@ void Scene::upload() {
     dev_.cdf_instances = d_cdf_inst_.as<float>();
     dev_.emissive_count = (uint32_t)emissive_data_.size();
     dev_.emissive_weight = emissive_total_;
+    for (int k = 0; k < 3; ++k) {
+        dev_.bounds_lo[k] = bounds_lo_[k];
+        dev_.bounds_hi[k] = bounds_hi_[k];
+    }
     resident_ = true;
 }
 

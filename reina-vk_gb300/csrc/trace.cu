@@ -63,11 +63,12 @@ __global__ void RT_TRACE_BOUNDS(BLOCK) raycast_kernel_grid(const Bvh8Node* __res
                                                           const TriRecord* __restrict__ tris, uint32_t node_count,
                                                           const Ray* __restrict__ rays, uint32_t n,
                                                           Hit* __restrict__ hits, unsigned long long* counters,
-                                                          uint32_t* err_flag) {
+                                                          uint32_t* err_flag, const uint32_t* __restrict__ order) {
     __shared__ uint2 stack[SS * BLOCK];
-    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     TraceCounters c{0u, 0u};
-    if (i < n) {
+    if (k < n) {
+        const uint64_t i = order ? order[k] : k;   // thread k traces the k-th ray of the coherence order
         const float4* rp = reinterpret_cast<const float4*>(rays) + 2ull * i;
         const float4 a = __ldcs(rp), b = __ldcs(rp + 1);
         const TraceRay r = make_trace_ray(a.x, a.y, a.z, b.x, b.y, b.z, a.w, b.w);
@@ -84,6 +85,134 @@ __global__ void RT_TRACE_BOUNDS(BLOCK) raycast_kernel_grid(const Bvh8Node* __res
     reduce_counters<COUNT>(c, counters);
 }
 
+// ------------------------------------------------------------------------------------------------
+// Coherence order: rays binned by (direction octant, Morton code of the origin's cell on an 8^3 grid
+// over the bounds of the ray origins), bins in Morton order, rays in input order within a bin per warp.
+// Threads that trace consecutive rays of this order follow similar paths through the tree; hits are
+// written to each ray's own slot, so results do not depend on the order.
+constexpr int kBinBits = 12;
+constexpr uint32_t kBins = 1u << kBinBits;
+constexpr int kBinBlock = 256;
+
+// Float bits mapped to an unsigned key with the same order (min/max by integer atomics).
+__device__ __forceinline__ uint32_t ordered_bits(float f) {
+    const uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float from_ordered(uint32_t k) {
+    return __uint_as_float((k & 0x80000000u) ? (k & 0x7FFFFFFFu) : ~k);
+}
+
+// bounds[0..2] = ordered min of the origins, bounds[3..5] = ordered max (pre-set to 0xFFFFFFFF / 0).
+__global__ void __launch_bounds__(kBinBlock) k_ray_bounds(const Ray* __restrict__ rays, uint32_t n,
+                                                          uint32_t* __restrict__ bounds) {
+    uint32_t lo[3] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu}, hi[3] = {0u, 0u, 0u};
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const float4 a = __ldg(reinterpret_cast<const float4*>(rays) + 2ull * i);
+        const uint32_t k[3] = {ordered_bits(a.x), ordered_bits(a.y), ordered_bits(a.z)};
+        for (int c = 0; c < 3; ++c) {
+            lo[c] = min(lo[c], k[c]);
+            hi[c] = max(hi[c], k[c]);
+        }
+    }
+    for (int c = 0; c < 3; ++c)
+        for (int o = 16; o > 0; o >>= 1) {
+            lo[c] = min(lo[c], __shfl_xor_sync(0xFFFFFFFFu, lo[c], o));
+            hi[c] = max(hi[c], __shfl_xor_sync(0xFFFFFFFFu, hi[c], o));
+        }
+    if ((threadIdx.x & 31) == 0)
+        for (int c = 0; c < 3; ++c) {
+            atomicMin(bounds + c, lo[c]);
+            atomicMax(bounds + 3 + c, hi[c]);
+        }
+}
+
+__device__ __forceinline__ uint32_t spread3(uint32_t v) {   // 3 bits -> bits 0, 3, 6
+    return (v & 1u) | ((v & 2u) << 2) | ((v & 4u) << 4);
+}
+
+__device__ __forceinline__ uint32_t ray_bin(const Ray* rays, uint64_t i, const uint32_t* bounds) {
+    const float4* rp = reinterpret_cast<const float4*>(rays) + 2ull * i;
+    const float4 a = __ldg(rp), b = __ldg(rp + 1);
+    const uint32_t oct = (b.x < 0.0f ? 4u : 0u) | (b.y < 0.0f ? 2u : 0u) | (b.z < 0.0f ? 1u : 0u);
+    auto cell = [&](float x, int c) {
+        const float lo = from_ordered(bounds[c]), hi = from_ordered(bounds[3 + c]);
+        const float t = hi > lo ? (x - lo) / (hi - lo) * 8.0f : 0.0f;
+        return t >= 7.0f ? 7u : (t > 0.0f ? (uint32_t)t : 0u);   // NaN -> 0
+    };
+    return (oct << 9) | (spread3(cell(a.x, 0)) << 2) | (spread3(cell(a.y, 1)) << 1) | spread3(cell(a.z, 2));
+}
+
+// Per-block shared histograms, added to the global one with one atomic per non-empty bin and block.
+__global__ void __launch_bounds__(kBinBlock) k_ray_bins(const Ray* __restrict__ rays, uint32_t n,
+                                                        const uint32_t* __restrict__ bounds, uint32_t* __restrict__ bin_of,
+                                                        uint32_t* __restrict__ hist) {
+    __shared__ uint32_t h[kBins];
+    for (uint32_t b = threadIdx.x; b < kBins; b += blockDim.x) h[b] = 0;
+    __syncthreads();
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t b = ray_bin(rays, i, bounds);
+        bin_of[i] = b;
+        atomicAdd(h + b, 1u);
+    }
+    __syncthreads();
+    for (uint32_t b = threadIdx.x; b < kBins; b += blockDim.x)
+        if (h[b]) atomicAdd(hist + b, h[b]);
+}
+
+// Exclusive prefix sum of the kBins counts, in place (one block of 1024 threads, 4 bins each).
+__global__ void __launch_bounds__(1024) k_bin_offsets(uint32_t* __restrict__ hist) {
+    __shared__ uint32_t part[1024];
+    constexpr uint32_t per = kBins / 1024;
+    uint32_t local[per];
+    uint32_t sum = 0;
+    for (uint32_t j = 0; j < per; ++j) {
+        local[j] = hist[threadIdx.x * per + j];
+        sum += local[j];
+    }
+    part[threadIdx.x] = sum;
+    __syncthreads();
+    for (uint32_t off = 1; off < 1024; off <<= 1) {   // Hillis-Steele inclusive scan
+        const uint32_t v = threadIdx.x >= off ? part[threadIdx.x - off] : 0u;
+        __syncthreads();
+        part[threadIdx.x] += v;
+        __syncthreads();
+    }
+    uint32_t run = part[threadIdx.x] - sum;
+    for (uint32_t j = 0; j < per; ++j) {
+        hist[threadIdx.x * per + j] = run;
+        run += local[j];
+    }
+}
+
+__global__ void __launch_bounds__(kBinBlock) k_ray_scatter(const uint32_t* __restrict__ bin_of, uint32_t n,
+                                                           uint32_t* __restrict__ cursor, uint32_t* __restrict__ order) {
+    for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < n; base += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t i = base + threadIdx.x;
+        const bool valid = i < n;
+        const uint32_t b = valid ? bin_of[i] : 0xFFFFFFFFu;
+        const unsigned same = __match_any_sync(0xFFFFFFFFu, b);
+        const int lane = threadIdx.x & 31, leader = __ffs(same) - 1;
+        uint32_t pos = 0;
+        if (valid && lane == leader) pos = atomicAdd(cursor + b, (uint32_t)__popc(same));
+        pos = __shfl_sync(0xFFFFFFFFu, pos, leader);
+        if (valid) order[pos + __popc(same & ((1u << lane) - 1u))] = (uint32_t)i;
+    }
+}
+
+// Builds the coherence order of n rays in `order` (scratch: n bin ids, kBins counters, 6 bound words).
+static void ray_order(const Ray* d_rays, uint64_t n, uint32_t* bin_of, uint32_t* hist, uint32_t* bounds,
+                      uint32_t* order, int sm_count, cudaStream_t st) {
+    const int grid = std::max(1, std::min<int>((int)((n + kBinBlock - 1) / kBinBlock), 2 * std::max(1, sm_count)));
+    check_cuda(cudaMemsetAsync(hist, 0, kBins * sizeof(uint32_t), st), "cudaMemsetAsync");
+    check_cuda(cudaMemsetAsync(bounds, 0xFF, 3 * sizeof(uint32_t), st), "cudaMemsetAsync");
+    check_cuda(cudaMemsetAsync(bounds + 3, 0, 3 * sizeof(uint32_t), st), "cudaMemsetAsync");
+    k_ray_bounds<<<grid, kBinBlock, 0, st>>>(d_rays, (uint32_t)n, bounds);
+    k_ray_bins<<<grid, kBinBlock, 0, st>>>(d_rays, (uint32_t)n, bounds, bin_of, hist);
+    k_bin_offsets<<<1, 1024, 0, st>>>(hist);
+    k_ray_scatter<<<grid * 4, kBinBlock, 0, st>>>(bin_of, (uint32_t)n, hist, order);
+}
+
 template <bool ANY, bool COUNT>
 static int persistent_grid(int sm_count) {
     static int per_sm = -1;
@@ -97,18 +226,18 @@ static int persistent_grid(int sm_count) {
 
 template <bool ANY, bool COUNT, int BLOCK, int SS>
 static void launch_grid(const DeviceScene& s, const Ray* d_rays, uint64_t n, Hit* d_hits,
-                        unsigned long long* d_counters, uint32_t* d_err, cudaStream_t st) {
+                        unsigned long long* d_counters, uint32_t* d_err, const uint32_t* order, cudaStream_t st) {
     const uint64_t blocks = (n + BLOCK - 1) / BLOCK;
-    raycast_kernel_grid<ANY, COUNT, BLOCK, SS><<<(unsigned)blocks, BLOCK, 0, st>>>(s.nodes, s.tris, s.node_count, d_rays,
-                                                                                 (uint32_t)n, d_hits, d_counters, d_err);
+    raycast_kernel_grid<ANY, COUNT, BLOCK, SS><<<(unsigned)blocks, BLOCK, 0, st>>>(
+        s.nodes, s.tris, s.node_count, d_rays, (uint32_t)n, d_hits, d_counters, d_err, order);
 }
 
 template <bool ANY, int BLOCK>
 static void launch_grid_stack(int stack, const DeviceScene& s, const Ray* d_rays, uint64_t n, Hit* d_hits,
-                              uint32_t* d_err, cudaStream_t st) {
-    if (stack == 8) launch_grid<ANY, false, BLOCK, 8>(s, d_rays, n, d_hits, nullptr, d_err, st);
-    else if (stack == 16) launch_grid<ANY, false, BLOCK, 16>(s, d_rays, n, d_hits, nullptr, d_err, st);
-    else launch_grid<ANY, false, BLOCK, kSmemStack>(s, d_rays, n, d_hits, nullptr, d_err, st);
+                              uint32_t* d_err, const uint32_t* order, cudaStream_t st) {
+    if (stack == 8) launch_grid<ANY, false, BLOCK, 8>(s, d_rays, n, d_hits, nullptr, d_err, order, st);
+    else if (stack == 16) launch_grid<ANY, false, BLOCK, 16>(s, d_rays, n, d_hits, nullptr, d_err, order, st);
+    else launch_grid<ANY, false, BLOCK, kSmemStack>(s, d_rays, n, d_hits, nullptr, d_err, order, st);
 }
 
 template <bool ANY>
@@ -116,9 +245,17 @@ static void launch(const DeviceScene& s, const Ray* d_rays, uint64_t n, Hit* d_h
                    int sm_count, const TraceConfig& cfg, cudaStream_t st) {
     // grid form (also for more than 2^31 rays, where the persistent form's fetch counter could wrap)
     if (cfg.refill <= 0 || n > (1ull << 31)) {
-        if (cfg.block == 64) launch_grid_stack<ANY, 64>(cfg.stack, s, d_rays, n, d_hits, d_err, st);
-        else if (cfg.block == 256) launch_grid_stack<ANY, 256>(cfg.stack, s, d_rays, n, d_hits, d_err, st);
-        else launch_grid_stack<ANY, kTraceBlock>(cfg.stack, s, d_rays, n, d_hits, d_err, st);
+        uint32_t* scratch = nullptr;
+        const uint32_t* order = nullptr;
+        if (cfg.sort) {   // stream-ordered scratch: concurrent calls on other streams do not share it
+            check_cuda(cudaMallocAsync((void**)&scratch, (2 * n + kBins + 8) * sizeof(uint32_t), st), "cudaMallocAsync");
+            ray_order(d_rays, n, scratch, scratch + 2 * n, scratch + 2 * n + kBins, scratch + n, sm_count, st);
+            order = scratch + n;
+        }
+        if (cfg.block == 64) launch_grid_stack<ANY, 64>(cfg.stack, s, d_rays, n, d_hits, d_err, order, st);
+        else if (cfg.block == 256) launch_grid_stack<ANY, 256>(cfg.stack, s, d_rays, n, d_hits, d_err, order, st);
+        else launch_grid_stack<ANY, kTraceBlock>(cfg.stack, s, d_rays, n, d_hits, d_err, order, st);
+        if (scratch) check_cuda(cudaFreeAsync(scratch, st), "cudaFreeAsync");
         return;
     }
     const uint64_t needed = (n + kTraceBlock - 1) / kTraceBlock;
@@ -131,7 +268,7 @@ static void launch(const DeviceScene& s, const Ray* d_rays, uint64_t n, Hit* d_h
 bool valid_trace_config(const TraceConfig& c) {
     const bool block_ok = c.block == 0 || c.block == 64 || c.block == 128 || c.block == 256;
     const bool stack_ok = c.stack == 0 || c.stack == 8 || c.stack == 12 || c.stack == 16;
-    return block_ok && stack_ok && c.refill >= 0 && c.refill <= 32;
+    return block_ok && stack_ok && c.refill >= 0 && c.refill <= 32 && (c.sort == 0 || c.sort == 1);
 }
 
 void launch_raycast(const DeviceScene& s, const Ray* d_rays, uint64_t n, Hit* d_hits, bool any, uint32_t* d_err,
@@ -150,8 +287,8 @@ void launch_raycast_counters(const DeviceScene& s, const Ray* d_rays, uint64_t n
     if (n == 0) return;
     // The counting build uses the default grid form: visit counts do not depend on block size or stack
     // depth (warps hold the same 32 consecutive rays in every grid variant).
-    if (any) launch_grid<true, true, kTraceBlock, kSmemStack>(s, d_rays, n, nullptr, d_counters, d_err, st);
-    else launch_grid<false, true, kTraceBlock, kSmemStack>(s, d_rays, n, nullptr, d_counters, d_err, st);
+    if (any) launch_grid<true, true, kTraceBlock, kSmemStack>(s, d_rays, n, nullptr, d_counters, d_err, nullptr, st);
+    else launch_grid<false, true, kTraceBlock, kSmemStack>(s, d_rays, n, nullptr, d_counters, d_err, nullptr, st);
 }
 
 }  // namespace rt

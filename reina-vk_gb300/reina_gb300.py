@@ -84,10 +84,12 @@ class _CtxOptions(C.Structure):
 
 class _Tuning(C.Structure):
     _fields_ = [("refill", C.c_uint32), ("wave_paths", C.c_uint32), ("batch_flags", C.c_uint32),
-                ("trace_block", C.c_uint32), ("trace_stack", C.c_uint32), ("reserved", C.c_uint32 * 3)]
+                ("trace_block", C.c_uint32), ("trace_stack", C.c_uint32), ("trace_order", C.c_uint32),
+                ("reserved", C.c_uint32 * 2)]
 
 
-TUNING_FIELDS = ("refill", "wave_paths", "batch_flags", "trace_block", "trace_stack")
+TUNING_FIELDS = ("refill", "wave_paths", "batch_flags", "trace_block", "trace_stack", "trace_order")
+ORDER_INPUT, ORDER_COHERENT = 0, 1
 
 
 DEFAULT_WAVE_PATHS = 2097152

@@ -1,5 +1,5 @@
 """The autotuner on the GPU: every traversal variant it chooses between (grid form in three block sizes
-x three stack depths, persistent form) gives bit-identical hits; autotuned ray casts, renders and batched
+x three stack depths x coherence / input ray order, persistent form) gives bit-identical hits; autotuned ray casts, renders and batched
 renders pick a valid configuration, cache it, and with the cache in use give exactly the results of the
 default configuration."""
 import numpy as np
@@ -9,7 +9,8 @@ import scenes
 
 pytestmark = pytest.mark.gpu
 
-VARIANTS = [dict(refill=0, trace_block=b, trace_stack=s) for b in (64, 128, 256) for s in (8, 12, 16)] + \
+VARIANTS = [dict(refill=0, trace_block=b, trace_stack=s, trace_order=o) for b in (64, 128, 256) for s in (8, 12, 16)
+            for o in (0, 1)] + \
            [dict(refill=8, trace_block=128, trace_stack=12), dict(refill=16, trace_block=128, trace_stack=12)]
 
 
@@ -43,7 +44,7 @@ def test_all_variants_give_identical_hits(R, rc_setup, flags):
             ref = h
         else:
             assert np.array_equal(h, ref), v
-    ctx.set_tuning(refill=0, trace_block=128, trace_stack=12)
+    ctx.set_tuning(refill=0, trace_block=128, trace_stack=12, trace_order=0)
 
 
 def test_autotune_raycast_caches_and_applies(R, rc_setup):
@@ -56,7 +57,7 @@ def test_autotune_raycast_caches_and_applies(R, rc_setup):
     d_hits = torch.empty((n, 4), dtype=torch.float32, device="cuda")
     res = R.autotune_raycast(ctx, scene, d_rays.data_ptr(), n, d_hits.data_ptr(), 0, sp)
     torch.cuda.synchronize()
-    assert res["candidates"] == 11 and 0 < res["best_ms"] <= res["default_ms"]
+    assert res["candidates"] == 12 and 0 < res["best_ms"] <= res["default_ms"]
     best = res["best"]
     assert best["trace_block"] in (64, 128, 256) and best["trace_stack"] in (8, 12, 16)
     assert R.autotune_lookup(ctx, R.TUNE_RAYCAST_CLOSEST, scene.stats()["triangle_count"], n) == best
@@ -94,7 +95,13 @@ def test_autotune_render_and_batch(R):
         R.autotune_set_mode(ctx, R.AUTOTUNE_CACHED)
         out, _, _ = R.render(ctx, sc, pc, opts)
         assert np.array_equal(out, ref)
-        alone = [R.render(ctx, j.scene, j.pc, j.opts)[0] for j in jobs]
+        alone = []
+        R.autotune_set_mode(ctx, R.AUTOTUNE_OFF)
+        for j in jobs:   # each job alone in a batch, default configuration
+            one = R.RenderJob(j.scene, j.pc, j.opts)
+            R.render_batch(ctx, [one])
+            alone.append(one.accum)
+        R.autotune_set_mode(ctx, R.AUTOTUNE_CACHED)
         R.render_batch(ctx, jobs)
         for j, a in zip(jobs, alone):
             assert np.array_equal(j.accum, a)

@@ -2,9 +2,10 @@
 run, admission by device-memory budget, LRU eviction of scenes and kept images, progressive
 accumulation under an image key, cancellation and budget rejection.
 
-Every finished request must hold exactly the image reina_render gives for the same scene, push
-constants and options alone (the served kernels trace the same per-path sample streams and sum each
-pixel's samples in sample order)."""
+Every finished request must hold exactly the image the same request gets alone (one job in a batched
+render): the served kernels trace the same per-path sample streams and sum each pixel's samples in
+sample order, whatever else is running.  Against the single-scene entry point the bar is the per-sample
+tolerance (see test_batch_gpu)."""
 import threading
 import time
 
@@ -46,16 +47,27 @@ def make_pc(R, scene_weight, W, H, spp, bounces):
     return R.push_consts(iv, ip, total_emissive_weight=scene_weight, spp=spp, max_bounces=bounces, focus_dist=3.4)
 
 
+def render_alone(R, ctx, scene, pc, opts, accum=None):
+    """The request's image rendered alone: one job in a batched render."""
+    j = R.RenderJob(scene, pc, opts, accum=accum)
+    R.render_batch(ctx, [j])
+    return j.accum
+
+
 @pytest.fixture(scope="module")
 def alone(R):
-    """Each request rendered alone with reina_render on a context of its own."""
+    """Each request rendered alone on a context of its own; checked against reina_render within the
+    per-sample tolerance."""
     ctx = R.Context(0)
     built = {k: d.to_product(R, ctx) for k, d in descs(R).items()}
     weights = {k: s.emissive_weight for k, s in built.items()}
     out = []
     for key, W, H, spp, b, mode, env_mode, env, seed in request_specs():
         pc = make_pc(R, weights[key], W, H, spp, b)
-        acc, _, _ = R.render(ctx, built[key], pc, R.render_options(W, H, mode, seed, env_mode, env))
+        opts = R.render_options(W, H, mode, seed, env_mode, env)
+        acc = render_alone(R, ctx, built[key], pc, opts)
+        single, _, _ = R.render(ctx, built[key], pc, opts)
+        assert np.abs(acc[..., :3] - single[..., :3]).mean() <= 1e-3 * max(np.abs(single[..., :3]).mean(), 1e-6)
         out.append(acc)
     for s in built.values():
         s.close()
@@ -165,8 +177,8 @@ def test_progressive_accumulation_under_a_key(R):
     pc1 = make_pc(R, lone.emissive_weight, W, H, 3, 6)
     pc1.sampleBatch = 1
     opts = R.render_options(W, H, 1, 5)
-    a0, _, _ = R.render(ctx, lone, pc0, opts)
-    a1, _, _ = R.render(ctx, lone, pc1, opts, accum=a0.copy())
+    a0 = render_alone(R, ctx, lone, pc0, opts)
+    a1 = render_alone(R, ctx, lone, pc1, opts, accum=a0.copy())
     srv = R.Server(ctx, wave_paths=2048)
     sid = srv.add_scene(d.to_product(R, ctx))
     out0 = np.zeros((H, W, 4), np.float32)
@@ -202,8 +214,7 @@ def test_kept_images_are_evicted_and_restored(R):
         pc = make_pc(R, lone.emissive_weight, W, H, 1, 4)
         opts = R.render_options(W, H, 1, key)
         srv.wait(srv.submit(sid, pc, opts, None, image_key=key), 60.0)
-        a, _, _ = R.render(ctx, lone, pc, opts)
-        firsts.append((pc, opts, a))
+        firsts.append((pc, opts, render_alone(R, ctx, lone, pc, opts)))
     s = srv.stats()
     assert s["image_evictions"] > 0
     for key in range(1, 6):
@@ -211,7 +222,7 @@ def test_kept_images_are_evicted_and_restored(R):
         pc.sampleBatch = 1
         st = srv.wait(srv.submit(sid, pc, opts, None, image_key=key), 60.0)
         assert st["state"] == R.REQ_DONE
-        want, _, _ = R.render(ctx, lone, pc, opts, accum=a.copy())
+        want = render_alone(R, ctx, lone, pc, opts, accum=a.copy())
         assert np.array_equal(srv.fetch_image(key), want), key
     assert srv.stats()["image_restores"] > 0
     srv.close()
