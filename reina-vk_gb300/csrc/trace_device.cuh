@@ -172,18 +172,6 @@ __device__ __forceinline__ float q15(uint32_t word, int byte) {
     return __uint_as_float(__byte_perm(word, 0x3F800000u, 0x7604u | ((uint32_t)byte << 4)));
 }
 
-// Three-input minimum / maximum (single instructions on sm_100 and later).
-__device__ __forceinline__ float max3f(float a, float b, float c) {
-    float d;
-    asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
-    return d;
-}
-__device__ __forceinline__ float min3f(float a, float b, float c) {
-    float d;
-    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
-    return d;
-}
-
 // Node meta bytes with the octant applied: internal children (meta bits 3 and 4 both set; leaf offsets
 // are below 24) get their bit index XOR-ed with the ray's inverse octant, four children per word.
 __device__ __forceinline__ uint32_t octant_meta(uint32_t m, uint32_t oct_inv) {
@@ -228,8 +216,8 @@ __device__ __forceinline__ uint32_t intersect_children(const TraceRay& r, const 
         const float tfx = fmaf(q15(i < 4 ? farx0 : farx1, b), sx, ox);
         const float tfy = fmaf(q15(i < 4 ? fary0 : fary1, b), sy, oy);
         const float tfz = fmaf(q15(i < 4 ? farz0 : farz1, b), sz, oz);
-        const float tn = fmaxf(max3f(tnx, tny, tnz), r.tmin);
-        const float tf = fminf(min3f(tfx, tfy, tfz), tmax);
+        const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, r.tmin));
+        const float tf = fminf(fminf(tfx, tfy), fminf(tfz, tmax));
         if (tn <= tf) {
             const uint32_t meta = ((i < 4 ? meta0 : meta1) >> (8 * b)) & 0xFFu;
             hitmask |= (meta >> 5) << (meta & 31u);
