@@ -5,7 +5,8 @@ plus 1,048,576 rays with origins uniform in the sphere's AABB expanded 1.5x and 
 the sphere — against the 1.3M-triangle scene (level-8 displaced icosphere, 1,310,720 triangles, plus a
 2-triangle ground plane and a 2-triangle area light; 1,310,724 triangles).  Inputs and outputs stay
 resident in HBM for `value`; `e2e` runs the same step through the host-buffer C ABI call
-(reina_raycast) with the rays copied in from pinned host memory and the hits copied back every step.
+(reina_raycast) with the rays in pinned host memory and the hits written back to pinned host memory every
+step (the kernel reads and writes them in place over the coherent CPU-GPU link).
 L2 (129 MB) is flushed by writing a 512 MB buffer between timed steps (outside the timed events).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]

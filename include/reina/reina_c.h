@@ -223,7 +223,9 @@ enum {
     REINA_RAY_ANY = 1            /* first hit found in [tmin, tmax]; terminate traversal */
 };
 
-/* Host buffers: copies the rays to the GPU, traces them and copies the hits back (blocking). */
+/* Host buffers (blocking).  Page-locked buffers of the context's device (cudaHostAlloc /
+ * cudaHostRegister) are read and written in place by the kernel over the coherent CPU-GPU link; other
+ * buffers are copied to the GPU and back in chunks overlapped with the traversal. */
 int reina_raycast(reina_ctx* ctx, const reina_scene* scene, const reina_ray* rays, uint64_t count,
                   reina_hit* hits, uint32_t flags);
 

@@ -135,6 +135,22 @@ uint32_t check_device_errors(reina_ctx* ctx, cudaStream_t st) {
     return e;
 }
 
+// Device address of a page-locked host buffer mapped for `device` (16-byte aligned), or NULL for any other
+// memory (pageable, device memory, or pinned for another device).
+const void* host_device_pointer(const void* p, int device) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();   // clear the error of an unknown pointer
+        return nullptr;
+    }
+    if (a.type != cudaMemoryTypeHost || a.device != device || !a.devicePointer || ((uintptr_t)a.devicePointer % 16) != 0)
+        return nullptr;
+    return a.devicePointer;
+}
+void* host_device_pointer(void* p, int device) {
+    return const_cast<void*>(host_device_pointer(static_cast<const void*>(p), device));
+}
+
 // The traversal configuration for a workload: the cached autotuned one when the context uses the
 // cache and has an entry, else the context's tuning.
 rt::TraceConfig trace_for(const reina_ctx* ctx, uint32_t kind, uint64_t triangles, uint64_t size) {
@@ -357,9 +373,23 @@ int reina_raycast(reina_ctx* ctx, const reina_scene* scene, const reina_ray* ray
         need(count == 0 || (rays && hits), "NULL ray or hit buffer");
         if (count == 0) return;
         use_device(ctx);
+        const rt::TraceConfig cfg = trace_for(ctx, flags, s.triangle_count(), count);
+        // Pinned (page-locked) host buffers: the kernel reads the rays and writes the hits in host memory
+        // directly over the coherent CPU-GPU link, with no staging copies.
+        const rt::Ray* zr = static_cast<const rt::Ray*>(host_device_pointer(rays, ctx->device));
+        rt::Hit* zh = static_cast<rt::Hit*>(host_device_pointer(hits, ctx->device));
+        if (zr && zh && count < (1ull << 32)) {
+            cudaStream_t st = ctx->streams[0];
+            rt::launch_raycast(s.device_view(), zr, count, zh, flags == REINA_RAY_ANY, ctx->err.as<uint32_t>(),
+                               ctx->next_fetch_counter(), ctx->sm_count, cfg, st);
+            check_cuda(cudaGetLastError(), "raycast launch");
+            const uint32_t e = check_device_errors(ctx, st);
+            if (e) fail(REINA_ERR_DEVICE, "traversal kernel raised error flag " + std::to_string(e));
+            return;
+        }
         ctx->rays.reserve(count * sizeof(rt::Ray));
         ctx->hits.reserve(count * sizeof(rt::Hit));
-        // Pipeline copies and traversal over chunks on two streams.
+        // Pageable buffers: pipeline copies and traversal over chunks on two streams.
         const uint64_t chunk = count < (1ull << 20) ? count : std::max<uint64_t>(1ull << 19, (count + 7) / 8);
         int k = 0;
         for (uint64_t off = 0; off < count; off += chunk, ++k) {
@@ -369,8 +399,7 @@ int reina_raycast(reina_ctx* ctx, const reina_scene* scene, const reina_ray* ray
             rt::Hit* dh = ctx->hits.as<rt::Hit>() + off;
             check_cuda(cudaMemcpyAsync(dr, rays + off, n * sizeof(rt::Ray), cudaMemcpyHostToDevice, st), "cudaMemcpyAsync H2D");
             rt::launch_raycast(s.device_view(), dr, n, dh, flags == REINA_RAY_ANY, ctx->err.as<uint32_t>(),
-                               ctx->next_fetch_counter(), ctx->sm_count, trace_for(ctx, flags, s.triangle_count(), count),
-                               st);
+                               ctx->next_fetch_counter(), ctx->sm_count, cfg, st);
             check_cuda(cudaGetLastError(), "raycast launch");
             check_cuda(cudaMemcpyAsync(hits + off, dh, n * sizeof(rt::Hit), cudaMemcpyDeviceToHost, st), "cudaMemcpyAsync D2H");
         }

@@ -164,3 +164,19 @@ def test_large_scene_subset_and_counters(R, O, gpu_ctx):
     per_ray_nodes = nodes / rays.shape[0]
     assert 1.0 <= per_ray_nodes < 200
     assert 0.0 < ntris / rays.shape[0] < 500
+
+
+def test_raycast_page_locked_host_buffers(R, gpu_ctx):
+    """Page-locked host buffers are traced in place (no staging copies); the hits equal the device path."""
+    import torch
+
+    scene, v, i = scenes.sphere_scene(R, gpu_ctx, 4)
+    rays = scenes.raycast_rays(R, 4, 64, 64, 4096, v)
+    n = rays.shape[0]
+    h_rays = torch.from_numpy(rays.view(np.float32).reshape(n, 8).copy()).pin_memory()
+    h_hits = torch.zeros((n, 4), dtype=torch.float32).pin_memory()
+    for flags in (R.RAY_CLOSEST, R.RAY_ANY):
+        R.raycast_into(gpu_ctx, scene, h_rays.data_ptr(), n, h_hits.data_ptr(), flags)
+        ref = R.raycast(gpu_ctx, scene, rays, flags)   # pageable: copied in chunks
+        assert np.array_equal(h_hits.numpy().view(np.uint32).reshape(-1), ref.view(np.uint32).reshape(-1))
+    scene.close()
