@@ -194,6 +194,12 @@ int reina_scene_get_stats(const reina_scene* scene, reina_scene_stats* out_stats
  * bytes) to host buffers, for inspection and structural checks.  Either pointer may be NULL. */
 int reina_scene_export_bvh(const reina_scene* scene, void* nodes_out, void* triangles_out);
 
+/* Copies the scene's InstanceProperties records (polyglot.h; the records the closest-hit shaders read,
+ * built as src/scene/Scene.cpp:27-54 builds them) to `out` (capacity records; NULL to query the count
+ * only).  *out_count receives the number of records.  Available before and after the build. */
+int reina_scene_export_properties(const reina_scene* scene, InstanceProperties* out, uint32_t capacity,
+                                  uint32_t* out_count);
+
 /* Maps a global triangle id (as returned in reina_hit.prim) to (instance index, primitive index
  * within the instance's object) — the pair (gl_InstanceID, gl_PrimitiveID) of the reference. */
 int reina_scene_prim_info(const reina_scene* scene, uint32_t prim, uint32_t* out_instance,
@@ -454,16 +460,43 @@ typedef struct reina_gltf_stats {
     uint32_t primitives;          /* objects defined (triangle primitives) */
     uint32_t instances;           /* instances added (node x primitive) */
     uint32_t skipped_primitives;  /* non-triangle or empty primitives */
-    uint32_t ignored_textures;    /* texture references left out (textures are not supported yet) */
+    uint32_t ignored_textures;    /* texture references left out (image missing or not decodable) */
 } reina_gltf_stats;
 /* gltf::loadScene (src/scene/gltf/gltfloader.cpp:432-456, less the build): adds the default scene of a
  * .gltf or .glb file (buffers embedded, base64 data URIs or files beside it) to an unbuilt scene — one
  * object per triangle primitive, one instance per (node, primitive) with the node's world matrix, the
  * material mapped as gltfloader.cpp:380-412 maps it (Disney; emissive factor x strength when there is
  * no emissive texture; metallic; roughness clamped to [0.1, 0.7]; base colour; cull unless double-sided;
- * KHR_materials_ior; KHR_materials_transmission -> specular transmission, no culling).  A primitive
- * without normals fails as in the reference. */
+ * KHR_materials_ior; KHR_materials_transmission -> specular transmission, no culling; baseColorTexture
+ * -> texture_id, normalTexture -> normal_map_id).  Every image of the file becomes a scene texture in
+ * image order (gltfloader.cpp:283-340; never flipped); images that do not decode (formats other than
+ * PNG) are left out and the references to them counted in ignored_textures.  A primitive without
+ * normals fails as in the reference. */
 int reina_scene_add_gltf(reina_scene* scene, const char* path, reina_gltf_stats* out_stats);
+
+/* Textures (Scene::defineTexture, src/scene/Scene.cpp:15-25; sampled by the closest-hit shaders through
+ * texture_id / normal_map_id / bump_map_id of reina_material).  Texels are 8-bit RGBA, rows top to
+ * bottom, row 0 at v = 0; sampling is bilinear at level 0 with REPEAT addressing (the sampler of
+ * src/tools/vktools.cpp:765-780 on an R8G8B8A8_UNORM image).  The returned ids count from 0 in
+ * definition order; material ids are checked against them at reina_scene_build (REINA_ERR_INVALID).
+ *   _rgba8:   raw texels (width*height*4 bytes)
+ *   _file:    an image file, rows flipped vertically as the reference loads paths (src/graphics/Image.cpp:14)
+ *   _encoded: an image file's bytes in memory, not flipped (src/graphics/Image.cpp:27-33)
+ * Image files: PNG (every colour type and bit depth, as stbi_load(..., 4) converts them); other formats
+ * fail with REINA_ERR_IO. */
+int reina_scene_define_texture_rgba8(reina_scene* scene, const uint8_t* rgba8, uint32_t width, uint32_t height,
+                                     uint32_t* out_texture_id);
+int reina_scene_define_texture_file(reina_scene* scene, const char* path, uint32_t* out_texture_id);
+int reina_scene_define_texture_encoded(reina_scene* scene, const void* data, uint64_t bytes, uint32_t* out_texture_id);
+int reina_scene_texture_count(const reina_scene* scene, uint32_t* out_count);
+/* Copies texture `texture_id`'s texels out (rgba8 = NULL: size only; else rgba8_capacity >= w*h*4). */
+int reina_scene_export_texture(const reina_scene* scene, uint32_t texture_id, uint32_t* out_width,
+                               uint32_t* out_height, uint8_t* rgba8, uint64_t rgba8_capacity);
+
+/* Decodes an image file's bytes to RGBA8 (the conversion the texture calls apply).  Pass rgba8 = NULL to
+ * receive only the size; otherwise rgba8_capacity must hold width*height*4 bytes. */
+int reina_decode_image(const void* data, uint64_t bytes, uint32_t* out_width, uint32_t* out_height, uint8_t* rgba8,
+                       uint64_t rgba8_capacity);
 
 /* Number of objects of a scene, and the model data stored for one (the arrays are copied out; pass NULL
  * for any of them, and *_count pointers receive the sizes in elements: vertices, indices, TBNs, UVs). */

@@ -163,7 +163,9 @@ _SHADING_SIGS.update({
     "oracle_scene_new": (C.c_void_p, []),
     "oracle_scene_free": (None, [C.c_void_p]),
     "oracle_scene_add_object": (C.c_uint32, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint64, C.c_void_p,
-                                             C.c_uint64, C.c_void_p, C.c_uint64]),
+                                             C.c_uint64, C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint64, C.c_void_p,
+                                             C.c_uint64]),
+    "oracle_scene_add_texture": (C.c_uint32, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32]),
     "oracle_scene_add_instance": (None, [C.c_void_p, C.c_uint32, C.c_void_p, C.POINTER(OMaterial), C.c_uint32,
                                          C.c_void_p]),
     "oracle_scene_finalize": (None, [C.c_void_p]),
@@ -189,13 +191,23 @@ class Scene:
         except Exception:
             pass
 
-    def add_object(self, v4, idx, tbn9=None, tbn_idx=None) -> int:
+    def add_object(self, v4, idx, tbn9=None, tbn_idx=None, uv=None, uv_idx=None) -> int:
         v = np.ascontiguousarray(v4, np.float32).reshape(-1, 4)
         i = np.ascontiguousarray(idx, np.uint32).reshape(-1)
         t = None if tbn9 is None else np.ascontiguousarray(tbn9, np.float32).reshape(-1, 9)
         ti = None if tbn_idx is None else np.ascontiguousarray(tbn_idx, np.uint32).reshape(-1)
+        u = None if uv is None else np.ascontiguousarray(uv, np.float32).reshape(-1, 2)
+        ui = None if uv_idx is None else np.ascontiguousarray(uv_idx, np.uint32).reshape(-1)
         return int(lib().oracle_scene_add_object(self._h, _p(v), v.shape[0], _p(i), i.size, _p(t),
-                                                 0 if t is None else t.shape[0], _p(ti), 0 if ti is None else ti.size))
+                                                 0 if t is None else t.shape[0], _p(ti), 0 if ti is None else ti.size,
+                                                 _p(u), 0 if u is None else u.shape[0], _p(ui),
+                                                 0 if ui is None else ui.size))
+
+    def add_texture(self, rgba8) -> int:
+        """An RGBA8 texture (H, W, 4) uint8, row 0 at v = 0."""
+        a = np.ascontiguousarray(rgba8, np.uint8)
+        self._keep.append(a)
+        return int(lib().oracle_scene_add_texture(self._h, _p(a), a.shape[1], a.shape[0]))
 
     def add_instance(self, obj: int, transform16, materials: list, face_material=None) -> None:
         T = np.ascontiguousarray(transform16, np.float32).reshape(16)

@@ -63,6 +63,14 @@ struct OObject {
     std::vector<uint32_t> idx;
     std::vector<float> tbn;      // 9 per entry (columns T, B, N)
     std::vector<uint32_t> tbn_idx;
+    std::vector<float> uv;       // 2 per entry
+    std::vector<uint32_t> uv_idx;   // 3 per triangle (0xFFFFFFFF: corner without UV)
+};
+
+// An RGBA8 texture, rows top to bottom (row 0 at v = 0), texel = r | g << 8 | b << 16 | a << 24.
+struct OTexture {
+    uint32_t w = 0, h = 0;
+    std::vector<uint32_t> texels;
 };
 
 struct OInstance {
@@ -86,6 +94,7 @@ struct OScene {
     std::vector<uint32_t> emissive;     // instance index per emissive position
     std::vector<float> cdf_instances, cdf_triangles;
     float total_weight = 0;
+    std::vector<OTexture> textures;
 };
 
 }  // namespace oracle
@@ -135,10 +144,11 @@ struct HitInfo {
     Vec3<T> worldPosition, worldNormal, worldNormalGeometry;
     bool frontFace;
     Mat3<T> tbn;
+    T uv[2];
 };
 
-// closestHitCommon.h.glsl:52-148 (UVs omitted: without textures they only feed the out-of-[0,1] skip,
-// which mod(uv, 1) makes unreachable).
+// closestHitCommon.h.glsl:52-148.  UV: barycentric blend of the corner texture coordinates, (0, 0) for a
+// model without them; a corner whose texture index is 0xFFFFFFFF contributes (0, 0).
 template <class T>
 HitInfo<T> getObjectHitInfo(const OScene& s, uint32_t prim, T bu, T bv, Vec3<T> rayDir) {
     const OInstance& inst = s.instances[s.prim_inst[prim]];
@@ -151,6 +161,16 @@ HitInfo<T> getObjectHitInfo(const OScene& s, uint32_t prim, T bu, T bv, Vec3<T> 
     HitInfo<T> h;
     const Vec3<T> objPos = v0 * b0 + v1 * bu + v2 * bv;
     h.worldPosition = xform_point(inst.T, objPos);
+    h.uv[0] = h.uv[1] = (T)0;
+    if (!o.uv.empty() && !o.uv_idx.empty()) {
+        T c[3][2];
+        for (int k = 0; k < 3; ++k) {
+            const uint32_t t = o.uv_idx[3 * lp + k];
+            c[k][0] = t == 0xFFFFFFFFu ? (T)0 : (T)o.uv[2ull * t];
+            c[k][1] = t == 0xFFFFFFFFu ? (T)0 : (T)o.uv[2ull * t + 1];
+        }
+        for (int a = 0; a < 2; ++a) h.uv[a] = c[0][a] * b0 + c[1][a] * bu + c[2][a] * bv;
+    }
     const Vec3<T> ng = normalize(cross(v1 - v0, v2 - v0));
     const bool have_tbn = !o.tbn_idx.empty();
     Vec3<T> on = ng;
@@ -199,6 +219,107 @@ HitInfo<T> getObjectHitInfo(const OScene& s, uint32_t prim, T bu, T bv, Vec3<T> 
     wN = wN * (h.frontFace ? (T)1 : (T)-1);
     h.tbn = Mat3<T>{wT, wB, wN};
     return h;
+}
+
+// ---- textures (texutils.h.glsl, the sampler of src/tools/vktools.cpp:765-780) ----------------------
+
+// One axis of bilinear addressing with REPEAT wrapping: coordinate c * size - 0.5, texels floor() and
+// floor() + 1 modulo the size, weight frac(); non-finite coordinates address texel 0 with weight 0.
+template <class T>
+void tex_axis(T c, uint32_t size, uint32_t& i0, uint32_t& i1, T& w) {
+    const T fs = (T)size;
+    T x = c * fs - (T)0.5;
+    if (!(std::fabs(x) <= (T)3.0e38)) x = 0;
+    const T fx = std::floor(x);
+    w = x - fx;
+    T r = std::fmod(fx, fs);
+    if (r < (T)0) r = r + fs;
+    i0 = (uint32_t)r;
+    i1 = i0 + 1u == size ? 0u : i0 + 1u;
+}
+
+// texture(sampler2D, uv) at level 0 on R8G8B8A8_UNORM texels: the four texels' 8-bit values blended with
+// the bilinear weights, then divided by 255.
+template <class T>
+void tex_sample(const OScene& s, int id, T u, T v, T out[4]) {
+    const OTexture& t = s.textures[(size_t)id];
+    uint32_t x0, x1, y0, y1;
+    T a, b;
+    tex_axis(u, t.w, x0, x1, a);
+    tex_axis(v, t.h, y0, y1, b);
+    const uint32_t c00 = t.texels[(size_t)y0 * t.w + x0], c10 = t.texels[(size_t)y0 * t.w + x1];
+    const uint32_t c01 = t.texels[(size_t)y1 * t.w + x0], c11 = t.texels[(size_t)y1 * t.w + x1];
+    const T na = (T)1 - a, nb = (T)1 - b;
+    const T w00 = na * nb, w10 = a * nb, w01 = na * b, w11 = a * b;
+    for (int k = 0; k < 4; ++k) {
+        const int sh = 8 * k;
+        T acc = w00 * (T)((c00 >> sh) & 255u);
+        acc = acc + w10 * (T)((c10 >> sh) & 255u);
+        acc = acc + w01 * (T)((c01 >> sh) & 255u);
+        acc = acc + w11 * (T)((c11 >> sh) & 255u);
+        out[k] = acc / (T)255;
+    }
+}
+
+// texutils.h.glsl:4-45 bumpMapping (parallax search of the height map's red channel).
+template <class T>
+void bumpMapping(const OScene& s, int id, T uv[2], Vec3<T> rayIn, const Mat3<T>& tbn) {
+    const T heightScale = (T)0.2, minLayers = (T)64, maxLayers = (T)512;
+    const Vec3<T> V = normalize(mulT(tbn, -rayIn));
+    if (V.z <= (T)0) return;
+    const T numLayers = mixs(maxLayers, minLayers, std::fmin(std::fmax(V.z, (T)0), (T)1));
+    const T layerDepth = (T)1 / numLayers;
+    const T P[2] = {V.x / V.z * heightScale, V.y / V.z * heightScale};
+    const T d[2] = {P[0] / numLayers, P[1] / numLayers};
+    T cur[2] = {uv[0], uv[1]};
+    T depthSum = 0;
+    T tex[4];
+    tex_sample(s, id, cur[0], cur[1], tex);
+    T h = tex[0] * heightScale;
+    for (int it = 0; depthSum < h && it < 1024; ++it) {
+        cur[0] = cur[0] - d[0];
+        cur[1] = cur[1] - d[1];
+        depthSum = depthSum + layerDepth;
+        tex_sample(s, id, cur[0], cur[1], tex);
+        h = tex[0] * heightScale;
+    }
+    const T prev[2] = {cur[0] + d[0], cur[1] + d[1]};
+    tex_sample(s, id, prev[0], prev[1], tex);
+    const T hPrev = tex[0] * heightScale;
+    const T sumPrev = depthSum - layerDepth;
+    const T after = h - depthSum;
+    const T before = hPrev - sumPrev;
+    const T weight = after / (after - before);
+    uv[0] = mixs(prev[0], cur[0], weight);
+    uv[1] = mixs(prev[1], cur[1], weight);
+}
+
+// The texture stage of the closest-hit shaders (lambertian.rchit.glsl:20-58, metal.rchit.glsl:18-50,
+// dielectric.rchit.glsl:54-73, disney.rchit.glsl:19-72): uv = mod(uv, 1), bump mapping, the
+// out-of-[0,1] skip (uv_check), the normal map, and the albedo texture with its alpha test (alpha_test).
+// Returns false when the hit is skipped.
+template <class T>
+bool apply_textures(const OScene& s, const HitInfo<T>& hit, const OMaterial& m, Vec3<T> rayDir, uint32_t& rng,
+                    bool uv_check, bool alpha_test, Vec3<T>& n, Vec3<T>& albedo) {
+    n = hit.worldNormal;
+    albedo = load3<T>(m.albedo);
+    if (m.texture_id < 0 && m.normal_map_id < 0 && m.bump_map_id < 0) return true;
+    T uv[2] = {hit.uv[0] - std::floor(hit.uv[0]), hit.uv[1] - std::floor(hit.uv[1])};
+    if (m.bump_map_id >= 0) bumpMapping(s, m.bump_map_id, uv, normalize(rayDir), hit.tbn);
+    if (uv_check && (uv[0] < (T)0 || uv[0] > (T)1 || uv[1] < (T)0 || uv[1] > (T)1)) return false;
+    T tex[4];
+    if (m.normal_map_id >= 0) {
+        tex_sample(s, m.normal_map_id, uv[0], uv[1], tex);
+        Vec3<T> tn(tex[0] * (T)2 - (T)1, tex[1] * (T)2 - (T)1, tex[2] * (T)2 - (T)1);
+        tn.y = tn.y * (T)-1;
+        n = normalize(mul(hit.tbn, tn));
+    }
+    if (m.texture_id >= 0) {
+        tex_sample(s, m.texture_id, uv[0], uv[1], tex);
+        if (alpha_test && tex[3] < (T)0.999 && rng_random<T>(rng) > tex[3]) return false;
+        albedo = albedo * Vec3<T>(tex[0], tex[1], tex[2]);
+    }
+    return true;
 }
 
 // Per-path payload (shaderCommon.h.glsl:18-36), the fields the raygen loop reads.
@@ -261,10 +382,11 @@ void trace_and_shade(const Ctx<T>& c, Vec3<T> org, Vec3<T> dir, Payload<T>& pld)
         pld.rayHitSky = false;
         pld.skip = true;
     };
-    const Vec3<T> worldNormal = hit.worldNormal;
+    Vec3<T> worldNormal, texAlbedo;
     if (m.material_idx == 0) {   // lambertian.rchit.glsl:11-78
         if (m.cull_backface && !hit.frontFace) { do_skip(); return; }
-        pld.color = load3<T>(m.albedo);
+        if (!apply_textures(c.s, hit, m, dir, pld.rng, true, true, worldNormal, texAlbedo)) { do_skip(); return; }
+        pld.color = texAlbedo;
         pld.albedo = pld.color;
         pld.emission = load3<T>(m.emission);
         pld.rayOrigin = offsetAlongNormal(hit.worldPosition, hit.worldNormalGeometry);
@@ -282,7 +404,8 @@ void trace_and_shade(const Ctx<T>& c, Vec3<T> org, Vec3<T> dir, Payload<T>& pld)
         pld.accumulatedDistance = 0;
     } else if (m.material_idx == 1) {   // metal.rchit.glsl:7-70
         if (m.cull_backface && !hit.frontFace) { do_skip(); return; }
-        pld.color = load3<T>(m.albedo);
+        if (!apply_textures(c.s, hit, m, dir, pld.rng, false, true, worldNormal, texAlbedo)) { do_skip(); return; }
+        pld.color = texAlbedo;
         pld.albedo = pld.color;
         pld.emission = load3<T>(m.emission);
         pld.rayOrigin = offsetAlongNormal(hit.worldPosition, hit.worldNormalGeometry);
@@ -302,12 +425,13 @@ void trace_and_shade(const Ctx<T>& c, Vec3<T> org, Vec3<T> dir, Payload<T>& pld)
         const T ior = (T)m.ior;
         const T ri = hit.frontFace ? (T)1 / ior : ior;
         const Vec3<T> unitDir = normalize(dir);
-        const T cosT = std::min(dot(-unitDir, worldNormal), (T)1);
+        const T cosT = std::min(dot(-unitDir, hit.worldNormal), (T)1);
         const T sinT = std::sqrt((T)1 - cosT * cosT);
         const bool cannot = ri * sinT > (T)1;
         const T refl = reflectance(cosT, ri);
         const bool prevInside = pld.insideDielectric;
-        const Vec3<T> albedo = load3<T>(m.albedo);
+        apply_textures(c.s, hit, m, dir, pld.rng, false, false, worldNormal, texAlbedo);
+        const Vec3<T> albedo = texAlbedo;
         if (cannot || refl > rng_random<T>(pld.rng)) {
             pld.rayDirection = fuzzyReflection<T>(unitDir, worldNormal, (T)m.roughness, pld.rng);
             pld.color = Vec3<T>((T)1, (T)1, (T)1);
@@ -337,7 +461,8 @@ void trace_and_shade(const Ctx<T>& c, Vec3<T> org, Vec3<T> dir, Payload<T>& pld)
         pld.eta = 0;
     } else {   // disney.rchit.glsl:36-198
         if (m.cull_backface && !hit.frontFace) { do_skip(); return; }
-        const Vec3<T> albedo = load3<T>(m.albedo);
+        if (!apply_textures(c.s, hit, m, dir, pld.rng, true, true, worldNormal, texAlbedo)) { do_skip(); return; }
+        const Vec3<T> albedo = texAlbedo;
         const T ior = (T)m.ior;
         const T eta = hit.frontFace ? (T)1 / ior : ior;
         const DisneyParams<T> p = disney_params<T>(m, albedo);
@@ -726,13 +851,16 @@ void oracle_scene_free(void* h) {
 }
 
 uint32_t oracle_scene_add_object(void* h, const float* v4, uint64_t nv, const uint32_t* idx, uint64_t nidx,
-                                 const float* tbn9, uint64_t ntbn, const uint32_t* tbn_idx, uint64_t ntbn_idx) {
+                                 const float* tbn9, uint64_t ntbn, const uint32_t* tbn_idx, uint64_t ntbn_idx,
+                                 const float* uv2, uint64_t nuv, const uint32_t* uv_idx, uint64_t nuv_idx) {
     OScene* s = static_cast<OScene*>(h);
     OObject o;
     o.v.assign(v4, v4 + 4 * nv);
     o.idx.assign(idx, idx + nidx);
     if (tbn9 && ntbn) o.tbn.assign(tbn9, tbn9 + 9 * ntbn);
     if (tbn_idx && ntbn_idx) o.tbn_idx.assign(tbn_idx, tbn_idx + ntbn_idx);
+    if (uv2 && nuv) o.uv.assign(uv2, uv2 + 2 * nuv);
+    if (uv_idx && nuv_idx) o.uv_idx.assign(uv_idx, uv_idx + nuv_idx);
     s->objects.push_back(std::move(o));
     return (uint32_t)(s->objects.size() - 1);
 }
@@ -746,6 +874,19 @@ void oracle_scene_add_instance(void* h, uint32_t obj, const float* T16, const OM
     inst.mats.assign(mats, mats + nmat);
     if (face_mat) inst.face_mat.assign(face_mat, face_mat + s->objects[obj].idx.size() / 3);
     s->instances.push_back(std::move(inst));
+}
+
+uint32_t oracle_scene_add_texture(void* h, const uint8_t* rgba8, uint32_t w, uint32_t hgt) {
+    OScene* s = static_cast<OScene*>(h);
+    OTexture t;
+    t.w = w;
+    t.h = hgt;
+    t.texels.resize((size_t)w * hgt);
+    for (size_t i = 0; i < t.texels.size(); ++i)
+        t.texels[i] = (uint32_t)rgba8[4 * i] | ((uint32_t)rgba8[4 * i + 1] << 8) | ((uint32_t)rgba8[4 * i + 2] << 16) |
+                      ((uint32_t)rgba8[4 * i + 3] << 24);
+    s->textures.push_back(std::move(t));
+    return (uint32_t)(s->textures.size() - 1);
 }
 
 void oracle_scene_finalize(void* h) { finalize_scene(*static_cast<OScene*>(h)); }

@@ -152,10 +152,10 @@ __global__ void __launch_bounds__(kBlock, kShadeMinBlocks) kb_shade(BatchLaunch 
             float acc = ps.acc[p];
             const bool inside = (flags & kFlagInside) != 0;
             Vertex vx;
-            if (MAT == 1) vx = shade_lambert(h, pr, rd, rng, inside, acc);
-            else if (MAT == 2) vx = shade_metal(h, pr, rd, rng, inside, acc);
-            else if (MAT == 3) vx = shade_dielectric(h, pr, ro, rd, rng, inside, acc);
-            else vx = shade_disney(h, pr, ro, rd, rng, inside, acc);
+            if (MAT == 1) vx = shade_lambert(J.s, h, pr, rd, rng, inside, acc);
+            else if (MAT == 2) vx = shade_metal(J.s, h, pr, rd, rng, inside, acc);
+            else if (MAT == 3) vx = shade_dielectric(J.s, h, pr, ro, rd, rng, inside, acc);
+            else vx = shade_disney(J.s, h, pr, ro, rd, rng, inside, acc);
             if (vx.skip) {
                 flags &= ~kFlagPrevNee;
             } else {
@@ -168,7 +168,7 @@ __global__ void __launch_bounds__(kBlock, kShadeMinBlocks) kb_shade(BatchLaunch 
                         if ((flags & kFlagPrevNee) && (vx.emission.x != 0.0f || vx.emission.y != 0.0f || vx.emission.z != 0.0f))
                             contrib = contrib * power_heuristic(ps.ppdf[p], light_pdf_sa(J.s, tw, prim, ro, vx.newO));
                         const bool do_nee = (MAT == 1 || MAT == 4) && J.s.emissive_count > 0;
-                        if (do_nee) emit = next_event(J.s, tw, rng, MAT == 4, vx.newO, h.n, vx.albedo, pr, h.tbn, rd, thr, sh);
+                        if (do_nee) emit = next_event(J.s, tw, rng, MAT == 4, vx.newO, vx.n, vx.albedo, pr, h.tbn, rd, thr, sh);
                         flags = do_nee ? (flags | kFlagPrevNee) : (flags & ~kFlagPrevNee);
                         ps.ppdf[p] = vx.pdf;
                     }

@@ -18,6 +18,7 @@
 #include "config.h"
 #include "errors.h"
 #include "generators.h"
+#include "image.h"
 #include "kernels.h"
 #include "loaders.h"
 #include "post.h"
@@ -1110,6 +1111,81 @@ int reina_scene_add_gltf(reina_scene* scene, const char* path, reina_gltf_stats*
             out->instances = st.instances;
             out->skipped_primitives = st.skipped_primitives;
             out->ignored_textures = st.ignored_textures;
+        }
+    });
+}
+
+int reina_scene_define_texture_rgba8(reina_scene* scene, const uint8_t* rgba8, uint32_t width, uint32_t height,
+                                     uint32_t* out_id) {
+    return guard([&] {
+        need(scene && scene->s && rgba8 && out_id, "NULL argument");
+        need(width > 0 && height > 0, "texture has zero size");
+        need((uint64_t)width * height <= (1ull << 28), "texture larger than 2^28 texels");
+        rt::Image img;
+        img.width = width;
+        img.height = height;
+        img.rgba.assign(rgba8, rgba8 + (size_t)width * height * 4);
+        *out_id = scene->s->define_texture(std::move(img));
+    });
+}
+
+int reina_scene_define_texture_file(reina_scene* scene, const char* path, uint32_t* out_id) {
+    return guard([&] {
+        need(scene && scene->s && path && out_id, "NULL argument");
+        *out_id = scene->s->define_texture(rt::load_image(path, true));
+    });
+}
+
+int reina_scene_define_texture_encoded(reina_scene* scene, const void* data, uint64_t bytes, uint32_t* out_id) {
+    return guard([&] {
+        need(scene && scene->s && data && out_id, "NULL argument");
+        *out_id = scene->s->define_texture(rt::decode_image(static_cast<const uint8_t*>(data), (size_t)bytes));
+    });
+}
+
+int reina_scene_export_properties(const reina_scene* scene, InstanceProperties* out, uint32_t capacity,
+                                  uint32_t* out_count) {
+    return guard([&] {
+        need(scene && scene->s && out_count, "NULL argument");
+        const std::vector<InstanceProperties>& p = scene->s->instance_properties();
+        *out_count = (uint32_t)p.size();
+        if (out) {
+            need(capacity >= p.size(), "capacity smaller than the number of records");
+            std::memcpy(out, p.data(), p.size() * sizeof(InstanceProperties));
+        }
+    });
+}
+
+int reina_scene_texture_count(const reina_scene* scene, uint32_t* out) {
+    return guard([&] {
+        need(scene && scene->s && out, "NULL argument");
+        *out = (uint32_t)scene->s->texture_count();
+    });
+}
+
+int reina_scene_export_texture(const reina_scene* scene, uint32_t id, uint32_t* w, uint32_t* h, uint8_t* rgba8,
+                               uint64_t cap) {
+    return guard([&] {
+        need(scene && scene->s && w && h, "NULL argument");
+        const rt::Image& img = scene->s->texture(id);
+        *w = img.width;
+        *h = img.height;
+        if (rgba8) {
+            need(cap >= img.rgba.size(), "rgba8_capacity smaller than width*height*4");
+            std::memcpy(rgba8, img.rgba.data(), img.rgba.size());
+        }
+    });
+}
+
+int reina_decode_image(const void* data, uint64_t bytes, uint32_t* w, uint32_t* h, uint8_t* rgba8, uint64_t cap) {
+    return guard([&] {
+        need(data && w && h, "NULL argument");
+        const rt::Image img = rt::decode_image(static_cast<const uint8_t*>(data), (size_t)bytes);
+        *w = img.width;
+        *h = img.height;
+        if (rgba8) {
+            need(cap >= img.rgba.size(), "rgba8_capacity smaller than width*height*4");
+            std::memcpy(rgba8, img.rgba.data(), img.rgba.size());
         }
     });
 }

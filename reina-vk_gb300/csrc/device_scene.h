@@ -3,6 +3,8 @@
 
 #include <stdint.h>
 
+#include <vector_types.h>
+
 #include "rt_common.h"
 #include "../../include/reina/polyglot.h"
 
@@ -48,6 +50,10 @@ struct DeviceScene {
     const float* cdf_instances = nullptr;     // numInstances entries
     uint32_t emissive_count = 0;
     float emissive_weight = 0.0f;             // the `allInstancesArea` field = Σ weights
+    // textures (src/scene/Scene.cpp:59-80; sampled as R8G8B8A8_UNORM, src/graphics/Image.cpp:56)
+    const uint32_t* tex_texels = nullptr;     // RGBA8 texels of all textures, one word each
+    const uint4* tex_info = nullptr;          // per texture: first texel, width, height, 0
+    uint32_t tex_count = 0;
     float bounds_lo[3] = {0.0f, 0.0f, 0.0f};  // world-space triangle bounds (ray binning frame)
     float bounds_hi[3] = {0.0f, 0.0f, 0.0f};
 };

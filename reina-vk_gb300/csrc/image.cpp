@@ -1,0 +1,492 @@
+// PNG decoding (PNG specification, ISO/IEC 15948) over an RFC 1950/1951 inflater, producing the RGBA8
+// texels the reference gets from stbi_load(..., 4) (src/graphics/Image.cpp:15, 29-33).
+#include "image.h"
+
+#include <algorithm>
+#include <cstring>
+#include <fstream>
+#include <iterator>
+
+#include "errors.h"
+
+namespace rt {
+
+namespace {
+
+[[noreturn]] void bad(const std::string& what) { fail(REINA_ERR_IO, what); }
+
+// ---- inflate -------------------------------------------------------------------------------------
+
+class Bits {
+public:
+    Bits(const uint8_t* p, size_t n) : p_(p), n_(n) {}
+    // Tops the bit buffer up to at least 57 bits (zeros past the end of the input; real_ counts the rest).
+    void fill() {
+        while (cnt_ <= 56) {
+            const uint64_t b = pos_ < n_ ? p_[pos_] : 0u;
+            if (pos_ < n_) real_ += 8;
+            ++pos_;
+            buf_ |= b << cnt_;
+            cnt_ += 8;
+        }
+    }
+    uint32_t peek(int k) {
+        if (cnt_ < k) fill();
+        return (uint32_t)(buf_ & ((1ull << k) - 1ull));
+    }
+    void drop(int k) {
+        if (k > real_) bad("truncated deflate stream");
+        buf_ >>= k;
+        cnt_ -= k;
+        real_ -= k;
+    }
+    uint32_t get(int k) {
+        if (k == 0) return 0;
+        const uint32_t v = peek(k);
+        drop(k);
+        return v;
+    }
+    void align() {
+        const int k = cnt_ & 7;
+        buf_ >>= k;
+        cnt_ -= k;
+        real_ = std::max(0, real_ - k);
+    }
+    // Byte-aligned input position (after align()).
+    size_t byte_pos() const { return pos_ - (size_t)(cnt_ / 8); }
+    void skip_to(size_t byte) {
+        pos_ = byte;
+        buf_ = 0;
+        cnt_ = 0;
+        real_ = 0;
+    }
+    size_t size() const { return n_; }
+    const uint8_t* data() const { return p_; }
+
+private:
+    const uint8_t* p_;
+    size_t n_;
+    size_t pos_ = 0;
+    uint64_t buf_ = 0;
+    int cnt_ = 0;    // bits in buf_
+    int real_ = 0;   // of which come from the input
+};
+
+// Canonical Huffman code: a 9-bit direct table for short codes plus the per-length walk for longer ones.
+class Huffman {
+public:
+    static constexpr int kFast = 9;
+    void build(const uint8_t* lengths, int n) {
+        std::memset(count_, 0, sizeof(count_));
+        for (int s = 0; s < n; ++s) count_[lengths[s]]++;
+        count_[0] = 0;
+        int left = 1;
+        for (int l = 1; l <= 15; ++l) {
+            left = left * 2 - count_[l];
+            if (left < 0) bad("over-subscribed Huffman code");
+        }
+        int offs[16];
+        offs[1] = 0;
+        for (int l = 1; l < 15; ++l) offs[l + 1] = offs[l] + count_[l];
+        sym_.assign((size_t)n, 0);
+        for (int s = 0; s < n; ++s)
+            if (lengths[s]) sym_[(size_t)offs[lengths[s]]++] = (uint16_t)s;
+        // direct table: canonical codes assigned in (length, symbol) order, stored bit-reversed
+        std::fill(std::begin(fast_), std::end(fast_), (uint16_t)0);
+        int code = 0, idx = 0;
+        for (int l = 1; l <= kFast; ++l) {
+            for (int k = 0; k < count_[l]; ++k, ++idx, ++code) {
+                int rev = 0;
+                for (int b = 0; b < l; ++b) rev |= ((code >> b) & 1) << (l - 1 - b);
+                for (int fill = rev; fill < (1 << kFast); fill += 1 << l)
+                    fast_[fill] = (uint16_t)((sym_[(size_t)idx] << 4) | l);
+            }
+            code <<= 1;
+        }
+    }
+    int decode(Bits& in) const {
+        const uint16_t e = fast_[in.peek(kFast)];
+        if (e) {
+            in.drop(e & 15);
+            return e >> 4;
+        }
+        int code = 0, first = 0, index = 0;
+        for (int l = 1; l <= 15; ++l) {
+            code |= (int)in.get(1);
+            const int c = count_[l];
+            if (code - first < c) return sym_[(size_t)(index + code - first)];
+            index += c;
+            first = (first + c) << 1;
+            code <<= 1;
+        }
+        bad("invalid Huffman code");
+    }
+
+private:
+    int count_[16];
+    std::vector<uint16_t> sym_;
+    uint16_t fast_[1 << kFast];
+};
+
+// RFC 1951 section 3.2.5 length and distance tables.
+constexpr uint16_t kLenBase[29] = {3, 4, 5, 6, 7, 8, 9, 10, 11, 13, 15, 17, 19, 23, 27, 31,
+                                   35, 43, 51, 59, 67, 83, 99, 115, 131, 163, 195, 227, 258};
+constexpr uint8_t kLenExtra[29] = {0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 2, 2, 2, 2, 3, 3, 3, 3, 4, 4, 4, 4, 5, 5, 5, 5, 0};
+constexpr uint16_t kDistBase[30] = {1, 2, 3, 4, 5, 7, 9, 13, 17, 25, 33, 49, 65, 97, 129, 193,
+                                    257, 385, 513, 769, 1025, 1537, 2049, 3073, 4097, 6145, 8193, 12289, 16385, 24577};
+constexpr uint8_t kDistExtra[30] = {0, 0, 0, 0, 1, 1, 2, 2, 3, 3, 4, 4, 5, 5, 6, 6, 7, 7, 8, 8, 9, 9, 10, 10, 11, 11, 12, 12, 13, 13};
+// Order of the code-length code lengths (section 3.2.7).
+constexpr uint8_t kClOrder[19] = {16, 17, 18, 0, 8, 7, 9, 6, 10, 5, 11, 4, 12, 3, 13, 2, 14, 1, 15};
+
+void inflate_block(Bits& in, const Huffman& lit, const Huffman& dist, std::vector<uint8_t>& out, size_t limit) {
+    for (;;) {
+        const int s = lit.decode(in);
+        if (s < 256) {
+            if (out.size() >= limit) bad("decompressed data larger than expected");
+            out.push_back((uint8_t)s);
+        } else if (s == 256) {
+            return;
+        } else {
+            if (s > 285) bad("invalid length symbol");
+            const size_t len = kLenBase[s - 257] + in.get(kLenExtra[s - 257]);
+            const int ds = dist.decode(in);
+            if (ds >= 30) bad("invalid distance symbol");
+            const size_t d = kDistBase[ds] + in.get(kDistExtra[ds]);
+            if (d > out.size()) bad("distance before the start of the output");
+            if (out.size() + len > limit) bad("decompressed data larger than expected");
+            const size_t from = out.size() - d;
+            for (size_t k = 0; k < len; ++k) out.push_back(out[from + k]);
+        }
+    }
+}
+
+}  // namespace
+
+std::vector<uint8_t> zlib_inflate(const uint8_t* data, size_t n, size_t limit) {
+    if (n < 2) bad("truncated zlib stream");
+    const uint8_t cmf = data[0], flg = data[1];
+    if ((cmf & 15) != 8 || (cmf >> 4) > 7) bad("zlib stream is not deflate");
+    if (((cmf << 8) | flg) % 31 != 0) bad("bad zlib header check");
+    if (flg & 32) bad("zlib preset dictionary not supported");
+    Bits in(data + 2, n - 2);
+    std::vector<uint8_t> out;
+    out.reserve(std::min<size_t>(limit, 1u << 26));
+    Huffman lit, dist;
+    bool fixed_built = false;
+    Huffman flit, fdist;
+    for (;;) {
+        const uint32_t final_block = in.get(1);
+        const uint32_t type = in.get(2);
+        if (type == 0) {
+            in.align();
+            const size_t p = in.byte_pos();
+            if (p + 4 > in.size()) bad("truncated stored block");
+            const uint8_t* d = in.data() + p;
+            const uint32_t len = d[0] | (d[1] << 8), nlen = d[2] | (d[3] << 8);
+            if ((len ^ 0xFFFFu) != nlen) bad("stored block length check failed");
+            if (p + 4 + len > in.size()) bad("truncated stored block");
+            if (out.size() + len > limit) bad("decompressed data larger than expected");
+            out.insert(out.end(), d + 4, d + 4 + len);
+            in.skip_to(p + 4 + len);
+        } else if (type == 1) {
+            if (!fixed_built) {
+                uint8_t l[288];
+                for (int s = 0; s < 288; ++s) l[s] = s < 144 ? 8 : s < 256 ? 9 : s < 280 ? 7 : 8;
+                flit.build(l, 288);
+                uint8_t d[30];
+                std::fill(d, d + 30, (uint8_t)5);
+                fdist.build(d, 30);
+                fixed_built = true;
+            }
+            inflate_block(in, flit, fdist, out, limit);
+        } else if (type == 2) {
+            const int hlit = (int)in.get(5) + 257, hdist = (int)in.get(5) + 1, hclen = (int)in.get(4) + 4;
+            uint8_t cl[19] = {0};
+            for (int k = 0; k < hclen; ++k) cl[kClOrder[k]] = (uint8_t)in.get(3);
+            Huffman clh;
+            clh.build(cl, 19);
+            uint8_t lens[288 + 32] = {0};
+            int k = 0;
+            while (k < hlit + hdist) {
+                const int s = clh.decode(in);
+                if (s < 16) {
+                    lens[k++] = (uint8_t)s;
+                } else {
+                    int rep = 0;
+                    uint8_t val = 0;
+                    if (s == 16) {
+                        if (k == 0) bad("repeat of a code length before the first");
+                        val = lens[k - 1];
+                        rep = 3 + (int)in.get(2);
+                    } else if (s == 17) {
+                        rep = 3 + (int)in.get(3);
+                    } else {
+                        rep = 11 + (int)in.get(7);
+                    }
+                    if (k + rep > hlit + hdist) bad("code lengths overflow");
+                    while (rep--) lens[k++] = val;
+                }
+            }
+            if (lens[256] == 0) bad("no end-of-block code");
+            lit.build(lens, hlit);
+            dist.build(lens + hlit, hdist);
+            inflate_block(in, lit, dist, out, limit);
+        } else {
+            bad("invalid deflate block type");
+        }
+        if (final_block) break;
+    }
+    // Adler-32 of the output (RFC 1950 section 2.2) follows the deflate data, byte aligned.
+    in.align();
+    const size_t p = in.byte_pos();
+    if (p + 4 <= in.size()) {
+        uint32_t a = 1, b = 0;
+        for (uint8_t c : out) {
+            a = (a + c) % 65521u;
+            b = (b + a) % 65521u;
+        }
+        const uint8_t* d = in.data() + p;
+        const uint32_t want = ((uint32_t)d[0] << 24) | ((uint32_t)d[1] << 16) | ((uint32_t)d[2] << 8) | d[3];
+        if (want != ((b << 16) | a)) bad("zlib Adler-32 check failed");
+    }
+    return out;
+}
+
+namespace {
+
+// ---- PNG -----------------------------------------------------------------------------------------
+
+uint32_t be32(const uint8_t* p) { return ((uint32_t)p[0] << 24) | ((uint32_t)p[1] << 16) | ((uint32_t)p[2] << 8) | p[3]; }
+
+uint8_t paeth(int a, int b, int c) {
+    const int p = a + b - c;
+    const int pa = std::abs(p - a), pb = std::abs(p - b), pc = std::abs(p - c);
+    if (pa <= pb && pa <= pc) return (uint8_t)a;
+    if (pb <= pc) return (uint8_t)b;
+    return (uint8_t)c;
+}
+
+// Reverses the row filters of one (sub)image in place; `rows` holds height * (1 + stride) bytes.
+void unfilter(uint8_t* rows, uint32_t height, size_t stride, size_t bpp, std::vector<uint8_t>& out) {
+    out.assign((size_t)height * stride, 0);
+    for (uint32_t y = 0; y < height; ++y) {
+        const uint8_t ft = rows[(size_t)y * (stride + 1)];
+        const uint8_t* src = rows + (size_t)y * (stride + 1) + 1;
+        uint8_t* cur = out.data() + (size_t)y * stride;
+        const uint8_t* prev = y ? cur - stride : nullptr;
+        for (size_t i = 0; i < stride; ++i) {
+            const int a = i >= bpp ? cur[i - bpp] : 0;
+            const int b = prev ? prev[i] : 0;
+            const int c = (prev && i >= bpp) ? prev[i - bpp] : 0;
+            int v = src[i];
+            switch (ft) {
+                case 0: break;
+                case 1: v += a; break;
+                case 2: v += b; break;
+                case 3: v += (a + b) >> 1; break;
+                case 4: v += paeth(a, b, c); break;
+                default: bad("invalid PNG filter type " + std::to_string(ft));
+            }
+            cur[i] = (uint8_t)v;
+        }
+    }
+}
+
+struct PngInfo {
+    uint32_t w = 0, h = 0;
+    int depth = 0, ctype = 0, interlace = 0;
+    int channels = 0;
+    uint8_t palette[256][4];
+    int pal_len = 0;
+    bool has_key = false;
+    uint16_t key[3] = {0, 0, 0};
+};
+
+// One sample (channel value at its bit depth) of row `row` at sample index `i`.
+inline uint32_t sample(const uint8_t* row, size_t i, int depth) {
+    if (depth == 8) return row[i];
+    if (depth == 16) return ((uint32_t)row[2 * i] << 8) | row[2 * i + 1];
+    const size_t bit = i * (size_t)depth;
+    const int shift = 8 - depth - (int)(bit & 7);
+    return (row[bit >> 3] >> shift) & ((1u << depth) - 1u);
+}
+
+inline uint8_t to8(uint32_t v, int depth) {
+    if (depth == 16) return (uint8_t)(v >> 8);
+    if (depth == 8) return (uint8_t)v;
+    return (uint8_t)(v * (255u / ((1u << depth) - 1u)));
+}
+
+// Converts one unfiltered (sub)image row of `n` pixels to RGBA8 at out[0], out[step], ...
+void convert_row(const PngInfo& pi, const uint8_t* row, uint32_t n, uint8_t* out, size_t step) {
+    for (uint32_t x = 0; x < n; ++x, out += step) {
+        const size_t s = (size_t)x * pi.channels;
+        switch (pi.ctype) {
+            case 0: {
+                const uint32_t g = sample(row, s, pi.depth);
+                out[0] = out[1] = out[2] = to8(g, pi.depth);
+                out[3] = (pi.has_key && g == pi.key[0]) ? 0 : 255;
+                break;
+            }
+            case 2: {
+                const uint32_t r = sample(row, s, pi.depth), g = sample(row, s + 1, pi.depth), b = sample(row, s + 2, pi.depth);
+                out[0] = to8(r, pi.depth);
+                out[1] = to8(g, pi.depth);
+                out[2] = to8(b, pi.depth);
+                out[3] = (pi.has_key && r == pi.key[0] && g == pi.key[1] && b == pi.key[2]) ? 0 : 255;
+                break;
+            }
+            case 3: {
+                const uint32_t k = sample(row, s, pi.depth);
+                if ((int)k < pi.pal_len) std::memcpy(out, pi.palette[k], 4);
+                else out[0] = out[1] = out[2] = 0, out[3] = 255;   // index past the palette: opaque black
+                break;
+            }
+            case 4: {
+                out[0] = out[1] = out[2] = to8(sample(row, s, pi.depth), pi.depth);
+                out[3] = to8(sample(row, s + 1, pi.depth), pi.depth);
+                break;
+            }
+            default: {
+                for (int c = 0; c < 4; ++c) out[c] = to8(sample(row, s + c, pi.depth), pi.depth);
+                break;
+            }
+        }
+    }
+}
+
+Image decode_png(const uint8_t* data, size_t n) {
+    PngInfo pi;
+    std::vector<uint8_t> idat;
+    size_t p = 8;
+    bool seen_ihdr = false, seen_iend = false;
+    while (p + 8 <= n && !seen_iend) {
+        const uint32_t len = be32(data + p);
+        const uint8_t* type = data + p + 4;
+        if (len > n - p - 8 || n - p - 8 - len < 4) bad("truncated PNG chunk");
+        const uint8_t* d = data + p + 8;
+        const std::string t(reinterpret_cast<const char*>(type), 4);
+        if (!seen_ihdr && t != "IHDR") bad("PNG does not start with IHDR");
+        if (t == "IHDR") {
+            if (len != 13) bad("bad IHDR length");
+            pi.w = be32(d);
+            pi.h = be32(d + 4);
+            pi.depth = d[8];
+            pi.ctype = d[9];
+            if (d[10] != 0 || d[11] != 0) bad("unknown PNG compression or filter method");
+            pi.interlace = d[12];
+            if (pi.interlace > 1) bad("unknown PNG interlace method");
+            if (pi.w == 0 || pi.h == 0) bad("PNG has zero size");
+            if (pi.w > (1u << 24) || pi.h > (1u << 24) || (uint64_t)pi.w * pi.h > (1ull << 28))
+                bad("PNG too large (more than 2^28 pixels)");
+            const int dp = pi.depth, ct = pi.ctype;
+            const bool ok = (ct == 0 && (dp == 1 || dp == 2 || dp == 4 || dp == 8 || dp == 16)) ||
+                            (ct == 3 && (dp == 1 || dp == 2 || dp == 4 || dp == 8)) ||
+                            ((ct == 2 || ct == 4 || ct == 6) && (dp == 8 || dp == 16));
+            if (!ok) bad("invalid PNG colour type / bit depth");
+            pi.channels = ct == 0 ? 1 : ct == 2 ? 3 : ct == 3 ? 1 : ct == 4 ? 2 : 4;
+            seen_ihdr = true;
+        } else if (t == "PLTE") {
+            if (len % 3 != 0 || len / 3 > 256) bad("bad PLTE chunk");
+            pi.pal_len = (int)(len / 3);
+            for (int k = 0; k < pi.pal_len; ++k) {
+                pi.palette[k][0] = d[3 * k];
+                pi.palette[k][1] = d[3 * k + 1];
+                pi.palette[k][2] = d[3 * k + 2];
+                pi.palette[k][3] = 255;
+            }
+        } else if (t == "tRNS") {
+            if (!idat.empty()) bad("tRNS after IDAT");
+            if (pi.ctype == 3) {
+                if (pi.pal_len == 0) bad("tRNS before PLTE");
+                if ((int)len > pi.pal_len) bad("tRNS longer than the palette");
+                for (uint32_t k = 0; k < len; ++k) pi.palette[k][3] = d[k];
+            } else if (pi.ctype == 0 || pi.ctype == 2) {
+                const uint32_t want = pi.ctype == 0 ? 2u : 6u;
+                if (len != want) bad("bad tRNS length");
+                for (uint32_t k = 0; k < want / 2; ++k) pi.key[k] = (uint16_t)((d[2 * k] << 8) | d[2 * k + 1]);
+                pi.has_key = true;
+            } else {
+                bad("tRNS on a PNG with an alpha channel");
+            }
+        } else if (t == "IDAT") {
+            idat.insert(idat.end(), d, d + len);
+        } else if (t == "IEND") {
+            seen_iend = true;
+        } else if (!(type[0] & 32)) {
+            bad("unknown critical PNG chunk " + t);
+        }
+        p += 12 + (size_t)len;
+    }
+    if (!seen_ihdr) bad("PNG has no IHDR");
+    if (pi.ctype == 3 && pi.pal_len == 0) bad("palette PNG without PLTE");
+    if (idat.empty()) bad("PNG has no image data");
+
+    const size_t bits_pp = (size_t)pi.channels * pi.depth;
+    const size_t bpp = std::max<size_t>(1, bits_pp / 8);
+    // passes (x0, y0, dx, dy): the whole image, or the seven Adam7 passes
+    static const int kAdam7[7][4] = {{0, 0, 8, 8}, {4, 0, 8, 8}, {0, 4, 4, 8}, {2, 0, 4, 4}, {0, 2, 2, 4}, {1, 0, 2, 2}, {0, 1, 1, 2}};
+    static const int kWhole[1][4] = {{0, 0, 1, 1}};
+    const int (*passes)[4] = pi.interlace ? kAdam7 : kWhole;
+    const int npass = pi.interlace ? 7 : 1;
+    size_t expect = 0;
+    for (int k = 0; k < npass; ++k) {
+        const uint64_t pw = (pi.w + (uint32_t)(passes[k][2] - 1 - passes[k][0])) / (uint32_t)passes[k][2];
+        const uint64_t ph = (pi.h + (uint32_t)(passes[k][3] - 1 - passes[k][1])) / (uint32_t)passes[k][3];
+        if (pw && ph) expect += (size_t)ph * (1 + (size_t)((pw * bits_pp + 7) / 8));
+    }
+    std::vector<uint8_t> raw = zlib_inflate(idat.data(), idat.size(), expect);
+    if (raw.size() < expect) bad("PNG image data too short");
+
+    Image img;
+    img.width = pi.w;
+    img.height = pi.h;
+    img.rgba.assign((size_t)pi.w * pi.h * 4, 0);
+    size_t off = 0;
+    std::vector<uint8_t> sub;
+    for (int k = 0; k < npass; ++k) {
+        const uint32_t x0 = (uint32_t)passes[k][0], y0 = (uint32_t)passes[k][1];
+        const uint32_t dx = (uint32_t)passes[k][2], dy = (uint32_t)passes[k][3];
+        const uint32_t pw = (pi.w + dx - 1 - x0) / dx, ph = (pi.h + dy - 1 - y0) / dy;
+        if (!pw || !ph) continue;
+        const size_t stride = ((size_t)pw * bits_pp + 7) / 8;
+        unfilter(raw.data() + off, ph, stride, bpp, sub);
+        off += (size_t)ph * (stride + 1);
+        for (uint32_t y = 0; y < ph; ++y)
+            convert_row(pi, sub.data() + (size_t)y * stride, pw,
+                        img.rgba.data() + (((size_t)(y0 + y * dy) * pi.w) + x0) * 4, (size_t)dx * 4);
+    }
+    return img;
+}
+
+}  // namespace
+
+Image decode_image(const uint8_t* data, size_t n) {
+    static const uint8_t kPngSig[8] = {137, 80, 78, 71, 13, 10, 26, 10};
+    if (n >= 8 && std::memcmp(data, kPngSig, 8) == 0) return decode_png(data, n);
+    if (n >= 2 && data[0] == 0xFF && data[1] == 0xD8) bad("JPEG images are not supported by this build (PNG only)");
+    bad("unknown image format (PNG expected)");
+}
+
+void flip_rows(Image& img) {
+    const size_t stride = (size_t)img.width * 4;
+    for (uint32_t y = 0; y < img.height / 2; ++y)
+        std::swap_ranges(img.rgba.begin() + (ptrdiff_t)(y * stride), img.rgba.begin() + (ptrdiff_t)((y + 1) * stride),
+                         img.rgba.begin() + (ptrdiff_t)((img.height - 1 - y) * stride));
+}
+
+Image load_image(const std::string& path, bool flip_vertically) {
+    std::ifstream f(path, std::ios::binary);
+    if (!f) fail(REINA_ERR_IO, "Could not load image at path: " + path);
+    std::vector<uint8_t> bytes((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+    Image img;
+    try {
+        img = decode_image(bytes.data(), bytes.size());
+    } catch (const Error& e) {
+        fail(e.code, "Could not load image at path: " + path + ": " + e.what());
+    }
+    if (flip_vertically) flip_rows(img);
+    return img;
+}
+
+}  // namespace rt

@@ -1,0 +1,32 @@
+// Texture image decoding for Scene::defineTexture (src/scene/Scene.cpp:15-25, src/graphics/Image.cpp:10-41):
+// an encoded image (PNG here; the reference links stb_image) becomes 8-bit RGBA texels, first row first.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace rt {
+
+struct Image {
+    uint32_t width = 0, height = 0;
+    std::vector<uint8_t> rgba;   // width * height * 4 bytes, rows top to bottom
+};
+
+// zlib stream (RFC 1950) holding deflate data (RFC 1951).  `limit` bounds the output size; a stream
+// that would produce more fails.  Throws Error(REINA_ERR_IO) on malformed input.
+std::vector<uint8_t> zlib_inflate(const uint8_t* data, size_t n, size_t limit);
+
+// Decodes an encoded image to RGBA8 the way stbi_load(..., 4) does: PNG of every colour type and bit
+// depth (1, 2, 4, 8, 16; 16-bit samples keep their high byte; grey levels below 8 bits are scaled to
+// 0..255; tRNS transparency; Adam7 interlacing).  Other formats fail with REINA_ERR_IO.
+Image decode_image(const uint8_t* data, size_t n);
+
+// Reads and decodes a file; `flip_vertically` reverses the row order (stbi_set_flip_vertically_on_load,
+// which the reference sets for textures loaded from a path, src/graphics/Image.cpp:14).
+Image load_image(const std::string& path, bool flip_vertically);
+
+void flip_rows(Image& img);
+
+}  // namespace rt

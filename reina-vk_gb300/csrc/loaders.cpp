@@ -4,6 +4,7 @@
 // src/scene/gltf/gltfloader.cpp:120-255, 380-430).
 #include "loaders.h"
 
+#include <cctype>
 #include <cmath>
 #include <cstring>
 #include <fstream>
@@ -13,6 +14,7 @@
 #include <unordered_map>
 
 #include "errors.h"
+#include "image.h"
 #include "json.h"
 
 namespace rt {
@@ -383,8 +385,77 @@ void node_local(const Json& n, float m[16]) {
     m[12] = tx; m[13] = ty; m[14] = tz; m[15] = 1.0f;
 }
 
-// gltfloader.cpp:380-412: the default material is Disney with albedo 1, ior 1.5, interpolated normals.
-reina_material gltf_material(const Gltf& g, int64_t mi, GltfLoadStats& st) {
+// Percent-decoding of a relative URI reference (RFC 3986 section 2.1).
+std::string uri_path(const std::string& uri) {
+    std::string out;
+    for (size_t i = 0; i < uri.size(); ++i) {
+        if (uri[i] == '%' && i + 2 < uri.size() && std::isxdigit((unsigned char)uri[i + 1]) &&
+            std::isxdigit((unsigned char)uri[i + 2])) {
+            out.push_back((char)std::stoi(uri.substr(i + 1, 2), nullptr, 16));
+            i += 2;
+        } else {
+            out.push_back(uri[i]);
+        }
+    }
+    return out;
+}
+
+// addTexturesToScene (gltfloader.cpp:283-340): every image of the asset becomes a scene texture, in image
+// order, decoded from its bytes without a vertical flip (the parser loads external image files into
+// memory, so every source reaches Scene::defineTexture(bytes)).  Returns the texture id per image; an
+// image that cannot be decoded (a format other than PNG) gets -1, and the material references to it are
+// counted as ignored.
+std::vector<int32_t> gltf_images(const Gltf& g, const std::string& base_dir, Scene& scene) {
+    const Json& imgs = g.doc["images"];
+    std::vector<int32_t> ids(imgs.size(), -1);
+    for (size_t i = 0; i < imgs.size(); ++i) {
+        const Json& im = imgs[i];
+        std::vector<uint8_t> bytes;
+        if (im.has("uri")) {
+            const std::string uri = im["uri"].string("");
+            if (uri.rfind("data:", 0) == 0) {
+                const size_t comma = uri.find(";base64,");
+                if (comma == std::string::npos) fail(REINA_ERR_IO, "glTF: only base64 data URIs are supported");
+                bytes = base64_decode(uri, comma + 8);
+            } else {
+                if (uri.find("://") != std::string::npos)
+                    fail(REINA_ERR_IO, "Non-local URIs are not supported for texture loading");
+                bytes = read_file(base_dir + "/" + uri_path(uri));
+            }
+        } else if (im.has("bufferView")) {
+            const Json& v = g.doc["bufferViews"][(size_t)im["bufferView"].integer(-1)];
+            const int64_t b = v["buffer"].integer(-1);
+            if (b < 0 || (size_t)b >= g.buffers.size()) fail(REINA_ERR_IO, "glTF: image buffer view references a missing buffer");
+            const std::vector<uint8_t>& buf = g.buffers[(size_t)b];
+            const size_t off = (size_t)v["byteOffset"].integer(0), len = (size_t)v["byteLength"].integer(0);
+            if (off > buf.size() || len > buf.size() - off) fail(REINA_ERR_IO, "glTF: image buffer view runs past its buffer");
+            bytes.assign(buf.begin() + (ptrdiff_t)off, buf.begin() + (ptrdiff_t)(off + len));
+        } else {
+            continue;
+        }
+        try {
+            ids[i] = (int32_t)scene.define_texture(decode_image(bytes.data(), bytes.size()));
+        } catch (const Error& e) {
+            if (e.code != REINA_ERR_IO) throw;
+        }
+    }
+    return ids;
+}
+
+// Scene texture id of a material's texture reference ({"index": texture}); -1 (counted) when unresolved.
+int32_t gltf_texture_ref(const Gltf& g, const Json& ref, const std::vector<int32_t>& image_ids, GltfLoadStats& st) {
+    const Json& t = g.doc["textures"][(size_t)ref["index"].integer(-1)];
+    const int64_t src = t["source"].integer(-1);
+    if (t.type != Json::Object || src < 0 || (size_t)src >= image_ids.size() || image_ids[(size_t)src] < 0) {
+        st.ignored_textures++;
+        return -1;
+    }
+    return image_ids[(size_t)src];
+}
+
+// gltfloader.cpp:380-430: the default material is Disney with albedo 1, ior 1.5, interpolated normals;
+// baseColorTexture -> texture_id, normalTexture -> normal_map_id.
+reina_material gltf_material(const Gltf& g, int64_t mi, const std::vector<int32_t>& image_ids, GltfLoadStats& st) {
     reina_material m;
     std::memset(&m, 0, sizeof(m));
     m.material_idx = 3;
@@ -410,9 +481,8 @@ reina_material gltf_material(const Gltf& g, int64_t mi, GltfLoadStats& st) {
         m.specular_transmission = (float)ext["KHR_materials_transmission"]["transmissionFactor"].number(0.0);
         m.cull_backface = 0;
     }
-    // textures are not supported yet: their ids stay -1
-    if (pbr.has("baseColorTexture")) st.ignored_textures++;
-    if (j.has("normalTexture")) st.ignored_textures++;
+    if (pbr.has("baseColorTexture")) m.texture_id = gltf_texture_ref(g, pbr["baseColorTexture"], image_ids, st);
+    if (j.has("normalTexture")) m.normal_map_id = gltf_texture_ref(g, j["normalTexture"], image_ids, st);
     return m;
 }
 
@@ -472,6 +542,7 @@ GltfLoadStats load_gltf_memory(const uint8_t* data, size_t size, const std::stri
     if (scene_idx >= scenes.size()) fail(REINA_ERR_IO, "glTF: default scene out of range");
 
     GltfLoadStats st;
+    const std::vector<int32_t> image_ids = gltf_images(g, base_dir, scene);
     std::unordered_map<int64_t, std::vector<std::pair<uint32_t, int64_t>>> mesh_objects;   // mesh -> (object, material)
     auto define_mesh = [&](int64_t mi) -> const std::vector<std::pair<uint32_t, int64_t>>& {
         auto it = mesh_objects.find(mi);
@@ -577,7 +648,7 @@ GltfLoadStats load_gltf_memory(const uint8_t* data, size_t size, const std::stri
         mat_mul(it.m, local, world);
         if (n.has("mesh")) {
             for (const auto& [obj, mat] : define_mesh(n["mesh"].integer(-1))) {
-                const reina_material m = gltf_material(g, mat, st);
+                const reina_material m = gltf_material(g, mat, image_ids, st);
                 scene.add_instance(obj, world, m);
                 st.instances++;
             }

@@ -161,10 +161,10 @@ __global__ void __launch_bounds__(kBlock, kShadeMinBlocks) k_shade(RenderLaunch 
             float acc = ps.acc[p];
             const bool inside = (flags & kFlagInside) != 0;
             Vertex vx;
-            if (MAT == 1) vx = shade_lambert(h, pr, rd, rng, inside, acc);
-            else if (MAT == 2) vx = shade_metal(h, pr, rd, rng, inside, acc);
-            else if (MAT == 3) vx = shade_dielectric(h, pr, ro, rd, rng, inside, acc);
-            else vx = shade_disney(h, pr, ro, rd, rng, inside, acc);
+            if (MAT == 1) vx = shade_lambert(L.s, h, pr, rd, rng, inside, acc);
+            else if (MAT == 2) vx = shade_metal(L.s, h, pr, rd, rng, inside, acc);
+            else if (MAT == 3) vx = shade_dielectric(L.s, h, pr, ro, rd, rng, inside, acc);
+            else vx = shade_disney(L.s, h, pr, ro, rd, rng, inside, acc);
             if (vx.skip) {
                 flags &= ~kFlagPrevNee;
             } else {
@@ -176,7 +176,7 @@ __global__ void __launch_bounds__(kBlock, kShadeMinBlocks) k_shade(RenderLaunch 
                         if ((flags & kFlagPrevNee) && (vx.emission.x != 0.0f || vx.emission.y != 0.0f || vx.emission.z != 0.0f))
                             contrib = contrib * power_heuristic(ps.ppdf[p], light_pdf_sa(L.s, L.pc.totalEmissiveWeight, prim, ro, vx.newO));
                         const bool do_nee = (MAT == 1 || MAT == 4) && L.s.emissive_count > 0;
-                        if (do_nee) emit = next_event(L.s, L.pc.totalEmissiveWeight, rng, MAT == 4, vx.newO, h.n, vx.albedo, pr, h.tbn, rd, thr, sh);
+                        if (do_nee) emit = next_event(L.s, L.pc.totalEmissiveWeight, rng, MAT == 4, vx.newO, vx.n, vx.albedo, pr, h.tbn, rd, thr, sh);
                         flags = do_nee ? (flags | kFlagPrevNee) : (flags & ~kFlagPrevNee);
                         ps.ppdf[p] = vx.pdf;
                     }
@@ -363,10 +363,10 @@ __global__ void __launch_bounds__(kBlock) k_megakernel(RenderLaunch L) {
                 const InstanceProperties& pr = L.s.props[hi.props];
                 const uint32_t mat = L.s.props_material[hi.props];
                 Vertex vx;
-                if (mat == 0) vx = shade_lambert(hi, pr, rd, rng, inside, acc);
-                else if (mat == 1) vx = shade_metal(hi, pr, rd, rng, inside, acc);
-                else if (mat == 2) vx = shade_dielectric(hi, pr, ro, rd, rng, inside, acc);
-                else vx = shade_disney(hi, pr, ro, rd, rng, inside, acc);
+                if (mat == 0) vx = shade_lambert(L.s, hi, pr, rd, rng, inside, acc);
+                else if (mat == 1) vx = shade_metal(L.s, hi, pr, rd, rng, inside, acc);
+                else if (mat == 2) vx = shade_dielectric(L.s, hi, pr, ro, rd, rng, inside, acc);
+                else vx = shade_disney(L.s, hi, pr, ro, rd, rng, inside, acc);
                 const V3 ray_org = ro, ray_in = rd;
                 ro = vx.newO;
                 rd = vx.newD;
@@ -383,7 +383,7 @@ __global__ void __launch_bounds__(kBlock) k_megakernel(RenderLaunch L) {
                         const bool do_nee = (mat == 0 || mat == 3) && L.s.emissive_count > 0;
                         if (do_nee) {
                             ShadowRec sh;
-                            if (next_event(L.s, L.pc.totalEmissiveWeight, rng, mat == 3, vx.newO, hi.n, vx.albedo, pr, hi.tbn, ray_in, thr, sh)) {
+                            if (next_event(L.s, L.pc.totalEmissiveWeight, rng, mat == 3, vx.newO, vx.n, vx.albedo, pr, hi.tbn, ray_in, thr, sh)) {
                                 const TraceRay sr = make_trace_ray(sh.o.x, sh.o.y, sh.o.z, sh.d.x, sh.d.y, sh.d.z, 0.0f, sh.tmax);
                                 Hit sh_hit;
                                 uint32_t e2 = 0;

@@ -48,7 +48,9 @@ uint32_t Scene::define_object(ModelData&& model) {
     r.first_normal = (uint32_t)tbns_offset;
     r.index_offset = (uint32_t)index_offset;
     r.tbns_index_offset = (uint32_t)tbns_indices_offset;
-    r.tex_index_offset = model.tex_coords.empty() ? 0xFFFFFFFFu : (uint32_t)tex_index_offset;
+    // A model without texture coordinates (or without the per-corner indices into them) reconstructs UV
+    // (0, 0) at every hit (closestHitCommon.h.glsl:96-98).
+    r.tex_index_offset = (model.tex_coords.empty() || model.tex_indices.empty()) ? 0xFFFFFFFFu : (uint32_t)tex_index_offset;
     r.index_count = (uint32_t)(model.indices.size() / 3);
     r.tbns_index_count = (uint32_t)(model.indices.size() / 3);
     r.tex_index_count = (uint32_t)(model.tex_indices.size() / 3);
@@ -101,10 +103,26 @@ InstanceProperties Scene::make_props(uint32_t object, const reina_material& m) c
     return p;
 }
 
+// Texture ids are checked against the scene's textures at build(), since textures may be defined after
+// the instances that use them (as with Scene::defineTexture).
 static void check_material(const reina_material& m) {
     if (m.material_idx > 3) fail(REINA_ERR_INVALID, "material_idx must be 0 (Lambertian), 1 (metal), 2 (dielectric) or 3 (Disney)");
-    if (m.texture_id >= 0 || m.normal_map_id >= 0 || m.bump_map_id >= 0)
-        fail(REINA_ERR_INVALID, "textures are not supported by this build of the trace path (texture ids must be -1)");
+}
+
+uint32_t Scene::define_texture(Image&& image) {
+    if (built_) fail(REINA_ERR_STATE, "cannot define a texture in a built scene");
+    if (image.width == 0 || image.height == 0) fail(REINA_ERR_INVALID, "texture has zero size");
+    if (image.rgba.size() != (size_t)image.width * image.height * 4) fail(REINA_ERR_INVALID, "texture data size mismatch");
+    size_t total = 0;
+    for (const Image& t : textures_) total += (size_t)t.width * t.height;
+    if (total + (size_t)image.width * image.height > 0xFFFFFFFFull) fail(REINA_ERR_INVALID, "textures exceed 2^32 texels in total");
+    textures_.push_back(std::move(image));
+    return (uint32_t)(textures_.size() - 1);
+}
+
+const Image& Scene::texture(uint32_t id) const {
+    if (id >= textures_.size()) fail(REINA_ERR_INVALID, "texture id out of range");
+    return textures_[id];
 }
 
 void Scene::add_instance(uint32_t object, const float transform[16], const reina_material& mat) {
@@ -280,6 +298,25 @@ void Scene::build(bool require_emissive) {
     const bool host_only = device_ < 0;
     if (!host_only) check_cuda(cudaSetDevice(device_), "cudaSetDevice");
 
+    const int64_t ntex = (int64_t)textures_.size();
+    for (const InstanceProperties& p : props_)
+        for (int32_t id : {p.textureID, p.normalMapTexID, p.bumpMapTexID})
+            if (id >= ntex) fail(REINA_ERR_INVALID, "material texture id " + std::to_string(id) + " out of range (" +
+                                                        std::to_string(ntex) + " textures defined)");
+    // All textures in one texel array (first texel, width, height per texture).
+    tex_texels_.clear();
+    tex_info_.clear();
+    for (const Image& t : textures_) {
+        tex_info_.insert(tex_info_.end(), {(uint32_t)tex_texels_.size(), t.width, t.height, 0u});
+        const size_t n = (size_t)t.width * t.height;
+        const size_t base = tex_texels_.size();
+        tex_texels_.resize(base + n);
+        for (size_t i = 0; i < n; ++i) {
+            const uint8_t* c = &t.rgba[4 * i];
+            tex_texels_[base + i] = (uint32_t)c[0] | ((uint32_t)c[1] << 8) | ((uint32_t)c[2] << 16) | ((uint32_t)c[3] << 24);
+        }
+    }
+
     // Emissive CDFs and packing (src/scene/Scene.cpp:102-114 -> Instances).
     for (InstanceRecord& inst : instances_) {
         if (inst.per_face) inst.light = EmissiveInfo{};
@@ -365,13 +402,14 @@ size_t Scene::upload_bytes() const {
            (all_indices_offset_.size() + all_tbns_indices_offset_.size() + all_tex_indices_offset_.size() +
             prim_instance_.size() + prim_props_.size() + props_material_.size()) * sizeof(uint32_t) +
            props_.size() * sizeof(InstanceProperties) + inst_gpu_.size() * sizeof(InstanceGpu) +
-           emissive_data_.size() * sizeof(EmissiveInstanceData) + has_tbn_.size();
+           emissive_data_.size() * sizeof(EmissiveInstanceData) + has_tbn_.size() +
+           (tex_texels_.size() + tex_info_.size()) * sizeof(uint32_t);
 }
 
 void Scene::release_device() {
     for (DeviceBuffer* b : {&d_nodes_, &d_tris_, &d_vertices_, &d_indices_, &d_tbns_, &d_tbn_indices_, &d_tex_coords_,
                             &d_tex_indices_, &d_props_, &d_instances_, &d_prim_instance_, &d_prim_props_, &d_emissive_,
-                            &d_cdf_tris_, &d_cdf_inst_, &d_props_material_, &d_has_tbn_})
+                            &d_cdf_tris_, &d_cdf_inst_, &d_props_material_, &d_has_tbn_, &d_tex_texels_, &d_tex_info_})
         b->release();
     const uint32_t nodes = dev_.node_count, tris = dev_.tri_count;
     dev_ = DeviceScene{};
@@ -407,6 +445,8 @@ void Scene::upload() {
     up(d_cdf_inst_, cdf_instances_.data(), cdf_instances_.size() * sizeof(float));
     up(d_props_material_, props_material_.data(), props_material_.size() * sizeof(uint32_t));
     up(d_has_tbn_, has_tbn_.data(), has_tbn_.size());
+    up(d_tex_texels_, tex_texels_.data(), tex_texels_.size() * sizeof(uint32_t));
+    up(d_tex_info_, tex_info_.data(), tex_info_.size() * sizeof(uint32_t));
 
     dev_ = DeviceScene{};
     dev_.nodes = d_nodes_.as<Bvh8Node>();
@@ -432,6 +472,9 @@ void Scene::upload() {
     dev_.cdf_instances = d_cdf_inst_.as<float>();
     dev_.emissive_count = (uint32_t)emissive_data_.size();
     dev_.emissive_weight = emissive_total_;
+    dev_.tex_texels = d_tex_texels_.as<uint32_t>();
+    dev_.tex_info = d_tex_info_.as<uint4>();
+    dev_.tex_count = (uint32_t)textures_.size();
     for (int k = 0; k < 3; ++k) {
         dev_.bounds_lo[k] = bounds_lo_[k];
         dev_.bounds_hi[k] = bounds_hi_[k];
@@ -443,7 +486,8 @@ size_t Scene::device_bytes() const {
     return d_nodes_.bytes() + d_tris_.bytes() + d_vertices_.bytes() + d_indices_.bytes() + d_tbns_.bytes() +
            d_tbn_indices_.bytes() + d_tex_coords_.bytes() + d_tex_indices_.bytes() + d_props_.bytes() +
            d_instances_.bytes() + d_prim_instance_.bytes() + d_prim_props_.bytes() + d_emissive_.bytes() +
-           d_cdf_tris_.bytes() + d_cdf_inst_.bytes() + d_props_material_.bytes() + d_has_tbn_.bytes();
+           d_cdf_tris_.bytes() + d_cdf_inst_.bytes() + d_props_material_.bytes() + d_has_tbn_.bytes() +
+           d_tex_texels_.bytes() + d_tex_info_.bytes();
 }
 
 const ModelData& Scene::model(uint32_t object) const {

@@ -9,6 +9,7 @@
 #include "bvh_build.h"
 #include "device_scene.h"
 #include "errors.h"
+#include "image.h"
 
 namespace rt {
 
@@ -52,6 +53,11 @@ public:
     explicit Scene(int device) : device_(device) {}
 
     uint32_t define_object(ModelData&& model);
+    // Scene::defineTexture (src/scene/Scene.cpp:15-25): RGBA8 texels, first row at v = 0.  Returns the id
+    // materials refer to (texture_id, normal_map_id, bump_map_id).
+    uint32_t define_texture(Image&& image);
+    size_t texture_count() const { return textures_.size(); }
+    const Image& texture(uint32_t id) const;
     void add_instance(uint32_t object, const float transform[16], const reina_material& mat);
     void add_instance_per_face(uint32_t object, const float transform[16], const reina_material* mats,
                                uint32_t mat_count, const uint32_t* face_material);
@@ -110,10 +116,14 @@ private:
     Bvh8 bvh_;
     std::vector<InstanceGpu> inst_gpu_;
     std::vector<uint8_t> has_tbn_;
+    // Textures: all texels in one array (one RGBA8 word each) and per texture its first texel and size
+    std::vector<Image> textures_;
+    std::vector<uint32_t> tex_texels_;
+    std::vector<uint32_t> tex_info_;   // 4 per texture: first texel, width, height, 0
     // Device buffers
     DeviceBuffer d_nodes_, d_tris_, d_vertices_, d_indices_, d_tbns_, d_tbn_indices_, d_tex_coords_,
         d_tex_indices_, d_props_, d_instances_, d_prim_instance_, d_prim_props_, d_emissive_, d_cdf_tris_,
-        d_cdf_inst_, d_props_material_, d_has_tbn_;
+        d_cdf_inst_, d_props_material_, d_has_tbn_, d_tex_texels_, d_tex_info_;
     DeviceScene dev_;
 };
 

@@ -116,12 +116,13 @@ struct HitInfo {
     M3 tbn;
     uint32_t props;
     uint32_t inst;
+    uint32_t lp;      // triangle index within its model
+    float bu, bv;     // barycentric weights of vertices 1 and 2
 };
 
-// getObjectHitInfo (closestHitCommon.h.glsl:52-148).  UVs are not reconstructed: without textures they
-// only feed the out-of-[0,1] skip, which mod(uv, 1) makes unreachable.  Models without TBN data use the
-// tangent frame (1,0,0), (0,1,0) and the geometric normal at every vertex (the reference reads its TBN
-// buffer unconditionally).
+// getObjectHitInfo (closestHitCommon.h.glsl:52-148).  The UV is reconstructed on demand by surface_uv()
+// (only textured materials read it).  Models without TBN data use the tangent frame (1,0,0), (0,1,0) and
+// the geometric normal at every vertex (the reference reads its TBN buffer unconditionally).
 __device__ __forceinline__ HitInfo hit_info(const DeviceScene& s, uint32_t prim, float bu, float bv, V3 rayDir) {
     HitInfo h;
     const uint32_t ii = s.prim_instance[prim];
@@ -130,6 +131,9 @@ __device__ __forceinline__ HitInfo hit_info(const DeviceScene& s, uint32_t prim,
     h.props = s.prim_props[prim];
     const InstanceProperties& pr = s.props[h.props];
     const uint32_t lp = prim - inst.first_prim;
+    h.lp = lp;
+    h.bu = bu;
+    h.bv = bv;
     const uint32_t i0 = s.indices[3 * lp + pr.indicesOffset + 0];
     const uint32_t i1 = s.indices[3 * lp + pr.indicesOffset + 1];
     const uint32_t i2 = s.indices[3 * lp + pr.indicesOffset + 2];
@@ -181,6 +185,123 @@ __device__ __forceinline__ HitInfo hit_info(const DeviceScene& s, uint32_t prim,
     wN = wN * (h.front ? 1.0f : -1.0f);
     h.tbn = M3{wT, wB, wN};
     return h;
+}
+
+// ---- textures ---------------------------------------------------------------------------------------
+
+// Hit UV (closestHitCommon.h.glsl:96-111): barycentric blend of the corner texture coordinates, (0, 0)
+// for a model without texture coordinates; a corner whose texture index is 0xFFFFFFFF contributes (0, 0).
+__device__ __forceinline__ float2 surface_uv(const DeviceScene& s, const InstanceProperties& pr, const HitInfo& h) {
+    if (pr.texIndicesOffset == 0xFFFFFFFFu) return make_float2(0.0f, 0.0f);
+    auto tc = [&](uint32_t k) {
+        const uint32_t t = s.tex_indices[3 * h.lp + pr.texIndicesOffset + k];
+        return t == 0xFFFFFFFFu ? make_float2(0.0f, 0.0f) : make_float2(s.tex_coords[2ull * t], s.tex_coords[2ull * t + 1]);
+    };
+    const float2 t0 = tc(0), t1 = tc(1), t2 = tc(2);
+    const float b0 = 1.0f - h.bu - h.bv;
+    return make_float2(t0.x * b0 + t1.x * h.bu + t2.x * h.bv, t0.y * b0 + t1.y * h.bu + t2.y * h.bv);
+}
+
+// One axis of bilinear addressing with REPEAT wrapping (the sampler of src/tools/vktools.cpp:765-780;
+// Vulkan texel filtering: coordinate c * size - 0.5, texels floor() and floor() + 1 modulo the size,
+// weight frac()).  Non-finite coordinates address texel 0 with weight 0.  Explicitly rounded FP32 so the
+// host restatement matches bit for bit.
+__device__ __forceinline__ void tex_axis(float c, uint32_t size, uint32_t& i0, uint32_t& i1, float& w) {
+    const float fs = (float)size;
+    float x = __fsub_rn(__fmul_rn(c, fs), 0.5f);
+    if (!(fabsf(x) <= 3.0e38f)) x = 0.0f;
+    const float fx = floorf(x);
+    w = __fsub_rn(x, fx);
+    float r = fmodf(fx, fs);
+    if (r < 0.0f) r = __fadd_rn(r, fs);
+    i0 = (uint32_t)r;
+    i1 = i0 + 1u == size ? 0u : i0 + 1u;
+}
+
+// texture(sampler2D, uv) at level 0 on R8G8B8A8_UNORM texels (src/graphics/Image.cpp:56): the four texels'
+// 8-bit values are blended with the bilinear weights, then scaled by 1/255 (one division per channel).
+template <int CH>
+__device__ __forceinline__ float4 tex_sample(const DeviceScene& s, int id, float u, float v) {
+    const uint4 ti = s.tex_info[id];
+    uint32_t x0, x1, y0, y1;
+    float a, b;
+    tex_axis(u, ti.y, x0, x1, a);
+    tex_axis(v, ti.z, y0, y1, b);
+    const uint32_t* t = s.tex_texels + ti.x;
+    const uint32_t c00 = __ldg(t + (size_t)y0 * ti.y + x0), c10 = __ldg(t + (size_t)y0 * ti.y + x1);
+    const uint32_t c01 = __ldg(t + (size_t)y1 * ti.y + x0), c11 = __ldg(t + (size_t)y1 * ti.y + x1);
+    const float na = __fsub_rn(1.0f, a), nb = __fsub_rn(1.0f, b);
+    const float w00 = __fmul_rn(na, nb), w10 = __fmul_rn(a, nb), w01 = __fmul_rn(na, b), w11 = __fmul_rn(a, b);
+    float out[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+    for (int k = 0; k < CH; ++k) {
+        const int sh = 8 * k;
+        float acc = __fmul_rn(w00, (float)((c00 >> sh) & 255u));
+        acc = __fadd_rn(acc, __fmul_rn(w10, (float)((c10 >> sh) & 255u)));
+        acc = __fadd_rn(acc, __fmul_rn(w01, (float)((c01 >> sh) & 255u)));
+        acc = __fadd_rn(acc, __fmul_rn(w11, (float)((c11 >> sh) & 255u)));
+        out[k] = __fdiv_rn(acc, 255.0f);
+    }
+    return make_float4(out[0], out[1], out[2], out[3]);
+}
+
+// bumpMapping (texutils.h.glsl:4-45): layered parallax search of the height map's red channel along the
+// tangent-space view direction.  The layer loop ends by itself within 0.2 * 512 + 1 steps for finite
+// input; the bound only guards NaN input.
+__device__ __forceinline__ float2 bump_mapping(const DeviceScene& s, int id, float2 uv, V3 rayIn, const M3& T) {
+    constexpr float kHeightScale = 0.2f, kMinLayers = 64.0f, kMaxLayers = 512.0f;
+    const V3 V = norm3(mulT(T, -rayIn));
+    if (V.z <= 0.0f) return uv;
+    const float numLayers = mixf(kMaxLayers, kMinLayers, fminf(fmaxf(V.z, 0.0f), 1.0f));
+    const float layerDepth = 1.0f / numLayers;
+    const float px = V.x / V.z * kHeightScale, py = V.y / V.z * kHeightScale;
+    const float dx = px / numLayers, dy = py / numLayers;
+    float cu = uv.x, cv = uv.y;
+    float depthSum = 0.0f;
+    float h = tex_sample<1>(s, id, cu, cv).x * kHeightScale;
+    for (int it = 0; depthSum < h && it < 1024; ++it) {
+        cu -= dx;
+        cv -= dy;
+        depthSum += layerDepth;
+        h = tex_sample<1>(s, id, cu, cv).x * kHeightScale;
+    }
+    const float pu = cu + dx, pv = cv + dy;
+    const float hPrev = tex_sample<1>(s, id, pu, pv).x * kHeightScale;
+    const float sumPrev = depthSum - layerDepth;
+    const float after = h - depthSum;
+    const float before = hPrev - sumPrev;
+    const float weight = after / (after - before);
+    return make_float2(mixf(pu, cu, weight), mixf(pv, cv, weight));
+}
+
+// The texture stage of the closest-hit shaders (lambertian.rchit.glsl:20-58, metal.rchit.glsl:18-50,
+// dielectric.rchit.glsl:54-73, disney.rchit.glsl:19-72): UV wrapped by mod(uv, 1), bump mapping, the
+// out-of-[0,1] skip (UVCHECK: Lambertian, Disney), the normal map (tangent normal rgb * 2 - 1 with y
+// negated, through the hit's TBN) and the albedo texture with its alpha test (ALPHA: a < 0.999 and a
+// uniform draw above a skips the hit; dielectrics only tint).  Returns false when the hit is skipped;
+// `n` and `albedo` receive the shading normal and the albedo.
+template <bool UVCHECK, bool ALPHA>
+__device__ __forceinline__ bool apply_textures(const DeviceScene& s, const HitInfo& h, const InstanceProperties& pr, V3 rd,
+                                               uint32_t& rng, V3& n, V3& albedo) {
+    n = h.n;
+    albedo = ld3(pr.albedo);
+    if ((pr.textureID & pr.normalMapTexID & pr.bumpMapTexID) < 0) return true;   // all three unset
+    float2 uv = surface_uv(s, pr, h);
+    uv.x = uv.x - floorf(uv.x);
+    uv.y = uv.y - floorf(uv.y);
+    if (pr.bumpMapTexID >= 0) uv = bump_mapping(s, pr.bumpMapTexID, uv, norm3(rd), h.tbn);
+    if (UVCHECK && (uv.x < 0.0f || uv.x > 1.0f || uv.y < 0.0f || uv.y > 1.0f)) return false;
+    if (pr.normalMapTexID >= 0) {
+        const float4 t = tex_sample<3>(s, pr.normalMapTexID, uv.x, uv.y);
+        const V3 tn{t.x * 2.0f - 1.0f, -(t.y * 2.0f - 1.0f), t.z * 2.0f - 1.0f};
+        n = norm3(mul(h.tbn, tn));
+    }
+    if (pr.textureID >= 0) {
+        const float4 t = tex_sample<4>(s, pr.textureID, uv.x, uv.y);
+        if (ALPHA && t.w < 0.999f && rng_next(rng) > t.w) return false;
+        albedo = albedo * V3{t.x, t.y, t.z};
+    }
+    return true;
 }
 
 // ---- brdfDisney.h.glsl ------------------------------------------------------------------------------

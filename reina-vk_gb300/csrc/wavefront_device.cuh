@@ -172,14 +172,15 @@ __device__ __forceinline__ bool next_event(const DeviceScene& s, float total_w, 
 }
 
 // ------------------------------------------------------------------------------------------------
-// Closest-hit shaders.  Each returns the payload fields the raygen loop reads next.
+// Closest-hit shaders.  Each returns the payload fields the raygen loop reads next; `n` is the shading
+// normal (the payload's surfaceNormal, which NEE uses).
 struct Vertex {
-    V3 color, albedo, emission, newO, newD;
+    V3 color, albedo, emission, newO, newD, n;
     float pdf;
     bool inside, skip;
 };
 
-// closestHitCommon.h.glsl:185-193
+// closestHitCommon.h.glsl:185-193 (offset along the unperturbed normal)
 __device__ __forceinline__ void skip_vertex(const HitInfo& h, V3 rd, Vertex& v) {
     v.newO = offset_along_normal(h.pos, -h.n);
     v.newD = rd;
@@ -187,44 +188,51 @@ __device__ __forceinline__ void skip_vertex(const HitInfo& h, V3 rd, Vertex& v) 
 }
 
 // lambertian.rchit.glsl:11-78
-__device__ __forceinline__ Vertex shade_lambert(const HitInfo& h, const InstanceProperties& pr, V3 rd, uint32_t& rng,
-                                                bool inside, float& acc) {
+__device__ __forceinline__ Vertex shade_lambert(const DeviceScene& s, const HitInfo& h, const InstanceProperties& pr,
+                                                V3 rd, uint32_t& rng, bool inside, float& acc) {
     Vertex v;
     v.skip = false;
     v.inside = inside;
     if (pr.cullBackface != 0u && !h.front) { skip_vertex(h, rd, v); return v; }
-    v.color = ld3(pr.albedo);
+    V3 n, albedo;
+    if (!apply_textures<true, true>(s, h, pr, rd, rng, n, albedo)) { skip_vertex(h, rd, v); return v; }
+    v.color = albedo;
     v.albedo = v.color;
     v.emission = ld3(pr.emission);
     v.newO = offset_along_normal(h.pos, h.ng);
-    v.newD = diffuse_reflection(h.n, rng);
+    v.newD = diffuse_reflection(n, rng);
     v.inside = false;
-    v.pdf = pdf_lambertian(h.n, v.newD);
+    v.n = n;
+    v.pdf = pdf_lambertian(n, v.newD);
     acc = 0.0f;
     return v;
 }
 
 // metal.rchit.glsl:7-70
-__device__ __forceinline__ Vertex shade_metal(const HitInfo& h, const InstanceProperties& pr, V3 rd, uint32_t& rng,
-                                              bool inside, float& acc) {
+__device__ __forceinline__ Vertex shade_metal(const DeviceScene& s, const HitInfo& h, const InstanceProperties& pr,
+                                              V3 rd, uint32_t& rng, bool inside, float& acc) {
     Vertex v;
     v.skip = false;
     v.inside = inside;
     if (pr.cullBackface != 0u && !h.front) { skip_vertex(h, rd, v); return v; }
-    v.color = ld3(pr.albedo);
+    V3 n, albedo;
+    if (!apply_textures<false, true>(s, h, pr, rd, rng, n, albedo)) { skip_vertex(h, rd, v); return v; }
+    v.color = albedo;
     v.albedo = v.color;
     v.emission = ld3(pr.emission);
     v.newO = offset_along_normal(h.pos, h.ng);
-    v.newD = fuzzy_reflection(rd, h.n, pr.roughness, rng);
+    v.newD = fuzzy_reflection(rd, n, pr.roughness, rng);
     v.inside = false;
+    v.n = n;
     v.pdf = 0.0f;
     acc = 0.0f;
     return v;
 }
 
-// dielectric.rchit.glsl:40-113
-__device__ __forceinline__ Vertex shade_dielectric(const HitInfo& h, const InstanceProperties& pr, V3 ro, V3 rd,
-                                                   uint32_t& rng, bool inside, float& acc) {
+// dielectric.rchit.glsl:40-113 (the Fresnel term uses the unperturbed normal; the normal map bends the
+// reflected and refracted directions; the albedo texture tints without an alpha test)
+__device__ __forceinline__ Vertex shade_dielectric(const DeviceScene& s, const HitInfo& h, const InstanceProperties& pr,
+                                                   V3 ro, V3 rd, uint32_t& rng, bool inside, float& acc) {
     Vertex v;
     v.skip = false;
     const float ri = h.front ? 1.0f / pr.ior : pr.ior;
@@ -234,15 +242,16 @@ __device__ __forceinline__ Vertex shade_dielectric(const HitInfo& h, const Insta
     const bool cannot = ri * sinT > 1.0f;
     const float refl = reflectance(cosT, ri);
     const bool prevInside = inside;
-    const V3 albedo = ld3(pr.albedo);
+    V3 n, albedo;
+    apply_textures<false, false>(s, h, pr, rd, rng, n, albedo);
     v.inside = inside;
     if (cannot || refl > rng_next(rng)) {
-        v.newD = fuzzy_reflection(unitDir, h.n, pr.roughness, rng);
+        v.newD = fuzzy_reflection(unitDir, n, pr.roughness, rng);
         v.color = V3{1.0f, 1.0f, 1.0f};
         v.newO = offset_along_normal(h.pos, h.ng);
     } else {
         v.inside = h.front;
-        v.newD = refract3(unitDir, h.n, ri) + random_unit_vec(rng) * pr.roughness;
+        v.newD = refract3(unitDir, n, ri) + random_unit_vec(rng) * pr.roughness;
         v.color = albedo;
         v.newO = offset_for_dielectric(h.pos, h.ng, unitDir);
     }
@@ -254,33 +263,36 @@ __device__ __forceinline__ Vertex shade_dielectric(const HitInfo& h, const Insta
     }
     v.albedo = v.color;
     v.emission = ld3(pr.emission);
+    v.n = n;
     v.pdf = 0.0f;
     return v;
 }
 
 // disney.rchit.glsl:36-198
-__device__ __forceinline__ Vertex shade_disney(const HitInfo& h, const InstanceProperties& pr, V3 ro, V3 rd,
-                                               uint32_t& rng, bool inside, float& acc) {
+__device__ __forceinline__ Vertex shade_disney(const DeviceScene& s, const HitInfo& h, const InstanceProperties& pr,
+                                               V3 ro, V3 rd, uint32_t& rng, bool inside, float& acc) {
     Vertex v;
     v.skip = false;
     v.inside = inside;
     if (pr.cullBackface != 0u && !h.front) { skip_vertex(h, rd, v); return v; }
-    const V3 albedo = ld3(pr.albedo);
+    V3 n, albedo;
+    if (!apply_textures<true, true>(s, h, pr, rd, rng, n, albedo)) { skip_vertex(h, rd, v); return v; }
     const float eta = h.front ? 1.0f / pr.ior : pr.ior;
     const DisneyParams dp = disney_params(pr, albedo);
     bool didRefract = false, choseGlass = false;
     const V3 wi = -rd;
-    const V3 dir = sample_disney(h.tbn, dp, eta, h.n, wi, didRefract, choseGlass, rng);
+    const V3 dir = sample_disney(h.tbn, dp, eta, n, wi, didRefract, choseGlass, rng);
     const V3 hv = norm3(dir + wi);
     float pdf;
-    const V3 f = eval_disney(h.tbn, dp, eta, didRefract, h.n, wi, dir, hv, pdf);
-    const float cosI = fmaxf(dot3(h.n, dir), 0.0f);
+    const V3 f = eval_disney(h.tbn, dp, eta, didRefract, n, wi, dir, hv, pdf);
+    const float cosI = fmaxf(dot3(n, dir), 0.0f);
     v.color = div3(f * cosI, pdf);
     v.albedo = albedo;
     v.pdf = pdf;
     v.emission = ld3(pr.emission);
     v.newO = offset_for_dielectric(h.pos, h.ng, dir);
     v.newD = dir;
+    v.n = n;
     v.inside = choseGlass;
     if (v.inside) acc += len3(h.pos - ro);
     else acc = 0.0f;

@@ -96,6 +96,16 @@ DEFAULT_WAVE_PATHS = 2097152
 BATCH_NO_GRAPHS = 1
 
 
+# InstanceProperties (polyglot.h), 120 bytes.
+INSTANCE_PROPERTIES_DTYPE = np.dtype([
+    ("indicesOffset", "<u4"), ("albedo", "<f4", 3), ("emission", "<f4", 3), ("tbnsIndicesOffset", "<u4"),
+    ("texIndicesOffset", "<u4"), ("roughness", "<f4"), ("ior", "<f4"), ("interpNormals", "<u4"),
+    ("absorption", "<f4"), ("textureID", "<i4"), ("normalMapTexID", "<i4"), ("bumpMapTexID", "<i4"),
+    ("cullBackface", "<u4"), ("anisotropic", "<f4"), ("subsurface", "<f4"), ("clearcoatGloss", "<f4"),
+    ("sheenTint", "<f4", 3), ("specularTint", "<f4", 3), ("metallic", "<f4"), ("clearcoat", "<f4"),
+    ("specularTransmission", "<f4"), ("sheen", "<f4")])
+
+
 class RtPushConsts(C.Structure):
     """polyglot/raytrace.h:43-54 (160 bytes; matrices column-major)."""
     _fields_ = [("invView", C.c_float * 16), ("invProjection", C.c_float * 16), ("sampleBatch", C.c_uint32),
@@ -312,6 +322,13 @@ def load_library() -> C.CDLL:
         "reina_save_schedule_destroy": (None, [P]),
         "reina_save_schedule_next": (I32, [P, U64, C.c_double, C.c_char_p, C.c_size_t]),
         "reina_write_png": (I32, [C.c_char_p, P, U32, U32]),
+        "reina_scene_define_texture_rgba8": (I32, [P, P, U32, U32, C.POINTER(U32)]),
+        "reina_scene_define_texture_file": (I32, [P, C.c_char_p, C.POINTER(U32)]),
+        "reina_scene_define_texture_encoded": (I32, [P, P, U64, C.POINTER(U32)]),
+        "reina_scene_texture_count": (I32, [P, C.POINTER(U32)]),
+        "reina_scene_export_properties": (I32, [P, P, U32, C.POINTER(U32)]),
+        "reina_scene_export_texture": (I32, [P, U32, C.POINTER(U32), C.POINTER(U32), P, U64]),
+        "reina_decode_image": (I32, [P, U64, C.POINTER(U32), C.POINTER(U32), P, U64]),
         "reina_autotune_raycast": (I32, [P, P, P, U64, P, U32, P, C.POINTER(_TuneResult)]),
         "reina_autotune_render": (I32, [P, P, C.POINTER(RtPushConsts), C.POINTER(RenderOptions), C.POINTER(_TuneResult)]),
         "reina_autotune_batch": (I32, [P, C.POINTER(_RenderJob), U32, C.POINTER(_TuneResult)]),
@@ -514,6 +531,49 @@ class Scene:
         st = _GltfStats()
         _check(_lib.reina_scene_add_gltf(self._h, str(path).encode(), C.byref(st)))
         return {f: int(getattr(st, f)) for f, _ in _GltfStats._fields_}
+
+    def define_texture_rgba8(self, rgba8) -> int:
+        """Scene::defineTexture from raw texels: (H, W, 4) uint8, row 0 at v = 0."""
+        a = np.ascontiguousarray(rgba8, np.uint8)
+        if a.ndim != 3 or a.shape[2] != 4:
+            raise ValueError("texture must be (H, W, 4) uint8")
+        out = C.c_uint32()
+        _check(_lib.reina_scene_define_texture_rgba8(self._h, _ptr(a), a.shape[1], a.shape[0], C.byref(out)))
+        return out.value
+
+    def define_texture(self, path) -> int:
+        """Scene::defineTexture(filepath) (src/scene/Scene.cpp:15): an image file, rows flipped vertically."""
+        out = C.c_uint32()
+        _check(_lib.reina_scene_define_texture_file(self._h, str(path).encode(), C.byref(out)))
+        return out.value
+
+    def define_texture_encoded(self, data: bytes) -> int:
+        """Scene::defineTexture(imageData, length) (src/scene/Scene.cpp:22): image file bytes, not flipped."""
+        buf = C.create_string_buffer(bytes(data), len(data))
+        out = C.c_uint32()
+        _check(_lib.reina_scene_define_texture_encoded(self._h, buf, len(data), C.byref(out)))
+        return out.value
+
+    def instance_properties(self) -> np.ndarray:
+        """The InstanceProperties records (structured array with the polyglot.h field names)."""
+        n = C.c_uint32()
+        _check(_lib.reina_scene_export_properties(self._h, None, 0, C.byref(n)))
+        out = np.zeros(n.value, INSTANCE_PROPERTIES_DTYPE)
+        _check(_lib.reina_scene_export_properties(self._h, _ptr(out), n.value, C.byref(n)))
+        return out
+
+    def export_texture(self, texture_id: int) -> np.ndarray:
+        """Texels of a defined texture, (H, W, 4) uint8, row 0 at v = 0."""
+        w, h = C.c_uint32(), C.c_uint32()
+        _check(_lib.reina_scene_export_texture(self._h, texture_id, C.byref(w), C.byref(h), None, 0))
+        out = np.empty((h.value, w.value, 4), np.uint8)
+        _check(_lib.reina_scene_export_texture(self._h, texture_id, C.byref(w), C.byref(h), _ptr(out), out.nbytes))
+        return out
+
+    def texture_count(self) -> int:
+        n = C.c_uint32()
+        _check(_lib.reina_scene_texture_count(self._h, C.byref(n)))
+        return n.value
 
     def object_count(self) -> int:
         n = C.c_uint32()
@@ -840,6 +900,17 @@ class SaveSchedule:
             self.close()
         except Exception:
             pass
+
+
+def decode_image(data: bytes) -> np.ndarray:
+    """An image file's bytes (PNG) decoded to (H, W, 4) uint8, as the texture calls decode them."""
+    L = load_library()
+    buf = C.create_string_buffer(bytes(data), len(data))
+    w, h = C.c_uint32(), C.c_uint32()
+    _check(L.reina_decode_image(buf, len(data), C.byref(w), C.byref(h), None, 0))
+    out = np.empty((h.value, w.value, 4), np.uint8)
+    _check(L.reina_decode_image(buf, len(data), C.byref(w), C.byref(h), _ptr(out), out.nbytes))
+    return out
 
 
 def write_png(path, rgba8: np.ndarray) -> None:

@@ -197,15 +197,20 @@ def col_major(m) -> np.ndarray:
 
 class SceneDesc:
     def __init__(self):
-        self.objects = []     # (v4, idx, tbn9, tbn_idx)
+        self.objects = []     # (v4, idx, tbn9, tbn_idx, uv, uv_idx)
         self.instances = []   # (obj, 4x4 math transform, [materials], face_material or None)
+        self.textures = []    # (H, W, 4) uint8, row 0 at v = 0
 
-    def add_object(self, v4, idx, tbn9=None, tbn_idx=None) -> int:
+    def add_object(self, v4, idx, tbn9=None, tbn_idx=None, uv=None, uv_idx=None) -> int:
         v4 = np.asarray(v4, np.float32)
         if v4.shape[1] == 3:
             v4 = np.concatenate([v4, np.ones((v4.shape[0], 1), np.float32)], 1)
-        self.objects.append((v4, np.asarray(idx, np.uint32).reshape(-1), tbn9, tbn_idx))
+        self.objects.append((v4, np.asarray(idx, np.uint32).reshape(-1), tbn9, tbn_idx, uv, uv_idx))
         return len(self.objects) - 1
+
+    def add_texture(self, rgba8) -> int:
+        self.textures.append(np.ascontiguousarray(rgba8, np.uint8))
+        return len(self.textures) - 1
 
     def add_instance(self, obj, transform=None, material=None, materials=None, face_material=None):
         T = np.eye(4, dtype=np.float32) if transform is None else np.asarray(transform, np.float32)
@@ -213,8 +218,10 @@ class SceneDesc:
 
     def to_product(self, R, ctx, require_emissive=False):
         s = R.Scene(ctx)
-        for v4, idx, t9, ti in self.objects:
-            s.define_object(v4, idx, tbns=t9, tbn_indices=ti)
+        for tex in self.textures:
+            s.define_texture_rgba8(tex)
+        for v4, idx, t9, ti, uv, ui in self.objects:
+            s.define_object(v4, idx, tbns=t9, tbn_indices=ti, tex_coords=uv, tex_indices=ui)
         for obj, T, mats, fm in self.instances:
             if fm is None:
                 s.add_instance(obj, T, mats[0])
@@ -225,8 +232,10 @@ class SceneDesc:
 
     def to_oracle(self, O):
         s = O.Scene()
-        for v4, idx, t9, ti in self.objects:
-            s.add_object(v4, idx, t9, ti)
+        for tex in self.textures:
+            s.add_texture(tex)
+        for v4, idx, t9, ti, uv, ui in self.objects:
+            s.add_object(v4, idx, t9, ti, uv, ui)
         for obj, T, mats, fm in self.instances:
             s.add_instance(obj, col_major(T), mats, fm)
         s.finalize()
@@ -320,4 +329,115 @@ def material_zoo(R, seed: int = 3) -> SceneDesc:
     for k, (m, p) in enumerate(zip(mats, pos)):
         T = translate(*p) @ rotate_y(20.0 * k) @ scale(0.22, 0.22 if k != 3 else 0.3, 0.22)
         d.add_instance(sph, T, m)
+    return d
+
+
+# ---------------------------------------------------------------------------------------------------
+# Textured room: the Cornell walls with UVs and tangent frames, seeded procedural textures (albedo with
+# transparent and half-transparent cells, tangent-space normal map, smooth height map, tint), and every
+# texture stage on every material: Disney floor (albedo + alpha, bump map, normal map, UVs x2 so they
+# wrap), Lambertian back wall (tint + normal map), metal left wall (tint + normal map), Lambertian right
+# wall (albedo + alpha, so paths pass through its transparent cells), ceiling textured without UVs
+# (samples UV (0, 0)), a bump-mapped Lambertian box, a dielectric box (tint + normal map) and a textured
+# Disney sphere with spherical UVs.
+
+def textured_quad(corner, e1, e2, uv_scale=1.0):
+    """Quad with UVs (0,0), (s,0), (s,s), (0,s) and the tangent frame T = e1, B = e2, N = e1 x e2."""
+    v, i = quad(corner, e1, e2)
+    uv = np.array([[0, 0], [1, 0], [1, 1], [0, 1]], np.float32) * uv_scale
+    t = np.asarray(e1, np.float64) / np.linalg.norm(e1)
+    b = np.asarray(e2, np.float64) / np.linalg.norm(e2)
+    n = np.cross(t, b)
+    tbn = np.tile(np.concatenate([t, b, n / np.linalg.norm(n)]).astype(np.float32), (4, 1))
+    return v, i, tbn, uv
+
+
+def merge_quads(quads):
+    vs, idx, tbns, uvs = [], [], [], []
+    base = 0
+    for v, i, t, u in quads:
+        vs.append(v)
+        idx.append(i + base)
+        tbns.append(t)
+        uvs.append(u)
+        base += len(v)
+    i = np.concatenate(idx).astype(np.uint32)
+    return np.concatenate(vs), i, np.concatenate(tbns), i.copy(), np.concatenate(uvs), i.copy()
+
+
+def textured_box(uv_scale=1.0):
+    """Unit cube as six textured quads (outward normals)."""
+    h = 0.5
+    faces = [((-h, -h, h), (1, 0, 0), (0, 1, 0)), ((h, -h, -h), (-1, 0, 0), (0, 1, 0)),
+             ((h, -h, h), (0, 0, -1), (0, 1, 0)), ((-h, -h, -h), (0, 0, 1), (0, 1, 0)),
+             ((-h, h, h), (1, 0, 0), (0, 0, -1)), ((-h, -h, -h), (1, 0, 0), (0, 0, 1))]
+    return merge_quads([textured_quad(c, a, b, uv_scale) for c, a, b in faces])
+
+
+def room_textures(seed: int = 1):
+    rng = np.random.default_rng(seed)
+    # 0: albedo checker 32x32 in 4x4 cells, alpha 0 / 128 / 255 per cell
+    cells = rng.integers(0, 6, (8, 8))
+    col = np.where((np.add.outer(np.arange(8), np.arange(8)) % 2)[..., None] == 0, [230, 200, 150], [60, 110, 190])
+    albedo = np.zeros((32, 32, 4), np.uint8)
+    albedo[..., :3] = np.kron(col, np.ones((4, 4, 1))).astype(np.uint8)
+    alpha = np.where(cells == 0, 0, np.where(cells == 1, 128, 255))
+    albedo[..., 3] = np.kron(alpha, np.ones((4, 4))).astype(np.uint8)
+    # 1: normal map 24x24: tilted tangent-space normals
+    nx, ny = rng.uniform(-0.6, 0.6, (2, 24, 24))
+    n = np.stack([nx, ny, np.ones_like(nx)], -1)
+    n /= np.linalg.norm(n, axis=-1, keepdims=True)
+    nmap = np.zeros((24, 24, 4), np.uint8)
+    nmap[..., :3] = np.clip(np.round((n * 0.5 + 0.5) * 255), 0, 255).astype(np.uint8)
+    nmap[..., 3] = 255
+    # 2: height map 32x32 (red channel): smooth bumps plus noise
+    y, x = np.mgrid[0:32, 0:32] / 32.0
+    hgt = 0.5 + 0.35 * np.sin(2 * np.pi * 2 * x) * np.cos(2 * np.pi * 3 * y) + rng.uniform(-0.1, 0.1, (32, 32))
+    height = np.zeros((32, 32, 4), np.uint8)
+    height[..., 0] = np.clip(np.round(hgt * 255), 0, 255).astype(np.uint8)
+    height[..., 1:3] = 40
+    height[..., 3] = 255
+    # 3: tint 16x16
+    tint = np.concatenate([rng.integers(90, 256, (16, 16, 3)), np.full((16, 16, 1), 255)], -1).astype(np.uint8)
+    return [albedo, nmap, height, tint]
+
+
+def textured_room(R, seed: int = 1) -> SceneDesc:
+    d = SceneDesc()
+    for t in room_textures(seed):
+        d.add_texture(t)
+    ALB, NRM, HGT, TNT = 0, 1, 2, 3
+    M = R.Material
+    one = dict(specular_tint=(1, 1, 1), sheen_tint=(1, 1, 1))
+    floor = textured_quad((-1, -1, 1), (2, 0, 0), (0, 0, -2), 2.0)
+    back = textured_quad((-1, -1, -1), (2, 0, 0), (0, 2, 0))
+    left = textured_quad((-1, -1, 1), (0, 0, -2), (0, 2, 0))
+    right = textured_quad((1, -1, -1), (0, 0, 2), (0, 2, 0))
+    for (v, i, t, uv), mat in [
+        (floor, M(material_idx=3, albedo=(0.9, 0.9, 0.9), roughness=0.5, texture_id=ALB, normal_map_id=NRM,
+                  bump_map_id=HGT, **one)),
+        (back, M(material_idx=0, albedo=(0.8, 0.8, 0.8), texture_id=TNT, normal_map_id=NRM)),
+        (left, M(material_idx=1, albedo=(0.9, 0.6, 0.5), roughness=0.25, texture_id=TNT, normal_map_id=NRM)),
+        (right, M(material_idx=0, albedo=(0.3, 0.8, 0.3), texture_id=ALB)),
+    ]:
+        d.add_instance(d.add_object(v, i, t, i, uv, i), None, mat)
+    cv, ci = quad((-1, 1, -1), (2, 0, 0), (0, 0, 2))   # ceiling, no UVs: samples UV (0, 0)
+    d.add_instance(d.add_object(cv, ci), None, M(material_idx=0, albedo=(0.8, 0.8, 0.8), texture_id=TNT))
+    bv, bi, bt, bti, buv, bui = textured_box(1.5)
+    box = d.add_object(bv, bi, bt, bti, buv, bui)
+    d.add_instance(box, translate(-0.4, -0.55, -0.35) @ rotate_y(25.0) @ scale(0.5, 0.9, 0.5),
+                   M(material_idx=0, albedo=(0.85, 0.85, 0.85), bump_map_id=HGT))
+    d.add_instance(box, translate(0.45, -0.75, 0.3) @ rotate_y(-20.0) @ scale(0.45, 0.5, 0.45),
+                   M(material_idx=2, albedo=(0.95, 0.95, 0.95), ior=1.5, absorption=0.8, roughness=0.02,
+                     texture_id=TNT, normal_map_id=NRM))
+    v, i, tbn, ti = sphere_tbn(3, 0.0, seed, R)
+    p = v[:, :3] / np.linalg.norm(v[:, :3], axis=1, keepdims=True)
+    uv = np.stack([np.arctan2(p[:, 2], p[:, 0]) / (2 * np.pi) + 0.5, np.arccos(np.clip(p[:, 1], -1, 1)) / np.pi], 1)
+    sph = d.add_object(v, i, tbn, ti, uv.astype(np.float32), i)
+    d.add_instance(sph, translate(0.1, 0.25, -0.2) @ scale(0.28, 0.28, 0.28),
+                   M(material_idx=3, albedo=(1, 1, 1), roughness=0.35, metallic=0.4, clearcoat=0.5, texture_id=ALB,
+                     normal_map_id=NRM, interp_normals=True, **one))
+    lv, li = quad((-0.25, 0.999, -0.2), (0.5, 0, 0), (0, 0, 0.4))
+    d.add_instance(d.add_object(lv, li), None,
+                   M(material_idx=0, albedo=(0.78, 0.78, 0.78), emission=CORNELL_LIGHT, cull_backface=True))
     return d

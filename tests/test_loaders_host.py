@@ -283,3 +283,69 @@ def test_png_round_trip(R, tmp_path, w, h):
     p = tmp_path / "o.png"
     R.write_png(p, img)
     assert np.array_equal(read_png(p.read_bytes()), img)
+
+
+def png_bytes(rgba: np.ndarray) -> bytes:
+    """A minimal RGBA8 PNG (filter 0 rows, zlib) written by the test."""
+    h, w = rgba.shape[:2]
+
+    def chunk(t, d):
+        return struct.pack(">I", len(d)) + t + d + struct.pack(">I", zlib.crc32(t + d) & 0xFFFFFFFF)
+
+    raw = b"".join(b"\0" + rgba[y].astype(np.uint8).tobytes() for y in range(h))
+    return (b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, 6, 0, 0, 0)) +
+            chunk(b"IDAT", zlib.compress(raw)) + chunk(b"IEND", b""))
+
+
+def test_gltf_textures(R, host_ctx, tmp_path):
+    """Images from a data URI, a buffer view and a percent-encoded relative file become scene textures in
+    image order (not flipped); a JPEG image is left out and its material reference counted as ignored."""
+    rng = np.random.default_rng(5)
+    imgs = [rng.integers(0, 256, (3 + k, 4 + k, 4)).astype(np.uint8) for k in range(3)]
+    pngs = [png_bytes(a) for a in imgs]
+    (tmp_path / "tex dir").mkdir()
+    (tmp_path / "tex dir" / "c.png").write_bytes(pngs[2])
+    pos = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0]], np.float32)
+    nrm = np.array([[0, 0, 1]] * 4, np.float32)
+    uv = np.array([[0, 0], [1, 0], [1, 1], [0, 1]], np.float32)
+    idx = np.array([0, 1, 2, 0, 2, 3], np.uint16)
+    data = b""
+    views = []
+    for bl in [pos.tobytes(), nrm.tobytes(), uv.tobytes(), idx.tobytes(), pngs[1]]:
+        while len(data) % 4:
+            data += b"\0"
+        views.append({"buffer": 0, "byteOffset": len(data), "byteLength": len(bl)})
+        data += bl
+    prim = {"attributes": {"POSITION": 0, "NORMAL": 1, "TEXCOORD_0": 2}, "indices": 3}
+    doc = {
+        "asset": {"version": "2.0"}, "scene": 0, "scenes": [{"nodes": [0]}], "nodes": [{"mesh": 0}],
+        "meshes": [{"primitives": [dict(prim, material=0), dict(prim, material=1), dict(prim, material=2)]}],
+        "materials": [{"pbrMetallicRoughness": {"baseColorTexture": {"index": 0}}, "normalTexture": {"index": 1}},
+                      {"pbrMetallicRoughness": {"baseColorTexture": {"index": 2}}, "normalTexture": {"index": 3}},
+                      {}],
+        "textures": [{"source": 0}, {"source": 1}, {"source": 2}, {"source": 3}],
+        "images": [{"uri": "data:image/png;base64," + base64.b64encode(pngs[0]).decode()},
+                   {"bufferView": 4, "mimeType": "image/png"},
+                   {"uri": "tex%20dir/c.png"},
+                   {"uri": "data:image/jpeg;base64," + base64.b64encode(b"\xff\xd8\xff\xe0 jpeg").decode()}],
+        "accessors": [{"bufferView": 0, "componentType": 5126, "count": 4, "type": "VEC3"},
+                      {"bufferView": 1, "componentType": 5126, "count": 4, "type": "VEC3"},
+                      {"bufferView": 2, "componentType": 5126, "count": 4, "type": "VEC2"},
+                      {"bufferView": 3, "componentType": 5123, "count": 6, "type": "SCALAR"}],
+        "bufferViews": views,
+        "buffers": [{"byteLength": len(data), "uri": "data:application/octet-stream;base64," +
+                     base64.b64encode(data).decode()}],
+    }
+    p = tmp_path / "t.gltf"
+    p.write_text(json.dumps(doc))
+    s = R.Scene(host_ctx)
+    st = s.add_gltf(p)
+    assert st["ignored_textures"] == 1 and st["instances"] == 3
+    assert s.texture_count() == 3
+    props = s.instance_properties()
+    assert list(props["textureID"]) == [0, 2, -1]
+    assert list(props["normalMapTexID"]) == [1, -1, -1]
+    assert list(props["bumpMapTexID"]) == [-1, -1, -1]
+    s.build()
+    for k in range(3):   # texels as written: no vertical flip for glTF images
+        assert np.array_equal(s.export_texture(k), imgs[k])
