@@ -19,9 +19,18 @@ struct Bvh8 {
     double seconds = 0.0;
 };
 
+// How the binary BVH is collapsed into 8-wide nodes: greedily (open the largest-area internal child until
+// 8 children), or by the SAH-optimal dynamic programme of Ylitie, Karras and Laine (HPG 2017, section
+// 3.1), which also merges subtrees of up to 3 triangles into one leaf child.
+enum BvhCollapse : int { kCollapseGreedy = 0, kCollapseSahDp = 1 };
+#ifndef RT_COLLAPSE
+#define RT_COLLAPSE 1
+#endif
+
 struct BvhBuildOptions {
     int sah_bins = 32;
     int max_threads = 0;           // 0 = std::thread::hardware_concurrency()
+    int collapse = RT_COLLAPSE;
 };
 
 // `verts` holds 9 floats per triangle (v0, v1, v2 in world space); triangle i gets id i.
