@@ -70,6 +70,23 @@ def rng(seed: int, n: int):
     return w, f, d
 
 
+_SHADING_SIGS["oracle_bvh8_raycast"] = (None, [C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p, C.c_uint64, C.c_int,
+                                               C.c_int, C.c_void_p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)])
+
+
+def bvh8_raycast(nodes: np.ndarray, tris: np.ndarray, rays: np.ndarray, any_hit: bool = False, threads: int = 0):
+    """Traverses the product's exported BVH8 (node bytes, 48-byte triangle records) on the CPU.  Returns
+    (hits with unrefined t/u/v, node visits, triangle tests)."""
+    nb = np.ascontiguousarray(nodes).view(np.uint8).reshape(-1)
+    tb = np.ascontiguousarray(tris).view(np.float32).reshape(-1)
+    r = np.ascontiguousarray(rays)
+    hits = np.zeros(r.shape[0], HIT_DTYPE)
+    nv, nt = C.c_uint64(0), C.c_uint64(0)
+    lib().oracle_bvh8_raycast(_p(nb), nb.size // 80, _p(tb), _p(r), r.shape[0], int(any_hit), threads, _p(hits),
+                              C.byref(nv), C.byref(nt))
+    return hits, nv.value, nt.value
+
+
 class Bvh:
     def __init__(self, tris9: np.ndarray):
         self.tris = np.ascontiguousarray(tris9, dtype=np.float32).reshape(-1, 9)

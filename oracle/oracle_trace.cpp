@@ -393,11 +393,142 @@ static void parallel_for(uint64_t n, int threads, F&& f) {
     for (auto& th : pool) th.join();
 }
 
+// ---------------------------------------------------------------------------------------------------
+// Traversal of the product's exported BVH8 (the compressed 8-wide layout of Ylitie, Karras and Laine,
+// HPG 2017, as the library's C ABI documents it: 80-byte nodes with a power-of-two quantization frame,
+// 8 child slots assigned by octant, meta byte per slot = triangle-count unary code << 5 | bit index,
+// internal children at bit indices 24 + slot; 48-byte triangle records v0 | id, v1, v2).  Written
+// from that description to count the node visits and triangle tests behind the ray cast's byte
+// accounting, and to check on the CPU that the exported tree finds the same hits as the oracle's own
+// BVH.  Closest hit visits children nearest-first by octant order and tests a node's triangles as soon
+// as it reaches them (no postponing).
+struct Bvh8View {
+    const uint8_t* nodes;
+    uint64_t node_count;
+    const float* tris;   // 12 floats per record
+};
+
+inline float f32_bits(uint32_t u) {
+    float f;
+    std::memcpy(&f, &u, 4);
+    return f;
+}
+
+inline uint32_t bvh8_children(const uint8_t* n, const PreRay<float>& r, float idx, float idy, float idz,
+                              uint32_t oct_inv, float tmax) {
+    float p[3];
+    std::memcpy(p, n, 12);
+    const float id[3] = {idx, idy, idz};
+    const float o[3] = {r.o.x, r.o.y, r.o.z};
+    float sc[3], of[3];
+    for (int k = 0; k < 3; ++k) {
+        sc[k] = f32_bits(((uint32_t)n[12 + k] + 15u) << 23) * id[k];   // 2^(e+15) in t units
+        of[k] = std::fma(p[k] - o[k], id[k], -sc[k]);
+    }
+    const uint8_t* meta = n + 24;
+    const uint8_t* qlo[3] = {n + 32, n + 40, n + 48};
+    const uint8_t* qhi[3] = {n + 56, n + 64, n + 72};
+    uint32_t hitmask = 0;
+    for (int i = 0; i < 8; ++i) {
+        float tn = r.tmin, tf = tmax;
+        for (int k = 0; k < 3; ++k) {
+            const uint8_t qn = id[k] < 0.0f ? qhi[k][i] : qlo[k][i];
+            const uint8_t qf = id[k] < 0.0f ? qlo[k][i] : qhi[k][i];
+            const float a = std::fma(1.0f + (float)qn * (1.0f / 32768.0f), sc[k], of[k]);
+            const float b = std::fma(1.0f + (float)qf * (1.0f / 32768.0f), sc[k], of[k]);
+            tn = std::fmax(tn, a);
+            tf = std::fmin(tf, b);
+        }
+        if (tn <= tf && meta[i] != 0) {
+            uint32_t m = meta[i];
+            if ((m & 0x18u) == 0x18u) m ^= oct_inv;   // internal child: bit index 24 + (slot ^ octant)
+            hitmask |= (m >> 5) << (m & 31u);
+        }
+    }
+    return hitmask;
+}
+
+BestHit<float> trace_bvh8(const Bvh8View& b, const RayRec& ray, bool any, uint64_t& visited, uint64_t& tested) {
+    const PreRay<float> r = precompute<float>(ray);
+    BestHit<float> best;
+    best.t = r.tmax;
+    if (b.node_count == 0) return best;
+    auto rcp = [](float d) { return std::fabs(d) > 1e-30f ? 1.0f / d : std::copysign(1e30f, d); };
+    const float idx = rcp(ray.dx), idy = rcp(ray.dy), idz = rcp(ray.dz);
+    const uint32_t oct = (ray.dx < 0.0f ? 1u : 0u) | (ray.dy < 0.0f ? 2u : 0u) | (ray.dz < 0.0f ? 4u : 0u);
+    const uint32_t oct_inv = 7u - oct;
+    uint32_t gbase = 0, gbits = 0x80000000u;   // node group: child base, hit bits 24..31 | internal mask
+    std::vector<std::pair<uint32_t, uint32_t>> stack;
+    for (;;) {
+        uint32_t tbase = 0, tbits = 0;
+        if (gbits > 0x00FFFFFFu) {
+            const uint32_t slot_bit = 31u - (uint32_t)__builtin_clz(gbits);
+            const uint32_t slot = (slot_bit - 24u) ^ oct_inv;
+            const uint32_t rel = (uint32_t)__builtin_popcount(gbits & ((1u << slot) - 1u));
+            const uint32_t child = gbase + rel;
+            gbits &= ~(1u << slot_bit);
+            if (gbits > 0x00FFFFFFu) stack.emplace_back(gbase, gbits);
+            if (child >= b.node_count) return best;   // malformed tree
+            const uint8_t* n = b.nodes + 80ull * child;
+            ++visited;
+            const uint32_t hm = bvh8_children(n, r, idx, idy, idz, oct_inv, best.t);
+            uint32_t cb, tb;
+            std::memcpy(&cb, n + 16, 4);
+            std::memcpy(&tb, n + 20, 4);
+            gbase = cb;
+            gbits = (hm & 0xFF000000u) | n[15];
+            tbase = tb;
+            tbits = hm & 0x00FFFFFFu;
+        }
+        while (tbits) {
+            const int k = __builtin_ctz(tbits);
+            tbits &= tbits - 1u;
+            const float* rec = b.tris + 12ull * (tbase + (uint32_t)k);
+            const float tri[9] = {rec[0], rec[1], rec[2], rec[4], rec[5], rec[6], rec[8], rec[9], rec[10]};
+            uint32_t id;
+            std::memcpy(&id, rec + 3, 4);
+            ++tested;
+            float t, u, v;
+            if (!watertight(r, tri, best.t, t, u, v)) continue;
+            if (any) {
+                best.prim = id; best.t = t; best.u = u; best.v = v;
+                return best;
+            }
+            if (t < best.t || id < best.prim) {
+                best.prim = id; best.t = t; best.u = u; best.v = v;
+            }
+        }
+        if (gbits <= 0x00FFFFFFu) {
+            if (stack.empty()) return best;
+            gbase = stack.back().first;
+            gbits = stack.back().second;
+            stack.pop_back();
+        }
+    }
+}
+
 }  // namespace oracle
 
 using namespace oracle;
 
 extern "C" {
+
+// Casts rays through an exported BVH8 (float mode, unrefined t/u/v); adds the node visits and triangle
+// tests to *visited and *tested.
+void oracle_bvh8_raycast(const uint8_t* nodes, uint64_t node_count, const float* tris, const RayRec* rays, uint64_t n,
+                         int any, int threads, HitRec* hits, uint64_t* visited, uint64_t* tested) {
+    const Bvh8View b{nodes, node_count, tris};
+    std::atomic<uint64_t> nv{0}, nt{0};
+    parallel_for(n, threads, [&](uint64_t i) {
+        uint64_t v = 0, t = 0;
+        const BestHit<float> h = trace_bvh8(b, rays[i], any != 0, v, t);
+        hits[i] = HitRec{h.prim, h.t, h.u, h.v};
+        nv += v;
+        nt += t;
+    });
+    *visited += nv.load();
+    *tested += nt.load();
+}
 
 int oracle_hw_threads(void) { return (int)std::max(1u, std::thread::hardware_concurrency()); }
 

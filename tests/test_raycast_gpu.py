@@ -164,6 +164,14 @@ def test_large_scene_subset_and_counters(R, O, gpu_ctx):
     per_ray_nodes = nodes / rays.shape[0]
     assert 1.0 <= per_ray_nodes < 200
     assert 0.0 < ntris / rays.shape[0] < 500
+    # the counts behind the byte accounting against the CPU traversal of the same exported BVH8, which
+    # tests triangles as soon as it reaches them (the GPU postpones some, so it may visit a few more nodes)
+    bvh_nodes, trecs = scene.export_bvh()
+    h8, cpu_nodes, cpu_tris = O.bvh8_raycast(bvh_nodes, trecs, rays)
+    assert np.array_equal(h8["prim"], hits["prim"])
+    print(f"node visits gpu/cpu {nodes / cpu_nodes:.4f}, triangle tests gpu/cpu {ntris / cpu_tris:.4f}")
+    assert 0.98 <= nodes / cpu_nodes <= 1.10
+    assert 0.98 <= ntris / cpu_tris <= 1.10
 
 
 def test_raycast_page_locked_host_buffers(R, gpu_ctx):
