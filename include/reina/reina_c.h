@@ -175,6 +175,18 @@ int reina_scene_build(reina_scene* scene, uint32_t require_emissive);
 /* Scene::getEmissiveWeight()  (src/scene/Scene.h:118): total emissive weight Σ area·luminance. */
 float reina_scene_emissive_weight(const reina_scene* scene);
 
+/* Acceleration structure of a scene, chosen before reina_scene_build:
+ *   REINA_ACCEL_AUTO       two levels when instancing repeats models (the flattened triangle count is at
+ *                          least twice the count of one copy per model) and every transform is invertible
+ *   REINA_ACCEL_FLAT       one BVH8 over all instances' world-space triangles
+ *   REINA_ACCEL_TWO_LEVEL  the reference's structure (src/scene/Scene.cpp:93-116): a top-level BVH8 over
+ *                          instances and one bottom-level BVH8 per model in object space; rays enter an
+ *                          instance through its inverse transform (REINA_ERR_INVALID at the build if a
+ *                          transform is singular).
+ * Hit ids are global triangle ids either way (instance's first triangle + triangle within the model). */
+enum { REINA_ACCEL_AUTO = 0, REINA_ACCEL_FLAT = 1, REINA_ACCEL_TWO_LEVEL = 2 };
+int reina_scene_set_accel(reina_scene* scene, int mode);
+
 typedef struct reina_scene_stats {
     uint64_t triangle_count;
     uint64_t instance_count;
@@ -187,12 +199,21 @@ typedef struct reina_scene_stats {
     double build_seconds;        /* host BVH build time */
     float bounds_min[3];
     float bounds_max[3];
+    uint32_t two_level;          /* 1: top level over instances + bottom levels per model */
+    uint32_t blas_count;         /* bottom-level BVHs (two-level scenes) */
 } reina_scene_stats;
 int reina_scene_get_stats(const reina_scene* scene, reina_scene_stats* out_stats);
 
 /* Copies the scene's BVH8 nodes (node_count * 80 bytes) and traversal triangles (triangle_count * 48
  * bytes) to host buffers, for inspection and structural checks.  Either pointer may be NULL. */
 int reina_scene_export_bvh(const reina_scene* scene, void* nodes_out, void* triangles_out);
+
+/* Two-level scenes: copies the per-instance traversal records (64 bytes each: world-to-object matrix as
+ * 12 floats row-major 3x4, bottom-level root node index, first global triangle id, 2 words of padding)
+ * and the top-level leaf entries (instance ids; a top-level leaf child's offset indexes them from the
+ * node's tri_base).  Either pointer may be NULL; the counts are written (0 for a flat scene). */
+int reina_scene_export_two_level(const reina_scene* scene, void* instance_records, uint32_t* tlas_refs,
+                                 uint32_t* out_instance_count, uint32_t* out_ref_count);
 
 /* Copies the scene's InstanceProperties records (polyglot.h; the records the closest-hit shaders read,
  * built as src/scene/Scene.cpp:27-54 builds them) to `out` (capacity records; NULL to query the count

@@ -87,6 +87,62 @@ def bvh8_raycast(nodes: np.ndarray, tris: np.ndarray, rays: np.ndarray, any_hit:
     return hits, nv.value, nt.value
 
 
+_SHADING_SIGS.update({
+    "oracle_instanced_new": (C.c_void_p, []),
+    "oracle_instanced_free": (None, [C.c_void_p]),
+    "oracle_instanced_add_model": (C.c_uint32, [C.c_void_p, C.c_void_p, C.c_uint64]),
+    "oracle_instanced_add_instance": (None, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32]),
+    "oracle_instanced_raycast": (None, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_int, C.c_int, C.c_void_p]),
+    "oracle_bvh8_two_level_raycast": (None, [C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                             C.c_uint64, C.c_int, C.c_int, C.c_void_p, C.POINTER(C.c_uint64),
+                                             C.POINTER(C.c_uint64)]),
+})
+
+
+class InstancedScene:
+    """The oracle's two-level restatement: models in object space (9 floats per triangle), instances as
+    (model, world-to-object 3x4 row-major matrix, first global triangle id)."""
+
+    def __init__(self):
+        self._h = lib().oracle_instanced_new()
+
+    def __del__(self):
+        try:
+            if self._h:
+                lib().oracle_instanced_free(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+    def add_model(self, tris9) -> int:
+        t = np.ascontiguousarray(tris9, np.float32).reshape(-1, 9)
+        return int(lib().oracle_instanced_add_model(self._h, _p(t), t.shape[0]))
+
+    def add_instance(self, model: int, inv12, first_prim: int) -> None:
+        m = np.ascontiguousarray(inv12, np.float32).reshape(12)
+        lib().oracle_instanced_add_instance(self._h, model, _p(m), first_prim)
+
+    def raycast(self, rays: np.ndarray, any_hit: bool = False, threads: int = 0) -> np.ndarray:
+        r = np.ascontiguousarray(rays)
+        hits = np.zeros(r.shape[0], HIT_DTYPE)
+        lib().oracle_instanced_raycast(self._h, _p(r), r.shape[0], int(any_hit), threads, _p(hits))
+        return hits
+
+
+def bvh8_two_level_raycast(nodes, tris, refs, inst_records, rays, any_hit: bool = False, threads: int = 0):
+    """Traverses an exported two-level BVH8 on the CPU: (hits with unrefined t/u/v, visits, tests)."""
+    nb = np.ascontiguousarray(nodes).view(np.uint8).reshape(-1)
+    tb = np.ascontiguousarray(tris).view(np.float32).reshape(-1)
+    rf = np.ascontiguousarray(refs, np.uint32)
+    ib = np.ascontiguousarray(inst_records).view(np.uint8).reshape(-1)
+    r = np.ascontiguousarray(rays)
+    hits = np.zeros(r.shape[0], HIT_DTYPE)
+    nv, nt = C.c_uint64(0), C.c_uint64(0)
+    lib().oracle_bvh8_two_level_raycast(_p(nb), nb.size // 80, _p(tb), _p(rf), _p(ib), _p(r), r.shape[0], int(any_hit),
+                                        threads, _p(hits), C.byref(nv), C.byref(nt))
+    return hits, nv.value, nt.value
+
+
 class Bvh:
     def __init__(self, tris9: np.ndarray):
         self.tris = np.ascontiguousarray(tris9, dtype=np.float32).reshape(-1, 9)

@@ -448,7 +448,8 @@ inline uint32_t bvh8_children(const uint8_t* n, const PreRay<float>& r, float id
     return hitmask;
 }
 
-BestHit<float> trace_bvh8(const Bvh8View& b, const RayRec& ray, bool any, uint64_t& visited, uint64_t& tested) {
+BestHit<float> trace_bvh8_from(const Bvh8View& b, uint32_t root, const RayRec& ray, bool any, uint64_t& visited,
+                               uint64_t& tested) {
     const PreRay<float> r = precompute<float>(ray);
     BestHit<float> best;
     best.t = r.tmax;
@@ -457,7 +458,7 @@ BestHit<float> trace_bvh8(const Bvh8View& b, const RayRec& ray, bool any, uint64
     const float idx = rcp(ray.dx), idy = rcp(ray.dy), idz = rcp(ray.dz);
     const uint32_t oct = (ray.dx < 0.0f ? 1u : 0u) | (ray.dy < 0.0f ? 2u : 0u) | (ray.dz < 0.0f ? 4u : 0u);
     const uint32_t oct_inv = 7u - oct;
-    uint32_t gbase = 0, gbits = 0x80000000u;   // node group: child base, hit bits 24..31 | internal mask
+    uint32_t gbase = root, gbits = 0x80000000u;   // node group: child base, hit bits 24..31 | internal mask
     std::vector<std::pair<uint32_t, uint32_t>> stack;
     for (;;) {
         uint32_t tbase = 0, tbits = 0;
@@ -507,11 +508,178 @@ BestHit<float> trace_bvh8(const Bvh8View& b, const RayRec& ray, bool any, uint64
     }
 }
 
+BestHit<float> trace_bvh8(const Bvh8View& b, const RayRec& ray, bool any, uint64_t& visited, uint64_t& tested) {
+    return trace_bvh8_from(b, 0u, ray, any, visited, tested);
+}
+
+// ---------------------------------------------------------------------------------------------------
+// Two-level scenes.  A ray enters an instance through the instance's world-to-object matrix (row-major
+// 3x4), evaluated as ((m0 x + m1 y) + m2 z) + m3 per row in IEEE binary32; t is unchanged by the affine
+// change of space.  Hit ids are global: the instance's first triangle + the triangle's index in its model.
+inline RayRec to_instance(const RayRec& w, const float* m) {
+    auto row = [&](int r, float x, float y, float z) { return (m[4 * r] * x + m[4 * r + 1] * y) + m[4 * r + 2] * z; };
+    RayRec o;
+    o.ox = row(0, w.ox, w.oy, w.oz) + m[3];
+    o.oy = row(1, w.ox, w.oy, w.oz) + m[7];
+    o.oz = row(2, w.ox, w.oy, w.oz) + m[11];
+    o.dx = row(0, w.dx, w.dy, w.dz);
+    o.dy = row(1, w.dx, w.dy, w.dz);
+    o.dz = row(2, w.dx, w.dy, w.dz);
+    o.tmin = w.tmin;
+    o.tmax = w.tmax;
+    return o;
+}
+
+// The oracle's own two-level restatement: per model its binary BVH over object-space triangles; every
+// instance is tried (no top level), keeping the closest hit (ties: lower global id) or the first hit.
+struct InstancedScene {
+    std::vector<std::unique_ptr<Bvh>> models;
+    struct Inst {
+        uint32_t model;
+        float inv[12];
+        uint32_t first_prim;
+    };
+    std::vector<Inst> insts;
+};
+
+inline HitRec trace_instanced(const InstancedScene& s, const RayRec& w, bool any) {
+    HitRec best{kMiss, w.tmax, 0.0f, 0.0f};
+    float best_t = w.tmax;
+    uint32_t best_inst = 0;
+    BestHit<float> bh;
+    for (size_t i = 0; i < s.insts.size(); ++i) {
+        const InstancedScene::Inst& in = s.insts[i];
+        RayRec r = to_instance(w, in.inv);
+        r.tmax = best_t;
+        const Bvh& b = *s.models[in.model];
+        const BestHit<float> h = trace_bvh<float>(b, r, any, nullptr);
+        if (h.prim == kMiss) continue;
+        const uint32_t g = in.first_prim + h.prim;
+        if (h.t < best_t || g < best.prim) {
+            best_t = h.t;
+            best = HitRec{g, h.t, h.u, h.v};
+            best_inst = (uint32_t)i;
+            bh = h;
+            if (any) break;
+        }
+    }
+    if (best.prim != kMiss) {   // refined in the instance's space, as the device reports it
+        const InstancedScene::Inst& in = s.insts[best_inst];
+        const RayRec r = to_instance(w, in.inv);
+        const Bvh& b = *s.models[in.model];
+        const HitRec f = finish32(bh, r, b.tris.data() + 9ull * (best.prim - in.first_prim));
+        best.t = f.t;
+        best.u = f.u;
+        best.v = f.v;
+    }
+    return best;
+}
+
+// Traversal of an exported two-level BVH8 (the device's layout: top-level root = node 0, its leaf entries
+// index `refs` (instance ids); per instance a 64-byte record: world-to-object matrix, bottom-level root
+// node, first global triangle).  Counts node visits and triangle tests; unrefined t/u/v.
+BestHit<float> trace_bvh8_two_level(const Bvh8View& b, const uint32_t* refs, const uint8_t* inst, const RayRec& wray,
+                                    bool any, uint64_t& visited, uint64_t& tested) {
+    BestHit<float> best;
+    best.t = wray.tmax;
+    // the top level with the world ray: gather every instance whose box the ray reaches (in the device's
+    // order the culling distance can be smaller; this is conservative), then traverse the instances
+    std::vector<uint32_t> pending;
+    {
+        const PreRay<float> r = precompute<float>(wray);
+        auto rcp = [](float d) { return std::fabs(d) > 1e-30f ? 1.0f / d : std::copysign(1e30f, d); };
+        const float idx = rcp(wray.dx), idy = rcp(wray.dy), idz = rcp(wray.dz);
+        const uint32_t oct = (wray.dx < 0.0f ? 1u : 0u) | (wray.dy < 0.0f ? 2u : 0u) | (wray.dz < 0.0f ? 4u : 0u);
+        std::vector<uint32_t> st = {0u};
+        while (!st.empty()) {
+            const uint32_t ni = st.back();
+            st.pop_back();
+            const uint8_t* n = b.nodes + 80ull * ni;
+            ++visited;
+            const uint32_t hm = bvh8_children(n, r, idx, idy, idz, 7u - oct, wray.tmax);
+            uint32_t cb, tb;
+            std::memcpy(&cb, n + 16, 4);
+            std::memcpy(&tb, n + 20, 4);
+            for (uint32_t bit = 24; bit < 32; ++bit)
+                if (hm >> bit & 1u) {
+                    const uint32_t slot = (bit - 24u) ^ (7u - oct);
+                    st.push_back(cb + (uint32_t)__builtin_popcount(n[15] & ((1u << slot) - 1u)));
+                }
+            for (uint32_t bit = 0; bit < 24; ++bit)
+                if (hm >> bit & 1u) pending.push_back(refs[tb + bit]);
+        }
+    }
+    std::sort(pending.begin(), pending.end());
+    for (uint32_t ii : pending) {
+        const uint8_t* rec = inst + 64ull * ii;
+        float m[12];
+        uint32_t root, first;
+        std::memcpy(m, rec, 48);
+        std::memcpy(&root, rec + 48, 4);
+        std::memcpy(&first, rec + 52, 4);
+        if (root == 0xFFFFFFFFu) continue;
+        RayRec r = to_instance(wray, m);
+        r.tmax = best.t;
+        // the instance's bottom level, nearest child first (the flat traversal from its root)
+        Bvh8View sub{b.nodes, b.node_count, b.tris};
+        const uint64_t v0 = visited;
+        BestHit<float> h = trace_bvh8_from(sub, root, r, any, visited, tested);
+        (void)v0;
+        if (h.prim == kMiss) continue;
+        const uint32_t g = first + h.prim;
+        if (h.t < best.t || g < best.prim) {
+            best.prim = g;
+            best.t = h.t;
+            best.u = h.u;
+            best.v = h.v;
+            if (any) break;
+        }
+    }
+    return best;
+}
+
 }  // namespace oracle
 
 using namespace oracle;
 
 extern "C" {
+
+void* oracle_instanced_new(void) { return new InstancedScene(); }
+void oracle_instanced_free(void* h) { delete static_cast<InstancedScene*>(h); }
+uint32_t oracle_instanced_add_model(void* h, const float* tris9, uint64_t n) {
+    InstancedScene* s = static_cast<InstancedScene*>(h);
+    s->models.emplace_back(build_bvh(tris9, n));
+    return (uint32_t)(s->models.size() - 1);
+}
+void oracle_instanced_add_instance(void* h, uint32_t model, const float* inv12, uint32_t first_prim) {
+    InstancedScene* s = static_cast<InstancedScene*>(h);
+    InstancedScene::Inst in;
+    in.model = model;
+    std::memcpy(in.inv, inv12, sizeof(in.inv));
+    in.first_prim = first_prim;
+    s->insts.push_back(in);
+}
+void oracle_instanced_raycast(void* h, const RayRec* rays, uint64_t n, int any, int threads, HitRec* hits) {
+    const InstancedScene& s = *static_cast<InstancedScene*>(h);
+    parallel_for(n, threads, [&](uint64_t i) { hits[i] = trace_instanced(s, rays[i], any != 0); });
+}
+
+// Exported two-level BVH8: hits (unrefined) and visit counts.
+void oracle_bvh8_two_level_raycast(const uint8_t* nodes, uint64_t node_count, const float* tris, const uint32_t* refs,
+                                   const uint8_t* inst, const RayRec* rays, uint64_t n, int any, int threads,
+                                   HitRec* hits, uint64_t* visited, uint64_t* tested) {
+    const Bvh8View b{nodes, node_count, tris};
+    std::atomic<uint64_t> nv{0}, nt{0};
+    parallel_for(n, threads, [&](uint64_t i) {
+        uint64_t v = 0, t = 0;
+        const BestHit<float> h = trace_bvh8_two_level(b, refs, inst, rays[i], any != 0, v, t);
+        hits[i] = HitRec{h.prim, h.t, h.u, h.v};
+        nv += v;
+        nt += t;
+    });
+    *visited += nv.load();
+    *tested += nt.load();
+}
 
 // Casts rays through an exported BVH8 (float mode, unrefined t/u/v); adds the node visits and triangle
 // tests to *visited and *tested.

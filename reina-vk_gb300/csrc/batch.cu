@@ -91,7 +91,7 @@ __global__ void __launch_bounds__(kBlock) kb_init(BatchLaunch B, const JobGpu* _
     }
 }
 
-template <int BLOCK, int SS>
+template <int BLOCK, int SS, bool TWO>
 __global__ void __launch_bounds__(BLOCK) kb_extend(BatchLaunch B, const JobGpu* __restrict__ jobs, int cur) {
     __shared__ uint2 stack[SS * BLOCK];
     const PathState& ps = B.bp.ps;
@@ -109,7 +109,7 @@ __global__ void __launch_bounds__(BLOCK) kb_extend(BatchLaunch B, const JobGpu* 
             Hit h;
             TraceCounters c{0u, 0u};
             uint32_t e = 0;
-            if (s.node_count) e = traverse<false, false, true, SS>(s.nodes, s.tris, r, stack + threadIdx.x, BLOCK, h, c);
+            if (s.node_count) e = trace_scene<false, false, true, SS, TWO>(s, r, stack + threadIdx.x, BLOCK, h, c);
             else h.prim = kMiss;
             if (e) atomicOr(ps.counters + kCntError, e);
             ps.hprim[p] = h.prim;
@@ -219,7 +219,7 @@ __global__ void __launch_bounds__(kBlock) kb_shade_miss(BatchLaunch B, const Job
     }
 }
 
-template <int BLOCK, int SS>
+template <int BLOCK, int SS, bool TWO>
 __global__ void __launch_bounds__(BLOCK) kb_shadow(BatchLaunch B, const JobGpu* __restrict__ jobs) {
     __shared__ uint2 stack[SS * BLOCK];
     const PathState& ps = B.bp.ps;
@@ -235,7 +235,7 @@ __global__ void __launch_bounds__(BLOCK) kb_shadow(BatchLaunch B, const JobGpu* 
             Hit h;
             TraceCounters c{0u, 0u};
             uint32_t e = 0;
-            if (s.node_count) e = traverse<true, false, false, SS>(s.nodes, s.tris, r, stack + threadIdx.x, BLOCK, h, c);
+            if (s.node_count) e = trace_scene<true, false, false, SS, TWO>(s, r, stack + threadIdx.x, BLOCK, h, c);
             else h.prim = kMiss;
             if (e) atomicOr(ps.counters + kCntError, e);
             if (h.prim == kMiss) store_rad(ps, p, load_rad(ps, p) + V3{ps.s_cr[i], ps.s_cg[i], ps.s_cb[i]});
@@ -324,9 +324,11 @@ BatchEngine::BatchEngine(int device, int sm_count, uint32_t wave_capacity, bool 
     desc_.alloc(desc_bytes_);
     check_cuda(cudaMallocHost(&host_desc_, desc_bytes_), "cudaMallocHost");
     with_trace_variant(trace_, [&](auto B, auto S) {
-        blocks_ext_ = resident_grid((const void*)kb_extend<B.value, S.value>, B.value, sm_count);
-        blocks_sh_ = resident_grid((const void*)kb_shadow<B.value, S.value>, B.value, sm_count);
+        blocks_ext_ = resident_grid((const void*)kb_extend<B.value, S.value, false>, B.value, sm_count);
+        blocks_sh_ = resident_grid((const void*)kb_shadow<B.value, S.value, false>, B.value, sm_count);
     });
+    blocks_ext_two_ = resident_grid((const void*)kb_extend<kTraceBlock, kDefaultTraceStack, true>, kTraceBlock, sm_count);
+    blocks_sh_two_ = resident_grid((const void*)kb_shadow<kTraceBlock, kDefaultTraceStack, true>, kTraceBlock, sm_count);
     blocks_shade_[1] = occupancy((const void*)kb_shade<1>, sm_count);
     blocks_shade_[2] = occupancy((const void*)kb_shade<2>, sm_count);
     blocks_shade_[3] = occupancy((const void*)kb_shade<3>, sm_count);
@@ -374,7 +376,7 @@ static JobGpu job_record(const BatchJob& j) {
     return g;
 }
 
-void BatchEngine::launch_wave(const WaveHeader& h, bool any_nee, cudaStream_t st) {
+void BatchEngine::launch_wave(const WaveHeader& h, bool any_nee, bool two, cudaStream_t st) {
     uint8_t* d = desc_.as<uint8_t>();
     BatchLaunch B;
     B.bp = layout_batch(paths_.as<uint32_t>(), capacity_);
@@ -391,17 +393,22 @@ void BatchEngine::launch_wave(const WaveHeader& h, bool any_nee, cudaStream_t st
         for (uint32_t seg = 0; seg < h.max_bounces; ++seg) {
             check_cuda(cudaMemsetAsync(cnt + kCntActive + (cur ^ 1), 0, sizeof(uint32_t), s), "cudaMemsetAsync");
             check_cuda(cudaMemsetAsync(cnt + kCntQueue, 0, 6 * sizeof(uint32_t), s), "cudaMemsetAsync");
-            with_trace_variant(trace_, [&](auto BS, auto SS) {
-                kb_extend<BS.value, SS.value><<<blocks_ext_, BS.value, 0, s>>>(B, B.jobs, cur);
-            });
+            if (two)   // a two-level scene in the wave: the default variant, both traversals
+                kb_extend<kTraceBlock, kDefaultTraceStack, true><<<blocks_ext_two_, kTraceBlock, 0, s>>>(B, B.jobs, cur);
+            else
+                with_trace_variant(trace_, [&](auto BS, auto SS) {
+                    kb_extend<BS.value, SS.value, false><<<blocks_ext_, BS.value, 0, s>>>(B, B.jobs, cur);
+                });
             kb_shade_miss<<<simple, kBlock, 0, s>>>(B, B.jobs);
             kb_shade<1><<<blocks_shade_[1], kBlock, 0, s>>>(B, B.jobs, cur);
             kb_shade<2><<<blocks_shade_[2], kBlock, 0, s>>>(B, B.jobs, cur);
             kb_shade<3><<<blocks_shade_[3], kBlock, 0, s>>>(B, B.jobs, cur);
             kb_shade<4><<<blocks_shade_[4], kBlock, 0, s>>>(B, B.jobs, cur);
-            if (any_nee)
+            if (any_nee && two)
+                kb_shadow<kTraceBlock, kDefaultTraceStack, true><<<blocks_sh_two_, kTraceBlock, 0, s>>>(B, B.jobs);
+            else if (any_nee)
                 with_trace_variant(trace_, [&](auto BS, auto SS) {
-                    kb_shadow<BS.value, SS.value><<<blocks_sh_, BS.value, 0, s>>>(B, B.jobs);
+                    kb_shadow<BS.value, SS.value, false><<<blocks_sh_, BS.value, 0, s>>>(B, B.jobs);
                 });
             cur ^= 1;
         }
@@ -414,7 +421,7 @@ void BatchEngine::launch_wave(const WaveHeader& h, bool any_nee, cudaStream_t st
     }
     GraphSlot* slot = nullptr;
     for (auto& g : graphs_)
-        if (g.bounces == h.max_bounces && g.nee == any_nee) slot = &g;
+        if (g.bounces == h.max_bounces && g.nee == any_nee && g.two == two) slot = &g;
     if (!slot) {
         cudaStream_t cap;
         check_cuda(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking), "cudaStreamCreate");
@@ -426,6 +433,7 @@ void BatchEngine::launch_wave(const WaveHeader& h, bool any_nee, cudaStream_t st
         GraphSlot g;
         g.bounces = h.max_bounces;
         g.nee = any_nee;
+        g.two = two;
         check_cuda(cudaGraphInstantiate(&g.exec, graph, 0), "cudaGraphInstantiate");
         cudaGraphDestroy(graph);
         graphs_.push_back(g);
@@ -463,7 +471,7 @@ uint64_t BatchEngine::run_wave(const std::vector<BatchJob*>& jobs, cudaStream_t 
     WaveSeg* segs = reinterpret_cast<WaveSeg*>(h + sizeof(WaveHeader));
     JobGpu* jt = reinterpret_cast<JobGpu*>(h + sizeof(WaveHeader) + kMaxWaveSegments * sizeof(WaveSeg));
     uint32_t nseg = 0, njobs = 0, wave_pos = 0, bounces = 0;
-    bool any_nee = false;
+    bool any_nee = false, two = false;
     for (size_t a = 0; a < active.size(); ++a) {
         if (take[a] == 0) continue;
         BatchJob* j = active[a];
@@ -472,6 +480,7 @@ uint64_t BatchEngine::run_wave(const std::vector<BatchJob*>& jobs, cudaStream_t 
         jt[ji] = job_record(*j);
         bounces = std::max(bounces, j->pc.maxBounces);
         any_nee = any_nee || j->opt.mode == kModeNeeMis;
+        two = two || j->scene.inst_trav != nullptr;
         uint64_t m = take[a];
         while (m > 0) {
             const uint64_t sample = j->cursor / px, pixel = j->cursor % px;
@@ -495,7 +504,7 @@ uint64_t BatchEngine::run_wave(const std::vector<BatchJob*>& jobs, cudaStream_t 
     check_cuda(cudaMemcpyAsync(d, h, sizeof(WaveHeader) + nseg * sizeof(WaveSeg), cudaMemcpyHostToDevice, st), "H2D wave");
     const size_t job_off = sizeof(WaveHeader) + kMaxWaveSegments * sizeof(WaveSeg);
     check_cuda(cudaMemcpyAsync(d + job_off, h + job_off, njobs * sizeof(JobGpu), cudaMemcpyHostToDevice, st), "H2D jobs");
-    launch_wave(*hdr, any_nee, st);
+    launch_wave(*hdr, any_nee, two, st);
     // resolve the jobs this wave completed
     for (size_t a = 0; a < active.size(); ++a) {
         BatchJob* j = active[a];

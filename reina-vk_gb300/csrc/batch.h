@@ -86,7 +86,7 @@ public:
     uint32_t waves() const { return waves_; }
 
 private:
-    void launch_wave(const WaveHeader& h, bool any_nee, cudaStream_t st);
+    void launch_wave(const WaveHeader& h, bool any_nee, bool two, cudaStream_t st);
     int device_, sm_count_;
     uint32_t capacity_;
     bool use_graphs_;
@@ -98,12 +98,14 @@ private:
     struct GraphSlot {
         uint32_t bounces = 0;
         bool nee = false;
+        bool two = false;   // the wave holds a two-level scene
         cudaGraphExec_t exec = nullptr;
     };
     std::vector<GraphSlot> graphs_;
     uint64_t rays_ = 0, shadow_rays_ = 0;
     uint32_t waves_ = 0;
     int blocks_ext_ = 0, blocks_shade_[5] = {0, 0, 0, 0, 0}, blocks_sh_ = 0, blocks_simple_ = 0;
+    int blocks_ext_two_ = 0, blocks_sh_two_ = 0;
 };
 
 }  // namespace rt

@@ -185,6 +185,7 @@ struct WideBuilder {
     Bvh8& out;
     double delta;   // conservative dilation of every quantized child box, in world units
     int collapse = kCollapseSahDp;
+    std::vector<uint32_t>* refs = nullptr;   // box mode: leaf entries are box indices appended here
 
     // Dynamic-programme tables per binary node: cost[i] = cost of the subtree as at most i + 1 wide
     // children; how[i] = 0 one leaf child, 1 one wide node, 2 split between the two binary children with
@@ -383,7 +384,7 @@ struct WideBuilder {
         // appended to the triangle array.
         uint32_t inner_bnodes[8];
         int n_inner = 0;
-        node.tri_base = (uint32_t)out.tris.size();
+        node.tri_base = (uint32_t)(refs ? refs->size() : out.tris.size());
         uint32_t tri_off = 0;
         uint8_t imask = 0;
         for (int s = 0; s < 8; ++s) {
@@ -414,6 +415,10 @@ struct WideBuilder {
                 node.meta[s] = (uint8_t)((unary << 5) | tri_off);
                 for (uint32_t j = 0; j < cnt; ++j) {
                     uint32_t prim = bb.idx[first + j];
+                    if (refs) {
+                        refs->push_back(prim);
+                        continue;
+                    }
                     const float* v = bb.verts + 9ull * prim;
                     TriRecord r;
                     r.v0x = v[0]; r.v0y = v[1]; r.v0z = v[2]; r.prim = prim;
@@ -435,33 +440,22 @@ struct WideBuilder {
 
 }  // namespace
 
-Bvh8 build_bvh8(const float* verts, uint64_t tri_count, const BvhBuildOptions& opt) {
+// Binary SAH build over primitive boxes, collapse and quantization; leaves become triangle records
+// (verts) or entries of `refs` (box mode).
+static Bvh8 build_core(std::vector<Box>&& boxes, double mag, const float* verts, std::vector<uint32_t>* refs,
+                       const BvhBuildOptions& opt) {
     auto t0 = std::chrono::steady_clock::now();
     Bvh8 out;
-    if (tri_count == 0) return out;
-    if (tri_count >= 0x7FFFFFFFull) throw std::runtime_error("BVH build: too many triangles");
-    const uint32_t n = (uint32_t)tri_count;
-
+    const uint32_t n = (uint32_t)boxes.size();
+    if (n == 0) return out;
     BinaryBuilder bb;
     bb.verts = verts;
     bb.bins = std::max(4, std::min(256, opt.sah_bins));
-    bb.prim_box.resize(n);
+    bb.prim_box = std::move(boxes);
     bb.centroid.resize(3ull * n);
     bb.idx.resize(n);
-    double mag = 0.0;
     for (uint32_t i = 0; i < n; ++i) {
-        const float* v = verts + 9ull * i;
-        Box b = empty_box();
-        for (int j = 0; j < 3; ++j) {
-            for (int k = 0; k < 3; ++k) {
-                float c = v[3 * j + k];
-                if (!std::isfinite(c)) throw std::runtime_error("BVH build: non-finite vertex coordinate");
-                b.lo[k] = std::min(b.lo[k], c);
-                b.hi[k] = std::max(b.hi[k], c);
-                mag = std::max(mag, (double)std::fabs(c));
-            }
-        }
-        bb.prim_box[i] = b;
+        const Box& b = bb.prim_box[i];
         for (int k = 0; k < 3; ++k) bb.centroid[3ull * i + k] = 0.5f * (b.lo[k] + b.hi[k]);
         bb.idx[i] = i;
     }
@@ -475,13 +469,55 @@ Bvh8 build_bvh8(const float* verts, uint64_t tri_count, const BvhBuildOptions& o
     // rounding of the slab test for ray origins within ~20x that magnitude.
     double delta = std::ldexp(std::max(mag, 1e-20), -18);
     out.nodes.resize(1);
-    out.tris.reserve(n);
-    WideBuilder wb{bb, out, delta, opt.collapse};
+    if (!refs) out.tris.reserve(n);
+    WideBuilder wb{bb, out, delta, opt.collapse, refs};
     wb.prepare();
     wb.emit(0, 0, 1);
     if (out.depth > kMaxBvhDepth) throw std::runtime_error("BVH build: tree deeper than the traversal stack");
     out.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     return out;
+}
+
+Bvh8 build_bvh8(const float* verts, uint64_t tri_count, const BvhBuildOptions& opt) {
+    if (tri_count == 0) return Bvh8{};
+    if (tri_count >= 0x7FFFFFFFull) throw std::runtime_error("BVH build: too many triangles");
+    const uint32_t n = (uint32_t)tri_count;
+    std::vector<Box> boxes(n);
+    double mag = 0.0;
+    for (uint32_t i = 0; i < n; ++i) {
+        const float* v = verts + 9ull * i;
+        Box b = empty_box();
+        for (int j = 0; j < 3; ++j) {
+            for (int k = 0; k < 3; ++k) {
+                float c = v[3 * j + k];
+                if (!std::isfinite(c)) throw std::runtime_error("BVH build: non-finite vertex coordinate");
+                b.lo[k] = std::min(b.lo[k], c);
+                b.hi[k] = std::max(b.hi[k], c);
+                mag = std::max(mag, (double)std::fabs(c));
+            }
+        }
+        boxes[i] = b;
+    }
+    return build_core(std::move(boxes), mag, verts, nullptr, opt);
+}
+
+Bvh8 build_bvh8_boxes(const float* boxes6, uint64_t box_count, std::vector<uint32_t>& refs, const BvhBuildOptions& opt) {
+    refs.clear();
+    if (box_count == 0) return Bvh8{};
+    if (box_count >= 0x7FFFFFFFull) throw std::runtime_error("BVH build: too many boxes");
+    const uint32_t n = (uint32_t)box_count;
+    std::vector<Box> boxes(n);
+    double mag = 0.0;
+    for (uint32_t i = 0; i < n; ++i) {
+        for (int k = 0; k < 3; ++k) {
+            const float lo = boxes6[6ull * i + k], hi = boxes6[6ull * i + 3 + k];
+            if (!std::isfinite(lo) || !std::isfinite(hi) || lo > hi) throw std::runtime_error("BVH build: invalid box");
+            boxes[i].lo[k] = lo;
+            boxes[i].hi[k] = hi;
+            mag = std::max(mag, std::max((double)std::fabs(lo), (double)std::fabs(hi)));
+        }
+    }
+    return build_core(std::move(boxes), mag, nullptr, &refs, opt);
 }
 
 }  // namespace rt

@@ -36,6 +36,13 @@ struct BvhBuildOptions {
 // `verts` holds 9 floats per triangle (v0, v1, v2 in world space); triangle i gets id i.
 Bvh8 build_bvh8(const float* verts, uint64_t tri_count, const BvhBuildOptions& opt = BvhBuildOptions());
 
+// BVH8 over axis-aligned boxes (6 floats each: lo x, y, z, hi x, y, z), for the top level of a two-level
+// scene: leaf children reference boxes instead of triangles — their entries (box indices) are appended
+// to `refs`, and a leaf child's offset indexes refs from the node's tri_base.  The result has no
+// triangle records.
+Bvh8 build_bvh8_boxes(const float* boxes6, uint64_t box_count, std::vector<uint32_t>& refs,
+                      const BvhBuildOptions& opt = BvhBuildOptions());
+
 // Maximum BVH8 depth the traversal kernels accept (their stack holds one entry per level).
 constexpr uint32_t kMaxBvhDepth = 64;
 // Largest quantization exponent of a node (scale 2^e): the traversal forms 2^(e+15) in single precision.

@@ -333,6 +333,15 @@ int reina_scene_get_stats(const reina_scene* scene, reina_scene_stats* out) {
         out->leaf_triangles_max = rt::kMaxLeafTris;
         out->build_seconds = s.bvh().seconds;
         s.bounds(out->bounds_min, out->bounds_max);
+        out->two_level = s.two_level() ? 1u : 0u;
+        out->blas_count = s.blas_count();
+    });
+}
+
+int reina_scene_set_accel(reina_scene* scene, int mode) {
+    return guard([&] {
+        need(scene && scene->s, "NULL argument");
+        scene->s->set_accel(mode);
     });
 }
 
@@ -1140,6 +1149,19 @@ int reina_scene_define_texture_encoded(reina_scene* scene, const void* data, uin
     return guard([&] {
         need(scene && scene->s && data && out_id, "NULL argument");
         *out_id = scene->s->define_texture(rt::decode_image(static_cast<const uint8_t*>(data), (size_t)bytes));
+    });
+}
+
+int reina_scene_export_two_level(const reina_scene* scene, void* records, uint32_t* refs, uint32_t* ninst,
+                                 uint32_t* nrefs) {
+    return guard([&] {
+        const rt::Scene& s = built_scene(scene);
+        const auto& it = s.instance_records();
+        const auto& r = s.tlas_refs();
+        if (ninst) *ninst = (uint32_t)it.size();
+        if (nrefs) *nrefs = (uint32_t)r.size();
+        if (records) std::memcpy(records, it.data(), it.size() * sizeof(rt::InstanceTrav));
+        if (refs) std::memcpy(refs, r.data(), r.size() * sizeof(uint32_t));
     });
 }
 

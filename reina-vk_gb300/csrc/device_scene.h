@@ -50,6 +50,10 @@ struct DeviceScene {
     const float* cdf_instances = nullptr;     // numInstances entries
     uint32_t emissive_count = 0;
     float emissive_weight = 0.0f;             // the `allInstancesArea` field = Σ weights
+    // two-level scenes: per-instance traversal records and the top-level leaf entries (instance ids);
+    // null for a flat scene (one BVH over world-space triangles)
+    const InstanceTrav* inst_trav = nullptr;
+    const uint32_t* tlas_refs = nullptr;
     // textures (src/scene/Scene.cpp:59-80; sampled as R8G8B8A8_UNORM, src/graphics/Image.cpp:56)
     const uint32_t* tex_texels = nullptr;     // RGBA8 texels of all textures, one word each
     const uint4* tex_info = nullptr;          // per texture: first texel, width, height, 0

@@ -62,7 +62,7 @@ __global__ void __launch_bounds__(kBlock) k_init(RenderLaunch L) {
 
 // ------------------------------------------------------------------------------------------------
 // extend: closest hit + classification.  Grid form: each warp takes 32 consecutive queue entries.
-template <int BLOCK, int SS>
+template <int BLOCK, int SS, bool TWO>
 __global__ void __launch_bounds__(BLOCK) k_extend_grid(RenderLaunch L, int cur) {
     __shared__ uint2 stack[SS * BLOCK];
     const PathState& ps = L.ps;
@@ -80,7 +80,7 @@ __global__ void __launch_bounds__(BLOCK) k_extend_grid(RenderLaunch L, int cur) 
             TraceCounters c{0u, 0u};
             uint32_t e = 0;
             if (L.s.node_count)
-                e = traverse<false, false, true, SS>(L.s.nodes, L.s.tris, r, stack + threadIdx.x, BLOCK, h, c);
+                e = trace_scene<false, false, true, SS, TWO>(L.s, r, stack + threadIdx.x, BLOCK, h, c);
             else h.prim = kMiss;
             if (e) atomicOr(ps.counters + kCntError, e);
             ps.hprim[p] = h.prim;
@@ -225,7 +225,7 @@ __global__ void __launch_bounds__(kBlock) k_shade_miss(RenderLaunch L) {
 }
 
 // nee.h.glsl:126-144: any hit in [0, dist - 0.001]; unoccluded contributions are added.  Grid form.
-template <int BLOCK, int SS>
+template <int BLOCK, int SS, bool TWO>
 __global__ void __launch_bounds__(BLOCK) k_shadow_grid(RenderLaunch L) {
     __shared__ uint2 stack[SS * BLOCK];
     const PathState& ps = L.ps;
@@ -240,7 +240,7 @@ __global__ void __launch_bounds__(BLOCK) k_shadow_grid(RenderLaunch L) {
             TraceCounters c{0u, 0u};
             uint32_t e = 0;
             if (L.s.node_count)
-                e = traverse<true, false, false, SS>(L.s.nodes, L.s.tris, r, stack + threadIdx.x, BLOCK, h, c);
+                e = trace_scene<true, false, false, SS, TWO>(L.s, r, stack + threadIdx.x, BLOCK, h, c);
             else h.prim = kMiss;
             if (e) atomicOr(ps.counters + kCntError, e);
             if (h.prim == kMiss) {
@@ -316,6 +316,7 @@ __global__ void __launch_bounds__(kBlock) k_resolve(RenderLaunch L) {
 // Plain form: the reference's megakernel structure (raytrace.rgen.glsl:250-285) — one thread per pixel
 // runs every sample and segment, with the closest-hit shading and NEE shadow rays inline.  Same device
 // functions as the wavefront kernels; used as the single-kernel baseline the wavefront is compared with.
+template <bool TWO>
 __global__ void __launch_bounds__(kBlock) k_megakernel(RenderLaunch L) {
     __shared__ uint2 stack[kSmemStack * kBlock];
     const PathState& ps = L.ps;
@@ -344,7 +345,7 @@ __global__ void __launch_bounds__(kBlock) k_megakernel(RenderLaunch L) {
                 Hit h;
                 TraceCounters c{0u, 0u};
                 uint32_t e = 0;
-                if (L.s.node_count) e = traverse<false, false, true>(L.s.nodes, L.s.tris, r, stack + threadIdx.x, kBlock, h, c);
+                if (L.s.node_count) e = trace_scene<false, false, true, kSmemStack, TWO>(L.s, r, stack + threadIdx.x, kBlock, h, c);
                 else h.prim = kMiss;
                 if (e) atomicOr(ps.counters + kCntError, e);
                 ++n_rays;
@@ -387,7 +388,7 @@ __global__ void __launch_bounds__(kBlock) k_megakernel(RenderLaunch L) {
                                 const TraceRay sr = make_trace_ray(sh.o.x, sh.o.y, sh.o.z, sh.d.x, sh.d.y, sh.d.z, 0.0f, sh.tmax);
                                 Hit sh_hit;
                                 uint32_t e2 = 0;
-                                e2 = traverse<true, false, false>(L.s.nodes, L.s.tris, sr, stack + threadIdx.x, kBlock, sh_hit, c);
+                                e2 = trace_scene<true, false, false, kSmemStack, TWO>(L.s, sr, stack + threadIdx.x, kBlock, sh_hit, c);
                                 if (e2) atomicOr(ps.counters + kCntError, e2);
                                 ++n_shadow;
                                 if (sh_hit.prim == kMiss) rad = rad + sh.contrib;
@@ -510,14 +511,17 @@ static void launch_frame(const PathState& ps, const DeviceScene& s, const RtPush
     const int simple_blocks = (int)std::min<uint64_t>((P + kBlock - 1) / kBlock, (uint64_t)g_simple);
     uint32_t* cnt = L.ps.counters;
     check_cuda(cudaMemsetAsync(cnt, 0, kNumCounters * sizeof(uint32_t), st), "cudaMemsetAsync counters");
+    const bool two = L.s.inst_trav != nullptr;
     if (opt.megakernel) {
-        static int g_mega = 0, g_mega_sm = -1;
+        static int g_mega[2] = {0, 0}, g_mega_sm = -1;
         if (g_mega_sm != sm_count) {
-            g_mega = occupancy_blocks((const void*)k_megakernel, sm_count);
+            g_mega[0] = occupancy_blocks((const void*)k_megakernel<false>, sm_count);
+            g_mega[1] = occupancy_blocks((const void*)k_megakernel<true>, sm_count);
             g_mega_sm = sm_count;
         }
-        const int blocks = (int)std::min<uint64_t>((P + kBlock - 1) / kBlock, (uint64_t)g_mega);
-        k_megakernel<<<blocks, kBlock, 0, st>>>(L);
+        const int blocks = (int)std::min<uint64_t>((P + kBlock - 1) / kBlock, (uint64_t)g_mega[two ? 1 : 0]);
+        if (two) k_megakernel<true><<<blocks, kBlock, 0, st>>>(L);
+        else k_megakernel<false><<<blocks, kBlock, 0, st>>>(L);
     }
     for (uint32_t smp = 0; smp < (opt.megakernel ? 0u : pc.samplesPerPixel); ++smp) {
         L.sample = smp;
@@ -528,16 +532,23 @@ static void launch_frame(const PathState& ps, const DeviceScene& s, const RtPush
             check_cuda(cudaMemsetAsync(cnt + kCntActive + (cur ^ 1), 0, sizeof(uint32_t), st), "cudaMemsetAsync");
             check_cuda(cudaMemsetAsync(cnt + kCntQueue, 0, 6 * sizeof(uint32_t), st), "cudaMemsetAsync");
             check_cuda(cudaMemsetAsync(cnt + kCntFetchExtend, 0, 2 * sizeof(uint32_t), st), "cudaMemsetAsync");
-            if (opt.trace.refill > 0) {
+            if (two) {   // two-level scenes: the default traversal variant
+                static int grid = 0, grid_sm = -1;
+                if (grid_sm != sm_count) {
+                    grid = resident_grid((const void*)k_extend_grid<kTraceBlock, kDefaultTraceStack, true>, kTraceBlock, sm_count);
+                    grid_sm = sm_count;
+                }
+                k_extend_grid<kTraceBlock, kDefaultTraceStack, true><<<grid, kTraceBlock, 0, st>>>(L, cur);
+            } else if (opt.trace.refill > 0) {
                 k_extend<<<g_ext, kBlock, 0, st>>>(L, cur);
             } else {
                 with_trace_variant(opt.trace, [&](auto B, auto S) {
                     static int grid = 0, grid_sm = -1;
                     if (grid_sm != sm_count) {
-                        grid = resident_grid((const void*)k_extend_grid<B.value, S.value>, B.value, sm_count);
+                        grid = resident_grid((const void*)k_extend_grid<B.value, S.value, false>, B.value, sm_count);
                         grid_sm = sm_count;
                     }
-                    k_extend_grid<B.value, S.value><<<grid, B.value, 0, st>>>(L, cur);
+                    k_extend_grid<B.value, S.value, false><<<grid, B.value, 0, st>>>(L, cur);
                 });
             }
             k_shade_miss<<<simple_blocks, kBlock, 0, st>>>(L);
@@ -546,16 +557,23 @@ static void launch_frame(const PathState& ps, const DeviceScene& s, const RtPush
             k_shade<3><<<g_shade[3], kBlock, 0, st>>>(L, cur);
             k_shade<4><<<g_shade[4], kBlock, 0, st>>>(L, cur);
             if (opt.mode == kModeNeeMis) {
-                if (opt.trace.refill > 0) {
+                if (two) {
+                    static int grid = 0, grid_sm = -1;
+                    if (grid_sm != sm_count) {
+                        grid = resident_grid((const void*)k_shadow_grid<kTraceBlock, kDefaultTraceStack, true>, kTraceBlock, sm_count);
+                        grid_sm = sm_count;
+                    }
+                    k_shadow_grid<kTraceBlock, kDefaultTraceStack, true><<<grid, kTraceBlock, 0, st>>>(L);
+                } else if (opt.trace.refill > 0) {
                     k_shadow<<<g_sh, kBlock, 0, st>>>(L);
                 } else {
                     with_trace_variant(opt.trace, [&](auto B, auto S) {
                         static int grid = 0, grid_sm = -1;
                         if (grid_sm != sm_count) {
-                            grid = resident_grid((const void*)k_shadow_grid<B.value, S.value>, B.value, sm_count);
+                            grid = resident_grid((const void*)k_shadow_grid<B.value, S.value, false>, B.value, sm_count);
                             grid_sm = sm_count;
                         }
-                        k_shadow_grid<B.value, S.value><<<grid, B.value, 0, st>>>(L);
+                        k_shadow_grid<B.value, S.value, false><<<grid, B.value, 0, st>>>(L);
                     });
                 }
             }

@@ -50,7 +50,8 @@ struct alignas(16) Bvh8Node {
 };
 static_assert(sizeof(Bvh8Node) == 80, "BVH8 node must be 80 bytes");
 
-// Traversal triangle record, 48 bytes: world-space vertices; v0.w holds the global triangle id bits.
+// Traversal triangle record, 48 bytes: world-space vertices and the global triangle id in v0.w (in a
+// two-level scene: the model's object-space vertices and the triangle's index within the model).
 struct alignas(16) TriRecord {
     float v0x, v0y, v0z;
     uint32_t prim;
@@ -58,6 +59,18 @@ struct alignas(16) TriRecord {
     float v2x, v2y, v2z, pad2;
 };
 static_assert(sizeof(TriRecord) == 48, "triangle record must be 48 bytes");
+
+// Instance record of a two-level scene (TLAS leaves reference these): the world-to-object transform
+// that carries a ray into the instance's model space, the node index of the model's bottom-level BVH
+// root, and the global triangle id of the model's triangle 0 in this instance (global id = first_prim +
+// the triangle record's local id).
+struct alignas(16) InstanceTrav {
+    float inv[12];          // row-major 3x4: object_r = sum_c inv[r*4+c] * world_c + inv[r*4+3]
+    uint32_t blas_root;
+    uint32_t first_prim;
+    uint32_t pad0, pad1;
+};
+static_assert(sizeof(InstanceTrav) == 64, "instance record must be 64 bytes");
 
 struct alignas(16) Ray {
     float ox, oy, oz, tmin;

@@ -2,6 +2,7 @@
 // the upload of the assembled buffers and the BVH8 to the device.
 #include "scene.h"
 
+#include <array>
 #include <cmath>
 #include <cstring>
 #include <limits>
@@ -293,6 +294,190 @@ static void normal_matrix(const float T[16], float out[9]) {
         for (int c = 0; c < 3; ++c) out[r * 3 + c] = det != 0.0f ? cof[r][c] / det : 0.0f;
 }
 
+void Scene::set_accel(int mode) {
+    if (built_) fail(REINA_ERR_STATE, "the acceleration structure is chosen before the build");
+    if (mode < REINA_ACCEL_AUTO || mode > REINA_ACCEL_TWO_LEVEL) fail(REINA_ERR_INVALID, "unknown acceleration structure mode");
+    accel_mode_ = mode;
+}
+
+// Inverse of an affine transform (column-major 4x4) as a row-major 3x4 world-to-object matrix: the
+// 3x3 inverse by cofactors over the determinant and the translation -inverse * t, in double, each entry
+// rounded to float.  Returns false for a singular (or non-finite) transform.
+bool affine_inverse(const float T[16], float inv[12]) {
+    auto M = [&](int r, int c) { return (double)T[c * 4 + r]; };
+    double cof[3][3];
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) {
+            const int r1 = (r + 1) % 3, r2 = (r + 2) % 3, c1 = (c + 1) % 3, c2 = (c + 2) % 3;
+            cof[r][c] = M(r1, c1) * M(r2, c2) - M(r1, c2) * M(r2, c1);
+        }
+    const double det = M(0, 0) * cof[0][0] + M(0, 1) * cof[0][1] + M(0, 2) * cof[0][2];
+    if (!(std::fabs(det) > 0.0) || !std::isfinite(det)) return false;
+    double m[3][3];
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) m[r][c] = cof[c][r] / det;   // inverse = adjugate / det
+    for (int r = 0; r < 3; ++r) {
+        const double t = -(m[r][0] * M(0, 3) + m[r][1] * M(1, 3) + m[r][2] * M(2, 3));
+        for (int c = 0; c < 3; ++c) inv[r * 4 + c] = (float)m[r][c];
+        inv[r * 4 + 3] = (float)t;
+        for (int c = 0; c < 4; ++c)
+            if (!std::isfinite(inv[r * 4 + c])) return false;
+    }
+    return true;
+}
+
+// Two levels when asked for, or (automatic) when instancing repeats models enough that the flattened
+// triangle records would take at least twice the memory of one copy per model, and every instance
+// transform is invertible.
+bool Scene::use_two_level() const {
+    if (accel_mode_ == REINA_ACCEL_FLAT || instances_.empty()) return false;
+    uint64_t unique = 0;
+    std::vector<uint8_t> used(models_.size(), 0);
+    for (const InstanceRecord& inst : instances_)
+        if (!used[inst.object]) {
+            used[inst.object] = 1;
+            unique += ranges_[inst.object].index_count;
+        }
+    bool invertible = true;
+    float inv[12];
+    for (const InstanceRecord& inst : instances_) invertible = invertible && affine_inverse(inst.transform, inv);
+    if (accel_mode_ == REINA_ACCEL_TWO_LEVEL) {
+        if (!invertible) fail(REINA_ERR_INVALID, "a two-level scene needs invertible instance transforms");
+        return true;
+    }
+    return invertible && tri_total_ >= 2 * unique;
+}
+
+// One BVH over all instances' world-space triangles.
+void Scene::build_flat() {
+    std::vector<float> world(9 * tri_total_);
+    for (int k = 0; k < 3; ++k) { bounds_lo_[k] = INFINITY; bounds_hi_[k] = -INFINITY; }
+    for (size_t ii = 0; ii < instances_.size(); ++ii) {
+        const InstanceRecord& inst = instances_[ii];
+        const ModelData& md = models_[inst.object];
+        const float* T = inst.transform;
+        const uint32_t ntri = ranges_[inst.object].index_count;
+        for (uint32_t t = 0; t < ntri; ++t) {
+            const uint64_t g = inst.first_prim + t;
+            for (int j = 0; j < 3; ++j) {
+                const uint32_t vi = md.indices[3 * t + j];
+                const float x = md.vertices[4 * vi + 0], y = md.vertices[4 * vi + 1], z = md.vertices[4 * vi + 2];
+                for (int r = 0; r < 3; ++r) {
+                    float s = T[0 * 4 + r] * x;
+                    s = s + T[1 * 4 + r] * y;
+                    s = s + T[2 * 4 + r] * z;
+                    s = s + T[3 * 4 + r];
+                    world[9 * g + 3 * j + r] = s;
+                    bounds_lo_[r] = std::min(bounds_lo_[r], s);
+                    bounds_hi_[r] = std::max(bounds_hi_[r], s);
+                }
+            }
+        }
+    }
+    bvh_ = build_bvh8(world.data(), tri_total_);
+    inst_trav_.clear();
+    tlas_refs_.clear();
+    blas_count_ = 0;
+}
+
+// The reference's structure (src/scene/Scene.cpp:93-116; BLAS per model, src/graphics/Blas.cpp; TLAS
+// over instances, src/tools/vktools.cpp:460-596): one bottom-level BVH8 per instanced model over its
+// object-space triangles (record ids = triangle index within the model), one top-level BVH8 over the
+// instances' world-space boxes, all nodes in one array (top-level root = node 0, each model's nodes
+// after it with their child and triangle bases offset) and all triangle records in one array.
+void Scene::build_two_level() {
+    const size_t ninst = instances_.size();
+    std::vector<int64_t> blas_of(models_.size(), -1);
+    std::vector<std::array<float, 6>> model_box(models_.size());
+    // object-space boxes of the used models
+    for (const InstanceRecord& inst : instances_) {
+        if (blas_of[inst.object] == -2) continue;
+        blas_of[inst.object] = -2;
+        const ModelData& md = models_[inst.object];
+        std::array<float, 6> b = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
+        for (uint32_t vi : md.indices)
+            for (int k = 0; k < 3; ++k) {
+                b[k] = std::min(b[k], md.vertices[4 * vi + k]);
+                b[3 + k] = std::max(b[3 + k], md.vertices[4 * vi + k]);
+            }
+        model_box[inst.object] = b;
+    }
+    // world boxes of the instances: the 8 transformed corners of the model box, in double, rounded outward
+    std::vector<float> boxes(6 * ninst);
+    for (int k = 0; k < 3; ++k) { bounds_lo_[k] = INFINITY; bounds_hi_[k] = -INFINITY; }
+    for (size_t ii = 0; ii < ninst; ++ii) {
+        const InstanceRecord& inst = instances_[ii];
+        const std::array<float, 6>& mb = model_box[inst.object];
+        const float* T = inst.transform;
+        double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+        const bool empty = ranges_[inst.object].index_count == 0;
+        for (int c = 0; c < 8 && !empty; ++c) {
+            const double p[3] = {mb[(c & 1) ? 3 : 0], mb[(c & 2) ? 4 : 1], mb[(c & 4) ? 5 : 2]};
+            for (int r = 0; r < 3; ++r) {
+                const double w = T[0 * 4 + r] * p[0] + T[1 * 4 + r] * p[1] + T[2 * 4 + r] * p[2] + T[3 * 4 + r];
+                lo[r] = std::min(lo[r], w);
+                hi[r] = std::max(hi[r], w);
+            }
+        }
+        for (int r = 0; r < 3; ++r) {
+            if (empty) { lo[r] = hi[r] = T[3 * 4 + r]; }
+            float fl = (float)lo[r], fh = (float)hi[r];
+            if ((double)fl > lo[r]) fl = std::nextafter(fl, -INFINITY);
+            if ((double)fh < hi[r]) fh = std::nextafter(fh, INFINITY);
+            boxes[6 * ii + r] = fl;
+            boxes[6 * ii + 3 + r] = fh;
+            bounds_lo_[r] = std::min(bounds_lo_[r], fl);
+            bounds_hi_[r] = std::max(bounds_hi_[r], fh);
+        }
+    }
+    Bvh8 tlas = build_bvh8_boxes(boxes.data(), ninst, tlas_refs_);
+    Bvh8 out;
+    out.nodes = std::move(tlas.nodes);
+    out.binary_nodes = tlas.binary_nodes;
+    double seconds = tlas.seconds;
+    uint32_t blas_depth = 0;
+    blas_count_ = 0;
+    for (size_t o = 0; o < models_.size(); ++o) {
+        if (blas_of[o] != -2) continue;
+        const ModelData& md = models_[o];
+        const size_t ntri = md.indices.size() / 3;
+        std::vector<float> tris(9 * ntri);
+        for (size_t t = 0; t < ntri; ++t)
+            for (int j = 0; j < 3; ++j)
+                for (int k = 0; k < 3; ++k) tris[9 * t + 3 * j + k] = md.vertices[4 * md.indices[3 * t + j] + k];
+        Bvh8 b = build_bvh8(tris.data(), ntri);
+        const uint32_t node_base = (uint32_t)out.nodes.size(), tri_base = (uint32_t)out.tris.size();
+        if (b.nodes.empty()) {   // a model without triangles: no bottom level (its instances have empty boxes)
+            blas_of[o] = -1;
+            continue;
+        }
+        for (Bvh8Node& n : b.nodes) {
+            n.child_base += node_base;
+            n.tri_base += tri_base;
+        }
+        out.nodes.insert(out.nodes.end(), b.nodes.begin(), b.nodes.end());
+        out.tris.insert(out.tris.end(), b.tris.begin(), b.tris.end());
+        blas_of[o] = node_base;
+        blas_depth = std::max(blas_depth, b.depth);
+        out.binary_nodes += b.binary_nodes;
+        seconds += b.seconds;
+        ++blas_count_;
+    }
+    out.depth = tlas.depth + blas_depth;
+    // the traversal stack holds both levels plus one marker between them
+    if (out.depth + 1 > kMaxBvhDepth) fail(REINA_ERR_INVALID, "two-level BVH deeper than the traversal stack");
+    out.seconds = seconds;
+    bvh_ = std::move(out);
+    inst_trav_.assign(ninst, InstanceTrav{});
+    for (size_t ii = 0; ii < ninst; ++ii) {
+        const InstanceRecord& inst = instances_[ii];
+        InstanceTrav& it = inst_trav_[ii];
+        affine_inverse(inst.transform, it.inv);
+        it.blas_root = blas_of[inst.object] >= 0 ? (uint32_t)blas_of[inst.object] : 0xFFFFFFFFu;
+        it.first_prim = inst.first_prim;
+    }
+}
+
 void Scene::build(bool require_emissive) {
     if (built_) fail(REINA_ERR_STATE, "Cannot call build more than once");
     const bool host_only = device_ < 0;
@@ -325,43 +510,26 @@ void Scene::build(bool require_emissive) {
     pack_emissives();
     if (cdf_triangles_.empty() && require_emissive) fail(REINA_ERR_NO_EMISSIVE, "Scene must have at least one emissive object");
 
-    // Flatten instances into world-space traversal triangles (one BVH over all instances).
     tri_total_ = 0;
     for (InstanceRecord& inst : instances_) {
         inst.first_prim = (uint32_t)tri_total_;
         tri_total_ += ranges_[inst.object].index_count;
     }
     if (tri_total_ >= 0x7FFFFFFFull) fail(REINA_ERR_INVALID, "scene has too many triangles");
-    std::vector<float> world(9 * tri_total_);
     prim_instance_.resize(tri_total_);
     prim_props_.resize(tri_total_);
-    for (int k = 0; k < 3; ++k) { bounds_lo_[k] = INFINITY; bounds_hi_[k] = -INFINITY; }
     for (size_t ii = 0; ii < instances_.size(); ++ii) {
         const InstanceRecord& inst = instances_[ii];
-        const ModelData& md = models_[inst.object];
-        const float* T = inst.transform;
         const uint32_t ntri = ranges_[inst.object].index_count;
         for (uint32_t t = 0; t < ntri; ++t) {
-            const uint64_t g = inst.first_prim + t;
-            prim_instance_[g] = (uint32_t)ii;
-            prim_props_[g] = inst.per_face ? inst.face_props[t] : inst.props_id;
-            for (int j = 0; j < 3; ++j) {
-                const uint32_t vi = md.indices[3 * t + j];
-                const float x = md.vertices[4 * vi + 0], y = md.vertices[4 * vi + 1], z = md.vertices[4 * vi + 2];
-                for (int r = 0; r < 3; ++r) {
-                    float s = T[0 * 4 + r] * x;
-                    s = s + T[1 * 4 + r] * y;
-                    s = s + T[2 * 4 + r] * z;
-                    s = s + T[3 * 4 + r];
-                    world[9 * g + 3 * j + r] = s;
-                    bounds_lo_[r] = std::min(bounds_lo_[r], s);
-                    bounds_hi_[r] = std::max(bounds_hi_[r], s);
-                }
-            }
+            prim_instance_[inst.first_prim + t] = (uint32_t)ii;
+            prim_props_[inst.first_prim + t] = inst.per_face ? inst.face_props[t] : inst.props_id;
         }
     }
+    two_level_ = use_two_level();
     try {
-        bvh_ = build_bvh8(world.data(), tri_total_);
+        if (two_level_) build_two_level();
+        else build_flat();
     } catch (const Error&) {
         throw;
     } catch (const std::exception& e) {
@@ -403,13 +571,15 @@ size_t Scene::upload_bytes() const {
             prim_instance_.size() + prim_props_.size() + props_material_.size()) * sizeof(uint32_t) +
            props_.size() * sizeof(InstanceProperties) + inst_gpu_.size() * sizeof(InstanceGpu) +
            emissive_data_.size() * sizeof(EmissiveInstanceData) + has_tbn_.size() +
-           (tex_texels_.size() + tex_info_.size()) * sizeof(uint32_t);
+           (tex_texels_.size() + tex_info_.size() + tlas_refs_.size()) * sizeof(uint32_t) +
+           inst_trav_.size() * sizeof(InstanceTrav);
 }
 
 void Scene::release_device() {
     for (DeviceBuffer* b : {&d_nodes_, &d_tris_, &d_vertices_, &d_indices_, &d_tbns_, &d_tbn_indices_, &d_tex_coords_,
                             &d_tex_indices_, &d_props_, &d_instances_, &d_prim_instance_, &d_prim_props_, &d_emissive_,
-                            &d_cdf_tris_, &d_cdf_inst_, &d_props_material_, &d_has_tbn_, &d_tex_texels_, &d_tex_info_})
+                            &d_cdf_tris_, &d_cdf_inst_, &d_props_material_, &d_has_tbn_, &d_tex_texels_, &d_tex_info_,
+                            &d_inst_trav_, &d_tlas_refs_})
         b->release();
     const uint32_t nodes = dev_.node_count, tris = dev_.tri_count;
     dev_ = DeviceScene{};
@@ -445,6 +615,8 @@ void Scene::upload() {
     up(d_cdf_inst_, cdf_instances_.data(), cdf_instances_.size() * sizeof(float));
     up(d_props_material_, props_material_.data(), props_material_.size() * sizeof(uint32_t));
     up(d_has_tbn_, has_tbn_.data(), has_tbn_.size());
+    up(d_inst_trav_, inst_trav_.data(), inst_trav_.size() * sizeof(InstanceTrav));
+    up(d_tlas_refs_, tlas_refs_.data(), tlas_refs_.size() * sizeof(uint32_t));
     up(d_tex_texels_, tex_texels_.data(), tex_texels_.size() * sizeof(uint32_t));
     up(d_tex_info_, tex_info_.data(), tex_info_.size() * sizeof(uint32_t));
 
@@ -472,6 +644,8 @@ void Scene::upload() {
     dev_.cdf_instances = d_cdf_inst_.as<float>();
     dev_.emissive_count = (uint32_t)emissive_data_.size();
     dev_.emissive_weight = emissive_total_;
+    dev_.inst_trav = two_level_ ? d_inst_trav_.as<InstanceTrav>() : nullptr;
+    dev_.tlas_refs = two_level_ ? d_tlas_refs_.as<uint32_t>() : nullptr;
     dev_.tex_texels = d_tex_texels_.as<uint32_t>();
     dev_.tex_info = d_tex_info_.as<uint4>();
     dev_.tex_count = (uint32_t)textures_.size();
@@ -487,7 +661,7 @@ size_t Scene::device_bytes() const {
            d_tbn_indices_.bytes() + d_tex_coords_.bytes() + d_tex_indices_.bytes() + d_props_.bytes() +
            d_instances_.bytes() + d_prim_instance_.bytes() + d_prim_props_.bytes() + d_emissive_.bytes() +
            d_cdf_tris_.bytes() + d_cdf_inst_.bytes() + d_props_material_.bytes() + d_has_tbn_.bytes() +
-           d_tex_texels_.bytes() + d_tex_info_.bytes();
+           d_tex_texels_.bytes() + d_tex_info_.bytes() + d_inst_trav_.bytes() + d_tlas_refs_.bytes();
 }
 
 const ModelData& Scene::model(uint32_t object) const {

@@ -62,6 +62,13 @@ public:
     void add_instance_per_face(uint32_t object, const float transform[16], const reina_material* mats,
                                uint32_t mat_count, const uint32_t* face_material);
     void build(bool require_emissive);
+    // Acceleration structure (REINA_ACCEL_*): one BVH over world-space triangles, or a top level over
+    // instances with one bottom level per model; set before the build.
+    void set_accel(int mode);
+    bool two_level() const { return two_level_; }
+    uint32_t blas_count() const { return blas_count_; }
+    const std::vector<InstanceTrav>& instance_records() const { return inst_trav_; }
+    const std::vector<uint32_t>& tlas_refs() const { return tlas_refs_; }
 
     bool built() const { return built_; }
     float emissive_weight() const { return emissive_total_; }
@@ -92,6 +99,9 @@ private:
     InstanceProperties make_props(uint32_t object, const reina_material& mat) const;
     void compute_emissive(InstanceRecord& inst, const float emission[3]);
     void pack_emissives();
+    bool use_two_level() const;
+    void build_flat();
+    void build_two_level();
 
     int device_;
     bool built_ = false;
@@ -116,6 +126,12 @@ private:
     Bvh8 bvh_;
     std::vector<InstanceGpu> inst_gpu_;
     std::vector<uint8_t> has_tbn_;
+    // Two-level acceleration structure
+    int accel_mode_ = REINA_ACCEL_AUTO;
+    bool two_level_ = false;
+    uint32_t blas_count_ = 0;
+    std::vector<InstanceTrav> inst_trav_;
+    std::vector<uint32_t> tlas_refs_;   // top-level leaf entries: instance indices
     // Textures: all texels in one array (one RGBA8 word each) and per texture its first texel and size
     std::vector<Image> textures_;
     std::vector<uint32_t> tex_texels_;
@@ -123,11 +139,12 @@ private:
     // Device buffers
     DeviceBuffer d_nodes_, d_tris_, d_vertices_, d_indices_, d_tbns_, d_tbn_indices_, d_tex_coords_,
         d_tex_indices_, d_props_, d_instances_, d_prim_instance_, d_prim_props_, d_emissive_, d_cdf_tris_,
-        d_cdf_inst_, d_props_material_, d_has_tbn_, d_tex_texels_, d_tex_info_;
+        d_cdf_inst_, d_props_material_, d_has_tbn_, d_tex_texels_, d_tex_info_, d_inst_trav_, d_tlas_refs_;
     DeviceScene dev_;
 };
 
 // glm-style column-major helpers shared by the scene code and the C ABI.
 void mat4_identity(float m[16]);
+bool affine_inverse(const float T[16], float inv[12]);
 
 }  // namespace rt

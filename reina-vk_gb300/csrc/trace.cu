@@ -85,6 +85,33 @@ __global__ void RT_TRACE_BOUNDS(BLOCK) raycast_kernel_grid(const Bvh8Node* __res
     reduce_counters<COUNT>(c, counters);
 }
 
+// The same for two-level scenes (top level over instances, bottom levels per model).
+template <bool ANY, bool COUNT>
+__global__ void RT_TRACE_BOUNDS(kTraceBlock) raycast_kernel_two_level(DeviceScene sc, const Ray* __restrict__ rays,
+                                                                      uint32_t n, Hit* __restrict__ hits,
+                                                                      unsigned long long* counters, uint32_t* err_flag,
+                                                                      const uint32_t* __restrict__ order) {
+    __shared__ uint2 stack[kSmemStack * kTraceBlock];
+    const uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    TraceCounters c{0u, 0u};
+    if (k < n) {
+        const uint64_t i = order ? order[k] : k;
+        const float4* rp = reinterpret_cast<const float4*>(rays) + 2ull * i;
+        const float4 a = __ldcs(rp), b = __ldcs(rp + 1);
+        const TraceRay r = make_trace_ray(a.x, a.y, a.z, b.x, b.y, b.z, a.w, b.w);
+        Hit h;
+        uint32_t e = 0;
+        if (sc.node_count) {
+            e = traverse_two_level<ANY, COUNT, true, kSmemStack>(sc, r, stack + threadIdx.x, kTraceBlock, h, c);
+        } else {
+            h.prim = kMiss; h.t = r.tmax; h.u = 0.0f; h.v = 0.0f;
+        }
+        if (hits) __stcs(reinterpret_cast<float4*>(hits) + i, make_float4(__uint_as_float(h.prim), h.t, h.u, h.v));
+        if (e) atomicOr(err_flag, e);
+    }
+    reduce_counters<COUNT>(c, counters);
+}
+
 // ------------------------------------------------------------------------------------------------
 // Coherence order: rays binned by (direction octant, Morton code of the origin's cell on an 8^3 grid
 // over the bounds of the ray origins), bins in Morton order, rays in input order within a bin per warp.
@@ -224,9 +251,16 @@ static int persistent_grid(int sm_count) {
     return per_sm * std::max(1, sm_count);
 }
 
+// Two-level scenes always run the default block size and stack depth.
 template <bool ANY, bool COUNT, int BLOCK, int SS>
 static void launch_grid(const DeviceScene& s, const Ray* d_rays, uint64_t n, Hit* d_hits,
                         unsigned long long* d_counters, uint32_t* d_err, const uint32_t* order, cudaStream_t st) {
+    if (s.inst_trav) {
+        const uint64_t blocks = (n + kTraceBlock - 1) / kTraceBlock;
+        raycast_kernel_two_level<ANY, COUNT><<<(unsigned)blocks, kTraceBlock, 0, st>>>(s, d_rays, (uint32_t)n, d_hits,
+                                                                                     d_counters, d_err, order);
+        return;
+    }
     const uint64_t blocks = (n + BLOCK - 1) / BLOCK;
     raycast_kernel_grid<ANY, COUNT, BLOCK, SS><<<(unsigned)blocks, BLOCK, 0, st>>>(
         s.nodes, s.tris, s.node_count, d_rays, (uint32_t)n, d_hits, d_counters, d_err, order);
@@ -243,8 +277,9 @@ static void launch_grid_stack(int stack, const DeviceScene& s, const Ray* d_rays
 template <bool ANY>
 static void launch(const DeviceScene& s, const Ray* d_rays, uint64_t n, Hit* d_hits, uint32_t* d_err, uint32_t* d_next,
                    int sm_count, const TraceConfig& cfg, cudaStream_t st) {
-    // grid form (also for more than 2^31 rays, where the persistent form's fetch counter could wrap)
-    if (cfg.refill <= 0 || n > (1ull << 31)) {
+    // grid form (also for more than 2^31 rays, where the persistent form's fetch counter could wrap, and
+    // for two-level scenes)
+    if (cfg.refill <= 0 || n > (1ull << 31) || s.inst_trav) {
         uint32_t* scratch = nullptr;
         const uint32_t* order = nullptr;
         if (cfg.sort) {   // stream-ordered scratch: concurrent calls on other streams do not share it

@@ -370,6 +370,154 @@ __device__ __forceinline__ uint32_t traverse(const Bvh8Node* __restrict__ nodes,
     return err;
 }
 
+// ------------------------------------------------------------------------------------------------
+// Two-level scenes: a top-level BVH8 over instances (leaf entries index DeviceScene::tlas_refs, which
+// holds instance ids) and one bottom-level BVH8 per model in object space, in the same node and triangle
+// arrays.  A ray enters an instance through the instance's world-to-object matrix; t is the same in both
+// spaces (the direction is transformed, not normalized), so the closest distance found so far culls
+// boxes at both levels.  The stack entry (kLevelMarker, 0) separates an instance's bottom-level entries
+// from the top-level entries below it; popping it returns to the world-space ray.
+
+constexpr uint32_t kLevelMarker = 0xFFFFFFFFu;
+
+// The world ray in an instance's model space: origin and direction through the 3x4 matrix with
+// explicitly rounded products and sums in a fixed order (the host restatement evaluates the same), and
+// the traversal constants of the new ray.
+__device__ __forceinline__ TraceRay instance_ray(const TraceRay& w, const InstanceTrav* __restrict__ it) {
+    const float4* q = reinterpret_cast<const float4*>(it);
+    const float4 m0 = __ldg(q), m1 = __ldg(q + 1), m2 = __ldg(q + 2);
+    auto row = [](float4 m, float x, float y, float z) {
+        return __fadd_rn(__fadd_rn(__fmul_rn(m.x, x), __fmul_rn(m.y, y)), __fmul_rn(m.z, z));
+    };
+    return make_trace_ray(__fadd_rn(row(m0, w.ox, w.oy, w.oz), m0.w), __fadd_rn(row(m1, w.ox, w.oy, w.oz), m1.w),
+                          __fadd_rn(row(m2, w.ox, w.oy, w.oz), m2.w), row(m0, w.dx, w.dy, w.dz),
+                          row(m1, w.dx, w.dy, w.dz), row(m2, w.dx, w.dy, w.dz), w.tmin, w.tmax);
+}
+
+// Closest / any hit through both levels; hit ids are global (instance's first triangle + the record's
+// triangle index within the model).  Ties in t go to the lower global id, as in the flat traversal.
+// Triangles are tested as soon as they are reached (no postponing).
+template <bool ANY, bool COUNT, bool REFINE = true, int SS = kSmemStack>
+__device__ __forceinline__ uint32_t traverse_two_level(const DeviceScene& sc, const TraceRay& wr, uint2* stack, int stride,
+                                                       Hit& hit, TraceCounters& cnt) {
+    const uint4* nptr = reinterpret_cast<const uint4*>(sc.nodes);
+    const float4* tptr = reinterpret_cast<const float4*>(sc.tris);
+    uint2 spill[kTotalStack - SS];
+    uint32_t err = 0, steps = 0;
+    TraceRay r = wr;
+    bool in_blas = false;
+    uint32_t cur_first = 0, cur_inst = 0, best_inst = 0, best_rec = 0;
+    float best_t = wr.tmax;
+    hit.prim = kMiss;
+    hit.t = wr.tmax;
+    hit.u = 0.0f;
+    hit.v = 0.0f;
+    uint2 group = make_uint2(0u, 0x80000000u);
+    int sp = 0;
+    auto push = [&](uint2 g) {
+        if (sp < SS) stack[sp * stride] = g;
+        else if (sp < kTotalStack) spill[sp - SS] = g;
+        else { err |= kErrStackOverflow; return false; }
+        ++sp;
+        return true;
+    };
+    auto pop = [&]() {
+        --sp;
+        return sp < SS ? stack[sp * stride] : spill[sp - SS];
+    };
+    for (;;) {
+        if (++steps > kMaxTraversalSteps) { err |= kErrStepLimit; break; }
+        uint2 tgroup;
+        if (group.y > 0x00FFFFFFu) {
+            const uint32_t slot_bit = 31u - __clz(group.y);
+            const uint32_t slot = (slot_bit - 24u) ^ r.oct_inv;
+            const uint32_t child = group.x + __popc(group.y & ((1u << slot) - 1u));
+            group.y &= ~(1u << slot_bit);
+            if (group.y > 0x00FFFFFFu && !push(group)) break;
+            const uint4* np = nptr + 5ull * child;
+            const uint4 w0 = __ldg(np + 0), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3), w4 = __ldg(np + 4);
+            if (COUNT) cnt.nodes++;
+            const uint32_t hm = intersect_children(r, w0, w1, w2, w3, w4, best_t);
+            group = make_uint2(w1.x, (hm & 0xFF000000u) | (w0.w >> 24));
+            tgroup = make_uint2(w1.y, hm & 0x00FFFFFFu);
+        } else {
+            tgroup = group;   // a pending leaf group
+            group = make_uint2(0u, 0u);
+        }
+        if (!in_blas) {
+            if (tgroup.y) {   // enter the nearest pending instance; the rest of the top level waits below a marker
+                const int k = __ffs(tgroup.y) - 1;
+                tgroup.y &= tgroup.y - 1u;
+                if (group.y > 0x00FFFFFFu && !push(group)) break;
+                if (tgroup.y && !push(tgroup)) break;
+                group = make_uint2(0u, 0u);
+                const uint32_t ii = __ldg(sc.tlas_refs + tgroup.x + (uint32_t)k);
+                const uint4 tail = __ldg(reinterpret_cast<const uint4*>(sc.inst_trav + ii) + 3);
+                if (tail.x != 0xFFFFFFFFu) {   // a model without triangles has no bottom level
+                    if (!push(make_uint2(kLevelMarker, 0u))) break;
+                    r = instance_ray(wr, sc.inst_trav + ii);
+                    in_blas = true;
+                    cur_inst = ii;
+                    cur_first = tail.y;
+                    group = make_uint2(tail.x, 0x80000000u);
+                    continue;
+                }
+            }
+        } else {
+            bool done = false;
+            while (tgroup.y) {
+                const int k = __ffs(tgroup.y) - 1;
+                tgroup.y &= tgroup.y - 1u;
+                const float4* tp = tptr + 3ull * (tgroup.x + (uint32_t)k);
+                const float4 a = __ldg(tp + 0), b = __ldg(tp + 1), c = __ldg(tp + 2);
+                if (COUNT) cnt.tris++;
+                float t, u, v;
+                if (intersect_triangle(r, a, b, c, best_t, t, u, v)) {
+                    const uint32_t prim = cur_first + __float_as_uint(a.w);
+                    if (ANY || t < best_t || prim < hit.prim) {   // t <= best_t holds; equal t: lower id wins
+                        best_t = t;
+                        hit.prim = prim; hit.t = t; hit.u = u; hit.v = v;
+                        best_rec = tgroup.x + (uint32_t)k;
+                        best_inst = cur_inst;
+                        if (ANY) { done = true; break; }
+                    }
+                }
+            }
+            if (done) break;
+        }
+        if (group.y <= 0x00FFFFFFu) {
+            if (sp == 0) break;
+            group = pop();
+            if (group.x == kLevelMarker && group.y == 0u) {   // back to the top level
+                r = wr;
+                in_blas = false;
+                if (sp == 0) break;
+                group = pop();
+            }
+        }
+    }
+    if (hit.prim == kMiss) {
+        hit.t = wr.tmax;
+    } else if (REFINE) {
+        const TraceRay ri = instance_ray(wr, sc.inst_trav + best_inst);
+        const float4* tp = tptr + 3ull * best_rec;
+        refine_hit(ri, __ldg(tp + 0), __ldg(tp + 1), __ldg(tp + 2), hit);
+    }
+    return err;
+}
+
+// Either traversal, by the scene's structure.  Kernels instantiated with TWO = false handle flat scenes
+// only (the two-level path costs registers: the world ray is kept while inside an instance); the
+// launchers pick TWO = true when a scene of the launch is two-level.
+template <bool ANY, bool COUNT, bool REFINE = true, int SS = kSmemStack, bool TWO = false>
+__device__ __forceinline__ uint32_t trace_scene(const DeviceScene& sc, const TraceRay& r, uint2* stack, int stride, Hit& hit,
+                                                TraceCounters& cnt) {
+    if constexpr (TWO) {
+        if (sc.inst_trav) return traverse_two_level<ANY, COUNT, REFINE, SS>(sc, r, stack, stride, hit, cnt);
+    }
+    return traverse<ANY, COUNT, REFINE, SS>(sc.nodes, sc.tris, r, stack, stride, hit, cnt);
+}
+
 // Persistent traversal with dynamic ray fetch (Aila and Laine, "Understanding the Efficiency of Ray
 // Traversal on GPUs", HPG 2009): every warp keeps 32 rays in flight; whenever at least `refill` lanes
 // have finished, those lanes take the next rays, so short rays do not idle their lane until the warp's

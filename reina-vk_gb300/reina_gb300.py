@@ -33,6 +33,7 @@ REINA_ERR_BUDGET = -8
 RAY_CLOSEST = 0
 RAY_ANY = 1
 MISS = 0xFFFFFFFF
+ACCEL_AUTO, ACCEL_FLAT, ACCEL_TWO_LEVEL = 0, 1, 2
 
 RAY_DTYPE = np.dtype([("org", np.float32, 3), ("tmin", np.float32), ("dir", np.float32, 3), ("tmax", np.float32)])
 HIT_DTYPE = np.dtype([("prim", np.uint32), ("t", np.float32), ("u", np.float32), ("v", np.float32)])
@@ -74,7 +75,8 @@ class _SceneStats(C.Structure):
         ("triangle_count", C.c_uint64), ("instance_count", C.c_uint64), ("node_count", C.c_uint64),
         ("node_bytes", C.c_uint64), ("triangle_bytes", C.c_uint64), ("device_bytes", C.c_uint64),
         ("max_depth", C.c_uint32), ("leaf_triangles_max", C.c_uint32), ("build_seconds", C.c_double),
-        ("bounds_min", C.c_float * 3), ("bounds_max", C.c_float * 3),
+        ("bounds_min", C.c_float * 3), ("bounds_max", C.c_float * 3), ("two_level", C.c_uint32),
+        ("blas_count", C.c_uint32),
     ]
 
 
@@ -326,6 +328,8 @@ def load_library() -> C.CDLL:
         "reina_scene_define_texture_file": (I32, [P, C.c_char_p, C.POINTER(U32)]),
         "reina_scene_define_texture_encoded": (I32, [P, P, U64, C.POINTER(U32)]),
         "reina_scene_texture_count": (I32, [P, C.POINTER(U32)]),
+        "reina_scene_set_accel": (I32, [P, C.c_int]),
+        "reina_scene_export_two_level": (I32, [P, P, P, C.POINTER(U32), C.POINTER(U32)]),
         "reina_scene_export_properties": (I32, [P, P, U32, C.POINTER(U32)]),
         "reina_scene_export_texture": (I32, [P, U32, C.POINTER(U32), C.POINTER(U32), P, U64]),
         "reina_decode_image": (I32, [P, U64, C.POINTER(U32), C.POINTER(U32), P, U64]),
@@ -569,6 +573,19 @@ class Scene:
         out = np.empty((h.value, w.value, 4), np.uint8)
         _check(_lib.reina_scene_export_texture(self._h, texture_id, C.byref(w), C.byref(h), _ptr(out), out.nbytes))
         return out
+
+    def export_two_level(self):
+        """(instance records (N, 16) as raw 32-bit words, top-level leaf entries); empty for flat scenes."""
+        ni, nr = C.c_uint32(), C.c_uint32()
+        _check(_lib.reina_scene_export_two_level(self._h, None, None, C.byref(ni), C.byref(nr)))
+        rec = np.zeros((ni.value, 16), np.uint32)
+        refs = np.zeros(nr.value, np.uint32)
+        _check(_lib.reina_scene_export_two_level(self._h, _ptr(rec), _ptr(refs), C.byref(ni), C.byref(nr)))
+        return rec, refs
+
+    def set_accel(self, mode: int) -> None:
+        """ACCEL_AUTO, ACCEL_FLAT or ACCEL_TWO_LEVEL (before build)."""
+        _check(_lib.reina_scene_set_accel(self._h, mode))
 
     def texture_count(self) -> int:
         n = C.c_uint32()

@@ -216,8 +216,10 @@ class SceneDesc:
         T = np.eye(4, dtype=np.float32) if transform is None else np.asarray(transform, np.float32)
         self.instances.append((obj, T, materials if materials is not None else [material], face_material))
 
-    def to_product(self, R, ctx, require_emissive=False):
+    def to_product(self, R, ctx, require_emissive=False, accel=None):
         s = R.Scene(ctx)
+        if accel is not None:
+            s.set_accel(accel)
         for tex in self.textures:
             s.define_texture_rgba8(tex)
         for v4, idx, t9, ti, uv, ui in self.objects:
@@ -441,3 +443,44 @@ def textured_room(R, seed: int = 1) -> SceneDesc:
     d.add_instance(d.add_object(lv, li), None,
                    M(material_idx=0, albedo=(0.78, 0.78, 0.78), emission=CORNELL_LIGHT, cull_backface=True))
     return d
+
+
+def rotate_axis(axis, deg):
+    a = np.asarray(axis, np.float64)
+    a = a / np.linalg.norm(a)
+    t = np.radians(deg)
+    K = np.array([[0, -a[2], a[1]], [a[2], 0, -a[0]], [-a[1], a[0], 0]])
+    R3 = np.eye(3) + np.sin(t) * K + (1 - np.cos(t)) * (K @ K)
+    m = np.eye(4)
+    m[:3, :3] = R3
+    return m
+
+
+def instanced_field(R, n: int = 24, seed: int = 7) -> SceneDesc:
+    """One displaced sphere model (level 3, with TBNs) instanced n times with seeded rotations, anisotropic
+    scales and translations inside the Cornell room, each with its own material; the room and its light
+    stay single instances.  Instancing repeats the sphere enough that the automatic choice builds two
+    levels."""
+    d = cornell(R, seed)
+    v, i, tbn, ti = sphere_tbn(3, 0.08, seed, R)
+    sph = d.add_object(v, i, tbn, ti)
+    u = uniform(9 * n, seed + 1).reshape(n, 9)
+    for k in range(n):
+        r = u[k]
+        T = (translate(-0.75 + 1.5 * r[0], -0.8 + 1.4 * r[1], -0.7 + 1.3 * r[2]) @ rotate_axis(r[3:6] - 0.5, 360 * r[6])
+             @ scale(0.08 + 0.12 * r[7], 0.08 + 0.12 * r[8], 0.1))
+        if k % 3 == 0:
+            m = R.Material(material_idx=1, albedo=(0.9, 0.8, 0.6), roughness=0.3 * r[0])
+        elif k % 3 == 1:
+            m = R.Material(material_idx=2, albedo=(0.9, 0.95, 0.9), ior=1.45, absorption=r[1], roughness=0.02)
+        else:
+            m = R.Material(material_idx=3, albedo=tuple(r[0:3]), roughness=0.2 + 0.6 * r[4], metallic=r[5],
+                           specular_tint=(1, 1, 1), sheen_tint=(1, 1, 1), interp_normals=True)
+        d.add_instance(sph, T, m)
+    return d
+
+
+def instance_models(d: SceneDesc):
+    """Object-space triangles (9 floats each) of every object of a scene description."""
+    return [np.ascontiguousarray(v4[np.asarray(idx).reshape(-1, 3)][:, :, :3].reshape(-1, 9), np.float32)
+            for v4, idx, *_ in d.objects]

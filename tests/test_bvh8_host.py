@@ -39,7 +39,8 @@ def test_exported_bvh8_instanced_scene(R, O, host_ctx):
     """Several instances of one model plus planes (the flattened instance layout); the oracle's BVH is
     built over the world-space triangles of the exported records, in id order."""
     d = scenes.material_zoo(R)
-    s = d.to_product(R, host_ctx)
+    s = d.to_product(R, host_ctx, accel=R.ACCEL_FLAT)
+    assert s.stats()["two_level"] == 0
     _, trecs = s.export_bvh()
     rec = trecs.copy().view(np.float32).reshape(-1, 12)
     ids = trecs.copy().view(np.uint32).reshape(-1, 12)[:, 3]

@@ -163,6 +163,7 @@ def test_gltf_scene(R, host_ctx, tmp_path, glb):
     p = tmp_path / ("s.glb" if glb else "s.gltf")
     p.write_bytes(make_gltf(glb))
     s = R.Scene(host_ctx)
+    s.set_accel(R.ACCEL_FLAT)   # the checks below read world-space triangle records
     st = s.add_gltf(p)
     assert st == {"meshes": 1, "primitives": 2, "instances": 4, "skipped_primitives": 0, "ignored_textures": 0}
     assert s.object_count() == 2
