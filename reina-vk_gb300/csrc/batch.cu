@@ -115,7 +115,7 @@ __global__ void __launch_bounds__(BLOCK) kb_extend(BatchLaunch B, const JobGpu* 
             ps.hprim[p] = h.prim;
             ps.hu[p] = h.u;
             ps.hv[p] = h.v;
-            m = h.prim == kMiss ? kQueueMiss : 1 + (int)s.props_material[s.prim_props[h.prim]];
+            m = h.prim == kMiss ? kQueueMiss : 1 + (int)s.props_material[prim_props_of(s, h.prim)];
         }
         warp_count64(reinterpret_cast<unsigned long long*>(ps.counters + kCntRays), active);
 #pragma unroll

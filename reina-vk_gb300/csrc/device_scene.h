@@ -20,6 +20,7 @@ struct alignas(16) InstanceGpu {
     uint32_t object;      // object (model) id
     float light_weight;   // emissive weight (Σ area·luminance, src/scene/Instance.cpp:15-53), 0 if not emissive
     float light_area;     // emissive area of the instance, 0 if not emissive
+    uint32_t face_base;   // per-face instances: first entry in DeviceScene::face_props; else 0xFFFFFFFF
 };
 
 struct DeviceScene {
@@ -38,8 +39,9 @@ struct DeviceScene {
     // instances
     const InstanceProperties* props = nullptr;
     const InstanceGpu* instances = nullptr;
-    const uint32_t* prim_instance = nullptr;  // per global triangle
-    const uint32_t* prim_props = nullptr;     // per global triangle: InstanceProperties index
+    const uint32_t* prim_instance = nullptr;  // per global triangle (flat scenes; null in two-level scenes)
+    const uint32_t* prim_props = nullptr;     // per global triangle: InstanceProperties index (flat scenes)
+    const uint32_t* face_props = nullptr;     // per-face instances' InstanceProperties ids, concatenated
     const uint32_t* props_material = nullptr; // per InstanceProperties: material_idx (the SBT offset)
     const uint8_t* has_tbn = nullptr;         // per object: 1 if the model supplied TBN data
     uint32_t instance_count = 0;
@@ -61,5 +63,32 @@ struct DeviceScene {
     float bounds_lo[3] = {0.0f, 0.0f, 0.0f};  // world-space triangle bounds (ray binning frame)
     float bounds_hi[3] = {0.0f, 0.0f, 0.0f};
 };
+
+#if defined(__CUDACC__)
+// Instance and InstanceProperties index of global triangle `prim`: the per-triangle tables of a flat
+// scene, or (two-level scenes, which keep no per-triangle tables) a binary search over the instances'
+// first triangles and the instance's material or per-face table.
+__device__ __forceinline__ void prim_lookup(const DeviceScene& s, uint32_t prim, uint32_t& inst, uint32_t& props) {
+    if (s.prim_instance) {
+        inst = s.prim_instance[prim];
+        props = s.prim_props[prim];
+        return;
+    }
+    uint32_t lo = 0, hi = s.instance_count - 1;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) / 2;
+        if (s.instances[mid].first_prim <= prim) lo = mid;
+        else hi = mid - 1;
+    }
+    inst = lo;
+    const InstanceGpu& g = s.instances[lo];
+    props = g.face_base == 0xFFFFFFFFu ? g.props : s.face_props[g.face_base + (prim - g.first_prim)];
+}
+__device__ __forceinline__ uint32_t prim_props_of(const DeviceScene& s, uint32_t prim) {
+    uint32_t inst, props;
+    prim_lookup(s, prim, inst, props);
+    return props;
+}
+#endif
 
 }  // namespace rt

@@ -86,7 +86,7 @@ __global__ void __launch_bounds__(BLOCK) k_extend_grid(RenderLaunch L, int cur) 
             ps.hprim[p] = h.prim;
             ps.hu[p] = h.u;
             ps.hv[p] = h.v;
-            m = h.prim == kMiss ? kQueueMiss : 1 + (int)L.s.props_material[L.s.prim_props[h.prim]];
+            m = h.prim == kMiss ? kQueueMiss : 1 + (int)L.s.props_material[prim_props_of(L.s, h.prim)];
         }
         warp_count64(reinterpret_cast<unsigned long long*>(ps.counters + kCntRays), active);
 #pragma unroll
@@ -119,7 +119,7 @@ __global__ void __launch_bounds__(kBlock) k_extend(RenderLaunch L, int cur) {
             ps.hprim[p] = h.prim;
             ps.hu[p] = h.u;
             ps.hv[p] = h.v;
-            m = h.prim == kMiss ? kQueueMiss : 1 + (int)L.s.props_material[L.s.prim_props[h.prim]];
+            m = h.prim == kMiss ? kQueueMiss : 1 + (int)L.s.props_material[prim_props_of(L.s, h.prim)];
         }
         warp_count64(reinterpret_cast<unsigned long long*>(ps.counters + kCntRays), valid);
 #pragma unroll

@@ -516,17 +516,29 @@ void Scene::build(bool require_emissive) {
         tri_total_ += ranges_[inst.object].index_count;
     }
     if (tri_total_ >= 0x7FFFFFFFull) fail(REINA_ERR_INVALID, "scene has too many triangles");
-    prim_instance_.resize(tri_total_);
-    prim_props_.resize(tri_total_);
+    two_level_ = use_two_level();
+    // Per-triangle instance and material tables for flat scenes; two-level scenes (whose point is not
+    // to hold per-triangle data for every instance) look both up from the instance records and keep only
+    // the per-face tables of per-face instances.
+    prim_instance_.clear();
+    prim_props_.clear();
+    face_props_.clear();
+    if (!two_level_) {
+        prim_instance_.resize(tri_total_);
+        prim_props_.resize(tri_total_);
+    }
     for (size_t ii = 0; ii < instances_.size(); ++ii) {
         const InstanceRecord& inst = instances_[ii];
         const uint32_t ntri = ranges_[inst.object].index_count;
+        if (two_level_) {
+            if (inst.per_face) face_props_.insert(face_props_.end(), inst.face_props.begin(), inst.face_props.end());
+            continue;
+        }
         for (uint32_t t = 0; t < ntri; ++t) {
             prim_instance_[inst.first_prim + t] = (uint32_t)ii;
             prim_props_[inst.first_prim + t] = inst.per_face ? inst.face_props[t] : inst.props_id;
         }
     }
-    two_level_ = use_two_level();
     try {
         if (two_level_) build_two_level();
         else build_flat();
@@ -537,6 +549,7 @@ void Scene::build(bool require_emissive) {
     }
 
     inst_gpu_.assign(instances_.size(), InstanceGpu{});
+    uint32_t face_base = 0;
     for (size_t ii = 0; ii < instances_.size(); ++ii) {
         const InstanceRecord& inst = instances_[ii];
         InstanceGpu& g = inst_gpu_[ii];
@@ -549,6 +562,11 @@ void Scene::build(bool require_emissive) {
         g.object = inst.object;
         g.light_weight = inst.light.emissive ? inst.light.weight : 0.0f;
         g.light_area = inst.light.emissive ? inst.light.area : 0.0f;
+        g.face_base = 0xFFFFFFFFu;
+        if (two_level_ && inst.per_face) {
+            g.face_base = face_base;
+            face_base += (uint32_t)inst.face_props.size();
+        }
     }
 
     has_tbn_.resize(models_.size());
@@ -571,7 +589,7 @@ size_t Scene::upload_bytes() const {
             prim_instance_.size() + prim_props_.size() + props_material_.size()) * sizeof(uint32_t) +
            props_.size() * sizeof(InstanceProperties) + inst_gpu_.size() * sizeof(InstanceGpu) +
            emissive_data_.size() * sizeof(EmissiveInstanceData) + has_tbn_.size() +
-           (tex_texels_.size() + tex_info_.size() + tlas_refs_.size()) * sizeof(uint32_t) +
+           (tex_texels_.size() + tex_info_.size() + tlas_refs_.size() + face_props_.size()) * sizeof(uint32_t) +
            inst_trav_.size() * sizeof(InstanceTrav);
 }
 
@@ -579,7 +597,7 @@ void Scene::release_device() {
     for (DeviceBuffer* b : {&d_nodes_, &d_tris_, &d_vertices_, &d_indices_, &d_tbns_, &d_tbn_indices_, &d_tex_coords_,
                             &d_tex_indices_, &d_props_, &d_instances_, &d_prim_instance_, &d_prim_props_, &d_emissive_,
                             &d_cdf_tris_, &d_cdf_inst_, &d_props_material_, &d_has_tbn_, &d_tex_texels_, &d_tex_info_,
-                            &d_inst_trav_, &d_tlas_refs_})
+                            &d_inst_trav_, &d_tlas_refs_, &d_face_props_})
         b->release();
     const uint32_t nodes = dev_.node_count, tris = dev_.tri_count;
     dev_ = DeviceScene{};
@@ -616,6 +634,7 @@ void Scene::upload() {
     up(d_props_material_, props_material_.data(), props_material_.size() * sizeof(uint32_t));
     up(d_has_tbn_, has_tbn_.data(), has_tbn_.size());
     up(d_inst_trav_, inst_trav_.data(), inst_trav_.size() * sizeof(InstanceTrav));
+    up(d_face_props_, face_props_.data(), face_props_.size() * sizeof(uint32_t));
     up(d_tlas_refs_, tlas_refs_.data(), tlas_refs_.size() * sizeof(uint32_t));
     up(d_tex_texels_, tex_texels_.data(), tex_texels_.size() * sizeof(uint32_t));
     up(d_tex_info_, tex_info_.data(), tex_info_.size() * sizeof(uint32_t));
@@ -633,8 +652,9 @@ void Scene::upload() {
     dev_.tex_indices = d_tex_indices_.as<uint32_t>();
     dev_.props = d_props_.as<InstanceProperties>();
     dev_.instances = d_instances_.as<InstanceGpu>();
-    dev_.prim_instance = d_prim_instance_.as<uint32_t>();
-    dev_.prim_props = d_prim_props_.as<uint32_t>();
+    dev_.prim_instance = two_level_ ? nullptr : d_prim_instance_.as<uint32_t>();
+    dev_.prim_props = two_level_ ? nullptr : d_prim_props_.as<uint32_t>();
+    dev_.face_props = d_face_props_.as<uint32_t>();
     dev_.props_material = d_props_material_.as<uint32_t>();
     dev_.has_tbn = d_has_tbn_.as<uint8_t>();
     dev_.instance_count = (uint32_t)instances_.size();
@@ -661,7 +681,8 @@ size_t Scene::device_bytes() const {
            d_tbn_indices_.bytes() + d_tex_coords_.bytes() + d_tex_indices_.bytes() + d_props_.bytes() +
            d_instances_.bytes() + d_prim_instance_.bytes() + d_prim_props_.bytes() + d_emissive_.bytes() +
            d_cdf_tris_.bytes() + d_cdf_inst_.bytes() + d_props_material_.bytes() + d_has_tbn_.bytes() +
-           d_tex_texels_.bytes() + d_tex_info_.bytes() + d_inst_trav_.bytes() + d_tlas_refs_.bytes();
+           d_tex_texels_.bytes() + d_tex_info_.bytes() + d_inst_trav_.bytes() + d_tlas_refs_.bytes() +
+           d_face_props_.bytes();
 }
 
 const ModelData& Scene::model(uint32_t object) const {
@@ -672,7 +693,18 @@ const ModelData& Scene::model(uint32_t object) const {
 void Scene::prim_info(uint32_t prim, uint32_t* inst, uint32_t* local) const {
     if (!built_) fail(REINA_ERR_STATE, "scene is not built");
     if (prim >= tri_total_) fail(REINA_ERR_INVALID, "triangle id out of range");
-    const uint32_t ii = prim_instance_[prim];
+    uint32_t ii;
+    if (!prim_instance_.empty()) {
+        ii = prim_instance_[prim];
+    } else {   // two-level: the last instance whose first triangle is at or before prim
+        size_t lo = 0, hi = instances_.size() - 1;
+        while (lo < hi) {
+            const size_t mid = (lo + hi + 1) / 2;
+            if (instances_[mid].first_prim <= prim) lo = mid;
+            else hi = mid - 1;
+        }
+        ii = (uint32_t)lo;
+    }
     if (inst) *inst = ii;
     if (local) *local = prim - instances_[ii].first_prim;
 }

@@ -132,6 +132,7 @@ private:
     uint32_t blas_count_ = 0;
     std::vector<InstanceTrav> inst_trav_;
     std::vector<uint32_t> tlas_refs_;   // top-level leaf entries: instance indices
+    std::vector<uint32_t> face_props_;  // two-level: per-face instances' material ids, concatenated
     // Textures: all texels in one array (one RGBA8 word each) and per texture its first texel and size
     std::vector<Image> textures_;
     std::vector<uint32_t> tex_texels_;
@@ -139,7 +140,8 @@ private:
     // Device buffers
     DeviceBuffer d_nodes_, d_tris_, d_vertices_, d_indices_, d_tbns_, d_tbn_indices_, d_tex_coords_,
         d_tex_indices_, d_props_, d_instances_, d_prim_instance_, d_prim_props_, d_emissive_, d_cdf_tris_,
-        d_cdf_inst_, d_props_material_, d_has_tbn_, d_tex_texels_, d_tex_info_, d_inst_trav_, d_tlas_refs_;
+        d_cdf_inst_, d_props_material_, d_has_tbn_, d_tex_texels_, d_tex_info_, d_inst_trav_, d_tlas_refs_,
+        d_face_props_;
     DeviceScene dev_;
 };
 

@@ -125,10 +125,11 @@ struct HitInfo {
 // the geometric normal at every vertex (the reference reads its TBN buffer unconditionally).
 __device__ __forceinline__ HitInfo hit_info(const DeviceScene& s, uint32_t prim, float bu, float bv, V3 rayDir) {
     HitInfo h;
-    const uint32_t ii = s.prim_instance[prim];
+    uint32_t ii, pid;
+    prim_lookup(s, prim, ii, pid);
     const InstanceGpu& inst = s.instances[ii];
     h.inst = ii;
-    h.props = s.prim_props[prim];
+    h.props = pid;
     const InstanceProperties& pr = s.props[h.props];
     const uint32_t lp = prim - inst.first_prim;
     h.lp = lp;

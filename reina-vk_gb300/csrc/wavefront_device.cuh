@@ -65,9 +65,11 @@ __device__ __forceinline__ void store_ray(const PathState& ps, uint32_t p, V3 o,
 
 // Light pdf (solid angle) of reaching `p` on emissive triangle `prim` from `from` (emission MIS).
 __device__ __forceinline__ float light_pdf_sa(const DeviceScene& s, float total_w, uint32_t prim, V3 from, V3 p) {
-    const InstanceGpu& inst = s.instances[s.prim_instance[prim]];
+    uint32_t ii, pid;
+    prim_lookup(s, prim, ii, pid);
+    const InstanceGpu& inst = s.instances[ii];
     if (!(inst.light_weight > 0.0f)) return 0.0f;
-    const InstanceProperties& pr = s.props[s.prim_props[prim]];
+    const InstanceProperties& pr = s.props[pid];
     const uint32_t lp = prim - inst.first_prim;
     const float* m = inst.m;
     auto wpos = [&](uint32_t k) {

@@ -477,6 +477,14 @@ def instanced_field(R, n: int = 24, seed: int = 7) -> SceneDesc:
             m = R.Material(material_idx=3, albedo=tuple(r[0:3]), roughness=0.2 + 0.6 * r[4], metallic=r[5],
                            specular_tint=(1, 1, 1), sheen_tint=(1, 1, 1), interp_normals=True)
         d.add_instance(sph, T, m)
+    # two more instances with per-face materials (Lambertian / Disney palette by face)
+    nf = i.size // 3
+    pal = [R.Material(material_idx=0, albedo=(0.8, 0.3, 0.2)), R.Material(material_idx=0, albedo=(0.2, 0.6, 0.8)),
+           R.Material(material_idx=3, albedo=(0.9, 0.9, 0.3), roughness=0.4, specular_tint=(1, 1, 1),
+                      sheen_tint=(1, 1, 1))]
+    for k, pos in enumerate([(-0.45, 0.45, 0.3), (0.5, 0.5, -0.3)]):
+        face = (uniform(nf, seed + 20 + k) * len(pal)).astype(np.uint32)
+        d.add_instance(sph, translate(*pos) @ scale(0.15, 0.15, 0.15), materials=pal, face_material=face)
     return d
 
 
