@@ -14,7 +14,9 @@ L2 (129 MB) is flushed by writing a 512 MB buffer between timed steps (outside t
 Beside the headline line's required keys, the JSON carries: `render` (the 1.3M-triangle scene at
 1920x1080, 64 spp, 12 bounces, NEE+MIS, wavefront vs plain megakernel; the Cornell room), `batched` (256
 seeded scenes rendered in one batched call vs one at a time; `--batch-scenes`), `served` (a Poisson
-request stream through the request server vs one at a time; `--serve-seconds`), and `cpu_baseline`.
+request stream through the request server vs one at a time; `--serve-seconds`), `instanced` (256
+instances of one sphere built flat and as two levels: device memory, build time, ray-cast time;
+`--instances`), and `cpu_baseline`.
 `--profile`, `--profile-render` and `--profile-batch` launch small fixed workloads for ncu and exit.
 
 `--impl reference` times the CPU restatement of the path (oracle/, FP32, all host threads) on a bounded
@@ -308,6 +310,8 @@ def run_ours(args) -> dict | None:
     }
     if not args.no_render:
         out["render"] = render_metrics(R, ctx, torch, args.render_frames, scene)
+    if args.instances > 0:
+        out["instanced"] = instanced_metrics(R, ctx, torch, args.instances, rays)
     if args.batch_scenes > 0:
         pool, setup_s = build_pool(R, ctx, args.batch_scenes)
         out["batched"] = batch_metrics(R, ctx, torch, pool, setup_s, args.batch_mega_scenes)
@@ -363,6 +367,56 @@ def render_metrics(R, ctx, torch, frames: int, scene_large) -> dict:
         out[f"cornell_{name}"] = {"s_per_frame": dt, "paths_per_s": 256 * 256 * 16 / dt,
                                   "segments_per_s": st["rays"] / dt,
                                   "rays_per_s": (st["rays"] + st["shadow_rays"]) / dt}
+    return out
+
+
+def instanced_metrics(R, ctx, torch, n_inst: int, rays) -> dict:
+    """n_inst seeded, rotated and scaled instances of one 20,480-triangle sphere in [-1, 1]^3, built flat and
+    as two levels: device memory, BVH build time and closest / any-hit ray cast time of the bench's rays
+    (camera + random rays, the same counts as the headline step)."""
+    import scenes
+
+    v, i, _ = R.icosphere(5, 0.1, 3)
+    u = scenes.uniform(7 * n_inst, 11).reshape(n_inst, 7)
+    stream = torch.cuda.current_stream()
+    n = rays.shape[0]
+    d_rays = torch.from_numpy(rays.view(np.float32).reshape(n, 8).copy()).cuda()
+    d_hits = torch.empty((n, 4), dtype=torch.float32, device="cuda")
+    flush = torch.empty(512 << 18, dtype=torch.float32, device="cuda")
+    out = {"workload": f"{n_inst} instances of a 20,480-triangle sphere ({n_inst * 20480:,} triangles), {n:,} rays"}
+    hits = {}
+    for name, accel in (("flat", R.ACCEL_FLAT), ("two_level", R.ACCEL_TWO_LEVEL)):
+        sc = R.Scene(ctx)
+        sc.set_accel(accel)
+        oid = sc.define_object(v, i)
+        for k in range(n_inst):
+            r = u[k]
+            T = (scenes.translate(-1 + 2 * r[0], -1 + 2 * r[1], -1 + 2 * r[2]) @ scenes.rotate_axis(r[3:6] - 0.5, 360 * r[6])
+                 @ scenes.scale(0.05, 0.05, 0.05))
+            sc.add_instance(oid, T, R.Material())
+        t0 = time.perf_counter()
+        sc.build()
+        build_s = time.perf_counter() - t0
+        res = {"device_bytes": sc.stats()["device_bytes"], "build_s": build_s}
+        for flags, key in ((R.RAY_CLOSEST, "closest_ms"), (R.RAY_ANY, "any_ms")):
+            for _ in range(3):
+                R.raycast_device(ctx, sc, d_rays.data_ptr(), n, d_hits.data_ptr(), flags, stream.cuda_stream)
+            tot = 0.0
+            for _ in range(5):
+                flush.zero_()
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                R.raycast_device(ctx, sc, d_rays.data_ptr(), n, d_hits.data_ptr(), flags, stream.cuda_stream)
+                b.record(stream)
+                torch.cuda.synchronize()
+                tot += a.elapsed_time(b)
+            res[key] = tot / 5
+            if flags == R.RAY_CLOSEST:
+                hits[name] = d_hits.cpu().numpy().view(np.uint32)[:, 0].copy()
+        res["closest_rays_per_s"] = n / (res["closest_ms"] * 1e-3)
+        out[name] = res
+        sc.close()
+    out["same_ids_fraction"] = float((hits["flat"] == hits["two_level"]).mean())
     return out
 
 
@@ -634,6 +688,8 @@ def main() -> int:
     ap.add_argument("--serve-seconds", type=float, default=4.0,
                     help="arrival window of the served workload (0 skips it; 120 is the full stream)")
     ap.add_argument("--serve-rate", type=float, default=50.0, help="Poisson arrival rate (requests/s)")
+    ap.add_argument("--instances", type=int, default=256,
+                    help="instances of the flat vs two-level instancing metrics (0 skips them)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     out = run_reference(args) if args.impl == "reference" else run_ours(args)
