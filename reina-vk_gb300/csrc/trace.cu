@@ -87,7 +87,7 @@ __global__ void RT_TRACE_BOUNDS(BLOCK) raycast_kernel_grid(const Bvh8Node* __res
 
 // The same for two-level scenes (top level over instances, bottom levels per model).  Closest hit is
 // held to 64 registers (8 blocks per SM): 4 % faster than the 80 it takes unbounded on 256 instances;
-// any hit was 1 % slower so bounded and keeps its own allocation.
+// any hit was 1 % slower when bounded, so it keeps its own allocation.
 template <bool ANY, bool COUNT>
 __global__ void __launch_bounds__(kTraceBlock, ANY ? 1 : 8) raycast_kernel_two_level(DeviceScene sc, const Ray* __restrict__ rays,
                                                                       uint32_t n, Hit* __restrict__ hits,
