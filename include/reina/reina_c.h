@@ -491,7 +491,7 @@ typedef struct reina_gltf_stats {
  * KHR_materials_ior; KHR_materials_transmission -> specular transmission, no culling; baseColorTexture
  * -> texture_id, normalTexture -> normal_map_id).  Every image of the file becomes a scene texture in
  * image order (gltfloader.cpp:283-340; never flipped); images that do not decode (formats other than
- * PNG) are left out and the references to them counted in ignored_textures.  A primitive without
+ * PNG and sequential JPEG) are left out and the references to them counted in ignored_textures.  A primitive without
  * normals fails as in the reference. */
 int reina_scene_add_gltf(reina_scene* scene, const char* path, reina_gltf_stats* out_stats);
 
@@ -503,7 +503,8 @@ int reina_scene_add_gltf(reina_scene* scene, const char* path, reina_gltf_stats*
  *   _rgba8:   raw texels (width*height*4 bytes)
  *   _file:    an image file, rows flipped vertically as the reference loads paths (src/graphics/Image.cpp:14)
  *   _encoded: an image file's bytes in memory, not flipped (src/graphics/Image.cpp:27-33)
- * Image files: PNG (every colour type and bit depth, as stbi_load(..., 4) converts them); other formats
+ * Image files: PNG (every colour type and bit depth, as stbi_load(..., 4) converts them) and sequential
+ * JPEG (baseline / extended Huffman; texels may differ by a few units from stb_image's); other formats
  * fail with REINA_ERR_IO. */
 int reina_scene_define_texture_rgba8(reina_scene* scene, const uint8_t* rgba8, uint32_t width, uint32_t height,
                                      uint32_t* out_texture_id);

@@ -3,6 +3,7 @@
 #include "image.h"
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <fstream>
 #include <iterator>
@@ -459,13 +460,366 @@ Image decode_png(const uint8_t* data, size_t n) {
     return img;
 }
 
+// ---- JPEG (ITU-T T.81: baseline and extended sequential Huffman, 8-bit samples) -----------------------
+
+// Natural (row-major) index of the k-th coefficient in zigzag order (T.81 figure A.6).
+constexpr uint8_t kZigzag[64] = {0,  1,  8,  16, 9,  2,  3,  10, 17, 24, 32, 25, 18, 11, 4,  5,
+                                 12, 19, 26, 33, 40, 48, 41, 34, 27, 20, 13, 6,  7,  14, 21, 28,
+                                 35, 42, 49, 56, 57, 50, 43, 36, 29, 22, 15, 23, 30, 37, 44, 51,
+                                 58, 59, 52, 45, 38, 31, 39, 46, 53, 60, 61, 54, 47, 55, 62, 63};
+
+struct JpegHuff {
+    bool defined = false;
+    int count[17] = {0};
+    std::vector<uint8_t> vals;
+    // canonical decoding (T.81 F.2.2.3): per length the first code and the index of its first value
+    int32_t mincode[17], maxcode[18], valptr[17];
+    void derive() {
+        int code = 0, k = 0;
+        for (int l = 1; l <= 16; ++l) {
+            valptr[l] = k;
+            mincode[l] = code;
+            code += count[l];
+            k += count[l];
+            maxcode[l] = count[l] ? code - 1 : -1;
+            code <<= 1;
+        }
+        maxcode[17] = 0x7FFFFFFF;
+        defined = true;
+    }
+};
+
+struct JpegComp {
+    int id = 0, h = 1, v = 1, tq = 0, td = 0, ta = 0;
+    int bw = 0, bh = 0;       // blocks across / down (padded to whole MCUs)
+    std::vector<uint8_t> plane;
+    int pred = 0;
+};
+
+class JpegBits {
+public:
+    JpegBits(const uint8_t* p, size_t n, size_t pos) : p_(p), n_(n), pos_(pos) {}
+    int bit() {
+        if (cnt_ == 0) fill();
+        --cnt_;
+        return (int)((buf_ >> cnt_) & 1u);
+    }
+    int bits(int k) {
+        int v = 0;
+        for (int i = 0; i < k; ++i) v = (v << 1) | bit();
+        return v;
+    }
+    // After a restart interval: skip to the RSTn marker and past it.
+    void restart() {
+        cnt_ = 0;
+        marker_ = false;
+        while (pos_ + 1 < n_ && !(p_[pos_] == 0xFF && p_[pos_ + 1] >= 0xD0 && p_[pos_ + 1] <= 0xD7)) ++pos_;
+        if (pos_ + 1 >= n_) bad("JPEG: missing restart marker");
+        pos_ += 2;
+    }
+    size_t pos() const { return pos_; }
+
+private:
+    void fill() {
+        // past a marker (or the end) the decoder reads zero bits; a valid stream never needs them
+        uint8_t b = 0;
+        if (!marker_ && pos_ < n_) {
+            b = p_[pos_];
+            if (b == 0xFF) {
+                const uint8_t nx = pos_ + 1 < n_ ? p_[pos_ + 1] : 0xD9;
+                if (nx == 0x00) pos_ += 2;
+                else { marker_ = true; b = 0; }
+            } else {
+                ++pos_;
+            }
+        }
+        buf_ = b;
+        cnt_ = 8;
+    }
+    const uint8_t* p_;
+    size_t n_, pos_;
+    uint32_t buf_ = 0;
+    int cnt_ = 0;
+    bool marker_ = false;
+};
+
+int huff_decode(JpegBits& in, const JpegHuff& h) {
+    int code = in.bit();
+    for (int l = 1; l <= 16; ++l) {
+        if (code <= h.maxcode[l]) return h.vals[(size_t)(h.valptr[l] + code - h.mincode[l])];
+        code = (code << 1) | in.bit();
+    }
+    bad("JPEG: invalid Huffman code");
+}
+
+inline int extend(int v, int t) { return t == 0 ? 0 : (v < (1 << (t - 1)) ? v - (1 << t) + 1 : v); }   // T.81 F.2.2.1
+
+// Separable 8x8 inverse DCT in double precision: f(x, y) = 1/4 sum C(u) C(v) F(u, v) cos((2x+1)u pi/16)
+// cos((2y+1)v pi/16) with C(0) = 1/sqrt(2), level-shifted by 128, rounded to nearest and clamped.
+void idct8x8(const double* F, uint8_t* out, int stride) {
+    static double cosv[8][8];
+    static bool init = false;
+    if (!init) {
+        for (int x = 0; x < 8; ++x)
+            for (int u = 0; u < 8; ++u)
+                cosv[x][u] = (u == 0 ? std::sqrt(0.5) : 1.0) * std::cos((2 * x + 1) * u * 3.14159265358979323846 / 16.0);
+        init = true;
+    }
+    double tmp[64];
+    for (int v = 0; v < 8; ++v)   // rows of F: inverse over u for every x
+        for (int x = 0; x < 8; ++x) {
+            double s = 0.0;
+            for (int u = 0; u < 8; ++u) s += cosv[x][u] * F[v * 8 + u];
+            tmp[v * 8 + x] = s;
+        }
+    for (int y = 0; y < 8; ++y)
+        for (int x = 0; x < 8; ++x) {
+            double s = 0.0;
+            for (int v = 0; v < 8; ++v) s += cosv[y][v] * tmp[v * 8 + x];
+            const double val = std::floor(s / 4.0 + 128.0 + 0.5);
+            out[y * stride + x] = (uint8_t)std::min(255.0, std::max(0.0, val));
+        }
+}
+
+Image decode_jpeg(const uint8_t* d, size_t n) {
+    uint16_t qt[4][64];
+    bool qt_def[4] = {false, false, false, false};
+    JpegHuff dc[4], ac[4];
+    std::vector<JpegComp> comps;
+    int W = 0, H = 0, hmax = 1, vmax = 1, mcux = 0, mcuy = 0;
+    int restart = 0;
+    int adobe_transform = -1;
+    bool frame = false, seen_scan = false;
+    size_t p = 2;
+    auto u16 = [&](size_t at) {
+        if (at + 2 > n) bad("JPEG: truncated");
+        return (int)((d[at] << 8) | d[at + 1]);
+    };
+    for (;;) {
+        while (p < n && d[p] != 0xFF) ++p;   // tolerate fill bytes between segments
+        while (p < n && d[p] == 0xFF) ++p;
+        if (p >= n) bad("JPEG: truncated (no EOI)");
+        const uint8_t m = d[p++];
+        if (m == 0xD9) break;   // EOI
+        if (m == 0xD8 || (m >= 0xD0 && m <= 0xD7) || m == 0x01) continue;
+        const int len = u16(p);
+        if (len < 2 || p + (size_t)len > n) bad("JPEG: truncated segment");
+        const uint8_t* s = d + p + 2;
+        const size_t sl = (size_t)len - 2;
+        if (m == 0xDB) {   // DQT
+            size_t k = 0;
+            while (k < sl) {
+                const int pq = s[k] >> 4, tq = s[k] & 15;
+                if (tq > 3 || pq > 1) bad("JPEG: bad quantization table");
+                ++k;
+                if (k + (pq ? 128u : 64u) > sl) bad("JPEG: truncated quantization table");
+                for (int i = 0; i < 64; ++i) qt[tq][i] = pq ? (uint16_t)((s[k + 2 * i] << 8) | s[k + 2 * i + 1]) : s[k + i];
+                k += pq ? 128 : 64;
+                qt_def[tq] = true;
+            }
+        } else if (m == 0xC4) {   // DHT
+            size_t k = 0;
+            while (k < sl) {
+                const int tc = s[k] >> 4, th = s[k] & 15;
+                if (tc > 1 || th > 3 || k + 17 > sl) bad("JPEG: bad Huffman table");
+                JpegHuff& h = tc ? ac[th] : dc[th];
+                int total = 0;
+                h.count[0] = 0;
+                for (int l = 1; l <= 16; ++l) total += (h.count[l] = s[k + (size_t)l]);
+                if (total > 256 || k + 17 + (size_t)total > sl) bad("JPEG: bad Huffman table");
+                h.vals.assign(s + k + 17, s + k + 17 + total);
+                h.derive();
+                k += 17 + (size_t)total;
+            }
+        } else if (m == 0xC0 || m == 0xC1) {   // SOF0 / SOF1: sequential Huffman
+            if (frame) bad("JPEG: more than one frame");
+            if (sl < 6 || s[0] != 8) bad("JPEG: only 8-bit samples are supported");
+            H = (s[1] << 8) | s[2];
+            W = (s[3] << 8) | s[4];
+            const int nc = s[5];
+            if (W == 0 || H == 0) bad("JPEG: zero size (DNL not supported)");
+            if ((uint64_t)W * H > (1ull << 28)) bad("JPEG too large (more than 2^28 pixels)");
+            if ((nc != 1 && nc != 3) || sl < 6 + 3 * (size_t)nc) bad("JPEG: only 1 or 3 components are supported");
+            comps.resize((size_t)nc);
+            for (int c = 0; c < nc; ++c) {
+                comps[c].id = s[6 + 3 * c];
+                comps[c].h = s[7 + 3 * c] >> 4;
+                comps[c].v = s[7 + 3 * c] & 15;
+                comps[c].tq = s[8 + 3 * c];
+                if (comps[c].h < 1 || comps[c].h > 4 || comps[c].v < 1 || comps[c].v > 4 || comps[c].tq > 3)
+                    bad("JPEG: bad component parameters");
+                hmax = std::max(hmax, comps[c].h);
+                vmax = std::max(vmax, comps[c].v);
+            }
+            mcux = (W + 8 * hmax - 1) / (8 * hmax);
+            mcuy = (H + 8 * vmax - 1) / (8 * vmax);
+            for (JpegComp& c : comps) {
+                c.bw = mcux * c.h;
+                c.bh = mcuy * c.v;
+                c.plane.assign((size_t)c.bw * 8 * c.bh * 8, 0);
+            }
+            frame = true;
+        } else if (m == 0xC2 || m == 0xC3 || (m >= 0xC5 && m <= 0xCF && m != 0xC8 && m != 0xCC)) {
+            bad("JPEG: progressive, lossless and arithmetic-coded JPEG are not supported");
+        } else if (m == 0xDD) {   // DRI
+            restart = u16(p + 2);
+        } else if (m == 0xEE) {   // APP14 (Adobe): colour transform flag
+            if (sl >= 12 && std::memcmp(s, "Adobe", 5) == 0) adobe_transform = s[11];
+        } else if (m == 0xDA) {   // SOS
+            if (!frame) bad("JPEG: scan before frame");
+            const int ns = s[0];
+            if (ns < 1 || ns > 4 || sl < 1 + 2 * (size_t)ns + 3) bad("JPEG: bad scan header");
+            std::vector<JpegComp*> sc;
+            for (int k = 0; k < ns; ++k) {
+                JpegComp* c = nullptr;
+                for (JpegComp& cc : comps)
+                    if (cc.id == s[1 + 2 * k]) c = &cc;
+                if (!c) bad("JPEG: scan references an unknown component");
+                c->td = s[2 + 2 * k] >> 4;
+                c->ta = s[2 + 2 * k] & 15;
+                if (c->td > 3 || c->ta > 3 || !dc[c->td].defined || !ac[c->ta].defined) bad("JPEG: missing Huffman table");
+                if (!qt_def[c->tq]) bad("JPEG: missing quantization table");
+                c->pred = 0;
+                sc.push_back(c);
+            }
+            const uint8_t ss = s[1 + 2 * ns], se = s[2 + 2 * ns], ahal = s[3 + 2 * ns];
+            if (ss != 0 || se != 63 || ahal != 0) bad("JPEG: not a sequential scan");
+            JpegBits in(d, n, p + (size_t)len);
+            // blocks of one MCU: interleaved scans take h x v blocks per component; a single-component scan
+            // takes the component's blocks one at a time in raster order over its own (unpadded) extent
+            const bool single = ns == 1;
+            int units_x = mcux, units_y = mcuy;
+            if (single) {
+                const JpegComp& c = *sc[0];
+                units_x = ((W * c.h + hmax - 1) / hmax + 7) / 8;
+                units_y = ((H * c.v + vmax - 1) / vmax + 7) / 8;
+            }
+            double F[64];
+            auto block = [&](JpegComp& c, int bx, int by) {
+                std::fill(F, F + 64, 0.0);
+                const uint16_t* q = qt[c.tq];
+                const int t = huff_decode(in, dc[c.td]);
+                if (t > 11) bad("JPEG: bad DC difference");
+                c.pred += extend(in.bits(t), t);
+                F[0] = (double)c.pred * q[0];
+                for (int k = 1; k < 64;) {
+                    const int rs = huff_decode(in, ac[c.ta]);
+                    const int r = rs >> 4, sz = rs & 15;
+                    if (sz == 0) {
+                        if (r != 15) break;   // end of block
+                        k += 16;
+                        continue;
+                    }
+                    k += r;
+                    if (k > 63) bad("JPEG: coefficient index past 63");
+                    F[kZigzag[k]] = (double)extend(in.bits(sz), sz) * q[k];
+                    ++k;
+                }
+                const int stride = c.bw * 8;
+                idct8x8(F, c.plane.data() + (size_t)by * 8 * stride + (size_t)bx * 8, stride);
+            };
+            int todo = restart;
+            for (int my = 0; my < units_y; ++my)
+                for (int mx = 0; mx < units_x; ++mx) {
+                    if (restart && todo == 0) {
+                        in.restart();
+                        for (JpegComp* c : sc) c->pred = 0;
+                        todo = restart;
+                    }
+                    if (single) {
+                        block(*sc[0], mx, my);
+                    } else {
+                        for (JpegComp* c : sc)
+                            for (int v = 0; v < c->v; ++v)
+                                for (int h = 0; h < c->h; ++h) block(*c, mx * c->h + h, my * c->v + v);
+                    }
+                    if (restart) --todo;
+                }
+            seen_scan = true;
+            p = in.pos();
+            continue;
+        }
+        p += (size_t)len;
+    }
+    if (!frame || !seen_scan) bad("JPEG: no image data");
+
+    // upsample every component to the full grid: 2:1 by the triangle filter (3/4 nearer + 1/4 farther
+    // sample, JFIF co-sited centres), other ratios by replication
+    const int fw = mcux * hmax * 8, fh = mcuy * vmax * 8;
+    std::vector<std::vector<uint8_t>> full(comps.size());
+    for (size_t ci = 0; ci < comps.size(); ++ci) {
+        const JpegComp& c = comps[ci];
+        const int cw = c.bw * 8, ch = c.bh * 8;
+        const int sx = hmax / c.h, sy = vmax / c.v;
+        if (hmax % c.h || vmax % c.v) bad("JPEG: non-integral sampling ratio");
+        std::vector<uint8_t>& o = full[ci];
+        o.assign((size_t)fw * fh, 0);
+        if (sx == 1 && sy == 1) {
+            o = c.plane;
+            continue;
+        }
+        if ((sx == 2 || sx == 1) && (sy == 2 || sy == 1)) {
+            // vertical then horizontal, in 16ths (2x2) or quarters (one direction)
+            const int used_w = (W * c.h + hmax - 1) / hmax, used_h = (H * c.v + vmax - 1) / vmax;
+            const int uw = std::max(1, std::min(cw, used_w)), uh = std::max(1, std::min(ch, used_h));
+            auto S = [&](int x, int y) { return (int)c.plane[(size_t)std::min(std::max(y, 0), uh - 1) * cw + std::min(std::max(x, 0), uw - 1)]; };
+            for (int y = 0; y < fh; ++y) {
+                const int yc = sy == 2 ? y / 2 : y;
+                const int yf = sy == 2 ? (y % 2 ? yc + 1 : yc - 1) : yc;   // farther row
+                for (int x = 0; x < fw; ++x) {
+                    const int xc = sx == 2 ? x / 2 : x;
+                    const int xf = sx == 2 ? (x % 2 ? xc + 1 : xc - 1) : xc;
+                    int val;
+                    if (sx == 2 && sy == 2) {
+                        const int t_near = 3 * S(xc, yc) + S(xc, yf), t_far = 3 * S(xf, yc) + S(xf, yf);
+                        val = (3 * t_near + t_far + 8) >> 4;
+                    } else if (sx == 2) {
+                        val = (3 * S(xc, yc) + S(xf, yc) + 2) >> 2;
+                    } else {
+                        val = (3 * S(xc, yc) + S(xc, yf) + 2) >> 2;
+                    }
+                    o[(size_t)y * fw + x] = (uint8_t)val;
+                }
+            }
+            continue;
+        }
+        for (int y = 0; y < fh; ++y)
+            for (int x = 0; x < fw; ++x) o[(size_t)y * fw + x] = c.plane[(size_t)std::min(y / sy, ch - 1) * cw + std::min(x / sx, cw - 1)];
+    }
+
+    Image img;
+    img.width = (uint32_t)W;
+    img.height = (uint32_t)H;
+    img.rgba.assign((size_t)W * H * 4, 255);
+    const bool rgb = comps.size() == 3 && (adobe_transform == 0 || (comps[0].id == 'R' && comps[1].id == 'G' && comps[2].id == 'B'));
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            uint8_t* o = &img.rgba[((size_t)y * W + x) * 4];
+            const size_t i = (size_t)y * fw + x;
+            if (comps.size() == 1) {
+                o[0] = o[1] = o[2] = full[0][i];
+            } else if (rgb) {
+                o[0] = full[0][i];
+                o[1] = full[1][i];
+                o[2] = full[2][i];
+            } else {   // JFIF YCbCr -> RGB
+                const double Y = full[0][i], cb = full[1][i] - 128.0, cr = full[2][i] - 128.0;
+                auto q = [](double v) { return (uint8_t)std::min(255.0, std::max(0.0, std::floor(v + 0.5))); };
+                o[0] = q(Y + 1.402 * cr);
+                o[1] = q(Y - 0.344136 * cb - 0.714136 * cr);
+                o[2] = q(Y + 1.772 * cb);
+            }
+        }
+    return img;
+}
+
 }  // namespace
 
 Image decode_image(const uint8_t* data, size_t n) {
     static const uint8_t kPngSig[8] = {137, 80, 78, 71, 13, 10, 26, 10};
     if (n >= 8 && std::memcmp(data, kPngSig, 8) == 0) return decode_png(data, n);
-    if (n >= 2 && data[0] == 0xFF && data[1] == 0xD8) bad("JPEG images are not supported by this build (PNG only)");
-    bad("unknown image format (PNG expected)");
+    if (n >= 3 && data[0] == 0xFF && data[1] == 0xD8 && data[2] == 0xFF) return decode_jpeg(data, n);
+    bad("unknown image format (PNG or JPEG expected)");
 }
 
 void flip_rows(Image& img) {

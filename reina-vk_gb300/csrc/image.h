@@ -1,5 +1,6 @@
 // Texture image decoding for Scene::defineTexture (src/scene/Scene.cpp:15-25, src/graphics/Image.cpp:10-41):
-// an encoded image (PNG here; the reference links stb_image) becomes 8-bit RGBA texels, first row first.
+// an encoded image (PNG or sequential JPEG here; the reference links stb_image) becomes 8-bit RGBA texels,
+// first row first.
 #pragma once
 
 #include <cstddef>
@@ -20,7 +21,12 @@ std::vector<uint8_t> zlib_inflate(const uint8_t* data, size_t n, size_t limit);
 
 // Decodes an encoded image to RGBA8 the way stbi_load(..., 4) does: PNG of every colour type and bit
 // depth (1, 2, 4, 8, 16; 16-bit samples keep their high byte; grey levels below 8 bits are scaled to
-// 0..255; tRNS transparency; Adam7 interlacing).  Other formats fail with REINA_ERR_IO.
+// 0..255; tRNS transparency; Adam7 interlacing), and sequential (baseline / extended Huffman, 8-bit) JPEG
+// with one or three components, any sampling factors, restart markers and multiple scans: inverse DCT
+// in double precision, 2:1 chroma upsampling by the triangle filter (replication for other ratios),
+// JFIF YCbCr -> RGB (Adobe RGB files kept as RGB).  stb_image's integer IDCT and fixed-point colour
+// conversion can give JPEG texels a few units apart from these.  Other formats (progressive JPEG, BMP,
+// TGA, GIF, HDR, ...) fail with REINA_ERR_IO.
 Image decode_image(const uint8_t* data, size_t n);
 
 // Reads and decodes a file; `flip_vertically` reverses the row order (stbi_set_flip_vertically_on_load,

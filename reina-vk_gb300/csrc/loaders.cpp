@@ -403,7 +403,7 @@ std::string uri_path(const std::string& uri) {
 // addTexturesToScene (gltfloader.cpp:283-340): every image of the asset becomes a scene texture, in image
 // order, decoded from its bytes without a vertical flip (the parser loads external image files into
 // memory, so every source reaches Scene::defineTexture(bytes)).  Returns the texture id per image; an
-// image that cannot be decoded (a format other than PNG) gets -1, and the material references to it are
+// image that cannot be decoded (a format other than PNG and sequential JPEG) gets -1, and the material references to it are
 // counted as ignored.
 std::vector<int32_t> gltf_images(const Gltf& g, const std::string& base_dir, Scene& scene) {
     const Json& imgs = g.doc["images"];

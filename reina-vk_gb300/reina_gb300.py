@@ -920,7 +920,7 @@ class SaveSchedule:
 
 
 def decode_image(data: bytes) -> np.ndarray:
-    """An image file's bytes (PNG) decoded to (H, W, 4) uint8, as the texture calls decode them."""
+    """An image file's bytes (PNG or sequential JPEG) decoded to (H, W, 4) uint8, as the texture calls decode them."""
     L = load_library()
     buf = C.create_string_buffer(bytes(data), len(data))
     w, h = C.c_uint32(), C.c_uint32()

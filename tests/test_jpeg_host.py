@@ -1,0 +1,342 @@
+"""JPEG texture decoding on the host: the test encodes seeded images as sequential (baseline) JPEG itself —
+its own forward DCT, quantization tables and Huffman tables built from the symbol frequencies, every
+chroma subsampling the decoder handles, restart intervals, single- and multi-scan files — and checks
+the library's decoding against the reconstruction of the coefficients it wrote (dequantization, the 8x8
+inverse DCT, the triangle-filter chroma upsampling and the JFIF YCbCr -> RGB conversion, restated in
+numpy), plus the reference's own JPEG textures when they are present."""
+import heapq
+import struct
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+REF_TEXTURES = Path("/root/reference/textures")
+
+ZIGZAG = np.array([0, 1, 8, 16, 9, 2, 3, 10, 17, 24, 32, 25, 18, 11, 4, 5, 12, 19, 26, 33, 40, 48, 41, 34, 27, 20, 13,
+                   6, 7, 14, 21, 28, 35, 42, 49, 56, 57, 50, 43, 36, 29, 22, 15, 23, 30, 37, 44, 51, 58, 59, 52, 45,
+                   38, 31, 39, 46, 53, 60, 61, 54, 47, 55, 62, 63])
+
+_u = np.arange(8)
+COS = np.cos((2 * _u[:, None] + 1) * _u[None, :] * np.pi / 16) * np.where(_u == 0, np.sqrt(0.5), 1.0)[None, :]
+
+
+def fdct(block):   # 8x8 forward DCT (T.81 A.3.3)
+    return COS.T @ block @ COS / 4.0
+
+
+def idct(F):
+    return COS @ F @ COS.T / 4.0
+
+
+def huff_lengths(freq: dict) -> dict:
+    """Code lengths (<= 16) for the symbols of `freq`, with one reserved longest code (never all ones)."""
+    f = dict(freq)
+    while True:
+        items = [(c, i, [s]) for i, (s, c) in enumerate(sorted(f.items()))] + [(1, -1, [256])]
+        heapq.heapify(items)
+        depth = {s: 0 for _, _, ss in items for s in ss}
+        k = len(items)
+        while len(items) > 1:
+            a, b = heapq.heappop(items), heapq.heappop(items)
+            for s in a[2] + b[2]:
+                depth[s] += 1
+            k += 1
+            heapq.heappush(items, (a[0] + b[0], k, a[2] + b[2]))
+        if max(depth.values()) <= 16:
+            depth.pop(256)
+            return depth
+        f = {s: (c + 1) // 2 for s, c in f.items()}
+
+
+def canonical(lengths: dict):
+    """(counts per length 1..16, symbols in code order, code table symbol -> (code, length))."""
+    order = sorted(lengths, key=lambda s: (lengths[s], s))
+    counts = [0] * 17
+    for s in order:
+        counts[lengths[s]] += 1
+    codes, code, prev = {}, 0, 0
+    for s in order:
+        code <<= lengths[s] - prev
+        prev = lengths[s]
+        codes[s] = (code, lengths[s])
+        code += 1
+    return counts[1:], order, codes
+
+
+class BitWriter:
+    def __init__(self):
+        self.out = bytearray()
+        self.acc = 0
+        self.n = 0
+
+    def put(self, v, n):
+        for i in range(n - 1, -1, -1):
+            self.acc = (self.acc << 1) | ((v >> i) & 1)
+            self.n += 1
+            if self.n == 8:
+                self.out.append(self.acc)
+                if self.acc == 0xFF:
+                    self.out.append(0)
+                self.acc = self.n = 0
+
+    def flush(self):
+        if self.n:
+            self.put((1 << (8 - self.n)) - 1, 8 - self.n)
+
+
+def category(v):
+    return 0 if v == 0 else int(abs(v)).bit_length()
+
+
+def bits_of(v, c):
+    return v if v >= 0 else v + (1 << c) - 1
+
+
+def encode_jpeg(rgb, sampling=((2, 2), (1, 1), (1, 1)), gray=False, restart=0, scans="interleaved", quality_step=1,
+                seed=0):
+    """Returns (file bytes, per-component quantized coefficient blocks, quant tables, component layout)."""
+    rng = np.random.default_rng(seed)
+    H, W = rgb.shape[:2]
+    x = rgb.astype(np.float64)
+    if gray:
+        planes = [0.299 * x[..., 0] + 0.587 * x[..., 1] + 0.114 * x[..., 2]]
+        sampling = ((1, 1),)
+    else:
+        Y = 0.299 * x[..., 0] + 0.587 * x[..., 1] + 0.114 * x[..., 2]
+        Cb = -0.168736 * x[..., 0] - 0.331264 * x[..., 1] + 0.5 * x[..., 2] + 128
+        Cr = 0.5 * x[..., 0] - 0.418688 * x[..., 1] - 0.081312 * x[..., 2] + 128
+        planes = [Y, Cb, Cr]
+    hmax = max(h for h, _ in sampling)
+    vmax = max(v for _, v in sampling)
+    mcux, mcuy = -(-W // (8 * hmax)), -(-H // (8 * vmax))
+    qts = [np.clip(1 + quality_step * (np.arange(64) // 3) + rng.integers(0, 3, 64), 1, 255).astype(np.int64)
+           for _ in range(2)]
+    comps = []
+    for ci, (p, (h, v)) in enumerate(zip(planes, sampling)):
+        sx, sy = hmax // h, vmax // v
+        cw, ch = -(-W // sx), -(-H // sy)
+        # subsample by averaging, pad by edge replication to whole MCUs
+        pp = np.pad(p, ((0, (-H) % sy), (0, (-W) % sx)), mode="edge")
+        sub = pp.reshape(pp.shape[0] // sy, sy, pp.shape[1] // sx, sx).mean(axis=(1, 3))[:ch, :cw]
+        bw, bh = mcux * h, mcuy * v
+        full = np.pad(sub, ((0, bh * 8 - ch), (0, bw * 8 - cw)), mode="edge")
+        q = qts[0 if ci == 0 else 1]
+        blocks = np.zeros((bh, bw, 64), np.int64)
+        for by in range(bh):
+            for bx in range(bw):
+                F = fdct(full[by * 8:by * 8 + 8, bx * 8:bx * 8 + 8] - 128.0).reshape(64)[ZIGZAG]
+                blocks[by, bx] = np.round(F / q).astype(np.int64)
+        comps.append(dict(id=ci + 1, h=h, v=v, tq=0 if ci == 0 else 1, blocks=blocks, cw=cw, ch=ch, bw=bw, bh=bh))
+
+    def units(scan_comps):
+        """Blocks of a scan in coding order: (component index, block x, block y, mcu index)."""
+        out = []
+        if len(scan_comps) == 1:
+            c = comps[scan_comps[0]]
+            ux, uy = -(-c["cw"] // 8), -(-c["ch"] // 8)
+            for by in range(uy):
+                for bx in range(ux):
+                    out.append((scan_comps[0], bx, by, by * ux + bx))
+        else:
+            for my in range(mcuy):
+                for mx in range(mcux):
+                    for ci in scan_comps:
+                        c = comps[ci]
+                        for vv in range(c["v"]):
+                            for hh in range(c["h"]):
+                                out.append((ci, mx * c["h"] + hh, my * c["v"] + vv, my * mcux + mx))
+        return out
+
+    scan_list = [list(range(len(comps)))] if scans == "interleaved" else [[c] for c in range(len(comps))]
+    seg = bytearray(b"\xff\xd8")
+    seg += b"\xff\xe0" + struct.pack(">H", 16) + b"JFIF\x00\x01\x01\x00\x00\x01\x00\x01\x00\x00"
+    for t, q in enumerate(qts[: 1 if gray else 2]):
+        seg += b"\xff\xdb" + struct.pack(">HB", 67, t) + bytes(q.astype(np.uint8))
+    seg += b"\xff\xc0" + struct.pack(">HBHHB", 8 + 3 * len(comps), 8, H, W, len(comps))
+    for c in comps:
+        seg += bytes([c["id"], c["h"] << 4 | c["v"], c["tq"]])
+    if restart:
+        seg += b"\xff\xdd" + struct.pack(">HH", 4, restart)
+    for sc in scan_list:
+        # symbols of this scan for the frequency-built tables (DC table per component class, AC likewise)
+        seq = units(sc)
+        syms = []
+        preds = {ci: 0 for ci in sc}
+        last_mcu = -1
+        n_mcu = 0
+        for ci, bx, by, mcu in seq:
+            if mcu != last_mcu:
+                if restart and n_mcu and n_mcu % restart == 0:
+                    preds = {c: 0 for c in sc}
+                    syms.append(("RST", None, None))
+                last_mcu = mcu
+                n_mcu += 1
+            blk = comps[ci]["blocks"][by, bx]
+            diff = int(blk[0]) - preds[ci]
+            preds[ci] = int(blk[0])
+            cls = 0 if ci == 0 else 1
+            syms.append(("DC", cls, (category(diff), diff)))
+            run = 0
+            last_nz = max([k for k in range(1, 64) if blk[k] != 0], default=0)
+            for k in range(1, last_nz + 1):
+                if blk[k] == 0:
+                    run += 1
+                    continue
+                while run > 15:
+                    syms.append(("AC", cls, (0xF0, None)))
+                    run -= 16
+                c = category(int(blk[k]))
+                syms.append(("AC", cls, ((run << 4) | c, int(blk[k]))))
+                run = 0
+            if last_nz < 63:
+                syms.append(("AC", cls, (0x00, None)))
+        tables = {}
+        for kind in ("DC", "AC"):
+            for cls in (0, 1):
+                freq = {}
+                for k, c, v in syms:
+                    if k == kind and c == cls:
+                        freq[v[0]] = freq.get(v[0], 0) + 1
+                if freq:
+                    tables[(kind, cls)] = canonical(huff_lengths(freq))
+        for (kind, cls), (counts, order, _) in tables.items():
+            tc = 0 if kind == "DC" else 1
+            seg += b"\xff\xc4" + struct.pack(">HB", 2 + 1 + 16 + len(order), tc << 4 | cls) + bytes(counts) + bytes(order)
+        seg += b"\xff\xda" + struct.pack(">HB", 6 + 2 * len(sc), len(sc))
+        for ci in sc:
+            cls = 0 if ci == 0 else 1
+            seg += bytes([comps[ci]["id"], cls << 4 | cls])
+        seg += bytes([0, 63, 0])
+        bw = BitWriter()
+        rst = 0
+        for kind, cls, v in syms:
+            if kind == "RST":
+                bw.flush()
+                seg += bw.out
+                bw = BitWriter()
+                seg += bytes([0xFF, 0xD0 + rst])
+                rst = (rst + 1) % 8
+                continue
+            code, n = tables[(kind, cls)][2][v[0]]
+            bw.put(code, n)
+            if kind == "DC":
+                if v[0]:
+                    bw.put(bits_of(v[1], v[0]), v[0])
+            elif v[1] is not None:
+                bw.put(bits_of(v[1], v[0] & 15), v[0] & 15)
+        bw.flush()
+        seg += bw.out
+    seg += b"\xff\xd9"
+    return bytes(seg), comps, qts, (hmax, vmax, mcux, mcuy)
+
+
+def reconstruct(comps, qts, layout, W, H, gray):
+    """The decoder's definitions restated: dequantize, IDCT (double), level shift, round, clamp; 2:1
+    triangle-filter upsampling (replication otherwise); JFIF YCbCr -> RGB with rounding."""
+    hmax, vmax, mcux, mcuy = layout
+    fw, fh = mcux * hmax * 8, mcuy * vmax * 8
+    full = []
+    for c in comps:
+        q = qts[c["tq"]]
+        plane = np.zeros((c["bh"] * 8, c["bw"] * 8), np.int64)
+        for by in range(c["bh"]):
+            for bx in range(c["bw"]):
+                F = np.zeros(64)
+                F[ZIGZAG] = c["blocks"][by, bx] * q
+                f = np.floor(idct(F.reshape(8, 8)) + 128.0 + 0.5)
+                plane[by * 8:by * 8 + 8, bx * 8:bx * 8 + 8] = np.clip(f, 0, 255)
+        sx, sy = hmax // c["h"], vmax // c["v"]
+        if sx == 1 and sy == 1:
+            full.append(plane)
+            continue
+        if sx > 2 or sy > 2:   # replication
+            ys, xs = np.arange(fh) // sy, np.arange(fw) // sx
+            full.append(plane[np.minimum(ys, plane.shape[0] - 1)[:, None], np.minimum(xs, plane.shape[1] - 1)[None, :]])
+            continue
+        uw = max(1, min(plane.shape[1], -(-(W * c["h"]) // hmax)))
+        uh = max(1, min(plane.shape[0], -(-(H * c["v"]) // vmax)))
+        ys, xs = np.arange(fh), np.arange(fw)
+        yc = ys // sy if sy == 2 else ys
+        xc = xs // sx if sx == 2 else xs
+        yf = np.where(ys % 2 == 1, yc + 1, yc - 1) if sy == 2 else yc
+        xf = np.where(xs % 2 == 1, xc + 1, xc - 1) if sx == 2 else xc
+        S = lambda yy, xx: plane[np.clip(yy, 0, uh - 1)[:, None], np.clip(xx, 0, uw - 1)[None, :]]
+        if sx == 2 and sy == 2:
+            out = (3 * (3 * S(yc, xc) + S(yf, xc)) + (3 * S(yc, xf) + S(yf, xf)) + 8) >> 4
+        elif sx == 2:
+            out = (3 * S(yc, xc) + S(yc, xf) + 2) >> 2
+        else:
+            out = (3 * S(yc, xc) + S(yf, xc) + 2) >> 2
+        full.append(out)
+    rgba = np.full((H, W, 4), 255, np.uint8)
+    if gray:
+        rgba[..., :3] = full[0][:H, :W, None]
+        return rgba
+    Y, cb, cr = (p[:H, :W].astype(np.float64) for p in full)
+    cb, cr = cb - 128.0, cr - 128.0
+    q = lambda v: np.clip(np.floor(v + 0.5), 0, 255).astype(np.uint8)
+    rgba[..., 0] = q(Y + 1.402 * cr)
+    rgba[..., 1] = q(Y - 0.344136 * cb - 0.714136 * cr)
+    rgba[..., 2] = q(Y + 1.772 * cb)
+    return rgba
+
+
+def sample_image(H, W, seed):
+    rng = np.random.default_rng(seed)
+    y, x = np.mgrid[0:H, 0:W]
+    img = np.stack([128 + 100 * np.sin(x / 7.0 + seed), 128 + 90 * np.cos(y / 5.0), (x * 3 + y * 2) % 256], -1)
+    img += rng.normal(0, 12, img.shape)
+    return np.clip(img, 0, 255).astype(np.uint8)
+
+
+CASES = [
+    dict(sampling=((1, 1), (1, 1), (1, 1))),                 # 4:4:4
+    dict(sampling=((2, 1), (1, 1), (1, 1))),                 # 4:2:2
+    dict(sampling=((2, 2), (1, 1), (1, 1))),                 # 4:2:0
+    dict(sampling=((1, 2), (1, 1), (1, 1))),                 # 4:4:0
+    dict(sampling=((4, 1), (1, 1), (1, 1))),                 # 4:1:1 (replicated chroma)
+    dict(sampling=((2, 2), (1, 1), (1, 1)), restart=3),
+    dict(sampling=((2, 2), (1, 1), (1, 1)), scans="separate"),
+    dict(sampling=((1, 1), (1, 1), (1, 1)), scans="separate", restart=5),
+    dict(gray=True),
+    dict(gray=True, restart=1),
+]
+
+
+@pytest.mark.parametrize("case", range(len(CASES)))
+def test_jpeg_decode_matches_restatement(R, case):
+    kw = CASES[case]
+    for seed, (H, W) in enumerate([(37, 53), (64, 64), (8, 9), (1, 17)]):
+        img = sample_image(H, W, seed + 10 * case)
+        data, comps, qts, layout = encode_jpeg(img, seed=seed, **kw)
+        got = R.decode_image(data)
+        want = reconstruct(comps, qts, layout, W, H, kw.get("gray", False))
+        assert got.shape == want.shape
+        d = np.abs(got.astype(np.int64) - want.astype(np.int64))
+        # the library sums the IDCT in another order: a value on a rounding boundary may move by one
+        assert d.max() <= 1 and (d == 0).mean() >= 0.999, (case, seed, d.max(), (d == 0).mean())
+        if not kw.get("gray"):
+            err = np.abs(got[..., :3].astype(np.int64) - img.astype(np.int64))
+            assert err.mean() < 12   # a lossy round trip, not a different image
+
+
+def test_jpeg_malformed_and_unsupported(R):
+    img = sample_image(16, 16, 1)
+    data = encode_jpeg(img)[0]
+    prog = data.replace(b"\xff\xc0", b"\xff\xc2", 1)   # progressive frame marker
+    cut = data[: len(data) // 2]
+    for bad in (prog, cut, data[:4] + b"\xff\xd9", b"\xff\xd8\xff\xc0\x00\x0b\x0c\x00\x10\x00\x10\x01\x01\x11\x00\xff\xd9"):
+        with pytest.raises(R.ReinaError) as e:
+            R.decode_image(bad)
+        assert e.value.code == R.REINA_ERR_IO
+
+
+@pytest.mark.skipif(not REF_TEXTURES.exists(), reason="reference texture files not present")
+def test_jpeg_reference_textures(R):
+    """The reference's JPEG textures decode; the tangent-space normal map points mostly along +z."""
+    alb = R.decode_image((REF_TEXTURES / "qgdpH_2K_Albedo.jpg").read_bytes())
+    nrm = R.decode_image((REF_TEXTURES / "qgdpH_2K_Normal.jpg").read_bytes())
+    assert alb.shape == (2048, 2048, 4) and nrm.shape == (2048, 2048, 4)
+    assert nrm[..., 2].mean() > 240 and abs(nrm[..., 0].mean() - 128) < 8 and abs(nrm[..., 1].mean() - 128) < 8
+    assert alb[..., 1].mean() > alb[..., 2].mean()   # a green-dominated albedo
