@@ -130,6 +130,22 @@ def _dist():
     return ws, rank, local
 
 
+def reduce_max_over_ranks(values, device: str) -> list:
+    """Per-rank timings reduced to their maximum over the replicas (the slowest replica sets the job's
+    time); the process group must be initialized."""
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(v) for v in values], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t.cpu()]
+
+
+def replica_throughput(world_size: int, units_per_rank: int, seconds: float) -> float:
+    """Whole-job throughput of N replicas: all ranks' units over the (max-reduced) time."""
+    return world_size * units_per_rank / seconds
+
+
 def _build_workload(R, ctx):
     import scenes
 
@@ -258,11 +274,7 @@ def run_ours(args) -> dict | None:
 
     mean_ms = float(np.mean(step_ms))
     if ws > 1:
-        import torch.distributed as dist
-
-        t = torch.tensor([mean_ms, e2e_s], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        mean_ms, e2e_s = float(t[0]), float(t[1])
+        mean_ms, e2e_s = reduce_max_over_ranks([mean_ms, e2e_s], "cuda")
     if rank != 0:
         return None
     peak, peak_kind = _peak_hbm()
@@ -271,7 +283,7 @@ def run_ours(args) -> dict | None:
     hits_np = d_hits.cpu().numpy().view(np.uint32)[:, 0]
     out = {
         "metric": METRIC,
-        "value": ws * n / (mean_ms * 1e-3),
+        "value": replica_throughput(ws, n, mean_ms * 1e-3),
         "unit": "rays/s",
         "n_gpus": ws,
         "steps": args.steps,
@@ -294,7 +306,7 @@ def run_ours(args) -> dict | None:
             "parallelism": f"replicas x{ws}",
             "hit_fraction": float((hits_np != 0xFFFFFFFF).mean()),
         },
-        "e2e": {"value": ws * n / e2e_s, "unit": "rays/s", "h2d_bytes_per_step": n * RAY_BYTES,
+        "e2e": {"value": replica_throughput(ws, n, e2e_s), "unit": "rays/s", "h2d_bytes_per_step": n * RAY_BYTES,
                 "d2h_bytes_per_step": n * HIT_BYTES},
         "gpu_launches": args.steps * 2,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
