@@ -402,7 +402,12 @@ void Scene::build_two_level() {
             }
         model_box[inst.object] = b;
     }
-    // world boxes of the instances: the 8 transformed corners of the model box, in double, rounded outward
+    // world boxes of the instances, in double and rounded outward: the box of the model's transformed
+    // vertices when that is affordable (at most 2^26 vertex transforms in all), else of the 8 transformed
+    // corners of the model box (looser for rotated instances)
+    uint64_t transforms = 0;
+    for (const InstanceRecord& inst : instances_) transforms += models_[inst.object].vertices.size() / 4;
+    const bool exact = transforms <= (1ull << 26);
     std::vector<float> boxes(6 * ninst);
     for (int k = 0; k < 3; ++k) { bounds_lo_[k] = INFINITY; bounds_hi_[k] = -INFINITY; }
     for (size_t ii = 0; ii < ninst; ++ii) {
@@ -411,13 +416,23 @@ void Scene::build_two_level() {
         const float* T = inst.transform;
         double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
         const bool empty = ranges_[inst.object].index_count == 0;
-        for (int c = 0; c < 8 && !empty; ++c) {
-            const double p[3] = {mb[(c & 1) ? 3 : 0], mb[(c & 2) ? 4 : 1], mb[(c & 4) ? 5 : 2]};
+        auto add = [&](const double p[3]) {
             for (int r = 0; r < 3; ++r) {
                 const double w = T[0 * 4 + r] * p[0] + T[1 * 4 + r] * p[1] + T[2 * 4 + r] * p[2] + T[3 * 4 + r];
                 lo[r] = std::min(lo[r], w);
                 hi[r] = std::max(hi[r], w);
             }
+        };
+        if (!empty && exact) {
+            const ModelData& md = models_[inst.object];   // every vertex (unreferenced ones only loosen the box)
+            for (size_t vi = 0; vi < md.vertices.size() / 4; ++vi) {
+                const double p[3] = {md.vertices[4 * vi], md.vertices[4 * vi + 1], md.vertices[4 * vi + 2]};
+                add(p);
+            }
+        }
+        for (int c = 0; c < 8 && !empty && !exact; ++c) {
+            const double p[3] = {mb[(c & 1) ? 3 : 0], mb[(c & 2) ? 4 : 1], mb[(c & 4) ? 5 : 2]};
+            add(p);
         }
         for (int r = 0; r < 3; ++r) {
             if (empty) { lo[r] = hi[r] = T[3 * 4 + r]; }
