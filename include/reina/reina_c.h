@@ -561,6 +561,16 @@ int reina_save_schedule_next(reina_save_schedule* schedule, uint64_t samples, do
  * the tone-mapped image with stb_image_write, src/Reina.cpp:19-47). */
 int reina_write_png(const char* path, const uint8_t* rgba8, uint32_t width, uint32_t height);
 
+/* Device self-check: evaluates single device shading functions on fixed inputs (case records of 40
+ * floats, host buffers; 4 floats out per case) so that a port can pin them against known answers:
+ *   REINA_KAT_OFFSET      offsetPositionAlongNormal (closestHitCommon.h.glsl:156-177): p = r[0..2], n = r[3..5]
+ *   REINA_KAT_GGX_VNDF    sampleGGXVNDF (brdfDisney.h.glsl:9-40): V = r[0..2], ax = r[6], ay = r[7], RNG
+ *                         state = bits of r[8]; out[3] = the RNG state after the two draws (bits)
+ *   REINA_KAT_EVAL_DISNEY evalDisney (brdfDisney.h.glsl:656-711): parameters in r[0..18], n r[19..21],
+ *                         wi r[22..24], wo r[25..27], TBN columns r[28..36]; out = f, pdf */
+enum { REINA_KAT_OFFSET = 0, REINA_KAT_GGX_VNDF = 1, REINA_KAT_EVAL_DISNEY = 2 };
+int reina_device_kat(reina_ctx* ctx, int kind, const float* records, uint64_t count, float* out);
+
 /* ------------------------------------------------------------------------------------------------ */
 /* Autotuner                                                                                          */
 /* ------------------------------------------------------------------------------------------------ */

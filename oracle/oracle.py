@@ -143,6 +143,18 @@ def bvh8_two_level_raycast(nodes, tris, refs, inst_records, rays, any_hit: bool 
     return hits, nv.value, nt.value
 
 
+_SHADING_SIGS["oracle_kat"] = (None, [C.c_int, C.c_void_p, C.c_uint64, C.c_int, C.c_void_p])
+KAT_OFFSET, KAT_GGX_VNDF, KAT_EVAL_DISNEY = 0, 1, 2
+
+
+def kat(kind: int, records: np.ndarray, precision: int = 32) -> np.ndarray:
+    """Single shading functions on 40-float case records (see oracle_kat.cpp): (n, 4) float64."""
+    r = np.ascontiguousarray(records, np.float32).reshape(-1, 40)
+    out = np.zeros((r.shape[0], 4), np.float64)
+    lib().oracle_kat(kind, _p(r), r.shape[0], precision, _p(out))
+    return out
+
+
 class Bvh:
     def __init__(self, tris9: np.ndarray):
         self.tris = np.ascontiguousarray(tris9, dtype=np.float32).reshape(-1, 9)

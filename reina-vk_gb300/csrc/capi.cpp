@@ -19,6 +19,7 @@
 #include "errors.h"
 #include "generators.h"
 #include "image.h"
+#include "kat.h"
 #include "kernels.h"
 #include "loaders.h"
 #include "post.h"
@@ -1149,6 +1150,22 @@ int reina_scene_define_texture_encoded(reina_scene* scene, const void* data, uin
     return guard([&] {
         need(scene && scene->s && data && out_id, "NULL argument");
         *out_id = scene->s->define_texture(rt::decode_image(static_cast<const uint8_t*>(data), (size_t)bytes));
+    });
+}
+
+int reina_device_kat(reina_ctx* ctx, int kind, const float* records, uint64_t count, float* out) {
+    return guard([&] {
+        need(ctx != nullptr, "ctx is NULL");
+        need(kind >= REINA_KAT_OFFSET && kind <= REINA_KAT_EVAL_DISNEY, "unknown kind");
+        need(count == 0 || (records && out), "NULL buffer");
+        need(count < (1ull << 24), "at most 2^24 cases per call");
+        use_device(ctx);
+        if (count == 0) return;
+        rt::DeviceBuffer d_rec(count * rt::kKatRecordFloats * sizeof(float)), d_out(count * 4 * sizeof(float));
+        check_cuda(cudaMemcpy(d_rec.get(), records, d_rec.bytes(), cudaMemcpyHostToDevice), "cudaMemcpy H2D");
+        rt::launch_kat(kind, d_rec.as<float>(), (uint32_t)count, d_out.as<float>(), nullptr);
+        check_cuda(cudaGetLastError(), "kat launch");
+        check_cuda(cudaMemcpy(out, d_out.get(), d_out.bytes(), cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
     });
 }
 

@@ -329,6 +329,7 @@ def load_library() -> C.CDLL:
         "reina_scene_define_texture_encoded": (I32, [P, P, U64, C.POINTER(U32)]),
         "reina_scene_texture_count": (I32, [P, C.POINTER(U32)]),
         "reina_scene_set_accel": (I32, [P, C.c_int]),
+        "reina_device_kat": (I32, [P, C.c_int, P, U64, P]),
         "reina_scene_export_two_level": (I32, [P, P, P, C.POINTER(U32), C.POINTER(U32)]),
         "reina_scene_export_properties": (I32, [P, P, U32, C.POINTER(U32)]),
         "reina_scene_export_texture": (I32, [P, U32, C.POINTER(U32), C.POINTER(U32), P, U64]),
@@ -917,6 +918,17 @@ class SaveSchedule:
             self.close()
         except Exception:
             pass
+
+
+KAT_OFFSET, KAT_GGX_VNDF, KAT_EVAL_DISNEY = 0, 1, 2
+
+
+def device_kat(ctx: "Context", kind: int, records: np.ndarray) -> np.ndarray:
+    """reina_device_kat: single device shading functions on 40-float case records -> (n, 4) float32."""
+    r = np.ascontiguousarray(records, np.float32).reshape(-1, 40)
+    out = np.zeros((r.shape[0], 4), np.float32)
+    _check(load_library().reina_device_kat(ctx._h, kind, _ptr(r), r.shape[0], _ptr(out)))
+    return out
 
 
 def decode_image(data: bytes) -> np.ndarray:

@@ -6,6 +6,8 @@ Python/numpy independently of the oracle's C++ (the reference itself ships no te
 rng_kat.json: `random()` of shaders/raytrace/shaderCommon.h.glsl:39-45 — state' = state*747796405 + 1
 (mod 2^32), word = ((state' >> ((state' >> 28) + 4)) ^ state') * 277803737, word ^= word >> 22,
 value = float(word) / 4294967295.0f — for the seeds {0, 1, 0xFFFFFFFF, 12345, 65536*256+7}, 16 draws each.
+offset_kat.json: offsetPositionAlongNormal (closestHitCommon.h.glsl:156-177) on float32 points and normals.
+ggx_kat.json: sampleGGXVNDF (brdfDisney.h.glsl:9-40) in float64 with the shader RNG's draws.
 """
 from __future__ import annotations
 
@@ -92,6 +94,49 @@ def bloom_f32(img: np.ndarray, radius: float, threshold: float, intensity: float
     return res
 
 
+def offset_f32(p: np.ndarray, n: np.ndarray) -> np.ndarray:
+    """offsetPositionAlongNormal (closestHitCommon.h.glsl:156-177) in float32: of_i = int(256 * n)
+    (truncation toward zero), p's bit pattern moved by of_i away from zero, and p + n / 65536 where
+    |p| < 1/32."""
+    p = p.astype(F)
+    n = n.astype(F)
+    of_i = np.trunc((F(256.0) * n).astype(F)).astype(np.int64)
+    bits = p.view(np.int32).astype(np.int64)
+    moved = np.where(p < 0, bits - of_i, bits + of_i).astype(np.int32).view(F)
+    near = (p + (F(1.0 / 65536.0) * n).astype(F)).astype(F)
+    return np.where(np.abs(p) < F(1.0 / 32.0), near, moved).astype(F)
+
+
+def ggx_vndf_f64(V, ax, ay, seed):
+    """sampleGGXVNDF (brdfDisney.h.glsl:9-40) in float64 with the shader RNG's two draws and the shaders'
+    k_pi = 3.14159265; returns the half vector and the RNG state after the draws."""
+    w = rng_words(seed, 2)
+    s = seed & M32
+    for _ in range(2):
+        s = (s * 747796405 + 1) & M32
+    r1, r2 = w[0] / 4294967295.0, w[1] / 4294967295.0
+    V = np.array(V, np.float64)
+    flip = V[2] < 0
+    if flip:
+        V[2] = -V[2]
+    Vh = np.array([ax * V[0], ay * V[1], V[2]])
+    Vh = Vh / np.sqrt(Vh @ Vh)
+    lensq = Vh[0] ** 2 + Vh[1] ** 2
+    T1 = np.array([-Vh[1], Vh[0], 0.0]) * (1.0 / np.sqrt(lensq)) if lensq > 0 else np.array([1.0, 0.0, 0.0])
+    T2 = np.cross(Vh, T1)
+    r = np.sqrt(r1)
+    phi = 2.0 * 3.14159265 * r2   # k_pi of shaderCommon.h.glsl:47, not the exact pi
+    t1 = r * np.cos(phi)
+    t2 = r * np.sin(phi)
+    sm = 0.5 * (1.0 + Vh[2])
+    t2 = (1.0 - sm) * np.sqrt(1.0 - t1 * t1) + sm * t2
+    Nh = T1 * t1 + T2 * t2 + Vh * np.sqrt(max(0.0, 1.0 - t1 * t1 - t2 * t2))
+    if flip:
+        Nh[2] = -Nh[2]
+    h = np.array([ax * Nh[0], ay * Nh[1], max(0.0, Nh[2])])
+    return (h / np.sqrt(h @ h)).tolist(), s
+
+
 def main() -> None:
     seeds = [0, 1, 0xFFFFFFFF, 12345, 65536 * 256 + 7]
     rng = {}
@@ -119,6 +164,32 @@ def main() -> None:
     (HERE / "bloom_kat.json").write_text(json.dumps({"radius": 25.0, "threshold": 1.0, "intensity": 0.3,
                                                      "image": img.tolist(), "combined": combined.tolist()}) + "\n")
     print("wrote", HERE / "bloom_kat.json")
+
+    # offset: points near and away from the origin threshold, both signs, large magnitudes; unit normals
+    pts = np.concatenate([g.uniform(-2, 2, (40, 3)), g.uniform(-0.04, 0.04, (20, 3)), g.uniform(-3e4, 3e4, (8, 3)),
+                          np.array([[0.0, -0.0, 1.0 / 32.0], [-1.0 / 32.0, 1e-30, 5e-39]])]).astype(F)
+    nrm = g.normal(size=(pts.shape[0], 3))
+    nrm = (nrm / np.linalg.norm(nrm, axis=1, keepdims=True)).astype(F)
+    off = offset_f32(pts, nrm)
+    (HERE / "offset_kat.json").write_text(json.dumps({
+        "p_bits": pts.view(np.uint32).tolist(), "n_bits": nrm.view(np.uint32).tolist(),
+        "out_bits": off.view(np.uint32).tolist()}) + "\n")
+    print("wrote", HERE / "offset_kat.json")
+
+    # GGX VNDF: view directions on both hemispheres, isotropic and anisotropic roughness, several seeds
+    cases = []
+    for k in range(48):
+        v = g.normal(size=3)
+        v /= np.linalg.norm(v)
+        ax, ay = float(g.uniform(0.01, 1.0)), float(g.uniform(0.01, 1.0)) if k % 2 else None
+        ay = ax if ay is None else ay
+        seed = int(g.integers(0, 2 ** 32))
+        vf = [float(F(x)) for x in v]
+        axf, ayf = float(F(ax)), float(F(ay))
+        h, s_after = ggx_vndf_f64(vf, axf, ayf, seed)
+        cases.append({"V": vf, "ax": axf, "ay": ayf, "seed": seed, "h": h, "state_after": s_after})
+    (HERE / "ggx_kat.json").write_text(json.dumps(cases, indent=0) + "\n")
+    print("wrote", HERE / "ggx_kat.json")
 
 
 if __name__ == "__main__":
