@@ -65,7 +65,7 @@ void reina_ctx_destroy(reina_ctx* ctx);
 int reina_ctx_sm_count(const reina_ctx* ctx);
 
 /* Launch parameters of the traversal kernels and of batched renders (no counterpart in the reference,
- * whose traversal and scheduling are the driver's).  Every setting gives the same results; only speed
+ * whose traversal and scheduling belong to the Vulkan implementation).  Every setting gives the same results; only speed
  * differs.  0 selects the default of a field.
  *   refill = 0: one thread per ray (grid form, the default); refill = 1..32: persistent warps that fetch
  *            new rays when `refill` of their 32 lanes are idle (block 128, stack 12).
