@@ -528,8 +528,8 @@ int reina_scene_export_object(const reina_scene* scene, uint32_t object_id, floa
                               float* tex_coords2, uint64_t* tex_coord_count);
 
 /* config/config.toml as the reference reads it (src/Reina.cpp:142-156,185,243-245;
- * src/tools/SaveManager.cpp:6-24).  Every key is required; defocus_multiplier is divided by 100 as in
- * src/Reina.cpp:150.  At most 64 save points of each kind. */
+ * src/tools/SaveManager.cpp:6-24).  Every key the reference reads is required; defocus_multiplier is
+ * divided by 100 as in src/Reina.cpp:150.  At most 64 save points of each kind. */
 enum { REINA_CONFIG_MAX_SAVES = 64 };
 typedef struct reina_config {
     float focus_dist;
@@ -544,6 +544,17 @@ typedef struct reina_config {
     uint32_t save_on_times_count;
     int64_t save_on_samples[REINA_CONFIG_MAX_SAVES];
     double save_on_times[REINA_CONFIG_MAX_SAVES];
+    /* optional keys of this build, defaulting to the reference's hard-coded values
+     * (src/Reina.cpp:54-55,91,138-140): [render] width, height, seed, mode = "reina" | "nee";
+     * [scene] path; [camera] pos = [x, y, z], look_at = [x, y, z], fov (degrees) */
+    uint32_t width;
+    uint32_t height;
+    uint32_t seed;
+    uint32_t mode;               /* REINA_MODE_REINA or REINA_MODE_NEE_MIS */
+    char scene_path[512];        /* "" when absent */
+    float camera_pos[3];
+    float look_at[3];
+    float fov_degrees;
 } reina_config;
 int reina_config_load(const char* path, reina_config* out_config);
 

@@ -31,7 +31,9 @@ bool ends_with(const std::string& s, const std::string& e) {
 
 void usage() {
     std::printf(
-        "usage: reina_render --config config.toml --scene file.{glb,gltf,obj} [options]\n"
+        "usage: reina_render --config config.toml [--scene file.{glb,gltf,obj}] [options]\n"
+        "  (defaults from the config's optional [render] width/height/seed/mode, [scene] path and\n"
+        "   [camera] pos/look_at/fov keys, else the reference's hard-coded values)\n"
         "  --width W --height H        image size (default 1080 x 1350)\n"
         "  --camera x,y,z              camera position (default -1.6899,0.317017,1.6386)\n"
         "  --look-at x,y,z             target (default 0,0.962,0)\n"
@@ -46,11 +48,11 @@ void usage() {
 
 int main(int argc, char** argv) {
     std::string config_path, scene_path, out_dir = ".", env = "sky";
-    uint32_t W = 1080, H = 1350, frames = 16, seed = 1, mode = REINA_MODE_REINA;
+    uint32_t W = 0, H = 0, frames = 16, seed = 0, mode = 0;
     double seconds = 0.0;
     int device = 0;
-    bool allow_no_emissive = false;
-    float cam[3] = {-1.6899f, 0.317017f, 1.6386f}, target[3] = {0.0f, 0.962f, 0.0f}, fov = 25.0f;
+    bool allow_no_emissive = false, set_cam = false, set_target = false, set_mode = false, set_seed = false;
+    float cam[3], target[3], fov = 0.0f;
     for (int i = 1; i < argc; ++i) {
         const std::string a = argv[i];
         auto val = [&]() -> const char* {
@@ -61,8 +63,8 @@ int main(int argc, char** argv) {
         else if (a == "--scene") scene_path = val();
         else if (a == "--width") W = (uint32_t)std::atoi(val());
         else if (a == "--height") H = (uint32_t)std::atoi(val());
-        else if (a == "--camera") { if (!parse3(val(), cam)) die("--camera wants x,y,z"); }
-        else if (a == "--look-at") { if (!parse3(val(), target)) die("--look-at wants x,y,z"); }
+        else if (a == "--camera") { if (!parse3(val(), cam)) die("--camera wants x,y,z"); set_cam = true; }
+        else if (a == "--look-at") { if (!parse3(val(), target)) die("--look-at wants x,y,z"); set_target = true; }
         else if (a == "--fov") fov = (float)std::atof(val());
         else if (a == "--frames") frames = (uint32_t)std::atoi(val());
         else if (a == "--seconds") seconds = std::atof(val());
@@ -72,18 +74,30 @@ int main(int argc, char** argv) {
             if (m == "reina") mode = REINA_MODE_REINA;
             else if (m == "nee") mode = REINA_MODE_NEE_MIS;
             else die("--mode is reina or nee");
-        } else if (a == "--seed") seed = (uint32_t)std::atoi(val());
+            set_mode = true;
+        } else if (a == "--seed") { seed = (uint32_t)std::atoi(val()); set_seed = true; }
         else if (a == "--device") device = std::atoi(val());
         else if (a == "--env") env = val();
         else if (a == "--allow-no-emissive") allow_no_emissive = true;
         else if (a == "--help" || a == "-h") { usage(); return 0; }
         else die("unknown option " + a);
     }
-    if (config_path.empty() || scene_path.empty()) { usage(); return 2; }
-    if (W == 0 || H == 0) die("image size must be positive");
-
+    if (config_path.empty()) { usage(); return 2; }
+    // the config's optional [render] / [scene] / [camera] keys are the defaults; options override them
     reina_config cfg;
     check(reina_config_load(config_path.c_str(), &cfg), "config");
+    if (scene_path.empty()) scene_path = cfg.scene_path;
+    if (scene_path.empty()) { usage(); return 2; }
+    if (W == 0) W = cfg.width;
+    if (H == 0) H = cfg.height;
+    if (!set_seed) seed = cfg.seed;
+    if (!set_mode) mode = cfg.mode;
+    if (fov == 0.0f) fov = cfg.fov_degrees;
+    for (int k = 0; k < 3; ++k) {
+        if (!set_cam) cam[k] = cfg.camera_pos[k];
+        if (!set_target) target[k] = cfg.look_at[k];
+    }
+    if (W == 0 || H == 0) die("image size must be positive");
     reina_ctx* ctx = nullptr;
     reina_ctx_options co{device, 0};
     check(reina_ctx_create(&co, &ctx), "context");

@@ -1273,6 +1273,17 @@ int reina_config_load(const char* path, reina_config* out) {
         out->save_on_times_count = (uint32_t)c.save_on_times.size();
         for (size_t k = 0; k < c.save_on_samples.size(); ++k) out->save_on_samples[k] = c.save_on_samples[k];
         for (size_t k = 0; k < c.save_on_times.size(); ++k) out->save_on_times[k] = c.save_on_times[k];
+        out->width = c.width;
+        out->height = c.height;
+        out->seed = c.seed;
+        out->mode = c.mode;
+        need(c.scene_path.size() < sizeof(out->scene_path), "scene.path longer than 511 bytes");
+        std::memcpy(out->scene_path, c.scene_path.c_str(), c.scene_path.size() + 1);
+        for (int k = 0; k < 3; ++k) {
+            out->camera_pos[k] = c.camera_pos[k];
+            out->look_at[k] = c.look_at[k];
+        }
+        out->fov_degrees = c.fov_degrees;
     });
 }
 

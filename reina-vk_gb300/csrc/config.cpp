@@ -180,6 +180,34 @@ RunConfig config_from_toml(const std::string& text, const std::string& name) {
     c.bloom_threshold = (float)num("postprocessing.bloom.threshold");
     c.bloom_intensity = (float)num("postprocessing.bloom.intensity");
     c.exposure = (float)num("postprocessing.tonemap.exposure");
+    // optional keys
+    auto has = [&](const std::string& k) { return t.find(k) != t.end(); };
+    if (has("render.width")) c.width = uint("render.width");
+    if (has("render.height")) c.height = uint("render.height");
+    if (has("render.seed")) c.seed = uint("render.seed");
+    if (has("render.mode")) {
+        const TomlValue& v = need("render.mode");
+        if (v.kind != TomlValue::String || (v.s != "reina" && v.s != "nee")) fail(REINA_ERR_IO, name + ": render.mode is \"reina\" or \"nee\"");
+        c.mode = v.s == "nee" ? 1u : 0u;
+    }
+    if (has("scene.path")) {
+        const TomlValue& v = need("scene.path");
+        if (v.kind != TomlValue::String) fail(REINA_ERR_IO, name + ": scene.path must be a string");
+        c.scene_path = v.s;
+    }
+    auto vec3 = [&](const std::string& k, float out[3]) {
+        const TomlValue& v = need(k);
+        if (v.kind != TomlValue::Array || v.arr.size() != 3) fail(REINA_ERR_IO, name + ": " + k + " must be an array of 3 numbers");
+        for (int i = 0; i < 3; ++i) {
+            if (v.arr[(size_t)i].kind != TomlValue::Int && v.arr[(size_t)i].kind != TomlValue::Float)
+                fail(REINA_ERR_IO, name + ": " + k + " must be an array of 3 numbers");
+            out[i] = (float)v.arr[(size_t)i].as_double();
+        }
+    };
+    if (has("camera.pos")) vec3("camera.pos", c.camera_pos);
+    if (has("camera.look_at")) vec3("camera.look_at", c.look_at);
+    if (has("camera.fov")) c.fov_degrees = (float)num("camera.fov");
+    if (c.width == 0 || c.height == 0) fail(REINA_ERR_IO, name + ": render.width and render.height must be positive");
     return c;
 }
 

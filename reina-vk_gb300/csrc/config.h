@@ -34,8 +34,18 @@ struct RunConfig {
     std::vector<double> save_on_times;
     float bloom_radius = 5.0f, bloom_threshold = 1.0f, bloom_intensity = 0.05f;
     float exposure = 0.0f;
+    // Optional keys of this build (the reference hard-codes these, src/Reina.cpp:54-55,91,138-140; the
+    // defaults are its values): [render] width, height, seed, mode ("reina" | "nee"); [scene] path;
+    // [camera] pos, look_at (3-element arrays), fov (degrees).
+    uint32_t width = 1080, height = 1350, seed = 1;
+    uint32_t mode = 0;   // 0 reina, 1 NEE + MIS
+    std::string scene_path;
+    float camera_pos[3] = {-1.6899f, 0.317017f, 1.6386f};
+    float look_at[3] = {0.0f, 0.962f, 0.0f};
+    float fov_degrees = 25.0f;
 };
-// Every key the reference reads is required (the reference's .value() throws when one is missing).
+// Every key the reference reads is required (the reference's .value() throws when one is missing); the
+// optional keys above keep their defaults when absent.
 RunConfig load_config(const std::string& path);
 RunConfig config_from_toml(const std::string& text, const std::string& name);
 

@@ -191,7 +191,10 @@ class RunConfig(C.Structure):
                 ("max_bounces", C.c_uint32), ("direct_clamp", C.c_float), ("indirect_clamp", C.c_float),
                 ("bloom", BloomPushConsts), ("tonemap", TonemappingPushConsts),
                 ("save_on_samples_count", C.c_uint32), ("save_on_times_count", C.c_uint32),
-                ("save_on_samples", C.c_int64 * CONFIG_MAX_SAVES), ("save_on_times", C.c_double * CONFIG_MAX_SAVES)]
+                ("save_on_samples", C.c_int64 * CONFIG_MAX_SAVES), ("save_on_times", C.c_double * CONFIG_MAX_SAVES),
+                ("width", C.c_uint32), ("height", C.c_uint32), ("seed", C.c_uint32), ("mode", C.c_uint32),
+                ("scene_path", C.c_char * 512), ("camera_pos", C.c_float * 3), ("look_at", C.c_float * 3),
+                ("fov_degrees", C.c_float)]
 
 
 class _RenderJob(C.Structure):

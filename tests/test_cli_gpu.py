@@ -52,3 +52,30 @@ def test_cli_renders_and_saves(R, tmp_path):
         s.close()
     finally:
         ctx.close()
+
+
+def test_cli_takes_scene_and_camera_from_config(R, tmp_path):
+    """The config's optional [render] / [scene] / [camera] keys stand in for the options: the same image
+    as passing them on the command line."""
+    import build as pkg_build
+
+    pkg_build.build()
+    cli = pkg_build.CLI
+    base = (CONFIG.replace("save_on_samples = [300, 100, 200]", "save_on_samples = []")
+            .replace("save_on_times = [30.5, 10]", "save_on_times = []"))
+    (tmp_path / "s.glb").write_bytes(make_gltf(True))
+    (tmp_path / "plain.toml").write_text(base)
+    (tmp_path / "keys.toml").write_text(base + f'\n[render]\nwidth = 40\nheight = 32\nseed = 3\nmode = "nee"\n'
+                                        f'[scene]\npath = "{tmp_path / "s.glb"}"\n'
+                                        f'[camera]\npos = [1, 0.5, 6]\nlook_at = [1, 0.5, 0]\nfov = 40\n')
+    outs = []
+    for name, extra in (("plain", ["--scene", str(tmp_path / "s.glb"), "--width", "40", "--height", "32", "--seed", "3",
+                                   "--mode", "nee", "--camera", "1,0.5,6", "--look-at", "1,0.5,0", "--fov", "40"]),
+                        ("keys", [])):
+        out = tmp_path / name
+        out.mkdir()
+        res = subprocess.run([str(cli), "--config", str(tmp_path / f"{name}.toml"), "--frames", "2", "--out", str(out),
+                              *extra], capture_output=True, text=True, timeout=300)
+        assert res.returncode == 0, res.stderr
+        outs.append(read_png((out / "output_final.png").read_bytes()))
+    assert outs[0].shape == (32, 40, 4) and np.array_equal(outs[0], outs[1])

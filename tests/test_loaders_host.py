@@ -250,6 +250,27 @@ def test_config_and_schedule(R, tmp_path):
     assert sch.next(10 ** 9, 1e9) == ""
 
 
+def test_config_optional_keys(R, tmp_path):
+    """Absent: the reference's hard-coded values (src/Reina.cpp:54-55,91,138-140); present: read."""
+    p = tmp_path / "config.toml"
+    p.write_text(CONFIG)
+    c = R.load_config(p)
+    assert (c.width, c.height, c.seed, c.mode) == (1080, 1350, 1, R.MODE_REINA)
+    assert c.scene_path == b"" and c.fov_degrees == 25.0
+    assert list(c.camera_pos) == pytest.approx([-1.6899, 0.317017, 1.6386]) and list(c.look_at) == pytest.approx([0, 0.962, 0])
+    p.write_text(CONFIG + '\n[render]\nwidth = 320\nheight = 200\nseed = 9\nmode = "nee"\n[scene]\npath = "scenes/a b.glb"\n'
+                 '[camera]\npos = [1, 2.5, -3]\nlook_at = [0, 0, 0]\nfov = 40.5\n')
+    c = R.load_config(p)
+    assert (c.width, c.height, c.seed, c.mode) == (320, 200, 9, R.MODE_NEE_MIS)
+    assert c.scene_path == b"scenes/a b.glb" and c.fov_degrees == pytest.approx(40.5)
+    assert list(c.camera_pos) == [1.0, 2.5, -3.0] and list(c.look_at) == [0.0, 0.0, 0.0]
+    for bad in ('[render]\nmode = "fast"\n', '[camera]\npos = [1, 2]\n', '[render]\nwidth = 0\n'):
+        p.write_text(CONFIG + "\n" + bad)
+        with pytest.raises(R.ReinaError) as e:
+            R.load_config(p)
+        assert e.value.code == R.REINA_ERR_IO
+
+
 @pytest.mark.parametrize("drop", ["max_bounces", "exposure", "save_on_times"])
 def test_config_missing_key(R, tmp_path, drop):
     p = tmp_path / "config.toml"
