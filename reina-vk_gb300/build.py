@@ -89,6 +89,39 @@ def build(force: bool = False, ptxas_verbose: bool = False, verbose: bool = Fals
     return LIB
 
 
+OUT_CHECKED = PKG / "_build_checked"
+LIB_CHECKED = OUT_CHECKED / "libreina_gb300.so"
+
+
+def build_checked(force: bool = False) -> Path:
+    """The checked build: every CUDA source again with -DRT_CHECKED (the wavefront kernels check each queue
+    position and path index and flag, instead of making, an out-of-bounds access), linked with the host
+    objects of the normal build into `_build_checked/libreina_gb300.so`.  Not part of build()."""
+    build()
+    OUT_CHECKED.mkdir(exist_ok=True)
+    newest_header = max((h.stat().st_mtime for h in _headers()), default=0.0)
+    objs, jobs = [], []
+    for src in sorted(list(CSRC.glob("*.cu")) + list(CSRC.glob("*.cpp"))):
+        if src.suffix != ".cu":
+            objs.append(OUT / (src.name + ".o"))
+            continue
+        obj = OUT_CHECKED / (src.name + ".o")
+        objs.append(obj)
+        if force or _stale(obj, src, newest_header):
+            jobs.append([NVCC, *ARCH, *NVCCFLAGS, "-DRT_CHECKED", *INCLUDES, "-c", str(src), "-o", str(obj)])
+    if jobs:
+        with cf.ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
+            for res in ex.map(lambda c: subprocess.run(c, capture_output=True, text=True), jobs):
+                if res.returncode != 0:
+                    raise RuntimeError(f"checked build failed:\n{res.stdout}\n{res.stderr}")
+    if force or jobs or not LIB_CHECKED.exists() or any(LIB_CHECKED.stat().st_mtime < o.stat().st_mtime for o in objs):
+        cmd = [NVCC, *ARCH, "-shared", "-o", str(LIB_CHECKED), *map(str, objs), "-lpthread", "-ldl", "-lrt"]
+        res = subprocess.run(cmd, capture_output=True, text=True)
+        if res.returncode != 0:
+            raise RuntimeError(f"checked link failed: {' '.join(cmd)}\n{res.stdout}\n{res.stderr}")
+    return LIB_CHECKED
+
+
 CLI_SRC = PKG / "cli" / "reina_render.cpp"
 CLI = OUT / "reina_render"
 

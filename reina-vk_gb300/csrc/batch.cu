@@ -87,7 +87,7 @@ __global__ void __launch_bounds__(kBlock) kb_init(BatchLaunch B, const JobGpu* _
         const uint32_t i = base + threadIdx.x;
         const bool live = i < n && init_slot(B, jobs, i);
         const uint32_t pos = warp_append(ps.counters + kCntActive, live);
-        if (live) ps.q_active[0][pos] = i;
+        if (live) ps.q_active[0][checked_index(pos, B.P, ps.counters + kCntError)] = i;
     }
 }
 
@@ -103,7 +103,7 @@ __global__ void __launch_bounds__(BLOCK) kb_extend(BatchLaunch B, const JobGpu* 
         int m = -1;
         uint32_t p = 0;
         if (active) {
-            p = q[i];
+            p = checked_index(q[i], B.P, ps.counters + kCntError);
             const DeviceScene& s = jobs[B.bp.job[p]].s;
             const TraceRay r = make_trace_ray(ps.ox[p], ps.oy[p], ps.oz[p], ps.dx[p], ps.dy[p], ps.dz[p], 0.0f, 10000.0f);
             Hit h;
@@ -122,7 +122,7 @@ __global__ void __launch_bounds__(BLOCK) kb_extend(BatchLaunch B, const JobGpu* 
         for (int k = 0; k < kNumQueues; ++k) {
             const bool mine = active && m == k;
             const uint32_t pos = warp_append(ps.counters + kCntQueue + k, mine);
-            if (mine) ps.q_shade[(size_t)k * B.P + pos] = p;
+            if (mine) ps.q_shade[(size_t)k * B.P + checked_index(pos, B.P, ps.counters + kCntError)] = p;
         }
     }
 }
@@ -139,7 +139,7 @@ __global__ void __launch_bounds__(kBlock, kShadeMinBlocks) kb_shade(BatchLaunch 
         ShadowRec sh;
         uint32_t p = 0;
         if (active) {
-            p = q[i];
+            p = checked_index(q[i], B.P, ps.counters + kCntError);
             const JobGpu& J = jobs[B.bp.job[p]];
             const bool nee = J.mode == kModeNeeMis;
             const V3 ro{ps.ox[p], ps.oy[p], ps.oz[p]};
@@ -189,14 +189,15 @@ __global__ void __launch_bounds__(kBlock, kShadeMinBlocks) kb_shade(BatchLaunch 
             cont = dep < J.max_bounces;
         }
         const uint32_t pos = warp_append(ps.counters + kCntActive + (cur ^ 1), cont);
-        if (cont) ps.q_active[cur ^ 1][pos] = p;
+        if (cont) ps.q_active[cur ^ 1][checked_index(pos, B.P, ps.counters + kCntError)] = p;
         const uint32_t spos = warp_append(ps.counters + kCntShadow, emit);
         if (emit) {
-            ps.q_shadow[spos] = p;
-            ps.s_ox[spos] = sh.o.x; ps.s_oy[spos] = sh.o.y; ps.s_oz[spos] = sh.o.z;
-            ps.s_dx[spos] = sh.d.x; ps.s_dy[spos] = sh.d.y; ps.s_dz[spos] = sh.d.z;
-            ps.s_tmax[spos] = sh.tmax;
-            ps.s_cr[spos] = sh.contrib.x; ps.s_cg[spos] = sh.contrib.y; ps.s_cb[spos] = sh.contrib.z;
+            const uint32_t sp_ = checked_index(spos, B.P, ps.counters + kCntError);
+            ps.q_shadow[sp_] = p;
+            ps.s_ox[sp_] = sh.o.x; ps.s_oy[sp_] = sh.o.y; ps.s_oz[sp_] = sh.o.z;
+            ps.s_dx[sp_] = sh.d.x; ps.s_dy[sp_] = sh.d.y; ps.s_dz[sp_] = sh.d.z;
+            ps.s_tmax[sp_] = sh.tmax;
+            ps.s_cr[sp_] = sh.contrib.x; ps.s_cg[sp_] = sh.contrib.y; ps.s_cb[sp_] = sh.contrib.z;
         }
     }
 }
@@ -205,7 +206,7 @@ __global__ void __launch_bounds__(kBlock) kb_shade_miss(BatchLaunch B, const Job
     const PathState& ps = B.bp.ps;
     const uint32_t n = ps.counters[kCntQueue + kQueueMiss];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint32_t p = ps.q_shade[i];
+        const uint32_t p = checked_index(ps.q_shade[i], B.P, ps.counters + kCntError);
         const JobGpu& J = jobs[B.bp.job[p]];
         V3 sky;
         if (J.env_mode == 1) {
@@ -228,7 +229,7 @@ __global__ void __launch_bounds__(BLOCK) kb_shadow(BatchLaunch B, const JobGpu* 
         const uint32_t i = base + threadIdx.x;
         const bool active = i < n;
         if (active) {
-            const uint32_t p = ps.q_shadow[i];
+            const uint32_t p = checked_index(ps.q_shadow[i], B.P, ps.counters + kCntError);
             const DeviceScene& s = jobs[B.bp.job[p]].s;
             const TraceRay r = make_trace_ray(ps.s_ox[i], ps.s_oy[i], ps.s_oz[i], ps.s_dx[i], ps.s_dy[i], ps.s_dz[i], 0.0f,
                                               ps.s_tmax[i]);

@@ -55,7 +55,7 @@ __global__ void __launch_bounds__(kBlock) k_init(RenderLaunch L) {
         ps.acc[i] = acc;
         ps.flags[i] = 0u;
         ps.ppdf[i] = 0.0f;
-        ps.q_active[0][i] = i;
+        ps.q_active[0][checked_index(i, L.P, ps.counters + kCntError)] = i;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) ps.counters[kCntActive] = L.P;
 }
@@ -74,7 +74,7 @@ __global__ void __launch_bounds__(BLOCK) k_extend_grid(RenderLaunch L, int cur) 
         int m = -1;
         uint32_t p = 0;
         if (active) {
-            p = q[i];
+            p = checked_index(q[i], L.P, ps.counters + kCntError);
             const TraceRay r = make_trace_ray(ps.ox[p], ps.oy[p], ps.oz[p], ps.dx[p], ps.dy[p], ps.dz[p], 0.0f, 10000.0f);
             Hit h;
             TraceCounters c{0u, 0u};
@@ -93,7 +93,7 @@ __global__ void __launch_bounds__(BLOCK) k_extend_grid(RenderLaunch L, int cur) 
         for (int k = 0; k < kNumQueues; ++k) {
             const bool mine = active && m == k;
             const uint32_t pos = warp_append(ps.counters + kCntQueue + k, mine);
-            if (mine) ps.q_shade[(size_t)k * L.P + pos] = p;
+            if (mine) ps.q_shade[(size_t)k * L.P + checked_index(pos, L.P, ps.counters + kCntError)] = p;
         }
     }
 }
@@ -106,7 +106,7 @@ __global__ void __launch_bounds__(kBlock) k_extend(RenderLaunch L, int cur) {
     const uint32_t* q = ps.q_active[cur];
     TraceCounters c{0u, 0u};
     auto load = [&](uint32_t i, TraceRay& r) {
-        const uint32_t p = q[i];
+        const uint32_t p = checked_index(q[i], L.P, ps.counters + kCntError);
         r = make_trace_ray(ps.ox[p], ps.oy[p], ps.oz[p], ps.dx[p], ps.dy[p], ps.dz[p], 0.0f, 10000.0f);
         return true;
     };
@@ -115,7 +115,7 @@ __global__ void __launch_bounds__(kBlock) k_extend(RenderLaunch L, int cur) {
         int m = -1;
         uint32_t p = 0;
         if (valid) {
-            p = q[i];
+            p = checked_index(q[i], L.P, ps.counters + kCntError);
             ps.hprim[p] = h.prim;
             ps.hu[p] = h.u;
             ps.hv[p] = h.v;
@@ -126,7 +126,7 @@ __global__ void __launch_bounds__(kBlock) k_extend(RenderLaunch L, int cur) {
         for (int k = 0; k < kNumQueues; ++k) {
             const bool mine = valid && m == k;
             const uint32_t pos = warp_append(ps.counters + kCntQueue + k, mine);
-            if (mine) ps.q_shade[(size_t)k * L.P + pos] = p;
+            if (mine) ps.q_shade[(size_t)k * L.P + checked_index(pos, L.P, ps.counters + kCntError)] = p;
         }
     };
     const uint32_t e = persistent_trace<false, false, true>(L.s.nodes, L.s.tris, L.s.node_count, n,
@@ -150,7 +150,7 @@ __global__ void __launch_bounds__(kBlock, kShadeMinBlocks) k_shade(RenderLaunch 
         ShadowRec sh;
         uint32_t p = 0;
         if (active) {
-            p = q[i];
+            p = checked_index(q[i], L.P, ps.counters + kCntError);
             const V3 ro{ps.ox[p], ps.oy[p], ps.oz[p]};
             const V3 rd{ps.dx[p], ps.dy[p], ps.dz[p]};
             const uint32_t prim = ps.hprim[p];
@@ -194,14 +194,15 @@ __global__ void __launch_bounds__(kBlock, kShadeMinBlocks) k_shade(RenderLaunch 
             ps.acc[p] = acc;
         }
         const uint32_t pos = warp_append(ps.counters + kCntActive + (cur ^ 1), active);
-        if (active) ps.q_active[cur ^ 1][pos] = p;
+        if (active) ps.q_active[cur ^ 1][checked_index(pos, L.P, ps.counters + kCntError)] = p;
         const uint32_t spos = warp_append(ps.counters + kCntShadow, emit);
         if (emit) {
-            ps.q_shadow[spos] = p;
-            ps.s_ox[spos] = sh.o.x; ps.s_oy[spos] = sh.o.y; ps.s_oz[spos] = sh.o.z;
-            ps.s_dx[spos] = sh.d.x; ps.s_dy[spos] = sh.d.y; ps.s_dz[spos] = sh.d.z;
-            ps.s_tmax[spos] = sh.tmax;
-            ps.s_cr[spos] = sh.contrib.x; ps.s_cg[spos] = sh.contrib.y; ps.s_cb[spos] = sh.contrib.z;
+            const uint32_t sp_ = checked_index(spos, L.P, ps.counters + kCntError);
+            ps.q_shadow[sp_] = p;
+            ps.s_ox[sp_] = sh.o.x; ps.s_oy[sp_] = sh.o.y; ps.s_oz[sp_] = sh.o.z;
+            ps.s_dx[sp_] = sh.d.x; ps.s_dy[sp_] = sh.d.y; ps.s_dz[sp_] = sh.d.z;
+            ps.s_tmax[sp_] = sh.tmax;
+            ps.s_cr[sp_] = sh.contrib.x; ps.s_cg[sp_] = sh.contrib.y; ps.s_cb[sp_] = sh.contrib.z;
         }
     }
 }
@@ -211,7 +212,7 @@ __global__ void __launch_bounds__(kBlock) k_shade_miss(RenderLaunch L) {
     const PathState& ps = L.ps;
     const uint32_t n = ps.counters[kCntQueue + kQueueMiss];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint32_t p = ps.q_shade[i];
+        const uint32_t p = checked_index(ps.q_shade[i], L.P, ps.counters + kCntError);
         V3 sky;
         if (L.env_mode == 1) {
             sky = V3{L.env[0], L.env[1], L.env[2]};
@@ -244,7 +245,7 @@ __global__ void __launch_bounds__(BLOCK) k_shadow_grid(RenderLaunch L) {
             else h.prim = kMiss;
             if (e) atomicOr(ps.counters + kCntError, e);
             if (h.prim == kMiss) {
-                const uint32_t p = ps.q_shadow[i];
+                const uint32_t p = checked_index(ps.q_shadow[i], L.P, ps.counters + kCntError);
                 store_rad(ps, p, load_rad(ps, p) + V3{ps.s_cr[i], ps.s_cg[i], ps.s_cb[i]});
             }
         }
@@ -264,7 +265,7 @@ __global__ void __launch_bounds__(kBlock) k_shadow(RenderLaunch L) {
     };
     auto store = [&](uint32_t i, const Hit& h, bool valid) {   // called by all 32 lanes
         if (valid && h.prim == kMiss) {
-            const uint32_t p = ps.q_shadow[i];
+            const uint32_t p = checked_index(ps.q_shadow[i], L.P, ps.counters + kCntError);
             store_rad(ps, p, load_rad(ps, p) + V3{ps.s_cr[i], ps.s_cg[i], ps.s_cb[i]});
         }
         warp_count64(reinterpret_cast<unsigned long long*>(ps.counters + kCntShadowRays), valid);

@@ -26,6 +26,24 @@ namespace rt {
 constexpr int kShadeMinBlocks = RT_SHADE_MINB;
 
 
+// Checked build (compiled with -DRT_CHECKED): every queue position and path index the wavefront kernels
+// read or write is checked against the path capacity; an index outside it is recorded in the error
+// word (bit kErrIndexBounds) and replaced by 0, so the access stays in bounds and the call fails with
+// REINA_ERR_DEVICE.  The normal build compiles the checks away.
+constexpr uint32_t kErrIndexBounds = 4u;
+__device__ __forceinline__ uint32_t checked_index(uint32_t i, uint64_t n, uint32_t* err) {
+#ifdef RT_CHECKED
+    if (i >= n) {
+        atomicOr(err, kErrIndexBounds);
+        return 0u;
+    }
+#else
+    (void)n;
+    (void)err;
+#endif
+    return i;
+}
+
 constexpr int kBlock = 128;
 constexpr uint32_t kFlagInside = 1u;
 constexpr uint32_t kFlagPrevNee = 2u;
