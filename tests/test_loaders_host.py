@@ -5,6 +5,7 @@ import base64
 import json
 import struct
 import zlib
+from pathlib import Path
 
 import numpy as np
 import pytest
@@ -371,3 +372,25 @@ def test_gltf_textures(R, host_ctx, tmp_path):
     s.build()
     for k in range(3):   # texels as written: no vertical flip for glTF images
         assert np.array_equal(s.export_texture(k), imgs[k])
+
+
+REF_MODELS = Path("/root/reference/models")
+
+
+@pytest.mark.skipif(not REF_MODELS.exists(), reason="reference model files not present")
+def test_reference_obj_models(R, host_ctx):
+    """Every OBJ the reference ships loads as one model: polygons fanned into triangles, one TBN and UV per
+    vertex when the file has UVs (Assimp's JoinIdenticalVertices / CalcTangentSpace / FlipUVs flags,
+    src/scene/Models.cpp:120), unit-length normals."""
+    for f in sorted(REF_MODELS.glob("*.obj")):
+        text = f.read_text()
+        faces = [l.split()[1:] for l in text.splitlines() if l.startswith("f ")]
+        want_tris = sum(len(fc) - 2 for fc in faces)
+        s = R.Scene(host_ctx)
+        oid = s.define_object_obj(f)
+        m = s.export_object(oid)
+        assert m["indices"].size == 3 * want_tris, f.name
+        n = m["tbns"].reshape(-1, 3, 3)[:, 2]
+        assert np.allclose(np.linalg.norm(n, axis=1), 1.0, atol=1e-4), f.name
+        has_vt = any(l.startswith("vt ") for l in text.splitlines())
+        assert (m["tex_coords"].shape[0] > 0) == has_vt, f.name
