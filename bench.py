@@ -578,8 +578,8 @@ def serve_metrics(R, ctx, torch, pool, seconds: float, rate: float) -> dict:
 
     # (b) served: the same stream through a request server (the scenes are handed to the first server
     # and stay with it; the second policy runs on a server of its own over fresh copies)
-    def serve(fifo: bool, scenes_pool) -> tuple[dict, bool]:
-        srv = R.Server(ctx, budget_bytes=120_000_000_000, fifo=fifo)
+    def serve(policy: str, scenes_pool) -> tuple[dict, bool]:
+        srv = R.Server(ctx, budget_bytes=120_000_000_000, fifo=policy == "fifo", shortest=policy == "shortest")
         ids = [srv.add_scene(s) for s, _ in scenes_pool]
         outs = [np.zeros((r[3].height, r[3].width, 4), np.float32) for r in reqs]
         rids = [None] * n
@@ -599,7 +599,7 @@ def serve_metrics(R, ctx, torch, pool, seconds: float, rate: float) -> dict:
         st = srv.stats()
         srv.close()
         span = st["first_submit_to_last_done_s"]
-        return ({"policy": "fifo" if fifo else "fair share",
+        return ({"policy": {"fair": "fair share", "fifo": "fifo", "shortest": "shortest remaining work"}[policy],
                  "p50_s": st["latency_p50_s"], "p99_s": st["latency_p99_s"], "mean_s": st["latency_mean_s"],
                  "renders_per_s": st["completed"] / span, "samples_per_s": samples / span,
                  "segments_per_s": st["rays"] / span, "rays_per_s": (st["rays"] + st["shadow_rays"]) / span,
@@ -607,13 +607,14 @@ def serve_metrics(R, ctx, torch, pool, seconds: float, rate: float) -> dict:
                  "scene_uploads": st["scene_uploads"], "scene_evictions": st["scene_evictions"],
                  "peak_resident_gb": st["peak_resident_bytes"] / 1e9}, all(s == R.REQ_DONE for s in states))
 
-    served, ok1 = serve(False, pool)
-    pool2 = [scenes.batch_scene(R, ctx, k) for k in range(len(pool))]
-    served_fifo, ok2 = serve(True, pool2)
+    served, ok1 = serve("fair", pool)
+    served_fifo, ok2 = serve("fifo", [scenes.batch_scene(R, ctx, k) for k in range(len(pool))])
+    served_shortest, ok3 = serve("shortest", [scenes.batch_scene(R, ctx, k) for k in range(len(pool))])
     return {"workload": f"Poisson {rate:g}/s for {seconds:g} s ({n} requests) over the {len(pool)}-scene pool, "
                         "side U[128,1024], spp U{1..64}, depth U{4..12}, NEE+MIS; 120 GB admission budget",
-            "requests": n, "samples_total": int(samples), "all_done": ok1 and ok2,
+            "requests": n, "samples_total": int(samples), "all_done": ok1 and ok2 and ok3,
             "plain_one_at_a_time": plain, "served": served, "served_fifo": served_fifo,
+            "served_shortest": served_shortest,
             "renders_per_s_ratio": served["renders_per_s"] / plain["renders_per_s"]}
 
 

@@ -372,12 +372,15 @@ typedef struct reina_server_options {
                                    * the wave path state (0 = 120e9 bytes) */
     uint32_t max_active_jobs;     /* requests sharing the waves, 1..512 (0 = 512) */
     uint32_t wave_paths;          /* path slots per wave (0 = REINA_DEFAULT_WAVE_PATHS) */
-    uint32_t flags;               /* REINA_BATCH_NO_GRAPHS, REINA_SERVER_FIFO */
+    uint32_t flags;               /* REINA_BATCH_NO_GRAPHS, REINA_SERVER_FIFO or REINA_SERVER_SHORTEST */
     uint32_t reserved;
 } reina_server_options;
-/* Wave slots go to the oldest running requests first (each takes all it can use), instead of an equal
- * share per request: lower latency for the requests at the head, higher for the ones behind them. */
-enum { REINA_SERVER_FIFO = 2 };
+/* Scheduling of the wave slots (default: an equal share per running request, leftovers to the oldest):
+ *   REINA_SERVER_FIFO      the oldest running requests first, each taking all it can use — lower latency
+ *                          for the requests at the head, higher for the ones behind them;
+ *   REINA_SERVER_SHORTEST  the running requests with the fewest samples left first (ties: the oldest),
+ *                          each taking all it can use — the shortest-remaining-work order. */
+enum { REINA_SERVER_FIFO = 2, REINA_SERVER_SHORTEST = 4 };
 
 /* A server runs on its context's GPU; destroying the context destroys its servers first. */
 int reina_server_create(reina_ctx* ctx, const reina_server_options* options, reina_server** out_server);

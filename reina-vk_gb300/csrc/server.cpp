@@ -388,12 +388,16 @@ void Server::loop() {
         std::vector<BatchJob*> jobs;
         jobs.reserve(running_.size());
         for (Request* r : running_) jobs.push_back(&r->job);
+        if (cfg_.shortest)   // fewest samples left first; stable: ties keep arrival order
+            std::stable_sort(jobs.begin(), jobs.end(), [](const BatchJob* a, const BatchJob* b) {
+                return a->total - a->cursor < b->total - b->cursor;
+            });
         lk.unlock();
         int code = 0;
         std::string err;
         const double t = now();
         try {
-            engine_->run_wave(jobs, stream_, cfg_.fifo);
+            engine_->run_wave(jobs, stream_, cfg_.fifo || cfg_.shortest);
         } catch (const Error& e) {
             code = e.code;
             err = e.what();

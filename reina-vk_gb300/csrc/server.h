@@ -29,6 +29,7 @@ struct ServerConfig {
     uint32_t wave_paths = 0;
     bool graphs = true;
     bool fifo = false;            // wave slots to the oldest requests first (default: fair share)
+    bool shortest = false;        // wave slots to the requests with the fewest samples left first
 };
 
 struct RequestSpec {

@@ -259,3 +259,10 @@ def test_server_needs_a_gpu_context(R, host_ctx):
     with pytest.raises(R.ReinaError) as e:
         R.Server(host_ctx)
     assert e.value.code == R.REINA_ERR_STATE
+
+
+def test_server_policy_flags_exclude_each_other(R, host_ctx):
+    with pytest.raises(R.ReinaError) as e:
+        R.Server(host_ctx, fifo=True, shortest=True)
+    assert e.value.code == R.REINA_ERR_INVALID
+

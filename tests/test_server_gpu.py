@@ -104,13 +104,13 @@ def submit_all(R, srv, ids, weights, specs, stagger_s=0.0, threads=1):
     return rids, outs
 
 
-@pytest.mark.parametrize("fifo", [False, True])
-def test_same_alone_and_in_the_mix(R, alone, fifo):
+@pytest.mark.parametrize("policy", ["fair", "fifo", "shortest"])
+def test_same_alone_and_in_the_mix(R, alone, policy):
     """Requests submitted from 3 threads while earlier ones run: each result equals its lone render
-    (fair-share and first-come first-served wave packing)."""
+    (fair-share, first-come first-served and shortest-remaining-work wave packing)."""
     weights, ref = alone
     ctx = R.Context(0)
-    ctx_srv, ids = start_server(R, ctx, wave_paths=4096, fifo=fifo)
+    ctx_srv, ids = start_server(R, ctx, wave_paths=4096, fifo=policy == "fifo", shortest=policy == "shortest")
     srv = ctx_srv
     rids, outs = submit_all(R, srv, ids, weights, request_specs(), stagger_s=0.002, threads=3)
     for n, rid in enumerate(rids):
