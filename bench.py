@@ -460,14 +460,21 @@ def batch_metrics(R, ctx, torch, built, setup_s: float, mega_scenes: int) -> dic
         accs.append(acc)
         jobs.append(R.DeviceRenderJob(scene, pc, opts, acc.data_ptr()))
     samples = [p["side"] ** 2 * p["spp"] for _, p in built]
-    # warm-up: small jobs of every depth (captures each wave graph), and the largest single-scene frame
-    # at 1 spp (grows the single-scene path state to its final size)
+    # autotune the batch (wave size x traversal block on a scaled-down subset of the jobs) and run the
+    # timed forms with the winner; the context's tuning is put back afterwards
+    saved_tuning = ctx.tuning()
+    t0 = time.perf_counter()
+    tune = R.autotune_batch(ctx, jobs)
+    tune_s = time.perf_counter() - t0
+    best = tune["best"]
+    ctx.set_tuning(wave_paths=best["wave_paths"], trace_block=best["trace_block"], trace_stack=best["trace_stack"])
+    # warm-up: one full wave (1024x1024 at 16 spp) of every depth, one batch each (builds the batch
+    # engine at its final size and captures each depth's wave graph), and the largest single-scene
+    # frame at 1 spp (grows the single-scene path state to its final size)
     warm_acc = torch.zeros((1024, 1024, 4), dtype=torch.float32, device="cuda")
-    warm = []
     for depth in range(4, 13):
-        pc, opts = scenes.batch_job(R, built[0][0], {"side": 8, "spp": 1, "depth": depth, "seed": 1})
-        warm.append(R.DeviceRenderJob(built[0][0], pc, opts, warm_acc.data_ptr()))
-    R.render_batch_device(ctx, warm, sptr)
+        pc, opts = scenes.batch_job(R, built[0][0], {"side": 1024, "spp": 16, "depth": depth, "seed": 1})
+        R.render_batch_device(ctx, [R.DeviceRenderJob(built[0][0], pc, opts, warm_acc.data_ptr())], sptr)
     big = max(range(n_scenes), key=lambda k: built[k][1]["side"])
     pc, opts = scenes.batch_job(R, built[big][0], dict(built[big][1], spp=1, depth=4))
     R.render_device(ctx, built[big][0], pc, opts, warm_acc.data_ptr(), 0, sptr)
@@ -504,6 +511,9 @@ def batch_metrics(R, ctx, torch, built, setup_s: float, mega_scenes: int) -> dic
         "samples_total": int(n_smp),
         "scene_setup_s": round(setup_s, 2),
         "wave_paths": ctx.tuning()["wave_paths"],
+        "autotune": {"s": round(tune_s, 3), "candidates": tune["candidates"], "best_ms": tune["best_ms"],
+                     "default_ms": tune["default_ms"],
+                     "chosen": {k: best[k] for k in ("wave_paths", "trace_block", "trace_stack")}},
         "batched": {"s": t_batch, "renders_per_s": n_scenes / t_batch, "segments_per_s": seg / t_batch,
                     "rays_per_s": (seg + shadow) / t_batch, "samples_per_s": n_smp / t_batch},
         "plain_wavefront": {"s": t_plain, "renders_per_s": n_scenes / t_plain, "segments_per_s": seg / t_plain,
@@ -521,6 +531,7 @@ def batch_metrics(R, ctx, torch, built, setup_s: float, mega_scenes: int) -> dic
             "batched": {"s": t_sub, "renders_per_s": m / t_sub},
             "plain_megakernel": {"s": t_mega, "renders_per_s": m / t_mega},
             "speedup_vs_plain_megakernel": t_mega / t_sub}
+    ctx.set_tuning(**saved_tuning)
     return out
 
 

@@ -75,9 +75,15 @@ int reina_ctx_sm_count(const reina_ctx* ctx);
  *            levels spill to local memory.
  *   trace_order: the order a ray cast traces its rays in (below).
  *   wave_paths: path slots of one wave of a batched render (0 = REINA_DEFAULT_WAVE_PATHS); the path
- *            state costs 164 bytes per slot.
+ *            state costs 164 bytes per slot.  A batch with fewer paths gets no more slots than it has
+ *            paths, rounded up to a power of two (at least 2^20); an engine already built with more
+ *            slots than that (up to wave_paths) is reused.
  *   batch_flags: REINA_BATCH_NO_GRAPHS launches each wave's kernels one by one instead of replaying a
- *            captured CUDA graph.
+ *            captured CUDA graph.  Waves are packed with the jobs in list order, each taking all it can
+ *            use (one sample of each of its pixels), so that a wave holds few scenes and their data
+ *            stays in L2 (on a 256-scene batch 9.06 s against 9.40 s for an equal share per job);
+ *            REINA_BATCH_FAIR_SHARE gives every unfinished job an equal share of each wave instead.
+ *            Neither changes an image.
  * Changing wave_paths, batch_flags, trace_block or trace_stack releases the batch engine; the next
  * batched call rebuilds it. */
 typedef struct reina_tuning {
@@ -96,8 +102,12 @@ typedef struct reina_tuning {
  * ray sets (on the 1.3M-triangle workload: random half 0.513 vs 0.525 ms, camera half 0.49 vs 0.46 ms);
  * the autotuner tries both. */
 enum { REINA_ORDER_INPUT = 0, REINA_ORDER_COHERENT = 1 };
-enum { REINA_DEFAULT_WAVE_PATHS = 2097152 };
-enum { REINA_BATCH_NO_GRAPHS = 1 };
+/* 2^24 slots (2.75 GB of path state): on a 256-scene batch (3.3G paths) 9.37 s, against 9.74 s at 2^23,
+ * 10.73 s at 2^22 and 12.94 s at 2^21 — every wave ends in a tail of a few long paths, and fewer,
+ * larger waves have fewer tails.  The server's waves are smaller (REINA_SERVER_WAVE_PATHS) so that new
+ * requests join sooner. */
+enum { REINA_DEFAULT_WAVE_PATHS = 16777216, REINA_SERVER_WAVE_PATHS = 2097152 };
+enum { REINA_BATCH_NO_GRAPHS = 1, REINA_BATCH_FAIR_SHARE = 2 };
 int reina_ctx_set_tuning(reina_ctx* ctx, const reina_tuning* tuning);
 int reina_ctx_get_tuning(const reina_ctx* ctx, reina_tuning* out_tuning);
 
@@ -371,7 +381,7 @@ typedef struct reina_server_options {
     uint64_t memory_budget_bytes; /* device memory for resident scenes, kept images, running requests and
                                    * the wave path state (0 = 120e9 bytes) */
     uint32_t max_active_jobs;     /* requests sharing the waves, 1..512 (0 = 512) */
-    uint32_t wave_paths;          /* path slots per wave (0 = REINA_DEFAULT_WAVE_PATHS) */
+    uint32_t wave_paths;          /* path slots per wave (0 = REINA_SERVER_WAVE_PATHS) */
     uint32_t flags;               /* REINA_BATCH_NO_GRAPHS, REINA_SERVER_FIFO or REINA_SERVER_SHORTEST */
     uint32_t reserved;
 } reina_server_options;

@@ -2,6 +2,7 @@
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <cmath>
 #include <cstring>
 #include <memory>
 #include <mutex>
@@ -225,7 +226,7 @@ int reina_ctx_set_tuning(reina_ctx* ctx, const reina_tuning* t) {
     return guard([&] {
         need(ctx && t, "NULL argument");
         need(t->refill <= 32, "refill must be in 0..32");
-        need((t->batch_flags & ~(uint32_t)REINA_BATCH_NO_GRAPHS) == 0, "unknown batch flags");
+        need((t->batch_flags & ~(uint32_t)(REINA_BATCH_NO_GRAPHS | REINA_BATCH_FAIR_SHARE)) == 0, "unknown batch flags");
         const uint32_t wave = t->wave_paths ? t->wave_paths : (uint32_t)REINA_DEFAULT_WAVE_PATHS;
         need(wave <= (1u << 26), "wave_paths must be at most 2^26");
         rt::TraceConfig tc;
@@ -544,6 +545,14 @@ static void batch_key(const reina_render_job* jobs, uint32_t count, uint64_t* tr
     }
 }
 
+// A wave of no more slots than the batch has paths (rounded up to a power of two, at least 2^20): a
+// small batch does not pay for the path state of a large wave.
+static uint32_t fit_wave(uint32_t wave, uint64_t samples) {
+    uint64_t fit = 1u << 20;
+    while (fit < samples && fit < wave) fit <<= 1;
+    return (uint32_t)std::min<uint64_t>(wave, fit);
+}
+
 // The context's batch engine, rebuilt when the wanted wave size or traversal variant changed (the
 // cached autotuned ones for this batch when the context uses the cache, else the context's tuning).
 static rt::BatchEngine& batch_engine(reina_ctx* ctx, const reina_render_job* jobs, uint32_t count) {
@@ -557,11 +566,14 @@ static rt::BatchEngine& batch_engine(reina_ctx* ctx, const reina_render_job* job
         trace = e.trace;
         if (e.wave_paths) wave = e.wave_paths;
     }
-    if (ctx->batch && (ctx->batch->capacity() != wave || ctx->batch->trace().block != trace.block ||
-                       ctx->batch->trace().stack != trace.stack))
+    // an engine between the batch's fitted size and the wanted one is kept (a job's images do not
+    // depend on how the waves are cut), so batches of changing sizes do not rebuild it each call
+    const uint32_t fitted = fit_wave(wave, samples);
+    if (ctx->batch && (ctx->batch->capacity() < fitted || ctx->batch->capacity() > wave ||
+                       ctx->batch->trace().block != trace.block || ctx->batch->trace().stack != trace.stack))
         ctx->batch.reset();
     if (!ctx->batch)
-        ctx->batch = std::make_unique<rt::BatchEngine>(ctx->device, ctx->sm_count, wave,
+        ctx->batch = std::make_unique<rt::BatchEngine>(ctx->device, ctx->sm_count, fitted,
                                                        (ctx->batch_flags & REINA_BATCH_NO_GRAPHS) == 0, trace);
     return *ctx->batch;
 }
@@ -612,7 +624,7 @@ static void render_batch(reina_ctx* ctx, const reina_render_job* jobs, uint32_t 
         ptrs[k] = &bj[k];
     }
     const uint64_t r0 = eng.rays(), s0 = eng.shadow_rays();
-    while (eng.run_wave(ptrs, st) > 0) {
+    while (eng.run_wave(ptrs, st, (ctx->batch_flags & REINA_BATCH_FAIR_SHARE) == 0) > 0) {
     }
     if (host) {
         for (uint32_t k = 0; k < count; ++k) {
@@ -1013,14 +1025,24 @@ int reina_autotune_batch(reina_ctx* ctx, const reina_render_job* jobs, uint32_t 
         uint64_t tris = 0, samples = 0;
         for (uint32_t k = 0; k < count; ++k) built_scene(jobs[k].scene);
         batch_key(jobs, count, &tris, &samples);
-        // up to 32 jobs (spread over the list) at no more than 2 samples per pixel, into scratch images
+        // up to 32 jobs (spread over the list), into scratch images, with their sample counts scaled
+        // down (never below 1 per pixel) so that the subset holds about 4 of the largest candidate waves
+        // or the whole batch, whichever is less: the wave size pays through the number of wave tails,
+        // which a subset smaller than one wave cannot show
         const uint32_t n = std::min<uint32_t>(count, 32);
+        const uint64_t kMaxWave = 1u << 24;
         std::vector<reina_render_job> sub(n);
         std::vector<rt::DeviceBuffer> scratch(n);
-        use_device(ctx);
+        uint64_t sub_samples = 0;
         for (uint32_t k = 0; k < n; ++k) {
             sub[k] = jobs[(uint64_t)k * count / n];
-            sub[k].push_consts.samplesPerPixel = std::min<uint32_t>(sub[k].push_consts.samplesPerPixel, 2);
+            sub_samples += (uint64_t)sub[k].options.width * sub[k].options.height * sub[k].push_consts.samplesPerPixel;
+        }
+        const double scale = std::min(1.0, (double)std::min<uint64_t>(4 * kMaxWave, samples) / (double)sub_samples);
+        use_device(ctx);
+        for (uint32_t k = 0; k < n; ++k) {
+            const uint32_t spp = sub[k].push_consts.samplesPerPixel;
+            sub[k].push_consts.samplesPerPixel = std::max<uint32_t>(1, (uint32_t)std::floor(spp * scale));
             sub[k].push_consts.sampleBatch = 0;
             scratch[k].alloc((size_t)sub[k].options.width * sub[k].options.height * 4 * sizeof(float));
             sub[k].accum_rgba32f = scratch[k].get();
@@ -1035,7 +1057,13 @@ int reina_autotune_batch(reina_ctx* ctx, const reina_render_job* jobs, uint32_t 
         best.best_ms = 1e30;
         uint32_t cands = 0;
         try {
-            for (uint32_t wave : {1u << 20, 1u << 21, 1u << 22})
+            // candidate waves as the batch would run them (a wave beyond the batch's size shrinks to it)
+            std::vector<uint32_t> waves;
+            for (uint32_t w : {1u << 21, 1u << 22, 1u << 23, (uint32_t)kMaxWave})
+                if (std::find(waves.begin(), waves.end(), fit_wave(w, samples)) == waves.end())
+                    waves.push_back(fit_wave(w, samples));
+            const uint32_t default_wave = fit_wave(REINA_DEFAULT_WAVE_PATHS, samples);
+            for (uint32_t wave : waves)
                 for (int block : {128, 256}) {
                     rt::TraceConfig c;
                     c.block = block;
@@ -1044,7 +1072,7 @@ int reina_autotune_batch(reina_ctx* ctx, const reina_render_job* jobs, uint32_t 
                     ctx->batch.reset();
                     const double ms = time_calls(st, 1, [&] { render_batch(ctx, sub.data(), n, false, st, nullptr); });
                     ++cands;
-                    if (is_default(c) && wave == (uint32_t)REINA_DEFAULT_WAVE_PATHS) best.default_ms = ms;
+                    if (is_default(c) && wave == default_wave) best.default_ms = ms;
                     if (ms < best.best_ms) {
                         best.best_ms = ms;
                         best.trace = c;
@@ -1062,6 +1090,13 @@ int reina_autotune_batch(reina_ctx* ctx, const reina_render_job* jobs, uint32_t 
         ctx->trace = saved_trace;
         ctx->autotune_mode = saved_mode;
         ctx->batch.reset();
+        // the subset holds only a few waves of the larger sizes, so near-ties between them are noise:
+        // the default stays unless another candidate is at least 2 % faster
+        if (best.default_ms > 0 && best.best_ms > 0.98 * best.default_ms) {
+            best.best_ms = best.default_ms;
+            best.trace = rt::TraceConfig();
+            best.wave_paths = fit_wave(REINA_DEFAULT_WAVE_PATHS, samples);
+        }
         finish_tune(ctx, rt::kTuneBatch, tris, samples, best, cands, out);
     });
 }

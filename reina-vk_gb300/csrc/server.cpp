@@ -23,7 +23,7 @@ double Server::now() const {
 Server::Server(int device, int sm_count, const ServerConfig& cfg) : device_(device), cfg_(cfg) {
     if (cfg_.max_active == 0 || cfg_.max_active > kMaxWaveSegments / 2)
         fail(REINA_ERR_INVALID, "max_active_jobs must be in 1.." + std::to_string(kMaxWaveSegments / 2));
-    const uint32_t wave = cfg_.wave_paths ? cfg_.wave_paths : 2097152u;
+    const uint32_t wave = cfg_.wave_paths ? cfg_.wave_paths : (uint32_t)REINA_SERVER_WAVE_PATHS;
     reserved_ = (uint64_t)wave * kPathBytes + (64u << 20);   // path state + descriptors and slack
     if (cfg_.budget < reserved_)
         fail(REINA_ERR_BUDGET, "memory budget " + std::to_string(cfg_.budget) + " B is below the engine's " +

@@ -94,8 +94,10 @@ TUNING_FIELDS = ("refill", "wave_paths", "batch_flags", "trace_block", "trace_st
 ORDER_INPUT, ORDER_COHERENT = 0, 1
 
 
-DEFAULT_WAVE_PATHS = 2097152
+DEFAULT_WAVE_PATHS = 16777216
+SERVER_WAVE_PATHS = 2097152
 BATCH_NO_GRAPHS = 1
+BATCH_FAIR_SHARE = 2
 
 
 # InstanceProperties (polyglot.h), 120 bytes.

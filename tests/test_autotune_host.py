@@ -53,8 +53,13 @@ def test_tuning_fields_validated(R, host_ctx):
         host_ctx.set_tuning(trace_block=96)
     with pytest.raises(R.ReinaError):
         host_ctx.set_tuning(trace_stack=10)
-    host_ctx.set_tuning(trace_block=256, trace_stack=16)
+    with pytest.raises(R.ReinaError):
+        host_ctx.set_tuning(batch_flags=4)
+    with pytest.raises(R.ReinaError):
+        host_ctx.set_tuning(wave_paths=(1 << 26) + 1)
+    assert old["wave_paths"] == R.DEFAULT_WAVE_PATHS
+    host_ctx.set_tuning(trace_block=256, trace_stack=16, batch_flags=R.BATCH_NO_GRAPHS | R.BATCH_FAIR_SHARE)
     t = host_ctx.tuning()
-    assert t["trace_block"] == 256 and t["trace_stack"] == 16
+    assert t["trace_block"] == 256 and t["trace_stack"] == 16 and t["batch_flags"] == 3
     host_ctx.set_tuning(**old)
     assert host_ctx.tuning() == old

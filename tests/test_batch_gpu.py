@@ -79,12 +79,13 @@ def check_same(batch, alone):
 
 
 @pytest.mark.parametrize("tuning", [dict(), dict(wave_paths=1000), dict(wave_paths=777, batch_flags=1),
-                                    dict(wave_paths=5000, batch_flags=1), dict(trace_block=256, trace_stack=8),
+                                    dict(wave_paths=5000, batch_flags=1), dict(wave_paths=3000, batch_flags=2),
+                                    dict(wave_paths=1500, batch_flags=3), dict(trace_block=256, trace_stack=8),
                                     dict(trace_block=64, trace_stack=16)])
 def test_batch_equals_alone(R, batch_setup, tuning):
     """All jobs in one call, with the default wave (every job's sample in one wave), with small waves
-    (each wave cut across jobs and pixels), with graphs and with direct launches, and with other
-    traversal variants."""
+    (each wave cut across jobs and pixels), packed in list order and with an equal share per job, with
+    graphs and with direct launches, and with other traversal variants."""
     ctx, jobs, alone = batch_setup
     ctx.set_tuning(**tuning)
     try:
