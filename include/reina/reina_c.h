@@ -75,7 +75,9 @@ int reina_ctx_sm_count(const reina_ctx* ctx);
  *            levels spill to local memory.
  *   trace_order: the order a ray cast traces its rays in (below).
  *   wave_paths: path slots of one wave of a batched render (0 = REINA_DEFAULT_WAVE_PATHS); the path
- *            state costs 164 bytes per slot.  A batch with fewer paths gets no more slots than it has
+ *            state costs 164 bytes per slot, twice over: a batched render keeps two waves in flight on
+ *            two streams, so that one wave's last bounces (few long paths) overlap the next wave's
+ *            first ones.  A batch with fewer paths gets no more slots than it has
  *            paths, rounded up to a power of two (at least 2^20); an engine already built with more
  *            slots than that (up to wave_paths) is reused.
  *   batch_flags: REINA_BATCH_NO_GRAPHS launches each wave's kernels one by one instead of replaying a
@@ -102,11 +104,12 @@ typedef struct reina_tuning {
  * ray sets (on the 1.3M-triangle workload: random half 0.513 vs 0.525 ms, camera half 0.49 vs 0.46 ms);
  * the autotuner tries both. */
 enum { REINA_ORDER_INPUT = 0, REINA_ORDER_COHERENT = 1 };
-/* 2^24 slots (2.75 GB of path state): on a 256-scene batch (3.3G paths) 9.37 s, against 9.74 s at 2^23,
- * 10.73 s at 2^22 and 12.94 s at 2^21 — every wave ends in a tail of a few long paths, and fewer,
- * larger waves have fewer tails.  The server's waves are smaller (REINA_SERVER_WAVE_PATHS) so that new
+/* 2^23 slots (two lanes of 1.4 GB of path state): on a 256-scene batch (3.1G paths) 7.75 s, against
+ * 7.77 s at 2^22, 7.89 s at 2^24 and 8.06 s at 2^21; with one wave in flight the same batch took
+ * 9.74 s at 2^23 and 12.94 s at 2^21 — every wave ends in a tail of a few long paths, which the second
+ * lane's wave now fills.  The server's waves are smaller (REINA_SERVER_WAVE_PATHS) so that new
  * requests join sooner. */
-enum { REINA_DEFAULT_WAVE_PATHS = 16777216, REINA_SERVER_WAVE_PATHS = 2097152 };
+enum { REINA_DEFAULT_WAVE_PATHS = 8388608, REINA_SERVER_WAVE_PATHS = 2097152 };
 enum { REINA_BATCH_NO_GRAPHS = 1, REINA_BATCH_FAIR_SHARE = 2 };
 int reina_ctx_set_tuning(reina_ctx* ctx, const reina_tuning* tuning);
 int reina_ctx_get_tuning(const reina_ctx* ctx, reina_tuning* out_tuning);

@@ -317,13 +317,23 @@ static int occupancy(const void* fn, int sm_count) {
     return std::max(1, per_sm) * std::max(1, sm_count);
 }
 
-BatchEngine::BatchEngine(int device, int sm_count, uint32_t wave_capacity, bool use_graphs, const TraceConfig& trace)
+BatchEngine::BatchEngine(int device, int sm_count, uint32_t wave_capacity, bool use_graphs, const TraceConfig& trace,
+                         int lanes)
     : device_(device), sm_count_(sm_count), capacity_(wave_capacity), use_graphs_(use_graphs), trace_(trace) {
     if (wave_capacity == 0) fail(REINA_ERR_INVALID, "wave capacity must be positive");
-    paths_.alloc((64 + kBatchWordsPerPath * (size_t)capacity_) * 4);
+    if (lanes < 1 || lanes > 2) fail(REINA_ERR_INVALID, "a batch engine has 1 or 2 lanes");
     desc_bytes_ = sizeof(WaveHeader) + kMaxWaveSegments * sizeof(WaveSeg) + kMaxWaveJobs * sizeof(JobGpu);
-    desc_.alloc(desc_bytes_);
-    check_cuda(cudaMallocHost(&host_desc_, desc_bytes_), "cudaMallocHost");
+    lanes_.resize((size_t)lanes);
+    for (Lane& L : lanes_) {
+        L.paths.alloc((64 + kBatchWordsPerPath * (size_t)capacity_) * 4);
+        L.desc.alloc(desc_bytes_);
+        check_cuda(cudaMallocHost(&L.host_desc, desc_bytes_), "cudaMallocHost");
+        check_cuda(cudaMallocHost(reinterpret_cast<void**>(&L.host_counters), kNumCounters * sizeof(uint32_t)),
+                   "cudaMallocHost");
+        check_cuda(cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        check_cuda(cudaEventCreateWithFlags(&L.finished, cudaEventDisableTiming), "cudaEventCreate");
+        check_cuda(cudaEventCreateWithFlags(&L.done, cudaEventDisableTiming), "cudaEventCreate");
+    }
     with_trace_variant(trace_, [&](auto B, auto S) {
         blocks_ext_ = resident_grid((const void*)kb_extend<B.value, S.value, false>, B.value, sm_count);
         blocks_sh_ = resident_grid((const void*)kb_shadow<B.value, S.value, false>, B.value, sm_count);
@@ -338,9 +348,16 @@ BatchEngine::BatchEngine(int device, int sm_count, uint32_t wave_capacity, bool 
 }
 
 BatchEngine::~BatchEngine() {
-    for (auto& g : graphs_)
-        if (g.exec) cudaGraphExecDestroy(g.exec);
-    if (host_desc_) cudaFreeHost(host_desc_);
+    for (Lane& L : lanes_) {
+        if (L.stream) cudaStreamSynchronize(L.stream);
+        for (auto& g : L.graphs)
+            if (g.exec) cudaGraphExecDestroy(g.exec);
+        if (L.finished) cudaEventDestroy(L.finished);
+        if (L.done) cudaEventDestroy(L.done);
+        if (L.stream) cudaStreamDestroy(L.stream);
+        if (L.host_desc) cudaFreeHost(L.host_desc);
+        if (L.host_counters) cudaFreeHost(L.host_counters);
+    }
 }
 
 void BatchEngine::prepare(BatchJob& job) {
@@ -377,16 +394,24 @@ static JobGpu job_record(const BatchJob& j) {
     return g;
 }
 
-void BatchEngine::launch_wave(const WaveHeader& h, bool any_nee, bool two, cudaStream_t st) {
-    uint8_t* d = desc_.as<uint8_t>();
+void BatchEngine::launch_body(Lane& L, const Packed& pk, cudaStream_t st) {
+    const WaveHeader& h = pk.hdr;
+    uint8_t* d = L.desc.as<uint8_t>();
+    const uint8_t* hd = static_cast<const uint8_t*>(L.host_desc);
+    check_cuda(cudaMemcpyAsync(d, hd, sizeof(WaveHeader) + h.nseg * sizeof(WaveSeg), cudaMemcpyHostToDevice, st),
+               "H2D wave");
+    const size_t job_off = sizeof(WaveHeader) + kMaxWaveSegments * sizeof(WaveSeg);
+    check_cuda(cudaMemcpyAsync(d + job_off, hd + job_off, h.njobs * sizeof(JobGpu), cudaMemcpyHostToDevice, st),
+               "H2D jobs");
     BatchLaunch B;
-    B.bp = layout_batch(paths_.as<uint32_t>(), capacity_);
+    B.bp = layout_batch(L.paths.as<uint32_t>(), capacity_);
     B.hdr = reinterpret_cast<const WaveHeader*>(d);
     B.segs = reinterpret_cast<const WaveSeg*>(d + sizeof(WaveHeader));
-    B.jobs = reinterpret_cast<const JobGpu*>(d + sizeof(WaveHeader) + kMaxWaveSegments * sizeof(WaveSeg));
+    B.jobs = reinterpret_cast<const JobGpu*>(d + job_off);
     B.P = capacity_;
     uint32_t* cnt = B.bp.ps.counters;
     const int simple = std::min<int>(blocks_simple_, (int)((capacity_ + kBlock - 1) / kBlock));
+    const bool any_nee = pk.any_nee, two = pk.two;
     auto sequence = [&](cudaStream_t s) {
         check_cuda(cudaMemsetAsync(cnt, 0, kNumCounters * sizeof(uint32_t), s), "cudaMemsetAsync");
         kb_init<<<simple, kBlock, 0, s>>>(B, B.jobs);
@@ -413,7 +438,6 @@ void BatchEngine::launch_wave(const WaveHeader& h, bool any_nee, bool two, cudaS
                 });
             cur ^= 1;
         }
-        kb_finish<<<simple, kBlock, 0, s>>>(B, B.jobs);
     };
     if (!use_graphs_) {
         sequence(st);
@@ -421,7 +445,7 @@ void BatchEngine::launch_wave(const WaveHeader& h, bool any_nee, bool two, cudaS
         return;
     }
     GraphSlot* slot = nullptr;
-    for (auto& g : graphs_)
+    for (auto& g : L.graphs)
         if (g.bounces == h.max_bounces && g.nee == any_nee && g.two == two) slot = &g;
     if (!slot) {
         cudaStream_t cap;
@@ -437,18 +461,57 @@ void BatchEngine::launch_wave(const WaveHeader& h, bool any_nee, bool two, cudaS
         g.two = two;
         check_cuda(cudaGraphInstantiate(&g.exec, graph, 0), "cudaGraphInstantiate");
         cudaGraphDestroy(graph);
-        graphs_.push_back(g);
-        slot = &graphs_.back();
+        L.graphs.push_back(g);
+        slot = &L.graphs.back();
     }
     check_cuda(cudaGraphLaunch(slot->exec, st), "cudaGraphLaunch");
 }
 
-uint64_t BatchEngine::run_wave(const std::vector<BatchJob*>& jobs, cudaStream_t st, bool fifo) {
+void BatchEngine::launch_finish(Lane& L, const Packed& pk, cudaStream_t st) {
+    const uint8_t* d = L.desc.as<uint8_t>();
+    BatchLaunch B;
+    B.bp = layout_batch(L.paths.as<uint32_t>(), capacity_);
+    B.hdr = reinterpret_cast<const WaveHeader*>(d);
+    B.segs = reinterpret_cast<const WaveSeg*>(d + sizeof(WaveHeader));
+    B.jobs = reinterpret_cast<const JobGpu*>(d + sizeof(WaveHeader) + kMaxWaveSegments * sizeof(WaveSeg));
+    B.P = capacity_;
+    const int simple = std::min<int>(blocks_simple_, (int)((capacity_ + kBlock - 1) / kBlock));
+    kb_finish<<<simple, kBlock, 0, st>>>(B, B.jobs);
+    for (BatchJob* j : pk.completed) {   // resolve the jobs this wave completed
+        const JobGpu g = job_record(*j);
+        const uint32_t px = g.W * g.H;
+        const int blocks = (int)std::min<uint32_t>((px + kBlock - 1) / kBlock, (uint32_t)blocks_simple_);
+        kb_resolve<<<blocks, kBlock, 0, st>>>(g);
+    }
+    check_cuda(cudaGetLastError(), "batch launch");
+    check_cuda(cudaEventRecord(L.finished, st), "cudaEventRecord");
+    check_cuda(cudaMemcpyAsync(L.host_counters, L.paths.get(), kNumCounters * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                               st), "D2H counters");
+    check_cuda(cudaEventRecord(L.done, st), "cudaEventRecord");
+    L.pending = true;
+}
+
+void BatchEngine::collect(Lane& L) {
+    if (!L.pending) return;
+    L.pending = false;
+    const uint32_t* c = L.host_counters;
+    uint64_t r, sr;
+    std::memcpy(&r, c + kCntRays, 8);
+    std::memcpy(&sr, c + kCntShadowRays, 8);
+    rays_ += r;
+    shadow_rays_ += sr;
+    waves_++;
+    if (c[kCntError]) fail(REINA_ERR_DEVICE, "batch wave kernels raised error flag " + std::to_string(c[kCntError]));
+}
+
+BatchEngine::Packed BatchEngine::pack(const std::vector<BatchJob*>& jobs, bool fifo, Lane& L) {
+    Packed pk;
+    std::memset(&pk.hdr, 0, sizeof(pk.hdr));
     // active jobs (at most kMaxWaveJobs per wave; the rest wait for a later wave)
     std::vector<BatchJob*> active;
     for (BatchJob* j : jobs)
         if (j->cursor < j->total && active.size() < kMaxWaveJobs) active.push_back(j);
-    if (active.empty()) return 0;
+    if (active.empty()) return pk;
     // fair share of the capacity, then leftovers to the oldest jobs (or, first-come first-served, each
     // job in order takes all it can use)
     std::vector<uint64_t> take(active.size(), 0);
@@ -467,12 +530,11 @@ uint64_t BatchEngine::run_wave(const std::vector<BatchJob*>& jobs, cudaStream_t 
         take[a] += more;
         used += more;
     }
-    uint8_t* h = static_cast<uint8_t*>(host_desc_);
+    uint8_t* h = static_cast<uint8_t*>(L.host_desc);
     WaveHeader* hdr = reinterpret_cast<WaveHeader*>(h);
     WaveSeg* segs = reinterpret_cast<WaveSeg*>(h + sizeof(WaveHeader));
     JobGpu* jt = reinterpret_cast<JobGpu*>(h + sizeof(WaveHeader) + kMaxWaveSegments * sizeof(WaveSeg));
     uint32_t nseg = 0, njobs = 0, wave_pos = 0, bounces = 0;
-    bool any_nee = false, two = false;
     for (size_t a = 0; a < active.size(); ++a) {
         if (take[a] == 0) continue;
         BatchJob* j = active[a];
@@ -480,8 +542,10 @@ uint64_t BatchEngine::run_wave(const std::vector<BatchJob*>& jobs, cudaStream_t 
         const uint32_t ji = njobs++;
         jt[ji] = job_record(*j);
         bounces = std::max(bounces, j->pc.maxBounces);
-        any_nee = any_nee || j->opt.mode == kModeNeeMis;
-        two = two || j->scene.inst_trav != nullptr;
+        pk.any_nee = pk.any_nee || j->opt.mode == kModeNeeMis;
+        // samples after a pixel's first start from the state its previous sample left (reference mode)
+        pk.carries = pk.carries || (j->opt.mode != kModeNeeMis && j->cursor + take[a] > px);
+        pk.two = pk.two || j->scene.inst_trav != nullptr;
         uint64_t m = take[a];
         while (m > 0) {
             const uint64_t sample = j->cursor / px, pixel = j->cursor % px;
@@ -496,39 +560,66 @@ uint64_t BatchEngine::run_wave(const std::vector<BatchJob*>& jobs, cudaStream_t 
             j->cursor += c;
             m -= c;
         }
+        if (j->cursor == j->total && !j->resolved) {
+            pk.completed.push_back(j);
+            j->resolved = true;
+        }
     }
     hdr->count = wave_pos;
     hdr->nseg = nseg;
     hdr->njobs = njobs;
     hdr->max_bounces = bounces;
-    uint8_t* d = desc_.as<uint8_t>();
-    check_cuda(cudaMemcpyAsync(d, h, sizeof(WaveHeader) + nseg * sizeof(WaveSeg), cudaMemcpyHostToDevice, st), "H2D wave");
-    const size_t job_off = sizeof(WaveHeader) + kMaxWaveSegments * sizeof(WaveSeg);
-    check_cuda(cudaMemcpyAsync(d + job_off, h + job_off, njobs * sizeof(JobGpu), cudaMemcpyHostToDevice, st), "H2D jobs");
-    launch_wave(*hdr, any_nee, two, st);
-    // resolve the jobs this wave completed
-    for (size_t a = 0; a < active.size(); ++a) {
-        BatchJob* j = active[a];
-        if (j->cursor == j->total && !j->resolved) {
-            const JobGpu g = job_record(*j);
-            const uint32_t px = g.W * g.H;
-            const int blocks = (int)std::min<uint32_t>((px + kBlock - 1) / kBlock, (uint32_t)blocks_simple_);
-            kb_resolve<<<blocks, kBlock, 0, st>>>(g);
-            j->resolved = true;
-        }
-    }
-    check_cuda(cudaGetLastError(), "batch launch");
-    uint32_t c[kNumCounters];
-    check_cuda(cudaMemcpyAsync(c, paths_.get(), sizeof(c), cudaMemcpyDeviceToHost, st), "D2H counters");
+    pk.hdr = *hdr;
+    return pk;
+}
+
+uint64_t BatchEngine::run_wave(const std::vector<BatchJob*>& jobs, cudaStream_t st, bool fifo) {
+    Lane& L = lanes_[0];
+    const Packed pk = pack(jobs, fifo, L);
+    if (pk.hdr.count == 0) return 0;
+    launch_body(L, pk, st);
+    launch_finish(L, pk, st);
     check_cuda(cudaStreamSynchronize(st), "cudaStreamSynchronize");
-    uint64_t r, sr;
-    std::memcpy(&r, c + kCntRays, 8);
-    std::memcpy(&sr, c + kCntShadowRays, 8);
-    rays_ += r;
-    shadow_rays_ += sr;
-    waves_++;
-    if (c[kCntError]) fail(REINA_ERR_DEVICE, "batch wave kernels raised error flag " + std::to_string(c[kCntError]));
-    return wave_pos;
+    collect(L);
+    return pk.hdr.count;
+}
+
+void BatchEngine::run_all(const std::vector<BatchJob*>& jobs, cudaStream_t st, bool fifo) {
+    cudaEvent_t start;
+    check_cuda(cudaEventCreateWithFlags(&start, cudaEventDisableTiming), "cudaEventCreate");
+    Lane* prev = nullptr;   // the lane of the previous wave
+    try {
+        check_cuda(cudaEventRecord(start, st), "cudaEventRecord");
+        for (Lane& L : lanes_) check_cuda(cudaStreamWaitEvent(L.stream, start, 0), "cudaStreamWaitEvent");
+        for (size_t k = 0;; ++k) {
+            Lane& L = lanes_[k % lanes_.size()];
+            if (L.pending) {   // the lane's previous wave (two waves back) is done: reuse its buffers
+                check_cuda(cudaEventSynchronize(L.done), "cudaEventSynchronize");
+                collect(L);
+            }
+            const Packed pk = pack(jobs, fifo, L);
+            if (pk.hdr.count == 0) break;
+            if (prev && prev != &L && pk.carries)
+                check_cuda(cudaStreamWaitEvent(L.stream, prev->finished, 0), "cudaStreamWaitEvent");
+            launch_body(L, pk, L.stream);
+            if (prev && prev != &L) check_cuda(cudaStreamWaitEvent(L.stream, prev->finished, 0), "cudaStreamWaitEvent");
+            launch_finish(L, pk, L.stream);
+            prev = &L;
+        }
+        for (Lane& L : lanes_) {
+            check_cuda(cudaEventSynchronize(L.done), "cudaEventSynchronize");
+            check_cuda(cudaStreamWaitEvent(st, L.done, 0), "cudaStreamWaitEvent");
+        }
+        for (Lane& L : lanes_) collect(L);
+    } catch (...) {
+        for (Lane& L : lanes_) {   // nothing of this call stays in flight
+            cudaStreamSynchronize(L.stream);
+            L.pending = false;
+        }
+        cudaEventDestroy(start);
+        throw;
+    }
+    cudaEventDestroy(start);
 }
 
 }  // namespace rt

@@ -67,8 +67,10 @@ struct BatchJob {
 
 class BatchEngine {
 public:
+    // `lanes` path-state buffers (1 or 2) of `wave_capacity` slots each; run_all alternates waves over
+    // them so that one wave's last bounces overlap the next wave's first ones.
     BatchEngine(int device, int sm_count, uint32_t wave_capacity, bool use_graphs,
-                const TraceConfig& trace = TraceConfig());
+                const TraceConfig& trace = TraceConfig(), int lanes = 1);
     ~BatchEngine();
     BatchEngine(const BatchEngine&) = delete;
     BatchEngine& operator=(const BatchEngine&) = delete;
@@ -76,32 +78,60 @@ public:
     // Allocates the job's per-pixel state (24 bytes per pixel); the job must outlive its waves.
     static void prepare(BatchJob& job);
     // Packs the next wave from `jobs` (fair share of the capacity, oldest first for leftovers; with
-    // `fifo`, each job in order takes all it can use), runs it and resolves the jobs it completes.
-    // Returns the number of paths traced (0 = nothing to do).  Synchronizes the stream at the end.
+    // `fifo`, each job in order takes all it can use), runs it on `st` in lane 0 and resolves the jobs
+    // it completes.  Returns the number of paths traced (0 = nothing to do).  Synchronizes the stream.
     uint64_t run_wave(const std::vector<BatchJob*>& jobs, cudaStream_t st, bool fifo = false);
+    // Runs waves (packed as run_wave packs them) until every job is resolved, two in flight on the
+    // lanes' own streams when the engine has two lanes.  Each wave's finish kernel (the per-pixel sums)
+    // runs after the previous wave's, so a pixel's samples are summed in sample order; a wave holding
+    // a job whose samples carry state from the pixel's previous sample (the reference's seeding mode)
+    // starts only after the previous wave's finish.  Ordered after the work queued on `st` before the
+    // call; returns with the work queued on `st` ordered after it, and every lane synchronized.
+    void run_all(const std::vector<BatchJob*>& jobs, cudaStream_t st, bool fifo = false);
     uint32_t capacity() const { return capacity_; }
+    int lanes() const { return (int)lanes_.size(); }
     const TraceConfig& trace() const { return trace_; }
     uint64_t rays() const { return rays_; }
     uint64_t shadow_rays() const { return shadow_rays_; }
     uint32_t waves() const { return waves_; }
 
 private:
-    void launch_wave(const WaveHeader& h, bool any_nee, bool two, cudaStream_t st);
-    int device_, sm_count_;
-    uint32_t capacity_;
-    bool use_graphs_;
-    TraceConfig trace_;           // grid-form traversal variant of the extend and shadow kernels
-    DeviceBuffer paths_;          // path state for `capacity_` slots (+ job, pixel, sample, depth arrays)
-    DeviceBuffer desc_;           // header + segments + job table
-    void* host_desc_ = nullptr;   // pinned staging of the descriptor
-    size_t desc_bytes_ = 0;
     struct GraphSlot {
         uint32_t bounces = 0;
         bool nee = false;
         bool two = false;   // the wave holds a two-level scene
         cudaGraphExec_t exec = nullptr;
     };
-    std::vector<GraphSlot> graphs_;
+    struct Lane {
+        DeviceBuffer paths;             // path state for the capacity's slots (+ job, pixel, sample, depth)
+        DeviceBuffer desc;              // header + segments + job table
+        void* host_desc = nullptr;      // pinned staging of the descriptor
+        uint32_t* host_counters = nullptr;   // pinned copy of the wave's counters
+        cudaStream_t stream = nullptr;  // run_all's stream for this lane
+        cudaEvent_t finished = nullptr; // after the lane's last finish kernel and resolves
+        cudaEvent_t done = nullptr;     // after the lane's last counter copy
+        bool pending = false;           // a wave whose counters are not collected yet
+        std::vector<GraphSlot> graphs;  // captured wave bodies (pointers into this lane's buffers)
+    };
+    struct Packed {
+        WaveHeader hdr;
+        bool any_nee = false, two = false, carries = false;
+        std::vector<BatchJob*> completed;
+    };
+    // Packs the next wave into the lane's host descriptor; hdr.count == 0 when nothing is left.
+    Packed pack(const std::vector<BatchJob*>& jobs, bool fifo, Lane& L);
+    // Descriptor upload + wave body (init and the bounce kernels) on `s`.
+    void launch_body(Lane& L, const Packed& pk, cudaStream_t s);
+    // Finish kernel, resolves of the completed jobs, counter copy on `s`.
+    void launch_finish(Lane& L, const Packed& pk, cudaStream_t s);
+    // Adds a synchronized lane's counters to the totals; throws on a device error flag.
+    void collect(Lane& L);
+    int device_, sm_count_;
+    uint32_t capacity_;
+    bool use_graphs_;
+    TraceConfig trace_;           // grid-form traversal variant of the extend and shadow kernels
+    size_t desc_bytes_ = 0;
+    std::vector<Lane> lanes_;
     uint64_t rays_ = 0, shadow_rays_ = 0;
     uint32_t waves_ = 0;
     int blocks_ext_ = 0, blocks_shade_[5] = {0, 0, 0, 0, 0}, blocks_sh_ = 0, blocks_simple_ = 0;

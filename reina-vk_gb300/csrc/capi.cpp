@@ -574,7 +574,7 @@ static rt::BatchEngine& batch_engine(reina_ctx* ctx, const reina_render_job* job
         ctx->batch.reset();
     if (!ctx->batch)
         ctx->batch = std::make_unique<rt::BatchEngine>(ctx->device, ctx->sm_count, fitted,
-                                                       (ctx->batch_flags & REINA_BATCH_NO_GRAPHS) == 0, trace);
+                                                       (ctx->batch_flags & REINA_BATCH_NO_GRAPHS) == 0, trace, 2);
     return *ctx->batch;
 }
 
@@ -624,8 +624,7 @@ static void render_batch(reina_ctx* ctx, const reina_render_job* jobs, uint32_t 
         ptrs[k] = &bj[k];
     }
     const uint64_t r0 = eng.rays(), s0 = eng.shadow_rays();
-    while (eng.run_wave(ptrs, st, (ctx->batch_flags & REINA_BATCH_FAIR_SHARE) == 0) > 0) {
-    }
+    eng.run_all(ptrs, st, (ctx->batch_flags & REINA_BATCH_FAIR_SHARE) == 0);
     if (host) {
         for (uint32_t k = 0; k < count; ++k) {
             const reina_render_job& j = jobs[k];

@@ -94,7 +94,7 @@ TUNING_FIELDS = ("refill", "wave_paths", "batch_flags", "trace_block", "trace_st
 ORDER_INPUT, ORDER_COHERENT = 0, 1
 
 
-DEFAULT_WAVE_PATHS = 16777216
+DEFAULT_WAVE_PATHS = 8388608
 SERVER_WAVE_PATHS = 2097152
 BATCH_NO_GRAPHS = 1
 BATCH_FAIR_SHARE = 2
