@@ -587,10 +587,11 @@ def serve_metrics(R, ctx, torch, pool, seconds: float, rate: float) -> dict:
     plain = {"p50_s": p50, "p99_s": p99, "mean_s": float(np.mean(lat)), "renders_per_s": n / plain_span,
              "samples_per_s": samples / plain_span, "span_s": plain_span}
 
-    # (b) served: the same stream through a request server (the scenes are handed to the first server
-    # and stay with it; the second policy runs on a server of its own over fresh copies)
+    # (b) served: the same stream through a request server, once per wave-slot policy (the scenes are
+    # handed to the first server and stay with it; the other policies run on servers of their own over
+    # fresh copies)
     def serve(policy: str, scenes_pool) -> tuple[dict, bool]:
-        srv = R.Server(ctx, budget_bytes=120_000_000_000, fifo=policy == "fifo", shortest=policy == "shortest")
+        srv = R.Server(ctx, budget_bytes=120_000_000_000, fifo=policy == "fifo", fair=policy == "fair")
         ids = [srv.add_scene(s) for s, _ in scenes_pool]
         outs = [np.zeros((r[3].height, r[3].width, 4), np.float32) for r in reqs]
         rids = [None] * n
@@ -618,14 +619,14 @@ def serve_metrics(R, ctx, torch, pool, seconds: float, rate: float) -> dict:
                  "scene_uploads": st["scene_uploads"], "scene_evictions": st["scene_evictions"],
                  "peak_resident_gb": st["peak_resident_bytes"] / 1e9}, all(s == R.REQ_DONE for s in states))
 
-    served, ok1 = serve("fair", pool)
+    served, ok1 = serve("shortest", pool)   # the server's default policy
     served_fifo, ok2 = serve("fifo", [scenes.batch_scene(R, ctx, k) for k in range(len(pool))])
-    served_shortest, ok3 = serve("shortest", [scenes.batch_scene(R, ctx, k) for k in range(len(pool))])
+    served_fair, ok3 = serve("fair", [scenes.batch_scene(R, ctx, k) for k in range(len(pool))])
     return {"workload": f"Poisson {rate:g}/s for {seconds:g} s ({n} requests) over the {len(pool)}-scene pool, "
                         "side U[128,1024], spp U{1..64}, depth U{4..12}, NEE+MIS; 120 GB admission budget",
             "requests": n, "samples_total": int(samples), "all_done": ok1 and ok2 and ok3,
             "plain_one_at_a_time": plain, "served": served, "served_fifo": served_fifo,
-            "served_shortest": served_shortest,
+            "served_fair_share": served_fair,
             "renders_per_s_ratio": served["renders_per_s"] / plain["renders_per_s"]}
 
 

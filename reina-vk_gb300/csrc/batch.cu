@@ -360,12 +360,13 @@ BatchEngine::~BatchEngine() {
     }
 }
 
-void BatchEngine::prepare(BatchJob& job) {
+void BatchEngine::prepare(BatchJob& job, cudaMemPool_t pool, cudaStream_t st) {
     const size_t px = (size_t)job.opt.width * job.opt.height;
     job.total = (uint64_t)job.pc.samplesPerPixel * px;
     job.cursor = 0;
     job.resolved = false;
-    job.pixel_state.alloc(px * 6 * sizeof(uint32_t));
+    if (pool) job.pixel_state.alloc_async(px * 6 * sizeof(uint32_t), pool, st);
+    else job.pixel_state.alloc(px * 6 * sizeof(uint32_t));
 }
 
 static JobGpu job_record(const BatchJob& j) {
@@ -541,6 +542,7 @@ BatchEngine::Packed BatchEngine::pack(const std::vector<BatchJob*>& jobs, bool f
         const uint64_t px = (uint64_t)j->opt.width * j->opt.height;
         const uint32_t ji = njobs++;
         jt[ji] = job_record(*j);
+        pk.members.push_back(j);
         bounces = std::max(bounces, j->pc.maxBounces);
         pk.any_nee = pk.any_nee || j->opt.mode == kModeNeeMis;
         // samples after a pixel's first start from the state its previous sample left (reference mode)
@@ -573,53 +575,70 @@ BatchEngine::Packed BatchEngine::pack(const std::vector<BatchJob*>& jobs, bool f
     return pk;
 }
 
-uint64_t BatchEngine::run_wave(const std::vector<BatchJob*>& jobs, cudaStream_t st, bool fifo) {
-    Lane& L = lanes_[0];
-    const Packed pk = pack(jobs, fifo, L);
-    if (pk.hdr.count == 0) return 0;
-    launch_body(L, pk, st);
-    launch_finish(L, pk, st);
-    check_cuda(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+bool BatchEngine::submit_wave(const std::vector<BatchJob*>& jobs, bool fifo, std::vector<BatchJob*>* members,
+                              std::vector<BatchJob*>* completed) {
+    Lane& L = lanes_[submitted_ % lanes_.size()];
+    if (L.pending) fail(REINA_ERR_STATE, "batch engine: no free lane");
+    Packed pk = pack(jobs, fifo, L);
+    if (pk.hdr.count == 0) return false;
+    Lane* prev = submitted_ > 0 ? &lanes_[(submitted_ - 1) % lanes_.size()] : nullptr;
+    if (prev == &L) prev = nullptr;   // one lane: stream order already chains the waves
+    if (prev && pk.carries) check_cuda(cudaStreamWaitEvent(L.stream, prev->finished, 0), "cudaStreamWaitEvent");
+    launch_body(L, pk, L.stream);
+    if (prev) check_cuda(cudaStreamWaitEvent(L.stream, prev->finished, 0), "cudaStreamWaitEvent");
+    launch_finish(L, pk, L.stream);
+    ++submitted_;
+    if (members) *members = std::move(pk.members);
+    if (completed) *completed = std::move(pk.completed);
+    return true;
+}
+
+void BatchEngine::wait_oldest() {
+    if (!pending()) return;
+    Lane& L = lanes_[retired_ % lanes_.size()];
+    ++retired_;
+    check_cuda(cudaEventSynchronize(L.done), "cudaEventSynchronize");
     collect(L);
-    return pk.hdr.count;
+}
+
+void BatchEngine::drain() {
+    for (Lane& L : lanes_) {
+        cudaStreamSynchronize(L.stream);
+        L.pending = false;
+    }
+    retired_ = submitted_;
+}
+
+void BatchEngine::order_after(cudaStream_t st) {
+    cudaEvent_t e;
+    check_cuda(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
+    cudaError_t err = cudaEventRecord(e, st);
+    for (Lane& L : lanes_)
+        if (err == cudaSuccess) err = cudaStreamWaitEvent(L.stream, e, 0);
+    cudaEventDestroy(e);
+    check_cuda(err, "ordering the lanes after the caller's stream");
+}
+
+void BatchEngine::order_before(cudaStream_t st) {
+    for (Lane& L : lanes_) {
+        check_cuda(cudaEventRecord(L.done, L.stream), "cudaEventRecord");
+        check_cuda(cudaStreamWaitEvent(st, L.done, 0), "cudaStreamWaitEvent");
+    }
 }
 
 void BatchEngine::run_all(const std::vector<BatchJob*>& jobs, cudaStream_t st, bool fifo) {
-    cudaEvent_t start;
-    check_cuda(cudaEventCreateWithFlags(&start, cudaEventDisableTiming), "cudaEventCreate");
-    Lane* prev = nullptr;   // the lane of the previous wave
     try {
-        check_cuda(cudaEventRecord(start, st), "cudaEventRecord");
-        for (Lane& L : lanes_) check_cuda(cudaStreamWaitEvent(L.stream, start, 0), "cudaStreamWaitEvent");
-        for (size_t k = 0;; ++k) {
-            Lane& L = lanes_[k % lanes_.size()];
-            if (L.pending) {   // the lane's previous wave (two waves back) is done: reuse its buffers
-                check_cuda(cudaEventSynchronize(L.done), "cudaEventSynchronize");
-                collect(L);
-            }
-            const Packed pk = pack(jobs, fifo, L);
-            if (pk.hdr.count == 0) break;
-            if (prev && prev != &L && pk.carries)
-                check_cuda(cudaStreamWaitEvent(L.stream, prev->finished, 0), "cudaStreamWaitEvent");
-            launch_body(L, pk, L.stream);
-            if (prev && prev != &L) check_cuda(cudaStreamWaitEvent(L.stream, prev->finished, 0), "cudaStreamWaitEvent");
-            launch_finish(L, pk, L.stream);
-            prev = &L;
+        order_after(st);
+        for (;;) {
+            if (!lane_free()) wait_oldest();   // reuse the lane of the wave two back
+            if (!submit_wave(jobs, fifo)) break;
         }
-        for (Lane& L : lanes_) {
-            check_cuda(cudaEventSynchronize(L.done), "cudaEventSynchronize");
-            check_cuda(cudaStreamWaitEvent(st, L.done, 0), "cudaStreamWaitEvent");
-        }
-        for (Lane& L : lanes_) collect(L);
+        while (pending()) wait_oldest();
+        order_before(st);
     } catch (...) {
-        for (Lane& L : lanes_) {   // nothing of this call stays in flight
-            cudaStreamSynchronize(L.stream);
-            L.pending = false;
-        }
-        cudaEventDestroy(start);
+        drain();   // nothing of this call stays in flight
         throw;
     }
-    cudaEventDestroy(start);
 }
 
 }  // namespace rt

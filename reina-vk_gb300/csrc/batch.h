@@ -62,7 +62,8 @@ struct BatchJob {
     uint64_t cursor = 0;     // next (sample * W*H + pixel) to schedule
     uint64_t total = 0;      // spp * W*H
     DeviceBuffer pixel_state;
-    bool resolved = false;
+    bool resolved = false;   // every sample is scheduled (set when the job's last wave is packed)
+    void* owner = nullptr;   // the caller's record of the job (the server's request)
 };
 
 class BatchEngine {
@@ -75,18 +76,34 @@ public:
     BatchEngine(const BatchEngine&) = delete;
     BatchEngine& operator=(const BatchEngine&) = delete;
 
-    // Allocates the job's per-pixel state (24 bytes per pixel); the job must outlive its waves.
-    static void prepare(BatchJob& job);
-    // Packs the next wave from `jobs` (fair share of the capacity, oldest first for leftovers; with
-    // `fifo`, each job in order takes all it can use), runs it on `st` in lane 0 and resolves the jobs
-    // it completes.  Returns the number of paths traced (0 = nothing to do).  Synchronizes the stream.
-    uint64_t run_wave(const std::vector<BatchJob*>& jobs, cudaStream_t st, bool fifo = false);
-    // Runs waves (packed as run_wave packs them) until every job is resolved, two in flight on the
-    // lanes' own streams when the engine has two lanes.  Each wave's finish kernel (the per-pixel sums)
-    // runs after the previous wave's, so a pixel's samples are summed in sample order; a wave holding
-    // a job whose samples carry state from the pixel's previous sample (the reference's seeding mode)
-    // starts only after the previous wave's finish.  Ordered after the work queued on `st` before the
-    // call; returns with the work queued on `st` ordered after it, and every lane synchronized.
+    // Allocates the job's per-pixel state (24 bytes per pixel); the job must outlive its waves.  With a
+    // pool, the allocation is stream-ordered on `st` (DeviceBuffer::alloc_async).
+    static void prepare(BatchJob& job, cudaMemPool_t pool = nullptr, cudaStream_t st = nullptr);
+    // Waves are packed from `jobs`: an equal share of the capacity per job with samples left, leftovers
+    // to the first jobs (or, with `fifo`, each job in list order taking all it can use), at most one
+    // sample of each pixel per wave.  Wave k runs on lane k mod lanes, on the lane's own stream.  Each
+    // wave's finish kernel (the per-pixel sums) runs after the previous wave's, so a pixel's samples are
+    // summed in sample order; a wave holding a job whose samples carry state from the pixel's previous
+    // sample (the reference's seeding mode) starts only after the previous wave's finish.
+    //
+    // Packs the next wave into the next lane, which must be free (lane_free()), and launches it.
+    // Returns false when no job has samples left to schedule.  `members` and `completed` (optional)
+    // receive the jobs in the wave and the jobs whose last samples it holds.
+    bool submit_wave(const std::vector<BatchJob*>& jobs, bool fifo, std::vector<BatchJob*>* members = nullptr,
+                     std::vector<BatchJob*>* completed = nullptr);
+    bool lane_free() const { return !lanes_[submitted_ % lanes_.size()].pending; }
+    bool pending() const { return retired_ < submitted_; }
+    // Waits for the oldest wave in flight and adds its ray counts; throws on a device error flag.
+    void wait_oldest();
+    // Waits for every wave in flight without reading their results (error and shutdown paths).
+    void drain();
+    // The lanes' next work waits for the work queued on `st` so far.
+    void order_after(cudaStream_t st);
+    // The work queued on `st` from now on waits for every wave submitted so far.
+    void order_before(cudaStream_t st);
+    // Runs waves until every job is resolved, two in flight when the engine has two lanes.  Ordered
+    // after the work queued on `st` before the call; returns with every wave complete and the work
+    // queued on `st` afterwards ordered after them.
     void run_all(const std::vector<BatchJob*>& jobs, cudaStream_t st, bool fifo = false);
     uint32_t capacity() const { return capacity_; }
     int lanes() const { return (int)lanes_.size(); }
@@ -116,7 +133,7 @@ private:
     struct Packed {
         WaveHeader hdr;
         bool any_nee = false, two = false, carries = false;
-        std::vector<BatchJob*> completed;
+        std::vector<BatchJob*> members, completed;
     };
     // Packs the next wave into the lane's host descriptor; hdr.count == 0 when nothing is left.
     Packed pack(const std::vector<BatchJob*>& jobs, bool fifo, Lane& L);
@@ -134,6 +151,7 @@ private:
     std::vector<Lane> lanes_;
     uint64_t rays_ = 0, shadow_rays_ = 0;
     uint32_t waves_ = 0;
+    uint64_t submitted_ = 0, retired_ = 0;   // waves launched / waited for
     int blocks_ext_ = 0, blocks_shade_[5] = {0, 0, 0, 0, 0}, blocks_sh_ = 0, blocks_simple_ = 0;
     int blocks_ext_two_ = 0, blocks_sh_two_ = 0;
 };

@@ -755,18 +755,20 @@ int reina_server_create(reina_ctx* ctx, const reina_server_options* o, reina_ser
     return guard([&] {
         need(ctx && out, "NULL argument");
         *out = nullptr;
-        need(!o || (o->flags & ~(uint32_t)(REINA_BATCH_NO_GRAPHS | REINA_SERVER_FIFO | REINA_SERVER_SHORTEST)) == 0,
-             "unknown server flags");
-        need(!o || (o->flags & (REINA_SERVER_FIFO | REINA_SERVER_SHORTEST)) != (REINA_SERVER_FIFO | REINA_SERVER_SHORTEST),
-             "REINA_SERVER_FIFO and REINA_SERVER_SHORTEST exclude each other");
+        const uint32_t policies = REINA_SERVER_FIFO | REINA_SERVER_SHORTEST | REINA_SERVER_FAIR_SHARE;
+        const uint32_t flags = o ? o->flags : 0u;
+        need((flags & ~(uint32_t)(REINA_BATCH_NO_GRAPHS | policies)) == 0, "unknown server flags");
+        const uint32_t policy = flags & policies;
+        need((policy & (policy - 1)) == 0,
+             "REINA_SERVER_SHORTEST, REINA_SERVER_FIFO and REINA_SERVER_FAIR_SHARE exclude each other");
         use_device(ctx);
         rt::ServerConfig cfg;
         cfg.budget = (o && o->memory_budget_bytes) ? o->memory_budget_bytes : 120000000000ull;
         cfg.max_active = (o && o->max_active_jobs) ? o->max_active_jobs : 512;
         cfg.wave_paths = o ? o->wave_paths : 0;
         cfg.graphs = !(o && (o->flags & REINA_BATCH_NO_GRAPHS));
-        cfg.fifo = o && (o->flags & REINA_SERVER_FIFO);
-        cfg.shortest = o && (o->flags & REINA_SERVER_SHORTEST);
+        cfg.fifo = policy == REINA_SERVER_FIFO;
+        cfg.shortest = policy == 0 || policy == REINA_SERVER_SHORTEST;
         auto s = std::make_unique<reina_server>();
         s->ctx = ctx;
         s->srv = std::make_unique<rt::Server>(ctx->device, ctx->sm_count, cfg);

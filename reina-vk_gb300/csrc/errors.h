@@ -32,9 +32,15 @@ public:
     ~DeviceBuffer() { release(); }
     DeviceBuffer(const DeviceBuffer&) = delete;
     DeviceBuffer& operator=(const DeviceBuffer&) = delete;
-    DeviceBuffer(DeviceBuffer&& o) noexcept : ptr_(o.ptr_), bytes_(o.bytes_) { o.ptr_ = nullptr; o.bytes_ = 0; }
+    DeviceBuffer(DeviceBuffer&& o) noexcept : ptr_(o.ptr_), bytes_(o.bytes_), stream_(o.stream_), async_(o.async_) {
+        o.ptr_ = nullptr; o.bytes_ = 0; o.async_ = false;
+    }
     DeviceBuffer& operator=(DeviceBuffer&& o) noexcept {
-        if (this != &o) { release(); ptr_ = o.ptr_; bytes_ = o.bytes_; o.ptr_ = nullptr; o.bytes_ = 0; }
+        if (this != &o) {
+            release();
+            ptr_ = o.ptr_; bytes_ = o.bytes_; stream_ = o.stream_; async_ = o.async_;
+            o.ptr_ = nullptr; o.bytes_ = 0; o.async_ = false;
+        }
         return *this;
     }
     void alloc(size_t bytes) {
@@ -43,12 +49,27 @@ public:
         check_cuda(cudaMalloc(&ptr_, bytes), "cudaMalloc");
         bytes_ = bytes;
     }
+    // Stream-ordered allocation from `pool` on `st`; release() then frees it on the same stream, without
+    // the device-wide synchronization a plain free can cause.  Usable on other streams once they are
+    // ordered after `st`.
+    void alloc_async(size_t bytes, cudaMemPool_t pool, cudaStream_t st) {
+        release();
+        if (bytes == 0) return;
+        check_cuda(cudaMallocFromPoolAsync(&ptr_, bytes, pool, st), "cudaMallocFromPoolAsync");
+        bytes_ = bytes;
+        stream_ = st;
+        async_ = true;
+    }
     // Grows (never shrinks) the allocation to at least `bytes`; contents are not preserved.
     void reserve(size_t bytes) { if (bytes > bytes_) alloc(bytes); }
     void release() {
-        if (ptr_) cudaFree(ptr_);
+        if (ptr_) {
+            if (async_) cudaFreeAsync(ptr_, stream_);
+            else cudaFree(ptr_);
+        }
         ptr_ = nullptr;
         bytes_ = 0;
+        async_ = false;
     }
     template <class T> T* as() const { return static_cast<T*>(ptr_); }
     void* get() const { return ptr_; }
@@ -61,6 +82,8 @@ public:
 private:
     void* ptr_ = nullptr;
     size_t bytes_ = 0;
+    cudaStream_t stream_ = nullptr;
+    bool async_ = false;
 };
 
 }  // namespace rt

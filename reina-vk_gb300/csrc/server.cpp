@@ -24,13 +24,23 @@ Server::Server(int device, int sm_count, const ServerConfig& cfg) : device_(devi
     if (cfg_.max_active == 0 || cfg_.max_active > kMaxWaveSegments / 2)
         fail(REINA_ERR_INVALID, "max_active_jobs must be in 1.." + std::to_string(kMaxWaveSegments / 2));
     const uint32_t wave = cfg_.wave_paths ? cfg_.wave_paths : (uint32_t)REINA_SERVER_WAVE_PATHS;
-    reserved_ = (uint64_t)wave * kPathBytes + (64u << 20);   // path state + descriptors and slack
+    reserved_ = 2 * (uint64_t)wave * kPathBytes + (64u << 20);   // two lanes of path state + descriptors and slack
     if (cfg_.budget < reserved_)
         fail(REINA_ERR_BUDGET, "memory budget " + std::to_string(cfg_.budget) + " B is below the engine's " +
                                    std::to_string(reserved_) + " B of path state");
     check_cuda(cudaSetDevice(device_), "cudaSetDevice");
     check_cuda(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
-    engine_ = std::make_unique<BatchEngine>(device_, sm_count, wave, cfg_.graphs);
+    // requests' pixel state and own images come from this pool, stream-ordered on stream_, so that
+    // admitting and finishing requests does not wait for the waves in flight
+    cudaMemPoolProps props;
+    std::memset(&props, 0, sizeof(props));
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = device_;
+    check_cuda(cudaMemPoolCreate(&pool_, &props), "cudaMemPoolCreate");
+    uint64_t keep = cfg_.budget;   // freed memory stays in the pool up to the budget
+    check_cuda(cudaMemPoolSetAttribute(pool_, cudaMemPoolAttrReleaseThreshold, &keep), "cudaMemPoolSetAttribute");
+    engine_ = std::make_unique<BatchEngine>(device_, sm_count, wave, cfg_.graphs, TraceConfig(), 2);
     t0_ = now();
     thread_ = std::thread([this] { loop(); });
 }
@@ -54,6 +64,8 @@ Server::~Server() {
     requests_.clear();
     images_.clear();
     engine_.reset();
+    if (stream_) cudaStreamSynchronize(stream_);
+    if (pool_) cudaMemPoolDestroy(pool_);
     if (stream_) cudaStreamDestroy(stream_);
 }
 
@@ -277,11 +289,11 @@ bool Server::try_admit(Request& r) {
             }
             d_accum = img->dev.as<float>();
         } else {
-            r.accum.alloc(px * kImageBytes);
+            r.accum.alloc_async(px * kImageBytes, pool_, stream_);
             resident_ += px * kImageBytes;
             if (s.pc.sampleBatch > 0)
-                check_cuda(cudaMemcpy(r.accum.get(), s.host_out, px * kImageBytes, cudaMemcpyHostToDevice),
-                           "H2D previous image");
+                check_cuda(cudaMemcpyAsync(r.accum.get(), s.host_out, px * kImageBytes, cudaMemcpyHostToDevice,
+                                           stream_), "H2D previous image");
             d_accum = r.accum.as<float>();
         }
         r.job.scene = sc.scene->device_view();
@@ -289,7 +301,10 @@ bool Server::try_admit(Request& r) {
         r.job.opt = s.opt;
         r.job.d_accum = d_accum;
         r.job.d_samples = nullptr;
-        BatchEngine::prepare(r.job);
+        r.job.owner = &r;
+        BatchEngine::prepare(r.job, pool_, stream_);
+        // the allocations (and the previous image) are complete before any lane uses them
+        check_cuda(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
     } catch (...) {
         if (r.accum.get()) {
             resident_ -= px * kImageBytes;
@@ -343,14 +358,31 @@ void Server::finish(Request& r, uint32_t state, int error, const std::string& ms
     }
 }
 
+// The loop keeps up to two waves in flight (the engine's two lanes): while one runs its last bounces the
+// next is already packed and running.  Between steps it drops cancelled requests that no wave in flight
+// holds, admits queued requests, and then either launches a wave on a free lane or waits for the oldest
+// wave; a request completes when the wave holding its last samples is done.
 void Server::loop() {
     cudaSetDevice(device_);
     std::unique_lock<std::mutex> lk(mu_);
+    std::deque<std::vector<Request*>> waves;   // the requests in each wave in flight, oldest first
+    double busy_from = 0;
+    auto schedulable = [&](const Request* r) { return !r->cancel && r->job.cursor < r->job.total; };
     for (;;) {
-        cv_work_.wait(lk, [&] { return stop_ || !queue_.empty() || !running_.empty(); });
-        if (stop_) return;
+        if (!engine_->pending())
+            cv_work_.wait(lk, [&] {
+                if (stop_ || !queue_.empty()) return true;
+                for (const Request* r : running_)
+                    if (schedulable(r) || (r->cancel && r->inflight == 0)) return true;
+                return false;
+            });
+        if (stop_) {
+            lk.unlock();
+            engine_->drain();
+            return;
+        }
         for (auto it = running_.begin(); it != running_.end();) {
-            if ((*it)->cancel) {
+            if ((*it)->cancel && (*it)->inflight == 0) {
                 finish(**it, kReqCancelled, 0, "cancelled");
                 it = running_.erase(it);
             } else {
@@ -384,55 +416,77 @@ void Server::loop() {
             running_.push_back(r);
         }
         cv_done_.notify_all();
-        if (running_.empty()) continue;
         std::vector<BatchJob*> jobs;
-        jobs.reserve(running_.size());
-        for (Request* r : running_) jobs.push_back(&r->job);
+        for (Request* r : running_)
+            if (schedulable(r)) jobs.push_back(&r->job);
         if (cfg_.shortest)   // fewest samples left first; stable: ties keep arrival order
             std::stable_sort(jobs.begin(), jobs.end(), [](const BatchJob* a, const BatchJob* b) {
                 return a->total - a->cursor < b->total - b->cursor;
             });
+        const bool launch = !jobs.empty() && engine_->lane_free();
+        if (!launch && !engine_->pending()) continue;
         lk.unlock();
         int code = 0;
         std::string err;
-        const double t = now();
+        std::vector<BatchJob*> members;
+        std::vector<Request*> done;
+        bool retired = false;
         try {
-            engine_->run_wave(jobs, stream_, cfg_.fifo || cfg_.shortest);
+            if (launch) {
+                if (!engine_->pending()) busy_from = now();
+                engine_->submit_wave(jobs, cfg_.fifo || cfg_.shortest, &members);
+            } else {
+                engine_->wait_oldest();
+                retired = true;
+            }
         } catch (const Error& e) {
             code = e.code;
             err = e.what();
+            engine_->drain();
         }
-        const double dt = now() - t;
-        // results of the requests this wave completed go to their host images outside the lock
-        std::vector<Request*> done;
-        if (!code) {
-            for (Request* r : running_)
-                if (r->job.resolved && r->spec.host_out) {
+        if (!code && retired) {
+            // the oldest wave is done: requests whose last samples it held are complete; their images go
+            // to the host outside the lock (the loop thread alone touches running requests' jobs)
+            for (Request* r : waves.front())
+                if (--r->inflight == 0 && r->job.resolved && !r->cancel) done.push_back(r);
+            waves.pop_front();
+            for (Request* r : done)
+                if (r->spec.host_out) {
                     const size_t bytes = (size_t)r->spec.opt.width * r->spec.opt.height * kImageBytes;
                     const cudaError_t ce = cudaMemcpy(r->spec.host_out, r->job.d_accum, bytes, cudaMemcpyDeviceToHost);
                     if (ce != cudaSuccess) {
                         code = REINA_ERR_CUDA;
                         err = std::string("D2H result: ") + cudaGetErrorString(ce);
+                        engine_->drain();
                         break;
                     }
                 }
         }
         lk.lock();
-        counters_.busy_s += dt;
+        if (!code && launch) {
+            std::vector<Request*> in_wave;
+            for (BatchJob* j : members) {
+                Request* r = static_cast<Request*>(j->owner);
+                r->inflight++;
+                in_wave.push_back(r);
+            }
+            waves.push_back(std::move(in_wave));
+        }
+        if (!engine_->pending()) counters_.busy_s += now() - busy_from;
         counters_.rays = engine_->rays();
         counters_.shadow_rays = engine_->shadow_rays();
         counters_.waves = engine_->waves();
         if (code) {
-            for (Request* r : running_) finish(*r, kReqFailed, code, err);
+            for (Request* r : running_) {
+                r->inflight = 0;
+                finish(*r, kReqFailed, code, err);
+            }
             running_.clear();
+            waves.clear();
         } else {
-            for (auto it = running_.begin(); it != running_.end();) {
-                if ((*it)->job.resolved) {
-                    finish(**it, kReqDone, 0, "");
-                    it = running_.erase(it);
-                } else {
-                    ++it;
-                }
+            for (Request* r : done) {
+                finish(*r, kReqDone, 0, "");
+                running_.erase(std::find(running_.begin(), running_.end(), r));
             }
         }
         cv_done_.notify_all();

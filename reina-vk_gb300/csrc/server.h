@@ -94,6 +94,7 @@ private:
         RequestStatus status;
         double t_submit = 0, t_admit = 0;
         bool cancel = false;
+        uint32_t inflight = 0;    // waves in flight holding samples of this request
         size_t job_bytes = 0;     // accounted while running
         BatchJob job;
         DeviceBuffer accum;       // own accumulation image when there is no image key
@@ -108,7 +109,8 @@ private:
 
     int device_;
     ServerConfig cfg_;
-    cudaStream_t stream_ = nullptr;
+    cudaStream_t stream_ = nullptr;   // orders the pool's allocations and frees
+    cudaMemPool_t pool_ = nullptr;    // requests' pixel state and own images
     std::unique_ptr<BatchEngine> engine_;
     std::thread thread_;
     std::mutex mu_;

@@ -169,6 +169,7 @@ class _ServerStats(C.Structure):
 REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED, REQ_CANCELLED = range(5)
 SERVER_FIFO = 2
 SERVER_SHORTEST = 4
+SERVER_FAIR_SHARE = 8
 
 
 class _TuneResult(C.Structure):
@@ -769,9 +770,12 @@ class Server:
     kept images resident with LRU eviction and runs admitted requests together in shared waves."""
 
     def __init__(self, ctx: Context, budget_bytes: int = 0, max_active: int = 0, wave_paths: int = 0,
-                 graphs: bool = True, fifo: bool = False, shortest: bool = False):
+                 graphs: bool = True, fifo: bool = False, shortest: bool = False, fair: bool = False):
+        """Wave-slot policy: shortest remaining work first (the default, or shortest=True), fifo=True or
+        fair=True (an equal share per running request); at most one may be given."""
         self.ctx = ctx
-        flags = (0 if graphs else BATCH_NO_GRAPHS) | (SERVER_FIFO if fifo else 0) | (SERVER_SHORTEST if shortest else 0)
+        flags = ((0 if graphs else BATCH_NO_GRAPHS) | (SERVER_FIFO if fifo else 0) | (SERVER_SHORTEST if shortest else 0)
+                 | (SERVER_FAIR_SHARE if fair else 0))
         o = _ServerOptions(budget_bytes, max_active, wave_paths, flags, 0)
         h = C.c_void_p()
         _check(_lib.reina_server_create(ctx.handle, C.byref(o), C.byref(h)))

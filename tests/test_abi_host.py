@@ -261,8 +261,10 @@ def test_server_needs_a_gpu_context(R, host_ctx):
     assert e.value.code == R.REINA_ERR_STATE
 
 
-def test_server_policy_flags_exclude_each_other(R, host_ctx):
+@pytest.mark.parametrize("kw", [dict(fifo=True, shortest=True), dict(fifo=True, fair=True),
+                                dict(shortest=True, fair=True)])
+def test_server_policy_flags_exclude_each_other(R, host_ctx, kw):
     with pytest.raises(R.ReinaError) as e:
-        R.Server(host_ctx, fifo=True, shortest=True)
+        R.Server(host_ctx, **kw)
     assert e.value.code == R.REINA_ERR_INVALID
 

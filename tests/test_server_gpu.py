@@ -110,7 +110,8 @@ def test_same_alone_and_in_the_mix(R, alone, policy):
     (fair-share, first-come first-served and shortest-remaining-work wave packing)."""
     weights, ref = alone
     ctx = R.Context(0)
-    ctx_srv, ids = start_server(R, ctx, wave_paths=4096, fifo=policy == "fifo", shortest=policy == "shortest")
+    ctx_srv, ids = start_server(R, ctx, wave_paths=4096, fifo=policy == "fifo", shortest=policy == "shortest",
+                                fair=policy == "fair")
     srv = ctx_srv
     rids, outs = submit_all(R, srv, ids, weights, request_specs(), stagger_s=0.002, threads=3)
     for n, rid in enumerate(rids):
@@ -137,7 +138,7 @@ def test_budget_forces_lru_eviction(R, alone):
         sizes[k] = s.stats()["device_bytes"]
         s.close()
     wave = 4096
-    reserved = wave * 164 + (64 << 20)
+    reserved = 2 * wave * 164 + (64 << 20)
     specs = request_specs()
     biggest_req = max(W * H * 40 for _, W, H, *_ in specs)
     budget = reserved + max(sizes.values()) + 2 * biggest_req + 4096
@@ -157,7 +158,7 @@ def test_budget_forces_lru_eviction(R, alone):
 def test_request_larger_than_budget_is_rejected(R):
     ctx = R.Context(0)
     wave = 4096
-    srv, ids = start_server(R, ctx, budget_bytes=wave * 164 + (64 << 20) + (8 << 20), wave_paths=wave)
+    srv, ids = start_server(R, ctx, budget_bytes=2 * wave * 164 + (64 << 20) + (8 << 20), wave_paths=wave)
     with pytest.raises(R.ReinaError) as e:
         srv.submit(ids["cornell"], make_pc(R, 1.0, 1024, 1024, 1, 1), R.render_options(1024, 1024),
                    np.zeros((1024, 1024, 4), np.float32))
@@ -206,7 +207,7 @@ def test_kept_images_are_evicted_and_restored(R):
     W, H = 64, 64
     wave = 4096
     # room for the scene and two kept images besides the running request (40 B/px): the third key evicts
-    budget = wave * 164 + (64 << 20) + scene_bytes + 2 * W * H * 40
+    budget = 2 * wave * 164 + (64 << 20) + scene_bytes + 2 * W * H * 40
     srv = R.Server(ctx, budget_bytes=budget, wave_paths=wave, max_active=1)
     sid = srv.add_scene(d.to_product(R, ctx))
     firsts = []
