@@ -349,8 +349,9 @@ def _timed_frames(torch, fn, frames: int) -> float:
 
 
 def render_metrics(R, ctx, torch, frames: int, scene_large) -> dict:
-    """The large scene (1920x1080, 64 spp, 12 bounces, NEE+MIS, light + constant environment) rendered by
-    the wavefront integrator and by the plain megakernel; and the Cornell room (256x256, 16 spp, 8)."""
+    """The large scene (1920x1080, 64 spp, 12 bounces, NEE+MIS, light + constant environment) rendered in
+    the three forms of reina_render_device (the wave engine, the default; the pass-by-pass wavefront; the
+    plain megakernel); and the Cornell room (256x256, 16 spp, 8 bounces) the same way."""
     import scenes
 
     out = {}
@@ -360,8 +361,9 @@ def render_metrics(R, ctx, torch, frames: int, scene_large) -> dict:
     pc = R.push_consts(iv, ip, total_emissive_weight=scene_large.emissive_weight, spp=64, max_bounces=12,
                        focus_dist=3.6)
     acc = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
-    for name, mega in (("wavefront", False), ("megakernel", True)):
-        opts = R.render_options(W, H, R.MODE_NEE_MIS, 1, R.ENV_CONSTANT, (0.3, 0.3, 0.35), megakernel=mega)
+    for name, mega, pbp in (("wavefront", False, False), ("pass_by_pass", False, True), ("megakernel", True, False)):
+        opts = R.render_options(W, H, R.MODE_NEE_MIS, 1, R.ENV_CONSTANT, (0.3, 0.3, 0.35), megakernel=mega,
+                                pass_by_pass=pbp)
         _, _, st = R.render(ctx, scene_large, pc, opts)   # ray counts of one frame
         dt = _timed_frames(torch, lambda: R.render_device(ctx, scene_large, pc, opts, acc.data_ptr(), 0, sptr), frames)
         out[f"large_{name}"] = {"s_per_frame": dt, "segments_per_s": st["rays"] / dt,
@@ -372,8 +374,8 @@ def render_metrics(R, ctx, torch, frames: int, scene_large) -> dict:
     iv, ip = scenes.cornell_camera(R, 256, 256)
     pc = R.push_consts(iv, ip, total_emissive_weight=sc.emissive_weight, spp=16, max_bounces=8)
     acc = torch.zeros((256, 256, 4), dtype=torch.float32, device="cuda")
-    for name, mega in (("wavefront", False), ("megakernel", True)):
-        opts = R.render_options(256, 256, R.MODE_NEE_MIS, 1, megakernel=mega)
+    for name, mega, pbp in (("wavefront", False, False), ("pass_by_pass", False, True), ("megakernel", True, False)):
+        opts = R.render_options(256, 256, R.MODE_NEE_MIS, 1, megakernel=mega, pass_by_pass=pbp)
         _, _, st = R.render(ctx, sc, pc, opts)
         dt = _timed_frames(torch, lambda: R.render_device(ctx, sc, pc, opts, acc.data_ptr(), 0, sptr), frames)
         out[f"cornell_{name}"] = {"s_per_frame": dt, "paths_per_s": 256 * 256 * 16 / dt,
@@ -444,10 +446,11 @@ def build_pool(R, ctx, n_scenes: int):
 def batch_metrics(R, ctx, torch, built, setup_s: float, mega_scenes: int) -> dict:
     """The batched workload: n_scenes independent scenes (geodesic spheres with 1k-500k triangles, per-face
     Disney/glass materials, ground, quad light, constant environment; side U[128,1024], spp U{1..64},
-    depth U{4..12}, NEE+MIS), all rendered once (a) in one reina_render_batch_device call and (b) one
-    scene at a time with the single-scene wavefront (reina_render_device); (a) and (b) give the same
-    images (checked here).  The first mega_scenes scenes are also rendered (c) one at a time by the plain
-    megakernel, with (a) re-timed on the same subset.  Device time by CUDA events around each form."""
+    depth U{4..12}, NEE+MIS), all rendered once (a) in one reina_render_batch_device call, (b) one scene
+    at a time with reina_render_device (each frame the wave engine's only job) and (c) one scene at a time
+    with the pass-by-pass wavefront; all three give the same images (checked here).  The first
+    mega_scenes scenes are also rendered (d) one at a time by the plain megakernel, with (a) re-timed on
+    the same subset.  Device time by CUDA events around each form."""
     import scenes
 
     n_scenes = len(built)
@@ -489,16 +492,18 @@ def batch_metrics(R, ctx, torch, built, setup_s: float, mega_scenes: int) -> dic
         torch.cuda.synchronize()
         return ev[0].elapsed_time(ev[1]) * 1e-3, r
 
-    def plain(js, mega: bool):
+    def plain(js, mega: bool = False, pbp: bool = False):
         for j in js:
             o = R.render_options(j.opts.width, j.opts.height, j.opts.mode, j.opts.seed, j.opts.env_mode,
-                                 tuple(j.opts.env_color), megakernel=mega)
+                                 tuple(j.opts.env_color), megakernel=mega, pass_by_pass=pbp)
             R.render_device(ctx, j.scene, j.pc, o, j.d_accum, 0, sptr)
 
     t_batch, st = timed(lambda: R.render_batch_device(ctx, jobs, sptr))
     batched_imgs = [a.clone() for a in accs]
-    t_plain, _ = timed(lambda: plain(jobs, False))
+    t_plain, _ = timed(lambda: plain(jobs))
     identical = all(torch.equal(a, b) for a, b in zip(accs, batched_imgs))
+    t_pbp, _ = timed(lambda: plain(jobs, pbp=True))
+    identical = identical and all(torch.equal(a, b) for a, b in zip(accs, batched_imgs))
     del batched_imgs
     seg, shadow = st["rays"], st["shadow_rays"]
     n_smp = sum(samples)
@@ -516,16 +521,19 @@ def batch_metrics(R, ctx, torch, built, setup_s: float, mega_scenes: int) -> dic
                      "chosen": {k: best[k] for k in ("wave_paths", "trace_block", "trace_stack")}},
         "batched": {"s": t_batch, "renders_per_s": n_scenes / t_batch, "segments_per_s": seg / t_batch,
                     "rays_per_s": (seg + shadow) / t_batch, "samples_per_s": n_smp / t_batch},
-        "plain_wavefront": {"s": t_plain, "renders_per_s": n_scenes / t_plain, "segments_per_s": seg / t_plain,
-                            "samples_per_s": n_smp / t_plain},
-        "images_identical_batched_vs_plain_wavefront": bool(identical),
-        "speedup_vs_plain_wavefront": t_plain / t_batch,
+        "one_at_a_time": {"s": t_plain, "renders_per_s": n_scenes / t_plain, "segments_per_s": seg / t_plain,
+                          "samples_per_s": n_smp / t_plain},
+        "one_at_a_time_pass_by_pass": {"s": t_pbp, "renders_per_s": n_scenes / t_pbp, "segments_per_s": seg / t_pbp,
+                                       "samples_per_s": n_smp / t_pbp},
+        "images_identical_all_forms": bool(identical),
+        "speedup_vs_one_at_a_time": t_plain / t_batch,
+        "speedup_vs_one_at_a_time_pass_by_pass": t_pbp / t_batch,
     }
     m = min(mega_scenes, n_scenes)
     if m > 0:
         sub = jobs[:m]
         t_sub, _ = timed(lambda: R.render_batch_device(ctx, sub, sptr))
-        t_mega, _ = timed(lambda: plain(sub, True))
+        t_mega, _ = timed(lambda: plain(sub, mega=True))
         out["megakernel_subset"] = {
             "scenes": m, "samples_total": int(sum(samples[:m])),
             "batched": {"s": t_sub, "renders_per_s": m / t_sub},
@@ -564,28 +572,35 @@ def serve_metrics(R, ctx, torch, pool, seconds: float, rate: float) -> dict:
     def pct(lat):
         return float(np.percentile(lat, 50)), float(np.percentile(lat, 99))
 
-    # (a) plain: one request at a time, in arrival order, images copied to the host
+    # (a) plain: one request at a time, in arrival order, images copied to the host; as the frame on
+    # the wave engine (reina_render_device's default) and as the pass-by-pass wavefront
     sptr = torch.cuda.current_stream().cuda_stream
     host = {}
     for at, si, pc, opts, side in reqs:
         host.setdefault(side, np.zeros((side, side, 4), np.float32))
     dev = torch.zeros((1024, 1024, 4), dtype=torch.float32, device="cuda")
-    torch.cuda.synchronize()
-    lat = []
-    rays = 0
-    t0 = time.perf_counter()
-    for at, si, pc, opts, side in reqs:
-        now = time.perf_counter() - t0
-        if now < at:
-            time.sleep(at - now)
-        R.render_device(ctx, pool[si][0], pc, opts, dev.data_ptr(), 0, sptr)
+
+    def one_at_a_time(pass_by_pass: bool) -> dict:
         torch.cuda.synchronize()
-        host[side][...] = dev.view(-1)[: side * side * 4].view(side, side, 4).cpu().numpy()
-        lat.append(time.perf_counter() - t0 - at)
-    plain_span = time.perf_counter() - t0 - reqs[0][0]
-    p50, p99 = pct(lat)
-    plain = {"p50_s": p50, "p99_s": p99, "mean_s": float(np.mean(lat)), "renders_per_s": n / plain_span,
-             "samples_per_s": samples / plain_span, "span_s": plain_span}
+        lat = []
+        t0 = time.perf_counter()
+        for at, si, pc, opts, side in reqs:
+            now = time.perf_counter() - t0
+            if now < at:
+                time.sleep(at - now)
+            o = R.render_options(opts.width, opts.height, opts.mode, opts.seed, opts.env_mode, tuple(opts.env_color),
+                                 pass_by_pass=pass_by_pass)
+            R.render_device(ctx, pool[si][0], pc, o, dev.data_ptr(), 0, sptr)
+            torch.cuda.synchronize()
+            host[side][...] = dev.view(-1)[: side * side * 4].view(side, side, 4).cpu().numpy()
+            lat.append(time.perf_counter() - t0 - at)
+        span = time.perf_counter() - t0 - reqs[0][0]
+        p50, p99 = pct(lat)
+        return {"p50_s": p50, "p99_s": p99, "mean_s": float(np.mean(lat)), "renders_per_s": n / span,
+                "samples_per_s": samples / span, "span_s": span}
+
+    plain = one_at_a_time(False)
+    plain_pbp = one_at_a_time(True)
 
     # (b) served: the same stream through a request server, once per wave-slot policy (the scenes are
     # handed to the first server and stay with it; the other policies run on servers of their own over
@@ -625,9 +640,10 @@ def serve_metrics(R, ctx, torch, pool, seconds: float, rate: float) -> dict:
     return {"workload": f"Poisson {rate:g}/s for {seconds:g} s ({n} requests) over the {len(pool)}-scene pool, "
                         "side U[128,1024], spp U{1..64}, depth U{4..12}, NEE+MIS; 120 GB admission budget",
             "requests": n, "samples_total": int(samples), "all_done": ok1 and ok2 and ok3,
-            "plain_one_at_a_time": plain, "served": served, "served_fifo": served_fifo,
-            "served_fair_share": served_fair,
-            "renders_per_s_ratio": served["renders_per_s"] / plain["renders_per_s"]}
+            "plain_one_at_a_time": plain, "plain_one_at_a_time_pass_by_pass": plain_pbp,
+            "served": served, "served_fifo": served_fifo, "served_fair_share": served_fair,
+            "renders_per_s_ratio": served["renders_per_s"] / plain["renders_per_s"],
+            "renders_per_s_ratio_vs_pass_by_pass": served["renders_per_s"] / plain_pbp["renders_per_s"]}
 
 
 def cpu_baseline(tris, rays, sample: int) -> dict:

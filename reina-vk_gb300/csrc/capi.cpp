@@ -458,14 +458,39 @@ static rt::RenderOpts render_opts(const RtPushConsts* pc, const reina_render_opt
     r.seed = o->seed;
     r.env_mode = o->env_mode;
     for (int k = 0; k < 3; ++k) r.env_color[k] = o->env_color[k];
-    need((o->flags & ~(uint32_t)REINA_RENDER_MEGAKERNEL) == 0, "unknown render flags");
+    need((o->flags & ~(uint32_t)(REINA_RENDER_MEGAKERNEL | REINA_RENDER_PASS_BY_PASS)) == 0, "unknown render flags");
+    need((o->flags & (REINA_RENDER_MEGAKERNEL | REINA_RENDER_PASS_BY_PASS)) !=
+             (REINA_RENDER_MEGAKERNEL | REINA_RENDER_PASS_BY_PASS),
+         "REINA_RENDER_MEGAKERNEL and REINA_RENDER_PASS_BY_PASS exclude each other");
     r.megakernel = (o->flags & REINA_RENDER_MEGAKERNEL) != 0;
+    r.pass_by_pass = (o->flags & REINA_RENDER_PASS_BY_PASS) != 0;
     return r;
 }
 
 static void check_render_scene(const rt::Scene& s, const RtPushConsts* pc, const reina_render_options* o) {
     if (o->mode == REINA_MODE_NEE_MIS && s.device_view().emissive_count > 0 && !(pc->totalEmissiveWeight > 0.0f))
         fail(REINA_ERR_INVALID, "totalEmissiveWeight must be positive for NEE (use reina_scene_emissive_weight)");
+}
+
+// Validates every job, then runs waves until all are resolved.  `host`: the job buffers are host memory
+// and are staged through device copies.  `force`: the traversal variant to use instead of the context's
+// (or the batch autotune cache's).
+static void render_batch(reina_ctx* ctx, const reina_render_job* jobs, uint32_t count, bool host, cudaStream_t st,
+                         reina_render_stats* stats, const rt::TraceConfig* force = nullptr);
+
+// One frame as the wave engine's only job (the default form of reina_render / reina_render_device).
+static void render_on_engine(reina_ctx* ctx, const reina_scene* scene, const RtPushConsts* pc,
+                             const reina_render_options* o, const rt::RenderOpts& r, void* accum, void* samples,
+                             bool host, cudaStream_t st, reina_render_stats* stats) {
+    reina_render_job job;
+    std::memset(&job, 0, sizeof(job));
+    job.scene = scene;
+    job.push_consts = *pc;
+    job.options = *o;
+    job.accum_rgba32f = static_cast<float*>(accum);
+    job.samples_rgb32f = static_cast<float*>(samples);
+    const rt::TraceConfig trace = r.trace;
+    render_batch(ctx, &job, 1, host, st, stats, &trace);
 }
 
 int reina_render_device(reina_ctx* ctx, const reina_scene* scene, const RtPushConsts* pc, const reina_render_options* o,
@@ -478,6 +503,10 @@ int reina_render_device(reina_ctx* ctx, const reina_scene* scene, const RtPushCo
         check_render_scene(s, pc, o);
         need(d_accum != nullptr && ((uintptr_t)d_accum % 16) == 0, "accumulation buffer must be non-NULL and 16-byte aligned");
         use_device(ctx);
+        if (!r.megakernel && !r.pass_by_pass) {
+            render_on_engine(ctx, scene, pc, o, r, d_accum, d_samples, false, static_cast<cudaStream_t>(stream), nullptr);
+            return;
+        }
         rt::render_frame(ctx->render, s.device_view(), *pc, r, static_cast<float*>(d_accum), static_cast<float*>(d_samples),
                          ctx->sm_count, static_cast<cudaStream_t>(stream), nullptr);
     });
@@ -508,6 +537,10 @@ int reina_render(reina_ctx* ctx, const reina_scene* scene, const RtPushConsts* p
         check_render_scene(s, pc, o);
         need(accum != nullptr, "accumulation buffer is NULL");
         use_device(ctx);
+        if (!r.megakernel && !r.pass_by_pass) {
+            render_on_engine(ctx, scene, pc, o, r, accum, samples, true, ctx->streams[0], stats);
+            return;
+        }
         auto t0 = std::chrono::steady_clock::now();
         const size_t P = (size_t)r.width * r.height;
         cudaStream_t st = ctx->streams[0];
@@ -555,17 +588,24 @@ static uint32_t fit_wave(uint32_t wave, uint64_t samples) {
 
 // The context's batch engine, rebuilt when the wanted wave size or traversal variant changed (the
 // cached autotuned ones for this batch when the context uses the cache, else the context's tuning).
-static rt::BatchEngine& batch_engine(reina_ctx* ctx, const reina_render_job* jobs, uint32_t count) {
+static rt::BatchEngine& batch_engine(reina_ctx* ctx, const reina_render_job* jobs, uint32_t count,
+                                     const rt::TraceConfig* force) {
     uint32_t wave = ctx->wave_paths;
     rt::TraceConfig trace = ctx->trace;
     rt::TuneEntry e;
     uint64_t tris = 0, samples = 0;
     batch_key(jobs, count, &tris, &samples);
-    if (ctx->autotune_mode == REINA_AUTOTUNE_CACHED &&
-        ctx->tune.get(rt::kTuneBatch, rt::tune_bucket(tris), rt::tune_bucket(samples), &e)) {
+    if (force) {
+        trace = *force;
+    } else if (ctx->autotune_mode == REINA_AUTOTUNE_CACHED &&
+               ctx->tune.get(rt::kTuneBatch, rt::tune_bucket(tris), rt::tune_bucket(samples), &e)) {
         trace = e.trace;
         if (e.wave_paths) wave = e.wave_paths;
     }
+    // a wave holds at most one sample of each pixel: no more slots than the jobs have pixels
+    uint64_t pixels = 0;
+    for (uint32_t k = 0; k < count; ++k) pixels += (uint64_t)jobs[k].options.width * jobs[k].options.height;
+    samples = std::min(samples, pixels);
     // an engine between the batch's fitted size and the wanted one is kept (a job's images do not
     // depend on how the waves are cut), so batches of changing sizes do not rebuild it each call
     const uint32_t fitted = fit_wave(wave, samples);
@@ -578,10 +618,8 @@ static rt::BatchEngine& batch_engine(reina_ctx* ctx, const reina_render_job* job
     return *ctx->batch;
 }
 
-// Validates every job, then runs waves until all are resolved.  `host`: the job buffers are host memory
-// and are staged through per-job device copies.
 static void render_batch(reina_ctx* ctx, const reina_render_job* jobs, uint32_t count, bool host, cudaStream_t st,
-                         reina_render_stats* stats) {
+                         reina_render_stats* stats, const rt::TraceConfig* force) {
     need(ctx != nullptr, "ctx is NULL");
     need(count == 0 || jobs != nullptr, "jobs is NULL");
     std::vector<rt::BatchJob> bj(count);
@@ -590,7 +628,7 @@ static void render_batch(reina_ctx* ctx, const reina_render_job* jobs, uint32_t 
         const rt::Scene& s = built_scene(j.scene);
         need(j.scene->ctx == ctx, "scene belongs to another context");
         const rt::RenderOpts r = render_opts(&j.push_consts, &j.options);
-        need(!r.megakernel, "batched jobs run the wavefront (options.flags must be 0)");
+        need(!r.megakernel && !r.pass_by_pass, "batched jobs run the wave engine (options.flags must be 0)");
         check_render_scene(s, &j.push_consts, &j.options);
         need(j.accum_rgba32f != nullptr, "accumulation buffer is NULL");
         if (!host) need(((uintptr_t)j.accum_rgba32f % 16) == 0, "accumulation buffer must be 16-byte aligned");
@@ -600,22 +638,29 @@ static void render_batch(reina_ctx* ctx, const reina_render_job* jobs, uint32_t 
     }
     use_device(ctx);
     const auto t0 = std::chrono::steady_clock::now();
-    rt::BatchEngine& eng = batch_engine(ctx, jobs, count);
-    std::vector<rt::DeviceBuffer> acc(host ? count : 0), smp(host ? count : 0);
+    rt::BatchEngine& eng = batch_engine(ctx, jobs, count, force);
+    // host buffers are staged through device copies: the context's own staging buffers for one job,
+    // buffers of the call's own for more
+    std::vector<rt::DeviceBuffer> acc_own(host && count > 1 ? count : 0), smp_own(host && count > 1 ? count : 0);
+    std::vector<rt::DeviceBuffer*> acc(host ? count : 0), smp(host ? count : 0);
+    for (uint32_t k = 0; k < acc.size(); ++k) {
+        acc[k] = count > 1 ? &acc_own[k] : &ctx->accum;
+        smp[k] = count > 1 ? &smp_own[k] : &ctx->samples;
+    }
     std::vector<rt::BatchJob*> ptrs(count);
     for (uint32_t k = 0; k < count; ++k) {
         const reina_render_job& j = jobs[k];
         const size_t px = (size_t)j.options.width * j.options.height;
         rt::BatchEngine::prepare(bj[k]);
         if (host) {
-            acc[k].alloc(px * 4 * sizeof(float));
+            acc[k]->reserve(px * 4 * sizeof(float));
             if (j.push_consts.sampleBatch > 0)
-                check_cuda(cudaMemcpyAsync(acc[k].get(), j.accum_rgba32f, px * 4 * sizeof(float), cudaMemcpyHostToDevice, st),
-                           "H2D accum");
-            bj[k].d_accum = acc[k].as<float>();
+                check_cuda(cudaMemcpyAsync(acc[k]->get(), j.accum_rgba32f, px * 4 * sizeof(float), cudaMemcpyHostToDevice,
+                                           st), "H2D accum");
+            bj[k].d_accum = acc[k]->as<float>();
             if (j.samples_rgb32f) {
-                smp[k].alloc(px * j.push_consts.samplesPerPixel * 3 * sizeof(float));
-                bj[k].d_samples = smp[k].as<float>();
+                smp[k]->reserve(px * j.push_consts.samplesPerPixel * 3 * sizeof(float));
+                bj[k].d_samples = smp[k]->as<float>();
             }
         } else {
             bj[k].d_accum = static_cast<float*>(j.accum_rgba32f);
@@ -629,10 +674,10 @@ static void render_batch(reina_ctx* ctx, const reina_render_job* jobs, uint32_t 
         for (uint32_t k = 0; k < count; ++k) {
             const reina_render_job& j = jobs[k];
             const size_t px = (size_t)j.options.width * j.options.height;
-            check_cuda(cudaMemcpyAsync(j.accum_rgba32f, acc[k].get(), px * 4 * sizeof(float), cudaMemcpyDeviceToHost, st),
+            check_cuda(cudaMemcpyAsync(j.accum_rgba32f, acc[k]->get(), px * 4 * sizeof(float), cudaMemcpyDeviceToHost, st),
                        "D2H accum");
             if (j.samples_rgb32f)
-                check_cuda(cudaMemcpyAsync(j.samples_rgb32f, smp[k].get(), px * j.push_consts.samplesPerPixel * 3 * sizeof(float),
+                check_cuda(cudaMemcpyAsync(j.samples_rgb32f, smp[k]->get(), px * j.push_consts.samplesPerPixel * 3 * sizeof(float),
                                            cudaMemcpyDeviceToHost, st),
                            "D2H samples");
         }
@@ -1006,8 +1051,11 @@ int reina_autotune_render(reina_ctx* ctx, const reina_scene* scene, const RtPush
         for (const rt::TraceConfig& c : cands) {
             r.trace = c;
             const double ms = time_calls(st, 2, [&] {
-                rt::render_frame(ctx->render, s.device_view(), one, r, ctx->accum.as<float>(), nullptr, ctx->sm_count, st,
-                                 nullptr);
+                if (r.pass_by_pass)
+                    rt::render_frame(ctx->render, s.device_view(), one, r, ctx->accum.as<float>(), nullptr, ctx->sm_count,
+                                     st, nullptr);
+                else   // the default form: the frame as the wave engine's one job
+                    render_on_engine(ctx, scene, &one, o, r, ctx->accum.get(), nullptr, false, st, nullptr);
             });
             if (is_default(c)) best.default_ms = ms;
             if (ms < best.best_ms) {

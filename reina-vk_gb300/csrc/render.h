@@ -21,6 +21,7 @@ struct RenderOpts {
     uint32_t env_mode = 0;          // 0 sky gradient (raytrace.rmiss.glsl), 1 constant colour
     float env_color[3] = {0, 0, 0};
     bool megakernel = false;        // plain form: one kernel, one thread per pixel (no queues)
+    bool pass_by_pass = false;      // wavefront one sample pass at a time, direct launches (not the wave engine)
     TraceConfig trace;              // traversal kernels' launch configuration (same images for every setting)
 };
 

@@ -124,6 +124,7 @@ class RenderOptions(C.Structure):
 
 
 RENDER_MEGAKERNEL = 1
+RENDER_PASS_BY_PASS = 2
 
 
 class BloomPushConsts(C.Structure):
@@ -230,11 +231,13 @@ def push_consts(inv_view, inv_proj, sample_batch=0, total_emissive_weight=0.0, f
 
 
 def render_options(width, height, mode=MODE_REINA, seed=1, env_mode=ENV_SKY, env_color=(0.0, 0.0, 0.0),
-                   megakernel=False) -> RenderOptions:
+                   megakernel=False, pass_by_pass=False) -> RenderOptions:
+    """reina_render_options.  Default form: the wave engine; megakernel=True: one thread per pixel;
+    pass_by_pass=True: the wavefront one sample pass at a time with direct launches."""
     o = RenderOptions(width, height, mode, seed, env_mode)
     for k in range(3):
         o.env_color[k] = float(env_color[k])
-    o.flags = RENDER_MEGAKERNEL if megakernel else 0
+    o.flags = (RENDER_MEGAKERNEL if megakernel else 0) | (RENDER_PASS_BY_PASS if pass_by_pass else 0)
     return o
 
 

@@ -218,9 +218,12 @@ def test_batch_validation_on_host(R, host_ctx):
     s.build()
     iv, ip = R.camera_matrices((0, 0, 3), (0, 0, -1))
     pc = R.push_consts(iv, ip, spp=1, total_emissive_weight=s.emissive_weight)
-    bad = R.render_options(4, 4, megakernel=True)
-    with pytest.raises(R.ReinaError) as e:
-        R.render_batch(host_ctx, [R.RenderJob(s, pc, bad)])
+    for bad in (R.render_options(4, 4, megakernel=True), R.render_options(4, 4, pass_by_pass=True)):
+        with pytest.raises(R.ReinaError) as e:
+            R.render_batch(host_ctx, [R.RenderJob(s, pc, bad)])
+        assert e.value.code == R.REINA_ERR_INVALID
+    with pytest.raises(R.ReinaError) as e:   # the two plain forms exclude each other
+        R.render(host_ctx, s, pc, R.render_options(4, 4, megakernel=True, pass_by_pass=True))
     assert e.value.code == R.REINA_ERR_INVALID
     with pytest.raises(R.ReinaError) as e:
         R.render_batch(host_ctx, [R.RenderJob(s, pc, R.render_options(4, 4))])

@@ -144,3 +144,25 @@ def test_megakernel_matches_wavefront(R, O, gpu_ctx, mode):
     osc = d.to_oracle(O)
     _, o_smp = osc.render(pc, W, H, mode=mode, want_samples=True)
     assert agree(s_m, o_smp).mean() >= 0.99
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+@pytest.mark.parametrize("sample_batch", [0, 2])
+def test_pass_by_pass_equals_wave_engine(R, gpu_ctx, mode, sample_batch):
+    """The default form (the frame as the wave engine's one job) and the pass-by-pass wavefront give the
+    same samples, image and ray counts, bit for bit, also when blending into a previous image."""
+    d = scenes.material_zoo(R)
+    scene = d.to_product(R, gpu_ctx)
+    W, H = 80, 56
+    iv, ip = scenes.cornell_camera(R, W, H)
+    pc = R.push_consts(iv, ip, total_emissive_weight=scene.emissive_weight, spp=5, max_bounces=9, focus_dist=3.4)
+    pc.sampleBatch = sample_batch
+    prev = np.random.default_rng(3).random((H, W, 4), dtype=np.float32)
+    out = []
+    for pbp in (False, True):
+        acc, smp, st = R.render(gpu_ctx, scene, pc, R.render_options(W, H, mode, 7, pass_by_pass=pbp),
+                                want_samples=True, accum=prev.copy())
+        out.append((acc, smp, st))
+    assert np.array_equal(out[0][0], out[1][0], equal_nan=True)
+    assert np.array_equal(out[0][1], out[1][1], equal_nan=True)
+    assert out[0][2]["rays"] == out[1][2]["rays"] and out[0][2]["shadow_rays"] == out[1][2]["shadow_rays"]
