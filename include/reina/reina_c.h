@@ -74,12 +74,13 @@ int reina_ctx_sm_count(const reina_ctx* ctx);
  *   trace_stack: shared-memory traversal stack entries per thread, 8, 12 or 16 (default 12); deeper
  *            levels spill to local memory.
  *   trace_order: the order a ray cast traces its rays in (below).
- *   wave_paths: path slots of one wave of a batched render (0 = REINA_DEFAULT_WAVE_PATHS); the path
- *            state costs 164 bytes per slot, twice over: a batched render keeps two waves in flight on
- *            two streams, so that one wave's last bounces (few long paths) overlap the next wave's
- *            first ones.  A batch with fewer paths gets no more slots than it has
- *            paths, rounded up to a power of two (at least 2^20); an engine already built with more
- *            slots than that (up to wave_paths) is reused.
+ *   wave_paths: path slots of one wave of a batched render or frame (0 = REINA_DEFAULT_WAVE_PATHS);
+ *            the path state costs 164 bytes per slot and wave in flight (wave_lanes): the waves run on
+ *            streams of their own, so that one wave's last bounces (few long paths) overlap the next
+ *            waves' first ones.  A wave holds at most one sample of each pixel, so a batch gets no more
+ *            slots than its jobs have pixels (or samples, if fewer), rounded up to a power of two (at
+ *            least 2^16); an engine already built with more slots than that (up to wave_paths) is
+ *            reused.
  *   batch_flags: REINA_BATCH_NO_GRAPHS launches each wave's kernels one by one instead of replaying a
  *            captured CUDA graph.  Waves are packed with the jobs in list order, each taking all it can
  *            use (one sample of each of its pixels), so that a wave holds few scenes and their data
@@ -95,7 +96,9 @@ typedef struct reina_tuning {
     uint32_t trace_block;
     uint32_t trace_stack;
     uint32_t trace_order;        /* ray casts, grid form: REINA_ORDER_INPUT (default) or REINA_ORDER_COHERENT */
-    uint32_t reserved[2];
+    uint32_t wave_lanes;         /* waves in flight in batched renders and frames, 1..16
+                                  * (0 = REINA_DEFAULT_WAVE_LANES) */
+    uint32_t reserved;
 } reina_tuning;
 /* REINA_ORDER_INPUT traces ray i on thread i.  REINA_ORDER_COHERENT first bins the rays by direction
  * octant and origin cell (Morton order on an 8^3 grid over the origins' bounds) and traces them in that
@@ -104,12 +107,19 @@ typedef struct reina_tuning {
  * ray sets (on the 1.3M-triangle workload: random half 0.513 vs 0.525 ms, camera half 0.49 vs 0.46 ms);
  * the autotuner tries both. */
 enum { REINA_ORDER_INPUT = 0, REINA_ORDER_COHERENT = 1 };
-/* 2^23 slots (two lanes of 1.4 GB of path state): on a 256-scene batch (3.1G paths) 7.75 s, against
- * 7.77 s at 2^22, 7.89 s at 2^24 and 8.06 s at 2^21; with one wave in flight the same batch took
- * 9.74 s at 2^23 and 12.94 s at 2^21 — every wave ends in a tail of a few long paths, which the second
- * lane's wave now fills.  The server's waves are smaller (REINA_SERVER_WAVE_PATHS) so that new
- * requests join sooner. */
-enum { REINA_DEFAULT_WAVE_PATHS = 8388608, REINA_SERVER_WAVE_PATHS = 2097152 };
+/* Waves of 2^21 slots, 8 in flight (2.75 GB of path state).  Every wave ends in a tail of a few long
+ * paths at low occupancy (late bounces are latency-bound chains of node fetches), which the other waves
+ * in flight fill.  On a 256-scene batch (3.1 G paths): one wave in flight 12.94 s at 2^21 slots and
+ * 9.05 s at 2^24; two 7.75 s (2^23); four 7.27 s (2^22); eight 7.07 s (2^21); sixteen 7.02 s (2^20).
+ * On a 1920x1080, 64 spp, 12-bounce frame (waves of one sample per pixel): one 0.599 s, two 0.400 s,
+ * four 0.331 s, eight 0.324 s.  The server's waves are as large, with fewer in flight
+ * (REINA_SERVER_WAVE_LANES) so that new requests join sooner. */
+enum {
+    REINA_DEFAULT_WAVE_PATHS = 2097152,
+    REINA_DEFAULT_WAVE_LANES = 8,
+    REINA_SERVER_WAVE_PATHS = 2097152,
+    REINA_SERVER_WAVE_LANES = 4
+};
 enum { REINA_BATCH_NO_GRAPHS = 1, REINA_BATCH_FAIR_SHARE = 2 };
 int reina_ctx_set_tuning(reina_ctx* ctx, const reina_tuning* tuning);
 int reina_ctx_get_tuning(const reina_ctx* ctx, reina_tuning* out_tuning);
@@ -382,8 +392,8 @@ int reina_render_batch_device(reina_ctx* ctx, const reina_render_job* jobs, uint
 /* frame (src/Reina.cpp:425-470 driven by src/main.cpp).  A server owns a loop thread that admits      */
 /* render requests as they arrive — while device memory within the budget allows — and runs every      */
 /* admitted request in shared waves of the batched wavefront; requests join and leave between waves,   */
-/* and two waves are in flight at once (the next is packed and running while the last bounces of the   */
-/* previous one finish).                                                                               */
+/* and several waves are in flight at once (the next are packed and running while the last bounces of  */
+/* the earlier ones finish).                                                                           */
 /* Scenes and kept images stay resident and are evicted least-recently-used when admission needs room */
 /* (evicted images are kept in host memory and restored on their next use).  A request's image is the */
 /* one reina_render gives for the same scene, push constants and options.                            */
@@ -392,13 +402,13 @@ typedef struct reina_server reina_server;
 
 typedef struct reina_server_options {
     uint64_t memory_budget_bytes; /* device memory for resident scenes, kept images, running requests and
-                                   * the path state of two waves in flight (2 x wave_paths x 164 bytes,
-                                   * + 64 MiB of descriptors and slack) (0 = 120e9 bytes) */
+                                   * the path state of the waves in flight (wave_lanes x wave_paths x
+                                   * 164 bytes, + 64 MiB of descriptors and slack) (0 = 120e9 bytes) */
     uint32_t max_active_jobs;     /* requests sharing the waves, 1..512 (0 = 512) */
     uint32_t wave_paths;          /* path slots per wave (0 = REINA_SERVER_WAVE_PATHS) */
     uint32_t flags;               /* REINA_BATCH_NO_GRAPHS, and at most one of REINA_SERVER_SHORTEST,
                                    * REINA_SERVER_FIFO, REINA_SERVER_FAIR_SHARE */
-    uint32_t reserved;
+    uint32_t wave_lanes;          /* waves in flight, 1..16 (0 = REINA_SERVER_WAVE_LANES) */
 } reina_server_options;
 /* Scheduling of the wave slots:
  *   REINA_SERVER_SHORTEST    (the default) the running requests with the fewest samples left first

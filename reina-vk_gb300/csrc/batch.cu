@@ -321,7 +321,7 @@ BatchEngine::BatchEngine(int device, int sm_count, uint32_t wave_capacity, bool 
                          int lanes)
     : device_(device), sm_count_(sm_count), capacity_(wave_capacity), use_graphs_(use_graphs), trace_(trace) {
     if (wave_capacity == 0) fail(REINA_ERR_INVALID, "wave capacity must be positive");
-    if (lanes < 1 || lanes > 2) fail(REINA_ERR_INVALID, "a batch engine has 1 or 2 lanes");
+    if (lanes < 1 || lanes > 16) fail(REINA_ERR_INVALID, "a batch engine has 1 to 16 lanes");
     desc_bytes_ = sizeof(WaveHeader) + kMaxWaveSegments * sizeof(WaveSeg) + kMaxWaveJobs * sizeof(JobGpu);
     lanes_.resize((size_t)lanes);
     for (Lane& L : lanes_) {

@@ -68,8 +68,8 @@ struct BatchJob {
 
 class BatchEngine {
 public:
-    // `lanes` path-state buffers (1 or 2) of `wave_capacity` slots each; run_all alternates waves over
-    // them so that one wave's last bounces overlap the next wave's first ones.
+    // `lanes` path-state buffers (1 to 4) of `wave_capacity` slots each; waves rotate over them so that
+    // one wave's last bounces overlap the next waves' first ones.
     BatchEngine(int device, int sm_count, uint32_t wave_capacity, bool use_graphs,
                 const TraceConfig& trace = TraceConfig(), int lanes = 1);
     ~BatchEngine();
@@ -101,7 +101,7 @@ public:
     void order_after(cudaStream_t st);
     // The work queued on `st` from now on waits for every wave submitted so far.
     void order_before(cudaStream_t st);
-    // Runs waves until every job is resolved, two in flight when the engine has two lanes.  Ordered
+    // Runs waves until every job is resolved, as many in flight as the engine has lanes.  Ordered
     // after the work queued on `st` before the call; returns with every wave complete and the work
     // queued on `st` afterwards ordered after them.
     void run_all(const std::vector<BatchJob*>& jobs, cudaStream_t st, bool fifo = false);

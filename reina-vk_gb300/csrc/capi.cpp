@@ -49,6 +49,7 @@ struct reina_ctx {
     rt::DeviceBuffer rgba8, combined;  // staging for host-buffer post-processing
     uint32_t wave_paths = REINA_DEFAULT_WAVE_PATHS;
     uint32_t batch_flags = 0;
+    uint32_t wave_lanes = REINA_DEFAULT_WAVE_LANES;   // waves in flight in the batch engine
     std::unique_ptr<rt::BatchEngine> batch;   // built on the first batched render
     rt::TuneCache tune;          // autotuned configurations
     uint32_t autotune_mode = REINA_AUTOTUNE_OFF;
@@ -227,6 +228,8 @@ int reina_ctx_set_tuning(reina_ctx* ctx, const reina_tuning* t) {
         need(ctx && t, "NULL argument");
         need(t->refill <= 32, "refill must be in 0..32");
         need((t->batch_flags & ~(uint32_t)(REINA_BATCH_NO_GRAPHS | REINA_BATCH_FAIR_SHARE)) == 0, "unknown batch flags");
+        need(t->wave_lanes <= 16, "wave_lanes must be in 0..16");
+        const uint32_t lanes = t->wave_lanes ? t->wave_lanes : (uint32_t)REINA_DEFAULT_WAVE_LANES;
         const uint32_t wave = t->wave_paths ? t->wave_paths : (uint32_t)REINA_DEFAULT_WAVE_PATHS;
         need(wave <= (1u << 26), "wave_paths must be at most 2^26");
         rt::TraceConfig tc;
@@ -238,11 +241,12 @@ int reina_ctx_set_tuning(reina_ctx* ctx, const reina_tuning* t) {
         need(rt::valid_trace_config(tc), "trace_block must be 64, 128 or 256 and trace_stack 8, 12 or 16");
         const bool engine_changed = tc.block != ctx->trace.block || tc.stack != ctx->trace.stack;
         ctx->trace = tc;
-        if (wave != ctx->wave_paths || t->batch_flags != ctx->batch_flags || engine_changed) {
+        if (wave != ctx->wave_paths || t->batch_flags != ctx->batch_flags || lanes != ctx->wave_lanes || engine_changed) {
             if (ctx->batch && ctx->device >= 0) check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
             ctx->batch.reset();
             ctx->wave_paths = wave;
             ctx->batch_flags = t->batch_flags;
+            ctx->wave_lanes = lanes;
         }
     });
 }
@@ -257,6 +261,7 @@ int reina_ctx_get_tuning(const reina_ctx* ctx, reina_tuning* out) {
         out->trace_order = ctx->trace.sort ? REINA_ORDER_COHERENT : REINA_ORDER_INPUT;
         out->wave_paths = ctx->wave_paths;
         out->batch_flags = ctx->batch_flags;
+        out->wave_lanes = ctx->wave_lanes;
     });
 }
 
@@ -578,10 +583,10 @@ static void batch_key(const reina_render_job* jobs, uint32_t count, uint64_t* tr
     }
 }
 
-// A wave of no more slots than the batch has paths (rounded up to a power of two, at least 2^20): a
+// A wave of no more slots than the batch has paths (rounded up to a power of two, at least 2^16): a
 // small batch does not pay for the path state of a large wave.
 static uint32_t fit_wave(uint32_t wave, uint64_t samples) {
-    uint64_t fit = 1u << 20;
+    uint64_t fit = 1u << 16;
     while (fit < samples && fit < wave) fit <<= 1;
     return (uint32_t)std::min<uint64_t>(wave, fit);
 }
@@ -610,11 +615,13 @@ static rt::BatchEngine& batch_engine(reina_ctx* ctx, const reina_render_job* job
     // depend on how the waves are cut), so batches of changing sizes do not rebuild it each call
     const uint32_t fitted = fit_wave(wave, samples);
     if (ctx->batch && (ctx->batch->capacity() < fitted || ctx->batch->capacity() > wave ||
+                       ctx->batch->lanes() != (int)ctx->wave_lanes ||
                        ctx->batch->trace().block != trace.block || ctx->batch->trace().stack != trace.stack))
         ctx->batch.reset();
     if (!ctx->batch)
         ctx->batch = std::make_unique<rt::BatchEngine>(ctx->device, ctx->sm_count, fitted,
-                                                       (ctx->batch_flags & REINA_BATCH_NO_GRAPHS) == 0, trace, 2);
+                                                       (ctx->batch_flags & REINA_BATCH_NO_GRAPHS) == 0, trace,
+                                                       (int)ctx->wave_lanes);
     return *ctx->batch;
 }
 
@@ -811,6 +818,8 @@ int reina_server_create(reina_ctx* ctx, const reina_server_options* o, reina_ser
         cfg.budget = (o && o->memory_budget_bytes) ? o->memory_budget_bytes : 120000000000ull;
         cfg.max_active = (o && o->max_active_jobs) ? o->max_active_jobs : 512;
         cfg.wave_paths = o ? o->wave_paths : 0;
+        cfg.lanes = o ? o->wave_lanes : 0;
+        need(cfg.lanes <= 16, "wave_lanes must be in 0..16");
         cfg.graphs = !(o && (o->flags & REINA_BATCH_NO_GRAPHS));
         cfg.fifo = policy == REINA_SERVER_FIFO;
         cfg.shortest = policy == 0 || policy == REINA_SERVER_SHORTEST;
@@ -971,6 +980,7 @@ void fill_tuning(const reina_ctx* ctx, const rt::TuneEntry& e, reina_tuning* t) 
     t->trace_order = e.trace.sort ? REINA_ORDER_COHERENT : REINA_ORDER_INPUT;
     t->wave_paths = e.wave_paths ? e.wave_paths : ctx->wave_paths;
     t->batch_flags = ctx->batch_flags;
+    t->wave_lanes = ctx->wave_lanes;
 }
 
 void finish_tune(reina_ctx* ctx, uint32_t kind, uint64_t tris, uint64_t size, const rt::TuneEntry& best,
@@ -1079,7 +1089,7 @@ int reina_autotune_batch(reina_ctx* ctx, const reina_render_job* jobs, uint32_t 
         // or the whole batch, whichever is less: the wave size pays through the number of wave tails,
         // which a subset smaller than one wave cannot show
         const uint32_t n = std::min<uint32_t>(count, 32);
-        const uint64_t kMaxWave = 1u << 24;
+        const uint64_t kMaxWave = 1u << 23;
         std::vector<reina_render_job> sub(n);
         std::vector<rt::DeviceBuffer> scratch(n);
         uint64_t sub_samples = 0;
@@ -1108,7 +1118,7 @@ int reina_autotune_batch(reina_ctx* ctx, const reina_render_job* jobs, uint32_t 
         try {
             // candidate waves as the batch would run them (a wave beyond the batch's size shrinks to it)
             std::vector<uint32_t> waves;
-            for (uint32_t w : {1u << 21, 1u << 22, 1u << 23, (uint32_t)kMaxWave})
+            for (uint32_t w : {1u << 20, 1u << 21, 1u << 22, (uint32_t)kMaxWave})
                 if (std::find(waves.begin(), waves.end(), fit_wave(w, samples)) == waves.end())
                     waves.push_back(fit_wave(w, samples));
             const uint32_t default_wave = fit_wave(REINA_DEFAULT_WAVE_PATHS, samples);

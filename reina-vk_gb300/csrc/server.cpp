@@ -24,7 +24,9 @@ Server::Server(int device, int sm_count, const ServerConfig& cfg) : device_(devi
     if (cfg_.max_active == 0 || cfg_.max_active > kMaxWaveSegments / 2)
         fail(REINA_ERR_INVALID, "max_active_jobs must be in 1.." + std::to_string(kMaxWaveSegments / 2));
     const uint32_t wave = cfg_.wave_paths ? cfg_.wave_paths : (uint32_t)REINA_SERVER_WAVE_PATHS;
-    reserved_ = 2 * (uint64_t)wave * kPathBytes + (64u << 20);   // two lanes of path state + descriptors and slack
+    const uint32_t lanes = cfg_.lanes ? cfg_.lanes : (uint32_t)REINA_SERVER_WAVE_LANES;
+    if (lanes > 16) fail(REINA_ERR_INVALID, "wave_lanes must be in 0..16");
+    reserved_ = lanes * (uint64_t)wave * kPathBytes + (64u << 20);   // path state of the lanes + descriptors and slack
     if (cfg_.budget < reserved_)
         fail(REINA_ERR_BUDGET, "memory budget " + std::to_string(cfg_.budget) + " B is below the engine's " +
                                    std::to_string(reserved_) + " B of path state");
@@ -40,7 +42,7 @@ Server::Server(int device, int sm_count, const ServerConfig& cfg) : device_(devi
     check_cuda(cudaMemPoolCreate(&pool_, &props), "cudaMemPoolCreate");
     uint64_t keep = cfg_.budget;   // freed memory stays in the pool up to the budget
     check_cuda(cudaMemPoolSetAttribute(pool_, cudaMemPoolAttrReleaseThreshold, &keep), "cudaMemPoolSetAttribute");
-    engine_ = std::make_unique<BatchEngine>(device_, sm_count, wave, cfg_.graphs, TraceConfig(), 2);
+    engine_ = std::make_unique<BatchEngine>(device_, sm_count, wave, cfg_.graphs, TraceConfig(), (int)lanes);
     t0_ = now();
     thread_ = std::thread([this] { loop(); });
 }
@@ -358,8 +360,8 @@ void Server::finish(Request& r, uint32_t state, int error, const std::string& ms
     }
 }
 
-// The loop keeps up to two waves in flight (the engine's two lanes): while one runs its last bounces the
-// next is already packed and running.  Between steps it drops cancelled requests that no wave in flight
+// The loop keeps up to one wave per engine lane in flight: while one runs its last bounces the next are
+// already packed and running.  Between steps it drops cancelled requests that no wave in flight
 // holds, admits queued requests, and then either launches a wave on a free lane or waits for the oldest
 // wave; a request completes when the wave holding its last samples is done.
 void Server::loop() {

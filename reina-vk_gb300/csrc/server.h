@@ -27,6 +27,7 @@ struct ServerConfig {
     uint64_t budget = 0;          // device bytes for scenes, images, requests and the engine's path state
     uint32_t max_active = 512;    // requests sharing the waves
     uint32_t wave_paths = 0;
+    uint32_t lanes = 0;           // waves in flight (0 = REINA_SERVER_WAVE_LANES)
     bool graphs = true;
     bool fifo = false;            // wave slots to the oldest requests first (default: fair share)
     bool shortest = false;        // wave slots to the requests with the fewest samples left first

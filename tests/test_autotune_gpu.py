@@ -91,8 +91,8 @@ def test_autotune_render_and_batch(R):
                                 focus_dist=3.4)
             jobs.append(R.RenderJob(sc, pc2, R.render_options(40 + 8 * k, 32, R.MODE_NEE_MIS, k + 1)))
         bres = R.autotune_batch(ctx, jobs)
-        # a batch of ~50k paths: every candidate wave shrinks to 2^20 slots, leaving the two block sizes
-        assert bres["candidates"] == 2 and bres["best"]["wave_paths"] == 1 << 20
+        # a batch of ~50k paths: every candidate wave shrinks to 2^16 slots, leaving the two block sizes
+        assert bres["candidates"] == 2 and bres["best"]["wave_paths"] == 1 << 16
         R.autotune_set_mode(ctx, R.AUTOTUNE_CACHED)
         out, _, _ = R.render(ctx, sc, pc, opts)
         assert np.array_equal(out, ref)

@@ -56,6 +56,9 @@ def test_tuning_fields_validated(R, host_ctx):
     with pytest.raises(R.ReinaError):
         host_ctx.set_tuning(batch_flags=4)
     with pytest.raises(R.ReinaError):
+        host_ctx.set_tuning(wave_lanes=17)
+    assert old["wave_lanes"] == R.DEFAULT_WAVE_LANES
+    with pytest.raises(R.ReinaError):
         host_ctx.set_tuning(wave_paths=(1 << 26) + 1)
     assert old["wave_paths"] == R.DEFAULT_WAVE_PATHS
     host_ctx.set_tuning(trace_block=256, trace_stack=16, batch_flags=R.BATCH_NO_GRAPHS | R.BATCH_FAIR_SHARE)

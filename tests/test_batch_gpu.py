@@ -80,12 +80,15 @@ def check_same(batch, alone):
 
 @pytest.mark.parametrize("tuning", [dict(), dict(wave_paths=1000), dict(wave_paths=777, batch_flags=1),
                                     dict(wave_paths=5000, batch_flags=1), dict(wave_paths=3000, batch_flags=2),
-                                    dict(wave_paths=1500, batch_flags=3), dict(trace_block=256, trace_stack=8),
+                                    dict(wave_paths=1500, batch_flags=3), dict(wave_paths=2000, wave_lanes=1),
+                                    dict(wave_paths=1200, wave_lanes=3), dict(wave_paths=900, wave_lanes=4),
+                                    dict(trace_block=256, trace_stack=8),
                                     dict(trace_block=64, trace_stack=16)])
 def test_batch_equals_alone(R, batch_setup, tuning):
     """All jobs in one call, with the default wave (every job's sample in one wave), with small waves
     (each wave cut across jobs and pixels), packed in list order and with an equal share per job, with
-    graphs and with direct launches, and with other traversal variants."""
+    one to four waves in flight, with graphs and with direct launches, and with other traversal
+    variants."""
     ctx, jobs, alone = batch_setup
     ctx.set_tuning(**tuning)
     try:
@@ -95,7 +98,7 @@ def test_batch_equals_alone(R, batch_setup, tuning):
         assert st["rays"] == sum(a[2]["rays"] for a in alone)
         assert st["shadow_rays"] == sum(a[2]["shadow_rays"] for a in alone)
     finally:
-        ctx.set_tuning(wave_paths=0, batch_flags=0, trace_block=128, trace_stack=12)
+        ctx.set_tuning(wave_paths=0, batch_flags=0, trace_block=128, trace_stack=12, wave_lanes=0)
 
 
 def test_batch_order_and_subsets(R, batch_setup):

@@ -138,7 +138,7 @@ def test_budget_forces_lru_eviction(R, alone):
         sizes[k] = s.stats()["device_bytes"]
         s.close()
     wave = 4096
-    reserved = 2 * wave * 164 + (64 << 20)
+    reserved = R.SERVER_WAVE_LANES * wave * 164 + (64 << 20)
     specs = request_specs()
     biggest_req = max(W * H * 40 for _, W, H, *_ in specs)
     budget = reserved + max(sizes.values()) + 2 * biggest_req + 4096
@@ -158,7 +158,7 @@ def test_budget_forces_lru_eviction(R, alone):
 def test_request_larger_than_budget_is_rejected(R):
     ctx = R.Context(0)
     wave = 4096
-    srv, ids = start_server(R, ctx, budget_bytes=2 * wave * 164 + (64 << 20) + (8 << 20), wave_paths=wave)
+    srv, ids = start_server(R, ctx, budget_bytes=R.SERVER_WAVE_LANES * wave * 164 + (64 << 20) + (8 << 20), wave_paths=wave)
     with pytest.raises(R.ReinaError) as e:
         srv.submit(ids["cornell"], make_pc(R, 1.0, 1024, 1024, 1, 1), R.render_options(1024, 1024),
                    np.zeros((1024, 1024, 4), np.float32))
@@ -207,7 +207,7 @@ def test_kept_images_are_evicted_and_restored(R):
     W, H = 64, 64
     wave = 4096
     # room for the scene and two kept images besides the running request (40 B/px): the third key evicts
-    budget = 2 * wave * 164 + (64 << 20) + scene_bytes + 2 * W * H * 40
+    budget = R.SERVER_WAVE_LANES * wave * 164 + (64 << 20) + scene_bytes + 2 * W * H * 40
     srv = R.Server(ctx, budget_bytes=budget, wave_paths=wave, max_active=1)
     sid = srv.add_scene(d.to_product(R, ctx))
     firsts = []
