@@ -521,13 +521,13 @@ def batch_metrics(R, ctx, torch, built, setup_s: float, mega_scenes: int) -> dic
                      "chosen": {k: best[k] for k in ("wave_paths", "trace_block", "trace_stack")}},
         "batched": {"s": t_batch, "renders_per_s": n_scenes / t_batch, "segments_per_s": seg / t_batch,
                     "rays_per_s": (seg + shadow) / t_batch, "samples_per_s": n_smp / t_batch},
-        "one_at_a_time": {"s": t_plain, "renders_per_s": n_scenes / t_plain, "segments_per_s": seg / t_plain,
-                          "samples_per_s": n_smp / t_plain},
-        "one_at_a_time_pass_by_pass": {"s": t_pbp, "renders_per_s": n_scenes / t_pbp, "segments_per_s": seg / t_pbp,
-                                       "samples_per_s": n_smp / t_pbp},
+        "plain_pass_by_pass_one_at_a_time": {"s": t_pbp, "renders_per_s": n_scenes / t_pbp,
+                                             "segments_per_s": seg / t_pbp, "samples_per_s": n_smp / t_pbp},
+        "wave_engine_one_at_a_time": {"s": t_plain, "renders_per_s": n_scenes / t_plain,
+                                      "segments_per_s": seg / t_plain, "samples_per_s": n_smp / t_plain},
         "images_identical_all_forms": bool(identical),
-        "speedup_vs_one_at_a_time": t_plain / t_batch,
-        "speedup_vs_one_at_a_time_pass_by_pass": t_pbp / t_batch,
+        "speedup_vs_plain_pass_by_pass": t_pbp / t_batch,
+        "speedup_vs_wave_engine_one_at_a_time": t_plain / t_batch,
     }
     m = min(mega_scenes, n_scenes)
     if m > 0:
@@ -640,10 +640,10 @@ def serve_metrics(R, ctx, torch, pool, seconds: float, rate: float) -> dict:
     return {"workload": f"Poisson {rate:g}/s for {seconds:g} s ({n} requests) over the {len(pool)}-scene pool, "
                         "side U[128,1024], spp U{1..64}, depth U{4..12}, NEE+MIS; 120 GB admission budget",
             "requests": n, "samples_total": int(samples), "all_done": ok1 and ok2 and ok3,
-            "plain_one_at_a_time": plain, "plain_one_at_a_time_pass_by_pass": plain_pbp,
+            "plain_pass_by_pass_one_at_a_time": plain_pbp, "wave_engine_one_at_a_time": plain,
             "served": served, "served_fifo": served_fifo, "served_fair_share": served_fair,
-            "renders_per_s_ratio": served["renders_per_s"] / plain["renders_per_s"],
-            "renders_per_s_ratio_vs_pass_by_pass": served["renders_per_s"] / plain_pbp["renders_per_s"]}
+            "renders_per_s_ratio_vs_plain_pass_by_pass": served["renders_per_s"] / plain_pbp["renders_per_s"],
+            "renders_per_s_ratio_vs_wave_engine_one_at_a_time": served["renders_per_s"] / plain["renders_per_s"]}
 
 
 def cpu_baseline(tris, rays, sample: int) -> dict:
