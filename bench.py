@@ -324,6 +324,8 @@ def run_ours(args) -> dict | None:
         out["render"] = render_metrics(R, ctx, torch, args.render_frames, scene)
     if args.instances > 0:
         out["instanced"] = instanced_metrics(R, ctx, torch, args.instances, rays)
+    if not args.no_render:
+        out["emissive_cdf"] = emissive_metrics(R, ctx)
     if args.batch_scenes > 0:
         pool, setup_s = build_pool(R, ctx, args.batch_scenes)
         out["batched"] = batch_metrics(R, ctx, torch, pool, setup_s, args.batch_mega_scenes)
@@ -381,6 +383,28 @@ def render_metrics(R, ctx, torch, frames: int, scene_large) -> dict:
         out[f"cornell_{name}"] = {"s_per_frame": dt, "paths_per_s": 256 * 256 * 16 / dt,
                                   "segments_per_s": st["rays"] / dt,
                                   "rays_per_s": (st["rays"] + st["shadow_rays"]) / dt}
+    return out
+
+
+def emissive_metrics(R, ctx) -> dict:
+    """The emissive CDF build of a scene whose 1.3M-triangle displaced sphere is emissive, on the host and on
+    the GPU (reina_scene_set_emissive_build): wall time of each (in reina_scene_build, BVH excluded) and
+    whether the packed sampling data agree bit for bit."""
+    import scenes
+
+    v, i, _ = R.icosphere(8, 0.1, 1)
+    fv, fi = scenes.quad((-2, -1.2, -2), (4, 0, 0), (0, 0, 4))
+    out, data = {"workload": f"one emissive mesh of {i.size // 3:,} triangles + a floor"}, []
+    for name, where in (("host", R.EMISSIVE_HOST), ("device", R.EMISSIVE_DEVICE)):
+        s = R.Scene(ctx)
+        s.add_object(v, i, material=R.Material(material_idx=0, albedo=(0.5, 0.5, 0.5), emission=(1.0, 0.8, 0.6)))
+        s.add_object(fv, fi, material=R.Material(material_idx=0, albedo=(0.5, 0.5, 0.5)))
+        s.set_emissive_build(where)
+        s.build()
+        out[f"{name}_s"] = s.stats()["emissive_seconds"]
+        data.append(s.export_emissive())
+        s.close()
+    out["identical"] = all(np.array_equal(a.view(np.uint8), b.view(np.uint8)) for a, b in zip(*data))
     return out
 
 

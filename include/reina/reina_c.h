@@ -210,6 +210,21 @@ float reina_scene_emissive_weight(const reina_scene* scene);
 enum { REINA_ACCEL_AUTO = 0, REINA_ACCEL_FLAT = 1, REINA_ACCEL_TWO_LEVEL = 2 };
 int reina_scene_set_accel(reina_scene* scene, int mode);
 
+/* Where reina_scene_build computes the emissive CDFs (Instance::computeCDF, src/scene/Instance.cpp:15-53)
+ * and their duplicate search (Instances.cpp:52-90): REINA_EMISSIVE_HOST (default) or REINA_EMISSIVE_DEVICE,
+ * the scene's GPU (REINA_ERR_STATE at the build on a host-only context).  The device build evaluates the
+ * same expressions in the same order with explicit rounding — vertex transform, triangle areas and
+ * normalization in parallel, each instance's running sum in one thread, pairwise comparison in parallel
+ * — so both give the same bits. */
+enum { REINA_EMISSIVE_HOST = 0, REINA_EMISSIVE_DEVICE = 1 };
+int reina_scene_set_emissive_build(reina_scene* scene, uint32_t where);
+
+/* The packed emissive sampling data of a built scene (the buffers NEE reads, Instances.cpp:92-114): one
+ * EmissiveInstanceData per emissive instance, the concatenated per-instance triangle CDFs and the
+ * instance CDF.  Pass NULL arrays to get the counts first; a non-NULL array must hold its count. */
+int reina_scene_export_emissive(const reina_scene* scene, EmissiveInstanceData* instances, uint32_t* n_instances,
+                                float* cdf_triangles, uint64_t* n_cdf_triangles, float* cdf_instances);
+
 typedef struct reina_scene_stats {
     uint64_t triangle_count;
     uint64_t instance_count;
@@ -224,6 +239,7 @@ typedef struct reina_scene_stats {
     float bounds_max[3];
     uint32_t two_level;          /* 1: top level over instances + bottom levels per model */
     uint32_t blas_count;         /* bottom-level BVHs (two-level scenes) */
+    double emissive_seconds;     /* wall time of the emissive CDF build and its duplicate search */
 } reina_scene_stats;
 int reina_scene_get_stats(const reina_scene* scene, reina_scene_stats* out_stats);
 

@@ -342,6 +342,7 @@ int reina_scene_get_stats(const reina_scene* scene, reina_scene_stats* out) {
         s.bounds(out->bounds_min, out->bounds_max);
         out->two_level = s.two_level() ? 1u : 0u;
         out->blas_count = s.blas_count();
+        out->emissive_seconds = s.emissive_seconds();
     });
 }
 
@@ -349,6 +350,30 @@ int reina_scene_set_accel(reina_scene* scene, int mode) {
     return guard([&] {
         need(scene && scene->s, "NULL argument");
         scene->s->set_accel(mode);
+    });
+}
+
+int reina_scene_set_emissive_build(reina_scene* scene, uint32_t where) {
+    return guard([&] {
+        need(scene && scene->s, "NULL argument");
+        need(where <= REINA_EMISSIVE_DEVICE, "where must be REINA_EMISSIVE_HOST or REINA_EMISSIVE_DEVICE");
+        scene->s->set_emissive_on_device(where == REINA_EMISSIVE_DEVICE);
+    });
+}
+
+int reina_scene_export_emissive(const reina_scene* scene, EmissiveInstanceData* instances, uint32_t* n_instances,
+                                float* cdf_triangles, uint64_t* n_cdf_triangles, float* cdf_instances) {
+    return guard([&] {
+        const rt::Scene& s = built_scene(scene);
+        need(n_instances && n_cdf_triangles, "NULL count");
+        const auto& d = s.emissive_data();
+        const auto& ct = s.cdf_triangles();
+        const auto& ci = s.cdf_instances();
+        *n_instances = (uint32_t)d.size();
+        *n_cdf_triangles = ct.size();
+        if (instances && !d.empty()) std::memcpy(instances, d.data(), d.size() * sizeof(EmissiveInstanceData));
+        if (cdf_triangles && !ct.empty()) std::memcpy(cdf_triangles, ct.data(), ct.size() * sizeof(float));
+        if (cdf_instances && !ci.empty()) std::memcpy(cdf_instances, ci.data(), ci.size() * sizeof(float));
     });
 }
 

@@ -2,7 +2,10 @@
 // the upload of the assembled buffers and the BVH8 to the device.
 #include "scene.h"
 
+#include "emissive.h"
+
 #include <array>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <limits>
@@ -170,12 +173,20 @@ void Scene::add_instance_per_face(uint32_t object, const float transform[16], co
 
 // Instance::Instance + Instance::computeCDF (src/scene/Instance.cpp:5-53).  The area uses the row-vector
 // product vec4(v, 1) * transform, i.e. the transpose of the transform applied by NEE (nee.h.glsl:113-115).
-void Scene::compute_emissive(InstanceRecord& inst, const float emission[3]) {
+static bool is_emissive(const float emission[3]) {
     const float dot = emission[0] * emission[0] + emission[1] * emission[1] + emission[2] * emission[2];
+    return dot > 0.00001f * 0.00001f;
+}
+
+static float luminance(const float emission[3]) {
+    return (float)(0.2126 * emission[0] + 0.7152 * emission[1] + 0.0722 * emission[2]);
+}
+
+void Scene::compute_emissive(InstanceRecord& inst, const float emission[3]) {
     inst.light = EmissiveInfo{};
-    if (!(dot > 0.00001f * 0.00001f)) return;
+    if (!is_emissive(emission)) return;
     inst.light.emissive = true;
-    const float brightness = (float)(0.2126 * emission[0] + 0.7152 * emission[1] + 0.0722 * emission[2]);
+    const float brightness = luminance(emission);
     const ModelData& md = models_[inst.object];
     const float* T = inst.transform;
     const size_t nv = md.vertices.size() / 4;
@@ -213,10 +224,46 @@ void Scene::compute_emissive(InstanceRecord& inst, const float emission[3]) {
     inst.light.weight = cumulative;
 }
 
+// The same CDFs, areas and weights for every emissive instance on the scene's GPU (emissive.cu), and the
+// duplicate search there; returns the pairwise "same CDF" table for pack_emissives.
+void Scene::compute_emissives_device() {
+    if (device_ < 0) fail(REINA_ERR_STATE, "the emissive CDF build on the device needs a GPU context");
+    std::vector<EmissiveInput> in;
+    std::vector<InstanceRecord*> targets;
+    for (InstanceRecord& inst : instances_) {
+        inst.light = EmissiveInfo{};
+        if (inst.per_face) continue;
+        const float* emission = props_[inst.props_id].emission;
+        if (!is_emissive(emission)) continue;
+        const ModelData& md = models_[inst.object];
+        EmissiveInput e;
+        e.vertices = md.vertices.data();
+        e.nv = md.vertices.size() / 4;
+        e.indices = md.indices.data();
+        e.ntri = md.indices.size() / 3;
+        e.model = inst.object;
+        std::memcpy(e.transform, inst.transform, sizeof(e.transform));
+        e.brightness = luminance(emission);
+        in.push_back(e);
+        targets.push_back(&inst);
+    }
+    std::vector<EmissiveOutput> out;
+    emissive_cdfs_device(device_, in, std::numeric_limits<float>::epsilon(), out, emissive_same_);
+    for (size_t k = 0; k < in.size(); ++k) {
+        EmissiveInfo& l = targets[k]->light;
+        l.emissive = true;
+        if (out[k].weight == 0.0f)
+            fail(REINA_ERR_INVALID, "Cannot calculate CDF for a mesh because the cumulative area is 0");
+        l.cdf = std::move(out[k].cdf);
+        l.area = out[k].area;
+        l.weight = out[k].weight;
+    }
+}
+
 // Instances::computeSamplingDataEmissives (src/scene/Instances.cpp:52-114), including its lookup of
 // duplicates by position in the emissive list (`duplicates.contains(instanceIdxIdx)`) and by instance
 // index (`duplicates.at(instanceIdx)`), which agree whenever every instance is emissive.
-void Scene::pack_emissives() {
+void Scene::pack_emissives(const std::vector<uint8_t>* same) {
     std::vector<int> emissive_idx;
     for (size_t i = 0; i < instances_.size(); ++i)
         if (instances_[i].light.emissive) emissive_idx.push_back((int)i);
@@ -229,11 +276,13 @@ void Scene::pack_emissives() {
         return true;
     };
     std::unordered_map<size_t, size_t> dup;
-    for (size_t ii = 0; ii < emissive_idx.size(); ++ii) {
+    const size_t ne = emissive_idx.size();
+    if (same && same->size() != ne * ne) fail(REINA_ERR_INVALID, "emissive CDF deduplication: table size mismatch");
+    for (size_t ii = 0; ii < ne; ++ii) {
         const int i = emissive_idx[ii];
-        for (size_t jj = ii + 1; jj < emissive_idx.size(); ++jj) {
+        for (size_t jj = ii + 1; jj < ne; ++jj) {
             const int j = emissive_idx[jj];
-            if (!same_cdf(instances_[i].light.cdf, instances_[j].light.cdf)) continue;
+            if (same ? !(*same)[ii * ne + jj] : !same_cdf(instances_[i].light.cdf, instances_[j].light.cdf)) continue;
             if (dup.find(j) == dup.end()) dup[j] = i;
         }
     }
@@ -518,11 +567,18 @@ void Scene::build(bool require_emissive) {
     }
 
     // Emissive CDFs and packing (src/scene/Scene.cpp:102-114 -> Instances).
-    for (InstanceRecord& inst : instances_) {
-        if (inst.per_face) inst.light = EmissiveInfo{};
-        else compute_emissive(inst, props_[inst.props_id].emission);
+    const auto t_em = std::chrono::steady_clock::now();
+    if (emissive_device_) {
+        compute_emissives_device();
+        pack_emissives(&emissive_same_);
+    } else {
+        for (InstanceRecord& inst : instances_) {
+            if (inst.per_face) inst.light = EmissiveInfo{};
+            else compute_emissive(inst, props_[inst.props_id].emission);
+        }
+        pack_emissives();
     }
-    pack_emissives();
+    emissive_seconds_ = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_em).count();
     if (cdf_triangles_.empty() && require_emissive) fail(REINA_ERR_NO_EMISSIVE, "Scene must have at least one emissive object");
 
     tri_total_ = 0;

@@ -65,6 +65,11 @@ public:
     // Acceleration structure (REINA_ACCEL_*): one BVH over world-space triangles, or a top level over
     // instances with one bottom level per model; set before the build.
     void set_accel(int mode);
+    // Where build() computes the emissive CDFs and their duplicate search: the host (default) or the
+    // scene's GPU (emissive.cu); both give the same bits.
+    void set_emissive_on_device(bool on) { emissive_device_ = on; }
+    bool emissive_on_device() const { return emissive_device_; }
+    double emissive_seconds() const { return emissive_seconds_; }
     bool two_level() const { return two_level_; }
     uint32_t blas_count() const { return blas_count_; }
     const std::vector<InstanceTrav>& instance_records() const { return inst_trav_; }
@@ -98,7 +103,9 @@ public:
 private:
     InstanceProperties make_props(uint32_t object, const reina_material& mat) const;
     void compute_emissive(InstanceRecord& inst, const float emission[3]);
-    void pack_emissives();
+    void compute_emissives_device();
+    // `same` (optional, from the device build): same[i * n + j] for emissive positions i < j.
+    void pack_emissives(const std::vector<uint8_t>* same = nullptr);
     bool use_two_level() const;
     void build_flat();
     void build_two_level();
@@ -128,6 +135,9 @@ private:
     std::vector<uint8_t> has_tbn_;
     // Two-level acceleration structure
     int accel_mode_ = REINA_ACCEL_AUTO;
+    bool emissive_device_ = false;
+    double emissive_seconds_ = 0.0;
+    std::vector<uint8_t> emissive_same_;   // device build: pairwise same-CDF table of the emissive instances
     bool two_level_ = false;
     uint32_t blas_count_ = 0;
     std::vector<InstanceTrav> inst_trav_;

@@ -76,7 +76,7 @@ class _SceneStats(C.Structure):
         ("node_bytes", C.c_uint64), ("triangle_bytes", C.c_uint64), ("device_bytes", C.c_uint64),
         ("max_depth", C.c_uint32), ("leaf_triangles_max", C.c_uint32), ("build_seconds", C.c_double),
         ("bounds_min", C.c_float * 3), ("bounds_max", C.c_float * 3), ("two_level", C.c_uint32),
-        ("blas_count", C.c_uint32),
+        ("blas_count", C.c_uint32), ("emissive_seconds", C.c_double),
     ]
 
 
@@ -110,6 +110,14 @@ INSTANCE_PROPERTIES_DTYPE = np.dtype([
     ("cullBackface", "<u4"), ("anisotropic", "<f4"), ("subsurface", "<f4"), ("clearcoatGloss", "<f4"),
     ("sheenTint", "<f4", 3), ("specularTint", "<f4", 3), ("metallic", "<f4"), ("clearcoat", "<f4"),
     ("specularTransmission", "<f4"), ("sheen", "<f4")])
+
+
+# EmissiveInstanceData (polyglot.h), 112 bytes.
+EMISSIVE_INSTANCE_DTYPE = np.dtype([
+    ("transform", "<f4", 16), ("materialOffset", "<u4"), ("cdfRangeStart", "<u4"), ("cdfRangeEnd", "<u4"),
+    ("indexOffset", "<u4"), ("emission", "<f4", 3), ("weight", "<f4"), ("area", "<f4"), ("cullBackface", "<u4"),
+    ("padding", "<f4", 2)])
+EMISSIVE_HOST, EMISSIVE_DEVICE = 0, 1
 
 
 class RtPushConsts(C.Structure):
@@ -341,6 +349,8 @@ def load_library() -> C.CDLL:
         "reina_scene_define_texture_encoded": (I32, [P, P, U64, C.POINTER(U32)]),
         "reina_scene_texture_count": (I32, [P, C.POINTER(U32)]),
         "reina_scene_set_accel": (I32, [P, C.c_int]),
+        "reina_scene_set_emissive_build": (I32, [P, U32]),
+        "reina_scene_export_emissive": (I32, [P, P, C.POINTER(U32), P, C.POINTER(U64), P]),
         "reina_device_kat": (I32, [P, C.c_int, P, U64, P]),
         "reina_scene_export_two_level": (I32, [P, P, P, C.POINTER(U32), C.POINTER(U32)]),
         "reina_scene_export_properties": (I32, [P, P, U32, C.POINTER(U32)]),
@@ -599,6 +609,20 @@ class Scene:
     def set_accel(self, mode: int) -> None:
         """ACCEL_AUTO, ACCEL_FLAT or ACCEL_TWO_LEVEL (before build)."""
         _check(_lib.reina_scene_set_accel(self._h, mode))
+
+    def set_emissive_build(self, where: int) -> None:
+        """EMISSIVE_HOST (default) or EMISSIVE_DEVICE: where build() computes the emissive CDFs."""
+        _check(_lib.reina_scene_set_emissive_build(self._h, where))
+
+    def export_emissive(self) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+        """(EmissiveInstanceData records, concatenated triangle CDFs, instance CDF) of the built scene."""
+        ni, nt = C.c_uint32(), C.c_uint64()
+        _check(_lib.reina_scene_export_emissive(self._h, None, C.byref(ni), None, C.byref(nt), None))
+        inst = np.zeros(ni.value, EMISSIVE_INSTANCE_DTYPE)
+        tris = np.zeros(nt.value, np.float32)
+        cdf_i = np.zeros(ni.value, np.float32)
+        _check(_lib.reina_scene_export_emissive(self._h, _ptr(inst), C.byref(ni), _ptr(tris), C.byref(nt), _ptr(cdf_i)))
+        return inst, tris, cdf_i
 
     def texture_count(self) -> int:
         n = C.c_uint32()

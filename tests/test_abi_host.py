@@ -271,3 +271,34 @@ def test_server_policy_flags_exclude_each_other(R, host_ctx, kw):
         R.Server(host_ctx, **kw)
     assert e.value.code == R.REINA_ERR_INVALID
 
+
+
+def test_emissive_export_and_device_build_on_host(R, host_ctx):
+    """The packed emissive data of a host build: each instance's triangle CDF ends at 1, the instance CDF
+    ends at 1, weights sum to the scene's emissive weight; the device build needs a GPU context."""
+    def make():
+        s = R.Scene(host_ctx)
+        v, i, _ = R.icosphere(2, 0.1, 4)
+        o = s.define_object(v, i)
+        for k, e in enumerate([(1.0, 1.0, 1.0), (2.0, 0.0, 0.5), (1.0, 1.0, 1.0)]):
+            t = np.eye(4, dtype=np.float32)
+            t[0, 3] = 0.5 * k
+            s.add_instance(o, t, R.Material(emission=e))
+        return s
+    s = make()
+    with pytest.raises(R.ReinaError) as e:
+        s.set_emissive_build(2)
+    assert e.value.code == R.REINA_ERR_INVALID
+    s.build()
+    inst, tris, cdf_i = s.export_emissive()
+    assert inst.size == 3 and cdf_i.size == 3 and cdf_i[-1] == 1.0
+    for r in inst:
+        assert tris[r["cdfRangeEnd"]] == 1.0 and r["cdfRangeEnd"] - r["cdfRangeStart"] + 1 == 320
+    assert abs(float(inst["weight"].sum()) - s.emissive_weight) <= 1e-5 * s.emissive_weight
+    # instances 0 and 2 have the same CDF (a translation does not change areas): one shared range
+    assert (inst[0]["cdfRangeStart"], inst[0]["cdfRangeEnd"]) == (inst[2]["cdfRangeStart"], inst[2]["cdfRangeEnd"])
+    d = make()
+    d.set_emissive_build(R.EMISSIVE_DEVICE)
+    with pytest.raises(R.ReinaError) as e:
+        d.build()
+    assert e.value.code == R.REINA_ERR_STATE
