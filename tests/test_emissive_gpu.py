@@ -32,10 +32,11 @@ def emissive_field(R, ctx):
     b = s.define_object(v2, i2)
     lv, li = scenes.quad((-0.3, 0.99, -0.3), (0.6, 0, 0), (0, 0, 0.6))
     m = lambda e: R.Material(material_idx=0, albedo=(0.7, 0.7, 0.7), emission=e)
-    for k, (obj, e) in enumerate([(a, (3.0, 2.0, 1.0)), (a, (3.0, 2.0, 1.0)), (a, (0.5, 4.0, 0.2)),
-                                  (b, (1.0, 1.0, 1.0)), (b, (2.0, 0.5, 0.5))]):
+    # (model, emission, pose): instances 0 and 1 share model and pose, so their CDFs are the same
+    for obj, e, k in [(a, (3.0, 2.0, 1.0), 0), (a, (3.0, 2.0, 1.0), 0), (a, (0.5, 4.0, 0.2), 1),
+                      (b, (1.0, 1.0, 1.0), 2), (b, (2.0, 0.5, 0.5), 3)]:
         t = np.eye(4, dtype=np.float32)
-        ang = 0.37 * (k % 3)
+        ang = 0.37 * k
         c, sn = np.cos(ang), np.sin(ang)
         t[:3, :3] = (0.2 + 0.05 * (k % 3)) * np.array([[c, 0, sn], [0, 1, 0], [-sn, 0, c]], np.float32)
         t[:3, 3] = (-0.6 + 0.3 * (k % 3), -0.2, -0.4)
