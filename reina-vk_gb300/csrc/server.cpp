@@ -421,10 +421,26 @@ void Server::loop() {
         std::vector<BatchJob*> jobs;
         for (Request* r : running_)
             if (schedulable(r)) jobs.push_back(&r->job);
-        if (cfg_.shortest)   // fewest samples left first; stable: ties keep arrival order
+        if (cfg_.shortest && cfg_.aging > 0.0) {
+            // estimated remaining time minus aging x waiting time; stable: ties keep arrival order
+            // samples per second: completed samples over the time since the first submission (a
+            // nominal 4e8 until the first request completes)
+            const double t = now();
+            const double rate = samples_done_ > 0.0 && t > first_submit_ ? samples_done_ / (t - first_submit_) : 4e8;
+            std::vector<std::pair<double, BatchJob*>> keyed;
+            keyed.reserve(jobs.size());
+            for (BatchJob* j : jobs) {
+                const Request* r = static_cast<const Request*>(j->owner);
+                keyed.emplace_back((double)(j->total - j->cursor) / rate - cfg_.aging * (t - r->t_submit), j);
+            }
+            std::stable_sort(keyed.begin(), keyed.end(),
+                             [](const auto& a, const auto& b) { return a.first < b.first; });
+            for (size_t k = 0; k < jobs.size(); ++k) jobs[k] = keyed[k].second;
+        } else if (cfg_.shortest) {   // fewest samples left first; stable: ties keep arrival order
             std::stable_sort(jobs.begin(), jobs.end(), [](const BatchJob* a, const BatchJob* b) {
                 return a->total - a->cursor < b->total - b->cursor;
             });
+        }
         const bool launch = !jobs.empty() && engine_->lane_free();
         if (!launch && !engine_->pending()) continue;
         lk.unlock();
@@ -487,6 +503,7 @@ void Server::loop() {
             waves.clear();
         } else {
             for (Request* r : done) {
+                samples_done_ += (double)r->job.total;
                 finish(*r, kReqDone, 0, "");
                 running_.erase(std::find(running_.begin(), running_.end(), r));
             }

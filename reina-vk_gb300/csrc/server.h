@@ -31,6 +31,7 @@ struct ServerConfig {
     bool graphs = true;
     bool fifo = false;            // wave slots to the oldest requests first (default: fair share)
     bool shortest = false;        // wave slots to the requests with the fewest samples left first
+    double aging = 0.0;           // shortest: seconds of priority per second since submission
 };
 
 struct RequestSpec {
@@ -127,6 +128,7 @@ private:
     std::vector<double> latencies_;
     ServerStats counters_;
     double t0_ = 0, first_submit_ = -1, last_done_ = 0;
+    double samples_done_ = 0;     // samples of completed requests (the aging key's rate estimate)
 };
 
 }  // namespace rt

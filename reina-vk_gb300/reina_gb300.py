@@ -98,6 +98,7 @@ DEFAULT_WAVE_PATHS = 2097152
 DEFAULT_WAVE_LANES = 8
 SERVER_WAVE_PATHS = 2097152
 SERVER_WAVE_LANES = 4
+SERVER_DEFAULT_AGING = 0.03
 BATCH_NO_GRAPHS = 1
 BATCH_FAIR_SHARE = 2
 
@@ -153,7 +154,7 @@ class _RenderStats(C.Structure):
 
 class _ServerOptions(C.Structure):
     _fields_ = [("memory_budget_bytes", C.c_uint64), ("max_active_jobs", C.c_uint32), ("wave_paths", C.c_uint32),
-                ("flags", C.c_uint32), ("wave_lanes", C.c_uint32)]
+                ("flags", C.c_uint32), ("wave_lanes", C.c_uint32), ("aging", C.c_float), ("reserved", C.c_uint32)]
 
 
 class _Request(C.Structure):
@@ -800,13 +801,13 @@ class Server:
 
     def __init__(self, ctx: Context, budget_bytes: int = 0, max_active: int = 0, wave_paths: int = 0,
                  graphs: bool = True, fifo: bool = False, shortest: bool = False, fair: bool = False,
-                 wave_lanes: int = 0):
+                 wave_lanes: int = 0, aging: float = 0.0):
         """Wave-slot policy: shortest remaining work first (the default, or shortest=True), fifo=True or
         fair=True (an equal share per running request); at most one may be given."""
         self.ctx = ctx
         flags = ((0 if graphs else BATCH_NO_GRAPHS) | (SERVER_FIFO if fifo else 0) | (SERVER_SHORTEST if shortest else 0)
                  | (SERVER_FAIR_SHARE if fair else 0))
-        o = _ServerOptions(budget_bytes, max_active, wave_paths, flags, wave_lanes)
+        o = _ServerOptions(budget_bytes, max_active, wave_paths, flags, wave_lanes, aging, 0)
         h = C.c_void_p()
         _check(_lib.reina_server_create(ctx.handle, C.byref(o), C.byref(h)))
         self._h = h

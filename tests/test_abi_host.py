@@ -265,7 +265,7 @@ def test_server_needs_a_gpu_context(R, host_ctx):
 
 
 @pytest.mark.parametrize("kw", [dict(fifo=True, shortest=True), dict(fifo=True, fair=True),
-                                dict(shortest=True, fair=True)])
+                                dict(shortest=True, fair=True), dict(aging=float("nan")), dict(wave_lanes=17)])
 def test_server_policy_flags_exclude_each_other(R, host_ctx, kw):
     with pytest.raises(R.ReinaError) as e:
         R.Server(host_ctx, **kw)

@@ -104,14 +104,17 @@ def submit_all(R, srv, ids, weights, specs, stagger_s=0.0, threads=1):
     return rids, outs
 
 
-@pytest.mark.parametrize("policy", ["fair", "fifo", "shortest"])
-def test_same_alone_and_in_the_mix(R, alone, policy):
+@pytest.mark.parametrize("policy,lanes", [("fair", 0), ("fifo", 0), ("shortest", 0), ("shortest_no_aging", 1),
+                                          ("shortest_strong_aging", 16)])
+def test_same_alone_and_in_the_mix(R, alone, policy, lanes):
     """Requests submitted from 3 threads while earlier ones run: each result equals its lone render
-    (fair-share, first-come first-served and shortest-remaining-work wave packing)."""
+    (fair-share, first-come first-served and shortest-remaining-work wave packing, with and without
+    aging; one to sixteen waves in flight)."""
     weights, ref = alone
     ctx = R.Context(0)
-    ctx_srv, ids = start_server(R, ctx, wave_paths=4096, fifo=policy == "fifo", shortest=policy == "shortest",
-                                fair=policy == "fair")
+    aging = {"shortest_no_aging": -1.0, "shortest_strong_aging": 5.0}.get(policy, 0.0)
+    ctx_srv, ids = start_server(R, ctx, wave_paths=4096, fifo=policy == "fifo", fair=policy == "fair",
+                                shortest=policy.startswith("shortest"), aging=aging, wave_lanes=lanes)
     srv = ctx_srv
     rids, outs = submit_all(R, srv, ids, weights, request_specs(), stagger_s=0.002, threads=3)
     for n, rid in enumerate(rids):
