@@ -77,10 +77,10 @@ int reina_ctx_sm_count(const reina_ctx* ctx);
  *   wave_paths: path slots of one wave of a batched render or frame (0 = REINA_DEFAULT_WAVE_PATHS);
  *            the path state costs 164 bytes per slot and wave in flight (wave_lanes): the waves run on
  *            streams of their own, so that one wave's last bounces (few long paths) overlap the next
- *            waves' first ones.  A wave holds at most one sample of each pixel, so a batch gets no more
- *            slots than its jobs have pixels (or samples, if fewer), rounded up to a power of two (at
- *            least 2^16); an engine already built with more slots than that (up to wave_paths) is
- *            reused.
+ *            waves' first ones.  A wave holds any number of samples of a pixel of a NEE+MIS job and at
+ *            most one of a job in the reference's mode; a batch gets no more slots than one wave can
+ *            hold of it, rounded up to a power of two (at least 2^16); an engine already built with
+ *            more slots than that (up to wave_paths) is reused.
  *   batch_flags: REINA_BATCH_NO_GRAPHS launches each wave's kernels one by one instead of replaying a
  *            captured CUDA graph.  Waves are packed with the jobs in list order, each taking all it can
  *            use (one sample of each of its pixels), so that a wave holds few scenes and their data

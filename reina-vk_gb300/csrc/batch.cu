@@ -245,27 +245,46 @@ __global__ void __launch_bounds__(BLOCK) kb_shadow(BatchLaunch B, const JobGpu* 
     }
 }
 
-// raytrace.rgen.glsl:264-275 per slot: clamp (NaN kept), sample output, NaN drop, sum; carry the
-// RNG state and accumulatedDistance to the pixel's next sample.
+// raytrace.rgen.glsl:264-275 per pixel of each job in the wave: clamp (NaN kept), sample output, NaN
+// drop, sum — over the pixel's samples in this wave in sample order (a job whose samples are independent
+// may have several samples of a pixel in one wave) — and carry the RNG state and accumulatedDistance of
+// the last one to the pixel's next sample.
 __global__ void __launch_bounds__(kBlock) kb_finish(BatchLaunch B, const JobGpu* __restrict__ jobs) {
     const PathState& ps = B.bp.ps;
-    const uint32_t n = B.hdr->count;
+    const uint32_t n = B.hdr->finish_total;
+    const int nj = (int)B.hdr->njobs;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const JobGpu& J = jobs[B.bp.job[i]];
-        const uint32_t pixel = B.bp.pix[i];
-        const V3 c = clamp_keep_nan(load_rad(ps, i), J.pc.directClamp);
-        if (J.samples) {
-            float* o = J.samples + 3ull * ((uint64_t)pixel * J.spp + B.bp.smp[i]);
-            o[0] = c.x; o[1] = c.y; o[2] = c.z;
+        int lo = 0, hi = nj - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) / 2;
+            if (jobs[mid].finish_start <= i) lo = mid;
+            else hi = mid - 1;
         }
-        if (!has_nan3(c)) {
-            J.sr[pixel] += c.x;
-            J.sg[pixel] += c.y;
-            J.sb[pixel] += c.z;
-            J.cnt[pixel] += 1;
+        const JobGpu& J = jobs[lo];
+        const uint64_t px = (uint64_t)J.W * J.H;
+        const uint64_t first = J.cursor0 + (i - J.finish_start), end = J.cursor0 + J.take;
+        const uint32_t pixel = (uint32_t)(first % px);
+        float sr = J.sr[pixel], sg = J.sg[pixel], sb = J.sb[pixel];
+        uint32_t cnt = J.cnt[pixel];
+        uint32_t slot = 0;
+        for (uint64_t idx = first; idx < end; idx += px) {
+            slot = J.wave_start + (uint32_t)(idx - J.cursor0);
+            const V3 c = clamp_keep_nan(load_rad(ps, slot), J.pc.directClamp);
+            if (J.samples) {
+                float* o = J.samples + 3ull * ((uint64_t)pixel * J.spp + idx / px);
+                o[0] = c.x; o[1] = c.y; o[2] = c.z;
+            }
+            if (!has_nan3(c)) {
+                sr += c.x;
+                sg += c.y;
+                sb += c.z;
+                cnt += 1;
+            }
         }
-        J.pix_rng[pixel] = ps.rng[i];
-        J.pix_acc[pixel] = ps.acc[i];
+        J.sr[pixel] = sr; J.sg[pixel] = sg; J.sb[pixel] = sb;
+        J.cnt[pixel] = cnt;
+        J.pix_rng[pixel] = ps.rng[slot];
+        J.pix_acc[pixel] = ps.acc[slot];
     }
 }
 
@@ -515,19 +534,23 @@ BatchEngine::Packed BatchEngine::pack(const std::vector<BatchJob*>& jobs, bool f
     if (active.empty()) return pk;
     // fair share of the capacity, then leftovers to the oldest jobs (or, first-come first-served, each
     // job in order takes all it can use)
+    // A job's samples per pixel in one wave: any number when its samples are independent (NEE+MIS: seeded
+    // by (pixel, sample); the finish kernel sums a pixel's samples of the wave in order); one in the
+    // reference's mode, where a pixel's next sample starts from the state its previous one left.
+    auto cap = [](const BatchJob* j) -> uint64_t {
+        return j->opt.mode == kModeNeeMis ? UINT64_MAX : (uint64_t)j->opt.width * j->opt.height;
+    };
     std::vector<uint64_t> take(active.size(), 0);
     const uint64_t fair = fifo ? (uint64_t)capacity_ : std::max<uint64_t>(1, capacity_ / active.size());
     uint64_t used = 0;
     for (size_t a = 0; a < active.size(); ++a) {
         const BatchJob* j = active[a];
-        const uint64_t px = (uint64_t)j->opt.width * j->opt.height;
-        take[a] = std::min({fair, px, j->total - j->cursor, (uint64_t)capacity_ - used});
+        take[a] = std::min({fair, cap(j), j->total - j->cursor, (uint64_t)capacity_ - used});
         used += take[a];
     }
     for (size_t a = 0; a < active.size() && used < capacity_; ++a) {
         const BatchJob* j = active[a];
-        const uint64_t px = (uint64_t)j->opt.width * j->opt.height;
-        const uint64_t more = std::min(std::min(px, j->total - j->cursor) - take[a], (uint64_t)capacity_ - used);
+        const uint64_t more = std::min(std::min(cap(j), j->total - j->cursor) - take[a], (uint64_t)capacity_ - used);
         take[a] += more;
         used += more;
     }
@@ -535,9 +558,10 @@ BatchEngine::Packed BatchEngine::pack(const std::vector<BatchJob*>& jobs, bool f
     WaveHeader* hdr = reinterpret_cast<WaveHeader*>(h);
     WaveSeg* segs = reinterpret_cast<WaveSeg*>(h + sizeof(WaveHeader));
     JobGpu* jt = reinterpret_cast<JobGpu*>(h + sizeof(WaveHeader) + kMaxWaveSegments * sizeof(WaveSeg));
-    uint32_t nseg = 0, njobs = 0, wave_pos = 0, bounces = 0;
+    uint32_t nseg = 0, njobs = 0, wave_pos = 0, bounces = 0, finish = 0;
     for (size_t a = 0; a < active.size(); ++a) {
         if (take[a] == 0) continue;
+        if (nseg >= kMaxWaveSegments) break;   // the descriptor is full: later jobs wait for the next wave
         BatchJob* j = active[a];
         const uint64_t px = (uint64_t)j->opt.width * j->opt.height;
         const uint32_t ji = njobs++;
@@ -545,11 +569,11 @@ BatchEngine::Packed BatchEngine::pack(const std::vector<BatchJob*>& jobs, bool f
         pk.members.push_back(j);
         bounces = std::max(bounces, j->pc.maxBounces);
         pk.any_nee = pk.any_nee || j->opt.mode == kModeNeeMis;
-        // samples after a pixel's first start from the state its previous sample left (reference mode)
-        pk.carries = pk.carries || (j->opt.mode != kModeNeeMis && j->cursor + take[a] > px);
         pk.two = pk.two || j->scene.inst_trav != nullptr;
+        const uint64_t c0 = j->cursor;
+        const uint32_t ws = wave_pos;
         uint64_t m = take[a];
-        while (m > 0) {
+        while (m > 0 && nseg < kMaxWaveSegments) {
             const uint64_t sample = j->cursor / px, pixel = j->cursor % px;
             const uint64_t c = std::min(m, px - pixel);
             WaveSeg& s = segs[nseg++];
@@ -562,6 +586,14 @@ BatchEngine::Packed BatchEngine::pack(const std::vector<BatchJob*>& jobs, bool f
             j->cursor += c;
             m -= c;
         }
+        const uint64_t placed = j->cursor - c0;
+        jt[ji].cursor0 = c0;
+        jt[ji].wave_start = ws;
+        jt[ji].take = (uint32_t)placed;
+        jt[ji].finish_start = finish;
+        finish += (uint32_t)std::min(placed, px);
+        // samples after a pixel's first start from the state its previous sample left (reference mode)
+        pk.carries = pk.carries || (j->opt.mode != kModeNeeMis && c0 + placed > px);
         if (j->cursor == j->total && !j->resolved) {
             pk.completed.push_back(j);
             j->resolved = true;
@@ -571,6 +603,7 @@ BatchEngine::Packed BatchEngine::pack(const std::vector<BatchJob*>& jobs, bool f
     hdr->nseg = nseg;
     hdr->njobs = njobs;
     hdr->max_bounces = bounces;
+    hdr->finish_total = finish;
     pk.hdr = *hdr;
     return pk;
 }

@@ -31,6 +31,14 @@ struct JobGpu {
     float* pix_acc;
     float *sr, *sg, *sb;
     uint32_t* cnt;
+    // this wave: the job's slots are [wave_start, wave_start + take), holding its (sample * W*H + pixel)
+    // indices [cursor0, cursor0 + take); finish threads [finish_start, finish_start + min(take, W*H)),
+    // one per pixel, sum each pixel's samples of the wave in sample order
+    uint64_t cursor0;
+    uint32_t wave_start;
+    uint32_t take;
+    uint32_t finish_start;
+    uint32_t pad3;
 };
 
 // A run of wave slots [wave_start, wave_start + count) holding pixels [pixel_start, ...) of one job's
@@ -49,7 +57,10 @@ struct WaveHeader {
     uint32_t nseg;
     uint32_t njobs;
     uint32_t max_bounces;    // segments to run (max over the wave's jobs)
+    uint32_t finish_total;   // finish threads (sum over jobs of min(take, W*H))
+    uint32_t pad[3];         // 32 bytes: the job table after the segments stays 16-byte aligned
 };
+static_assert(sizeof(WaveHeader) == 32, "WaveHeader must stay 32 bytes");
 
 // Host-side description of one job.
 struct BatchJob {
@@ -80,8 +91,9 @@ public:
     // pool, the allocation is stream-ordered on `st` (DeviceBuffer::alloc_async).
     static void prepare(BatchJob& job, cudaMemPool_t pool = nullptr, cudaStream_t st = nullptr);
     // Waves are packed from `jobs`: an equal share of the capacity per job with samples left, leftovers
-    // to the first jobs (or, with `fifo`, each job in list order taking all it can use), at most one
-    // sample of each pixel per wave.  Wave k runs on lane k mod lanes, on the lane's own stream.  Each
+    // to the first jobs (or, with `fifo`, each job in list order taking all it can use); a job in the
+    // reference's mode places at most one sample of each pixel in a wave, a NEE+MIS job any number (the
+    // finish kernel sums each pixel's samples of the wave in sample order).  Wave k runs on lane k mod lanes, on the lane's own stream.  Each
     // wave's finish kernel (the per-pixel sums) runs after the previous wave's, so a pixel's samples are
     // summed in sample order; a wave holding a job whose samples carry state from the pixel's previous
     // sample (the reference's seeding mode) starts only after the previous wave's finish.

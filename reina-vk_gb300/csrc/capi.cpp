@@ -632,10 +632,14 @@ static rt::BatchEngine& batch_engine(reina_ctx* ctx, const reina_render_job* job
         trace = e.trace;
         if (e.wave_paths) wave = e.wave_paths;
     }
-    // a wave holds at most one sample of each pixel: no more slots than the jobs have pixels
-    uint64_t pixels = 0;
-    for (uint32_t k = 0; k < count; ++k) pixels += (uint64_t)jobs[k].options.width * jobs[k].options.height;
-    samples = std::min(samples, pixels);
+    // the paths one wave can hold: every sample of a NEE+MIS job, one sample per pixel of a job in the
+    // reference's mode
+    uint64_t room = 0;
+    for (uint32_t k = 0; k < count; ++k) {
+        const uint64_t px = (uint64_t)jobs[k].options.width * jobs[k].options.height;
+        room += jobs[k].options.mode == REINA_MODE_NEE_MIS ? px * jobs[k].push_consts.samplesPerPixel : px;
+    }
+    samples = std::min(samples, room);
     // an engine between the batch's fitted size and the wanted one is kept (a job's images do not
     // depend on how the waves are cut), so batches of changing sizes do not rebuild it each call
     const uint32_t fitted = fit_wave(wave, samples);
