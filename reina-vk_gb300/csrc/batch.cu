@@ -92,7 +92,7 @@ __global__ void __launch_bounds__(kBlock) kb_init(BatchLaunch B, const JobGpu* _
 }
 
 template <int BLOCK, int SS, bool TWO>
-__global__ void __launch_bounds__(BLOCK) kb_extend(BatchLaunch B, const JobGpu* __restrict__ jobs, int cur) {
+__global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) kb_extend(BatchLaunch B, const JobGpu* __restrict__ jobs, int cur) {
     __shared__ uint2 stack[SS * BLOCK];
     const PathState& ps = B.bp.ps;
     const uint32_t n = ps.counters[kCntActive + cur];
