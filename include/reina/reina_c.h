@@ -338,10 +338,11 @@ enum {
                                     * (no CUDA graphs, no overlap between passes), instead of the wave
                                     * engine of the batched renders with the frame as its one job */
 };
-/* Without a flag a frame runs on the context's wave engine (reina_render_batch with one job): waves of
- * one sample of every pixel, two in flight on two streams, each replayed from a CUDA graph — on the
- * 1920x1080, 64 spp, 12-bounce frame 0.40 s against 0.58 s pass by pass.  The three forms give the same
- * images.  The grid-form traversal variant comes from the render autotune cache (REINA_AUTOTUNE_CACHED)
+/* Without a flag a frame runs on the context's wave engine (reina_render_batch with one job): waves
+ * of its samples (several per pixel in REINA_MODE_NEE_MIS, one per pixel in REINA_MODE_REINA), eight in
+ * flight on their own streams (tuning.wave_lanes), each replayed from a CUDA graph — on the 1920x1080,
+ * 64 spp, 12-bounce frame 0.32 s against 0.59 s pass by pass.  The three forms give the same images. */
+/* The grid-form traversal variant of a frame comes from the render autotune cache (REINA_AUTOTUNE_CACHED)
  * or the context's tuning; the persistent form (tuning.refill > 0) applies to the pass-by-pass form only. */
 
 typedef struct reina_render_stats {
