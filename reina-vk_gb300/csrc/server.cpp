@@ -31,18 +31,25 @@ Server::Server(int device, int sm_count, const ServerConfig& cfg) : device_(devi
         fail(REINA_ERR_BUDGET, "memory budget " + std::to_string(cfg_.budget) + " B is below the engine's " +
                                    std::to_string(reserved_) + " B of path state");
     check_cuda(cudaSetDevice(device_), "cudaSetDevice");
-    check_cuda(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
-    // requests' pixel state and own images come from this pool, stream-ordered on stream_, so that
-    // admitting and finishing requests does not wait for the waves in flight
-    cudaMemPoolProps props;
-    std::memset(&props, 0, sizeof(props));
-    props.allocType = cudaMemAllocationTypePinned;
-    props.location.type = cudaMemLocationTypeDevice;
-    props.location.id = device_;
-    check_cuda(cudaMemPoolCreate(&pool_, &props), "cudaMemPoolCreate");
-    uint64_t keep = cfg_.budget;   // freed memory stays in the pool up to the budget
-    check_cuda(cudaMemPoolSetAttribute(pool_, cudaMemPoolAttrReleaseThreshold, &keep), "cudaMemPoolSetAttribute");
-    engine_ = std::make_unique<BatchEngine>(device_, sm_count, wave, cfg_.graphs, TraceConfig(), (int)lanes);
+    try {
+        check_cuda(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+        // requests' pixel state and own images come from this pool, stream-ordered on stream_, so that
+        // admitting and finishing requests does not wait for the waves in flight
+        cudaMemPoolProps props;
+        std::memset(&props, 0, sizeof(props));
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = device_;
+        check_cuda(cudaMemPoolCreate(&pool_, &props), "cudaMemPoolCreate");
+        uint64_t keep = cfg_.budget;   // freed memory stays in the pool up to the budget
+        check_cuda(cudaMemPoolSetAttribute(pool_, cudaMemPoolAttrReleaseThreshold, &keep), "cudaMemPoolSetAttribute");
+        engine_ = std::make_unique<BatchEngine>(device_, sm_count, wave, cfg_.graphs, TraceConfig(), (int)lanes);
+    } catch (...) {   // the destructor does not run for a constructor that throws
+        engine_.reset();
+        if (pool_) cudaMemPoolDestroy(pool_);
+        if (stream_) cudaStreamDestroy(stream_);
+        throw;
+    }
     t0_ = now();
     thread_ = std::thread([this] { loop(); });
 }
