@@ -343,15 +343,20 @@ BatchEngine::BatchEngine(int device, int sm_count, uint32_t wave_capacity, bool 
     if (lanes < 1 || lanes > 16) fail(REINA_ERR_INVALID, "a batch engine has 1 to 16 lanes");
     desc_bytes_ = sizeof(WaveHeader) + kMaxWaveSegments * sizeof(WaveSeg) + kMaxWaveJobs * sizeof(JobGpu);
     lanes_.resize((size_t)lanes);
-    for (Lane& L : lanes_) {
-        L.paths.alloc((64 + kBatchWordsPerPath * (size_t)capacity_) * 4);
-        L.desc.alloc(desc_bytes_);
-        check_cuda(cudaMallocHost(&L.host_desc, desc_bytes_), "cudaMallocHost");
-        check_cuda(cudaMallocHost(reinterpret_cast<void**>(&L.host_counters), kNumCounters * sizeof(uint32_t)),
-                   "cudaMallocHost");
-        check_cuda(cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking), "cudaStreamCreate");
-        check_cuda(cudaEventCreateWithFlags(&L.finished, cudaEventDisableTiming), "cudaEventCreate");
-        check_cuda(cudaEventCreateWithFlags(&L.done, cudaEventDisableTiming), "cudaEventCreate");
+    try {
+        for (Lane& L : lanes_) {
+            L.paths.alloc((64 + kBatchWordsPerPath * (size_t)capacity_) * 4);
+            L.desc.alloc(desc_bytes_);
+            check_cuda(cudaMallocHost(&L.host_desc, desc_bytes_), "cudaMallocHost");
+            check_cuda(cudaMallocHost(reinterpret_cast<void**>(&L.host_counters), kNumCounters * sizeof(uint32_t)),
+                       "cudaMallocHost");
+            check_cuda(cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking), "cudaStreamCreate");
+            check_cuda(cudaEventCreateWithFlags(&L.finished, cudaEventDisableTiming), "cudaEventCreate");
+            check_cuda(cudaEventCreateWithFlags(&L.done, cudaEventDisableTiming), "cudaEventCreate");
+        }
+    } catch (...) {   // the destructor does not run for a constructor that throws
+        release_lanes();
+        throw;
     }
     with_trace_variant(trace_, [&](auto B, auto S) {
         blocks_ext_ = resident_grid((const void*)kb_extend<B.value, S.value, false>, B.value, sm_count);
@@ -366,7 +371,9 @@ BatchEngine::BatchEngine(int device, int sm_count, uint32_t wave_capacity, bool 
     blocks_simple_ = occupancy((const void*)kb_finish, sm_count);
 }
 
-BatchEngine::~BatchEngine() {
+BatchEngine::~BatchEngine() { release_lanes(); }
+
+void BatchEngine::release_lanes() {
     for (Lane& L : lanes_) {
         if (L.stream) cudaStreamSynchronize(L.stream);
         for (auto& g : L.graphs)
@@ -377,6 +384,7 @@ BatchEngine::~BatchEngine() {
         if (L.host_desc) cudaFreeHost(L.host_desc);
         if (L.host_counters) cudaFreeHost(L.host_counters);
     }
+    lanes_.clear();
 }
 
 void BatchEngine::prepare(BatchJob& job, cudaMemPool_t pool, cudaStream_t st) {

@@ -155,6 +155,8 @@ private:
     void launch_finish(Lane& L, const Packed& pk, cudaStream_t s);
     // Adds a synchronized lane's counters to the totals; throws on a device error flag.
     void collect(Lane& L);
+    // Waits for and releases every lane's streams, events, graphs and buffers.
+    void release_lanes();
     int device_, sm_count_;
     uint32_t capacity_;
     bool use_graphs_;
