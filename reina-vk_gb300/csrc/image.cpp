@@ -493,6 +493,7 @@ struct JpegComp {
     int id = 0, h = 1, v = 1, tq = 0, td = 0, ta = 0;
     int bw = 0, bh = 0;       // blocks across / down (padded to whole MCUs)
     std::vector<uint8_t> plane;
+    std::vector<int16_t> coef;   // progressive frames: quantized coefficients, 64 per block in zigzag order
     int pred = 0;
 };
 
@@ -589,7 +590,7 @@ Image decode_jpeg(const uint8_t* d, size_t n) {
     int W = 0, H = 0, hmax = 1, vmax = 1, mcux = 0, mcuy = 0;
     int restart = 0;
     int adobe_transform = -1;
-    bool frame = false, seen_scan = false;
+    bool frame = false, seen_scan = false, progressive = false;
     size_t p = 2;
     auto u16 = [&](size_t at) {
         if (at + 2 > n) bad("JPEG: truncated");
@@ -631,8 +632,9 @@ Image decode_jpeg(const uint8_t* d, size_t n) {
                 h.derive();
                 k += 17 + (size_t)total;
             }
-        } else if (m == 0xC0 || m == 0xC1) {   // SOF0 / SOF1: sequential Huffman
+        } else if (m == 0xC0 || m == 0xC1 || m == 0xC2) {   // SOF0 / SOF1 sequential, SOF2 progressive (Huffman)
             if (frame) bad("JPEG: more than one frame");
+            progressive = m == 0xC2;
             if (sl < 6 || s[0] != 8) bad("JPEG: only 8-bit samples are supported");
             H = (s[1] << 8) | s[2];
             W = (s[3] << 8) | s[4];
@@ -657,10 +659,11 @@ Image decode_jpeg(const uint8_t* d, size_t n) {
                 c.bw = mcux * c.h;
                 c.bh = mcuy * c.v;
                 c.plane.assign((size_t)c.bw * 8 * c.bh * 8, 0);
+                if (progressive) c.coef.assign((size_t)c.bw * c.bh * 64, 0);
             }
             frame = true;
-        } else if (m == 0xC2 || m == 0xC3 || (m >= 0xC5 && m <= 0xCF && m != 0xC8 && m != 0xCC)) {
-            bad("JPEG: progressive, lossless and arithmetic-coded JPEG are not supported");
+        } else if (m == 0xC3 || (m >= 0xC5 && m <= 0xCF && m != 0xC8 && m != 0xCC)) {
+            bad("JPEG: lossless, hierarchical and arithmetic-coded JPEG are not supported");
         } else if (m == 0xDD) {   // DRI
             restart = u16(p + 2);
         } else if (m == 0xEE) {   // APP14 (Adobe): colour transform flag
@@ -677,13 +680,28 @@ Image decode_jpeg(const uint8_t* d, size_t n) {
                 if (!c) bad("JPEG: scan references an unknown component");
                 c->td = s[2 + 2 * k] >> 4;
                 c->ta = s[2 + 2 * k] & 15;
-                if (c->td > 3 || c->ta > 3 || !dc[c->td].defined || !ac[c->ta].defined) bad("JPEG: missing Huffman table");
+                if (c->td > 3 || c->ta > 3) bad("JPEG: bad Huffman table selector");
                 if (!qt_def[c->tq]) bad("JPEG: missing quantization table");
                 c->pred = 0;
                 sc.push_back(c);
             }
-            const uint8_t ss = s[1 + 2 * ns], se = s[2 + 2 * ns], ahal = s[3 + 2 * ns];
-            if (ss != 0 || se != 63 || ahal != 0) bad("JPEG: not a sequential scan");
+            const int ss = s[1 + 2 * ns], se = s[2 + 2 * ns], ah = s[3 + 2 * ns] >> 4, al = s[3 + 2 * ns] & 15;
+            if (!progressive) {
+                if (ss != 0 || se != 63 || ah != 0 || al != 0) bad("JPEG: not a sequential scan");
+                for (JpegComp* c : sc)
+                    if (!dc[c->td].defined || !ac[c->ta].defined) bad("JPEG: missing Huffman table");
+            } else {
+                // T.81 G.1.1.1: a DC scan (Ss = Se = 0) may interleave components; an AC scan
+                // (1 <= Ss <= Se <= 63) holds one; a refinement scan lowers the point transform by one bit
+                const bool dc_scan = ss == 0;
+                if (dc_scan ? se != 0 : (se < ss || se > 63 || ns != 1)) bad("JPEG: bad progressive scan band");
+                if (al > 13 || (ah != 0 && ah != al + 1)) bad("JPEG: bad successive-approximation parameters");
+                for (JpegComp* c : sc) {
+                    if (dc_scan && ah == 0 && !dc[c->td].defined) bad("JPEG: missing Huffman table");
+                    if (!dc_scan && !ac[c->ta].defined) bad("JPEG: missing Huffman table");
+                }
+            }
+            int eobrun = 0;   // progressive AC scans: blocks left in the current end-of-band run
             JpegBits in(d, n, p + (size_t)len);
             // blocks of one MCU: interleaved scans take h x v blocks per component; a single-component scan
             // takes the component's blocks one at a time in raster order over its own (unpadded) extent
@@ -718,20 +736,100 @@ Image decode_jpeg(const uint8_t* d, size_t n) {
                 const int stride = c.bw * 8;
                 idct8x8(F, c.plane.data() + (size_t)by * 8 * stride + (size_t)bx * 8, stride);
             };
+            // progressive scans (T.81 G.1.2): one band of one bit level of the coefficients per scan
+            const int p1 = 1 << al, m1 = -(1 << al);
+            auto refine = [&](int16_t& c) {   // a correction bit for a coefficient already nonzero
+                if (in.bit() && (c & p1) == 0) c = (int16_t)(c + (c >= 0 ? p1 : m1));
+            };
+            auto pblock = [&](JpegComp& c, int bx, int by) {
+                int16_t* blk = c.coef.data() + ((size_t)by * c.bw + bx) * 64;
+                if (ss == 0) {
+                    if (ah == 0) {   // DC first: difference of the point-transformed DC
+                        const int t = huff_decode(in, dc[c.td]);
+                        if (t > 11) bad("JPEG: bad DC difference");
+                        c.pred += extend(in.bits(t), t);
+                        blk[0] = (int16_t)(c.pred * (1 << al));
+                    } else if (in.bit()) {   // DC refinement: one more bit
+                        blk[0] = (int16_t)(blk[0] | p1);
+                    }
+                    return;
+                }
+                int k = ss;
+                if (ah == 0) {   // AC first: run/size symbols and end-of-band runs
+                    if (eobrun > 0) {
+                        --eobrun;
+                        return;
+                    }
+                    for (; k <= se; ++k) {
+                        const int rs = huff_decode(in, ac[c.ta]);
+                        const int r = rs >> 4, sz = rs & 15;
+                        if (sz == 0) {
+                            if (r == 15) {   // sixteen zeros
+                                k += 15;
+                                continue;
+                            }
+                            eobrun = (1 << r) - 1 + (r ? in.bits(r) : 0);   // this block and eobrun more
+                            break;
+                        }
+                        k += r;
+                        if (k > se) bad("JPEG: coefficient index past the band");
+                        blk[k] = (int16_t)(extend(in.bits(sz), sz) * (1 << al));
+                    }
+                    return;
+                }
+                // AC refinement: newly nonzero coefficients (magnitude 1 at this bit level) with their
+                // zero runs, and a correction bit for every coefficient that was already nonzero
+                if (eobrun == 0) {
+                    for (; k <= se; ++k) {
+                        const int rs = huff_decode(in, ac[c.ta]);
+                        int r = rs >> 4;
+                        const int sz = rs & 15;
+                        int val = 0;
+                        if (sz != 0) {
+                            if (sz != 1) bad("JPEG: bad refinement coefficient size");
+                            val = in.bit() ? p1 : m1;
+                        } else if (r != 15) {
+                            eobrun = (1 << r) + (r ? in.bits(r) : 0);
+                            break;
+                        }
+                        // pass r zero coefficients (correcting the nonzero ones on the way); stop at the
+                        // next zero, where a new coefficient goes (a run of sixteen leaves it zero)
+                        for (; k <= se; ++k) {
+                            if (blk[k] != 0) refine(blk[k]);
+                            else if (r == 0) break;
+                            else --r;
+                        }
+                        if (val != 0) {
+                            if (k > se) bad("JPEG: coefficient index past the band");
+                            blk[k] = (int16_t)val;
+                        }
+                    }
+                }
+                if (eobrun > 0) {   // the rest of the band is in an end-of-band run: corrections only
+                    for (; k <= se; ++k)
+                        if (blk[k] != 0) refine(blk[k]);
+                    --eobrun;
+                }
+            };
+            auto unit = [&](JpegComp& c, int bx, int by) {
+                if (progressive) pblock(c, bx, by);
+                else block(c, bx, by);
+            };
             int todo = restart;
             for (int my = 0; my < units_y; ++my)
                 for (int mx = 0; mx < units_x; ++mx) {
                     if (restart && todo == 0) {
                         in.restart();
                         for (JpegComp* c : sc) c->pred = 0;
+                        eobrun = 0;
                         todo = restart;
                     }
                     if (single) {
-                        block(*sc[0], mx, my);
+                        unit(*sc[0], mx, my);
                     } else {
                         for (JpegComp* c : sc)
                             for (int v = 0; v < c->v; ++v)
-                                for (int h = 0; h < c->h; ++h) block(*c, mx * c->h + h, my * c->v + v);
+                                for (int h = 0; h < c->h; ++h) unit(*c, mx * c->h + h, my * c->v + v);
                     }
                     if (restart) --todo;
                 }
@@ -742,6 +840,19 @@ Image decode_jpeg(const uint8_t* d, size_t n) {
         p += (size_t)len;
     }
     if (!frame || !seen_scan) bad("JPEG: no image data");
+    if (progressive) {   // every scan is in: dequantize and transform each block once
+        double F[64];
+        for (JpegComp& c : comps) {
+            const uint16_t* q = qt[c.tq];
+            const int stride = c.bw * 8;
+            for (int by = 0; by < c.bh; ++by)
+                for (int bx = 0; bx < c.bw; ++bx) {
+                    const int16_t* blk = c.coef.data() + ((size_t)by * c.bw + bx) * 64;
+                    for (int k = 0; k < 64; ++k) F[kZigzag[k]] = (double)blk[k] * q[k];
+                    idct8x8(F, c.plane.data() + (size_t)by * 8 * stride + (size_t)bx * 8, stride);
+                }
+        }
+    }
 
     // upsample every component to the full grid: 2:1 by the triangle filter (3/4 nearer + 1/4 farther
     // sample, JFIF co-sited centres), other ratios by replication

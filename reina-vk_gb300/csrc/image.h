@@ -21,12 +21,13 @@ std::vector<uint8_t> zlib_inflate(const uint8_t* data, size_t n, size_t limit);
 
 // Decodes an encoded image to RGBA8 the way stbi_load(..., 4) does: PNG of every colour type and bit
 // depth (1, 2, 4, 8, 16; 16-bit samples keep their high byte; grey levels below 8 bits are scaled to
-// 0..255; tRNS transparency; Adam7 interlacing), and sequential (baseline / extended Huffman, 8-bit) JPEG
-// with one or three components, any sampling factors, restart markers and multiple scans: inverse DCT
-// in double precision, 2:1 chroma upsampling by the triangle filter (replication for other ratios),
-// JFIF YCbCr -> RGB (Adobe RGB files kept as RGB).  stb_image's integer IDCT and fixed-point colour
-// conversion can give JPEG texels a few units apart from these.  Other formats (progressive JPEG, BMP,
-// TGA, GIF, HDR, ...) fail with REINA_ERR_IO.
+// 0..255; tRNS transparency; Adam7 interlacing), and sequential (baseline / extended Huffman, 8-bit) and
+// progressive (spectral selection and successive approximation, T.81 Annex G) Huffman JPEG with one or
+// three components, any sampling factors, restart markers and multiple scans: inverse DCT in double
+// precision, 2:1 chroma upsampling by the triangle filter (replication for other ratios), JFIF YCbCr ->
+// RGB (Adobe RGB files kept as RGB).  stb_image's integer IDCT and fixed-point colour conversion can
+// give JPEG texels a few units apart from these.  Other formats (lossless, hierarchical or
+// arithmetic-coded JPEG, BMP, TGA, GIF, HDR, ...) fail with REINA_ERR_IO.
 Image decode_image(const uint8_t* data, size_t n);
 
 // Reads and decodes a file; `flip_vertically` reverses the row order (stbi_set_flip_vertically_on_load,

@@ -3,7 +3,9 @@ its own forward DCT, quantization tables and Huffman tables built from the symbo
 chroma subsampling the decoder handles, restart intervals, single- and multi-scan files — and checks
 the library's decoding against the reconstruction of the coefficients it wrote (dequantization, the 8x8
 inverse DCT, the triangle-filter chroma upsampling and the JFIF YCbCr -> RGB conversion, restated in
-numpy), plus the reference's own JPEG textures when they are present."""
+numpy), plus the reference's own JPEG textures when they are present.  The same coefficients are also
+written as progressive JPEG (spectral selection and successive approximation) and must decode to the
+sequential file's pixels exactly."""
 import heapq
 import struct
 from pathlib import Path
@@ -340,3 +342,213 @@ def test_jpeg_reference_textures(R):
     assert alb.shape == (2048, 2048, 4) and nrm.shape == (2048, 2048, 4)
     assert nrm[..., 2].mean() > 240 and abs(nrm[..., 0].mean() - 128) < 8 and abs(nrm[..., 1].mean() - 128) < 8
     assert alb[..., 1].mean() > alb[..., 2].mean()   # a green-dominated albedo
+
+
+# ------------------------------------------------------------------------------------------------
+# Progressive JPEG (T.81 Annex G): the same quantized coefficients written as progressive scans —
+# spectral selection (DC, then AC bands of one component each) and successive approximation (a first
+# scan at a reduced bit level, then one refinement scan per bit), with end-of-band runs, zero-run
+# codes, correction bits and restart intervals — must decode to exactly the pixels of the sequential
+# file.
+
+def units_of(comps, layout, scan_comps):
+    """Blocks of a scan in coding order: (component index, block x, block y, mcu index)."""
+    hmax, vmax, mcux, mcuy = layout
+    out = []
+    if len(scan_comps) == 1:
+        c = comps[scan_comps[0]]
+        ux, uy = -(-c["cw"] // 8), -(-c["ch"] // 8)
+        for by in range(uy):
+            for bx in range(ux):
+                out.append((scan_comps[0], bx, by, by * ux + bx))
+    else:
+        for my in range(mcuy):
+            for mx in range(mcux):
+                for ci in scan_comps:
+                    c = comps[ci]
+                    for vv in range(c["v"]):
+                        for hh in range(c["h"]):
+                            out.append((ci, mx * c["h"] + hh, my * c["v"] + vv, my * mcux + mx))
+    return out
+
+
+def ac_point(v, al):   # AC point transform: magnitude shifted, sign kept (division toward zero)
+    return -((-v) >> al) if v < 0 else v >> al
+
+
+def progressive_events(comps, layout, sc, ss, se, ah, al, restart):
+    """One scan as a list of ("S", kind, class, symbol) / ("B", value, nbits) / ("R",) events."""
+    ev = []
+    acls = 0 if sc[0] == 0 else 1
+    st = {"eobrun": 0, "be": []}
+
+    def flush_eob():
+        n = st["eobrun"]
+        if n:
+            r = n.bit_length() - 1
+            ev.append(("S", "AC", acls, r << 4))
+            if r:
+                ev.append(("B", n - (1 << r), r))
+            ev.extend(("B", b, 1) for b in st["be"])
+            st["eobrun"], st["be"] = 0, []
+
+    preds = {ci: 0 for ci in sc}
+    last_mcu, n_mcu = -1, 0
+    for ci, bx, by, mcu in units_of(comps, layout, sc):
+        cls = 0 if ci == 0 else 1
+        if mcu != last_mcu:
+            if restart and n_mcu and n_mcu % restart == 0:
+                flush_eob()
+                ev.append(("R",))
+                preds = {c: 0 for c in sc}
+            last_mcu, n_mcu = mcu, n_mcu + 1
+        blk = comps[ci]["blocks"][by, bx]
+        if ss == 0:
+            if ah == 0:
+                v = int(blk[0]) >> al
+                diff, preds[ci] = v - preds[ci], v
+                cat = category(diff)
+                ev.append(("S", "DC", cls, cat))
+                if cat:
+                    ev.append(("B", bits_of(diff, cat), cat))
+            else:
+                ev.append(("B", (int(blk[0]) >> al) & 1, 1))
+            continue
+        band = [int(blk[k]) for k in range(ss, se + 1)]
+        if ah == 0:   # first scan of the band
+            vals = [ac_point(v, al) for v in band]
+            nz = [i for i, v in enumerate(vals) if v]
+            if nz:
+                flush_eob()
+                run = 0
+                for i in range(nz[-1] + 1):
+                    if vals[i] == 0:
+                        run += 1
+                        continue
+                    while run > 15:
+                        ev.append(("S", "AC", cls, 0xF0))
+                        run -= 16
+                    cat = category(vals[i])
+                    ev.append(("S", "AC", cls, (run << 4) | cat))
+                    ev.append(("B", bits_of(vals[i], cat), cat))
+                    run = 0
+            if not nz or nz[-1] < len(vals) - 1:
+                st["eobrun"] += 1
+                if st["eobrun"] == 0x7FFF:
+                    flush_eob()
+            continue
+        # refinement: one more bit of every coefficient of the band
+        absv = [abs(v) >> al for v in band]
+        news = [i for i, a in enumerate(absv) if a == 1]
+        last_new = news[-1] if news else -1
+        run, br = 0, []
+        for i, a in enumerate(absv):
+            if a == 0:
+                run += 1
+                continue
+            while run > 15 and i <= last_new:
+                flush_eob()
+                ev.append(("S", "AC", cls, 0xF0))
+                run -= 16
+                ev.extend(("B", b, 1) for b in br)
+                br = []
+            if a > 1:   # already nonzero: a correction bit
+                br.append(a & 1)
+                continue
+            flush_eob()
+            ev.append(("S", "AC", cls, (run << 4) | 1))
+            ev.append(("B", 0 if band[i] < 0 else 1, 1))
+            ev.extend(("B", b, 1) for b in br)
+            run, br = 0, []
+        if run > 0 or br:
+            st["eobrun"] += 1
+            st["be"] += br
+            if st["eobrun"] == 0x7FFF or len(st["be"]) > 900:
+                flush_eob()
+    flush_eob()
+    return ev
+
+
+SCRIPT_SA = ("dc:0:1", "ac:1:5:0:2", "ac:6:63:0:1", "dc:1:0", "ac:1:5:2:1", "ac:1:5:1:0", "ac:6:63:1:0")
+SCRIPT_SPECTRAL = ("dc:0:0", "ac:1:2:0:0", "ac:3:20:0:0", "ac:21:63:0:0")
+
+
+def encode_progressive(comps, qts, layout, H, W, gray, restart=0, script=SCRIPT_SA):
+    """The coefficients of `comps` as a progressive JPEG (SOF2) following `script`."""
+    seg = bytearray(b"\xff\xd8")
+    for t, q in enumerate(qts[: 1 if gray else 2]):
+        seg += b"\xff\xdb" + struct.pack(">HB", 67, t) + bytes(q.astype(np.uint8))
+    seg += b"\xff\xc2" + struct.pack(">HBHHB", 8 + 3 * len(comps), 8, H, W, len(comps))
+    for c in comps:
+        seg += bytes([c["id"], c["h"] << 4 | c["v"], c["tq"]])
+    if restart:
+        seg += b"\xff\xdd" + struct.pack(">HH", 4, restart)
+    scans = []
+    for item in script:
+        f = item.split(":")
+        if f[0] == "dc":
+            scans.append((list(range(len(comps))), 0, 0, int(f[1]), int(f[2])))
+        else:
+            for ci in range(len(comps)):
+                scans.append(([ci], int(f[1]), int(f[2]), int(f[3]), int(f[4])))
+    for sc, ss, se, ah, al in scans:
+        ev = progressive_events(comps, layout, sc, ss, se, ah, al, restart)
+        tables = {}
+        for kind in ("DC", "AC"):
+            for cls in (0, 1):
+                freq = {}
+                for e in ev:
+                    if e[0] == "S" and e[1] == kind and e[2] == cls:
+                        freq[e[3]] = freq.get(e[3], 0) + 1
+                if freq:
+                    tables[(kind, cls)] = canonical(huff_lengths(freq))
+        for (kind, cls), (counts, order, _) in tables.items():
+            tc = 0 if kind == "DC" else 1
+            seg += b"\xff\xc4" + struct.pack(">HB", 2 + 1 + 16 + len(order), tc << 4 | cls) + bytes(counts) + bytes(order)
+        seg += b"\xff\xda" + struct.pack(">HB", 6 + 2 * len(sc), len(sc))
+        for ci in sc:
+            cls = 0 if ci == 0 else 1
+            seg += bytes([comps[ci]["id"], cls << 4 | cls])
+        seg += bytes([ss, se, ah << 4 | al])
+        bw = BitWriter()
+        rst = 0
+        for e in ev:
+            if e[0] == "R":
+                bw.flush()
+                seg += bw.out
+                bw = BitWriter()
+                seg += bytes([0xFF, 0xD0 + rst])
+                rst = (rst + 1) % 8
+            elif e[0] == "S":
+                code, n = tables[(e[1], e[2])][2][e[3]]
+                bw.put(code, n)
+            else:
+                bw.put(e[1], e[2])
+        bw.flush()
+        seg += bw.out
+    seg += b"\xff\xd9"
+    return bytes(seg)
+
+
+PROGRESSIVE_CASES = [
+    dict(gray=True),
+    dict(sampling=((2, 2), (1, 1), (1, 1))),
+    dict(sampling=((1, 1), (1, 1), (1, 1)), restart=2),
+    dict(sampling=((2, 1), (1, 1), (1, 1)), script=SCRIPT_SPECTRAL),
+    dict(gray=True, restart=1, script=SCRIPT_SPECTRAL),
+]
+
+
+@pytest.mark.parametrize("case", range(len(PROGRESSIVE_CASES)))
+def test_progressive_jpeg_equals_sequential(R, case):
+    kw = dict(PROGRESSIVE_CASES[case])
+    script = kw.pop("script", SCRIPT_SA)
+    restart = kw.get("restart", 0)
+    gray = kw.get("gray", False)
+    for seed, (H, W) in enumerate([(37, 53), (64, 64), (8, 9), (1, 17), (96, 40)]):
+        img = sample_image(H, W, seed + 7 * case)
+        # quality_step 0: fine quantization, so many coefficients are large (several refinement bits)
+        data, comps, qts, layout = encode_jpeg(img, seed=seed, quality_step=0, **kw)
+        prog = encode_progressive(comps, qts, layout, H, W, gray, restart=restart, script=script)
+        assert prog[2:] != data[2:] and b"\xff\xc2" in prog
+        assert np.array_equal(R.decode_image(prog), R.decode_image(data)), (case, seed)
