@@ -552,3 +552,15 @@ def test_progressive_jpeg_equals_sequential(R, case):
         prog = encode_progressive(comps, qts, layout, H, W, gray, restart=restart, script=script)
         assert prog[2:] != data[2:] and b"\xff\xc2" in prog
         assert np.array_equal(R.decode_image(prog), R.decode_image(data)), (case, seed)
+
+
+def test_progressive_jpeg_refinements_matter(R):
+    """Leaving out any refinement scan (AC high band, AC low band, DC) changes the decoded pixels: the
+    refinement paths of the decoder are exercised, not bypassed."""
+    img = sample_image(64, 64, 3)
+    data, comps, qts, layout = encode_jpeg(img, seed=1, quality_step=0, sampling=((2, 2), (1, 1), (1, 1)))
+    full = R.decode_image(data)
+    for drop in ("ac:6:63:1:0", "ac:1:5:1:0", "dc:1:0"):
+        script = tuple(s for s in SCRIPT_SA if s != drop)
+        got = R.decode_image(encode_progressive(comps, qts, layout, 64, 64, False, script=script))
+        assert not np.array_equal(got, full), drop
