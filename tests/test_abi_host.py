@@ -302,3 +302,30 @@ def test_emissive_export_and_device_build_on_host(R, host_ctx):
     with pytest.raises(R.ReinaError) as e:
         d.build()
     assert e.value.code == R.REINA_ERR_STATE
+
+
+@pytest.mark.parametrize("pos,front,up,fovy,aspect", [((0, 0, 3.4), (0, 0, -1), (0, 1, 0), 40.0, 1.0),
+                                                      ((0.0, 0.4, 3.6), (0.0, -0.12, -1.0), (0, 1, 0), 40.0, 16 / 9),
+                                                      ((2, -1, 0.5), (-1, 0.3, 0.2), (0, 1, 0), 25.0, 0.8)])
+def test_camera_matrices_invert_lookat_and_perspective(R, pos, front, up, fovy, aspect):
+    """Camera::getInvViewMatrix / getInvProjMatrix (src/graphics/Camera.cpp:10-11): the inverses of
+    lookAt(pos, pos + front, up) and perspective(fovy, aspect, 0.1, 100) (right-handed, clip depth -1..1),
+    restated here in float64 and checked by multiplying out."""
+    iv, ip = R.camera_matrices(pos, front, up, np.radians(fovy), aspect)
+    IV = np.asarray(iv, np.float64).reshape(4, 4).T   # column-major storage
+    IP = np.asarray(ip, np.float64).reshape(4, 4).T
+    p, f, u = np.asarray(pos, float), np.asarray(front, float), np.asarray(up, float)
+    f = f / np.linalg.norm(f)
+    s = np.cross(f, u)
+    s /= np.linalg.norm(s)
+    uu = np.cross(s, f)
+    view = np.eye(4)
+    view[0, :3], view[1, :3], view[2, :3] = s, uu, -f
+    view[:3, 3] = [-s @ p, -uu @ p, f @ p]
+    t = np.tan(np.radians(fovy) / 2)
+    n, fa = 0.1, 100.0
+    proj = np.zeros((4, 4))
+    proj[0, 0], proj[1, 1] = 1 / (aspect * t), 1 / t
+    proj[2, 2], proj[2, 3], proj[3, 2] = -(fa + n) / (fa - n), -2 * fa * n / (fa - n), -1.0
+    assert np.allclose(IV @ view, np.eye(4), atol=1e-5)
+    assert np.allclose(IP @ proj, np.eye(4), atol=1e-5)
