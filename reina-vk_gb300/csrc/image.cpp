@@ -926,11 +926,203 @@ Image decode_jpeg(const uint8_t* d, size_t n) {
 
 }  // namespace
 
+namespace {
+
+uint32_t le16(const uint8_t* p) { return (uint32_t)p[0] | ((uint32_t)p[1] << 8); }
+uint32_t le32(const uint8_t* p) { return le16(p) | (le16(p + 2) << 16); }
+
+// Value of the bits of `v` under `mask`, scaled to 0..255 (a mask of zero gives `none`).
+uint8_t masked(uint32_t v, uint32_t mask, uint8_t none) {
+    if (mask == 0) return none;
+    int shift = 0;
+    while (((mask >> shift) & 1u) == 0) ++shift;
+    const uint32_t m = mask >> shift;
+    int bits = 0;
+    while ((m >> bits) & 1u) ++bits;
+    const uint32_t x = (v & mask) >> shift, top = (1u << bits) - 1u;
+    return (uint8_t)((x * 255u + top / 2) / top);
+}
+
+// Windows / OS/2 bitmap: 1, 4, 8 (palette), 16 (5-5-5 or bit fields), 24 and 32 (BGRA or bit fields) bits
+// per pixel, bottom-up or top-down, uncompressed.  32-bit pixels whose alpha is zero everywhere are opaque.
+Image decode_bmp(const uint8_t* d, size_t n) {
+    if (n < 26) bad("BMP: truncated");
+    const uint32_t offset = le32(d + 10), hsize = le32(d + 14);
+    int64_t w, h;
+    uint32_t bpp, comp = 0, ncolors = 0;
+    size_t pal_entry = 4;
+    if (hsize == 12) {   // OS/2 core header
+        w = le16(d + 18);
+        h = le16(d + 20);
+        bpp = le16(d + 24);
+        pal_entry = 3;
+    } else if (hsize >= 40 && n >= 14 + 40) {
+        w = (int32_t)le32(d + 18);
+        h = (int32_t)le32(d + 22);
+        bpp = le16(d + 28);
+        comp = le32(d + 30);
+        ncolors = le32(d + 46);
+    } else {
+        bad("BMP: unsupported header");
+    }
+    const bool top_down = h < 0;
+    if (h < 0) h = -h;
+    if (w <= 0 || h <= 0 || (uint64_t)w * (uint64_t)h > (1ull << 28)) bad("BMP: bad size");
+    if (comp != 0 && comp != 3) bad("BMP: compressed bitmaps are not supported");
+    if (bpp != 1 && bpp != 4 && bpp != 8 && bpp != 16 && bpp != 24 && bpp != 32) bad("BMP: unsupported bit depth");
+    uint32_t mr = 0, mg = 0, mb = 0, ma = 0;
+    if (bpp == 16) { mr = 0x7C00; mg = 0x03E0; mb = 0x001F; }
+    if (bpp == 32) { mr = 0x00FF0000; mg = 0x0000FF00; mb = 0x000000FF; ma = 0xFF000000; }
+    if (comp == 3) {
+        if (bpp != 16 && bpp != 32) bad("BMP: bit fields need 16 or 32 bits per pixel");
+        if (n < 14 + 40 + 12) bad("BMP: truncated");
+        mr = le32(d + 54);
+        mg = le32(d + 58);
+        mb = le32(d + 62);
+        ma = hsize >= 56 && n >= 14 + 56 ? le32(d + 66) : 0;
+    }
+    std::vector<uint8_t> pal;   // RGBA
+    if (bpp <= 8) {
+        const uint32_t count = ncolors ? ncolors : (1u << bpp);
+        if (count > 256) bad("BMP: bad palette size");
+        const size_t at = 14 + hsize;
+        if (at + count * pal_entry > n) bad("BMP: truncated palette");
+        pal.resize((size_t)count * 4);
+        for (uint32_t i = 0; i < count; ++i) {
+            const uint8_t* e = d + at + i * pal_entry;
+            pal[4 * i + 0] = e[2];
+            pal[4 * i + 1] = e[1];
+            pal[4 * i + 2] = e[0];
+            pal[4 * i + 3] = 255;
+        }
+    }
+    const size_t stride = (((size_t)w * bpp + 31) / 32) * 4;
+    if (offset > n || (size_t)h * stride > n - offset) bad("BMP: truncated pixel data");
+    Image img;
+    img.width = (uint32_t)w;
+    img.height = (uint32_t)h;
+    img.rgba.assign((size_t)w * h * 4, 255);
+    bool any_alpha = false;
+    for (int64_t y = 0; y < h; ++y) {
+        const uint8_t* row = d + offset + (size_t)(top_down ? y : h - 1 - y) * stride;
+        uint8_t* o = &img.rgba[(size_t)y * w * 4];
+        for (int64_t x = 0; x < w; ++x, o += 4) {
+            if (bpp <= 8) {
+                const size_t bit = (size_t)x * bpp;
+                const uint32_t idx = (row[bit / 8] >> (8 - bpp - bit % 8)) & ((1u << bpp) - 1u);
+                if ((size_t)idx * 4 >= pal.size()) bad("BMP: palette index out of range");
+                std::memcpy(o, &pal[(size_t)idx * 4], 4);
+            } else if (bpp == 24) {
+                o[0] = row[3 * x + 2];
+                o[1] = row[3 * x + 1];
+                o[2] = row[3 * x + 0];
+            } else {
+                const uint32_t v = bpp == 16 ? le16(row + 2 * x) : le32(row + 4 * x);
+                o[0] = masked(v, mr, 0);
+                o[1] = masked(v, mg, 0);
+                o[2] = masked(v, mb, 0);
+                o[3] = masked(v, ma, 255);
+                any_alpha = any_alpha || o[3] != 0;
+            }
+        }
+    }
+    if (bpp == 32 && ma != 0 && !any_alpha)   // an unused alpha channel: opaque
+        for (size_t i = 3; i < img.rgba.size(); i += 4) img.rgba[i] = 255;
+    return img;
+}
+
+// Truevision TGA: colour-mapped (8-bit indices into 15/16/24/32-bit entries), true-colour (15/16, 24, 32
+// bits) and grey (8 bits) images, uncompressed or run-length encoded, either origin.
+bool looks_like_tga(const uint8_t* d, size_t n) {
+    if (n < 18) return false;
+    const int cmap = d[1], type = d[2], depth = d[16];
+    if (cmap > 1) return false;
+    if (type != 1 && type != 2 && type != 3 && type != 9 && type != 10 && type != 11) return false;
+    if ((type == 1 || type == 9) ? (cmap != 1 || depth != 8) : (depth != 8 && depth != 15 && depth != 16 && depth != 24 && depth != 32))
+        return false;
+    return le16(d + 12) > 0 && le16(d + 14) > 0;
+}
+
+Image decode_tga(const uint8_t* d, size_t n) {
+    if (!looks_like_tga(d, n)) bad("TGA: bad header");
+    const uint32_t id_len = d[0], cmap_type = d[1], type = d[2];
+    const uint32_t cmap_first = le16(d + 3), cmap_len = le16(d + 5), cmap_bits = d[7];
+    const uint32_t w = le16(d + 12), h = le16(d + 14), depth = d[16], desc = d[17];
+    const bool rle = type >= 9, gray = type == 3 || type == 11, mapped = type == 1 || type == 9;
+    size_t p = 18 + id_len;
+    auto texel = [](const uint8_t* e, uint32_t bits, uint8_t* o) {   // one stored value -> RGBA
+        if (bits == 15 || bits == 16) {
+            const uint32_t v = le16(e);
+            o[0] = (uint8_t)((((v >> 10) & 31u) * 255u + 15u) / 31u);
+            o[1] = (uint8_t)((((v >> 5) & 31u) * 255u + 15u) / 31u);
+            o[2] = (uint8_t)(((v & 31u) * 255u + 15u) / 31u);
+            o[3] = 255;
+        } else {
+            o[0] = e[2];
+            o[1] = e[1];
+            o[2] = e[0];
+            o[3] = bits == 32 ? e[3] : 255;
+        }
+    };
+    std::vector<uint8_t> pal;
+    if (cmap_type == 1) {
+        if (cmap_bits != 15 && cmap_bits != 16 && cmap_bits != 24 && cmap_bits != 32) bad("TGA: bad colour map");
+        const size_t eb = (cmap_bits + 7) / 8;
+        if (p + cmap_len * eb > n) bad("TGA: truncated colour map");
+        pal.resize((size_t)(cmap_first + cmap_len) * 4, 0);
+        for (uint32_t i = 0; i < cmap_len; ++i) texel(d + p + i * eb, cmap_bits, &pal[(size_t)(cmap_first + i) * 4]);
+        p += cmap_len * eb;
+    }
+    const size_t pb = (depth + 7) / 8;
+    Image img;
+    img.width = w;
+    img.height = h;
+    img.rgba.assign((size_t)w * h * 4, 255);
+    auto put = [&](const uint8_t* e, size_t i) {
+        uint8_t* o = &img.rgba[i * 4];
+        if (mapped) {
+            if ((size_t)e[0] * 4 + 4 > pal.size()) bad("TGA: colour index out of range");
+            std::memcpy(o, &pal[(size_t)e[0] * 4], 4);
+        } else if (gray) {
+            o[0] = o[1] = o[2] = e[0];
+        } else {
+            texel(e, depth, o);
+        }
+    };
+    const size_t total = (size_t)w * h;
+    size_t i = 0;
+    while (i < total) {
+        if (!rle) {
+            if (p + pb > n) bad("TGA: truncated pixel data");
+            put(d + p, i++);
+            p += pb;
+            continue;
+        }
+        if (p >= n) bad("TGA: truncated pixel data");
+        const uint32_t hdr = d[p++], count = (hdr & 0x7F) + 1;
+        if (i + count > total) bad("TGA: run past the image");
+        if (hdr & 0x80) {   // one value repeated
+            if (p + pb > n) bad("TGA: truncated pixel data");
+            for (uint32_t k = 0; k < count; ++k) put(d + p, i++);
+            p += pb;
+        } else {
+            if (p + count * pb > n) bad("TGA: truncated pixel data");
+            for (uint32_t k = 0; k < count; ++k, p += pb) put(d + p, i++);
+        }
+    }
+    if ((desc & 0x20) == 0) flip_rows(img);   // stored bottom row first
+    return img;
+}
+
+}  // namespace
+
 Image decode_image(const uint8_t* data, size_t n) {
     static const uint8_t kPngSig[8] = {137, 80, 78, 71, 13, 10, 26, 10};
     if (n >= 8 && std::memcmp(data, kPngSig, 8) == 0) return decode_png(data, n);
     if (n >= 3 && data[0] == 0xFF && data[1] == 0xD8 && data[2] == 0xFF) return decode_jpeg(data, n);
-    bad("unknown image format (PNG or JPEG expected)");
+    if (n >= 2 && data[0] == 'B' && data[1] == 'M') return decode_bmp(data, n);
+    if (looks_like_tga(data, n)) return decode_tga(data, n);   // TGA has no signature: a plausible header
+    bad("unknown image format (PNG, JPEG, BMP or TGA expected)");
 }
 
 void flip_rows(Image& img) {

@@ -26,8 +26,11 @@ std::vector<uint8_t> zlib_inflate(const uint8_t* data, size_t n, size_t limit);
 // three components, any sampling factors, restart markers and multiple scans: inverse DCT in double
 // precision, 2:1 chroma upsampling by the triangle filter (replication for other ratios), JFIF YCbCr ->
 // RGB (Adobe RGB files kept as RGB).  stb_image's integer IDCT and fixed-point colour conversion can
-// give JPEG texels a few units apart from these.  Other formats (lossless, hierarchical or
-// arithmetic-coded JPEG, BMP, TGA, GIF, HDR, ...) fail with REINA_ERR_IO.
+// give JPEG texels a few units apart from these.  BMP (1/4/8-bit palettes, 16-bit 5-5-5 or bit fields,
+// 24 and 32 bits, either row order, uncompressed; a 32-bit alpha that is zero everywhere reads as opaque)
+// and TGA (colour-mapped, true-colour 15/16/24/32-bit and grey, raw or run-length encoded, either
+// origin).  Other formats (lossless, hierarchical or arithmetic-coded JPEG, RLE bitmaps, GIF, HDR, ...)
+// fail with REINA_ERR_IO.
 Image decode_image(const uint8_t* data, size_t n);
 
 // Reads and decodes a file; `flip_vertically` reverses the row order (stbi_set_flip_vertically_on_load,

@@ -1,0 +1,163 @@
+"""BMP and TGA texture decoding on the host (the formats stbi_load reads besides PNG and JPEG, behind
+Scene::defineTexture, src/graphics/Image.cpp:10-41): the test writes seeded images in each layout itself
+— BMP with 1/4/8-bit palettes, 16-bit 5-5-5 and bit fields, 24-bit, 32-bit with and without alpha,
+bottom-up and top-down; TGA true-colour 16/24/32-bit, grey, colour-mapped, uncompressed and run-length
+encoded, both origins — and requires the decoded RGBA8 (rows top to bottom) to equal the image it wrote."""
+import struct
+
+import numpy as np
+import pytest
+
+
+def rgba_image(H, W, seed, alpha=True):
+    rng = np.random.default_rng(seed)
+    img = rng.integers(0, 256, (H, W, 4), dtype=np.uint8)
+    if not alpha:
+        img[..., 3] = 255
+    return img
+
+
+def bmp(img, bpp=24, top_down=False, palette=None, fields=None):
+    H, W = img.shape[:2]
+    rows = []
+    for y in range(H):
+        px = img[y]
+        if bpp == 24:
+            raw = px[:, [2, 1, 0]].tobytes()
+        elif bpp == 32:
+            raw = px[:, [2, 1, 0, 3]].tobytes()
+        elif bpp == 16:
+            v = ((px[:, 0].astype(np.uint32) >> 3) << 10) | ((px[:, 1].astype(np.uint32) >> 3) << 5) | (px[:, 2] >> 3)
+            if fields:   # 5-6-5
+                v = ((px[:, 0].astype(np.uint32) >> 3) << 11) | ((px[:, 1].astype(np.uint32) >> 2) << 5) | (px[:, 2] >> 3)
+            raw = v.astype("<u2").tobytes()
+        else:   # indices into `palette` (image holds palette colours)
+            idx = [palette.index(tuple(int(c) for c in p[:3])) for p in px]
+            bits = "".join(format(i, f"0{bpp}b") for i in idx)
+            bits += "0" * (-len(bits) % 8)
+            raw = bytes(int(bits[k:k + 8], 2) for k in range(0, len(bits), 8))
+        raw += b"\0" * (-len(raw) % 4)
+        rows.append(raw)
+    if not top_down:
+        rows = rows[::-1]
+    pal = b"".join(bytes([b, g, r, 0]) for r, g, b in (palette or []))
+    masks = struct.pack("<III", *fields) if fields else b""
+    offset = 14 + 40 + len(masks) + len(pal)
+    data = b"".join(rows)
+    hdr = b"BM" + struct.pack("<IHHI", offset + len(data), 0, 0, offset)
+    dib = struct.pack("<IiiHHIIiiII", 40, W, -H if top_down else H, 1, bpp, 3 if fields else 0, len(data), 2835, 2835,
+                      len(palette or []), 0)
+    return hdr + dib + masks + pal + data
+
+
+def to5(c):
+    return (((c.astype(np.uint32) >> 3) * 255 + 15) // 31).astype(np.uint8)
+
+
+def to6(c):
+    return (((c.astype(np.uint32) >> 2) * 255 + 31) // 63).astype(np.uint8)
+
+
+def tga(img, kind="rgb32", rle=False, top_left=False):
+    H, W = img.shape[:2]
+    rows = list(img) if top_left else list(img[::-1])
+    cmap = b""
+    cmap_type, cmap_len, cmap_bits = 0, 0, 0
+    if kind == "rgb32":
+        vals = [bytes([p[2], p[1], p[0], p[3]]) for r in rows for p in r]
+        itype, depth, desc = 2, 32, 8
+    elif kind == "rgb24":
+        vals = [bytes([p[2], p[1], p[0]]) for r in rows for p in r]
+        itype, depth, desc = 2, 24, 0
+    elif kind == "rgb16":
+        vals = [struct.pack("<H", ((int(p[0]) >> 3) << 10) | ((int(p[1]) >> 3) << 5) | (int(p[2]) >> 3)) for r in rows for p in r]
+        itype, depth, desc = 2, 16, 0
+    elif kind == "gray":
+        vals = [bytes([p[0]]) for r in rows for p in r]
+        itype, depth, desc = 3, 8, 0
+    else:   # colour-mapped, 24-bit entries
+        colours = sorted({tuple(int(c) for c in p[:3]) for r in rows for p in r})
+        cmap = b"".join(bytes([b, g, r]) for r, g, b in colours)
+        vals = [bytes([colours.index(tuple(int(c) for c in p[:3]))]) for r in rows for p in r]
+        itype, depth, desc = 1, 8, 0
+        cmap_type, cmap_len, cmap_bits = 1, len(colours), 24
+    if top_left:
+        desc |= 0x20
+    body = b""
+    if not rle:
+        body = b"".join(vals)
+    else:
+        i = 0
+        while i < len(vals):   # runs of equal values as run packets, the rest as raw packets (<= 128)
+            j = i
+            while j + 1 < len(vals) and vals[j + 1] == vals[i] and j + 1 - i < 128:
+                j += 1
+            if j > i:
+                body += bytes([0x80 | (j - i)]) + vals[i]
+                i = j + 1
+            else:
+                k = i
+                while k + 1 < len(vals) and vals[k + 1] != vals[k] and k + 1 - i < 128:
+                    k += 1
+                body += bytes([k - i]) + b"".join(vals[i:k + 1])
+                i = k + 1
+        itype += 8
+    hdr = struct.pack("<BBBHHBHHHHBB", 0, cmap_type, itype, 0, cmap_len, cmap_bits, 0, 0, W, H, depth, desc)
+    return hdr + cmap + body
+
+
+@pytest.mark.parametrize("H,W", [(5, 7), (16, 16), (1, 3), (9, 1)])
+def test_bmp_layouts(R, H, W):
+    img = rgba_image(H, W, H * 31 + W)
+    opaque = img.copy()
+    opaque[..., 3] = 255
+    assert np.array_equal(R.decode_image(bmp(img, 24)), opaque)
+    assert np.array_equal(R.decode_image(bmp(img, 24, top_down=True)), opaque)
+    assert np.array_equal(R.decode_image(bmp(img, 32)), img)
+    no_alpha = img.copy()
+    no_alpha[..., 3] = 0   # an unused alpha channel decodes opaque
+    assert np.array_equal(R.decode_image(bmp(no_alpha, 32, top_down=True)), opaque)
+    want16 = np.stack([to5(img[..., 0]), to5(img[..., 1]), to5(img[..., 2]), np.full((H, W), 255, np.uint8)], -1)
+    assert np.array_equal(R.decode_image(bmp(img, 16)), want16)
+    want565 = np.stack([to5(img[..., 0]), to6(img[..., 1]), to5(img[..., 2]), np.full((H, W), 255, np.uint8)], -1)
+    assert np.array_equal(R.decode_image(bmp(img, 16, fields=(0xF800, 0x07E0, 0x001F))), want565)
+    for bpp in (1, 4, 8):
+        rng = np.random.default_rng(bpp)
+        palette = [tuple(int(c) for c in rng.integers(0, 256, 3)) for _ in range(1 << bpp)]
+        pal_img = np.zeros((H, W, 4), np.uint8)
+        pal_img[..., 3] = 255
+        idx = rng.integers(0, 1 << bpp, (H, W))
+        for y in range(H):
+            for x in range(W):
+                pal_img[y, x, :3] = palette[idx[y, x]]
+        assert np.array_equal(R.decode_image(bmp(pal_img, bpp, palette=palette)), pal_img), bpp
+
+
+@pytest.mark.parametrize("rle", [False, True])
+@pytest.mark.parametrize("top_left", [False, True])
+def test_tga_layouts(R, rle, top_left):
+    H, W = 11, 13
+    img = rgba_image(H, W, 7 + rle + 2 * top_left)
+    img[3:6, 2:9] = img[3, 2]   # runs for the run-length packets
+    opaque = img.copy()
+    opaque[..., 3] = 255
+    assert np.array_equal(R.decode_image(tga(img, "rgb32", rle, top_left)), img)
+    assert np.array_equal(R.decode_image(tga(img, "rgb24", rle, top_left)), opaque)
+    want16 = np.stack([to5(img[..., 0]), to5(img[..., 1]), to5(img[..., 2]), np.full((H, W), 255, np.uint8)], -1)
+    assert np.array_equal(R.decode_image(tga(img, "rgb16", rle, top_left)), want16)
+    gray = np.stack([img[..., 0]] * 3 + [np.full((H, W), 255, np.uint8)], -1)
+    assert np.array_equal(R.decode_image(tga(img, "gray", rle, top_left)), gray)
+    few = img.copy()
+    few[..., :3] = (few[..., :3] // 64) * 64   # at most 64 colours for the colour map
+    few[..., 3] = 255
+    assert np.array_equal(R.decode_image(tga(few, "mapped", rle, top_left)), few)
+
+
+def test_bmp_tga_malformed(R):
+    img = rgba_image(4, 4, 1)
+    good_bmp, good_tga = bmp(img, 24), tga(img, "rgb32", rle=True)
+    bad = [good_bmp[:40], good_bmp[:-5], good_tga[:-3], good_bmp[:30] + struct.pack("<I", 1) + good_bmp[34:]]
+    for data in bad:
+        with pytest.raises(R.ReinaError) as e:
+            R.decode_image(data)
+        assert e.value.code == R.REINA_ERR_IO
