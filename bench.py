@@ -12,11 +12,13 @@ L2 (129 MB) is flushed by writing a 512 MB buffer between timed steps (outside t
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 Beside the headline line's required keys, the JSON carries: `render` (the 1.3M-triangle scene at
-1920x1080, 64 spp, 12 bounces, NEE+MIS, wavefront vs plain megakernel; the Cornell room), `batched` (256
-seeded scenes rendered in one batched call vs one at a time; `--batch-scenes`), `served` (a Poisson
-request stream through the request server vs one at a time; `--serve-seconds`), `instanced` (256
-instances of one sphere built flat and as two levels: device memory, build time, ray-cast time;
-`--instances`), and `cpu_baseline`.
+1920x1080, 64 spp, 12 bounces, NEE+MIS, and the Cornell room, each in the three forms: the wave engine,
+the pass-by-pass wavefront and the plain megakernel), `batched` (256 seeded scenes rendered in one
+autotuned batched call vs one at a time in the plain forms and on the wave engine; `--batch-scenes`),
+`served` (a Poisson request stream through the request server under each wave-slot policy vs one at a
+time; `--serve-seconds`), `instanced` (256 instances of one sphere built flat and as two levels: device
+memory, build time, ray-cast time; `--instances`), `emissive_cdf` (the emissive CDF build of a
+1.3M-triangle emissive mesh on the host and on the GPU), and `cpu_baseline`.
 `--profile`, `--profile-render` and `--profile-batch` launch small fixed workloads for ncu and exit.
 
 `--impl reference` times the CPU restatement of the path (oracle/, FP32, all host threads) on a bounded
