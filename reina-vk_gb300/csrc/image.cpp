@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <fstream>
 #include <iterator>
@@ -1114,6 +1115,81 @@ Image decode_tga(const uint8_t* d, size_t n) {
     return img;
 }
 
+// Radiance RGBE (.hdr): "-Y H +X W" scanlines, flat or run-length encoded per channel.  A texture read
+// as 8-bit RGBA is tone mapped like stbi_load does for HDR files (its documented defaults): each channel
+// m * 2^(e - 136), then 255 * x^(1/2.2) + 0.5 truncated and clamped; alpha 255.
+Image decode_hdr(const uint8_t* d, size_t n) {
+    size_t p = 0;
+    auto line = [&]() {
+        std::string l;
+        while (p < n && d[p] != '\n') l.push_back((char)d[p++]);
+        if (p >= n) bad("HDR: truncated header");
+        ++p;
+        return l;
+    };
+    const std::string magic = line();
+    if (magic != "#?RADIANCE" && magic != "#?RGBE") bad("HDR: bad signature");
+    for (;;) {
+        const std::string l = line();
+        if (l.empty()) break;
+        if (l.rfind("FORMAT=", 0) == 0 && l != "FORMAT=32-bit_rle_rgbe") bad("HDR: only 32-bit_rle_rgbe is supported");
+    }
+    int H = 0, W = 0;
+    {
+        const std::string res = line();
+        char ya[3] = {0}, xa[3] = {0};
+        if (std::sscanf(res.c_str(), "%2s %d %2s %d", ya, &H, xa, &W) != 4 || std::string(ya) != "-Y" ||
+            std::string(xa) != "+X")
+            bad("HDR: only -Y H +X W orientation is supported");
+    }
+    if (W <= 0 || H <= 0 || (uint64_t)W * H > (1ull << 28)) bad("HDR: bad size");
+    Image img;
+    img.width = (uint32_t)W;
+    img.height = (uint32_t)H;
+    img.rgba.assign((size_t)W * H * 4, 255);
+    std::vector<uint8_t> scan((size_t)W * 4);
+    auto to8 = [](uint8_t m, uint8_t e) {
+        if (e == 0) return (uint8_t)0;
+        const float f = std::ldexp((float)m, (int)e - 136);
+        const float z = std::pow(f, 1.0f / 2.2f) * 255.0f + 0.5f;
+        return (uint8_t)(z < 0.0f ? 0.0f : (z > 255.0f ? 255.0f : z));
+    };
+    for (int y = 0; y < H; ++y) {
+        const bool rle = W >= 8 && W < 32768 && p + 4 <= n && d[p] == 2 && d[p + 1] == 2 &&
+                         (((int)d[p + 2] << 8) | d[p + 3]) == W;
+        if (rle) {
+            p += 4;
+            for (int c = 0; c < 4; ++c) {   // each channel of the scanline in turn
+                int x = 0;
+                while (x < W) {
+                    if (p >= n) bad("HDR: truncated scanline");
+                    int count = d[p++];
+                    if (count > 128) {
+                        count -= 128;
+                        if (p >= n || x + count > W) bad("HDR: bad run");
+                        for (int k = 0; k < count; ++k) scan[(size_t)(x + k) * 4 + c] = d[p];
+                        ++p;
+                    } else {
+                        if (count == 0 || x + count > W || p + (size_t)count > n) bad("HDR: bad literal run");
+                        for (int k = 0; k < count; ++k) scan[(size_t)(x + k) * 4 + c] = d[p++];
+                    }
+                    x += count;
+                }
+            }
+        } else {
+            if (p + (size_t)W * 4 > n) bad("HDR: truncated scanline");
+            std::memcpy(scan.data(), d + p, (size_t)W * 4);
+            p += (size_t)W * 4;
+        }
+        for (int x = 0; x < W; ++x) {
+            const uint8_t* e = &scan[(size_t)x * 4];
+            uint8_t* o = &img.rgba[((size_t)y * W + x) * 4];
+            for (int c = 0; c < 3; ++c) o[c] = to8(e[c], e[3]);
+        }
+    }
+    return img;
+}
+
 }  // namespace
 
 Image decode_image(const uint8_t* data, size_t n) {
@@ -1121,8 +1197,10 @@ Image decode_image(const uint8_t* data, size_t n) {
     if (n >= 8 && std::memcmp(data, kPngSig, 8) == 0) return decode_png(data, n);
     if (n >= 3 && data[0] == 0xFF && data[1] == 0xD8 && data[2] == 0xFF) return decode_jpeg(data, n);
     if (n >= 2 && data[0] == 'B' && data[1] == 'M') return decode_bmp(data, n);
+    if (n >= 6 && (std::memcmp(data, "#?RADIANCE", std::min<size_t>(n, 10)) == 0 || std::memcmp(data, "#?RGBE", 6) == 0))
+        return decode_hdr(data, n);
     if (looks_like_tga(data, n)) return decode_tga(data, n);   // TGA has no signature: a plausible header
-    bad("unknown image format (PNG, JPEG, BMP or TGA expected)");
+    bad("unknown image format (PNG, JPEG, BMP, TGA or HDR expected)");
 }
 
 void flip_rows(Image& img) {

@@ -29,8 +29,9 @@ std::vector<uint8_t> zlib_inflate(const uint8_t* data, size_t n, size_t limit);
 // give JPEG texels a few units apart from these.  BMP (1/4/8-bit palettes, 16-bit 5-5-5 or bit fields,
 // 24 and 32 bits, either row order, uncompressed; a 32-bit alpha that is zero everywhere reads as opaque)
 // and TGA (colour-mapped, true-colour 15/16/24/32-bit and grey, raw or run-length encoded, either
-// origin).  Other formats (lossless, hierarchical or arithmetic-coded JPEG, RLE bitmaps, GIF, HDR, ...)
-// fail with REINA_ERR_IO.
+// origin), and Radiance RGBE (.hdr, flat or run-length scanlines) tone mapped as stbi_load does for 8-bit
+// output (255 x^(1/2.2) + 0.5).  Other formats (lossless, hierarchical or arithmetic-coded JPEG, RLE
+// bitmaps, GIF, ...) fail with REINA_ERR_IO.
 Image decode_image(const uint8_t* data, size_t n);
 
 // Reads and decodes a file; `flip_vertically` reverses the row order (stbi_set_flip_vertically_on_load,

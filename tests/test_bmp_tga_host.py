@@ -1,8 +1,9 @@
-"""BMP and TGA texture decoding on the host (the formats stbi_load reads besides PNG and JPEG, behind
+"""BMP, TGA and Radiance HDR texture decoding on the host (the formats stbi_load reads besides PNG and JPEG, behind
 Scene::defineTexture, src/graphics/Image.cpp:10-41): the test writes seeded images in each layout itself
 — BMP with 1/4/8-bit palettes, 16-bit 5-5-5 and bit fields, 24-bit, 32-bit with and without alpha,
 bottom-up and top-down; TGA true-colour 16/24/32-bit, grey, colour-mapped, uncompressed and run-length
-encoded, both origins — and requires the decoded RGBA8 (rows top to bottom) to equal the image it wrote."""
+encoded, both origins; HDR with flat and run-length scanlines — and requires the decoded RGBA8 (rows
+top to bottom) to equal the image it wrote (HDR: its tone mapping restated in numpy, within one level)."""
 import struct
 
 import numpy as np
@@ -158,6 +159,61 @@ def test_bmp_tga_malformed(R):
     good_bmp, good_tga = bmp(img, 24), tga(img, "rgb32", rle=True)
     bad = [good_bmp[:40], good_bmp[:-5], good_tga[:-3], good_bmp[:30] + struct.pack("<I", 1) + good_bmp[34:]]
     for data in bad:
+        with pytest.raises(R.ReinaError) as e:
+            R.decode_image(data)
+        assert e.value.code == R.REINA_ERR_IO
+
+
+def hdr_file(rgbe, rle):
+    H, W = rgbe.shape[:2]
+    out = b"#?RADIANCE\n# written by the test\nFORMAT=32-bit_rle_rgbe\n\n" + f"-Y {H} +X {W}\n".encode()
+    for y in range(H):
+        if not rle:
+            out += rgbe[y].tobytes()
+            continue
+        out += bytes([2, 2, W >> 8, W & 255])
+        for c in range(4):   # runs of >= 3 equal bytes as run codes, the rest as literals (<= 128 / 127)
+            ch = rgbe[y, :, c].tolist()
+            x = 0
+            while x < W:
+                r = 1
+                while x + r < W and ch[x + r] == ch[x] and r < 127:
+                    r += 1
+                if r >= 3:
+                    out += bytes([128 + r, ch[x]])
+                    x += r
+                    continue
+                lit = 1
+                while x + lit < W and lit < 128 and not (x + lit + 2 < W and ch[x + lit] == ch[x + lit + 1] == ch[x + lit + 2]):
+                    lit += 1
+                out += bytes([lit]) + bytes(ch[x:x + lit])
+                x += lit
+    return out
+
+
+@pytest.mark.parametrize("rle", [False, True])
+def test_hdr_rgbe(R, rle):
+    """Radiance RGBE read as an 8-bit texture the way stbi_load does (gamma 1/2.2, scale 1)."""
+    rng = np.random.default_rng(5 + rle)
+    H, W = 9, 40
+    rgbe = np.zeros((H, W, 4), np.uint8)
+    rgbe[..., :3] = rng.integers(0, 256, (H, W, 3))
+    rgbe[..., 3] = rng.integers(124, 140, (H, W))
+    rgbe[2, 5:30] = rgbe[2, 5]   # runs for the run-length scanlines
+    rgbe[4, :, 3] = 0            # exponent 0: black
+    got = R.decode_image(hdr_file(rgbe, rle))
+    f = rgbe[..., :3].astype(np.float32) * np.ldexp(np.float32(1), rgbe[..., 3:4].astype(np.int32) - 136).astype(np.float32)
+    want = np.clip(np.floor(np.power(f, np.float32(1 / 2.2)) * 255 + 0.5), 0, 255).astype(np.int64)
+    want[rgbe[..., 3] == 0] = 0
+    assert got.shape == (H, W, 4) and (got[..., 3] == 255).all()
+    d = np.abs(got[..., :3].astype(np.int64) - want)
+    assert d.max() <= 1 and (d == 0).mean() >= 0.99, (d.max(), (d == 0).mean())
+
+
+def test_hdr_malformed(R):
+    rgbe = np.full((3, 8, 4), 128, np.uint8)
+    good = hdr_file(rgbe, True)
+    for data in (good[:-4], good.replace(b"-Y 3 +X 8", b"+Y 3 +X 8"), good.replace(b"rle_rgbe", b"rle_xyze")):
         with pytest.raises(R.ReinaError) as e:
             R.decode_image(data)
         assert e.value.code == R.REINA_ERR_IO
