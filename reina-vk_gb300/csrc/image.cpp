@@ -1190,6 +1190,142 @@ Image decode_hdr(const uint8_t* d, size_t n) {
     return img;
 }
 
+// GIF (87a / 89a): the first image, placed on a canvas of the logical screen size that starts transparent
+// black; global or local colour table, the graphic-control transparent index, interlaced rows.  LZW codes
+// grow from min size + 1 bits to 12 as the table fills (clear and end codes as the format defines).
+Image decode_gif(const uint8_t* d, size_t n) {
+    if (n < 13 || (std::memcmp(d, "GIF87a", 6) != 0 && std::memcmp(d, "GIF89a", 6) != 0)) bad("GIF: bad signature");
+    const uint32_t W = le16(d + 6), H = le16(d + 8), flags = d[10];
+    if (W == 0 || H == 0) bad("GIF: bad size");
+    size_t p = 13;
+    std::vector<uint8_t> gct;
+    if (flags & 0x80) {
+        const size_t sz = 3u << ((flags & 7) + 1);
+        if (p + sz > n) bad("GIF: truncated colour table");
+        gct.assign(d + p, d + p + sz);
+        p += sz;
+    }
+    int transparent = -1;
+    for (;;) {
+        if (p >= n) bad("GIF: truncated");
+        const uint8_t b = d[p++];
+        if (b == 0x3B) bad("GIF: no image");
+        if (b == 0x21) {   // extension: graphic control keeps the transparent index; the rest is skipped
+            if (p >= n) bad("GIF: truncated extension");
+            const uint8_t label = d[p++];
+            bool first = true;
+            for (;;) {
+                if (p >= n) bad("GIF: truncated extension");
+                const uint8_t len = d[p++];
+                if (len == 0) break;
+                if (p + len > n) bad("GIF: truncated extension");
+                if (label == 0xF9 && first && len >= 4 && (d[p] & 1)) transparent = d[p + 3];
+                first = false;
+                p += len;
+            }
+            continue;
+        }
+        if (b != 0x2C) bad("GIF: unknown block");
+        if (p + 9 > n) bad("GIF: truncated image descriptor");
+        const uint32_t left = le16(d + p), top = le16(d + p + 2), iw = le16(d + p + 4), ih = le16(d + p + 6), f = d[p + 8];
+        p += 9;
+        std::vector<uint8_t> table = gct;
+        if (f & 0x80) {
+            const size_t sz = 3u << ((f & 7) + 1);
+            if (p + sz > n) bad("GIF: truncated colour table");
+            table.assign(d + p, d + p + sz);
+            p += sz;
+        }
+        if (table.empty()) bad("GIF: no colour table");
+        if (p >= n) bad("GIF: truncated image data");
+        const int min_size = d[p++];
+        if (min_size < 2 || min_size > 8) bad("GIF: bad LZW code size");
+        std::vector<uint8_t> lzw;   // the data sub-blocks joined
+        for (;;) {
+            if (p >= n) bad("GIF: truncated image data");
+            const uint8_t len = d[p++];
+            if (len == 0) break;
+            if (p + len > n) bad("GIF: truncated image data");
+            lzw.insert(lzw.end(), d + p, d + p + len);
+            p += len;
+        }
+        // LZW: table entries as (prefix code, last byte); strings are rebuilt back to front
+        const int clear = 1 << min_size, end = clear + 1;
+        std::vector<uint16_t> prefix(4096);
+        std::vector<uint8_t> suffix(4096), first_byte(4096), stack;
+        std::vector<uint16_t> length(4096);
+        for (int c = 0; c < clear; ++c) { prefix[c] = 0xFFFF; suffix[c] = first_byte[c] = (uint8_t)c; length[c] = 1; }
+        std::vector<uint8_t> idx;
+        idx.reserve((size_t)iw * ih);
+        int size = min_size + 1, next = end + 1, prev = -1;
+        size_t bitpos = 0;
+        const size_t total_bits = lzw.size() * 8;
+        while (idx.size() < (size_t)iw * ih) {
+            if (bitpos + (size_t)size > total_bits) break;   // short data: the rest stays transparent
+            int code = 0;
+            for (int k = 0; k < size; ++k, ++bitpos) code |= ((lzw[bitpos / 8] >> (bitpos % 8)) & 1) << k;
+            if (code == clear) {
+                size = min_size + 1;
+                next = end + 1;
+                prev = -1;
+                continue;
+            }
+            if (code == end) break;
+            if (prev < 0) {
+                if (code >= clear) bad("GIF: bad first code");
+                idx.push_back((uint8_t)code);
+                prev = code;
+                continue;
+            }
+            int out = code;
+            uint8_t fb;
+            if (code < next) {
+                fb = first_byte[code];
+            } else if (code == next) {   // the string being defined: previous string + its first byte
+                fb = first_byte[prev];
+            } else {
+                bad("GIF: bad LZW code");
+            }
+            if (next < 4096) {
+                prefix[next] = (uint16_t)prev;
+                suffix[next] = fb;
+                first_byte[next] = first_byte[prev];
+                length[next] = (uint16_t)(length[prev] + 1);
+                ++next;
+                if (next == (1 << size) && size < 12) ++size;
+            }
+            stack.clear();
+            for (int c = out; c != 0xFFFF; c = prefix[c]) stack.push_back(suffix[c]);
+            for (size_t k = stack.size(); k-- > 0;) idx.push_back(stack[k]);
+            prev = code;
+        }
+        Image img;
+        img.width = W;
+        img.height = H;
+        img.rgba.assign((size_t)W * H * 4, 0);
+        const bool interlaced = (f & 0x40) != 0;
+        std::vector<uint32_t> rows(ih);
+        if (interlaced) {
+            uint32_t r = 0;
+            for (const auto& pass : {std::make_pair(0u, 8u), std::make_pair(4u, 8u), std::make_pair(2u, 4u), std::make_pair(1u, 2u)})
+                for (uint32_t y = pass.first; y < ih; y += pass.second) rows[r++] = y;
+        } else {
+            for (uint32_t y = 0; y < ih; ++y) rows[y] = y;
+        }
+        for (size_t i = 0; i < idx.size() && i < (size_t)iw * ih; ++i) {
+            const uint32_t x = left + (uint32_t)(i % iw), y = top + rows[i / iw];
+            if (x >= W || y >= H || idx[i] == transparent) continue;
+            if ((size_t)idx[i] * 3 + 3 > table.size()) bad("GIF: colour index out of range");
+            uint8_t* o = &img.rgba[((size_t)y * W + x) * 4];
+            o[0] = table[idx[i] * 3u];
+            o[1] = table[idx[i] * 3u + 1];
+            o[2] = table[idx[i] * 3u + 2];
+            o[3] = 255;
+        }
+        return img;
+    }
+}
+
 }  // namespace
 
 Image decode_image(const uint8_t* data, size_t n) {
@@ -1199,8 +1335,9 @@ Image decode_image(const uint8_t* data, size_t n) {
     if (n >= 2 && data[0] == 'B' && data[1] == 'M') return decode_bmp(data, n);
     if (n >= 6 && (std::memcmp(data, "#?RADIANCE", std::min<size_t>(n, 10)) == 0 || std::memcmp(data, "#?RGBE", 6) == 0))
         return decode_hdr(data, n);
+    if (n >= 6 && (std::memcmp(data, "GIF87a", 6) == 0 || std::memcmp(data, "GIF89a", 6) == 0)) return decode_gif(data, n);
     if (looks_like_tga(data, n)) return decode_tga(data, n);   // TGA has no signature: a plausible header
-    bad("unknown image format (PNG, JPEG, BMP, TGA or HDR expected)");
+    bad("unknown image format (PNG, JPEG, BMP, GIF, TGA or HDR expected)");
 }
 
 void flip_rows(Image& img) {

@@ -30,8 +30,9 @@ std::vector<uint8_t> zlib_inflate(const uint8_t* data, size_t n, size_t limit);
 // 24 and 32 bits, either row order, uncompressed; a 32-bit alpha that is zero everywhere reads as opaque)
 // and TGA (colour-mapped, true-colour 15/16/24/32-bit and grey, raw or run-length encoded, either
 // origin), and Radiance RGBE (.hdr, flat or run-length scanlines) tone mapped as stbi_load does for 8-bit
-// output (255 x^(1/2.2) + 0.5).  Other formats (lossless, hierarchical or arithmetic-coded JPEG, RLE
-// bitmaps, GIF, ...) fail with REINA_ERR_IO.
+// output (255 x^(1/2.2) + 0.5), and GIF (the first image on a transparent canvas of the logical screen
+// size; transparency, interlacing, local tables).  Other formats (lossless, hierarchical or
+// arithmetic-coded JPEG, RLE bitmaps, ...) fail with REINA_ERR_IO.
 Image decode_image(const uint8_t* data, size_t n);
 
 // Reads and decodes a file; `flip_vertically` reverses the row order (stbi_set_flip_vertically_on_load,

@@ -1,8 +1,9 @@
-"""BMP, TGA and Radiance HDR texture decoding on the host (the formats stbi_load reads besides PNG and JPEG, behind
+"""BMP, TGA, GIF and Radiance HDR texture decoding on the host (the formats stbi_load reads besides PNG and JPEG, behind
 Scene::defineTexture, src/graphics/Image.cpp:10-41): the test writes seeded images in each layout itself
 — BMP with 1/4/8-bit palettes, 16-bit 5-5-5 and bit fields, 24-bit, 32-bit with and without alpha,
 bottom-up and top-down; TGA true-colour 16/24/32-bit, grey, colour-mapped, uncompressed and run-length
-encoded, both origins; HDR with flat and run-length scanlines — and requires the decoded RGBA8 (rows
+encoded, both origins; GIF through its own LZW encoder (growing code widths, a full table cleared,
+transparency, interlacing, local tables, an offset image); HDR with flat and run-length scanlines — and requires the decoded RGBA8 (rows
 top to bottom) to equal the image it wrote (HDR: its tone mapping restated in numpy, within one level)."""
 import struct
 
@@ -214,6 +215,102 @@ def test_hdr_malformed(R):
     rgbe = np.full((3, 8, 4), 128, np.uint8)
     good = hdr_file(rgbe, True)
     for data in (good[:-4], good.replace(b"-Y 3 +X 8", b"+Y 3 +X 8"), good.replace(b"rle_rgbe", b"rle_xyze")):
+        with pytest.raises(R.ReinaError) as e:
+            R.decode_image(data)
+        assert e.value.code == R.REINA_ERR_IO
+
+
+def lzw_gif(indices, min_size):
+    """GIF's LZW: codes of min_size + 1 bits growing to 12, a clear code first and when the table fills."""
+    clear, end = 1 << min_size, (1 << min_size) + 1
+    codes = [(clear, min_size + 1)]
+    size, nxt = min_size + 1, end + 1
+    table = {(i,): i for i in range(clear)}
+    w = ()
+    for k in indices:
+        wk = w + (int(k),)
+        if wk in table:
+            w = wk
+            continue
+        codes.append((table[w], size))
+        table[wk] = nxt
+        nxt += 1
+        if nxt - 1 == (1 << size) and size < 12:   # the decoder adds its entries one code later
+            size += 1
+        if nxt == 4096:
+            codes.append((clear, size))
+            table = {(i,): i for i in range(clear)}
+            size, nxt = min_size + 1, end + 1
+        w = (int(k),)
+    if w:
+        codes.append((table[w], size))
+    if nxt == (1 << size) and size < 12:
+        size += 1
+    codes.append((end, size))
+    acc, nbits, out = 0, 0, bytearray()
+    for c, s in codes:
+        acc |= c << nbits
+        nbits += s
+        while nbits >= 8:
+            out.append(acc & 255)
+            acc >>= 8
+            nbits -= 8
+    if nbits:
+        out.append(acc & 255)
+    return bytes(out)
+
+
+def gif_file(idx, palette, W, H, left=0, top=0, transparent=None, interlace=False, local=False):
+    ih, iw = idx.shape
+    bits = max(1, (len(palette) - 1).bit_length())
+    table = b"".join(bytes(c) for c in palette) + b"\0" * (3 * (1 << bits) - 3 * len(palette))
+    out = b"GIF89a" + struct.pack("<HHBBB", W, H, 0 if local else 0x80 | (bits - 1), 0, 0)
+    if not local:
+        out += table
+    if transparent is not None:
+        out += b"\x21\xf9\x04" + bytes([1, 0, 0, transparent, 0])
+    out += b"\x2c" + struct.pack("<HHHHB", left, top, iw, ih, (0x80 | (bits - 1) if local else 0) | (0x40 if interlace else 0))
+    if local:
+        out += table
+    rows = list(range(ih))
+    if interlace:
+        rows = list(range(0, ih, 8)) + list(range(4, ih, 8)) + list(range(2, ih, 4)) + list(range(1, ih, 2))
+    min_size = max(2, bits)
+    data = lzw_gif(idx[rows].reshape(-1), min_size)
+    out += bytes([min_size])
+    for k in range(0, len(data), 255):
+        out += bytes([len(data[k:k + 255])]) + data[k:k + 255]
+    return out + b"\x00\x3b"
+
+
+@pytest.mark.parametrize("case", range(5))
+def test_gif_first_frame(R, case):
+    W, H, ncol, left, top, transp, inter, local = [
+        (17, 13, 4, 0, 0, None, False, False),
+        (64, 40, 16, 3, 5, 2, False, True),
+        (33, 29, 4, 0, 0, None, True, False),
+        (90, 80, 256, 0, 0, 7, False, False),    # random colours: the code table fills and is cleared
+        (40, 40, 2, 4, 4, None, True, True),
+    ][case]
+    rng = np.random.default_rng(case)
+    palette = [tuple(int(c) for c in rng.integers(0, 256, 3)) for _ in range(ncol)]
+    iw, ih = W - left, H - top
+    idx = rng.integers(0, ncol, (ih, iw)).astype(np.uint8)
+    if ncol <= 16:   # runs, so that LZW strings repeat
+        idx[: ih // 2] = idx[0, 0]
+    got = R.decode_image(gif_file(idx, palette, W, H, left, top, transp, inter, local))
+    want = np.zeros((H, W, 4), np.uint8)
+    for y in range(ih):
+        for x in range(iw):
+            if idx[y, x] != transp:
+                want[top + y, left + x] = (*palette[idx[y, x]], 255)
+    assert np.array_equal(got, want)
+
+
+def test_gif_malformed(R):
+    idx = np.zeros((4, 4), np.uint8)
+    good = gif_file(idx, [(1, 2, 3), (4, 5, 6)], 4, 4)
+    for data in (good[:12], good[:-10], good.replace(b"\x2c", b"\x99", 1), b"GIF89a" + good[6:13] + b"\x3b"):
         with pytest.raises(R.ReinaError) as e:
             R.decode_image(data)
         assert e.value.code == R.REINA_ERR_IO
