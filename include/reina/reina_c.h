@@ -375,7 +375,10 @@ int reina_render_device(reina_ctx* ctx, const reina_scene* scene, const RtPushCo
  * passes the accumulation image (and, optionally, the per-sample buffer) as device memory.
  *   - width*height above REINA_NOALLOC_MAX_PIXELS is rejected with REINA_ERR_INVALID.
  *   - The first call on a device looks up the array's device address (cudaGetSymbolAddress) with that
- *     device current; make that first call before any stream capture.
+ *     device current; make that first call before any stream capture.  Under CUDA's default lazy module
+ *     loading, that first call (or the first call of any entry point that runs the pass-by-pass
+ *     wavefront) is also when the driver loads the library's module on the device and reserves the
+ *     array; set CUDA_MODULE_LOADING=EAGER to have it reserved when the context is created instead.
  *   - Every call uses the same array: calls whose work overlaps on the GPU (different streams, or
  *     different host threads) race and corrupt each other's images; serialize them. */
 enum { REINA_NOALLOC_MAX_PIXELS = 65536 };

@@ -559,14 +559,16 @@ inline int extend(int v, int t) { return t == 0 ? 0 : (v < (1 << (t - 1)) ? v - 
 // Separable 8x8 inverse DCT in double precision: f(x, y) = 1/4 sum C(u) C(v) F(u, v) cos((2x+1)u pi/16)
 // cos((2y+1)v pi/16) with C(0) = 1/sqrt(2), level-shifted by 128, rounded to nearest and clamped.
 void idct8x8(const double* F, uint8_t* out, int stride) {
-    static double cosv[8][8];
-    static bool init = false;
-    if (!init) {
-        for (int x = 0; x < 8; ++x)
-            for (int u = 0; u < 8; ++u)
-                cosv[x][u] = (u == 0 ? std::sqrt(0.5) : 1.0) * std::cos((2 * x + 1) * u * 3.14159265358979323846 / 16.0);
-        init = true;
-    }
+    struct Table {
+        double v[8][8];
+        Table() {
+            for (int x = 0; x < 8; ++x)
+                for (int u = 0; u < 8; ++u)
+                    v[x][u] = (u == 0 ? std::sqrt(0.5) : 1.0) * std::cos((2 * x + 1) * u * 3.14159265358979323846 / 16.0);
+        }
+    };
+    static const Table table;   // built once, thread-safely (a function-local static)
+    const auto& cosv = table.v;
     double tmp[64];
     for (int v = 0; v < 8; ++v)   // rows of F: inverse over u for every x
         for (int x = 0; x < 8; ++x) {
@@ -939,9 +941,10 @@ uint8_t masked(uint32_t v, uint32_t mask, uint8_t none) {
     while (((mask >> shift) & 1u) == 0) ++shift;
     const uint32_t m = mask >> shift;
     int bits = 0;
-    while ((m >> bits) & 1u) ++bits;
-    const uint32_t x = (v & mask) >> shift, top = (1u << bits) - 1u;
-    return (uint8_t)((x * 255u + top / 2) / top);
+    while (bits < 32 && ((m >> bits) & 1u)) ++bits;
+    // 64-bit arithmetic: a full 32-bit mask has top = 2^32 - 1 and x * 255 needs more than 32 bits
+    const uint64_t x = (v & mask) >> shift, top = bits >= 32 ? 0xFFFFFFFFull : (1ull << bits) - 1ull;
+    return (uint8_t)((x * 255ull + top / 2) / top);
 }
 
 // Windows / OS/2 bitmap: 1, 4, 8 (palette), 16 (5-5-5 or bit fields), 24 and 32 (BGRA or bit fields) bits
@@ -1075,6 +1078,8 @@ Image decode_tga(const uint8_t* d, size_t n) {
         p += cmap_len * eb;
     }
     const size_t pb = (depth + 7) / 8;
+    if ((uint64_t)w * h > (1ull << 28)) bad("TGA: too large (more than 2^28 pixels)");
+    if (!rle && p + (size_t)w * h * pb > n) bad("TGA: truncated pixel data");
     Image img;
     img.width = w;
     img.height = h;
@@ -1154,10 +1159,18 @@ Image decode_hdr(const uint8_t* d, size_t n) {
         const float z = std::pow(f, 1.0f / 2.2f) * 255.0f + 0.5f;
         return (uint8_t)(z < 0.0f ? 0.0f : (z > 255.0f ? 255.0f : z));
     };
+    // Run-length or flat is decided once, by the first scanline, as stbi_load decides it: widths outside
+    // [8, 32768) are always flat; otherwise the file is run-length encoded when the first scanline starts
+    // with 2, 2 and a length byte below 128.  A flat file is then read flat to the end (a later row that
+    // happens to start with those bytes is pixels), and in a run-length file every scanline must carry the
+    // header with the image's width (stbi_load fails on a wrong length and restarts its flat decoding from
+    // the first pixel on a missing header; both are rejected here).
+    const bool rle_file = W >= 8 && W < 32768 && p + 3 <= n && d[p] == 2 && d[p + 1] == 2 && (d[p + 2] & 0x80) == 0;
     for (int y = 0; y < H; ++y) {
-        const bool rle = W >= 8 && W < 32768 && p + 4 <= n && d[p] == 2 && d[p + 1] == 2 &&
-                         (((int)d[p + 2] << 8) | d[p + 3]) == W;
-        if (rle) {
+        if (rle_file) {
+            if (p + 4 > n) bad("HDR: truncated scanline");
+            if (d[p] != 2 || d[p + 1] != 2 || (d[p + 2] & 0x80) != 0) bad("HDR: scanline without a run-length header");
+            if ((((int)d[p + 2] << 8) | d[p + 3]) != W) bad("HDR: invalid decoded scanline length");
             p += 4;
             for (int c = 0; c < 4; ++c) {   // each channel of the scanline in turn
                 int x = 0;
@@ -1197,6 +1210,7 @@ Image decode_gif(const uint8_t* d, size_t n) {
     if (n < 13 || (std::memcmp(d, "GIF87a", 6) != 0 && std::memcmp(d, "GIF89a", 6) != 0)) bad("GIF: bad signature");
     const uint32_t W = le16(d + 6), H = le16(d + 8), flags = d[10];
     if (W == 0 || H == 0) bad("GIF: bad size");
+    if ((uint64_t)W * H > (1ull << 28)) bad("GIF: too large (more than 2^28 pixels)");
     size_t p = 13;
     std::vector<uint8_t> gct;
     if (flags & 0x80) {
@@ -1229,6 +1243,7 @@ Image decode_gif(const uint8_t* d, size_t n) {
         if (p + 9 > n) bad("GIF: truncated image descriptor");
         const uint32_t left = le16(d + p), top = le16(d + p + 2), iw = le16(d + p + 4), ih = le16(d + p + 6), f = d[p + 8];
         p += 9;
+        if ((uint64_t)iw * ih > (1ull << 28)) bad("GIF: image too large (more than 2^28 pixels)");
         std::vector<uint8_t> table = gct;
         if (f & 0x80) {
             const size_t sz = 3u << ((f & 7) + 1);

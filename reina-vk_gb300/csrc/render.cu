@@ -12,7 +12,9 @@
 
 #include <algorithm>
 #include <cstring>
+#include <map>
 #include <mutex>
+#include <tuple>
 #include <string>
 
 #include "kernels.h"
@@ -472,11 +474,24 @@ void RenderWorkspace::ensure(uint32_t paths) {
     capacity_ = paths;
 }
 
-static int occupancy_blocks(const void* fn, int sm_count) {
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kBlock, 0);
-    return std::max(1, per_sm) * std::max(1, sm_count);
+// Resident grid (blocks per SM x SMs) of a kernel at a block size, computed once per (kernel, block size,
+// SM count) and kept in a table that any thread rendering may read or fill (under a lock).
+static int cached_grid(const void* fn, int block, int sm_count) {
+    static std::mutex mu;
+    static std::map<std::tuple<const void*, int, int>, int> table;
+    const auto key = std::make_tuple(fn, block, sm_count);
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        const auto it = table.find(key);
+        if (it != table.end()) return it->second;
+    }
+    const int g = resident_grid(fn, block, sm_count);
+    std::lock_guard<std::mutex> lock(mu);
+    table[key] = g;
+    return g;
 }
+
+static int occupancy_blocks(const void* fn, int sm_count) { return cached_grid(fn, kBlock, sm_count); }
 
 // The frame's launch sequence over path state `ps` (at least width*height slots).
 static void launch_frame(const PathState& ps, const DeviceScene& s, const RtPushConsts& pc, const RenderOpts& opt,
@@ -497,29 +512,20 @@ static void launch_frame(const PathState& ps, const DeviceScene& s, const RtPush
     L.samples = d_samples;
     L.refill = opt.trace.refill;
 
-    static int g_ext = 0, g_sh = 0, g_shade[5] = {0, 0, 0, 0, 0}, g_simple = 0;
-    static int g_sm = -1;
-    if (g_sm != sm_count) {
-        g_ext = occupancy_blocks((const void*)k_extend, sm_count);
-        g_sh = occupancy_blocks((const void*)k_shadow, sm_count);
-        g_shade[1] = occupancy_blocks((const void*)k_shade<1>, sm_count);
-        g_shade[2] = occupancy_blocks((const void*)k_shade<2>, sm_count);
-        g_shade[3] = occupancy_blocks((const void*)k_shade<3>, sm_count);
-        g_shade[4] = occupancy_blocks((const void*)k_shade<4>, sm_count);
-        g_simple = occupancy_blocks((const void*)k_finish, sm_count);
-        g_sm = sm_count;
-    }
+    const int g_ext = occupancy_blocks((const void*)k_extend, sm_count);
+    const int g_sh = occupancy_blocks((const void*)k_shadow, sm_count);
+    const int g_shade[5] = {0, occupancy_blocks((const void*)k_shade<1>, sm_count),
+                            occupancy_blocks((const void*)k_shade<2>, sm_count),
+                            occupancy_blocks((const void*)k_shade<3>, sm_count),
+                            occupancy_blocks((const void*)k_shade<4>, sm_count)};
+    const int g_simple = occupancy_blocks((const void*)k_finish, sm_count);
     const int simple_blocks = (int)std::min<uint64_t>((P + kBlock - 1) / kBlock, (uint64_t)g_simple);
     uint32_t* cnt = L.ps.counters;
     check_cuda(cudaMemsetAsync(cnt, 0, kNumCounters * sizeof(uint32_t), st), "cudaMemsetAsync counters");
     const bool two = L.s.inst_trav != nullptr;
     if (opt.megakernel) {
-        static int g_mega[2] = {0, 0}, g_mega_sm = -1;
-        if (g_mega_sm != sm_count) {
-            g_mega[0] = occupancy_blocks((const void*)k_megakernel<false>, sm_count);
-            g_mega[1] = occupancy_blocks((const void*)k_megakernel<true>, sm_count);
-            g_mega_sm = sm_count;
-        }
+        const int g_mega[2] = {occupancy_blocks((const void*)k_megakernel<false>, sm_count),
+                               occupancy_blocks((const void*)k_megakernel<true>, sm_count)};
         const int blocks = (int)std::min<uint64_t>((P + kBlock - 1) / kBlock, (uint64_t)g_mega[two ? 1 : 0]);
         if (two) k_megakernel<true><<<blocks, kBlock, 0, st>>>(L);
         else k_megakernel<false><<<blocks, kBlock, 0, st>>>(L);
@@ -534,21 +540,13 @@ static void launch_frame(const PathState& ps, const DeviceScene& s, const RtPush
             check_cuda(cudaMemsetAsync(cnt + kCntQueue, 0, 6 * sizeof(uint32_t), st), "cudaMemsetAsync");
             check_cuda(cudaMemsetAsync(cnt + kCntFetchExtend, 0, 2 * sizeof(uint32_t), st), "cudaMemsetAsync");
             if (two) {   // two-level scenes: the default traversal variant
-                static int grid = 0, grid_sm = -1;
-                if (grid_sm != sm_count) {
-                    grid = resident_grid((const void*)k_extend_grid<kTraceBlock, kDefaultTraceStack, true>, kTraceBlock, sm_count);
-                    grid_sm = sm_count;
-                }
+                const int grid = cached_grid((const void*)k_extend_grid<kTraceBlock, kDefaultTraceStack, true>, kTraceBlock, sm_count);
                 k_extend_grid<kTraceBlock, kDefaultTraceStack, true><<<grid, kTraceBlock, 0, st>>>(L, cur);
             } else if (opt.trace.refill > 0) {
                 k_extend<<<g_ext, kBlock, 0, st>>>(L, cur);
             } else {
                 with_trace_variant(opt.trace, [&](auto B, auto S) {
-                    static int grid = 0, grid_sm = -1;
-                    if (grid_sm != sm_count) {
-                        grid = resident_grid((const void*)k_extend_grid<B.value, S.value, false>, B.value, sm_count);
-                        grid_sm = sm_count;
-                    }
+                    const int grid = cached_grid((const void*)k_extend_grid<B.value, S.value, false>, B.value, sm_count);
                     k_extend_grid<B.value, S.value, false><<<grid, B.value, 0, st>>>(L, cur);
                 });
             }
@@ -559,21 +557,13 @@ static void launch_frame(const PathState& ps, const DeviceScene& s, const RtPush
             k_shade<4><<<g_shade[4], kBlock, 0, st>>>(L, cur);
             if (opt.mode == kModeNeeMis) {
                 if (two) {
-                    static int grid = 0, grid_sm = -1;
-                    if (grid_sm != sm_count) {
-                        grid = resident_grid((const void*)k_shadow_grid<kTraceBlock, kDefaultTraceStack, true>, kTraceBlock, sm_count);
-                        grid_sm = sm_count;
-                    }
+                    const int grid = cached_grid((const void*)k_shadow_grid<kTraceBlock, kDefaultTraceStack, true>, kTraceBlock, sm_count);
                     k_shadow_grid<kTraceBlock, kDefaultTraceStack, true><<<grid, kTraceBlock, 0, st>>>(L);
                 } else if (opt.trace.refill > 0) {
                     k_shadow<<<g_sh, kBlock, 0, st>>>(L);
                 } else {
                     with_trace_variant(opt.trace, [&](auto B, auto S) {
-                        static int grid = 0, grid_sm = -1;
-                        if (grid_sm != sm_count) {
-                            grid = resident_grid((const void*)k_shadow_grid<B.value, S.value, false>, B.value, sm_count);
-                            grid_sm = sm_count;
-                        }
+                        const int grid = cached_grid((const void*)k_shadow_grid<B.value, S.value, false>, B.value, sm_count);
                         k_shadow_grid<B.value, S.value, false><<<grid, B.value, 0, st>>>(L);
                     });
                 }

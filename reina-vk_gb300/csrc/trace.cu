@@ -244,12 +244,11 @@ static void ray_order(const Ray* d_rays, uint64_t n, uint32_t* bin_of, uint32_t*
 
 template <bool ANY, bool COUNT>
 static int persistent_grid(int sm_count) {
-    static int per_sm = -1;
-    if (per_sm < 0) {
+    static const int per_sm = [] {   // initialised once, thread-safely (a function-local static)
         int b = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, raycast_kernel<ANY, COUNT>, kTraceBlock, 0);
-        per_sm = std::max(1, b);
-    }
+        return std::max(1, b);
+    }();
     return per_sm * std::max(1, sm_count);
 }
 

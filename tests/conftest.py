@@ -1,3 +1,4 @@
+import os
 import sys
 from pathlib import Path
 
@@ -8,6 +9,17 @@ PKG = ROOT / "reina-vk_gb300"
 for p in (str(ROOT), str(PKG)):
     if p not in sys.path:
         sys.path.insert(0, p)
+
+
+def reference_dir(sub: str = "") -> Path | None:
+    """A checkout of the reference (reina-vk) named by the REINA_REFERENCE_DIR environment variable, or None
+    when the variable is unset or the directory is absent; tests that read the reference's own files skip
+    then."""
+    env = os.environ.get("REINA_REFERENCE_DIR")
+    if not env:
+        return None
+    p = Path(env) / sub
+    return p if p.exists() else None
 
 
 def pytest_configure(config):

@@ -314,3 +314,55 @@ def test_gif_malformed(R):
         with pytest.raises(R.ReinaError) as e:
             R.decode_image(data)
         assert e.value.code == R.REINA_ERR_IO
+
+
+def test_oversized_headers_are_rejected_before_allocating(R):
+    """A few bytes that declare a 65535 x 65535 image (2^32 pixels, 17 GB as RGBA8) fail at once, before the
+    decoder reserves the canvas: the cap is 2^28 pixels, as for PNG, JPEG, BMP and HDR."""
+    big_gif = b"GIF89a" + struct.pack("<HHBBB", 0xFFFF, 0xFFFF, 0x80, 0, 0) + b"\0" * 6 + b"\x2c" + b"\0" * 9 + b"\x02\x00\x3b"
+    small_screen_big_frame = (b"GIF89a" + struct.pack("<HHBBB", 4, 4, 0x80, 0, 0) + b"\0" * 6 + b"\x2c" +
+                              struct.pack("<HHHHB", 0, 0, 0xFFFF, 0xFFFF, 0) + b"\x02\x00\x3b")
+    big_tga = struct.pack("<BBBHHBHHHHBB", 0, 0, 2, 0, 0, 0, 0, 0, 0xFFFF, 0xFFFF, 32, 0) + b"\0" * 8
+    big_tga_rle = struct.pack("<BBBHHBHHHHBB", 0, 0, 10, 0, 0, 0, 0, 0, 0xFFFF, 0xFFFF, 32, 0) + b"\0" * 8
+    short_tga = struct.pack("<BBBHHBHHHHBB", 0, 0, 2, 0, 0, 0, 0, 0, 100, 100, 32, 0) + b"\0" * 64
+    for data in (big_gif, small_screen_big_frame, big_tga, big_tga_rle, short_tga):
+        with pytest.raises(R.ReinaError) as e:
+            R.decode_image(data)
+        assert e.value.code == R.REINA_ERR_IO
+
+
+def test_hdr_mode_is_decided_by_the_first_scanline(R):
+    """A flat file whose later row starts with the bytes of a run-length header (2, 2, W >> 8, W & 255) reads
+    that row as pixels, as stbi_load does; a run-length file whose later scanline lacks the header fails."""
+    H, W = 3, 8
+    rgbe = np.full((H, W, 4), 130, np.uint8)
+    rgbe[1, 0] = (2, 2, 0, W)            # pixel bytes equal to a run-length header
+    rgbe[1, 1] = (200, 10, 10, 129)
+    got = R.decode_image(hdr_file(rgbe, False))
+    assert got.shape == (H, W, 4)
+    f = rgbe[..., :3].astype(np.float32) * np.ldexp(np.float32(1), rgbe[..., 3:4].astype(np.int32) - 136).astype(np.float32)
+    want = np.clip(np.floor(np.power(f, np.float32(1 / 2.2)) * 255 + 0.5), 0, 255).astype(np.int64)
+    assert np.abs(got[..., :3].astype(np.int64) - want).max() <= 1
+    rle = hdr_file(np.full((H, W, 4), 130, np.uint8), True)
+    head, body = rle.split(b"+X 8\n", 1)
+    rows = body.split(bytes([2, 2, 0, W]))[1:]
+    broken = head + b"+X 8\n" + bytes([2, 2, 0, W]) + rows[0] + bytes(rgbe[1].tobytes()) + bytes([2, 2, 0, W]) + rows[2]
+    with pytest.raises(R.ReinaError) as e:
+        R.decode_image(broken)
+    assert e.value.code == R.REINA_ERR_IO
+
+
+def test_bmp_full_width_bit_field(R):
+    """A 32-bit bit-field BMP whose red mask is all 32 bits: red scales from 32 bits (no shift by 32)."""
+    H, W = 2, 3
+    px = np.array([[0, 0xFFFFFFFF, 0x80000000], [0x7FFFFFFF, 1, 0xC0000000]], np.uint32)
+    data = px.astype("<u4").tobytes()
+    masks = struct.pack("<III", 0xFFFFFFFF, 0, 0)
+    offset = 14 + 40 + len(masks)
+    hdr = b"BM" + struct.pack("<IHHI", offset + len(data), 0, 0, offset)
+    dib = struct.pack("<IiiHHIIiiII", 40, W, -H, 1, 32, 3, len(data), 2835, 2835, 0, 0)
+    got = R.decode_image(hdr + dib + masks + data)
+    top = 0xFFFFFFFF
+    want_r = (px.astype(np.uint64) * 255 + top // 2) // top
+    assert np.array_equal(got[..., 0], want_r.astype(np.uint8))
+    assert (got[..., 1] == 0).all() and (got[..., 2] == 0).all()

@@ -12,8 +12,9 @@ from pathlib import Path
 
 import numpy as np
 import pytest
+from conftest import reference_dir
 
-REF_TEXTURES = Path("/root/reference/textures")
+REF_TEXTURES = reference_dir("textures")
 
 ZIGZAG = np.array([0, 1, 8, 16, 9, 2, 3, 10, 17, 24, 32, 25, 18, 11, 4, 5, 12, 19, 26, 33, 40, 48, 41, 34, 27, 20, 13,
                    6, 7, 14, 21, 28, 35, 42, 49, 56, 57, 50, 43, 36, 29, 22, 15, 23, 30, 37, 44, 51, 58, 59, 52, 45,
@@ -334,7 +335,7 @@ def test_jpeg_malformed_and_unsupported(R):
         assert e.value.code == R.REINA_ERR_IO
 
 
-@pytest.mark.skipif(not REF_TEXTURES.exists(), reason="reference texture files not present")
+@pytest.mark.skipif(REF_TEXTURES is None, reason="REINA_REFERENCE_DIR unset or without textures/")
 def test_jpeg_reference_textures(R):
     """The reference's JPEG textures decode; the tangent-space normal map points mostly along +z."""
     alb = R.decode_image((REF_TEXTURES / "qgdpH_2K_Albedo.jpg").read_bytes())

@@ -9,6 +9,7 @@ from pathlib import Path
 
 import numpy as np
 import pytest
+from conftest import reference_dir
 
 CUBE_OBJ = """# unit cube, quads, normals per face, uvs
 v -0.5 -0.5 -0.5
@@ -374,10 +375,10 @@ def test_gltf_textures(R, host_ctx, tmp_path):
         assert np.array_equal(s.export_texture(k), imgs[k])
 
 
-REF_MODELS = Path("/root/reference/models")
+REF_MODELS = reference_dir("models")
 
 
-@pytest.mark.skipif(not REF_MODELS.exists(), reason="reference model files not present")
+@pytest.mark.skipif(REF_MODELS is None, reason="REINA_REFERENCE_DIR unset or without models/")
 def test_reference_obj_models(R, host_ctx):
     """Every OBJ the reference ships loads as one model: polygons fanned into triangles, one TBN and UV per
     vertex when the file has UVs (Assimp's JoinIdenticalVertices / CalcTangentSpace / FlipUVs flags,

@@ -11,8 +11,9 @@ import numpy as np
 import pytest
 
 import scenes
+from conftest import reference_dir
 
-REF_TEXTURES = Path("/root/reference/textures")
+REF_TEXTURES = reference_dir("textures")
 
 CHANNELS = {0: 1, 2: 3, 3: 1, 4: 2, 6: 4}
 ADAM7 = [(0, 0, 8, 8), (4, 0, 8, 8), (0, 4, 4, 8), (2, 0, 4, 4), (0, 2, 2, 4), (1, 0, 2, 2), (0, 1, 1, 2)]
@@ -234,7 +235,7 @@ def numpy_png_decode(data: bytes) -> np.ndarray:
     return expected_rgba(samples, ctype, depth, pal, trns)
 
 
-@pytest.mark.skipif(not REF_TEXTURES.exists(), reason="reference texture files not present")
+@pytest.mark.skipif(REF_TEXTURES is None, reason="REINA_REFERENCE_DIR unset or without textures/")
 @pytest.mark.parametrize("name", ["toybox/diffuse.png", "toybox/parallax.png", "bricks2/normal.png",
                                   "cornell_texture.png", "brick_normal.png"])
 def test_png_reference_textures(R, name):

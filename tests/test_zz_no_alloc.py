@@ -15,14 +15,6 @@ import scenes
 
 pytestmark = pytest.mark.gpu
 
-RTOL = 1e-4
-
-
-def _agree(a, b):
-    a = np.asarray(a, np.float64)
-    b = np.asarray(b, np.float64)
-    return ((np.abs(a - b) <= RTOL * np.abs(b) + 1e-6) | (np.isnan(a) & np.isnan(b))).all(axis=-1)
-
 
 @pytest.mark.parametrize("mode,W,H", [(1, 256, 256), (0, 160, 96)])
 def test_noalloc_render_matches_regular_render_twice(R, gpu_ctx, mode, W, H):
@@ -44,17 +36,21 @@ def test_noalloc_render_matches_regular_render_twice(R, gpu_ctx, mode, W, H):
 
     outs = [(torch.full((H, W, 4), -7.0, dtype=torch.float32, device="cuda"),
              torch.full((W * H, spp, 3), -7.0, dtype=torch.float32, device="cuda")) for _ in range(2)]
+    # A first call loads the library's module on the device if nothing has yet (CUDA's lazy module loading),
+    # which reserves the fixed array; free memory is compared over the calls after it.
+    warm = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
+    R.render_device_noalloc(gpu_ctx, scene, pc, opts, warm.data_ptr(), 0, stream)
     torch.cuda.synchronize()
     free_before = torch.cuda.mem_get_info()[0]
     for acc, smp in outs:
         R.render_device_noalloc(gpu_ctx, scene, pc, opts, acc.data_ptr(), smp.data_ptr(), stream)
     torch.cuda.synchronize()
     assert torch.cuda.mem_get_info()[0] == free_before, "the allocation-free render changed free device memory"
+    # The pass-by-pass wavefront and the wave engine give bit-identical images, so equality is exact.
     for call, (acc, smp) in enumerate(outs):
         a, s = acc.cpu().numpy(), smp.cpu().numpy()
-        assert _agree(s, ref_smp).mean() >= 0.995, call
-        ok = np.abs(a - ref_acc) <= RTOL * np.abs(ref_acc) + 1e-6
-        assert ok.mean() >= 0.995, call
+        assert np.array_equal(s, ref_smp, equal_nan=True), call
+        assert np.array_equal(a, ref_acc, equal_nan=True), call
 
 
 def test_noalloc_render_rejects_images_above_its_limit(R, gpu_ctx):
