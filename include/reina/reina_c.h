@@ -650,8 +650,25 @@ int reina_write_png(const char* path, const uint8_t* rgba8, uint32_t width, uint
  *   REINA_KAT_GGX_VNDF    sampleGGXVNDF (brdfDisney.h.glsl:9-40): V = r[0..2], ax = r[6], ay = r[7], RNG
  *                         state = bits of r[8]; out[3] = the RNG state after the two draws (bits)
  *   REINA_KAT_EVAL_DISNEY evalDisney (brdfDisney.h.glsl:656-711): parameters in r[0..18], n r[19..21],
- *                         wi r[22..24], wo r[25..27], TBN columns r[28..36]; out = f, pdf */
-enum { REINA_KAT_OFFSET = 0, REINA_KAT_GGX_VNDF = 1, REINA_KAT_EVAL_DISNEY = 2 };
+ *                         wi r[22..24], wo r[25..27], TBN columns r[28..36]; out = f, pdf
+ *   REINA_KAT_RANDOM      random (shaderCommon.h.glsl:39-45): state = bits of r[0]; out = three draws and
+ *                         the state after (bits)
+ *   REINA_KAT_OFFSET_DIELECTRIC offsetPositionForDielectric (dielectric.rchit.glsl:14-38): p = r[0..2],
+ *                         n = r[3..5], ray direction r[6..8]
+ *   REINA_KAT_SAMPLE_DISNEY sampleDisney (brdfDisney.h.glsl:609-654): base r[0..2], anisotropic r[9],
+ *                         roughness r[10], clearcoatGloss r[12], metallic r[13], clearcoat r[14],
+ *                         specularTransmission r[15], eta r[17], n r[19..21], wi r[22..24], TBN columns
+ *                         r[28..36], state = bits of r[37]; out = the direction, the state after (bits)
+ *   REINA_KAT_SAMPLE_DISNEY_LOBE the same sample; out = didRefract, choseGlass (0 or 1)
+ *   REINA_KAT_DIFFUSE_REFLECTION diffuseReflection (closestHitCommon.h.glsl:215-222): n = r[0..2],
+ *                         state = bits of r[8]; out = the direction, the state after (bits)
+ *   REINA_KAT_RANDOM_UNIT_VEC randomUnitVec (closestHitCommon.h.glsl:195-205): state = bits of r[8];
+ *                         out = the vector, the state after (bits) */
+enum {
+    REINA_KAT_OFFSET = 0, REINA_KAT_GGX_VNDF = 1, REINA_KAT_EVAL_DISNEY = 2, REINA_KAT_RANDOM = 3,
+    REINA_KAT_OFFSET_DIELECTRIC = 4, REINA_KAT_SAMPLE_DISNEY = 5, REINA_KAT_DIFFUSE_REFLECTION = 6,
+    REINA_KAT_RANDOM_UNIT_VEC = 7, REINA_KAT_SAMPLE_DISNEY_LOBE = 15
+};
 int reina_device_kat(reina_ctx* ctx, int kind, const float* records, uint64_t count, float* out);
 
 /* ------------------------------------------------------------------------------------------------ */

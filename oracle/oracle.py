@@ -144,7 +144,9 @@ def bvh8_two_level_raycast(nodes, tris, refs, inst_records, rays, any_hit: bool 
 
 
 _SHADING_SIGS["oracle_kat"] = (None, [C.c_int, C.c_void_p, C.c_uint64, C.c_int, C.c_void_p])
-KAT_OFFSET, KAT_GGX_VNDF, KAT_EVAL_DISNEY = 0, 1, 2
+_SHADING_SIGS["oracle_kat8"] = (None, [C.c_int, C.c_void_p, C.c_uint64, C.c_int, C.c_void_p])
+KAT_OFFSET, KAT_GGX_VNDF, KAT_EVAL_DISNEY, KAT_RANDOM, KAT_OFFSET_DIELECTRIC, KAT_SAMPLE_DISNEY = 0, 1, 2, 3, 4, 5
+KAT_DIFFUSE_REFLECTION, KAT_RANDOM_UNIT_VEC, KAT_REFLECTANCE, KAT_PDFS = 6, 7, 10, 14
 
 
 def kat(kind: int, records: np.ndarray, precision: int = 32) -> np.ndarray:
@@ -152,6 +154,14 @@ def kat(kind: int, records: np.ndarray, precision: int = 32) -> np.ndarray:
     r = np.ascontiguousarray(records, np.float32).reshape(-1, 40)
     out = np.zeros((r.shape[0], 4), np.float64)
     lib().oracle_kat(kind, _p(r), r.shape[0], precision, _p(out))
+    return out
+
+
+def kat8(kind: int, records: np.ndarray, precision: int = 32) -> np.ndarray:
+    """The same on 8 outputs per case (see oracle_kat.cpp): (n, 8) float64."""
+    r = np.ascontiguousarray(records, np.float32).reshape(-1, 40)
+    out = np.zeros((r.shape[0], 8), np.float64)
+    lib().oracle_kat8(kind, _p(r), r.shape[0], precision, _p(out))
     return out
 
 

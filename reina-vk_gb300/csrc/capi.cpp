@@ -1287,7 +1287,8 @@ int reina_scene_define_texture_encoded(reina_scene* scene, const void* data, uin
 int reina_device_kat(reina_ctx* ctx, int kind, const float* records, uint64_t count, float* out) {
     return guard([&] {
         need(ctx != nullptr, "ctx is NULL");
-        need(kind >= REINA_KAT_OFFSET && kind <= REINA_KAT_EVAL_DISNEY, "unknown kind");
+        need((kind >= REINA_KAT_OFFSET && kind <= REINA_KAT_RANDOM_UNIT_VEC) || kind == REINA_KAT_SAMPLE_DISNEY_LOBE,
+             "unknown kind");
         need(count == 0 || (records && out), "NULL buffer");
         need(count < (1ull << 24), "at most 2^24 cases per call");
         use_device(ctx);

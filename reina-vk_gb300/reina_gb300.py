@@ -961,7 +961,8 @@ class SaveSchedule:
             pass
 
 
-KAT_OFFSET, KAT_GGX_VNDF, KAT_EVAL_DISNEY = 0, 1, 2
+KAT_OFFSET, KAT_GGX_VNDF, KAT_EVAL_DISNEY, KAT_RANDOM, KAT_OFFSET_DIELECTRIC, KAT_SAMPLE_DISNEY = 0, 1, 2, 3, 4, 5
+KAT_DIFFUSE_REFLECTION, KAT_RANDOM_UNIT_VEC, KAT_SAMPLE_DISNEY_LOBE = 6, 7, 15
 
 
 def device_kat(ctx: "Context", kind: int, records: np.ndarray) -> np.ndarray:
