@@ -336,7 +336,12 @@ def run_ours(args) -> dict | None:
         pool, setup_s = build_pool(R, ctx, args.batch_scenes)
         out["batched"] = batch_metrics(R, ctx, torch, pool, setup_s, args.batch_mega_scenes)
         if args.serve_seconds > 0:
-            out["served"] = serve_metrics(R, ctx, torch, pool, args.serve_seconds, args.serve_rate)
+            out["served"] = serve_metrics(R, ctx, torch, pool, args.serve_seconds, args.serve_rate,
+                                          all_policies=args.serve_all_policies)
+        if args.serve_budget_seconds > 0:
+            out["served_budget_bound"] = served_budget_bound(R, ctx, torch, args)
+    if args.rmse_spp > 0:
+        out["rmse_vs_fp64_4096spp"] = rmse_metrics(R, ctx, args.rmse_spp)
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(tris, rays, args.cpu_sample)
     return out
@@ -377,6 +382,8 @@ def render_metrics(R, ctx, torch, frames: int, scene_large) -> dict:
         out[f"large_{name}"] = {"s_per_frame": dt, "segments_per_s": st["rays"] / dt,
                                 "rays_per_s": (st["rays"] + st["shadow_rays"]) / dt,
                                 "segments_per_frame": st["rays"], "shadow_rays_per_frame": st["shadow_rays"]}
+        if st["nodes_visited"]:
+            out[f"large_{name}"]["roofline"] = segment_roofline(st, dt)
     d = scenes.cornell(R)
     sc = d.to_product(R, ctx)
     iv, ip = scenes.cornell_camera(R, 256, 256)
@@ -390,6 +397,33 @@ def render_metrics(R, ctx, torch, frames: int, scene_large) -> dict:
                                   "segments_per_s": st["rays"] / dt,
                                   "rays_per_s": (st["rays"] + st["shadow_rays"]) / dt}
     return out
+
+
+# Algorithmic bytes of the wavefront kernels (per unit; the SoA records of render.cu / batch.cu):
+#   extension, per path segment: the ray read (24 B), the queue entry read and the shade-queue entry
+#     written (8 B), the hit written (12 B), plus 80 B per BVH8 node visited and 48 B per triangle tested;
+#   shadow ray: its 44-byte record, plus 80 B per node and 48 B per triangle;
+#   shaded hit: the path state read and written (~76 B), three vertices' index, position, TBN and TBN
+#     index (3 x 60 B) and the InstanceProperties record (120 B) = 376 B; a miss-shaded segment 28 B.
+SEG_BYTES, SHADOW_REC_BYTES, SHADE_BYTES, MISS_BYTES = 44, 44, 376, 28
+
+
+def segment_roofline(st: dict, seconds: float) -> dict:
+    """Algorithmic bytes of one frame's wavefront kernels (counted by the cooperative kernels) over the
+    frame time, against the measured HBM copy peak."""
+    peak, kind = _peak_hbm()
+    ext = st["rays"] * SEG_BYTES + NODE_BYTES * st["nodes_visited"] + TRI_BYTES * st["triangles_tested"]
+    sha = st["shadow_rays"] * SHADOW_REC_BYTES + NODE_BYTES * st["shadow_nodes_visited"] + TRI_BYTES * st["shadow_triangles_tested"]
+    shade = st["shaded_hits"] * SHADE_BYTES + (st["rays"] - st["shaded_hits"]) * MISS_BYTES
+    total = ext + sha + shade
+    achieved = total / seconds / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "peak_source": kind, "unit": "GB/s",
+            "frac": achieved / peak, "bytes_per_frame": total, "extension_bytes": ext, "shadow_bytes": sha,
+            "shade_bytes": shade, "nodes_per_segment": st["nodes_visited"] / max(1, st["rays"]),
+            "tris_per_segment": st["triangles_tested"] / max(1, st["rays"]),
+            "nodes_per_shadow_ray": st["shadow_nodes_visited"] / max(1, st["shadow_rays"]),
+            "tris_per_shadow_ray": st["shadow_triangles_tested"] / max(1, st["shadow_rays"]),
+            "algorithmic_bytes_per_segment": total / max(1, st["rays"])}
 
 
 def emissive_metrics(R, ctx) -> dict:
@@ -573,12 +607,15 @@ def batch_metrics(R, ctx, torch, built, setup_s: float, mega_scenes: int) -> dic
     return out
 
 
-def serve_metrics(R, ctx, torch, pool, seconds: float, rate: float) -> dict:
+def serve_metrics(R, ctx, torch, pool, seconds: float, rate: float, all_policies: bool = False,
+                  budget_bytes: int = 120_000_000_000, plain: bool = True) -> dict:
     """The served workload: a seeded Poisson stream of requests (rate per second over `seconds`), each a
     scene of the pool with side/spp/depth drawn like the batched workload, submitted in real time (a)
-    one request at a time to reina_render_device in arrival order (the plain form) and (b) to the
-    request server (120 GB admission budget, continuous batching).  Latency is arrival -> image on the
-    host; throughput is requests and rays over first arrival -> last completion."""
+    one request at a time to reina_render_device in arrival order (the plain form: the frame on the wave
+    engine; with `all_policies` also pass by pass) and (b) to the request server (admission budget
+    `budget_bytes`, continuous batching; shortest remaining work first, and with `all_policies` also
+    first-come and fair share).  Latency is arrival -> image on the host; throughput is requests and rays
+    over first arrival -> last completion.  The scenes are handed to the (first) server."""
     import scenes
 
     rng = np.random.default_rng(2026)
@@ -629,14 +666,14 @@ def serve_metrics(R, ctx, torch, pool, seconds: float, rate: float) -> dict:
         return {"p50_s": p50, "p99_s": p99, "mean_s": float(np.mean(lat)), "renders_per_s": n / span,
                 "samples_per_s": samples / span, "span_s": span}
 
-    plain = one_at_a_time(False)
-    plain_pbp = one_at_a_time(True)
+    plain_one = one_at_a_time(False) if plain else None
+    plain_pbp = one_at_a_time(True) if (plain and all_policies) else None
 
     # (b) served: the same stream through a request server, once per wave-slot policy (the scenes are
     # handed to the first server and stay with it; the other policies run on servers of their own over
     # fresh copies)
     def serve(policy: str, scenes_pool) -> tuple[dict, bool]:
-        srv = R.Server(ctx, budget_bytes=120_000_000_000, fifo=policy == "fifo", fair=policy == "fair")
+        srv = R.Server(ctx, budget_bytes=budget_bytes, fifo=policy == "fifo", fair=policy == "fair")
         ids = [srv.add_scene(s) for s, _ in scenes_pool]
         outs = [np.zeros((r[3].height, r[3].width, 4), np.float32) for r in reqs]
         rids = [None] * n
@@ -663,18 +700,64 @@ def serve_metrics(R, ctx, torch, pool, seconds: float, rate: float) -> dict:
                  "segments_per_s": st["rays"] / span, "rays_per_s": (st["rays"] + st["shadow_rays"]) / span,
                  "span_s": span, "completed": st["completed"], "failed": st["failed"], "waves": st["waves"],
                  "scene_uploads": st["scene_uploads"], "scene_evictions": st["scene_evictions"],
-                 "peak_resident_gb": st["peak_resident_bytes"] / 1e9}, all(s == R.REQ_DONE for s in states))
+                 "peak_resident_gb": st["peak_resident_bytes"] / 1e9, "budget_gb": st["budget_bytes"] / 1e9,
+                 "reserved_gb": st["reserved_bytes"] / 1e9}, all(s == R.REQ_DONE for s in states))
 
-    served, ok1 = serve("shortest", pool)   # the server's default policy (shortest first, aging 0.03)
-    served_fifo, ok2 = serve("fifo", [scenes.batch_scene(R, ctx, k) for k in range(len(pool))])
-    served_fair, ok3 = serve("fair", [scenes.batch_scene(R, ctx, k) for k in range(len(pool))])
-    return {"workload": f"Poisson {rate:g}/s for {seconds:g} s ({n} requests) over the {len(pool)}-scene pool, "
-                        "side U[128,1024], spp U{1..64}, depth U{4..12}, NEE+MIS; 120 GB admission budget",
-            "requests": n, "samples_total": int(samples), "all_done": ok1 and ok2 and ok3,
-            "plain_pass_by_pass_one_at_a_time": plain_pbp, "wave_engine_one_at_a_time": plain,
-            "served": served, "served_fifo": served_fifo, "served_fair_share": served_fair,
-            "renders_per_s_ratio_vs_plain_pass_by_pass": served["renders_per_s"] / plain_pbp["renders_per_s"],
-            "renders_per_s_ratio_vs_wave_engine_one_at_a_time": served["renders_per_s"] / plain["renders_per_s"]}
+    served, ok = serve("shortest", pool)   # the server's default policy (shortest first, aging 0.03)
+    out = {"workload": f"Poisson {rate:g}/s for {seconds:g} s ({n} requests) over the {len(pool)}-scene pool, "
+                       f"side U[128,1024], spp U{{1..64}}, depth U{{4..12}}, NEE+MIS; "
+                       f"{budget_bytes / 1e9:g} GB admission budget",
+           "requests": n, "samples_total": int(samples), "served": served}
+    if plain_one is not None:
+        out["wave_engine_one_at_a_time"] = plain_one
+        out["renders_per_s_ratio_vs_wave_engine_one_at_a_time"] = served["renders_per_s"] / plain_one["renders_per_s"]
+    if all_policies:
+        served_fifo, ok2 = serve("fifo", [scenes.batch_scene(R, ctx, k) for k in range(len(pool))])
+        served_fair, ok3 = serve("fair", [scenes.batch_scene(R, ctx, k) for k in range(len(pool))])
+        ok = ok and ok2 and ok3
+        out.update({"served_fifo": served_fifo, "served_fair_share": served_fair})
+        if plain_pbp is not None:
+            out["plain_pass_by_pass_one_at_a_time"] = plain_pbp
+            out["renders_per_s_ratio_vs_plain_pass_by_pass"] = served["renders_per_s"] / plain_pbp["renders_per_s"]
+    out["all_done"] = ok
+    return out
+
+
+def served_budget_bound(R, ctx, torch, args) -> dict:
+    """The served workload under an admission budget smaller than what its scenes occupy on the device: a
+    pool of `--serve-budget-scenes` fresh scenes of the batched distribution, budget = the waves' reserved
+    path state + half of the pool's scene bytes, so that least-recently-used idle scenes must be evicted
+    (and uploaded again on demand) while the stream runs."""
+    import scenes
+
+    pool = [scenes.batch_scene(R, ctx, k) for k in range(args.serve_budget_scenes)]
+    scene_bytes = sum(int(sc.stats()["device_bytes"]) for sc, _ in pool)
+    probe = R.Server(ctx, budget_bytes=120_000_000_000)
+    reserved = int(probe.stats()["reserved_bytes"])
+    probe.close()
+    budget = reserved + scene_bytes // 2
+    out = serve_metrics(R, ctx, torch, pool, args.serve_budget_seconds, args.serve_rate, budget_bytes=budget,
+                        plain=False)
+    out["pool_scene_gb"] = scene_bytes / 1e9
+    return out
+
+
+def rmse_metrics(R, ctx, spp: int) -> dict:
+    """Converged-image error of the GPU against the FP64 oracle at `spp` samples per pixel (NEE+MIS) on the
+    same per-pixel sample streams, per workload (tests/converged.py): the Cornell room (C0), three 32x32
+    windows of the 1.3M-triangle scene at 1920x1080 (C2), one scene of the batched workload rendered
+    through the batched entry point (C3).  Value per workload: the largest window RMSE / window mean."""
+    import converged
+    from oracle import oracle as O
+
+    out = {}
+    for key, name in (("C0_cornell_256", "cornell_256"), ("C2_large_1920x1080_windows", "large_1920x1080"),
+                      ("C3_batch_scene", "batch_scene_3")):
+        res = converged.converged_rmse(R, O, ctx, name, spp=spp)
+        out[key] = max(res["rmse"])
+        out[key + "_detail"] = res
+    out["spp"] = spp
+    return out
 
 
 def cpu_baseline(tris, rays, sample: int) -> dict:
@@ -757,9 +840,15 @@ def main() -> int:
                     help="scenes of the batched-render metrics (0 skips them)")
     ap.add_argument("--batch-mega-scenes", type=int, default=32,
                     help="leading scenes also rendered one at a time by the plain megakernel")
-    ap.add_argument("--serve-seconds", type=float, default=4.0,
+    ap.add_argument("--serve-seconds", type=float, default=120.0,
                     help="arrival window of the served workload (0 skips it; 120 is the full stream)")
     ap.add_argument("--serve-rate", type=float, default=50.0, help="Poisson arrival rate (requests/s)")
+    ap.add_argument("--serve-all-policies", action="store_true",
+                    help="also serve with first-come and fair-share wave slots, and pass by pass one at a time")
+    ap.add_argument("--serve-budget-seconds", type=float, default=30.0,
+                    help="seconds of the stream served under a binding memory budget (0: skip)")
+    ap.add_argument("--serve-budget-scenes", type=int, default=64)
+    ap.add_argument("--rmse-spp", type=int, default=4096, help="converged-image RMSE vs the FP64 oracle (0: skip)")
     ap.add_argument("--instances", type=int, default=256,
                     help="instances of the flat vs two-level instancing metrics (0 skips them)")
     args = ap.parse_args()

@@ -67,13 +67,18 @@ int reina_ctx_sm_count(const reina_ctx* ctx);
 /* Launch parameters of the traversal kernels and of batched renders (no counterpart in the reference,
  * whose traversal and scheduling belong to the Vulkan implementation).  Every setting gives the same results; only speed
  * differs.  0 selects the default of a field.
- *   refill = 0: one thread per ray (grid form, the default); refill = 1..32: persistent warps that fetch
- *            new rays when `refill` of their 32 lanes are idle (block 128, stack 12).
+ *   refill: the traversal launch form.  1..32 (0 = the default, 8): the warp-cooperative persistent form
+ *            (flat scenes; block 128, stack 12): warps keep 32 rays in flight, take new rays once `refill`
+ *            of their lanes are idle, and share each step's triangle tests and the finished rays' hit
+ *            refinement over all 32 lanes; REINA_REFILL_GRID: one thread per ray (the grid form, the
+ *            only form of two-level scenes, which use it whatever this field says).  On the
+ *            1.3M-triangle ray cast (2,097,152 rays) closest hit 0.58 ms cooperative against 0.82 ms
+ *            grid, any hit 0.36 against 0.51 ms.
  *   trace_block: threads per block of the grid-form traversal kernels (ray cast, wavefront extend and
- *            shadow): 64, 128 or 256 (default 128).
+ *            shadow): 64, 128 or 256 (default 128).  Grid form only.
  *   trace_stack: shared-memory traversal stack entries per thread, 8, 12 or 16 (default 12); deeper
  *            levels spill to local memory.
- *   trace_order: the order a ray cast traces its rays in (below).
+ *   trace_order: the order a grid-form ray cast traces its rays in (below).
  *   wave_paths: path slots of one wave of a batched render or frame (0 = REINA_DEFAULT_WAVE_PATHS);
  *            the path state costs 164 bytes per slot and wave in flight (wave_lanes): the waves run on
  *            streams of their own, so that one wave's last bounces (few long paths) overlap the next
@@ -87,8 +92,8 @@ int reina_ctx_sm_count(const reina_ctx* ctx);
  *            stays in L2 (on a 256-scene batch 9.06 s against 9.40 s for an equal share per job);
  *            REINA_BATCH_FAIR_SHARE gives every unfinished job an equal share of each wave instead.
  *            Neither changes an image.
- * Changing wave_paths, batch_flags, trace_block or trace_stack releases the batch engine; the next
- * batched call rebuilds it. */
+ * Changing wave_paths, batch_flags, refill, trace_block or trace_stack releases the batch engine; the
+ * next batched call rebuilds it. */
 typedef struct reina_tuning {
     uint32_t refill;
     uint32_t wave_paths;
@@ -107,6 +112,7 @@ typedef struct reina_tuning {
  * ray sets (on the 1.3M-triangle workload: random half 0.513 vs 0.525 ms, camera half 0.49 vs 0.46 ms);
  * the autotuner tries both. */
 enum { REINA_ORDER_INPUT = 0, REINA_ORDER_COHERENT = 1 };
+enum { REINA_REFILL_GRID = 255 };
 /* Waves of 2^21 slots, 8 in flight (2.75 GB of path state).  Every wave ends in a tail of a few long
  * paths at low occupancy (late bounces are latency-bound chains of node fetches), which the other waves
  * in flight fill.  On a 256-scene batch (3.1 G paths): one wave in flight 12.94 s at 2^21 slots and
@@ -343,12 +349,21 @@ enum {
  * flight on their own streams (tuning.wave_lanes), each replayed from a CUDA graph — on the 1920x1080,
  * 64 spp, 12-bounce frame 0.32 s against 0.59 s pass by pass.  The three forms give the same images. */
 /* The grid-form traversal variant of a frame comes from the render autotune cache (REINA_AUTOTUNE_CACHED)
- * or the context's tuning; the persistent form (tuning.refill > 0) applies to the pass-by-pass form only. */
+ * or the context's tuning; the cooperative form (the default) runs the extension and shadow kernels of
+ * both the wave engine and the pass-by-pass form for flat scenes. */
 
 typedef struct reina_render_stats {
     uint64_t rays;               /* closest-hit rays traced (path segments) */
     uint64_t shadow_rays;        /* any-hit shadow rays traced */
     double seconds;              /* wall time of the call */
+    /* traversal work of the cooperative extension and shadow kernels (flat scenes; 0 where a frame ran the
+     * grid form or the megakernel): BVH8 nodes visited and triangles tested by the path segments and by
+     * the shadow rays, and the hits shaded by a material kernel */
+    uint64_t nodes_visited;
+    uint64_t triangles_tested;
+    uint64_t shadow_nodes_visited;
+    uint64_t shadow_triangles_tested;
+    uint64_t shaded_hits;
 } reina_render_stats;
 
 /* One frame of the wavefront path tracer: push_consts->samplesPerPixel samples per pixel, at most
@@ -364,6 +379,16 @@ int reina_render(reina_ctx* ctx, const reina_scene* scene, const RtPushConsts* p
 int reina_render_device(reina_ctx* ctx, const reina_scene* scene, const RtPushConsts* push_consts,
                         const reina_render_options* options, void* d_accum_rgba32f, void* d_samples_rgb32f,
                         void* stream);
+
+/* Device error flags of the asynchronous entry points (reina_raycast_device, reina_render_device,
+ * reina_render_device_noalloc).  Their kernels never trap: a traversal that overflows its stack (bit 1)
+ * or runs past the traversal step limit (bit 2), or — in the checked build — an out-of-range queue index
+ * (bit 4), sets a bit in the context's device error word and the ray or path ends.  This call orders a
+ * read of that word after the work queued on `stream`, waits for it, writes the bits to *out_flags
+ * (optional), clears the word and returns REINA_ERR_DEVICE if any bit was set.  The synchronous entry
+ * points check the word themselves and fail with REINA_ERR_DEVICE.  Reference: the run loop's errors
+ * surface as exceptions caught in main (src/main.cpp:11-14). */
+int reina_ctx_device_error(reina_ctx* ctx, void* stream, uint32_t* out_flags);
 
 /* Allocation-free render.  No counterpart in the reference: this entry point exists for callers that
  * cannot call cudaMalloc while they run — a host whose allocator owns all device memory and gives none

@@ -91,35 +91,52 @@ def build(force: bool = False, ptxas_verbose: bool = False, verbose: bool = Fals
 
 OUT_CHECKED = PKG / "_build_checked"
 LIB_CHECKED = OUT_CHECKED / "libreina_gb300.so"
+OUT_WATCHDOG = PKG / "_build_watchdog"
+LIB_WATCHDOG = OUT_WATCHDOG / "libreina_gb300.so"
+WATCHDOG_STEPS = 2
 
 
-def build_checked(force: bool = False) -> Path:
-    """The checked build: every CUDA source again with -DRT_CHECKED (the wavefront kernels check each queue
-    position and path index and flag, instead of making, an out-of-bounds access), linked with the host
-    objects of the normal build into `_build_checked/libreina_gb300.so`.  Not part of build()."""
+def _build_variant(out_dir: Path, defines: list[str], force: bool) -> Path:
+    """Every CUDA source again with `defines`, linked with the host objects of the normal build into
+    `out_dir/libreina_gb300.so`."""
     build()
-    OUT_CHECKED.mkdir(exist_ok=True)
+    lib = out_dir / "libreina_gb300.so"
+    out_dir.mkdir(exist_ok=True)
     newest_header = max((h.stat().st_mtime for h in _headers()), default=0.0)
     objs, jobs = [], []
     for src in sorted(list(CSRC.glob("*.cu")) + list(CSRC.glob("*.cpp"))):
         if src.suffix != ".cu":
             objs.append(OUT / (src.name + ".o"))
             continue
-        obj = OUT_CHECKED / (src.name + ".o")
+        obj = out_dir / (src.name + ".o")
         objs.append(obj)
         if force or _stale(obj, src, newest_header):
-            jobs.append([NVCC, *ARCH, *NVCCFLAGS, "-DRT_CHECKED", *INCLUDES, "-c", str(src), "-o", str(obj)])
+            jobs.append([NVCC, *ARCH, *NVCCFLAGS, *defines, *INCLUDES, "-c", str(src), "-o", str(obj)])
     if jobs:
         with cf.ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
             for res in ex.map(lambda c: subprocess.run(c, capture_output=True, text=True), jobs):
                 if res.returncode != 0:
-                    raise RuntimeError(f"checked build failed:\n{res.stdout}\n{res.stderr}")
-    if force or jobs or not LIB_CHECKED.exists() or any(LIB_CHECKED.stat().st_mtime < o.stat().st_mtime for o in objs):
-        cmd = [NVCC, *ARCH, "-shared", "-o", str(LIB_CHECKED), *map(str, objs), "-lpthread", "-ldl", "-lrt"]
+                    raise RuntimeError(f"variant build failed:\n{res.stdout}\n{res.stderr}")
+    if force or jobs or not lib.exists() or any(lib.stat().st_mtime < o.stat().st_mtime for o in objs):
+        cmd = [NVCC, *ARCH, "-shared", "-o", str(lib), *map(str, objs), "-lpthread", "-ldl", "-lrt"]
         res = subprocess.run(cmd, capture_output=True, text=True)
         if res.returncode != 0:
-            raise RuntimeError(f"checked link failed: {' '.join(cmd)}\n{res.stdout}\n{res.stderr}")
-    return LIB_CHECKED
+            raise RuntimeError(f"variant link failed: {' '.join(cmd)}\n{res.stdout}\n{res.stderr}")
+    return lib
+
+
+def build_checked(force: bool = False) -> Path:
+    """The checked build: every CUDA source again with -DRT_CHECKED (the wavefront kernels check each queue
+    position and path index and flag, instead of making, an out-of-bounds access), linked with the host
+    objects of the normal build into `_build_checked/libreina_gb300.so`.  Not part of build()."""
+    return _build_variant(OUT_CHECKED, ["-DRT_CHECKED"], force)
+
+
+def build_watchdog(force: bool = False) -> Path:
+    """The watchdog build: the traversal step limit lowered to WATCHDOG_STEPS, so that ordinary rays run
+    past it and the device error path (flag set, ray ended, REINA_ERR_DEVICE at the C ABI) can be tested
+    without a faulty scene.  `_build_watchdog/libreina_gb300.so`; not part of build()."""
+    return _build_variant(OUT_WATCHDOG, [f"-DRT_MAX_TRAVERSAL_STEPS={WATCHDOG_STEPS}"], force)
 
 
 CLI_SRC = PKG / "cli" / "reina_render.cpp"

@@ -84,7 +84,7 @@ void TuneCache::load(const std::string& path) {
     for (const auto& [k, e] : add) map_[k] = e;
 }
 
-std::vector<TraceConfig> trace_candidates(bool with_persistent) {
+std::vector<TraceConfig> trace_candidates(bool with_order) {
     std::vector<TraceConfig> out;
     for (int block : {64, 128, 256})
         for (int stack : {8, 12, 16}) {
@@ -94,17 +94,17 @@ std::vector<TraceConfig> trace_candidates(bool with_persistent) {
             c.refill = 0;
             out.push_back(c);
         }
-    if (with_persistent) {   // ray casts: also coherence order, in the default block size and stack depth
+    if (with_order) {   // ray casts: also coherence order, in the default block size and stack depth
         TraceConfig c;
+        c.refill = 0;
         c.sort = 1;
         out.push_back(c);
     }
-    if (with_persistent)
-        for (int refill : {8, 16}) {
-            TraceConfig c;
-            c.refill = refill;
-            out.push_back(c);
-        }
+    for (int refill : {4, 8, 16}) {   // the cooperative form
+        TraceConfig c;
+        c.refill = refill;
+        out.push_back(c);
+    }
     return out;
 }
 

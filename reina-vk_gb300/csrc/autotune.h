@@ -45,6 +45,6 @@ private:
 
 // Candidate traversal configurations: the grid form in every block size x stack depth, and (for ray
 // casts) the persistent form at two refill thresholds.
-std::vector<TraceConfig> trace_candidates(bool with_persistent);
+std::vector<TraceConfig> trace_candidates(bool with_order);
 
 }  // namespace rt

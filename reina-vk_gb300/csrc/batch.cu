@@ -11,6 +11,7 @@
 #include <cstring>
 
 #include "batch.h"
+#include "coop_trace.cuh"
 #include "trace_device.cuh"
 #include "wavefront_device.cuh"
 
@@ -125,6 +126,52 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) kb_extend(BatchLaunch B, 
             if (mine) ps.q_shade[(size_t)k * B.P + checked_index(pos, B.P, ps.counters + kCntError)] = p;
         }
     }
+}
+
+// Cooperative persistent form of the extension kernel (coop_trace.cuh; waves of flat scenes): warps
+// refill idle lanes from the active queue once at most `refill_at` lanes still trace; each lane's ray
+// uses its own job's scene.
+__global__ void __launch_bounds__(kTraceBlock, kCoopMinBlocks) kb_extend_coop(BatchLaunch B, const JobGpu* __restrict__ jobs, int cur,
+                                                             uint32_t refill_at) {
+    __shared__ CoopWarp warps[kTraceBlock / 32];
+    __shared__ uint2 stack[kSmemStack * kTraceBlock];
+    const PathState& ps = B.bp.ps;
+    const uint32_t n = ps.counters[kCntActive + cur];
+    const uint32_t* q = ps.q_active[cur];
+    TraceCounters c{0u, 0u};
+    auto load = [&](uint32_t i, TraceRay& r, CoopScene& sc) {
+        const uint32_t p = checked_index(q[i], B.P, ps.counters + kCntError);
+        const DeviceScene& s = jobs[B.bp.job[p]].s;
+        r = make_trace_ray(ps.ox[p], ps.oy[p], ps.oz[p], ps.dx[p], ps.dy[p], ps.dz[p], 0.0f, 10000.0f);
+        sc = CoopScene{s.nodes, s.tris, s.node_count};
+        return true;
+    };
+    auto store = [&](uint32_t i, const Hit& h, bool valid) {   // called by all 32 lanes
+        int m = -1;
+        uint32_t p = 0;
+        if (valid) {
+            p = checked_index(q[i], B.P, ps.counters + kCntError);
+            const DeviceScene& s = jobs[B.bp.job[p]].s;
+            ps.hprim[p] = h.prim;
+            ps.hu[p] = h.u;
+            ps.hv[p] = h.v;
+            m = h.prim == kMiss ? kQueueMiss : 1 + (int)s.props_material[prim_props_of(s, h.prim)];
+        }
+        warp_count64(reinterpret_cast<unsigned long long*>(ps.counters + kCntRays), valid);
+        warp_count64(reinterpret_cast<unsigned long long*>(ps.counters + kCntShaded), valid && m != kQueueMiss);
+#pragma unroll
+        for (int k = 0; k < kNumQueues; ++k) {
+            const bool mine = valid && m == k;
+            const uint32_t pos = warp_append(ps.counters + kCntQueue + k, mine);
+            if (mine) ps.q_shade[(size_t)k * B.P + checked_index(pos, B.P, ps.counters + kCntError)] = p;
+        }
+    };
+    const uint32_t e = coop_trace<false, true, true, true, kSmemStack>(CoopScene{nullptr, nullptr, 0u}, n,
+                                                                       ps.counters + kCntFetchExtend, refill_at,
+                                                                 warps[threadIdx.x >> 5], stack + threadIdx.x,
+                                                                 kTraceBlock, load, store, c);
+    if (e) atomicOr(ps.counters + kCntError, e);
+    coop_add_counts(c, ps.counters, kCntNodes, kCntTris);
 }
 
 template <int MAT>
@@ -245,6 +292,36 @@ __global__ void __launch_bounds__(BLOCK) kb_shadow(BatchLaunch B, const JobGpu* 
     }
 }
 
+// Cooperative persistent form of the shadow kernel (waves of flat scenes).
+__global__ void __launch_bounds__(kTraceBlock, kCoopMinBlocks) kb_shadow_coop(BatchLaunch B, const JobGpu* __restrict__ jobs,
+                                                             uint32_t refill_at) {
+    __shared__ CoopWarp warps[kTraceBlock / 32];
+    __shared__ uint2 stack[kSmemStack * kTraceBlock];
+    const PathState& ps = B.bp.ps;
+    const uint32_t n = ps.counters[kCntShadow];
+    TraceCounters c{0u, 0u};
+    auto load = [&](uint32_t i, TraceRay& r, CoopScene& sc) {
+        const uint32_t p = checked_index(ps.q_shadow[i], B.P, ps.counters + kCntError);
+        const DeviceScene& s = jobs[B.bp.job[p]].s;
+        r = make_trace_ray(ps.s_ox[i], ps.s_oy[i], ps.s_oz[i], ps.s_dx[i], ps.s_dy[i], ps.s_dz[i], 0.0f, ps.s_tmax[i]);
+        sc = CoopScene{s.nodes, s.tris, s.node_count};
+        return true;
+    };
+    auto store = [&](uint32_t i, const Hit& h, bool valid) {   // called by all 32 lanes
+        if (valid && h.prim == kMiss) {
+            const uint32_t p = checked_index(ps.q_shadow[i], B.P, ps.counters + kCntError);
+            store_rad(ps, p, load_rad(ps, p) + V3{ps.s_cr[i], ps.s_cg[i], ps.s_cb[i]});
+        }
+        warp_count64(reinterpret_cast<unsigned long long*>(ps.counters + kCntShadowRays), valid);
+    };
+    const uint32_t e = coop_trace<true, true, false, true, kSmemStack>(CoopScene{nullptr, nullptr, 0u}, n,
+                                                                       ps.counters + kCntFetchShadow, refill_at,
+                                                                 warps[threadIdx.x >> 5], stack + threadIdx.x,
+                                                                 kTraceBlock, load, store, c);
+    if (e) atomicOr(ps.counters + kCntError, e);
+    coop_add_counts(c, ps.counters, kCntShadowNodes, kCntShadowTris);
+}
+
 // raytrace.rgen.glsl:264-275 per pixel of each job in the wave: clamp (NaN kept), sample output, NaN
 // drop, sum — over the pixel's samples in this wave in sample order (a job whose samples are independent
 // may have several samples of a pixel in one wave) — and carry the RNG state and accumulatedDistance of
@@ -358,10 +435,15 @@ BatchEngine::BatchEngine(int device, int sm_count, uint32_t wave_capacity, bool 
         release_lanes();
         throw;
     }
-    with_trace_variant(trace_, [&](auto B, auto S) {
-        blocks_ext_ = resident_grid((const void*)kb_extend<B.value, S.value, false>, B.value, sm_count);
-        blocks_sh_ = resident_grid((const void*)kb_shadow<B.value, S.value, false>, B.value, sm_count);
-    });
+    if (trace_.refill > 0) {
+        blocks_ext_ = resident_grid((const void*)kb_extend_coop, kTraceBlock, sm_count);
+        blocks_sh_ = resident_grid((const void*)kb_shadow_coop, kTraceBlock, sm_count);
+    } else {
+        with_trace_variant(trace_, [&](auto B, auto S) {
+            blocks_ext_ = resident_grid((const void*)kb_extend<B.value, S.value, false>, B.value, sm_count);
+            blocks_sh_ = resident_grid((const void*)kb_shadow<B.value, S.value, false>, B.value, sm_count);
+        });
+    }
     blocks_ext_two_ = resident_grid((const void*)kb_extend<kTraceBlock, kDefaultTraceStack, true>, kTraceBlock, sm_count);
     blocks_sh_two_ = resident_grid((const void*)kb_shadow<kTraceBlock, kDefaultTraceStack, true>, kTraceBlock, sm_count);
     blocks_shade_[1] = occupancy((const void*)kb_shade<1>, sm_count);
@@ -447,8 +529,12 @@ void BatchEngine::launch_body(Lane& L, const Packed& pk, cudaStream_t st) {
         for (uint32_t seg = 0; seg < h.max_bounces; ++seg) {
             check_cuda(cudaMemsetAsync(cnt + kCntActive + (cur ^ 1), 0, sizeof(uint32_t), s), "cudaMemsetAsync");
             check_cuda(cudaMemsetAsync(cnt + kCntQueue, 0, 6 * sizeof(uint32_t), s), "cudaMemsetAsync");
-            if (two)   // a two-level scene in the wave: the default variant, both traversals
+            if (!two && trace_.refill > 0)
+                check_cuda(cudaMemsetAsync(cnt + kCntFetchExtend, 0, 2 * sizeof(uint32_t), s), "cudaMemsetAsync");
+            if (two)   // a two-level scene in the wave: the default grid variant, both traversals
                 kb_extend<kTraceBlock, kDefaultTraceStack, true><<<blocks_ext_two_, kTraceBlock, 0, s>>>(B, B.jobs, cur);
+            else if (trace_.refill > 0)
+                kb_extend_coop<<<blocks_ext_, kTraceBlock, 0, s>>>(B, B.jobs, cur, (uint32_t)(32 - trace_.refill));
             else
                 with_trace_variant(trace_, [&](auto BS, auto SS) {
                     kb_extend<BS.value, SS.value, false><<<blocks_ext_, BS.value, 0, s>>>(B, B.jobs, cur);
@@ -460,6 +546,8 @@ void BatchEngine::launch_body(Lane& L, const Packed& pk, cudaStream_t st) {
             kb_shade<4><<<blocks_shade_[4], kBlock, 0, s>>>(B, B.jobs, cur);
             if (any_nee && two)
                 kb_shadow<kTraceBlock, kDefaultTraceStack, true><<<blocks_sh_two_, kTraceBlock, 0, s>>>(B, B.jobs);
+            else if (any_nee && trace_.refill > 0)
+                kb_shadow_coop<<<blocks_sh_, kTraceBlock, 0, s>>>(B, B.jobs, (uint32_t)(32 - trace_.refill));
             else if (any_nee)
                 with_trace_variant(trace_, [&](auto BS, auto SS) {
                     kb_shadow<BS.value, SS.value, false><<<blocks_sh_, BS.value, 0, s>>>(B, B.jobs);
@@ -523,13 +611,18 @@ void BatchEngine::collect(Lane& L) {
     if (!L.pending) return;
     L.pending = false;
     const uint32_t* c = L.host_counters;
-    uint64_t r, sr;
-    std::memcpy(&r, c + kCntRays, 8);
-    std::memcpy(&sr, c + kCntShadowRays, 8);
-    rays_ += r;
-    shadow_rays_ += sr;
+    auto u64 = [&](int at) { uint64_t v; std::memcpy(&v, c + at, 8); return v; };
+    rays_ += u64(kCntRays);
+    shadow_rays_ += u64(kCntShadowRays);
+    work_.nodes += u64(kCntNodes);
+    work_.tris += u64(kCntTris);
+    work_.shadow_nodes += u64(kCntShadowNodes);
+    work_.shadow_tris += u64(kCntShadowTris);
+    work_.shaded += u64(kCntShaded);
     waves_++;
-    if (c[kCntError]) fail(REINA_ERR_DEVICE, "batch wave kernels raised error flag " + std::to_string(c[kCntError]));
+    if (c[kCntError])
+        fail(REINA_ERR_DEVICE, "batch wave kernels raised error flag " + std::to_string(c[kCntError]) +
+                                   device_error_text(c[kCntError]));
 }
 
 BatchEngine::Packed BatchEngine::pack(const std::vector<BatchJob*>& jobs, bool fifo, Lane& L) {

@@ -122,6 +122,9 @@ public:
     const TraceConfig& trace() const { return trace_; }
     uint64_t rays() const { return rays_; }
     uint64_t shadow_rays() const { return shadow_rays_; }
+    // traversal work counted by the cooperative kernels (nodes, triangles of closest and any-hit rays,
+    // shaded hits) over the waves collected so far
+    const RenderStats& work() const { return work_; }
     uint32_t waves() const { return waves_; }
 
 private:
@@ -164,6 +167,7 @@ private:
     size_t desc_bytes_ = 0;
     std::vector<Lane> lanes_;
     uint64_t rays_ = 0, shadow_rays_ = 0;
+    RenderStats work_;
     uint32_t waves_ = 0;
     uint64_t submitted_ = 0, retired_ = 0;   // waves launched / waited for
     int blocks_ext_ = 0, blocks_shade_[5] = {0, 0, 0, 0, 0}, blocks_sh_ = 0, blocks_simple_ = 0;

@@ -226,20 +226,20 @@ int reina_ctx_sm_count(const reina_ctx* ctx) { return ctx ? ctx->sm_count : 0; }
 int reina_ctx_set_tuning(reina_ctx* ctx, const reina_tuning* t) {
     return guard([&] {
         need(ctx && t, "NULL argument");
-        need(t->refill <= 32, "refill must be in 0..32");
+        need(t->refill <= 32 || t->refill == REINA_REFILL_GRID, "refill must be in 0..32 or REINA_REFILL_GRID");
         need((t->batch_flags & ~(uint32_t)(REINA_BATCH_NO_GRAPHS | REINA_BATCH_FAIR_SHARE)) == 0, "unknown batch flags");
         need(t->wave_lanes <= 16, "wave_lanes must be in 0..16");
         const uint32_t lanes = t->wave_lanes ? t->wave_lanes : (uint32_t)REINA_DEFAULT_WAVE_LANES;
         const uint32_t wave = t->wave_paths ? t->wave_paths : (uint32_t)REINA_DEFAULT_WAVE_PATHS;
         need(wave <= (1u << 26), "wave_paths must be at most 2^26");
         rt::TraceConfig tc;
-        tc.refill = (int)t->refill;
+        tc.refill = t->refill == 0 ? rt::kDefaultRefill : (t->refill == REINA_REFILL_GRID ? 0 : (int)t->refill);
         tc.block = (int)(t->trace_block ? t->trace_block : rt::kTraceBlock);
         tc.stack = (int)(t->trace_stack ? t->trace_stack : rt::kDefaultTraceStack);
         need(t->trace_order <= REINA_ORDER_COHERENT, "trace_order must be REINA_ORDER_INPUT or REINA_ORDER_COHERENT");
         tc.sort = t->trace_order == REINA_ORDER_COHERENT ? 1 : 0;
         need(rt::valid_trace_config(tc), "trace_block must be 64, 128 or 256 and trace_stack 8, 12 or 16");
-        const bool engine_changed = tc.block != ctx->trace.block || tc.stack != ctx->trace.stack;
+        const bool engine_changed = tc.block != ctx->trace.block || tc.stack != ctx->trace.stack || tc.refill != ctx->trace.refill;
         ctx->trace = tc;
         if (wave != ctx->wave_paths || t->batch_flags != ctx->batch_flags || lanes != ctx->wave_lanes || engine_changed) {
             if (ctx->batch && ctx->device >= 0) check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
@@ -255,7 +255,7 @@ int reina_ctx_get_tuning(const reina_ctx* ctx, reina_tuning* out) {
     return guard([&] {
         need(ctx && out, "NULL argument");
         std::memset(out, 0, sizeof(*out));
-        out->refill = (uint32_t)ctx->trace.refill;
+        out->refill = ctx->trace.refill == 0 ? (uint32_t)REINA_REFILL_GRID : (uint32_t)ctx->trace.refill;
         out->trace_block = (uint32_t)ctx->trace.block;
         out->trace_stack = (uint32_t)ctx->trace.stack;
         out->trace_order = ctx->trace.sort ? REINA_ORDER_COHERENT : REINA_ORDER_INPUT;
@@ -406,6 +406,16 @@ int reina_raycast_device(reina_ctx* ctx, const reina_scene* scene, const void* d
     });
 }
 
+int reina_ctx_device_error(reina_ctx* ctx, void* stream, uint32_t* out_flags) {
+    return guard([&] {
+        need(ctx != nullptr, "ctx is NULL");
+        use_device(ctx);
+        const uint32_t e = check_device_errors(ctx, static_cast<cudaStream_t>(stream));
+        if (out_flags) *out_flags = e;
+        if (e) fail(REINA_ERR_DEVICE, "device kernels raised error flag " + std::to_string(e) + rt::device_error_text(e));
+    });
+}
+
 int reina_raycast(reina_ctx* ctx, const reina_scene* scene, const reina_ray* rays, uint64_t count, reina_hit* hits,
                   uint32_t flags) {
     return guard([&] {
@@ -426,7 +436,7 @@ int reina_raycast(reina_ctx* ctx, const reina_scene* scene, const reina_ray* ray
                                ctx->next_fetch_counter(), ctx->sm_count, cfg, st);
             check_cuda(cudaGetLastError(), "raycast launch");
             const uint32_t e = check_device_errors(ctx, st);
-            if (e) fail(REINA_ERR_DEVICE, "traversal kernel raised error flag " + std::to_string(e));
+            if (e) fail(REINA_ERR_DEVICE, "traversal kernel raised error flag " + std::to_string(e) + rt::device_error_text(e));
             return;
         }
         ctx->rays.reserve(count * sizeof(rt::Ray));
@@ -447,7 +457,7 @@ int reina_raycast(reina_ctx* ctx, const reina_scene* scene, const reina_ray* ray
         }
         check_cuda(cudaStreamSynchronize(ctx->streams[1]), "cudaStreamSynchronize");
         const uint32_t e = check_device_errors(ctx, ctx->streams[0]);
-        if (e) fail(REINA_ERR_DEVICE, "traversal kernel raised error flag " + std::to_string(e));
+        if (e) fail(REINA_ERR_DEVICE, "traversal kernel raised error flag " + std::to_string(e) + rt::device_error_text(e));
     });
 }
 
@@ -538,7 +548,7 @@ int reina_render_device(reina_ctx* ctx, const reina_scene* scene, const RtPushCo
             return;
         }
         rt::render_frame(ctx->render, s.device_view(), *pc, r, static_cast<float*>(d_accum), static_cast<float*>(d_samples),
-                         ctx->sm_count, static_cast<cudaStream_t>(stream), nullptr);
+                         ctx->sm_count, static_cast<cudaStream_t>(stream), nullptr, ctx->err.as<uint32_t>());
     });
 }
 
@@ -553,7 +563,8 @@ int reina_render_device_noalloc(reina_ctx* ctx, const reina_scene* scene, const 
         need(d_accum != nullptr && ((uintptr_t)d_accum % 16) == 0, "accumulation buffer must be non-NULL and 16-byte aligned");
         use_device(ctx);
         rt::render_frame_noalloc(ctx->device, s.device_view(), *pc, r, static_cast<float*>(d_accum),
-                                 static_cast<float*>(d_samples), ctx->sm_count, static_cast<cudaStream_t>(stream));
+                                 static_cast<float*>(d_samples), ctx->sm_count, static_cast<cudaStream_t>(stream),
+                                 ctx->err.as<uint32_t>());
     });
 }
 
@@ -588,10 +599,15 @@ int reina_render(reina_ctx* ctx, const reina_scene* scene, const RtPushConsts* p
             check_cuda(cudaMemcpyAsync(samples, d_samples, P * pc->samplesPerPixel * 3 * sizeof(float), cudaMemcpyDeviceToHost, st),
                        "D2H samples");
         check_cuda(cudaStreamSynchronize(st), "cudaStreamSynchronize");
-        if (rs.error) fail(REINA_ERR_DEVICE, "render kernel raised error flag " + std::to_string(rs.error));
+        if (rs.error) fail(REINA_ERR_DEVICE, "render kernel raised error flag " + std::to_string(rs.error) + rt::device_error_text(rs.error));
         if (stats) {
             stats->rays = rs.rays;
             stats->shadow_rays = rs.shadow_rays;
+            stats->nodes_visited = rs.nodes;
+            stats->triangles_tested = rs.tris;
+            stats->shadow_nodes_visited = rs.shadow_nodes;
+            stats->shadow_triangles_tested = rs.shadow_tris;
+            stats->shaded_hits = rs.shaded;
             stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         }
     });
@@ -645,7 +661,8 @@ static rt::BatchEngine& batch_engine(reina_ctx* ctx, const reina_render_job* job
     const uint32_t fitted = fit_wave(wave, samples);
     if (ctx->batch && (ctx->batch->capacity() < fitted || ctx->batch->capacity() > wave ||
                        ctx->batch->lanes() != (int)ctx->wave_lanes ||
-                       ctx->batch->trace().block != trace.block || ctx->batch->trace().stack != trace.stack))
+                       ctx->batch->trace().block != trace.block || ctx->batch->trace().stack != trace.stack ||
+                       ctx->batch->trace().refill != trace.refill))
         ctx->batch.reset();
     if (!ctx->batch)
         ctx->batch = std::make_unique<rt::BatchEngine>(ctx->device, ctx->sm_count, fitted,
@@ -705,6 +722,7 @@ static void render_batch(reina_ctx* ctx, const reina_render_job* jobs, uint32_t 
         ptrs[k] = &bj[k];
     }
     const uint64_t r0 = eng.rays(), s0 = eng.shadow_rays();
+    const rt::RenderStats w0 = eng.work();
     eng.run_all(ptrs, st, (ctx->batch_flags & REINA_BATCH_FAIR_SHARE) == 0);
     if (host) {
         for (uint32_t k = 0; k < count; ++k) {
@@ -722,6 +740,12 @@ static void render_batch(reina_ctx* ctx, const reina_render_job* jobs, uint32_t 
     if (stats) {
         stats->rays = eng.rays() - r0;
         stats->shadow_rays = eng.shadow_rays() - s0;
+        const rt::RenderStats& w = eng.work();
+        stats->nodes_visited = w.nodes - w0.nodes;
+        stats->triangles_tested = w.tris - w0.tris;
+        stats->shadow_nodes_visited = w.shadow_nodes - w0.shadow_nodes;
+        stats->shadow_triangles_tested = w.shadow_tris - w0.shadow_tris;
+        stats->shaded_hits = w.shaded - w0.shaded;
         stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     }
 }
@@ -1007,7 +1031,7 @@ double time_calls(cudaStream_t st, int reps, F&& fn) {
 
 void fill_tuning(const reina_ctx* ctx, const rt::TuneEntry& e, reina_tuning* t) {
     std::memset(t, 0, sizeof(*t));
-    t->refill = (uint32_t)e.trace.refill;
+    t->refill = e.trace.refill == 0 ? (uint32_t)REINA_REFILL_GRID : (uint32_t)e.trace.refill;
     t->trace_block = (uint32_t)e.trace.block;
     t->trace_stack = (uint32_t)e.trace.stack;
     t->trace_order = e.trace.sort ? REINA_ORDER_COHERENT : REINA_ORDER_INPUT;
@@ -1033,7 +1057,7 @@ void finish_tune(reina_ctx* ctx, uint32_t kind, uint64_t tris, uint64_t size, co
 }
 
 bool is_default(const rt::TraceConfig& c) {
-    return c.refill == 0 && c.block == rt::kTraceBlock && c.stack == rt::kDefaultTraceStack && c.sort == 0;
+    return c.refill == rt::kDefaultRefill && c.block == rt::kTraceBlock && c.stack == rt::kDefaultTraceStack && c.sort == 0;
 }
 
 }  // namespace
@@ -1068,7 +1092,7 @@ int reina_autotune_raycast(reina_ctx* ctx, const reina_scene* scene, const void*
             }
         }
         const uint32_t e = check_device_errors(ctx, st);
-        if (e) fail(REINA_ERR_DEVICE, "traversal kernel raised error flag " + std::to_string(e));
+        if (e) fail(REINA_ERR_DEVICE, "traversal kernel raised error flag " + std::to_string(e) + rt::device_error_text(e));
         finish_tune(ctx, flags, s.triangle_count(), count, best, (uint32_t)cands.size(), out);
     });
 }
@@ -1156,9 +1180,9 @@ int reina_autotune_batch(reina_ctx* ctx, const reina_render_job* jobs, uint32_t 
                     waves.push_back(fit_wave(w, samples));
             const uint32_t default_wave = fit_wave(REINA_DEFAULT_WAVE_PATHS, samples);
             for (uint32_t wave : waves)
-                for (int block : {128, 256}) {
+                for (int refill : {rt::kDefaultRefill, 0}) {   // the cooperative form, the grid form
                     rt::TraceConfig c;
-                    c.block = block;
+                    c.refill = refill;
                     ctx->wave_paths = wave;
                     ctx->trace = c;
                     ctx->batch.reset();

@@ -1,6 +1,8 @@
 // Error type used inside the library; the C ABI converts it into a status code and a message.
 #pragma once
 
+#include <stdint.h>
+
 #include <stdexcept>
 #include <string>
 
@@ -16,6 +18,16 @@ struct Error : std::runtime_error {
 };
 
 [[noreturn]] inline void fail(int code, const std::string& msg) { throw Error(code, msg); }
+
+// The meaning of the bits of a device error word, for messages: bit 1 traversal stack overflow, bit 2
+// traversal step limit, bit 4 queue or path index out of range (checked build).
+inline std::string device_error_text(uint32_t e) {
+    std::string t;
+    if (e & 1u) t += " (traversal stack overflow)";
+    if (e & 2u) t += " (traversal step limit)";
+    if (e & 4u) t += " (queue or path index out of range, checked build)";
+    return t;
+}
 
 inline void check_cuda(cudaError_t e, const char* what) {
     if (e != cudaSuccess) {

@@ -19,6 +19,7 @@
 
 #include "kernels.h"
 #include "render.h"
+#include "coop_trace.cuh"
 #include "shading_device.cuh"
 #include "trace_device.cuh"
 #include "wavefront_device.cuh"
@@ -100,20 +101,22 @@ __global__ void __launch_bounds__(BLOCK) k_extend_grid(RenderLaunch L, int cur) 
     }
 }
 
-// Persistent form: warps refill idle lanes from the queue (dynamic ray fetch).
-__global__ void __launch_bounds__(kBlock) k_extend(RenderLaunch L, int cur) {
+// Cooperative persistent form (coop_trace.cuh): warps refill idle lanes from the queue; triangle tests
+// and hit refinement are spread over the warp.  Flat scenes.
+__global__ void __launch_bounds__(kBlock, kCoopMinBlocks) k_extend(RenderLaunch L, int cur) {
+    __shared__ CoopWarp warps[kBlock / 32];
     __shared__ uint2 stack[kSmemStack * kBlock];
     const PathState& ps = L.ps;
     const uint32_t n = ps.counters[kCntActive + cur];
     const uint32_t* q = ps.q_active[cur];
     TraceCounters c{0u, 0u};
-    auto load = [&](uint32_t i, TraceRay& r) {
+    auto load = [&](uint32_t i, TraceRay& r, CoopScene& sc) {
         const uint32_t p = checked_index(q[i], L.P, ps.counters + kCntError);
         r = make_trace_ray(ps.ox[p], ps.oy[p], ps.oz[p], ps.dx[p], ps.dy[p], ps.dz[p], 0.0f, 10000.0f);
+        (void)sc;
         return true;
     };
     auto store = [&](uint32_t i, const Hit& h, bool valid) {   // called by all 32 lanes
-        if (__ballot_sync(0xFFFFFFFFu, valid) == 0u) return;
         int m = -1;
         uint32_t p = 0;
         if (valid) {
@@ -124,6 +127,7 @@ __global__ void __launch_bounds__(kBlock) k_extend(RenderLaunch L, int cur) {
             m = h.prim == kMiss ? kQueueMiss : 1 + (int)L.s.props_material[prim_props_of(L.s, h.prim)];
         }
         warp_count64(reinterpret_cast<unsigned long long*>(ps.counters + kCntRays), valid);
+        warp_count64(reinterpret_cast<unsigned long long*>(ps.counters + kCntShaded), valid && m != kQueueMiss);
 #pragma unroll
         for (int k = 0; k < kNumQueues; ++k) {
             const bool mine = valid && m == k;
@@ -131,10 +135,12 @@ __global__ void __launch_bounds__(kBlock) k_extend(RenderLaunch L, int cur) {
             if (mine) ps.q_shade[(size_t)k * L.P + checked_index(pos, L.P, ps.counters + kCntError)] = p;
         }
     };
-    const uint32_t e = persistent_trace<false, false, true>(L.s.nodes, L.s.tris, L.s.node_count, n,
-                                                           ps.counters + kCntFetchExtend, stack + threadIdx.x, kBlock,
-                                                           L.refill, load, store, c);
+    const uint32_t e = coop_trace<false, true, true, false, kSmemStack>(CoopScene{L.s.nodes, L.s.tris, L.s.node_count}, n,
+                                                                        ps.counters + kCntFetchExtend, (uint32_t)(32 - L.refill),
+                                                                 warps[threadIdx.x >> 5], stack + threadIdx.x, kBlock,
+                                                                 load, store, c);
     if (e) atomicOr(ps.counters + kCntError, e);
+    coop_add_counts(c, ps.counters, kCntNodes, kCntTris);
 }
 
 // One kernel per material queue (MAT = 1 Lambertian, 2 metal, 3 dielectric, 4 Disney): the closest-hit
@@ -255,14 +261,16 @@ __global__ void __launch_bounds__(BLOCK) k_shadow_grid(RenderLaunch L) {
     }
 }
 
-// Persistent form of the shadow kernel.
-__global__ void __launch_bounds__(kBlock) k_shadow(RenderLaunch L) {
+// Cooperative persistent form of the shadow kernel (flat scenes).
+__global__ void __launch_bounds__(kBlock, kCoopMinBlocks) k_shadow(RenderLaunch L) {
+    __shared__ CoopWarp warps[kBlock / 32];
     __shared__ uint2 stack[kSmemStack * kBlock];
     const PathState& ps = L.ps;
     const uint32_t n = ps.counters[kCntShadow];
     TraceCounters c{0u, 0u};
-    auto load = [&](uint32_t i, TraceRay& r) {
+    auto load = [&](uint32_t i, TraceRay& r, CoopScene& sc) {
         r = make_trace_ray(ps.s_ox[i], ps.s_oy[i], ps.s_oz[i], ps.s_dx[i], ps.s_dy[i], ps.s_dz[i], 0.0f, ps.s_tmax[i]);
+        (void)sc;
         return true;
     };
     auto store = [&](uint32_t i, const Hit& h, bool valid) {   // called by all 32 lanes
@@ -272,10 +280,12 @@ __global__ void __launch_bounds__(kBlock) k_shadow(RenderLaunch L) {
         }
         warp_count64(reinterpret_cast<unsigned long long*>(ps.counters + kCntShadowRays), valid);
     };
-    const uint32_t e = persistent_trace<true, false, false>(L.s.nodes, L.s.tris, L.s.node_count, n,
-                                                           ps.counters + kCntFetchShadow, stack + threadIdx.x, kBlock,
-                                                           L.refill, load, store, c);
+    const uint32_t e = coop_trace<true, true, false, false, kSmemStack>(CoopScene{L.s.nodes, L.s.tris, L.s.node_count}, n,
+                                                                        ps.counters + kCntFetchShadow, (uint32_t)(32 - L.refill),
+                                                                 warps[threadIdx.x >> 5], stack + threadIdx.x, kBlock,
+                                                                 load, store, c);
     if (e) atomicOr(ps.counters + kCntError, e);
+    coop_add_counts(c, ps.counters, kCntShadowNodes, kCntShadowTris);
 }
 
 // raytrace.rgen.glsl:264-275: clamp to [0, directClamp] (NaN kept), drop NaN samples, sum the rest.
@@ -578,21 +588,34 @@ static void launch_frame(const PathState& ps, const DeviceScene& s, const RtPush
         uint32_t c[kNumCounters];
         check_cuda(cudaMemcpyAsync(c, cnt, sizeof(c), cudaMemcpyDeviceToHost, st), "cudaMemcpyAsync counters");
         check_cuda(cudaStreamSynchronize(st), "cudaStreamSynchronize");
-        uint64_t rays, srays;
-        std::memcpy(&rays, c + kCntRays, 8);
-        std::memcpy(&srays, c + kCntShadowRays, 8);
-        stats->rays = rays;
-        stats->shadow_rays = srays;
+        auto u64 = [&](int at) { uint64_t v; std::memcpy(&v, c + at, 8); return v; };
+        stats->rays = u64(kCntRays);
+        stats->shadow_rays = u64(kCntShadowRays);
+        stats->nodes = u64(kCntNodes);
+        stats->tris = u64(kCntTris);
+        stats->shadow_nodes = u64(kCntShadowNodes);
+        stats->shadow_tris = u64(kCntShadowTris);
+        stats->shaded = u64(kCntShaded);
         stats->error = c[kCntError];
     }
 }
 
+// ORs a frame's error word into the caller's error word (one thread; enqueued after the frame).
+__global__ void k_or_error(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst) {
+    if (threadIdx.x == 0 && *src) atomicOr(dst, *src);
+}
+
 void render_frame(RenderWorkspace& ws, const DeviceScene& s, const RtPushConsts& pc, const RenderOpts& opt,
-                  float* d_accum, float* d_samples, int sm_count, cudaStream_t st, RenderStats* stats) {
+                  float* d_accum, float* d_samples, int sm_count, cudaStream_t st, RenderStats* stats,
+                  uint32_t* err_accum) {
     const uint32_t P = opt.width * opt.height;
     if (P == 0) return;
     ws.ensure(P);
     launch_frame(ws.view(), s, pc, opt, d_accum, d_samples, sm_count, st, stats);
+    if (err_accum) {
+        k_or_error<<<1, 32, 0, st>>>(ws.view().counters + kCntError, err_accum);
+        check_cuda(cudaGetLastError(), "error word launch");
+    }
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -621,14 +644,19 @@ static uint32_t* noalloc_scratch(int device) {
 }
 
 void render_frame_noalloc(int device, const DeviceScene& s, const RtPushConsts& pc, const RenderOpts& opt,
-                          float* d_accum, float* d_samples, int sm_count, cudaStream_t st) {
+                          float* d_accum, float* d_samples, int sm_count, cudaStream_t st, uint32_t* err_accum) {
     const uint64_t P = (uint64_t)opt.width * opt.height;
     if (P > kNoAllocMaxPixels)
         fail(REINA_ERR_INVALID, "allocation-free render is limited to " + std::to_string(kNoAllocMaxPixels) +
                                     " pixels (e.g. 256x256); got " + std::to_string(opt.width) + "x" + std::to_string(opt.height));
     if (P == 0) return;
     uint32_t* base = noalloc_scratch(device);
-    launch_frame(layout_path_state(base, P), s, pc, opt, d_accum, d_samples, sm_count, st, nullptr);
+    const PathState ps = layout_path_state(base, P);
+    launch_frame(ps, s, pc, opt, d_accum, d_samples, sm_count, st, nullptr);
+    if (err_accum) {
+        k_or_error<<<1, 32, 0, st>>>(ps.counters + kCntError, err_accum);
+        check_cuda(cudaGetLastError(), "error word launch");
+    }
 }
 
 }  // namespace rt

@@ -37,9 +37,16 @@ constexpr int kCntShadow = 7;
 constexpr int kCntError = 8;
 constexpr int kCntRays = 10;
 constexpr int kCntShadowRays = 12;
-constexpr int kCntFetchExtend = 14;   // ray-fetch counters of the persistent extend / shadow kernels
+constexpr int kCntFetchExtend = 14;   // ray-fetch counters of the cooperative extend / shadow kernels
 constexpr int kCntFetchShadow = 15;
-constexpr int kNumCounters = 16;
+// Traversal work of the cooperative kernels (u64 each): BVH8 nodes visited and triangles tested by the
+// closest-hit (extension) and any-hit (shadow) rays, and the hits shaded by a material kernel.
+constexpr int kCntNodes = 16;
+constexpr int kCntTris = 18;
+constexpr int kCntShadowNodes = 20;
+constexpr int kCntShadowTris = 22;
+constexpr int kCntShaded = 24;
+constexpr int kNumCounters = 26;
 
 // Plain-pointer view of the path state (SoA) passed to every kernel.
 struct PathState {
@@ -93,20 +100,23 @@ private:
 struct RenderStats {
     uint64_t rays = 0;          // closest-hit rays traced (path segments)
     uint64_t shadow_rays = 0;
+    uint64_t nodes = 0, tris = 0, shadow_nodes = 0, shadow_tris = 0, shaded = 0;   // cooperative kernels' counts
     uint32_t error = 0;
 };
 
 // Renders one frame (RtPushConsts::samplesPerPixel samples per pixel, running mean with the image when
 // sampleBatch > 0) into d_accum.  Enqueued on `st`; if `stats` is given the call synchronizes and
-// reads the counters.
+// reads the counters; if `err_accum` is given, the frame's device error flags are OR-ed into that word
+// on `st` after the frame (the asynchronous entry points' error word, read by reina_ctx_device_error).
 void render_frame(RenderWorkspace& ws, const DeviceScene& s, const RtPushConsts& pc, const RenderOpts& opt,
-                  float* d_accum, float* d_samples, int sm_count, cudaStream_t st, RenderStats* stats);
+                  float* d_accum, float* d_samples, int sm_count, cudaStream_t st, RenderStats* stats,
+                  uint32_t* err_accum = nullptr);
 
 // The same frame with the path state in a fixed device array of the library (no allocation); at most
 // kNoAllocMaxPixels pixels.  `device` must be the current device.
 constexpr uint32_t kNoAllocMaxPixels = 65536;
 constexpr int kNoAllocMaxDevices = 64;
 void render_frame_noalloc(int device, const DeviceScene& s, const RtPushConsts& pc, const RenderOpts& opt,
-                          float* d_accum, float* d_samples, int sm_count, cudaStream_t st);
+                          float* d_accum, float* d_samples, int sm_count, cudaStream_t st, uint32_t* err_accum);
 
 }  // namespace rt

@@ -5,6 +5,7 @@
 
 #include <algorithm>
 
+#include "coop_trace.cuh"
 #include "kernels.h"
 #include "trace_device.cuh"
 
@@ -34,25 +35,30 @@ __device__ __forceinline__ void reduce_counters(const TraceCounters& c, unsigned
     }
 }
 
+// Warp-cooperative persistent form (coop_trace.cuh): warps refill idle lanes once at most `refill_at` of
+// their lanes still trace; triangle tests and hit refinement are spread over the warp.
 template <bool ANY, bool COUNT>
-__global__ void RT_TRACE_BOUNDS(kTraceBlock) raycast_kernel(const Bvh8Node* __restrict__ nodes,
-                                                           const TriRecord* __restrict__ tris, uint32_t node_count,
-                                                           const Ray* __restrict__ rays, uint32_t n,
-                                                           Hit* __restrict__ hits, unsigned long long* counters,
-                                                           uint32_t* err_flag, uint32_t* next, int refill) {
+__global__ void __launch_bounds__(kTraceBlock, kCoopMinBlocks) raycast_kernel(const Bvh8Node* __restrict__ nodes,
+                                                              const TriRecord* __restrict__ tris, uint32_t node_count,
+                                                              const Ray* __restrict__ rays, uint32_t n,
+                                                              Hit* __restrict__ hits, unsigned long long* counters,
+                                                              uint32_t* err_flag, uint32_t* next, uint32_t refill_at) {
+    __shared__ CoopWarp warps[kTraceBlock / 32];
     __shared__ uint2 stack[kSmemStack * kTraceBlock];
     TraceCounters c{0u, 0u};
-    auto load = [&](uint32_t i, TraceRay& r) {
+    auto load = [&](uint32_t i, TraceRay& r, CoopScene& sc) {
         const float4* rp = reinterpret_cast<const float4*>(rays) + 2ull * i;
         const float4 a = __ldcs(rp), b = __ldcs(rp + 1);
         r = make_trace_ray(a.x, a.y, a.z, b.x, b.y, b.z, a.w, b.w);
+        (void)sc;
         return true;
     };
     auto store = [&](uint32_t i, const Hit& h, bool valid) {
         if (valid && hits) __stcs(reinterpret_cast<float4*>(hits) + i, make_float4(__uint_as_float(h.prim), h.t, h.u, h.v));
     };
-    const uint32_t e = persistent_trace<ANY, COUNT, true>(nodes, tris, node_count, n, next, stack + threadIdx.x,
-                                                         kTraceBlock, refill, load, store, c);
+    const uint32_t e = coop_trace<ANY, COUNT, true, false, kSmemStack>(CoopScene{nodes, tris, node_count}, n, next, refill_at,
+                                                                       warps[threadIdx.x >> 5], stack + threadIdx.x,
+                                                                       kTraceBlock, load, store, c);
     if (e) atomicOr(err_flag, e);
     reduce_counters<COUNT>(c, counters);
 }
@@ -298,7 +304,7 @@ static void launch(const DeviceScene& s, const Ray* d_rays, uint64_t n, Hit* d_h
     check_cuda(cudaMemsetAsync(d_next, 0, sizeof(uint32_t), st), "cudaMemsetAsync");
     const int grid = (int)std::min<uint64_t>(needed, (uint64_t)persistent_grid<ANY, false>(sm_count));
     raycast_kernel<ANY, false><<<grid, kTraceBlock, 0, st>>>(s.nodes, s.tris, s.node_count, d_rays, (uint32_t)n, d_hits,
-                                                             nullptr, d_err, d_next, cfg.refill);
+                                                             nullptr, d_err, d_next, (uint32_t)(32 - cfg.refill));
 }
 
 bool valid_trace_config(const TraceConfig& c) {
@@ -318,13 +324,26 @@ void launch_raycast(const DeviceScene& s, const Ray* d_rays, uint64_t n, Hit* d_
 void launch_raycast_counters(const DeviceScene& s, const Ray* d_rays, uint64_t n, bool any,
                              unsigned long long* d_counters, uint32_t* d_err, uint32_t* d_next, int sm_count,
                              cudaStream_t st) {
-    (void)d_next;
-    (void)sm_count;
     if (n == 0) return;
-    // The counting build uses the default grid form: visit counts do not depend on block size or stack
-    // depth (warps hold the same 32 consecutive rays in every grid variant).
-    if (any) launch_grid<true, true, kTraceBlock, kSmemStack>(s, d_rays, n, nullptr, d_counters, d_err, nullptr, st);
-    else launch_grid<false, true, kTraceBlock, kSmemStack>(s, d_rays, n, nullptr, d_counters, d_err, nullptr, st);
+    // The counting build of the default form: the cooperative form for flat scenes (its deferred triangle
+    // tests cull later, so it may visit a few more nodes than the grid form), the grid form otherwise.
+    if (s.inst_trav || n > (1ull << 31)) {
+        if (any) launch_grid<true, true, kTraceBlock, kSmemStack>(s, d_rays, n, nullptr, d_counters, d_err, nullptr, st);
+        else launch_grid<false, true, kTraceBlock, kSmemStack>(s, d_rays, n, nullptr, d_counters, d_err, nullptr, st);
+        return;
+    }
+    check_cuda(cudaMemsetAsync(d_next, 0, sizeof(uint32_t), st), "cudaMemsetAsync");
+    const uint64_t needed = (n + kTraceBlock - 1) / kTraceBlock;
+    const uint32_t refill_at = (uint32_t)(32 - kDefaultRefill);
+    if (any) {
+        const int grid = (int)std::min<uint64_t>(needed, (uint64_t)persistent_grid<true, true>(sm_count));
+        raycast_kernel<true, true><<<grid, kTraceBlock, 0, st>>>(s.nodes, s.tris, s.node_count, d_rays, (uint32_t)n,
+                                                                 nullptr, d_counters, d_err, d_next, refill_at);
+    } else {
+        const int grid = (int)std::min<uint64_t>(needed, (uint64_t)persistent_grid<false, true>(sm_count));
+        raycast_kernel<false, true><<<grid, kTraceBlock, 0, st>>>(s.nodes, s.tris, s.node_count, d_rays, (uint32_t)n,
+                                                                  nullptr, d_counters, d_err, d_next, refill_at);
+    }
 }
 
 }  // namespace rt

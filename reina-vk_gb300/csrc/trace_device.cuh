@@ -21,7 +21,13 @@ namespace rt {
 #endif
 constexpr int kSmemStack = RT_SMEM_STACK;
 constexpr int kTotalStack = 64;          // == kMaxBvhDepth: one entry per BVH8 level at most
-constexpr uint32_t kMaxTraversalSteps = 1u << 22;
+// Watchdog: a ray's traversal ends with kErrStepLimit after this many steps (a node visit and its
+// triangle tests each).  Far above any finite traversal of a valid tree; a build may lower it
+// (-DRT_MAX_TRAVERSAL_STEPS=n) to exercise the error path on ordinary scenes.
+#ifndef RT_MAX_TRAVERSAL_STEPS
+#define RT_MAX_TRAVERSAL_STEPS (1u << 22)
+#endif
+constexpr uint32_t kMaxTraversalSteps = RT_MAX_TRAVERSAL_STEPS;
 
 constexpr uint32_t kErrStackOverflow = 1u;
 constexpr uint32_t kErrStepLimit = 2u;
@@ -516,83 +522,6 @@ __device__ __forceinline__ uint32_t trace_scene(const DeviceScene& sc, const Tra
         if (sc.inst_trav) return traverse_two_level<ANY, COUNT, REFINE, SS>(sc, r, stack, stride, hit, cnt);
     }
     return traverse<ANY, COUNT, REFINE, SS>(sc.nodes, sc.tris, r, stack, stride, hit, cnt);
-}
-
-// Persistent traversal with dynamic ray fetch (Aila and Laine, "Understanding the Efficiency of Ray
-// Traversal on GPUs", HPG 2009): every warp keeps 32 rays in flight; whenever at least `refill` lanes
-// have finished, those lanes take the next rays, so short rays do not idle their lane until the warp's
-// longest ray ends.  Rays are handed out from a warp-private chunk of kFetchChunk consecutive items,
-// refilled from the global counter `next` (one atomic per chunk, not per refill), which keeps the rays
-// of a warp close together in the input order.
-//   load(idx, ray) -> false if item idx has no ray to trace (then store is called at once with a miss)
-//   store(idx, hit, valid): called by all 32 lanes after every step; valid marks lanes that finished
-//   an item in that step (store may use warp-collective operations).
-// Requires blockDim.x to be a multiple of 32.
-#ifndef RT_FETCH_CHUNK
-#define RT_FETCH_CHUNK 128
-#endif
-constexpr uint32_t kFetchChunk = RT_FETCH_CHUNK;
-static_assert(kFetchChunk >= 32, "a chunk must cover a whole warp");
-
-template <bool ANY, bool COUNT, bool REFINE, class Load, class Store, int SS = kSmemStack>
-__device__ __forceinline__ uint32_t persistent_trace(const Bvh8Node* __restrict__ nodes, const TriRecord* __restrict__ tris,
-                                                     uint32_t node_count, uint32_t n, uint32_t* next, uint2* stack,
-                                                     int stride, int refill, Load load, Store store, TraceCounters& cnt) {
-    const uint32_t lane = threadIdx.x & 31u;
-    uint2 spill[kTotalStack - SS];
-    uint32_t err = 0;
-    bool has = false, exhausted = false;
-    uint32_t idx = 0;
-    uint32_t chunk_next = 0, chunk_end = 0;   // warp-uniform: the warp's unclaimed items [next, end)
-    TraceRay r;
-    TravState st;
-    Hit hit;
-    for (;;) {
-        const unsigned idle = __ballot_sync(0xFFFFFFFFu, !has);
-        const uint32_t n_idle = (uint32_t)__popc(idle);
-        if (!exhausted && n_idle >= (uint32_t)refill) {
-            const uint32_t rem = chunk_end - chunk_next;
-            uint32_t base = 0;
-            if (rem < n_idle) {   // the chunk runs out: the rest of it, then a fresh chunk
-                if (lane == 0) base = atomicAdd(next, kFetchChunk);
-                base = __shfl_sync(0xFFFFFFFFu, base, 0);
-            }
-            const uint32_t rank = (uint32_t)__popc(idle & ((1u << lane) - 1u));
-            bool fresh = false;
-            if (!has) {
-                idx = rank < rem ? chunk_next + rank : base + (rank - rem);
-                if (idx < n && (rank < rem || base < n)) {
-                    fresh = true;
-                    if (load(idx, r) && node_count) {
-                        trav_init(r, st, hit);
-                        has = true;
-                    } else {
-                        hit.prim = kMiss; hit.t = r.tmax; hit.u = 0.0f; hit.v = 0.0f;
-                    }
-                }
-            }
-            if (rem < n_idle) {
-                chunk_next = base + (n_idle - rem);
-                chunk_end = base + kFetchChunk;
-                if (base >= n) exhausted = true;
-                if (chunk_end > n) chunk_end = n > chunk_next ? n : chunk_next;
-            } else {
-                chunk_next += n_idle;
-            }
-            store(idx, hit, fresh && !has);   // items without a ray (or an empty scene) finish at once
-        }
-        if (exhausted && __ballot_sync(0xFFFFFFFFu, has) == 0u) break;
-        bool done = false;
-        if (has) {
-            done = trav_step<ANY, COUNT, SS>(nodes, tris, r, st, hit, stack, stride, spill, cnt, err);
-            if (done) {
-                trav_finish<REFINE>(nodes, tris, r, st, hit);
-                has = false;
-            }
-        }
-        store(idx, hit, done);
-    }
-    return err;
 }
 
 }  // namespace rt

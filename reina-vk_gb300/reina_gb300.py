@@ -34,6 +34,7 @@ RAY_CLOSEST = 0
 RAY_ANY = 1
 MISS = 0xFFFFFFFF
 ACCEL_AUTO, ACCEL_FLAT, ACCEL_TWO_LEVEL = 0, 1, 2
+REFILL_GRID = 255   # tuning.refill: one thread per ray (grid form); 0 = the default cooperative form
 
 RAY_DTYPE = np.dtype([("org", np.float32, 3), ("tmin", np.float32), ("dir", np.float32, 3), ("tmax", np.float32)])
 HIT_DTYPE = np.dtype([("prim", np.uint32), ("t", np.float32), ("u", np.float32), ("v", np.float32)])
@@ -149,7 +150,13 @@ class TonemappingPushConsts(C.Structure):
 
 
 class _RenderStats(C.Structure):
-    _fields_ = [("rays", C.c_uint64), ("shadow_rays", C.c_uint64), ("seconds", C.c_double)]
+    _fields_ = [("rays", C.c_uint64), ("shadow_rays", C.c_uint64), ("seconds", C.c_double),
+                ("nodes_visited", C.c_uint64), ("triangles_tested", C.c_uint64), ("shadow_nodes_visited", C.c_uint64),
+                ("shadow_triangles_tested", C.c_uint64), ("shaded_hits", C.c_uint64)]
+
+
+def _stats_dict(st: "_RenderStats") -> dict:
+    return {f[0]: getattr(st, f[0]) for f in _RenderStats._fields_}
 
 
 class _ServerOptions(C.Structure):
@@ -353,6 +360,7 @@ def load_library() -> C.CDLL:
         "reina_scene_set_emissive_build": (I32, [P, U32]),
         "reina_scene_export_emissive": (I32, [P, P, C.POINTER(U32), P, C.POINTER(U64), P]),
         "reina_device_kat": (I32, [P, C.c_int, P, U64, P]),
+        "reina_ctx_device_error": (I32, [P, P, C.POINTER(U32)]),
         "reina_scene_export_two_level": (I32, [P, P, P, C.POINTER(U32), C.POINTER(U32)]),
         "reina_scene_export_properties": (I32, [P, P, U32, C.POINTER(U32)]),
         "reina_scene_export_texture": (I32, [P, U32, C.POINTER(U32), C.POINTER(U32), P, U64]),
@@ -717,7 +725,7 @@ def render(ctx: Context, scene: Scene, pc: RtPushConsts, opts: RenderOptions, ac
     st = _RenderStats()
     _check(_lib.reina_render(ctx.handle, scene.handle, C.byref(pc), C.byref(opts), _ptr(accum), _ptr(samples),
                              C.byref(st)))
-    return accum, samples, {"rays": st.rays, "shadow_rays": st.shadow_rays, "seconds": st.seconds}
+    return accum, samples, _stats_dict(st)
 
 
 def render_device(ctx: Context, scene: Scene, pc: RtPushConsts, opts: RenderOptions, d_accum: int, d_samples: int = 0,
@@ -773,7 +781,7 @@ def render_batch(ctx: Context, jobs: list) -> dict:
     arr = _jobs_array(jobs, False)
     st = _RenderStats()
     _check(_lib.reina_render_batch(ctx.handle, arr, len(jobs), C.byref(st)))
-    return {"rays": st.rays, "shadow_rays": st.shadow_rays, "seconds": st.seconds}
+    return _stats_dict(st)
 
 
 class DeviceRenderJob:
@@ -787,7 +795,7 @@ def render_batch_device(ctx: Context, jobs: list, stream: int = 0) -> dict:
     arr = _jobs_array(jobs, True)
     st = _RenderStats()
     _check(_lib.reina_render_batch_device(ctx.handle, arr, len(jobs), C.c_void_p(stream), C.byref(st)))
-    return {"rays": st.rays, "shadow_rays": st.shadow_rays, "seconds": st.seconds}
+    return _stats_dict(st)
 
 
 def _status(st: _RequestStatus) -> dict:
@@ -963,6 +971,14 @@ class SaveSchedule:
 
 KAT_OFFSET, KAT_GGX_VNDF, KAT_EVAL_DISNEY, KAT_RANDOM, KAT_OFFSET_DIELECTRIC, KAT_SAMPLE_DISNEY = 0, 1, 2, 3, 4, 5
 KAT_DIFFUSE_REFLECTION, KAT_RANDOM_UNIT_VEC, KAT_SAMPLE_DISNEY_LOBE = 6, 7, 15
+
+
+def device_error(ctx: "Context", stream: int = 0) -> int:
+    """reina_ctx_device_error: the device error bits of the asynchronous calls queued on `stream` so far
+    (raises ReinaError REINA_ERR_DEVICE when any is set; the word is cleared either way)."""
+    out = C.c_uint32()
+    _check(_lib.reina_ctx_device_error(ctx.handle, C.c_void_p(stream), C.byref(out)))
+    return int(out.value)
 
 
 def device_kat(ctx: "Context", kind: int, records: np.ndarray) -> np.ndarray:

@@ -113,6 +113,41 @@ def tbn_from_normals(n: np.ndarray) -> np.ndarray:
     return np.concatenate([t, b, n], axis=1).astype(np.float32)
 
 
+def large_scene_desc(R, level: int = 8, seed: int = 1, light_emission=(17.0, 12.0, 4.0)) -> "SceneDesc":
+    """The large scene as a description (both the product and the oracle can build it)."""
+    geo = large_scene_geometry(R, level, seed)
+    (sv, si), (pv, pi), (lv, li) = geo
+    mats, face = large_scene_materials(R, si.size // 3, seed)
+    d = SceneDesc()
+    d.add_instance(d.add_object(sv, si, large_scene_tbn(R, level, seed), si), None, materials=mats, face_material=face)
+    d.add_instance(d.add_object(pv, pi), None, R.Material(material_idx=0, albedo=(0.5, 0.5, 0.5)))
+    d.add_instance(d.add_object(lv, li), None,
+                   R.Material(material_idx=0, albedo=(0.9, 0.9, 0.9), emission=light_emission, cull_backface=True))
+    return d
+
+
+LARGE_ENV = (0.3, 0.3, 0.35)
+
+
+def large_camera(R, W: int = 1920, H: int = 1080):
+    """The large scene's camera (1920x1080 frame of the render workload)."""
+    return R.camera_matrices((0.0, 0.4, 3.6), (0.0, -0.12, -1.0), (0.0, 1.0, 0.0), np.radians(40.0), W / H)
+
+
+def batch_scene_desc(R, index: int, seed: int = 1, n_mat: int = 256) -> "SceneDesc":
+    """Scene `index` of the batched workload as a description (see batch_scene)."""
+    p = batch_job_params(index, seed)
+    v, i, n = R.geodesic(p["frequency"], 0.1, 7919 * seed + index)
+    mats, face = large_scene_materials(R, i.size // 3, 7919 * seed + index, n_mat)
+    d = SceneDesc()
+    d.add_instance(d.add_object(v, i, tbn_from_normals(n), i), None, materials=mats, face_material=face)
+    _, (pv, pi), (lv, li) = large_scene_geometry_planes()
+    d.add_instance(d.add_object(pv, pi), None, R.Material(material_idx=0, albedo=(0.5, 0.5, 0.5)))
+    d.add_instance(d.add_object(lv, li), None,
+                   R.Material(material_idx=0, albedo=(0.9, 0.9, 0.9), emission=(17.0, 12.0, 4.0), cull_backface=True))
+    return d
+
+
 def large_scene(R, ctx, level: int = 8, seed: int = 1, light_emission=(17.0, 12.0, 4.0)):
     geo = large_scene_geometry(R, level, seed)
     scene = R.Scene(ctx)

@@ -13,7 +13,7 @@ def test_cache_round_trip_and_buckets(R, host_ctx, tmp_path):
     R.autotune_load(host_ctx, src)
     # 1,310,724 triangles -> bucket 20; 2,097,152 rays -> bucket 21; anything in [2^20, 2^21) matches
     t = R.autotune_lookup(host_ctx, R.TUNE_RAYCAST_CLOSEST, 1310724, 2097152)
-    assert t is not None and t["trace_block"] == 256 and t["trace_stack"] == 8 and t["refill"] == 0
+    assert t is not None and t["trace_block"] == 256 and t["trace_stack"] == 8 and t["refill"] == R.REFILL_GRID
     assert R.autotune_lookup(host_ctx, R.TUNE_RAYCAST_CLOSEST, (1 << 21) - 1, (1 << 22) - 1) is not None
     assert R.autotune_lookup(host_ctx, R.TUNE_RAYCAST_CLOSEST, 1 << 21, 2097152) is None
     assert R.autotune_lookup(host_ctx, R.TUNE_RAYCAST_ANY, 1310724, 2097152) is None
