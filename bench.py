@@ -326,6 +326,7 @@ def run_ours(args) -> dict | None:
         "clocks": clk,
         "wall_timed_s": wall,
     }
+    out["bvh_device_build"] = bvh_device_metrics(R, ctx, scene)
     if not args.no_render:
         out["render"] = render_metrics(R, ctx, torch, args.render_frames, scene)
     if args.instances > 0:
@@ -337,7 +338,7 @@ def run_ours(args) -> dict | None:
         out["batched"] = batch_metrics(R, ctx, torch, pool, setup_s, args.batch_mega_scenes)
         if args.serve_seconds > 0:
             out["served"] = serve_metrics(R, ctx, torch, pool, args.serve_seconds, args.serve_rate,
-                                          all_policies=args.serve_all_policies)
+                                          all_policies=args.serve_all_policies, lanes=args.serve_lanes)
         if args.serve_budget_seconds > 0:
             out["served_budget_bound"] = served_budget_bound(R, ctx, torch, args)
     if args.rmse_spp > 0:
@@ -608,7 +609,7 @@ def batch_metrics(R, ctx, torch, built, setup_s: float, mega_scenes: int) -> dic
 
 
 def serve_metrics(R, ctx, torch, pool, seconds: float, rate: float, all_policies: bool = False,
-                  budget_bytes: int = 120_000_000_000, plain: bool = True) -> dict:
+                  budget_bytes: int = 120_000_000_000, plain: bool = True, lanes: int = 0) -> dict:
     """The served workload: a seeded Poisson stream of requests (rate per second over `seconds`), each a
     scene of the pool with side/spp/depth drawn like the batched workload, submitted in real time (a)
     one request at a time to reina_render_device in arrival order (the plain form: the frame on the wave
@@ -673,7 +674,7 @@ def serve_metrics(R, ctx, torch, pool, seconds: float, rate: float, all_policies
     # handed to the first server and stay with it; the other policies run on servers of their own over
     # fresh copies)
     def serve(policy: str, scenes_pool) -> tuple[dict, bool]:
-        srv = R.Server(ctx, budget_bytes=budget_bytes, fifo=policy == "fifo", fair=policy == "fair")
+        srv = R.Server(ctx, budget_bytes=budget_bytes, fifo=policy == "fifo", fair=policy == "fair", wave_lanes=lanes)
         ids = [srv.add_scene(s) for s, _ in scenes_pool]
         outs = [np.zeros((r[3].height, r[3].width, 4), np.float32) for r in reqs]
         rids = [None] * n
@@ -701,7 +702,8 @@ def serve_metrics(R, ctx, torch, pool, seconds: float, rate: float, all_policies
                  "span_s": span, "completed": st["completed"], "failed": st["failed"], "waves": st["waves"],
                  "scene_uploads": st["scene_uploads"], "scene_evictions": st["scene_evictions"],
                  "peak_resident_gb": st["peak_resident_bytes"] / 1e9, "budget_gb": st["budget_bytes"] / 1e9,
-                 "reserved_gb": st["reserved_bytes"] / 1e9}, all(s == R.REQ_DONE for s in states))
+                 "reserved_gb": st["reserved_bytes"] / 1e9, "wave_lanes": lanes or R.SERVER_WAVE_LANES},
+                all(s == R.REQ_DONE for s in states))
 
     served, ok = serve("shortest", pool)   # the server's default policy (shortest first, aging 0.03)
     out = {"workload": f"Poisson {rate:g}/s for {seconds:g} s ({n} requests) over the {len(pool)}-scene pool, "
@@ -732,14 +734,31 @@ def served_budget_bound(R, ctx, torch, args) -> dict:
 
     pool = [scenes.batch_scene(R, ctx, k) for k in range(args.serve_budget_scenes)]
     scene_bytes = sum(int(sc.stats()["device_bytes"]) for sc, _ in pool)
-    probe = R.Server(ctx, budget_bytes=120_000_000_000)
+    probe = R.Server(ctx, budget_bytes=120_000_000_000, wave_lanes=args.serve_lanes)
     reserved = int(probe.stats()["reserved_bytes"])
     probe.close()
     budget = reserved + scene_bytes // 2
     out = serve_metrics(R, ctx, torch, pool, args.serve_budget_seconds, args.serve_rate, budget_bytes=budget,
-                        plain=False)
+                        plain=False, lanes=args.serve_lanes)
     out["pool_scene_gb"] = scene_bytes / 1e9
     return out
+
+
+def bvh_device_metrics(R, ctx, scene) -> dict:
+    """The workload's scene built again with the device BVH builder: wall time of both builders (the host
+    build is multithreaded C++ on every host core), the device build's kernel time, and whether the two
+    structures are byte-identical (nodes and triangle records)."""
+    import scenes
+
+    dev, _, _ = scenes.large_scene(R, ctx, 8, bvh=R.BVH_DEVICE)
+    sh, sd = scene.stats(), dev.stats()
+    hn, ht = scene.export_bvh()
+    dn, dt = dev.export_bvh()
+    same = bool(np.array_equal(hn, dn) and np.array_equal(ht, dt))
+    del dev
+    return {"host_s": sh["build_seconds"], "device_s": sd["build_seconds"],
+            "device_kernel_s": sd["bvh_kernel_seconds"], "speedup": sh["build_seconds"] / sd["build_seconds"],
+            "identical_bytes": same, "nodes": int(sd["node_count"]), "host_threads": os.cpu_count()}
 
 
 def rmse_metrics(R, ctx, spp: int) -> dict:
@@ -776,17 +795,29 @@ def cpu_baseline(tris, rays, sample: int) -> dict:
             "seconds": dt}
 
 
+def _oracle_workload():
+    """The ray-cast workload (same triangles and rays as the GPU arm, bit for bit) from the oracle's own
+    generators, so that the CPU arm loads no product code."""
+    import scenes
+    from oracle import oracle as O
+
+    v, i = O.icosphere(8, 0.1, 1)
+    _, plane, light = scenes.large_scene_geometry_planes()
+    tris = np.concatenate([scenes.world_triangles(a, b) for a, b in ((v, i), plane, light)])
+    lo, hi = v[:, :3].min(axis=0), v[:, :3].max(axis=0)
+    c, h = (lo + hi) / 2, (hi - lo) / 2 * 1.5
+    rays = O.raycast_rays(N_CAMERA_SIDE, N_CAMERA_SIDE, (0.0, 0.0, 3.0), (0.0, 0.0, 0.0), 45.0, N_RANDOM, c - h, c + h,
+                          seed=1)
+    return tris, rays
+
+
 def run_reference(args) -> dict | None:
     ws, rank, local = _dist()
     if rank != 0:
         return None
-    import build as pkg_build
-    import reina_gb300 as R
     from oracle import oracle as O
 
-    pkg_build.build()
-    ctx = R.Context(-1)   # host-only: scene assembly only, no GPU work
-    scene, tris, rays, _ = _build_workload(R, ctx)
+    tris, rays = _oracle_workload()
     sample = args.cpu_sample
     sub = np.ascontiguousarray(rays[:: max(1, rays.shape[0] // sample)][:sample])
     b = O.Bvh(tris)
@@ -848,6 +879,7 @@ def main() -> int:
     ap.add_argument("--serve-budget-seconds", type=float, default=30.0,
                     help="seconds of the stream served under a binding memory budget (0: skip)")
     ap.add_argument("--serve-budget-scenes", type=int, default=64)
+    ap.add_argument("--serve-lanes", type=int, default=0, help="server waves in flight (0: the server default)")
     ap.add_argument("--rmse-spp", type=int, default=4096, help="converged-image RMSE vs the FP64 oracle (0: skip)")
     ap.add_argument("--instances", type=int, default=256,
                     help="instances of the flat vs two-level instancing metrics (0 skips them)")

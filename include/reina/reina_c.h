@@ -73,7 +73,9 @@ int reina_ctx_sm_count(const reina_ctx* ctx);
  *            refinement over all 32 lanes; REINA_REFILL_GRID: one thread per ray (the grid form, the
  *            only form of two-level scenes, which use it whatever this field says).  On the
  *            1.3M-triangle ray cast (2,097,152 rays) closest hit 0.58 ms cooperative against 0.82 ms
- *            grid, any hit 0.36 against 0.51 ms.
+ *            grid, any hit 0.36 against 0.51 ms.  Ray casts only: the wavefront kernels of frames and
+ *            batches take wave_refill, whose default is the grid form (a 1920x1080 64-spp frame of that
+ *            scene 318 ms grid against 352 ms cooperative, a 256x256 Cornell room 2.48 against 3.79 ms).
  *   trace_block: threads per block of the grid-form traversal kernels (ray cast, wavefront extend and
  *            shadow): 64, 128 or 256 (default 128).  Grid form only.
  *   trace_stack: shared-memory traversal stack entries per thread, 8, 12 or 16 (default 12); deeper
@@ -92,8 +94,8 @@ int reina_ctx_sm_count(const reina_ctx* ctx);
  *            stays in L2 (on a 256-scene batch 9.06 s against 9.40 s for an equal share per job);
  *            REINA_BATCH_FAIR_SHARE gives every unfinished job an equal share of each wave instead.
  *            Neither changes an image.
- * Changing wave_paths, batch_flags, refill, trace_block or trace_stack releases the batch engine; the
- * next batched call rebuilds it. */
+ * Changing wave_paths, batch_flags, wave_refill, trace_block or trace_stack releases the batch engine; the
+ * next batched call rebuilds it.  The request server's engine uses the defaults. */
 typedef struct reina_tuning {
     uint32_t refill;
     uint32_t wave_paths;
@@ -103,7 +105,8 @@ typedef struct reina_tuning {
     uint32_t trace_order;        /* ray casts, grid form: REINA_ORDER_INPUT (default) or REINA_ORDER_COHERENT */
     uint32_t wave_lanes;         /* waves in flight in batched renders and frames, 1..16
                                   * (0 = REINA_DEFAULT_WAVE_LANES) */
-    uint32_t reserved;
+    uint32_t wave_refill;        /* launch form of the wavefront extension and shadow kernels (frames,
+                                  * batches): like `refill`, but 0 = the default REINA_REFILL_GRID */
 } reina_tuning;
 /* REINA_ORDER_INPUT traces ray i on thread i.  REINA_ORDER_COHERENT first bins the rays by direction
  * octant and origin cell (Morton order on an 8^3 grid over the origins' bounds) and traces them in that
@@ -225,6 +228,16 @@ int reina_scene_set_accel(reina_scene* scene, int mode);
 enum { REINA_EMISSIVE_HOST = 0, REINA_EMISSIVE_DEVICE = 1 };
 int reina_scene_set_emissive_build(reina_scene* scene, uint32_t where);
 
+/* Where reina_scene_build builds the triangle BVHs (the BLAS builds of src/graphics/Blas.cpp:41-113 and,
+ * for flat scenes, the whole-scene structure): REINA_BVH_HOST (default, multithreaded C++) or
+ * REINA_BVH_DEVICE, the scene's GPU (REINA_ERR_STATE at the build on a host-only context).  The top level
+ * of a two-level scene (instance boxes) is always built on the host.  Both builders run the same binned
+ * SAH, collapse and quantization with the same explicitly rounded arithmetic and write byte-identical
+ * nodes and triangle records.  `sah_bins`: bins per axis (0: 32; the device build takes 4..64);
+ * `median_depth`: binary depth from which every split is an object median (0: 48). */
+enum { REINA_BVH_HOST = 0, REINA_BVH_DEVICE = 1 };
+int reina_scene_set_bvh_build(reina_scene* scene, uint32_t where, uint32_t sah_bins, uint32_t median_depth);
+
 /* The packed emissive sampling data of a built scene (the buffers NEE reads, Instances.cpp:92-114): one
  * EmissiveInstanceData per emissive instance, the concatenated per-instance triangle CDFs and the
  * instance CDF.  Pass NULL arrays to get the counts first; a non-NULL array must hold its count. */
@@ -240,12 +253,15 @@ typedef struct reina_scene_stats {
     uint64_t device_bytes;       /* device memory held by the scene */
     uint32_t max_depth;          /* depth of the BVH8 tree (root = 1) */
     uint32_t leaf_triangles_max; /* largest triangle count of one leaf child (<= 3) */
-    double build_seconds;        /* host BVH build time */
+    double build_seconds;        /* wall time of the BVH build (host or device builder) */
     float bounds_min[3];
     float bounds_max[3];
     uint32_t two_level;          /* 1: top level over instances + bottom levels per model */
     uint32_t blas_count;         /* bottom-level BVHs (two-level scenes) */
     double emissive_seconds;     /* wall time of the emissive CDF build and its duplicate search */
+    uint32_t bvh_device;         /* 1: triangle BVHs built on the GPU (REINA_BVH_DEVICE) */
+    uint32_t pad0;
+    double bvh_kernel_seconds;   /* device builds: GPU time of their kernels (CUDA events) */
 } reina_scene_stats;
 int reina_scene_get_stats(const reina_scene* scene, reina_scene_stats* out_stats);
 

@@ -70,6 +70,32 @@ def rng(seed: int, n: int):
     return w, f, d
 
 
+_SHADING_SIGS["oracle_icosphere_counts"] = (None, [C.c_uint32, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)])
+_SHADING_SIGS["oracle_gen_icosphere"] = (None, [C.c_uint32, C.c_float, C.c_uint64, C.c_void_p, C.c_void_p])
+_SHADING_SIGS["oracle_gen_rays"] = (None, [C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_float, C.c_uint64,
+                                           C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p])
+
+
+def icosphere(level: int, amplitude: float = 0.0, seed: int = 1) -> tuple[np.ndarray, np.ndarray]:
+    """The synthetic displaced icosphere (oracle_gen.cpp): vertices (N, 4) and indices (3M,)."""
+    nv, nt = C.c_uint64(), C.c_uint64()
+    lib().oracle_icosphere_counts(level, C.byref(nv), C.byref(nt))
+    v = np.zeros((nv.value, 4), np.float32)
+    i = np.zeros(3 * nt.value, np.uint32)
+    lib().oracle_gen_icosphere(level, float(amplitude), seed, _p(v), _p(i))
+    return v, i
+
+
+def raycast_rays(width: int, height: int, cam_pos, cam_target, fovy_degrees: float, n_random: int, box_min, box_max,
+                 seed: int = 1) -> np.ndarray:
+    """The synthetic ray set (oracle_gen.cpp): camera rays then box rays, as RAY_DTYPE records."""
+    out = np.zeros(width * height + n_random, RAY_DTYPE)
+    f3 = lambda a: np.ascontiguousarray(a, np.float32).reshape(3)
+    cp, ct, lo, hi = f3(cam_pos), f3(cam_target), f3(box_min), f3(box_max)
+    lib().oracle_gen_rays(width, height, _p(cp), _p(ct), float(fovy_degrees), n_random, _p(lo), _p(hi), seed, _p(out))
+    return out
+
+
 _SHADING_SIGS["oracle_bvh8_raycast"] = (None, [C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p, C.c_uint64, C.c_int,
                                                C.c_int, C.c_void_p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)])
 

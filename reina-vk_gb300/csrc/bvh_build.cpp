@@ -1,4 +1,5 @@
-// Binned-SAH BVH build, 8-wide collapse and conservative 8-bit child-box quantization (host C++).
+// Binned-SAH BVH build, 8-wide collapse and conservative 8-bit child-box quantization (host C++).  The
+// arithmetic lives in bvh_sah.h, shared with the device builder (bvh_gpu.cu), which writes the same bytes.
 #include "bvh_build.h"
 
 #include <algorithm>
@@ -8,6 +9,8 @@
 #include <cstring>
 #include <stdexcept>
 #include <thread>
+
+#include "bvh_sah.h"
 
 namespace rt {
 namespace {
@@ -32,11 +35,7 @@ inline void grow(Box& b, const Box& o) {
     }
 }
 
-inline float half_area(const Box& b) {
-    float d[3];
-    for (int k = 0; k < 3; ++k) d[k] = std::max(0.0f, b.hi[k] - b.lo[k]);
-    return d[0] * d[1] + d[1] * d[2] + d[2] * d[0];
-}
+inline float half_area(const Box& b) { return sah::half_area(b.lo, b.hi); }
 
 struct BNode {
     Box box;
@@ -44,8 +43,6 @@ struct BNode {
     uint32_t first;   // leaf: first entry of the primitive index array
     uint32_t count;   // leaf: primitive count (0 for internal nodes)
 };
-
-constexpr int kForceMedianDepth = 48;   // past this depth splits are object medians (bounds the depth)
 
 struct BinaryBuilder {
     const float* verts = nullptr;
@@ -56,6 +53,7 @@ struct BinaryBuilder {
     std::atomic<uint32_t> next{1};
     std::atomic<int> spare_threads{0};
     int bins = 32;
+    int median_depth = sah::kForceMedianDepth;
 
     void range_bounds(uint32_t b, uint32_t e, Box& box, Box& cbox) const {
         box = empty_box();
@@ -77,17 +75,17 @@ struct BinaryBuilder {
         nodes[node].left = 0;
     }
 
-    // Splits idx[b, e) at its middle along the largest centroid axis (object median).
+    // Splits idx[b, e) at its middle along the largest centroid axis (object median; ties by index).
     uint32_t median_split(uint32_t b, uint32_t e, const Box& cbox) {
         int axis = 0;
         float best = -1.0f;
         for (int k = 0; k < 3; ++k) {
-            float ext = cbox.hi[k] - cbox.lo[k];
+            const float ext = sah::sub(cbox.hi[k], cbox.lo[k]);
             if (ext > best) { best = ext; axis = k; }
         }
         uint32_t mid = b + (e - b) / 2;
         std::nth_element(idx.begin() + b, idx.begin() + mid, idx.begin() + e, [&](uint32_t x, uint32_t y) {
-            float cx = centroid[3 * x + axis], cy = centroid[3 * y + axis];
+            const float cx = sah::median_key(centroid[3 * x + axis]), cy = sah::median_key(centroid[3 * y + axis]);
             return cx < cy || (cx == cy && x < y);
         });
         return mid;
@@ -101,7 +99,7 @@ struct BinaryBuilder {
         if (n <= 1) { make_leaf(node, b, e); return; }
 
         uint32_t mid = b;
-        if (depth >= kForceMedianDepth) {
+        if (depth >= median_depth) {
             if (n <= (uint32_t)kMaxLeafTris) { make_leaf(node, b, e); return; }
             mid = median_split(b, e, cbox);
         } else {
@@ -114,13 +112,13 @@ struct BinaryBuilder {
             std::vector<float> right_area(bins);
             std::vector<uint32_t> right_cnt(bins);
             for (int axis = 0; axis < 3; ++axis) {
-                const float lo = cbox.lo[axis], ext = cbox.hi[axis] - cbox.lo[axis];
-                if (!(ext > 0.0f)) continue;
-                const float scale = (float)bins / ext;
+                const float lo = cbox.lo[axis];
+                float scale;
+                if (!sah::bin_scale(lo, cbox.hi[axis], bins, scale)) continue;
                 for (int i = 0; i < bins; ++i) { bin_box[i] = empty_box(); bin_cnt[i] = 0; }
                 for (uint32_t i = b; i < e; ++i) {
                     uint32_t p = idx[i];
-                    int bi = std::min(bins - 1, (int)((centroid[3 * p + axis] - lo) * scale));
+                    const int bi = sah::bin_of(centroid[3 * p + axis], lo, scale, bins);
                     grow(bin_box[bi], prim_box[p]);
                     bin_cnt[bi]++;
                 }
@@ -138,7 +136,7 @@ struct BinaryBuilder {
                     grow(acc, bin_box[i]);
                     cnt += bin_cnt[i];
                     if (cnt == 0 || right_cnt[i + 1] == 0) continue;
-                    float cost = 1.0f + (half_area(acc) * cnt + right_area[i + 1] * right_cnt[i + 1]) / parent_area;
+                    const float cost = sah::split_cost(half_area(acc), cnt, right_area[i + 1], right_cnt[i + 1], parent_area);
                     if (cost < best_cost) { best_cost = cost; best_axis = axis; best_bin = i; }
                 }
             }
@@ -147,11 +145,11 @@ struct BinaryBuilder {
                 if (n <= (uint32_t)kMaxLeafTris) { make_leaf(node, b, e); return; }
                 mid = median_split(b, e, cbox);
             } else {
-                const float lo = cbox.lo[best_axis], ext = cbox.hi[best_axis] - cbox.lo[best_axis];
-                const float scale = (float)bins / ext;
+                const float lo = cbox.lo[best_axis];
+                float scale = 0.0f;
+                sah::bin_scale(lo, cbox.hi[best_axis], bins, scale);
                 auto it = std::partition(idx.begin() + b, idx.begin() + e, [&](uint32_t p) {
-                    int bi = std::min(bins - 1, (int)((centroid[3 * p + best_axis] - lo) * scale));
-                    return bi <= best_bin;
+                    return sah::bin_of(centroid[3 * p + best_axis], lo, scale, bins) <= best_bin;
                 });
                 mid = (uint32_t)(it - idx.begin());
                 if (mid == b || mid == e) mid = median_split(b, e, cbox);
@@ -172,13 +170,7 @@ struct BinaryBuilder {
     }
 };
 
-// SAH costs of the collapse: one node test = 1, one triangle test = 1 (Ylitie et al. use 0.3; on the
-// 1.3M-triangle ray cast 0.6-1.2 measured 2 % faster than 0.3, as fewer 3-triangle leaves are merged).
-#ifndef RT_COST_TRI
-#define RT_COST_TRI 1.0f
-#endif
-constexpr float kCostNode = 1.0f, kCostTri = RT_COST_TRI;
-constexpr uint32_t kLeafMax = 3;   // triangles per leaf child (3 bits of the node's meta byte)
+using sah::kLeafMax;
 
 struct WideBuilder {
     const BinaryBuilder& bb;
@@ -187,31 +179,18 @@ struct WideBuilder {
     int collapse = kCollapseSahDp;
     std::vector<uint32_t>* refs = nullptr;   // box mode: leaf entries are box indices appended here
 
-    // Dynamic-programme tables per binary node: cost[i] = cost of the subtree as at most i + 1 wide
-    // children; how[i] = 0 one leaf child, 1 one wide node, 2 split between the two binary children with
-    // left[i] slots on the left and used[i] slots in all.
-    struct Dp {
-        float cost[8];
-        uint8_t how[8], left[8], used[8];
-    };
-    std::vector<Dp> dp;
+    std::vector<sah::Dp> dp;
     std::vector<uint32_t> sub_first, sub_count;   // triangle range of every binary subtree
 
     bool is_leaf(uint32_t n) const { return bb.nodes[n].count > 0; }
 
     void solve(uint32_t n) {
         const BNode& b = bb.nodes[n];
-        Dp& d = dp[n];
         const float area = half_area(b.box);
         if (b.count > 0) {
             sub_first[n] = b.first;
             sub_count[n] = b.count;
-            for (int i = 0; i < 8; ++i) {
-                d.cost[i] = area * (float)b.count * kCostTri;
-                d.how[i] = 0;
-                d.left[i] = 0;
-                d.used[i] = 1;
-            }
+            sah::dp_leaf(dp[n], area, b.count);
             return;
         }
         const uint32_t l = b.left, r = b.left + 1;
@@ -219,42 +198,12 @@ struct WideBuilder {
         solve(r);
         sub_first[n] = std::min(sub_first[l], sub_first[r]);
         sub_count[n] = sub_count[l] + sub_count[r];
-        const Dp& L = dp[l];
-        const Dp& R = dp[r];
-        float dist[9];
-        uint8_t dist_k[9];
-        for (int j = 2; j <= 8; ++j) {
-            dist[j] = INFINITY;
-            dist_k[j] = 1;
-            for (int k = 1; k < j; ++k) {
-                const float c = L.cost[k - 1] + R.cost[j - k - 1];
-                if (c < dist[j]) { dist[j] = c; dist_k[j] = (uint8_t)k; }
-            }
-        }
-        const float leaf = sub_count[n] <= kLeafMax ? area * (float)sub_count[n] * kCostTri : INFINITY;
-        const float inner = dist[8] + area * kCostNode;
-        d.cost[0] = std::min(leaf, inner);
-        d.how[0] = leaf <= inner ? 0 : 1;
-        d.left[0] = 0;
-        d.used[0] = 1;
-        for (int i = 2; i <= 8; ++i) {
-            if (dist[i] < d.cost[i - 2]) {
-                d.cost[i - 1] = dist[i];
-                d.how[i - 1] = 2;
-                d.left[i - 1] = dist_k[i];
-                d.used[i - 1] = (uint8_t)i;
-            } else {
-                d.cost[i - 1] = d.cost[i - 2];
-                d.how[i - 1] = d.how[i - 2];
-                d.left[i - 1] = d.left[i - 2];
-                d.used[i - 1] = d.used[i - 2];
-            }
-        }
+        sah::dp_inner(dp[n], dp[l], dp[r], area, sub_count[n]);
     }
 
     // Wide children of binary subtree `n` given `slots`: (binary node, as one leaf child).
     void gather(uint32_t n, int slots, uint32_t* ch, bool* leaf, int& nch) const {
-        const Dp& d = dp[n];
+        const sah::Dp& d = dp[n];
         const int i = slots - 1;
         if (d.how[i] == 0) { ch[nch] = n; leaf[nch++] = true; return; }
         if (d.how[i] == 1) { ch[nch] = n; leaf[nch++] = false; return; }
@@ -282,14 +231,7 @@ struct WideBuilder {
             leaf[nch++] = true;
         } else if (collapse == kCollapseSahDp) {
             // The node itself is internal: distribute its subtree over 8 slots (dist(n, 8)).
-            const Dp& L = dp[bb.nodes[bn].left];
-            const Dp& R = dp[bb.nodes[bn].left + 1];
-            int best_k = 1;
-            float best = INFINITY;
-            for (int k = 1; k < 8; ++k) {
-                const float c = L.cost[k - 1] + R.cost[8 - k - 1];
-                if (c < best) { best = c; best_k = k; }
-            }
+            const int best_k = sah::dp_root_split(dp[bb.nodes[bn].left], dp[bb.nodes[bn].left + 1]);
             gather(bb.nodes[bn].left, best_k, ch, leaf, nch);
             gather(bb.nodes[bn].left + 1, 8 - best_k, ch, leaf, nch);
         } else {
@@ -315,61 +257,29 @@ struct WideBuilder {
             }
         }
 
-        // Union box and octant-based slot assignment (greedy maximum of dot(centroid - centre, dir_s)).
+        // Union box and octant-based slot assignment.
+        float clo[8][3], chi[8][3];
         Box u = empty_box();
-        for (int i = 0; i < nch; ++i) grow(u, bb.nodes[ch[i]].box);
-        float centre[3];
-        for (int k = 0; k < 3; ++k) centre[k] = 0.5f * (u.lo[k] + u.hi[k]);
-        int slot_of[8];
-        int child_in_slot[8];
-        for (int s = 0; s < 8; ++s) child_in_slot[s] = -1;
-        bool assigned[8] = {false, false, false, false, false, false, false, false};
-        for (int step = 0; step < nch; ++step) {
-            float best = -INFINITY;
-            int bc = -1, bs = -1;
-            for (int i = 0; i < nch; ++i) {
-                if (assigned[i]) continue;
-                const Box& cb = bb.nodes[ch[i]].box;
-                float c[3];
-                for (int k = 0; k < 3; ++k) c[k] = 0.5f * (cb.lo[k] + cb.hi[k]) - centre[k];
-                for (int s = 0; s < 8; ++s) {
-                    if (child_in_slot[s] >= 0) continue;
-                    float score = ((s & 1) ? c[0] : -c[0]) + ((s & 2) ? c[1] : -c[1]) + ((s & 4) ? c[2] : -c[2]);
-                    if (score > best) { best = score; bc = i; bs = s; }
-                }
+        for (int i = 0; i < nch; ++i) {
+            const Box& cb = bb.nodes[ch[i]].box;
+            grow(u, cb);
+            for (int k = 0; k < 3; ++k) {
+                clo[i][k] = cb.lo[k];
+                chi[i][k] = cb.hi[k];
             }
-            assigned[bc] = true;
-            slot_of[bc] = bs;
-            child_in_slot[bs] = bc;
         }
-        (void)slot_of;
+        int child_in_slot[8];
+        sah::assign_slots(nch, clo, chi, child_in_slot);
 
         Bvh8Node node;
         std::memset(&node, 0, sizeof(node));
-
-        // Quantization frame: p = union.lo - delta - slack, scale 2^e with 255 * 2^e >= extent + 2 delta
-        // + 2 slack, where slack = 2^-7 quanta.  The slack keeps every child's quantized box at least
-        // 2^-8 quanta outside its (delta-dilated) bounds without clamping at 0 or 255, which covers the
-        // extra rounding of the traversal's plane offsets (at most 2^-9 quanta, see intersect_children).
         double scale[3];
         float p[3];
         uint8_t ebias[3];
         for (int k = 0; k < 3; ++k) {
-            const double lo = (double)u.lo[k] - delta;
-            const double hi = (double)u.hi[k] + delta;
             int e = 0;
-            std::frexp((hi - lo) / 255.0, &e);
-            if (e < -126) e = -126;
-            float pf = 0.0f;
-            for (;;) {
-                if (e > kMaxQuantExponent) throw std::runtime_error("BVH build: scene coordinates out of range");
-                const double slack = std::ldexp(1.0, e - 7);
-                pf = (float)(lo - slack);
-                if ((double)pf > lo - slack) pf = std::nextafter(pf, -INFINITY);
-                if (std::ldexp(255.0, e) >= (hi + slack) - (double)pf) break;
-                ++e;
-            }
-            p[k] = pf;
+            if (!sah::quant_axis(u.lo[k], u.hi[k], delta, p[k], e))
+                throw std::runtime_error("BVH build: scene coordinates out of range");
             scale[k] = std::ldexp(1.0, e);
             ebias[k] = (uint8_t)(e + 127);
         }
@@ -393,12 +303,7 @@ struct WideBuilder {
             const BNode& c = bb.nodes[ch[ci]];
             const bool as_leaf = leaf[ci];
             auto q = [&](int k, float lo, float hi, uint8_t& qlo, uint8_t& qhi) {
-                double a = std::floor(((double)lo - delta - (double)p[k]) / scale[k] - 0.00390625);
-                double b = std::ceil(((double)hi + delta - (double)p[k]) / scale[k] + 0.00390625);
-                a = std::max(0.0, std::min(255.0, a));
-                b = std::max(0.0, std::min(255.0, b));
-                qlo = (uint8_t)a;
-                qhi = (uint8_t)b;
+                sah::quant_child(lo, hi, delta, p[k], scale[k], qlo, qhi);
             };
             q(0, c.box.lo[0], c.box.hi[0], node.qlo_x[s], node.qhi_x[s]);
             q(1, c.box.lo[1], c.box.hi[1], node.qlo_y[s], node.qhi_y[s]);
@@ -413,8 +318,11 @@ struct WideBuilder {
                 const uint32_t cnt = is_leaf(ch[ci]) ? c.count : sub_count[ch[ci]];   // 1..3
                 const uint32_t unary = (1u << cnt) - 1u;
                 node.meta[s] = (uint8_t)((unary << 5) | tri_off);
+                uint32_t prims[kLeafMax];   // a leaf child's triangles in ascending id order
+                for (uint32_t j = 0; j < cnt; ++j) prims[j] = bb.idx[first + j];
+                std::sort(prims, prims + cnt);
                 for (uint32_t j = 0; j < cnt; ++j) {
-                    uint32_t prim = bb.idx[first + j];
+                    const uint32_t prim = prims[j];
                     if (refs) {
                         refs->push_back(prim);
                         continue;
@@ -451,12 +359,13 @@ static Bvh8 build_core(std::vector<Box>&& boxes, double mag, const float* verts,
     BinaryBuilder bb;
     bb.verts = verts;
     bb.bins = std::max(4, std::min(256, opt.sah_bins));
+    bb.median_depth = opt.median_depth;
     bb.prim_box = std::move(boxes);
     bb.centroid.resize(3ull * n);
     bb.idx.resize(n);
     for (uint32_t i = 0; i < n; ++i) {
         const Box& b = bb.prim_box[i];
-        for (int k = 0; k < 3; ++k) bb.centroid[3ull * i + k] = 0.5f * (b.lo[k] + b.hi[k]);
+        for (int k = 0; k < 3; ++k) bb.centroid[3ull * i + k] = sah::centroid(b.lo[k], b.hi[k]);
         bb.idx[i] = i;
     }
     bb.nodes.resize(2ull * n);
@@ -465,9 +374,7 @@ static Bvh8 build_core(std::vector<Box>&& boxes, double mag, const float* verts,
     bb.build(0, 0, n, 0);
     out.binary_nodes = bb.next.load();
 
-    // Dilation of quantized boxes: 2^-18 of the scene's coordinate magnitude, which covers the float
-    // rounding of the slab test for ray origins within ~20x that magnitude.
-    double delta = std::ldexp(std::max(mag, 1e-20), -18);
+    const double delta = sah::quant_delta((float)mag);
     out.nodes.resize(1);
     if (!refs) out.tris.reserve(n);
     WideBuilder wb{bb, out, delta, opt.collapse, refs};

@@ -7,6 +7,7 @@
 #include <cstdint>
 #include <vector>
 
+#include "bvh_sah.h"
 #include "rt_common.h"
 
 namespace rt {
@@ -31,6 +32,7 @@ struct BvhBuildOptions {
     int sah_bins = 32;
     int max_threads = 0;           // 0 = std::thread::hardware_concurrency()
     int collapse = RT_COLLAPSE;
+    int median_depth = sah::kForceMedianDepth;   // binary depth from which every split is an object median
 };
 
 // `verts` holds 9 floats per triangle (v0, v1, v2 in world space); triangle i gets id i.
@@ -46,6 +48,13 @@ Bvh8 build_bvh8_boxes(const float* boxes6, uint64_t box_count, std::vector<uint3
 // Maximum BVH8 depth the traversal kernels accept (their stack holds one entry per level).
 constexpr uint32_t kMaxBvhDepth = 64;
 // Largest quantization exponent of a node (scale 2^e): the traversal forms 2^(e+15) in single precision.
-constexpr int kMaxQuantExponent = 110;
+constexpr int kMaxQuantExponent = sah::kMaxQuantExponent;
+
+// The same BVH8 built on the GPU `device` (bvh_gpu.cu): byte-identical nodes and triangle records for the
+// same input and options (SAH collapse only, at most 64 bins).  `kernel_seconds` receives the device
+// time of the build kernels.  Synchronous.
+Bvh8 build_bvh8_device(int device, const float* verts, uint64_t tri_count, const BvhBuildOptions& opt = BvhBuildOptions(),
+                       double* kernel_seconds = nullptr);
+constexpr int kMaxDeviceSahBins = 64;
 
 }  // namespace rt

@@ -39,7 +39,13 @@ struct reina_ctx {
     rt::DeviceBuffer counters;   // u64 x 2 traversal counters
     rt::DeviceBuffer fetch;      // ring of u32 ray-fetch counters, one per ray-cast launch in flight
     std::atomic<uint32_t> fetch_slot{0};
-    rt::TraceConfig trace;       // traversal launch configuration (reina_tuning)
+    rt::TraceConfig trace;       // ray-cast traversal launch configuration (reina_tuning)
+    rt::TraceConfig wave_trace = wave_default();   // the wavefront kernels' (reina_tuning.wave_refill)
+    static rt::TraceConfig wave_default() {
+        rt::TraceConfig c;
+        c.refill = rt::kDefaultWaveRefill;
+        return c;
+    }
     uint32_t* next_fetch_counter() { return fetch.as<uint32_t>() + (fetch_slot.fetch_add(1) % kFetchSlots); }
     static constexpr uint32_t kFetchSlots = 256;
     rt::DeviceBuffer rays, hits; // staging for host-buffer ray casts
@@ -162,8 +168,12 @@ rt::TraceConfig trace_for(const reina_ctx* ctx, uint32_t kind, uint64_t triangle
     if (ctx->autotune_mode == REINA_AUTOTUNE_CACHED &&
         ctx->tune.get(kind, rt::tune_bucket(triangles), rt::tune_bucket(size), &e))
         return e.trace;
-    return ctx->trace;
+    return kind == rt::kTuneRender || kind == rt::kTuneBatch ? ctx->wave_trace : ctx->trace;
 }
+
+// reina_tuning's refill fields <-> TraceConfig::refill (0 = grid form).
+int refill_from_abi(uint32_t v, int dflt) { return v == 0 ? dflt : (v == REINA_REFILL_GRID ? 0 : (int)v); }
+uint32_t refill_to_abi(int r) { return r == 0 ? (uint32_t)REINA_REFILL_GRID : (uint32_t)r; }
 
 }  // namespace
 
@@ -227,20 +237,27 @@ int reina_ctx_set_tuning(reina_ctx* ctx, const reina_tuning* t) {
     return guard([&] {
         need(ctx && t, "NULL argument");
         need(t->refill <= 32 || t->refill == REINA_REFILL_GRID, "refill must be in 0..32 or REINA_REFILL_GRID");
+        need(t->wave_refill <= 32 || t->wave_refill == REINA_REFILL_GRID,
+             "wave_refill must be in 0..32 or REINA_REFILL_GRID");
         need((t->batch_flags & ~(uint32_t)(REINA_BATCH_NO_GRAPHS | REINA_BATCH_FAIR_SHARE)) == 0, "unknown batch flags");
         need(t->wave_lanes <= 16, "wave_lanes must be in 0..16");
         const uint32_t lanes = t->wave_lanes ? t->wave_lanes : (uint32_t)REINA_DEFAULT_WAVE_LANES;
         const uint32_t wave = t->wave_paths ? t->wave_paths : (uint32_t)REINA_DEFAULT_WAVE_PATHS;
         need(wave <= (1u << 26), "wave_paths must be at most 2^26");
         rt::TraceConfig tc;
-        tc.refill = t->refill == 0 ? rt::kDefaultRefill : (t->refill == REINA_REFILL_GRID ? 0 : (int)t->refill);
+        tc.refill = refill_from_abi(t->refill, rt::kDefaultRefill);
         tc.block = (int)(t->trace_block ? t->trace_block : rt::kTraceBlock);
         tc.stack = (int)(t->trace_stack ? t->trace_stack : rt::kDefaultTraceStack);
         need(t->trace_order <= REINA_ORDER_COHERENT, "trace_order must be REINA_ORDER_INPUT or REINA_ORDER_COHERENT");
         tc.sort = t->trace_order == REINA_ORDER_COHERENT ? 1 : 0;
         need(rt::valid_trace_config(tc), "trace_block must be 64, 128 or 256 and trace_stack 8, 12 or 16");
-        const bool engine_changed = tc.block != ctx->trace.block || tc.stack != ctx->trace.stack || tc.refill != ctx->trace.refill;
+        rt::TraceConfig wc = tc;
+        wc.refill = refill_from_abi(t->wave_refill, rt::kDefaultWaveRefill);
+        wc.sort = 0;
+        const bool engine_changed = wc.block != ctx->wave_trace.block || wc.stack != ctx->wave_trace.stack ||
+                                    wc.refill != ctx->wave_trace.refill;
         ctx->trace = tc;
+        ctx->wave_trace = wc;
         if (wave != ctx->wave_paths || t->batch_flags != ctx->batch_flags || lanes != ctx->wave_lanes || engine_changed) {
             if (ctx->batch && ctx->device >= 0) check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
             ctx->batch.reset();
@@ -255,7 +272,8 @@ int reina_ctx_get_tuning(const reina_ctx* ctx, reina_tuning* out) {
     return guard([&] {
         need(ctx && out, "NULL argument");
         std::memset(out, 0, sizeof(*out));
-        out->refill = ctx->trace.refill == 0 ? (uint32_t)REINA_REFILL_GRID : (uint32_t)ctx->trace.refill;
+        out->refill = refill_to_abi(ctx->trace.refill);
+        out->wave_refill = refill_to_abi(ctx->wave_trace.refill);
         out->trace_block = (uint32_t)ctx->trace.block;
         out->trace_stack = (uint32_t)ctx->trace.stack;
         out->trace_order = ctx->trace.sort ? REINA_ORDER_COHERENT : REINA_ORDER_INPUT;
@@ -343,6 +361,8 @@ int reina_scene_get_stats(const reina_scene* scene, reina_scene_stats* out) {
         out->two_level = s.two_level() ? 1u : 0u;
         out->blas_count = s.blas_count();
         out->emissive_seconds = s.emissive_seconds();
+        out->bvh_device = s.bvh_on_device() ? 1u : 0u;
+        out->bvh_kernel_seconds = s.bvh_kernel_seconds();
     });
 }
 
@@ -358,6 +378,22 @@ int reina_scene_set_emissive_build(reina_scene* scene, uint32_t where) {
         need(scene && scene->s, "NULL argument");
         need(where <= REINA_EMISSIVE_DEVICE, "where must be REINA_EMISSIVE_HOST or REINA_EMISSIVE_DEVICE");
         scene->s->set_emissive_on_device(where == REINA_EMISSIVE_DEVICE);
+    });
+}
+
+int reina_scene_set_bvh_build(reina_scene* scene, uint32_t where, uint32_t sah_bins, uint32_t median_depth) {
+    return guard([&] {
+        need(scene && scene->s, "NULL argument");
+        need(where <= REINA_BVH_DEVICE, "where must be REINA_BVH_HOST or REINA_BVH_DEVICE");
+        need(sah_bins == 0 || (sah_bins >= 4 && sah_bins <= 256), "sah_bins must be 0 or 4..256");
+        static_assert(rt::kMaxDeviceSahBins == 64, "message below");
+        need(where == REINA_BVH_HOST || sah_bins <= (uint32_t)rt::kMaxDeviceSahBins,
+             "the device BVH build takes at most 64 SAH bins");
+        need(median_depth <= 1024, "median_depth must be at most 1024");
+        rt::BvhBuildOptions opt;
+        if (sah_bins) opt.sah_bins = (int)sah_bins;
+        if (median_depth) opt.median_depth = (int)median_depth;
+        scene->s->set_bvh_build(where == REINA_BVH_DEVICE, opt);
     });
 }
 
@@ -637,7 +673,7 @@ static uint32_t fit_wave(uint32_t wave, uint64_t samples) {
 static rt::BatchEngine& batch_engine(reina_ctx* ctx, const reina_render_job* jobs, uint32_t count,
                                      const rt::TraceConfig* force) {
     uint32_t wave = ctx->wave_paths;
-    rt::TraceConfig trace = ctx->trace;
+    rt::TraceConfig trace = ctx->wave_trace;
     rt::TuneEntry e;
     uint64_t tris = 0, samples = 0;
     batch_key(jobs, count, &tris, &samples);
@@ -1029,9 +1065,13 @@ double time_calls(cudaStream_t st, int reps, F&& fn) {
     return ms[ms.size() / 2];
 }
 
-void fill_tuning(const reina_ctx* ctx, const rt::TuneEntry& e, reina_tuning* t) {
+// An autotuned entry as tuning fields: its launch form is the ray casts' (refill) for ray-cast kinds and
+// the wavefront kernels' (wave_refill) for renders and batches; the other field is the context's.
+void fill_tuning(const reina_ctx* ctx, uint32_t kind, const rt::TuneEntry& e, reina_tuning* t) {
     std::memset(t, 0, sizeof(*t));
-    t->refill = e.trace.refill == 0 ? (uint32_t)REINA_REFILL_GRID : (uint32_t)e.trace.refill;
+    const bool wave = kind == rt::kTuneRender || kind == rt::kTuneBatch;
+    t->refill = refill_to_abi(wave ? ctx->trace.refill : e.trace.refill);
+    t->wave_refill = refill_to_abi(wave ? e.trace.refill : ctx->wave_trace.refill);
     t->trace_block = (uint32_t)e.trace.block;
     t->trace_stack = (uint32_t)e.trace.stack;
     t->trace_order = e.trace.sort ? REINA_ORDER_COHERENT : REINA_ORDER_INPUT;
@@ -1046,7 +1086,7 @@ void finish_tune(reina_ctx* ctx, uint32_t kind, uint64_t tris, uint64_t size, co
     ctx->tune.put(kind, tb, sb, best);
     if (out) {
         std::memset(out, 0, sizeof(*out));
-        fill_tuning(ctx, best, &out->best);
+        fill_tuning(ctx, kind, best, &out->best);
         out->best_ms = best.best_ms;
         out->default_ms = best.default_ms;
         out->candidates = candidates;
@@ -1056,8 +1096,10 @@ void finish_tune(reina_ctx* ctx, uint32_t kind, uint64_t tris, uint64_t size, co
     }
 }
 
-bool is_default(const rt::TraceConfig& c) {
-    return c.refill == rt::kDefaultRefill && c.block == rt::kTraceBlock && c.stack == rt::kDefaultTraceStack && c.sort == 0;
+// The default launch configuration of a tuning kind (ray casts: cooperative; renders and batches: grid).
+bool is_default(const rt::TraceConfig& c, uint32_t kind) {
+    const int refill = kind == rt::kTuneRender || kind == rt::kTuneBatch ? rt::kDefaultWaveRefill : rt::kDefaultRefill;
+    return c.refill == refill && c.block == rt::kTraceBlock && c.stack == rt::kDefaultTraceStack && c.sort == 0;
 }
 
 }  // namespace
@@ -1085,7 +1127,7 @@ int reina_autotune_raycast(reina_ctx* ctx, const reina_scene* scene, const void*
                                    c, st);
                 check_cuda(cudaGetLastError(), "raycast launch");
             });
-            if (is_default(c)) best.default_ms = ms;
+            if (is_default(c, flags == REINA_RAY_ANY ? rt::kTuneRaycastAny : rt::kTuneRaycastClosest)) best.default_ms = ms;
             if (ms < best.best_ms) {
                 best.best_ms = ms;
                 best.trace = c;
@@ -1124,7 +1166,7 @@ int reina_autotune_render(reina_ctx* ctx, const reina_scene* scene, const RtPush
                 else   // the default form: the frame as the wave engine's one job
                     render_on_engine(ctx, scene, &one, o, r, ctx->accum.get(), nullptr, false, st, nullptr);
             });
-            if (is_default(c)) best.default_ms = ms;
+            if (is_default(c, rt::kTuneRender)) best.default_ms = ms;
             if (ms < best.best_ms) {
                 best.best_ms = ms;
                 best.trace = c;
@@ -1165,7 +1207,7 @@ int reina_autotune_batch(reina_ctx* ctx, const reina_render_job* jobs, uint32_t 
             sub[k].samples_rgb32f = nullptr;
         }
         const uint32_t saved_wave = ctx->wave_paths;
-        const rt::TraceConfig saved_trace = ctx->trace;
+        const rt::TraceConfig saved_trace = ctx->wave_trace;
         const uint32_t saved_mode = ctx->autotune_mode;
         ctx->autotune_mode = REINA_AUTOTUNE_OFF;
         cudaStream_t st = ctx->streams[0];
@@ -1180,15 +1222,15 @@ int reina_autotune_batch(reina_ctx* ctx, const reina_render_job* jobs, uint32_t 
                     waves.push_back(fit_wave(w, samples));
             const uint32_t default_wave = fit_wave(REINA_DEFAULT_WAVE_PATHS, samples);
             for (uint32_t wave : waves)
-                for (int refill : {rt::kDefaultRefill, 0}) {   // the cooperative form, the grid form
+                for (int refill : {rt::kDefaultWaveRefill, rt::kDefaultRefill}) {   // the grid form, the cooperative form
                     rt::TraceConfig c;
                     c.refill = refill;
                     ctx->wave_paths = wave;
-                    ctx->trace = c;
+                    ctx->wave_trace = c;
                     ctx->batch.reset();
                     const double ms = time_calls(st, 1, [&] { render_batch(ctx, sub.data(), n, false, st, nullptr); });
                     ++cands;
-                    if (is_default(c) && wave == default_wave) best.default_ms = ms;
+                    if (is_default(c, rt::kTuneBatch) && wave == default_wave) best.default_ms = ms;
                     if (ms < best.best_ms) {
                         best.best_ms = ms;
                         best.trace = c;
@@ -1197,20 +1239,20 @@ int reina_autotune_batch(reina_ctx* ctx, const reina_render_job* jobs, uint32_t 
                 }
         } catch (...) {
             ctx->wave_paths = saved_wave;
-            ctx->trace = saved_trace;
+            ctx->wave_trace = saved_trace;
             ctx->autotune_mode = saved_mode;
             ctx->batch.reset();
             throw;
         }
         ctx->wave_paths = saved_wave;
-        ctx->trace = saved_trace;
+        ctx->wave_trace = saved_trace;
         ctx->autotune_mode = saved_mode;
         ctx->batch.reset();
         // the subset holds only a few waves of the larger sizes, so near-ties between them are noise:
         // the default stays unless another candidate is at least 2 % faster
         if (best.default_ms > 0 && best.best_ms > 0.98 * best.default_ms) {
             best.best_ms = best.default_ms;
-            best.trace = rt::TraceConfig();
+            best.trace = reina_ctx::wave_default();
             best.wave_paths = fit_wave(REINA_DEFAULT_WAVE_PATHS, samples);
         }
         finish_tune(ctx, rt::kTuneBatch, tris, samples, best, cands, out);
@@ -1232,7 +1274,7 @@ int reina_autotune_lookup(reina_ctx* ctx, uint32_t kind, uint64_t triangles, uin
         need(kind <= REINA_TUNE_BATCH, "unknown tune kind");
         rt::TuneEntry e;
         *found = ctx->tune.get(kind, rt::tune_bucket(triangles), rt::tune_bucket(size), &e) ? 1 : 0;
-        if (*found) fill_tuning(ctx, e, out);
+        if (*found) fill_tuning(ctx, kind, e, out);
         else std::memset(out, 0, sizeof(*out));
     });
 }

@@ -173,7 +173,11 @@ __device__ __forceinline__ void coop_store_finished(CoopWarp& S, uint32_t lane, 
 // at launch); a warp refills its idle lanes once at most `refill_at` lanes still trace.  Requires
 // blockDim.x to be a multiple of 32; `stack` points at this thread's first shared stack entry, entries
 // `stride` apart.  Returns the device error bits of the warp's rays.
-template <bool ANY, bool COUNT, bool REFINE, bool MIXED, int SS, class Load, class Store>
+// CHUNK, FLUSH: the fetch chunk and the triangle flush size; INNER: node visits per round of the warp's
+// bookkeeping (a lane whose visit found no leaf triangles takes another step while at least CONT lanes
+// can), 1 = one visit per round.
+template <bool ANY, bool COUNT, bool REFINE, bool MIXED, int SS, uint32_t CHUNK = kCoopChunk, uint32_t FLUSH = kFlushTris,
+          int INNER = 1, int CONT = 16, class Load, class Store>
 __device__ __forceinline__ uint32_t coop_trace(const CoopScene& uniform, uint32_t n, uint32_t* next, uint32_t refill_at,
                                                CoopWarp& S, uint2* stack, int stride, Load load, Store store,
                                                TraceCounters& cnt) {
@@ -203,7 +207,7 @@ __device__ __forceinline__ uint32_t coop_trace(const CoopScene& uniform, uint32_
             const uint32_t rem = chunk_end - chunk_next;
             uint32_t base = 0;
             if (rem < n_idle) {
-                if (lane == 0) base = atomicAdd(next, kCoopChunk);
+                if (lane == 0) base = atomicAdd(next, CHUNK);
                 base = __shfl_sync(0xFFFFFFFFu, base, 0);
             }
             bool empty_item = false;
@@ -234,7 +238,7 @@ __device__ __forceinline__ uint32_t coop_trace(const CoopScene& uniform, uint32_
             }
             if (rem < n_idle) {
                 chunk_next = base + (n_idle - rem);
-                chunk_end = base + kCoopChunk;
+                chunk_end = base + CHUNK;
                 if (base >= n) exhausted = true;
                 if (chunk_end > n) chunk_end = n > chunk_next ? n : chunk_next;
             } else {
@@ -261,31 +265,43 @@ __device__ __forceinline__ uint32_t coop_trace(const CoopScene& uniform, uint32_
             if (exhausted) break;
             continue;
         }
-        // one node visit per tracing lane
+        // one node visit per tracing lane (INNER > 1: more while the lane finds no leaf triangles)
         uint32_t tbase = 0, tmask = 0;
-        if (has && group.y > 0x00FFFFFFu) {
-            if (++steps > kMaxTraversalSteps) {
-                err |= kErrStepLimit;
-                group = make_uint2(0u, 0u);
-                sp = 0;
-            } else {
-                const uint32_t slot_bit = 31u - __clz(group.y);
-                const uint32_t slot = (slot_bit - 24u) ^ r.oct_inv;
-                const uint32_t child = group.x + (uint32_t)__popc(group.y & ((1u << slot) - 1u));
-                group.y &= ~(1u << slot_bit);
-                if (group.y > 0x00FFFFFFu) {
-                    if (sp < SS) stack[sp * stride] = group;
-                    else if (sp < kTotalStack) spill[sp - SS] = group;
-                    else err |= kErrStackOverflow;
-                    if (sp < kTotalStack) ++sp;
+#pragma unroll 1
+        for (int it = 0; it < INNER; ++it) {
+            if (has && tmask == 0u && group.y > 0x00FFFFFFu) {
+                if (++steps > kMaxTraversalSteps) {
+                    err |= kErrStepLimit;
+                    group = make_uint2(0u, 0u);
+                    sp = 0;
+                } else {
+                    const uint32_t slot_bit = 31u - __clz(group.y);
+                    const uint32_t slot = (slot_bit - 24u) ^ r.oct_inv;
+                    const uint32_t child = group.x + (uint32_t)__popc(group.y & ((1u << slot) - 1u));
+                    group.y &= ~(1u << slot_bit);
+                    if (group.y > 0x00FFFFFFu) {
+                        if (sp < SS) stack[sp * stride] = group;
+                        else if (sp < kTotalStack) spill[sp - SS] = group;
+                        else err |= kErrStackOverflow;
+                        if (sp < kTotalStack) ++sp;
+                    }
+                    const uint4* np = reinterpret_cast<const uint4*>(MIXED ? sc.nodes : uniform.nodes) + 5ull * child;
+                    const uint4 w0 = __ldg(np + 0), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3),
+                                w4 = __ldg(np + 4);
+                    if (COUNT) cnt.nodes++;
+                    const uint32_t hm = intersect_children(r, w0, w1, w2, w3, w4, best_t);
+                    group = make_uint2(w1.x, (hm & 0xFF000000u) | (w0.w >> 24));
+                    tbase = w1.y;
+                    tmask = hm & 0x00FFFFFFu;
                 }
-                const uint4* np = reinterpret_cast<const uint4*>(MIXED ? sc.nodes : uniform.nodes) + 5ull * child;
-                const uint4 w0 = __ldg(np + 0), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3), w4 = __ldg(np + 4);
-                if (COUNT) cnt.nodes++;
-                const uint32_t hm = intersect_children(r, w0, w1, w2, w3, w4, best_t);
-                group = make_uint2(w1.x, (hm & 0xFF000000u) | (w0.w >> 24));
-                tbase = w1.y;
-                tmask = hm & 0x00FFFFFFu;
+            }
+            if (INNER > 1 && it + 1 < INNER) {
+                if (has && tmask == 0u && group.y <= 0x00FFFFFFu && sp > 0) {
+                    --sp;
+                    group = sp < SS ? stack[sp * stride] : spill[sp - SS];
+                }
+                const bool more = has && tmask == 0u && group.y > 0x00FFFFFFu;
+                if (__popc(__ballot_sync(0xFFFFFFFFu, more)) < CONT) break;
             }
         }
         // the node's leaf triangles join the warp's list
@@ -306,7 +322,7 @@ __device__ __forceinline__ uint32_t coop_trace(const CoopScene& uniform, uint32_
         }
         // test the list when it is full enough, could overflow next step, or holds groups of a finished lane
         const bool waiting = has && group.y <= 0x00FFFFFFu && sp == 0 && my_groups > 0;
-        if (n_groups && (__any_sync(0xFFFFFFFFu, waiting) || n_tris >= kFlushTris || n_groups > 32u)) {
+        if (n_groups && (__any_sync(0xFFFFFFFFu, waiting) || n_tris >= FLUSH || n_groups > 32u)) {
             __syncwarp();
             coop_test_groups<COUNT, MIXED>(S, lane, n_groups, utris, cnt);
             n_groups = 0;

@@ -397,6 +397,15 @@ bool Scene::use_two_level() const {
     return invertible && tri_total_ >= 2 * unique;
 }
 
+// A triangle BVH on the host or on the scene's GPU (same bytes either way).
+Bvh8 Scene::build_triangles(const float* verts, uint64_t tri_count) {
+    if (!bvh_device_) return build_bvh8(verts, tri_count, bvh_opt_);
+    double k = 0.0;
+    Bvh8 b = build_bvh8_device(device_, verts, tri_count, bvh_opt_, &k);
+    bvh_kernel_seconds_ += k;
+    return b;
+}
+
 // One BVH over all instances' world-space triangles.
 void Scene::build_flat() {
     std::vector<float> world(9 * tri_total_);
@@ -423,7 +432,7 @@ void Scene::build_flat() {
             }
         }
     }
-    bvh_ = build_bvh8(world.data(), tri_total_);
+    bvh_ = build_triangles(world.data(), tri_total_);
     inst_trav_.clear();
     tlas_refs_.clear();
     blas_count_ = 0;
@@ -509,7 +518,7 @@ void Scene::build_two_level() {
         for (size_t t = 0; t < ntri; ++t)
             for (int j = 0; j < 3; ++j)
                 for (int k = 0; k < 3; ++k) tris[9 * t + 3 * j + k] = md.vertices[4 * md.indices[3 * t + j] + k];
-        Bvh8 b = build_bvh8(tris.data(), ntri);
+        Bvh8 b = build_triangles(tris.data(), ntri);
         const uint32_t node_base = (uint32_t)out.nodes.size(), tri_base = (uint32_t)out.tris.size();
         if (b.nodes.empty()) {   // a model without triangles: no bottom level (its instances have empty boxes)
             blas_of[o] = -1;
@@ -546,6 +555,8 @@ void Scene::build(bool require_emissive) {
     if (built_) fail(REINA_ERR_STATE, "Cannot call build more than once");
     const bool host_only = device_ < 0;
     if (!host_only) check_cuda(cudaSetDevice(device_), "cudaSetDevice");
+    if (host_only && bvh_device_) fail(REINA_ERR_STATE, "device BVH build requested on a host-only context");
+    bvh_kernel_seconds_ = 0.0;
 
     const int64_t ntex = (int64_t)textures_.size();
     for (const InstanceProperties& p : props_)

@@ -70,6 +70,15 @@ public:
     void set_emissive_on_device(bool on) { emissive_device_ = on; }
     bool emissive_on_device() const { return emissive_device_; }
     double emissive_seconds() const { return emissive_seconds_; }
+    // Where build() builds the triangle BVHs (the flat BVH, or every bottom level of a two-level scene;
+    // the top level over instance boxes stays on the host): the host (default) or the scene's GPU
+    // (bvh_gpu.cu); both give the same bytes.  `opt` carries the SAH bin count and the median depth.
+    void set_bvh_build(bool on_device, const BvhBuildOptions& opt) {
+        bvh_device_ = on_device;
+        bvh_opt_ = opt;
+    }
+    bool bvh_on_device() const { return bvh_device_; }
+    double bvh_kernel_seconds() const { return bvh_kernel_seconds_; }
     bool two_level() const { return two_level_; }
     uint32_t blas_count() const { return blas_count_; }
     const std::vector<InstanceTrav>& instance_records() const { return inst_trav_; }
@@ -136,6 +145,10 @@ private:
     // Two-level acceleration structure
     int accel_mode_ = REINA_ACCEL_AUTO;
     bool emissive_device_ = false;
+    bool bvh_device_ = false;
+    BvhBuildOptions bvh_opt_;
+    double bvh_kernel_seconds_ = 0.0;
+    Bvh8 build_triangles(const float* verts, uint64_t tri_count);
     double emissive_seconds_ = 0.0;
     std::vector<uint8_t> emissive_same_;   // device build: pairwise same-CDF table of the emissive instances
     bool two_level_ = false;

@@ -43,7 +43,9 @@ Server::Server(int device, int sm_count, const ServerConfig& cfg) : device_(devi
         check_cuda(cudaMemPoolCreate(&pool_, &props), "cudaMemPoolCreate");
         uint64_t keep = cfg_.budget;   // freed memory stays in the pool up to the budget
         check_cuda(cudaMemPoolSetAttribute(pool_, cudaMemPoolAttrReleaseThreshold, &keep), "cudaMemPoolSetAttribute");
-        engine_ = std::make_unique<BatchEngine>(device_, sm_count, wave, cfg_.graphs, TraceConfig(), (int)lanes);
+        TraceConfig trace;
+        trace.refill = kDefaultWaveRefill;
+        engine_ = std::make_unique<BatchEngine>(device_, sm_count, wave, cfg_.graphs, trace, (int)lanes);
     } catch (...) {   // the destructor does not run for a constructor that throws
         engine_.reset();
         if (pool_) cudaMemPoolDestroy(pool_);

@@ -77,7 +77,8 @@ class _SceneStats(C.Structure):
         ("node_bytes", C.c_uint64), ("triangle_bytes", C.c_uint64), ("device_bytes", C.c_uint64),
         ("max_depth", C.c_uint32), ("leaf_triangles_max", C.c_uint32), ("build_seconds", C.c_double),
         ("bounds_min", C.c_float * 3), ("bounds_max", C.c_float * 3), ("two_level", C.c_uint32),
-        ("blas_count", C.c_uint32), ("emissive_seconds", C.c_double),
+        ("blas_count", C.c_uint32), ("emissive_seconds", C.c_double), ("bvh_device", C.c_uint32),
+        ("pad0", C.c_uint32), ("bvh_kernel_seconds", C.c_double),
     ]
 
 
@@ -88,10 +89,11 @@ class _CtxOptions(C.Structure):
 class _Tuning(C.Structure):
     _fields_ = [("refill", C.c_uint32), ("wave_paths", C.c_uint32), ("batch_flags", C.c_uint32),
                 ("trace_block", C.c_uint32), ("trace_stack", C.c_uint32), ("trace_order", C.c_uint32),
-                ("wave_lanes", C.c_uint32), ("reserved", C.c_uint32)]
+                ("wave_lanes", C.c_uint32), ("wave_refill", C.c_uint32)]
 
 
-TUNING_FIELDS = ("refill", "wave_paths", "batch_flags", "trace_block", "trace_stack", "trace_order", "wave_lanes")
+TUNING_FIELDS = ("refill", "wave_paths", "batch_flags", "trace_block", "trace_stack", "trace_order", "wave_lanes",
+                 "wave_refill")
 ORDER_INPUT, ORDER_COHERENT = 0, 1
 
 
@@ -120,6 +122,7 @@ EMISSIVE_INSTANCE_DTYPE = np.dtype([
     ("indexOffset", "<u4"), ("emission", "<f4", 3), ("weight", "<f4"), ("area", "<f4"), ("cullBackface", "<u4"),
     ("padding", "<f4", 2)])
 EMISSIVE_HOST, EMISSIVE_DEVICE = 0, 1
+BVH_HOST, BVH_DEVICE = 0, 1
 
 
 class RtPushConsts(C.Structure):
@@ -358,6 +361,7 @@ def load_library() -> C.CDLL:
         "reina_scene_texture_count": (I32, [P, C.POINTER(U32)]),
         "reina_scene_set_accel": (I32, [P, C.c_int]),
         "reina_scene_set_emissive_build": (I32, [P, U32]),
+        "reina_scene_set_bvh_build": (I32, [P, U32, U32, U32]),
         "reina_scene_export_emissive": (I32, [P, P, C.POINTER(U32), P, C.POINTER(U64), P]),
         "reina_device_kat": (I32, [P, C.c_int, P, U64, P]),
         "reina_ctx_device_error": (I32, [P, P, C.POINTER(U32)]),
@@ -622,6 +626,11 @@ class Scene:
     def set_emissive_build(self, where: int) -> None:
         """EMISSIVE_HOST (default) or EMISSIVE_DEVICE: where build() computes the emissive CDFs."""
         _check(_lib.reina_scene_set_emissive_build(self._h, where))
+
+    def set_bvh_build(self, where: int, sah_bins: int = 0, median_depth: int = 0) -> None:
+        """BVH_HOST (default) or BVH_DEVICE: where build() builds the triangle BVHs (same bytes either way);
+        sah_bins / median_depth 0 keep the defaults (32 bins, object medians from depth 48)."""
+        _check(_lib.reina_scene_set_bvh_build(self._h, where, sah_bins, median_depth))
 
     def export_emissive(self) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
         """(EmissiveInstanceData records, concatenated triangle CDFs, instance CDF) of the built scene."""

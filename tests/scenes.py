@@ -148,9 +148,11 @@ def batch_scene_desc(R, index: int, seed: int = 1, n_mat: int = 256) -> "SceneDe
     return d
 
 
-def large_scene(R, ctx, level: int = 8, seed: int = 1, light_emission=(17.0, 12.0, 4.0)):
+def large_scene(R, ctx, level: int = 8, seed: int = 1, light_emission=(17.0, 12.0, 4.0), bvh=None):
     geo = large_scene_geometry(R, level, seed)
     scene = R.Scene(ctx)
+    if bvh is not None:   # R.BVH_HOST or R.BVH_DEVICE
+        scene.set_bvh_build(bvh)
     (sv, si), (pv, pi), (lv, li) = geo
     sid = scene.define_object(sv, si, tbns=large_scene_tbn(R, level, seed), tbn_indices=si)
     mats, face = large_scene_materials(R, si.size // 3, seed)

@@ -113,3 +113,28 @@ def test_autotune_render_and_batch(R):
         sc.close()
     finally:
         ctx.close()
+
+
+def test_wave_refill_forms_give_identical_images(R):
+    """The wavefront extension and shadow kernels in the grid form (the default) and the cooperative form
+    (wave_refill 4, 8, 16): the same frame, bit for bit, through the wave engine and pass by pass."""
+    ctx = R.Context(0)
+    try:
+        d = scenes.material_zoo(R)
+        sc = d.to_product(R, ctx)
+        W, H = 80, 56
+        iv, ip = scenes.cornell_camera(R, W, H)
+        pc = R.push_consts(iv, ip, total_emissive_weight=sc.emissive_weight, spp=4, max_bounces=6, focus_dist=3.4)
+        assert ctx.tuning()["wave_refill"] == R.REFILL_GRID and ctx.tuning()["refill"] == 8
+        ref = None
+        for wr in (0, 4, 8, 16):
+            ctx.set_tuning(wave_refill=wr)
+            for pbp in (False, True):
+                out, _, st = R.render(ctx, sc, pc, R.render_options(W, H, R.MODE_NEE_MIS, 5, pass_by_pass=pbp))
+                if ref is None:
+                    ref = out
+                assert np.array_equal(out, ref), (wr, pbp)
+        ctx.set_tuning(wave_refill=0)
+        sc.close()
+    finally:
+        ctx.close()

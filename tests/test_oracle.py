@@ -143,3 +143,22 @@ def test_bloom_spreads_nan_like_the_reference(O):
     K = int(40 * 5.0 / 100 * 3 + 0.5)
     assert np.isnan(comb[4, 20 - K:20 + K + 1, 0]).all()
     assert not np.isnan(comb[4, 20 + K + 1:, 0]).any()
+
+
+@pytest.mark.parametrize("level,amp,seed", [(0, 0.0, 1), (3, 0.1, 1), (6, 0.1, 1), (5, 0.25, 9)])
+def test_oracle_icosphere_equals_product(R, O, level, amp, seed):
+    """The oracle's own generator of the ray-cast workload (used by the timed CPU arm, which loads no
+    product code) writes the product generator's bits."""
+    v, i, _ = R.icosphere(level, amp, seed)
+    ov, oi = O.icosphere(level, amp, seed)
+    assert np.array_equal(v.view(np.uint32), ov.view(np.uint32))
+    assert np.array_equal(np.asarray(i).reshape(-1), oi)
+
+
+def test_oracle_rays_equal_product(R, O):
+    v, _ = O.icosphere(4, 0.1, 1)
+    lo, hi = v[:, :3].min(axis=0), v[:, :3].max(axis=0)
+    c, h = (lo + hi) / 2, (hi - lo) / 2 * 1.5
+    a = R.raycast_rays(96, 64, (0.0, 0.0, 3.0), (0.0, 0.0, 0.0), 45.0, 20000, c - h, c + h, seed=1)
+    b = O.raycast_rays(96, 64, (0.0, 0.0, 3.0), (0.0, 0.0, 0.0), 45.0, 20000, c - h, c + h, seed=1)
+    assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
