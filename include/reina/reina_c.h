@@ -372,9 +372,10 @@ typedef struct reina_render_stats {
     uint64_t rays;               /* closest-hit rays traced (path segments) */
     uint64_t shadow_rays;        /* any-hit shadow rays traced */
     double seconds;              /* wall time of the call */
-    /* traversal work of the cooperative extension and shadow kernels (flat scenes; 0 where a frame ran the
-     * grid form or the megakernel): BVH8 nodes visited and triangles tested by the path segments and by
-     * the shadow rays, and the hits shaded by a material kernel */
+    /* traversal work of the wave engine's extension and shadow kernels (0 where a frame ran pass by pass or
+     * as the megakernel): BVH8 nodes visited and triangles tested by the path segments and by the shadow
+     * rays, and the hits shaded by a material kernel.  A call that fills these runs the counting kernels
+     * of its traversal form (the same traversal, so the same image). */
     uint64_t nodes_visited;
     uint64_t triangles_tested;
     uint64_t shadow_nodes_visited;

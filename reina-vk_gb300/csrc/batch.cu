@@ -92,12 +92,14 @@ __global__ void __launch_bounds__(kBlock) kb_init(BatchLaunch B, const JobGpu* _
     }
 }
 
-template <int BLOCK, int SS, bool TWO>
+// COUNT: the traversal work (nodes visited, triangles tested) is added to the wave's counters.
+template <int BLOCK, int SS, bool TWO, bool COUNT = false>
 __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) kb_extend(BatchLaunch B, const JobGpu* __restrict__ jobs, int cur) {
     __shared__ uint2 stack[SS * BLOCK];
     const PathState& ps = B.bp.ps;
     const uint32_t n = ps.counters[kCntActive + cur];
     const uint32_t* q = ps.q_active[cur];
+    TraceCounters c{0u, 0u};
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         const uint32_t i = base + threadIdx.x;
         const bool active = i < n;
@@ -108,9 +110,8 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) kb_extend(BatchLaunch B, 
             const DeviceScene& s = jobs[B.bp.job[p]].s;
             const TraceRay r = make_trace_ray(ps.ox[p], ps.oy[p], ps.oz[p], ps.dx[p], ps.dy[p], ps.dz[p], 0.0f, 10000.0f);
             Hit h;
-            TraceCounters c{0u, 0u};
             uint32_t e = 0;
-            if (s.node_count) e = trace_scene<false, false, true, SS, TWO>(s, r, stack + threadIdx.x, BLOCK, h, c);
+            if (s.node_count) e = trace_scene<false, COUNT, true, SS, TWO>(s, r, stack + threadIdx.x, BLOCK, h, c);
             else h.prim = kMiss;
             if (e) atomicOr(ps.counters + kCntError, e);
             ps.hprim[p] = h.prim;
@@ -119,6 +120,7 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) kb_extend(BatchLaunch B, 
             m = h.prim == kMiss ? kQueueMiss : 1 + (int)s.props_material[prim_props_of(s, h.prim)];
         }
         warp_count64(reinterpret_cast<unsigned long long*>(ps.counters + kCntRays), active);
+        if (COUNT) warp_count64(reinterpret_cast<unsigned long long*>(ps.counters + kCntShaded), active && m != kQueueMiss);
 #pragma unroll
         for (int k = 0; k < kNumQueues; ++k) {
             const bool mine = active && m == k;
@@ -126,6 +128,7 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) kb_extend(BatchLaunch B, 
             if (mine) ps.q_shade[(size_t)k * B.P + checked_index(pos, B.P, ps.counters + kCntError)] = p;
         }
     }
+    if (COUNT) coop_add_counts(c, ps.counters, kCntNodes, kCntTris);
 }
 
 // Cooperative persistent form of the extension kernel (coop_trace.cuh; waves of flat scenes): warps
@@ -267,11 +270,12 @@ __global__ void __launch_bounds__(kBlock) kb_shade_miss(BatchLaunch B, const Job
     }
 }
 
-template <int BLOCK, int SS, bool TWO>
+template <int BLOCK, int SS, bool TWO, bool COUNT = false>
 __global__ void __launch_bounds__(BLOCK) kb_shadow(BatchLaunch B, const JobGpu* __restrict__ jobs) {
     __shared__ uint2 stack[SS * BLOCK];
     const PathState& ps = B.bp.ps;
     const uint32_t n = ps.counters[kCntShadow];
+    TraceCounters c{0u, 0u};
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         const uint32_t i = base + threadIdx.x;
         const bool active = i < n;
@@ -281,15 +285,15 @@ __global__ void __launch_bounds__(BLOCK) kb_shadow(BatchLaunch B, const JobGpu* 
             const TraceRay r = make_trace_ray(ps.s_ox[i], ps.s_oy[i], ps.s_oz[i], ps.s_dx[i], ps.s_dy[i], ps.s_dz[i], 0.0f,
                                               ps.s_tmax[i]);
             Hit h;
-            TraceCounters c{0u, 0u};
             uint32_t e = 0;
-            if (s.node_count) e = trace_scene<true, false, false, SS, TWO>(s, r, stack + threadIdx.x, BLOCK, h, c);
+            if (s.node_count) e = trace_scene<true, COUNT, false, SS, TWO>(s, r, stack + threadIdx.x, BLOCK, h, c);
             else h.prim = kMiss;
             if (e) atomicOr(ps.counters + kCntError, e);
             if (h.prim == kMiss) store_rad(ps, p, load_rad(ps, p) + V3{ps.s_cr[i], ps.s_cg[i], ps.s_cb[i]});
         }
         warp_count64(reinterpret_cast<unsigned long long*>(ps.counters + kCntShadowRays), active);
     }
+    if (COUNT) coop_add_counts(c, ps.counters, kCntShadowNodes, kCntShadowTris);
 }
 
 // Cooperative persistent form of the shadow kernel (waves of flat scenes).
@@ -521,7 +525,13 @@ void BatchEngine::launch_body(Lane& L, const Packed& pk, cudaStream_t st) {
     B.P = capacity_;
     uint32_t* cnt = B.bp.ps.counters;
     const int simple = std::min<int>(blocks_simple_, (int)((capacity_ + kBlock - 1) / kBlock));
-    const bool any_nee = pk.any_nee, two = pk.two;
+    const bool any_nee = pk.any_nee, two = pk.two, count = count_;
+    if (count && blocks_ext_cnt_ == 0) {   // grids of the counting kernels (default block and stack)
+        blocks_ext_cnt_ = resident_grid((const void*)kb_extend<kTraceBlock, kDefaultTraceStack, false, true>, kTraceBlock, sm_count_);
+        blocks_sh_cnt_ = resident_grid((const void*)kb_shadow<kTraceBlock, kDefaultTraceStack, false, true>, kTraceBlock, sm_count_);
+        blocks_ext_two_cnt_ = resident_grid((const void*)kb_extend<kTraceBlock, kDefaultTraceStack, true, true>, kTraceBlock, sm_count_);
+        blocks_sh_two_cnt_ = resident_grid((const void*)kb_shadow<kTraceBlock, kDefaultTraceStack, true, true>, kTraceBlock, sm_count_);
+    }
     auto sequence = [&](cudaStream_t s) {
         check_cuda(cudaMemsetAsync(cnt, 0, kNumCounters * sizeof(uint32_t), s), "cudaMemsetAsync");
         kb_init<<<simple, kBlock, 0, s>>>(B, B.jobs);
@@ -531,10 +541,14 @@ void BatchEngine::launch_body(Lane& L, const Packed& pk, cudaStream_t st) {
             check_cuda(cudaMemsetAsync(cnt + kCntQueue, 0, 6 * sizeof(uint32_t), s), "cudaMemsetAsync");
             if (!two && trace_.refill > 0)
                 check_cuda(cudaMemsetAsync(cnt + kCntFetchExtend, 0, 2 * sizeof(uint32_t), s), "cudaMemsetAsync");
-            if (two)   // a two-level scene in the wave: the default grid variant, both traversals
+            if (two && count)
+                kb_extend<kTraceBlock, kDefaultTraceStack, true, true><<<blocks_ext_two_cnt_, kTraceBlock, 0, s>>>(B, B.jobs, cur);
+            else if (two)   // a two-level scene in the wave: the default grid variant, both traversals
                 kb_extend<kTraceBlock, kDefaultTraceStack, true><<<blocks_ext_two_, kTraceBlock, 0, s>>>(B, B.jobs, cur);
             else if (trace_.refill > 0)
                 kb_extend_coop<<<blocks_ext_, kTraceBlock, 0, s>>>(B, B.jobs, cur, (uint32_t)(32 - trace_.refill));
+            else if (count)
+                kb_extend<kTraceBlock, kDefaultTraceStack, false, true><<<blocks_ext_cnt_, kTraceBlock, 0, s>>>(B, B.jobs, cur);
             else
                 with_trace_variant(trace_, [&](auto BS, auto SS) {
                     kb_extend<BS.value, SS.value, false><<<blocks_ext_, BS.value, 0, s>>>(B, B.jobs, cur);
@@ -544,10 +558,14 @@ void BatchEngine::launch_body(Lane& L, const Packed& pk, cudaStream_t st) {
             kb_shade<2><<<blocks_shade_[2], kBlock, 0, s>>>(B, B.jobs, cur);
             kb_shade<3><<<blocks_shade_[3], kBlock, 0, s>>>(B, B.jobs, cur);
             kb_shade<4><<<blocks_shade_[4], kBlock, 0, s>>>(B, B.jobs, cur);
-            if (any_nee && two)
+            if (any_nee && two && count)
+                kb_shadow<kTraceBlock, kDefaultTraceStack, true, true><<<blocks_sh_two_cnt_, kTraceBlock, 0, s>>>(B, B.jobs);
+            else if (any_nee && two)
                 kb_shadow<kTraceBlock, kDefaultTraceStack, true><<<blocks_sh_two_, kTraceBlock, 0, s>>>(B, B.jobs);
             else if (any_nee && trace_.refill > 0)
                 kb_shadow_coop<<<blocks_sh_, kTraceBlock, 0, s>>>(B, B.jobs, (uint32_t)(32 - trace_.refill));
+            else if (any_nee && count)
+                kb_shadow<kTraceBlock, kDefaultTraceStack, false, true><<<blocks_sh_cnt_, kTraceBlock, 0, s>>>(B, B.jobs);
             else if (any_nee)
                 with_trace_variant(trace_, [&](auto BS, auto SS) {
                     kb_shadow<BS.value, SS.value, false><<<blocks_sh_, BS.value, 0, s>>>(B, B.jobs);
@@ -562,7 +580,7 @@ void BatchEngine::launch_body(Lane& L, const Packed& pk, cudaStream_t st) {
     }
     GraphSlot* slot = nullptr;
     for (auto& g : L.graphs)
-        if (g.bounces == h.max_bounces && g.nee == any_nee && g.two == two) slot = &g;
+        if (g.bounces == h.max_bounces && g.nee == any_nee && g.two == two && g.count == count) slot = &g;
     if (!slot) {
         cudaStream_t cap;
         check_cuda(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking), "cudaStreamCreate");
@@ -575,6 +593,7 @@ void BatchEngine::launch_body(Lane& L, const Packed& pk, cudaStream_t st) {
         g.bounces = h.max_bounces;
         g.nee = any_nee;
         g.two = two;
+        g.count = count;
         check_cuda(cudaGraphInstantiate(&g.exec, graph, 0), "cudaGraphInstantiate");
         cudaGraphDestroy(graph);
         L.graphs.push_back(g);

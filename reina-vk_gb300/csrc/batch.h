@@ -122,9 +122,12 @@ public:
     const TraceConfig& trace() const { return trace_; }
     uint64_t rays() const { return rays_; }
     uint64_t shadow_rays() const { return shadow_rays_; }
-    // traversal work counted by the cooperative kernels (nodes, triangles of closest and any-hit rays,
-    // shaded hits) over the waves collected so far
+    // traversal work (nodes, triangles of closest and any-hit rays, shaded hits) over the waves collected
+    // so far: counted by the cooperative kernels always, and by the grid-form kernels while counting is on
     const RenderStats& work() const { return work_; }
+    // Counting on: waves launched from now on run the grid form's counting kernels (default block size and
+    // stack depth; the same traversal, so the same images) where they would run the grid form.
+    void set_counting(bool on) { count_ = on; }
     uint32_t waves() const { return waves_; }
 
 private:
@@ -132,6 +135,7 @@ private:
         uint32_t bounces = 0;
         bool nee = false;
         bool two = false;   // the wave holds a two-level scene
+        bool count = false; // counting kernels (traversal work)
         cudaGraphExec_t exec = nullptr;
     };
     struct Lane {
@@ -172,6 +176,8 @@ private:
     uint64_t submitted_ = 0, retired_ = 0;   // waves launched / waited for
     int blocks_ext_ = 0, blocks_shade_[5] = {0, 0, 0, 0, 0}, blocks_sh_ = 0, blocks_simple_ = 0;
     int blocks_ext_two_ = 0, blocks_sh_two_ = 0;
+    int blocks_ext_cnt_ = 0, blocks_sh_cnt_ = 0, blocks_ext_two_cnt_ = 0, blocks_sh_two_cnt_ = 0;
+    bool count_ = false;
 };
 
 }  // namespace rt

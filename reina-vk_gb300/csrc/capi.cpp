@@ -759,6 +759,12 @@ static void render_batch(reina_ctx* ctx, const reina_render_job* jobs, uint32_t 
     }
     const uint64_t r0 = eng.rays(), s0 = eng.shadow_rays();
     const rt::RenderStats w0 = eng.work();
+    // a call that returns statistics counts the traversal work of every form
+    struct Counting {
+        rt::BatchEngine& e;
+        Counting(rt::BatchEngine& eng, bool on) : e(eng) { e.set_counting(on); }
+        ~Counting() { e.set_counting(false); }
+    } counting(eng, stats != nullptr);
     eng.run_all(ptrs, st, (ctx->batch_flags & REINA_BATCH_FAIR_SHARE) == 0);
     if (host) {
         for (uint32_t k = 0; k < count; ++k) {

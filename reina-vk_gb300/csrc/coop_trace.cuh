@@ -83,9 +83,11 @@ __device__ __forceinline__ void coop_add_counts(const TraceCounters& c, uint32_t
 }
 
 // Tests the collected triangle groups, one (ray, triangle) pair per lane per round.  MIXED: each lane's ray
-// has its own scene (S.tris); otherwise every ray uses `tris`.
+// has its own scene (S.tris); otherwise every ray uses `tris`.  Not inlined, like coop_store_finished: both
+// run once per several traversal steps, and kept out of the traversal loop they leave it more registers
+// (1.3M-triangle ray cast: 0.566 -> 0.534 ms, the loop's register copies moved off the ALU pipe).
 template <bool COUNT, bool MIXED>
-__device__ __forceinline__ void coop_test_groups(CoopWarp& S, uint32_t lane, uint32_t n_groups, const float4* tris,
+__device__ __noinline__ void coop_test_groups(CoopWarp& S, uint32_t lane, uint32_t n_groups, const float4* tris,
                                                  TraceCounters& cnt) {
     const uint32_t c0 = lane < n_groups ? __popc(S.gmo[lane] & 0x00FFFFFFu) : 0u;
     const uint32_t c1 = lane + 32u < n_groups ? __popc(S.gmo[lane + 32u] & 0x00FFFFFFu) : 0u;
@@ -139,7 +141,7 @@ __device__ __forceinline__ void coop_test_groups(CoopWarp& S, uint32_t lane, uin
 
 // Refines (REFINE) and stores the finished rays of the list, one per lane; store is called by all lanes.
 template <bool REFINE, bool MIXED, class Store>
-__device__ __forceinline__ void coop_store_finished(CoopWarp& S, uint32_t lane, uint32_t n_fin, const float4* tris,
+__device__ __noinline__ void coop_store_finished(CoopWarp& S, uint32_t lane, uint32_t n_fin, const float4* tris,
                                                     Store& store) {
     __syncwarp();
     const bool valid = lane < n_fin;

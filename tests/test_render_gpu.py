@@ -166,3 +166,35 @@ def test_pass_by_pass_equals_wave_engine(R, gpu_ctx, mode, sample_batch):
     assert np.array_equal(out[0][0], out[1][0], equal_nan=True)
     assert np.array_equal(out[0][1], out[1][1], equal_nan=True)
     assert out[0][2]["rays"] == out[1][2]["rays"] and out[0][2]["shadow_rays"] == out[1][2]["shadow_rays"]
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_render_stats_count_traversal_work(R, gpu_ctx, mode):
+    """A frame whose call returns statistics runs the counting kernels of its traversal form: the traversal
+    work (nodes, triangles of segments and shadow rays, shaded hits) is reported, the counts repeat from
+    call to call, and the image equals the one of the device entry point, which does not count."""
+    torch = pytest.importorskip("torch")
+    d = scenes.material_zoo(R)
+    scene = d.to_product(R, gpu_ctx)
+    W, H = 96, 64
+    iv, ip = scenes.cornell_camera(R, W, H)
+    pc = R.push_consts(iv, ip, total_emissive_weight=scene.emissive_weight, spp=3, max_bounces=6, focus_dist=3.4)
+    opts = R.render_options(W, H, mode, 5)
+    acc1, _, st1 = R.render(gpu_ctx, scene, pc, opts)
+    acc2, _, st2 = R.render(gpu_ctx, scene, pc, opts)
+    keys = ("rays", "shadow_rays", "nodes_visited", "triangles_tested", "shadow_nodes_visited",
+            "shadow_triangles_tested", "shaded_hits")
+    assert all(st1[k] == st2[k] for k in keys), (st1, st2)
+    assert st1["nodes_visited"] >= st1["rays"] > 0
+    assert st1["triangles_tested"] > 0
+    assert 0 < st1["shaded_hits"] <= st1["rays"]
+    if mode == 1:
+        assert st1["shadow_nodes_visited"] >= st1["shadow_rays"] > 0
+    else:
+        assert st1["shadow_rays"] == 0 and st1["shadow_nodes_visited"] == 0
+    d_acc = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    R.render_device(gpu_ctx, scene, pc, opts, d_acc.data_ptr(), 0, stream)
+    torch.cuda.synchronize()
+    assert np.array_equal(acc1, acc2, equal_nan=True)
+    assert np.array_equal(d_acc.cpu().numpy(), acc1, equal_nan=True)
