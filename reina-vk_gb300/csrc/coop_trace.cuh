@@ -7,8 +7,10 @@
 //   * refill (Aila and Laine, "Understanding the Efficiency of Ray Traversal on GPUs", HPG 2009): when at
 //     most `refill_at` lanes still trace, the idle lanes take the next rays from a warp-private chunk of
 //     the global fetch counter;
-//   * node visits: every tracing lane visits its nearest pending child node each step (the step of
-//     trace_device.cuh: box test of the 8 quantized children, near-to-far order by ray octant);
+//   * node visits: every tracing lane visits its nearest pending child node (the step of trace_device.cuh:
+//     box test of the 8 quantized children, near-to-far order by ray octant), kCoopVisits times between
+//     two rounds of the warp's bookkeeping (refill, list tests, finishing), so that the bookkeeping is
+//     paid once per several visits;
 //   * triangle tests: a node's leaf triangles are not tested by the lane that found them; the warp
 //     collects (ray, triangle group) pairs in a shared list and, once it holds kFlushTris triangles (or a
 //     lane with groups in the list has no nodes left), tests them with one (ray, triangle) pair per lane,
@@ -55,6 +57,12 @@ constexpr uint32_t kCoopChunk = 32;
 // shared memory each, 210 KB per SM).
 constexpr int kCoopMinBlocks = 7;
 constexpr uint32_t kFlushTris = 24;    // triangles collected before the warp tests them
+// Node visits per lane per round of bookkeeping (1.3M-triangle ray cast, closest hit: 1 visit 0.539 ms,
+// 2 visits 0.505 ms with 0.7 % more node visits, 3 visits 0.556 ms, 4 visits 0.620 ms).
+#ifndef RT_COOP_VISITS
+#define RT_COOP_VISITS 2
+#endif
+constexpr int kCoopVisits = RT_COOP_VISITS;
 
 __device__ __forceinline__ uint32_t coop_ordered(float f) {
     const uint32_t b = __float_as_uint(f);
@@ -175,11 +183,11 @@ __device__ __noinline__ void coop_store_finished(CoopWarp& S, uint32_t lane, uin
 // at launch); a warp refills its idle lanes once at most `refill_at` lanes still trace.  Requires
 // blockDim.x to be a multiple of 32; `stack` points at this thread's first shared stack entry, entries
 // `stride` apart.  Returns the device error bits of the warp's rays.
-// CHUNK, FLUSH: the fetch chunk and the triangle flush size; INNER: node visits per round of the warp's
-// bookkeeping (a lane whose visit found no leaf triangles takes another step while at least CONT lanes
-// can), 1 = one visit per round.
+// CHUNK, FLUSH: the fetch chunk and the triangle flush size; VISITS: node visits per lane between two
+// rounds of the warp's bookkeeping (the triangles found meanwhile are tested at the next flush, so the
+// closest distance a visit culls with may lag by up to VISITS - 1 visits: a few more nodes, same hits).
 template <bool ANY, bool COUNT, bool REFINE, bool MIXED, int SS, uint32_t CHUNK = kCoopChunk, uint32_t FLUSH = kFlushTris,
-          int INNER = 1, int CONT = 16, class Load, class Store>
+          int VISITS = kCoopVisits, class Load, class Store>
 __device__ __forceinline__ uint32_t coop_trace(const CoopScene& uniform, uint32_t n, uint32_t* next, uint32_t refill_at,
                                                CoopWarp& S, uint2* stack, int stride, Load load, Store store,
                                                TraceCounters& cnt) {
@@ -199,6 +207,22 @@ __device__ __forceinline__ uint32_t coop_trace(const CoopScene& uniform, uint32_
     uint32_t n_groups = 0, n_tris = 0, n_fin = 0;   // warp-uniform list sizes
     uint32_t chunk_next = 0, chunk_end = 0;         // warp-uniform: unclaimed items [next, end) of the chunk
     bool exhausted = false;
+    // tests the warp's triangle list (all lanes together) and takes each lane's result
+    auto flush = [&]() {
+        __syncwarp();
+        coop_test_groups<COUNT, MIXED>(S, lane, n_groups, utris, cnt);
+        n_groups = 0;
+        n_tris = 0;
+        if (has && my_groups) {
+            const unsigned long long key = S.best[lane];
+            if (ANY) {
+                if ((uint32_t)key != 0xFFFFFFFFu) { group = make_uint2(0u, 0u); sp = 0; }
+            } else {
+                best_t = coop_unordered((uint32_t)(key >> 32));
+            }
+        }
+        my_groups = 0;
+    };
     for (;;) {
         // refill idle lanes
         const uint32_t active = __ballot_sync(0xFFFFFFFFu, has);
@@ -267,11 +291,12 @@ __device__ __forceinline__ uint32_t coop_trace(const CoopScene& uniform, uint32_
             if (exhausted) break;
             continue;
         }
-        // one node visit per tracing lane (INNER > 1: more while the lane finds no leaf triangles)
-        uint32_t tbase = 0, tmask = 0;
-#pragma unroll 1
-        for (int it = 0; it < INNER; ++it) {
-            if (has && tmask == 0u && group.y > 0x00FFFFFFu) {
+        // VISITS node visits per tracing lane, each followed by its stack pop; every visit's leaf triangles
+        // join the warp's list (tested before the list could overflow, between visits if need be)
+#pragma unroll
+        for (int v = 0; v < VISITS; ++v) {
+            uint32_t tbase = 0, tmask = 0;
+            if (has && group.y > 0x00FFFFFFu) {
                 if (++steps > kMaxTraversalSteps) {
                     err |= kErrStepLimit;
                     group = make_uint2(0u, 0u);
@@ -297,48 +322,26 @@ __device__ __forceinline__ uint32_t coop_trace(const CoopScene& uniform, uint32_
                     tmask = hm & 0x00FFFFFFu;
                 }
             }
-            if (INNER > 1 && it + 1 < INNER) {
-                if (has && tmask == 0u && group.y <= 0x00FFFFFFu && sp > 0) {
-                    --sp;
-                    group = sp < SS ? stack[sp * stride] : spill[sp - SS];
+            if (has && group.y <= 0x00FFFFFFu && sp > 0) {
+                --sp;
+                group = sp < SS ? stack[sp * stride] : spill[sp - SS];
+            }
+            const uint32_t app = __ballot_sync(0xFFFFFFFFu, tmask != 0u);
+            if (app) {
+                if (tmask) {
+                    const uint32_t pos = n_groups + (uint32_t)__popc(app & lanemask_lt());
+                    S.gbase[pos] = tbase;
+                    S.gmo[pos] = (lane << 24) | tmask;
+                    ++my_groups;
                 }
-                const bool more = has && tmask == 0u && group.y > 0x00FFFFFFu;
-                if (__popc(__ballot_sync(0xFFFFFFFFu, more)) < CONT) break;
+                n_groups += (uint32_t)__popc(app);
+                n_tris += __reduce_add_sync(0xFFFFFFFFu, (uint32_t)__popc(tmask));
             }
-        }
-        // the node's leaf triangles join the warp's list
-        const uint32_t app = __ballot_sync(0xFFFFFFFFu, tmask != 0u);
-        if (app) {
-            if (tmask) {
-                const uint32_t pos = n_groups + (uint32_t)__popc(app & lanemask_lt());
-                S.gbase[pos] = tbase;
-                S.gmo[pos] = (lane << 24) | tmask;
-                ++my_groups;
-            }
-            n_groups += (uint32_t)__popc(app);
-            n_tris += __reduce_add_sync(0xFFFFFFFFu, (uint32_t)__popc(tmask));
-        }
-        if (has && group.y <= 0x00FFFFFFu && sp > 0) {
-            --sp;
-            group = sp < SS ? stack[sp * stride] : spill[sp - SS];
+            if (v + 1 < VISITS && n_groups > 32u) flush();
         }
         // test the list when it is full enough, could overflow next step, or holds groups of a finished lane
         const bool waiting = has && group.y <= 0x00FFFFFFu && sp == 0 && my_groups > 0;
-        if (n_groups && (__any_sync(0xFFFFFFFFu, waiting) || n_tris >= FLUSH || n_groups > 32u)) {
-            __syncwarp();
-            coop_test_groups<COUNT, MIXED>(S, lane, n_groups, utris, cnt);
-            n_groups = 0;
-            n_tris = 0;
-            if (has && my_groups) {
-                const unsigned long long key = S.best[lane];
-                if (ANY) {
-                    if ((uint32_t)key != 0xFFFFFFFFu) { group = make_uint2(0u, 0u); sp = 0; }
-                } else {
-                    best_t = coop_unordered((uint32_t)(key >> 32));
-                }
-            }
-            my_groups = 0;
-        }
+        if (n_groups && (__any_sync(0xFFFFFFFFu, waiting) || n_tris >= FLUSH || n_groups > 32u)) flush();
         // finished rays join the warp's finished list
         const bool done = has && group.y <= 0x00FFFFFFu && sp == 0 && my_groups == 0;
         const uint32_t dm = __ballot_sync(0xFFFFFFFFu, done);
