@@ -55,8 +55,14 @@ struct CoopScene {
 constexpr uint32_t kCoopChunk = 32;
 // Blocks of 128 threads per SM the cooperative kernels are compiled for: 7 (at most 72 registers; 30 KB of
 // shared memory each, 210 KB per SM).
-constexpr int kCoopMinBlocks = 7;
-constexpr uint32_t kFlushTris = 24;    // triangles collected before the warp tests them
+#ifndef RT_COOP_MINB
+#define RT_COOP_MINB 7
+#endif
+constexpr int kCoopMinBlocks = RT_COOP_MINB;
+#ifndef RT_COOP_FLUSH_TRIS
+#define RT_COOP_FLUSH_TRIS 24
+#endif
+constexpr uint32_t kFlushTris = RT_COOP_FLUSH_TRIS;   // triangles collected before the warp tests them
 // Node visits per lane per round of bookkeeping (1.3M-triangle ray cast, closest hit: 1 visit 0.539 ms,
 // 2 visits 0.505 ms with 0.7 % more node visits, 3 visits 0.556 ms, 4 visits 0.620 ms).
 #ifndef RT_COOP_VISITS
