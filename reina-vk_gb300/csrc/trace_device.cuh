@@ -172,10 +172,16 @@ __device__ __forceinline__ void refine_hit(const TraceRay& r, const float4& a4, 
     h.t = __fadd_rn(t0, __fdiv_rn(dot2_f(e20, e21, e22, q0, q1, q2), det));
 }
 
+// The bits of 1.0f, read by the byte permutes of the box test from the constant bank: as an immediate the
+// compiler materialises it in a register before each permute (one register move per plane, 48 per node
+// visit), as a constant-bank operand the permute reads it directly (1.3M-triangle ray cast: 426 M -> 394 M
+// warp instructions, 0.507 -> 0.487 ms).
+static __constant__ uint32_t kOneBits = 0x3F800000u;
+
 // Byte `byte` of `word` as the float 1 + q * 2^-15, exactly: the byte placed in mantissa bits 8..15 of
 // 1.0 by one byte permute (no conversion or subtraction).
 __device__ __forceinline__ float q15(uint32_t word, int byte) {
-    return __uint_as_float(__byte_perm(word, 0x3F800000u, 0x7604u | ((uint32_t)byte << 4)));
+    return __uint_as_float(__byte_perm(word, kOneBits, 0x7604u | ((uint32_t)byte << 4)));
 }
 
 // Node meta bytes with the octant applied: internal children (meta bits 3 and 4 both set; leaf offsets
