@@ -297,36 +297,44 @@ __device__ __forceinline__ uint32_t coop_trace(const CoopScene& uniform, uint32_
             if (exhausted) break;
             continue;
         }
+        // watchdog: a ray's traversal ends with kErrStepLimit after kMaxTraversalSteps visit slots
+        if (has) {
+            steps += VISITS;
+            if (steps > kMaxTraversalSteps) {
+                err |= kErrStepLimit;
+                group = make_uint2(0u, 0u);
+                sp = 0;
+            }
+        }
         // VISITS node visits per tracing lane, each followed by its stack pop; every visit's leaf triangles
         // join the warp's list (tested before the list could overflow, between visits if need be)
 #pragma unroll
         for (int v = 0; v < VISITS; ++v) {
             uint32_t tbase = 0, tmask = 0;
             if (has && group.y > 0x00FFFFFFu) {
-                if (++steps > kMaxTraversalSteps) {
-                    err |= kErrStepLimit;
-                    group = make_uint2(0u, 0u);
-                    sp = 0;
-                } else {
-                    const uint32_t slot_bit = 31u - __clz(group.y);
-                    const uint32_t slot = (slot_bit - 24u) ^ r.oct_inv;
-                    const uint32_t child = group.x + (uint32_t)__popc(group.y & ((1u << slot) - 1u));
-                    group.y &= ~(1u << slot_bit);
-                    if (group.y > 0x00FFFFFFu) {
-                        if (sp < SS) stack[sp * stride] = group;
-                        else if (sp < kTotalStack) spill[sp - SS] = group;
-                        else err |= kErrStackOverflow;
-                        if (sp < kTotalStack) ++sp;
+                const uint32_t slot_bit = 31u - __clz(group.y);
+                const uint32_t slot = (slot_bit - 24u) ^ r.oct_inv;
+                const uint32_t child = group.x + (uint32_t)__popc(group.y & ((1u << slot) - 1u));
+                group.y &= ~(1u << slot_bit);
+                if (group.y > 0x00FFFFFFu) {
+                    if (sp < SS) {
+                        stack[sp * stride] = group;
+                        ++sp;
+                    } else if (sp < kTotalStack) {
+                        spill[sp - SS] = group;
+                        ++sp;
+                    } else {
+                        err |= kErrStackOverflow;
                     }
-                    const uint4* np = reinterpret_cast<const uint4*>(MIXED ? sc.nodes : uniform.nodes) + 5ull * child;
-                    const uint4 w0 = __ldg(np + 0), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3),
-                                w4 = __ldg(np + 4);
-                    if (COUNT) cnt.nodes++;
-                    const uint32_t hm = intersect_children(r, w0, w1, w2, w3, w4, best_t);
-                    group = make_uint2(w1.x, (hm & 0xFF000000u) | (w0.w >> 24));
-                    tbase = w1.y;
-                    tmask = hm & 0x00FFFFFFu;
                 }
+                const uint4* np = reinterpret_cast<const uint4*>(MIXED ? sc.nodes : uniform.nodes) + 5ull * child;
+                const uint4 w0 = __ldg(np + 0), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3),
+                            w4 = __ldg(np + 4);
+                if (COUNT) cnt.nodes++;
+                const uint32_t hm = intersect_children(r, w0, w1, w2, w3, w4, best_t);
+                group = make_uint2(w1.x, (hm & 0xFF000000u) | (w0.w >> 24));
+                tbase = w1.y;
+                tmask = hm & 0x00FFFFFFu;
             }
             if (has && group.y <= 0x00FFFFFFu && sp > 0) {
                 --sp;
