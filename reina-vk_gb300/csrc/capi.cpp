@@ -39,6 +39,11 @@ struct reina_ctx {
     rt::DeviceBuffer counters;   // u64 x 2 traversal counters
     rt::DeviceBuffer fetch;      // ring of u32 ray-fetch counters, one per ray-cast launch in flight
     std::atomic<uint32_t> fetch_slot{0};
+    uint32_t* err_host = nullptr;   // page-locked ring of words the error flag is read back into
+    std::atomic<uint32_t> err_slot{0};
+    ~reina_ctx() {
+        if (err_host) cudaFreeHost(err_host);
+    }
     rt::TraceConfig trace;       // ray-cast traversal launch configuration (reina_tuning)
     rt::TraceConfig wave_trace = wave_default();   // the wavefront kernels' (reina_tuning.wave_refill)
     static rt::TraceConfig wave_default() {
@@ -135,9 +140,12 @@ rt::ModelData to_model(const reina_model_data* m) {
 }
 
 uint32_t check_device_errors(reina_ctx* ctx, cudaStream_t st) {
-    uint32_t e = 0;
-    check_cuda(cudaMemcpyAsync(&e, ctx->err.get(), sizeof(uint32_t), cudaMemcpyDeviceToHost, st), "cudaMemcpyAsync err");
+    // read back into a page-locked word (a pageable destination would stage the copy): one word of the
+    // ring per call, so that calls on other streams do not share it
+    uint32_t* w = ctx->err_host + (ctx->err_slot.fetch_add(1) % reina_ctx::kFetchSlots);
+    check_cuda(cudaMemcpyAsync(w, ctx->err.get(), sizeof(uint32_t), cudaMemcpyDeviceToHost, st), "cudaMemcpyAsync err");
     check_cuda(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+    const uint32_t e = *w;
     if (e) {
         check_cuda(cudaMemsetAsync(ctx->err.get(), 0, sizeof(uint32_t), st), "cudaMemsetAsync err");
         check_cuda(cudaStreamSynchronize(st), "cudaStreamSynchronize");
@@ -208,6 +216,8 @@ int reina_ctx_create(const reina_ctx_options* options, reina_ctx** out_ctx) {
         ctx->err.alloc(sizeof(uint32_t));
         ctx->counters.alloc(2 * sizeof(unsigned long long));
         ctx->fetch.alloc(reina_ctx::kFetchSlots * sizeof(uint32_t));
+        check_cuda(cudaMallocHost(reinterpret_cast<void**>(&ctx->err_host), reina_ctx::kFetchSlots * sizeof(uint32_t)),
+                   "cudaMallocHost");
         check_cuda(cudaMemset(ctx->err.get(), 0, sizeof(uint32_t)), "cudaMemset");
         *out_ctx = ctx.release();
     });
